@@ -1,0 +1,478 @@
+"""Benchmark: DRR + grad-NCC pose evaluations per second on one GB300.
+
+Workload (N=1): 256^3 float32 phantom at 1 mm, detector 1536^2 at 0.194 mm
+downsampled 4x to 384^2, populations of lambda = 100 candidate poses (rotations
+~ N(0, 10 deg), translations ~ N(0, 20 mm)), grad-NCC (5x5 Gaussian + Sobel) against
+a noisy fixed image; one step = one population evaluation, captured as a CUDA
+graph.  Inputs are seeded synthetic data with those shapes (no dataset exists
+for this path).
+
+  value     poses/s with the populations already in device memory, CUDA events
+            around each step; L2 (129 MB) is flushed between steps by writing a
+            256 MB buffer outside the timed events.
+  e2e       poses/s through the public C ABI (xr_obj_eval) from pinned host
+            poses to host similarity values, copies inside the timed region.
+  roofline  DRR kernel: algorithmic bytes 8 * bytes_per_voxel * samples per
+            launch over its CUDA-event duration, against MEASURED_PEAKS.json.
+  cpu_baseline  the CPU oracle (a restatement of xReg's TBB CPU path) on a
+            bounded sample of the same workload, all host cores.
+
+--impl reference times that CPU path alone as the reference arm.
+Multi-GPU: replicas only (each rank evaluates its own populations; no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+POP = 100
+PEAK_FALLBACK_GBS = 6800.0
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--voxel", default="f32", choices=["f32", "f16", "bf16"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
+    p.add_argument("--no-extras", action="store_true")
+    return p.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _workload(seed=0):
+    from xreg_gb300 import synth
+    w = synth.batched_population(seed, POP)
+    return w
+
+
+def _populations(w, n, seed):
+    from xreg_gb300 import synth
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, POP, 4, 4))
+    for k in range(n):
+        out[k] = synth.sample_poses(w.vol, w.gt, POP, w.rot_sigma, w.trans_sigma, seed=int(rng.integers(1 << 30)))
+    return out
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"], "samples": 0}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return PEAK_FALLBACK_GBS, "fallback"
+
+
+def _ncu_traffic(workload_tag: str):
+    """Per-launch DRAM traffic of the DRR kernel from a committed ncu summary
+    (profiles/*.md line 'traffic_bytes_per_launch[<tag>]: N'), else None."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    key = f"traffic_bytes_per_launch[{workload_tag}]:"
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith(".md"):
+            continue
+        with open(os.path.join(d, fn)) as f:
+            for line in f:
+                if line.strip().startswith(key):
+                    try:
+                        return float(line.split(":", 1)[1].strip())
+                    except ValueError:
+                        return None
+    return None
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_baseline(w, fixed, budget_s: float):
+    """The oracle's FP32 DRR + grad-NCC on all host cores, on as many poses of the
+    workload as fit the time budget (at least 1)."""
+    from oracle import oracle as O
+    from tests.helpers import oracle_cams, oracle_geom
+    cores = O.set_threads(os.cpu_count() or 1)
+    geom, cams = oracle_geom(w.vol), oracle_cams(w.cams)
+    poses = _populations(w, 1, 999)[0]
+    done, t_used, i = 0, 0.0, 0
+    while True:
+        t0 = time.perf_counter()
+        d = O.drr_f32(w.vol.voxels, geom, cams, poses[i % POP][None], step=w.step)
+        O.grad_ncc(fixed, d)
+        t_used += time.perf_counter() - t0
+        done += 1
+        i += 1
+        if t_used >= budget_s or done >= POP:
+            break
+    return {"value": done / t_used, "unit": "poses/s", "cores": cores, "kind": "port",
+            "sample": f"{done} poses of the 256^3 / 384^2 / grad-NCC workload (FP32 DRR + grad-NCC, "
+                      f"{t_used:.1f} s of CPU work)"}
+
+
+# ----------------------------------------------------------------- our arm
+def run_ours(a, rank, world, local):
+    import torch
+    import xreg_gb300 as xr
+    from xreg_gb300 import synth
+
+    torch.cuda.set_device(local)
+    dev = local
+    xr.load()
+    w = _workload(seed=rank)
+    vt = {"f32": 0, "f16": 1, "bf16": 2}[a.voxel]
+    stream = torch.cuda.Stream(device=dev)
+
+    # fixed image: DRR at the ground-truth pose + 1% noise (computed on the GPU)
+    rc0 = xr.RayCasterLineIntCUDA(dev)
+    rc0.set_volume(w.vol)
+    rc0.set_camera_model(w.cams[0])
+    rc0.set_ray_step_size(w.step)
+    rc0.set_num_projs(1)
+    rc0.allocate_resources()
+    rc0.distribute_xforms_among_cam_models(synth.fixed_pose(w)[None])
+    rc0.compute()
+    fixed = synth.add_noise(rc0.proj(0), 0.01, w.seed + 2)
+    rc0.close()
+
+    rc = xr.RayCasterLineIntCUDA(dev)
+    rc.set_stream(stream.cuda_stream)
+    rc.set_volume(w.vol, vt)
+    rc.set_camera_model(w.cams[0])
+    rc.set_ray_step_size(w.step)
+    m = xr.ImgSimMetric2DGradNCCCUDA(dev)
+    m.set_fixed_image(fixed)
+    obj = xr.PopulationObjective(rc, [m], POP)
+
+    nsteps = a.warmup + a.steps
+    pops = _populations(w, nsteps, 1234 + rank)
+    d_pops = torch.from_numpy(pops.reshape(nsteps, POP, 16).copy()).to(f"cuda:{dev}")
+    d_sims = torch.empty((nsteps, POP), dtype=torch.float32, device=f"cuda:{dev}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    torch.cuda.synchronize()
+
+    def step(k):
+        obj.eval_device(POP, d_pops[k].data_ptr(), d_sims[k].data_ptr())
+
+    with torch.cuda.stream(stream):
+        for k in range(a.warmup):
+            step(k)
+    stream.synchronize()
+
+    # ---- timed region (device-resident inputs)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    _barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        with torch.cuda.stream(stream):
+            for i in range(a.steps):
+                flush.fill_(float(i))  # > L2, outside the events
+                evs[i][0].record(stream)
+                step(a.warmup + i)
+                evs[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms = [s.elapsed_time(e) for s, e in evs]
+    t_total = _max_over_ranks(sum(ms) / 1e3, world)
+    value = world * a.steps * POP / t_total
+
+    # ---- e2e through the C ABI with host buffers (pinned poses in, sims out)
+    h_pops = torch.empty((a.steps, POP, 16), dtype=torch.float64, pin_memory=True)
+    h_pops.copy_(torch.from_numpy(pops[a.warmup:].reshape(a.steps, POP, 16)))
+    h_sims = torch.empty((a.steps, POP), dtype=torch.float32, pin_memory=True)
+    hp, hs = h_pops.numpy(), h_sims.numpy()
+    obj.eval(hp[0])  # settle the host-entry path
+    e2e_t = 0.0
+    for i in range(a.steps):
+        flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hs[i] = obj.eval(hp[i])
+        e2e_t += time.perf_counter() - t0
+    e2e_t = _max_over_ranks(e2e_t, world)
+    e2e = world * a.steps * POP / e2e_t
+    np.testing.assert_array_equal(hs, d_sims[a.warmup:].cpu().numpy())  # same values both ways
+
+    # ---- DRR kernel alone: duration and exact sample count (roofline)
+    rc.set_count_samples(True)
+    rc.distribute_xforms_device(POP, d_pops[a.warmup].data_ptr())
+    rc.compute()
+    samples = rc.last_num_samples()
+    rc.set_count_samples(False)
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(a.steps):
+            flush.fill_(float(i))
+            rc.distribute_xforms_device(POP, d_pops[a.warmup + i].data_ptr())
+            kev[i][0].record(stream)
+            rc.compute()
+            kev[i][1].record(stream)
+    torch.cuda.synchronize()
+    drr_ms = float(np.mean([s.elapsed_time(e) for s, e in kev]))
+    bvox = 4 if vt == 0 else 2
+    alg_bytes = 8.0 * bvox * samples
+    achieved = alg_bytes / (drr_ms / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    tag = f"batched-256^3-384^2-pop100-{a.voxel}"
+    traffic = _ncu_traffic(tag)
+
+    extras = {}
+    if not a.no_extras and rank == 0:
+        extras = _extras(xr, w, fixed, dev, stream, pops[a.warmup], d_sims, a)
+
+    res = {
+        "metric": "poses/sec (DRR+grad-NCC pose evaluations, batched population)",
+        "value": round(value, 2),
+        "unit": "poses/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": round(t_total * 1e3 / a.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"f32": "f32", "f16": "f16-volume/f32-accum", "bf16": "bf16-volume/f32-accum"}[a.voxel],
+        "data": "synthetic (seeded ellipsoid phantom, sampled poses, noisy fixed DRR)",
+        "config": {"workload": "batched population: 256^3 phantom @1 mm, 1536^2@0.194 mm detector ds 4x -> 384^2, "
+                               "lambda=100, grad-NCC 5x5 Gaussian + Sobel, CUDA graph",
+                   "volume": "256x256x256 " + a.voxel, "detector": "384x384", "pop": POP, "step_mm": w.step,
+                   "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e, 2), "unit": "poses/s", "h2d_bytes_per_step": POP * 16 * 8,
+                "d2h_bytes_per_step": POP * 4},
+        "gpu_launches": a.steps * 5,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4),
+                     "traffic": None if traffic is None else traffic,
+                     "kernel": "drr_kernel<f32,sum>" if vt == 0 else f"drr_kernel<{a.voxel},sum>",
+                     "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s",
+                     "alg_bytes_per_launch": alg_bytes, "samples_per_launch": samples,
+                     "kernel_ms": round(drr_ms, 4),
+                     "note": "algorithmic bytes count 8 neighbour reads per trilinear sample; they are served "
+                             "mostly from L1/L2, so frac compares gather throughput with the HBM copy peak"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        res["cpu_baseline"] = cpu_baseline(w, fixed, a.cpu_seconds)
+        res.update(extras)
+    return res
+
+
+def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
+    """Plain single-pose path (one DRR + one metric launch per pose, host sync per
+    pose as xReg's OpenCL path does) and half-precision volumes, for context."""
+    import torch
+    out = {}
+    rc = xr.RayCasterLineIntCUDA(dev)
+    rc.set_volume(w.vol)
+    rc.set_camera_model(w.cams[0])
+    rc.set_ray_step_size(w.step)
+    rc.set_num_projs(1)
+    rc.allocate_resources()
+    m = xr.ImgSimMetric2DGradNCCCUDA(dev)
+    m.set_fixed_image(fixed)
+    m.set_num_moving_images(1)
+    m.set_mov_imgs_buf_from_ray_caster(rc, 0)
+    m.allocate_resources()
+    vals = []
+    n = 20
+    for i in range(3):
+        rc.distribute_xforms_among_cam_models(poses[i][None])
+        rc.compute()
+        m.compute()
+        m.sim_vals()
+    t0 = time.perf_counter()
+    for i in range(n):
+        rc.distribute_xforms_among_cam_models(poses[i][None])
+        rc.compute()
+        m.compute()
+        vals.append(m.sim_vals()[0])
+    plain = n / (time.perf_counter() - t0)
+    out["plain_single_pose_fp32"] = {"value": round(plain, 2), "unit": "poses/s",
+                                     "how": "per pose: pose upload, DRR launch, grad-NCC launches, host read"}
+    ref = d_sims[a.warmup][:n].cpu().numpy()
+    out["plain_single_pose_fp32"]["max_abs_diff_vs_batched"] = float(np.max(np.abs(np.array(vals) - ref)))
+    for vname, vt in (("f16", 1), ("bf16", 2)):
+        rch = xr.RayCasterLineIntCUDA(dev)
+        rch.set_stream(stream.cuda_stream)
+        rch.set_volume(w.vol, vt)
+        rch.set_camera_model(w.cams[0])
+        rch.set_ray_step_size(w.step)
+        mh = xr.ImgSimMetric2DGradNCCCUDA(dev)
+        mh.set_fixed_image(fixed)
+        objh = xr.PopulationObjective(rch, [mh], POP)
+        dp = torch.from_numpy(poses.reshape(POP, 16).copy()).to(f"cuda:{dev}")
+        ds = torch.empty(POP, dtype=torch.float32, device=f"cuda:{dev}")
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                objh.eval_device(POP, dp.data_ptr(), ds.data_ptr())
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+        with torch.cuda.stream(stream):
+            for s, e in evs:
+                s.record(stream)
+                objh.eval_device(POP, dp.data_ptr(), ds.data_ptr())
+                e.record(stream)
+        torch.cuda.synchronize()
+        t = np.mean([s.elapsed_time(e) for s, e in evs]) / 1e3
+        out[f"batched_{vname}_volume"] = {"value": round(POP / t, 2), "unit": "poses/s",
+                                          "max_abs_sim_diff_vs_f32": float(
+                                              np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
+        objh.close()
+    return out
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(a, rank, world):
+    """The reference's CPU path (restated: the reference cannot be compiled here)
+    timed on the host cores: each step evaluates a bounded sample of poses."""
+    if rank != 0:
+        return None
+    from xreg_gb300 import synth
+    from oracle import oracle as O
+    from tests.helpers import oracle_cams, oracle_geom
+    w = _workload(0)
+    cores = O.set_threads(os.cpu_count() or 1)
+    geom, cams = oracle_geom(w.vol), oracle_cams(w.cams)
+    fixed = synth.add_noise(O.drr_f32(w.vol.voxels, geom, cams, synth.fixed_pose(w)[None], step=w.step)[0], 0.01,
+                            w.seed + 2)
+    poses = _populations(w, 1, 999)[0]
+    per_step = 2
+
+    def one_step(k):
+        d = O.drr_f32(w.vol.voxels, geom, cams, poses[(k * per_step) % POP:(k * per_step) % POP + per_step],
+                      step=w.step)
+        O.grad_ncc(fixed, d)
+
+    for k in range(a.warmup):
+        one_step(k)
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        one_step(a.warmup + k)
+    t = time.perf_counter() - t0
+    v = a.steps * per_step / t
+    return {
+        "impl": "reference",
+        "metric": "poses/sec (DRR+grad-NCC pose evaluations, batched population)",
+        "value": round(v, 3), "unit": "poses/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": round(t * 1e3 / a.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched population: 256^3 phantom @1 mm, 384^2 detector, grad-NCC",
+                   "pop_per_step": per_step},
+        "cpu_baseline": {"value": round(v, 3), "unit": "poses/s", "cores": cores, "kind": "port",
+                         "sample": f"{per_step} poses per step; xReg's CPU ray caster + grad-NCC restated in C "
+                                   "(the reference needs ITK/OpenCV/TBB, absent here)"},
+        "e2e": {"value": round(v, 3), "unit": "poses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    a = _args()
+    rank, world, local = _dist()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "gloo" if a.impl == "reference" else "nccl"
+        if a.impl != "reference":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    if a.impl == "reference":
+        res = run_reference(a, rank, world)
+    else:
+        res = run_ours(a, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

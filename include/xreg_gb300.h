@@ -1,0 +1,232 @@
+/*
+ * xreg_gb300.h -- C ABI of the GB300-native line-integral DRR ray caster and 2D
+ * similarity metrics.  Plain C types only (no CUDA, torch or C++ types in the
+ * signatures); every entry point returns an xr_status (0 = success) and never
+ * throws.  The message of the last failure on the calling thread is available
+ * from xr_last_error().
+ *
+ * The entry points mirror xReg's operator surface so a thin C++ class (see
+ * include/xreg_gb300/xreg_gb300.hpp) can stand in for xReg's RayCaster and
+ * ImgSimMetric2D objects inside its registration pipeline.  Citations below are
+ * paths inside the xReg project.
+ *
+ * Threading and ordering: each handle owns one CUDA stream (or uses the stream
+ * given with xr_*_set_stream).  compute calls are asynchronous on that stream;
+ * calls that return host data (xr_rc_proj, xr_rc_copy_projs_to_host,
+ * xr_sm_sim_vals) synchronise the stream first.  A handle must not be used from
+ * two threads at once (same rule as xReg's objects).
+ */
+#ifndef XREG_GB300_H_
+#define XREG_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define XR_API __declspec(dllexport)
+#else
+#define XR_API __attribute__((visibility("default")))
+#endif
+
+/* ---------------------------------------------------------------- status -- */
+typedef int32_t xr_status;
+enum {
+  XR_OK = 0,
+  XR_ERR_INVALID_ARG = -1,    /* bad pointer, size, index or order of calls    */
+  XR_ERR_CUDA = -2,           /* a CUDA runtime call failed                    */
+  XR_ERR_OUT_OF_MEMORY = -3,  /* device allocation refused                     */
+  XR_ERR_UNSUPPORTED = -4,    /* UnsupportedOperationException in xReg         */
+  XR_ERR_NOT_ALLOCATED = -5,  /* compute before allocate_resources             */
+  XR_ERR_DEVICE_CHECK = -6    /* a kernel's own bounds/timeout check tripped   */
+};
+
+/* Message of the last failing call on this thread ("" if none). */
+XR_API const char* xr_last_error(void);
+/* Library version string. */
+XR_API const char* xr_version(void);
+
+/* ----------------------------------------------------------- plain types -- */
+/* Volume geometry in ITK conventions: n = size along index x, y, z (x fastest
+ * in the voxel buffer); physical point = origin + direction * diag(spacing) * idx
+ * (xregITKBasicImageUtils.h:133-165). */
+typedef struct {
+  int64_t n[3];
+  double spacing[3];
+  double origin[3];
+  double direction[9]; /* row-major */
+} xr_volume_desc;
+
+/* Camera model (xregPerspectiveXform.h:108-273).  intrins is K (row-major 3x3),
+ * extrins maps "world" to camera (row-major 4x4).  coord_frame_type:
+ * 0 = origin at focal point, +z to detector; 1 = origin at focal point, -z to
+ * detector (xReg's default); 2 = origin on detector. */
+typedef struct {
+  double intrins[9];
+  double extrins[16];
+  int64_t num_det_rows;
+  int64_t num_det_cols;
+  double det_row_spacing;
+  double det_col_spacing;
+  double focal_len;
+  int32_t coord_frame_type;
+  int32_t reserved;
+} xr_camera_desc;
+
+enum { XR_VOXEL_F32 = 0, XR_VOXEL_F16 = 1, XR_VOXEL_BF16 = 2 };
+enum { XR_LINE_INT_SUM = 0, XR_LINE_INT_MAX = 1 };          /* RayCastLineIntKernel */
+enum { XR_PROJ_STORE_REPLACE = 0, XR_PROJ_STORE_ACCUM = 1 }; /* ProjPixelStoreMethod */
+enum { XR_INTERP_LINEAR = 0, XR_INTERP_NN = 1, XR_INTERP_SINC = 2, XR_INTERP_BSPLINE = 3 };
+enum { XR_CAM_FOCAL_POS_Z = 0, XR_CAM_FOCAL_NEG_Z = 1, XR_CAM_ON_DETECTOR = 2 };
+
+/* ------------------------------------------------------- camera helpers -- */
+/* CameraModel::setup(focal_len, nr, nc, rs, cs) with MakeNaiveIntrins
+ * (xregPerspectiveXform.cpp:200-254). */
+XR_API xr_status xr_camera_setup_naive(double focal_len, int64_t num_rows, int64_t num_cols,
+                                       double row_spacing, double col_spacing,
+                                       int32_t coord_frame_type, xr_camera_desc* out);
+/* DownsampleCameraModel (xregPerspectiveXform.cpp:654-689). */
+XR_API xr_status xr_camera_downsample(const xr_camera_desc* src, double ds_factor,
+                                      int32_t force_even_dims, xr_camera_desc* out);
+
+/* ------------------------------------------------------------ ray caster -- */
+/* Replaces RayCasterLineIntCPU / RayCasterLineIntOCL
+ * (xregRayCastLineIntCPU.h:33, xregRayCastLineIntOCL.h:36) behind the RayCaster
+ * interface (xregRayCastInterface.h:43-434). */
+typedef struct xr_raycaster_s* xr_raycaster;
+
+/* device < 0 selects the current device. */
+XR_API xr_status xr_rc_create(int32_t device, xr_raycaster* out);
+XR_API xr_status xr_rc_destroy(xr_raycaster rc);
+/* Use a caller-owned cudaStream_t (passed as void*); NULL restores the handle's own stream. */
+XR_API xr_status xr_rc_set_stream(xr_raycaster rc, void* cuda_stream);
+XR_API xr_status xr_rc_synchronize(xr_raycaster rc);
+
+/* RayCaster::set_volumes (xregRayCastInterface.cpp:38-43).  Voxels are float32 on
+ * the host; they are copied to the device now and stored as voxel_type
+ * (XR_VOXEL_F16 / BF16 store scale * mu and undo the scale after the ray sum;
+ * scale <= 0 picks a power of two automatically). */
+XR_API xr_status xr_rc_set_volumes(xr_raycaster rc, int32_t num_vols, const xr_volume_desc* descs,
+                                   const float* const* host_voxels, int32_t voxel_type, float scale);
+/* Same, with float32 voxels already in device memory (copied, not borrowed). */
+XR_API xr_status xr_rc_set_volumes_device(xr_raycaster rc, int32_t num_vols, const xr_volume_desc* descs,
+                                          const float* const* device_voxels, int32_t voxel_type, float scale);
+/* RayCaster::set_camera_models (xregRayCastInterface.cpp:55-59). */
+XR_API xr_status xr_rc_set_camera_models(xr_raycaster rc, int32_t num_cams, const xr_camera_desc* cams);
+/* RayCaster::set_num_projs (xregRayCastInterface.cpp:124-132). */
+XR_API xr_status xr_rc_set_num_projs(xr_raycaster rc, int64_t num_projs);
+XR_API xr_status xr_rc_num_projs(xr_raycaster rc, int64_t* out);
+/* RayCaster::set_ray_step_size (default 1, xregRayCastInterface.h:390). */
+XR_API xr_status xr_rc_set_ray_step_size(xr_raycaster rc, float step_mm);
+/* RayCaster::set_interp_method; only XR_INTERP_LINEAR is implemented (as in
+ * RayCasterOCL, xregRayCastBaseOCL.cpp:338-341); others give XR_ERR_UNSUPPORTED at compute. */
+XR_API xr_status xr_rc_set_interp_method(xr_raycaster rc, int32_t method);
+/* use_proj_store_replace_method / use_proj_store_accum_method (xregRayCastInterface.cpp:262-280). */
+XR_API xr_status xr_rc_set_proj_store_method(xr_raycaster rc, int32_t method);
+/* set_default_bg_pixel_val (xregRayCastInterface.cpp:343-346). */
+XR_API xr_status xr_rc_set_default_bg_pixel_val(xr_raycaster rc, float bg);
+/* RayCastLineIntParamInterface::set_kernel_id (xregRayCastInterface.h:575-591). */
+XR_API xr_status xr_rc_set_kernel_id(xr_raycaster rc, int32_t kernel_id);
+/* set_bg_projs: one host image per camera model (rows*cols floats each), copied;
+ * use_bg_projs toggles their use (xregRayCastInterface.cpp:303-333). */
+XR_API xr_status xr_rc_set_bg_projs(xr_raycaster rc, const float* const* host_imgs, int32_t use_bg_projs);
+XR_API xr_status xr_rc_set_use_bg_projs(xr_raycaster rc, int32_t use_bg_projs);
+/* set_xforms_cam_to_itk_phys: also sets num_projs (xregRayCastInterface.cpp:168-172).
+ * xforms: row-major 4x4 doubles, camera -> ITK physical. */
+XR_API xr_status xr_rc_set_xforms_cam_to_itk_phys(xr_raycaster rc, int64_t num_xforms, const double* xforms);
+/* distribute_xforms_among_cam_models (xregRayCastInterface.cpp:97-114): projection
+ * (cam * num_xforms + i) gets xform i and camera cam; requires
+ * num_xforms * num_cams == num_projs. */
+XR_API xr_status xr_rc_distribute_xforms_among_cam_models(xr_raycaster rc, int64_t num_xforms,
+                                                          const double* xforms);
+/* Same, with the xforms already in device memory (num_xforms * 16 doubles). */
+XR_API xr_status xr_rc_distribute_xforms_device(xr_raycaster rc, int64_t num_xforms, const double* d_xforms);
+/* set_camera_model_proj_associations (xregRayCastInterface.cpp:73-80). */
+XR_API xr_status xr_rc_set_camera_model_proj_associations(xr_raycaster rc, int64_t n, const int32_t* cam_idx);
+/* RayCaster::allocate_resources + RayCasterCPU::allocate_resources
+ * (xregRayCastInterface.cpp:248-260, xregRayCastBaseCPU.cpp:50-88). */
+XR_API xr_status xr_rc_allocate_resources(xr_raycaster rc);
+/* max_num_projs_possible (xregRayCastInterface.h:296): from free device memory. */
+XR_API xr_status xr_rc_max_num_projs_possible(xr_raycaster rc, int64_t* out);
+/* RayCasterLineIntCPU::compute (xregRayCastLineIntCPU.cpp:294-349); asynchronous. */
+XR_API xr_status xr_rc_compute(xr_raycaster rc, int32_t vol_idx);
+/* proj(idx) as a host copy (xregRayCastBaseCPU.cpp:90-117); synchronises. */
+XR_API xr_status xr_rc_proj(xr_raycaster rc, int64_t proj_idx, float* host_dst);
+/* raw_host_pixel_buf analogue: copies all num_projs images; synchronises. */
+XR_API xr_status xr_rc_copy_projs_to_host(xr_raycaster rc, float* host_dst);
+/* to_cuda_buf(): device address of the projection buffer (view-major, row-major
+ * images, num_projs * rows * cols floats), valid until the next allocate_resources. */
+XR_API xr_status xr_rc_device_pixel_buf(xr_raycaster rc, float** out);
+/* Exact number of trilinear samples the last compute took (algorithmic-bytes
+ * accounting); synchronises. */
+XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* out);
+/* Enables (1) or disables (0) per-compute sample counting (default off). */
+XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
+
+/* ------------------------------------------------------ similarity metric -- */
+/* Replaces ImgSimMetric2D{NCC,GradNCC,PatchNCC,PatchGradNCC}{CPU,OCL}
+ * (xregImgSimMetric2D.h:42-159). */
+typedef struct xr_simmetric_s* xr_simmetric;
+enum { XR_SIM_NCC = 0, XR_SIM_GRAD_NCC = 1, XR_SIM_PATCH_NCC = 2, XR_SIM_PATCH_GRAD_NCC = 3 };
+
+XR_API xr_status xr_sm_create(int32_t kind, int32_t device, xr_simmetric* out);
+XR_API xr_status xr_sm_destroy(xr_simmetric sm);
+XR_API xr_status xr_sm_set_stream(xr_simmetric sm, void* cuda_stream);
+/* set_fixed_image (xregImgSimMetric2D.h:69): host float image, copied. */
+XR_API xr_status xr_sm_set_fixed_image(xr_simmetric sm, const float* host_img, int64_t rows, int64_t cols);
+/* set_mask (xregImgSimMetric2D.h:130): host uint8 image (nonzero = use), NULL clears.
+ * Supported for XR_SIM_NCC and XR_SIM_GRAD_NCC. */
+XR_API xr_status xr_sm_set_mask(xr_simmetric sm, const uint8_t* host_mask);
+/* set_num_moving_images (xregImgSimMetric2D.h:93). */
+XR_API xr_status xr_sm_set_num_moving_images(xr_simmetric sm, int64_t n);
+/* set_mov_imgs_buf_from_ray_caster (xregImgSimMetric2DCPU.cpp:43-72): the moving
+ * images are read in place from the ray caster's device buffer at proj_offset. */
+XR_API xr_status xr_sm_set_mov_imgs_buf_from_ray_caster(xr_simmetric sm, xr_raycaster rc, int64_t proj_offset);
+/* set_mov_imgs_host_buf analogue for device memory (xregImgSimMetric2DCPU.cpp:74-88). */
+XR_API xr_status xr_sm_set_mov_imgs_device_buf(xr_simmetric sm, const float* d_imgs, int64_t proj_offset);
+/* ImgSimMetric2DGradImgParamInterface::set_smooth_img_before_sobel_kernel_radius
+ * (default 5 = 5x5 Gaussian; 0 = no smoothing; 3 = 3x3). */
+XR_API xr_status xr_sm_set_smooth_img_before_sobel_kernel_radius(xr_simmetric sm, int32_t r);
+/* ImgSimMetric2DPatchCommon::set_patch_radius / set_patch_stride (defaults 5 and 1). */
+XR_API xr_status xr_sm_set_patch_radius(xr_simmetric sm, int32_t r);
+XR_API xr_status xr_sm_set_patch_stride(xr_simmetric sm, int32_t s);
+/* allocate_resources (xregImgSimMetric2D.h:81): fixed-image statistics, gradients
+ * and patch statistics are computed once here and stay on the device. */
+XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm);
+/* compute() (xregImgSimMetric2D.h:88); asynchronous. */
+XR_API xr_status xr_sm_compute(xr_simmetric sm);
+/* sim_vals() (xregImgSimMetric2D.h:105-112): copies num_moving_images floats; synchronises. */
+XR_API xr_status xr_sm_sim_vals(xr_simmetric sm, float* host_dst);
+/* Device address of the float[num_moving_images] similarity values. */
+XR_API xr_status xr_sm_device_sim_vals(xr_simmetric sm, float** out);
+
+/* ------------------------------------------- population objective (fused) -- */
+/* One registration objective: a ray caster (one volume, num_views camera models)
+ * and one metric per view, evaluated for a population of candidate poses.  This
+ * is Intensity2D3DRegi::obj_fn (xregIntensity2D3DRegi.cpp:571-742) restricted to
+ * one object: DRR per (view, pose), metric per view, mean over views
+ * (ImgSimMetric2DCombineMean, xregImgSimMetric2DCombine.cpp:79-96). The fused
+ * path keeps the DRRs in on-chip/L2 memory and never hands them to the host. */
+typedef struct xr_objective_s* xr_objective;
+
+/* The ray caster must have its volume and num_views camera models set; metrics
+ * must have their fixed images set (one per view, all XR_SIM_NCC or all
+ * XR_SIM_GRAD_NCC or all XR_SIM_PATCH_GRAD_NCC).  max_pop is the largest population. */
+XR_API xr_status xr_obj_create(xr_raycaster rc, int32_t vol_idx, int32_t num_views, const xr_simmetric* metrics,
+                               int64_t max_pop, xr_objective* out);
+XR_API xr_status xr_obj_destroy(xr_objective obj);
+/* Evaluates pop poses (row-major 4x4 doubles, camera -> ITK physical, the same
+ * pose for every view, like distribute_xforms_among_cam_models) and writes pop
+ * floats: the mean over views of each view's metric.  host pointers; synchronises. */
+XR_API xr_status xr_obj_eval(xr_objective obj, int64_t pop, const double* host_xforms, float* host_sims);
+/* Same with device pointers; asynchronous on the ray caster's stream. */
+XR_API xr_status xr_obj_eval_device(xr_objective obj, int64_t pop, const double* d_xforms, float* d_sims);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

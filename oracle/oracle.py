@@ -1,0 +1,229 @@
+"""ctypes wrapper of the CPU oracle (oracle/xr_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker.  The product never imports it.
+Parity status: unpinned against the reference binary (it cannot be built here
+and ships no golden vectors); pinned by analytic known-answer tests.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libxr_oracle.so"
+CMAES_REF = HERE / "_ref" / "libcmaes_ref.so"
+
+
+class vol_geom(C.Structure):
+    _fields_ = [("n", C.c_int64 * 3), ("spacing", C.c_double * 3), ("origin", C.c_double * 3),
+                ("direction", C.c_double * 9)]
+
+
+class camera(C.Structure):
+    _fields_ = [("intrins", C.c_double * 9), ("extrins", C.c_double * 16), ("num_det_rows", C.c_int64),
+                ("num_det_cols", C.c_int64), ("det_row_spacing", C.c_double), ("det_col_spacing", C.c_double),
+                ("focal_len", C.c_double), ("coord_frame_type", C.c_int32), ("pad_", C.c_int32)]
+
+
+class proj_geom(C.Structure):
+    _fields_ = [(n, C.c_float * 3) for n in ("src", "d0", "dc", "dr", "e0", "ec", "er", "pad")]
+
+
+def build(force: bool = False) -> Path:
+    if force or not LIB.exists() or LIB.stat().st_mtime < (HERE / "xr_oracle.c").stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE), "_build/libxr_oracle.so"], check=True)
+    return LIB
+
+
+def build_ref(ref_dir: str = "/root/reference") -> Path | None:
+    """Compiles the reference's vendored CMA-ES when its sources are present."""
+    if CMAES_REF.exists():
+        return CMAES_REF
+    if not Path(ref_dir, "third_party", "cmaes", "cmaes.c").exists():
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_DIR={ref_dir}"], check=True)
+    return CMAES_REF
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P = C.c_void_p
+        i64 = C.c_int64
+        L.xo_set_num_threads.argtypes = [C.c_int]
+        L.xo_get_num_threads.restype = C.c_int
+        L.xo_drr_f32.argtypes = [P, C.POINTER(vol_geom), C.POINTER(camera), i64, P, P, i64, C.c_float, C.c_int,
+                                 C.c_int, C.c_float, P, P, P]
+        L.xo_drr_f64.argtypes = [P, C.POINTER(vol_geom), C.POINTER(camera), i64, P, P, i64, C.c_float, C.c_int,
+                                 C.c_double, P, P]
+        L.xo_proj_geoms.argtypes = [C.POINTER(vol_geom), C.POINTER(camera), P, P, i64, C.POINTER(proj_geom)]
+        L.xo_camera_setup_naive.argtypes = [C.c_double, i64, i64, C.c_double, C.c_double, C.c_int32,
+                                            C.POINTER(camera)]
+        L.xo_camera_downsample.argtypes = [C.POINTER(camera), C.c_double, C.c_int, C.POINTER(camera)]
+        L.xo_grad_images.argtypes = [P, i64, i64, C.c_int, P, P]
+        L.xo_ncc.argtypes = [P, P, i64, i64, P, P]
+        L.xo_grad_ncc.argtypes = [P, P, i64, i64, i64, C.c_int, P, P]
+        L.xo_grad_ncc_par.argtypes = [P, P, i64, i64, i64, C.c_int, P]
+        L.xo_patch_ncc.argtypes = [P, P, i64, i64, i64, i64, i64, P]
+        L.xo_patch_grad_ncc.argtypes = [P, P, i64, i64, i64, C.c_int, i64, i64, P]
+        L.xo_hu_to_lin_att.argtypes = [P, i64, P]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int | None = None) -> int:
+    n = n or os.cpu_count() or 1
+    lib().xo_set_num_threads(int(n))
+    return n
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+def vol_geom_of(voxels: np.ndarray, spacing, origin=(0, 0, 0), direction=None) -> vol_geom:
+    g = vol_geom()
+    nz, ny, nx = voxels.shape
+    g.n[0], g.n[1], g.n[2] = nx, ny, nz
+    d = np.eye(3) if direction is None else np.asarray(direction, dtype=np.float64)
+    for i in range(3):
+        g.spacing[i] = float(spacing[i])
+        g.origin[i] = float(origin[i])
+    for i in range(9):
+        g.direction[i] = float(d.reshape(9)[i])
+    return g
+
+
+def camera_from_tuple(t) -> camera:
+    """From the product's CameraModel.as_tuple() (same fields)."""
+    c = camera()
+    intr, extr, nr, nc, rs, cs, f, frame = t
+    for i in range(9):
+        c.intrins[i] = intr[i]
+    for i in range(16):
+        c.extrins[i] = extr[i]
+    c.num_det_rows, c.num_det_cols = nr, nc
+    c.det_row_spacing, c.det_col_spacing, c.focal_len, c.coord_frame_type = rs, cs, f, frame
+    return c
+
+
+def camera_naive(f, nr, nc, rs, cs, frame=1) -> camera:
+    c = camera()
+    lib().xo_camera_setup_naive(f, nr, nc, rs, cs, frame, C.byref(c))
+    return c
+
+
+def camera_downsample(c: camera, ds: float, force_even: bool = False) -> camera:
+    d = camera()
+    lib().xo_camera_downsample(C.byref(c), ds, int(force_even), C.byref(d))
+    return d
+
+
+def drr_f32(voxels, geom: vol_geom, cams, poses, cam_idx=None, step=1.0, kernel=0, store=0, default_bg=0.0,
+            bg_projs=None, out=None, count=False):
+    """FP32 xReg-CPU semantics.  poses: [n, 4, 4] cam -> ITK phys. Returns [n, rows, cols]."""
+    voxels = np.ascontiguousarray(voxels, dtype=np.float32)
+    poses = np.ascontiguousarray(np.asarray(poses, dtype=np.float64).reshape(-1, 16))
+    n = poses.shape[0]
+    cams = list(cams)
+    ci = np.zeros(n, dtype=np.int32) if cam_idx is None else np.ascontiguousarray(cam_idx, dtype=np.int32)
+    carr = (camera * len(cams))(*cams)
+    rows, cols = cams[0].num_det_rows, cams[0].num_det_cols
+    if out is None:
+        out = np.zeros((n, rows, cols), dtype=np.float32)
+    bg = None if bg_projs is None else np.ascontiguousarray(bg_projs, dtype=np.float32)
+    ns = np.zeros((n, rows, cols), dtype=np.uint64) if count else None
+    rc = lib().xo_drr_f32(_p(voxels), C.byref(geom), carr, len(cams), _p(poses), _p(ci), n, step, kernel, store,
+                          default_bg, None if bg is None else _p(bg), _p(out), None if ns is None else _p(ns))
+    assert rc == 0
+    return (out, ns) if count else out
+
+
+def drr_f64(voxels, geom: vol_geom, cams, poses, cam_idx=None, step=1.0, kernel=0, default_bg=0.0, count=False):
+    voxels = np.ascontiguousarray(voxels, dtype=np.float32)
+    poses = np.ascontiguousarray(np.asarray(poses, dtype=np.float64).reshape(-1, 16))
+    n = poses.shape[0]
+    cams = list(cams)
+    ci = np.zeros(n, dtype=np.int32) if cam_idx is None else np.ascontiguousarray(cam_idx, dtype=np.int32)
+    carr = (camera * len(cams))(*cams)
+    rows, cols = cams[0].num_det_rows, cams[0].num_det_cols
+    out = np.zeros((n, rows, cols), dtype=np.float64)
+    ns = np.zeros((n, rows, cols), dtype=np.uint64) if count else None
+    rc = lib().xo_drr_f64(_p(voxels), C.byref(geom), carr, len(cams), _p(poses), _p(ci), n, step, kernel,
+                          default_bg, _p(out), None if ns is None else _p(ns))
+    assert rc == 0
+    return (out, ns) if count else out
+
+
+def proj_geoms(geom: vol_geom, cams, poses, cam_idx=None) -> np.ndarray:
+    poses = np.ascontiguousarray(np.asarray(poses, dtype=np.float64).reshape(-1, 16))
+    n = poses.shape[0]
+    ci = np.zeros(n, dtype=np.int32) if cam_idx is None else np.ascontiguousarray(cam_idx, dtype=np.int32)
+    carr = (camera * len(cams))(*cams)
+    out = (proj_geom * n)()
+    lib().xo_proj_geoms(C.byref(geom), carr, _p(poses), _p(ci), n, out)
+    return np.frombuffer(out, dtype=np.float32).reshape(n, 24).copy()
+
+
+def grad_images(img, smooth_ksize=5):
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    gx = np.zeros(img.shape, dtype=np.float64)
+    gy = np.zeros(img.shape, dtype=np.float64)
+    assert lib().xo_grad_images(_p(img), img.shape[0], img.shape[1], smooth_ksize, _p(gx), _p(gy)) == 0
+    return gx, gy
+
+
+def ncc(fixed, movs, mask=None) -> np.ndarray:
+    f = np.ascontiguousarray(fixed, dtype=np.float32)
+    m = np.ascontiguousarray(movs, dtype=np.float32).reshape(-1, f.size)
+    out = np.zeros(m.shape[0], dtype=np.float64)
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+    lib().xo_ncc(_p(f), _p(m), f.size, m.shape[0], None if mk is None else _p(mk), _p(out))
+    return out
+
+
+def grad_ncc(fixed, movs, smooth_ksize=5, mask=None) -> np.ndarray:
+    f = np.ascontiguousarray(fixed, dtype=np.float32)
+    m = np.ascontiguousarray(movs, dtype=np.float32).reshape(-1, *f.shape)
+    out = np.zeros(m.shape[0], dtype=np.float64)
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+    if mk is None:
+        lib().xo_grad_ncc_par(_p(f), _p(m), f.shape[0], f.shape[1], m.shape[0], smooth_ksize, _p(out))
+    else:
+        assert lib().xo_grad_ncc(_p(f), _p(m), f.shape[0], f.shape[1], m.shape[0], smooth_ksize, _p(mk),
+                                 _p(out)) == 0
+    return out
+
+
+def patch_ncc(fixed, movs, radius=5, stride=1) -> np.ndarray:
+    f = np.ascontiguousarray(fixed, dtype=np.float32)
+    m = np.ascontiguousarray(movs, dtype=np.float32).reshape(-1, *f.shape)
+    out = np.zeros(m.shape[0], dtype=np.float64)
+    lib().xo_patch_ncc(_p(f), _p(m), f.shape[0], f.shape[1], m.shape[0], radius, stride, _p(out))
+    return out
+
+
+def patch_grad_ncc(fixed, movs, smooth_ksize=5, radius=5, stride=1) -> np.ndarray:
+    f = np.ascontiguousarray(fixed, dtype=np.float32)
+    m = np.ascontiguousarray(movs, dtype=np.float32).reshape(-1, *f.shape)
+    out = np.zeros(m.shape[0], dtype=np.float64)
+    assert lib().xo_patch_grad_ncc(_p(f), _p(m), f.shape[0], f.shape[1], m.shape[0], smooth_ksize, radius, stride,
+                                   _p(out)) == 0
+    return out
+
+
+def hu_to_lin_att(hu) -> np.ndarray:
+    h = np.ascontiguousarray(hu, dtype=np.float32)
+    out = np.empty_like(h)
+    lib().xo_hu_to_lin_att(_p(h), h.size, _p(out))
+    return out

@@ -1,0 +1,833 @@
+/*
+ * xr_oracle.c -- CPU restatement of xReg's CPU line-integral ray caster and its
+ * 2D similarity metrics.  TEST INFRASTRUCTURE ONLY: tests/, the smoke check and
+ * the CPU-baseline leg of bench.py load this library as the checker; the product
+ * (xreg_gb300) never links, loads or calls it.
+ *
+ * Parity status: the reference cannot be compiled here (ITK, Eigen, OpenCV, TBB
+ * are absent) and its repository holds no golden vectors or known-answer tests,
+ * so this restatement is "parity unpinned" with respect to the reference binary.
+ * It is pinned instead by analytic known-answer tests (uniform-box chords,
+ * OpenCV kernel identities, NCC self/negation identities) and by its own FP64
+ * twin; see tests/test_oracle_*.py.
+ *
+ * Followed reference code (paths inside the xReg project):
+ *   lib/ray_cast/xregRayCastLineIntCPU.cpp:106-290  per-ray loop (clip, nudge,
+ *        floor(len/step)+1 samples, sum*step, replace/accum, sum/max kernels)
+ *   lib/ray_cast/xregRayCastBaseCPU.cpp:128-158     pre_compute (bg fill / keep)
+ *   lib/spatial/xregSpatialPrimitives.cpp:176-221   RayRectIntersect slab test
+ *   lib/itk/xregITKBasicImageUtils.h:56-75,133-165  index bounds, index->phys
+ *   lib/transforms/xregPerspectiveXform.cpp:200-254,401-414,654-689 camera model
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DNCCCPU.cpp:53-63,164-209  NCC
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DGradImgCPU.cpp:32-102 blur+Sobel
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DGradNCCCPU.cpp:51-65  grad-NCC
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchCommon.cpp:256-300 patch grid
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchNCCCPU.cpp:74-300,332-441,
+ *        558-619                                    patch NCC
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchGradNCCCPU.cpp:104-230
+ *   lib/image/xregHUToLinAtt.cpp:45-69              HU -> linear attenuation
+ *
+ * Third-party arithmetic restated from published descriptions (absent here):
+ *   ITK 5.1.1 LinearInterpolateImageFunction: trilinear at a continuous index,
+ *     voxel centres at integer indices, a neighbour past the last index is not
+ *     used (the in-bounds voxel keeps full weight); computed in double and
+ *     rounded to the float pixel type before the float ray sum.
+ *   OpenCV 3.4 GaussianBlur(ksize 5x5, sigma 0): separable, the fixed small
+ *     kernel [1 4 6 4 1]/16; Sobel(ksize 3): [-1 0 1] x [1 2 1]; both with the
+ *     default border BORDER_REFLECT_101 (gfedcb|abcdefgh|gfedcba).
+ *
+ * Geometry precision contract (shared with the CUDA kernels on purpose): the
+ * per-projection set-up (index<->physical inverse, camera inverse, pose
+ * composition) is done in double with a fixed operation order, rounded to float,
+ * and the per-ray work is done in float with a fixed operation order and no
+ * fused multiply-add.  Compile with -ffp-contract=off.  This makes the sample
+ * count floor(len/step)+1 of every ray identical between this file and the GPU,
+ * so one-sample flips cannot break the DRR tolerance.
+ */
+#include <math.h>
+#include <float.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <pthread.h>
+
+#if defined(__FP_FAST_FMA) && !defined(XO_ALLOW_CONTRACT)
+/* nothing: contraction is controlled by -ffp-contract=off */
+#endif
+
+#define XO_EXPORT __attribute__((visibility("default")))
+
+/* ------------------------------------------------------------------------- */
+/* Shared layouts (mirrored in the product's include/xreg_gb300.h)            */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int64_t n[3];           /* size along index x, y, z (x fastest in memory)   */
+  double spacing[3];
+  double origin[3];
+  double direction[9];    /* row-major ITK direction matrix                   */
+} xo_vol_geom;
+
+typedef struct {
+  double intrins[9];      /* row-major 3x3 K                                  */
+  double extrins[16];     /* row-major 4x4 world -> camera                    */
+  int64_t num_det_rows;
+  int64_t num_det_cols;
+  double det_row_spacing;
+  double det_col_spacing;
+  double focal_len;
+  int32_t coord_frame_type; /* 0 focal pt +z, 1 focal pt -z (default), 2 on detector */
+  int32_t pad_;
+} xo_camera;
+
+/* Per-projection ray set-up, all in volume index coordinates. */
+typedef struct {
+  float src[3];   /* pinhole                                                  */
+  float d0[3];    /* pinhole -> detector pixel (0,0)                          */
+  float dc[3];    /* + per detector column                                    */
+  float dr[3];    /* + per detector row                                       */
+  float e0[3];    /* same vectors in camera-world coords (for the mm length)  */
+  float ec[3];
+  float er[3];
+  float pad[3];
+} xo_proj_geom;
+
+/* ------------------------------------------------------------------------- */
+/* Small parallel-for (stands in for TBB parallel_for over a flat range)       */
+/* ------------------------------------------------------------------------- */
+typedef void (*xo_range_fn)(void* ctx, int64_t begin, int64_t end);
+
+typedef struct {
+  xo_range_fn fn;
+  void* ctx;
+  int64_t n;
+  int64_t chunk;
+  int64_t next;            /* guarded by mu */
+  pthread_mutex_t mu;
+} xo_pool_job;
+
+static int g_num_threads = 1;
+
+XO_EXPORT void xo_set_num_threads(int n) { g_num_threads = n < 1 ? 1 : n; }
+XO_EXPORT int xo_get_num_threads(void) { return g_num_threads; }
+
+static void* xo_worker(void* arg) {
+  xo_pool_job* job = (xo_pool_job*)arg;
+  for (;;) {
+    int64_t b;
+    pthread_mutex_lock(&job->mu);
+    b = job->next;
+    job->next += job->chunk;
+    pthread_mutex_unlock(&job->mu);
+    if (b >= job->n) break;
+    int64_t e = b + job->chunk;
+    if (e > job->n) e = job->n;
+    job->fn(job->ctx, b, e);
+  }
+  return NULL;
+}
+
+static void xo_parallel_for(xo_range_fn fn, void* ctx, int64_t n, int64_t chunk) {
+  if (n <= 0) return;
+  if (g_num_threads <= 1 || n <= chunk) { fn(ctx, 0, n); return; }
+  xo_pool_job job;
+  job.fn = fn; job.ctx = ctx; job.n = n; job.chunk = chunk; job.next = 0;
+  pthread_mutex_init(&job.mu, NULL);
+  int nt = g_num_threads;
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nt);
+  for (int i = 1; i < nt; ++i) pthread_create(&th[i], NULL, xo_worker, &job);
+  xo_worker(&job);
+  for (int i = 1; i < nt; ++i) pthread_join(th[i], NULL);
+  free(th);
+  pthread_mutex_destroy(&job.mu);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Double helpers with a fixed evaluation order                              */
+/* ------------------------------------------------------------------------- */
+static void m3_inverse(const double a[9], double out[9]) {
+  const double c00 = a[4] * a[8] - a[5] * a[7];
+  const double c01 = a[5] * a[6] - a[3] * a[8];
+  const double c02 = a[3] * a[7] - a[4] * a[6];
+  const double det = (a[0] * c00 + a[1] * c01) + a[2] * c02;
+  const double id = 1.0 / det;
+  out[0] = c00 * id;
+  out[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+  out[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+  out[3] = c01 * id;
+  out[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+  out[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+  out[6] = c02 * id;
+  out[7] = (a[1] * a[6] - a[0] * a[7]) * id;
+  out[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+}
+
+static void m3_mul(const double a[9], const double b[9], double out[9]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      out[i * 3 + j] = (a[i * 3 + 0] * b[0 * 3 + j] + a[i * 3 + 1] * b[1 * 3 + j]) + a[i * 3 + 2] * b[2 * 3 + j];
+}
+
+static void m3_vec(const double a[9], const double v[3], double out[3]) {
+  for (int i = 0; i < 3; ++i)
+    out[i] = (a[i * 3 + 0] * v[0] + a[i * 3 + 1] * v[1]) + a[i * 3 + 2] * v[2];
+}
+
+/* Per-projection set-up in double.  The CUDA geometry kernel evaluates the same
+ * expressions in the same order (explicitly rounded double ops). */
+XO_EXPORT void xo_proj_geom_one(const xo_vol_geom* vg, const xo_camera* cam,
+                                const double pose_cam_to_phys[16], xo_proj_geom* out) {
+  /* index -> physical: A = D * diag(spacing), origin o (xregITKBasicImageUtils.h:133-165) */
+  double A[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A[i * 3 + j] = vg->direction[i * 3 + j] * vg->spacing[j];
+  double Ai[9];
+  m3_inverse(A, Ai);
+  double ti[3];
+  m3_vec(Ai, vg->origin, ti);
+  ti[0] = -ti[0]; ti[1] = -ti[1]; ti[2] = -ti[2];
+
+  /* camera: K^-1, extrinsic inverse (rigid), pinhole (xregPerspectiveXform.cpp:230-334) */
+  double Ki[9];
+  m3_inverse(cam->intrins, Ki);
+  double ER[9], Et[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) ER[i * 3 + j] = cam->extrins[j * 4 + i];  /* R^T */
+  {
+    double t[3] = {cam->extrins[3], cam->extrins[7], cam->extrins[11]};
+    m3_vec(ER, t, Et);
+    Et[0] = -Et[0]; Et[1] = -Et[1]; Et[2] = -Et[2];
+  }
+  const double f = cam->focal_len;
+  double pin[3];
+  if (cam->coord_frame_type == 2) {
+    double pz[3] = {0.0, 0.0, f}, tmp[3];
+    m3_vec(ER, pz, tmp);
+    pin[0] = tmp[0] + Et[0]; pin[1] = tmp[1] + Et[1]; pin[2] = tmp[2] + Et[2];
+  } else {
+    pin[0] = Et[0]; pin[1] = Et[1]; pin[2] = Et[2];
+  }
+  const double dz = (cam->coord_frame_type == 1) ? -f : f;
+  const double zadj = (cam->coord_frame_type == 2) ? -f : 0.0;
+
+  /* detector point of pixel (c, r): E^-1 (K^-1 (dz [c r 1]) + zadj) (xregPerspectiveXform.cpp:401-414) */
+  double kc[3] = {Ki[0] * dz, Ki[3] * dz, Ki[6] * dz};
+  double kr[3] = {Ki[1] * dz, Ki[4] * dz, Ki[7] * dz};
+  double k0[3] = {Ki[2] * dz, Ki[5] * dz, Ki[8] * dz + zadj};
+  double dcol[3], drow[3], det0[3];
+  m3_vec(ER, kc, dcol);
+  m3_vec(ER, kr, drow);
+  m3_vec(ER, k0, det0);
+  det0[0] += Et[0]; det0[1] += Et[1]; det0[2] += Et[2];
+  double e0[3] = {det0[0] - pin[0], det0[1] - pin[1], det0[2] - pin[2]};
+
+  /* camera -> index: M = phys_to_idx * pose (xregRayCastLineIntCPU.cpp:207-208) */
+  double TR[9], Tt[3];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) TR[i * 3 + j] = pose_cam_to_phys[i * 4 + j];
+    Tt[i] = pose_cam_to_phys[i * 4 + 3];
+  }
+  double MR[9], Mt[3];
+  m3_mul(Ai, TR, MR);
+  m3_vec(Ai, Tt, Mt);
+  Mt[0] += ti[0]; Mt[1] += ti[1]; Mt[2] += ti[2];
+
+  double src[3], d0[3], dc[3], dr[3];
+  m3_vec(MR, pin, src);
+  src[0] += Mt[0]; src[1] += Mt[1]; src[2] += Mt[2];
+  m3_vec(MR, e0, d0);
+  m3_vec(MR, dcol, dc);
+  m3_vec(MR, drow, dr);
+
+  for (int k = 0; k < 3; ++k) {
+    out->src[k] = (float)src[k];
+    out->d0[k] = (float)d0[k];
+    out->dc[k] = (float)dc[k];
+    out->dr[k] = (float)dr[k];
+    out->e0[k] = (float)e0[k];
+    out->ec[k] = (float)dcol[k];
+    out->er[k] = (float)drow[k];
+    out->pad[k] = 0.0f;
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Trilinear interpolation with ITK's boundary rule                           */
+/* ------------------------------------------------------------------------- */
+static inline double xo_clampd(double x, double hi) {
+  return x < 0.0 ? 0.0 : (x > hi ? hi : x);
+}
+
+static inline double xo_trilinear(const float* vol, int64_t nx, int64_t ny, int64_t nz,
+                                  double x, double y, double z) {
+  x = xo_clampd(x, (double)(nx - 1));
+  y = xo_clampd(y, (double)(ny - 1));
+  z = xo_clampd(z, (double)(nz - 1));
+  int64_t ix = (int64_t)floor(x), iy = (int64_t)floor(y), iz = (int64_t)floor(z);
+  if (ix > nx - 2) ix = nx - 2;
+  if (iy > ny - 2) iy = ny - 2;
+  if (iz > nz - 2) iz = nz - 2;
+  const double fx = x - (double)ix, fy = y - (double)iy, fz = z - (double)iz;
+  const int64_t sy = nx, sz = nx * ny;
+  const float* p = vol + iz * sz + iy * sy + ix;
+  const double v000 = p[0], v100 = p[1], v010 = p[sy], v110 = p[sy + 1];
+  const double v001 = p[sz], v101 = p[sz + 1], v011 = p[sz + sy], v111 = p[sz + sy + 1];
+  const double a00 = v000 + (v100 - v000) * fx;
+  const double a10 = v010 + (v110 - v010) * fx;
+  const double a01 = v001 + (v101 - v001) * fx;
+  const double a11 = v011 + (v111 - v011) * fx;
+  const double b0 = a00 + (a10 - a00) * fy;
+  const double b1 = a01 + (a11 - a01) * fy;
+  return b0 + (b1 - b0) * fz;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Line integrals                                                             */
+/* ------------------------------------------------------------------------- */
+enum { XO_KERNEL_SUM = 0, XO_KERNEL_MAX = 1 };
+enum { XO_STORE_REPLACE = 0, XO_STORE_ACCUM = 1 };
+
+typedef struct {
+  const float* vol;
+  int64_t n[3];
+  const xo_proj_geom* geo;   /* [num_projs] */
+  int64_t rows, cols;
+  float step;
+  int kernel;
+  float* out;
+  double* out64;             /* FP64 mode output (NULL in FP32 mode) */
+  uint64_t* nsamples;        /* optional per-ray sample count */
+  const double* geo64;       /* FP64 mode: per projection 21 doubles */
+} xo_drr_ctx;
+
+/* FP32 per-ray semantics (the "xReg CPU" target), fixed op order, no FMA. */
+static void xo_drr_f32_range(void* vctx, int64_t b, int64_t e) {
+  xo_drr_ctx* c = (xo_drr_ctx*)vctx;
+  const int64_t npix = c->rows * c->cols;
+  const float maxb[3] = {(float)(c->n[0] - 1), (float)(c->n[1] - 1), (float)(c->n[2] - 1)};
+  for (int64_t idx = b; idx < e; ++idx) {
+    const int64_t p = idx / npix;
+    const int64_t off = idx - p * npix;
+    const int64_t row = off / c->cols;
+    const int64_t col = off - row * c->cols;
+    const xo_proj_geom* g = &c->geo[p];
+    const float fc = (float)col, fr = (float)row;
+    float dir[3], v[3];
+    for (int k = 0; k < 3; ++k) {
+      float t1 = fc * g->dc[k];
+      float t2 = g->d0[k] + t1;
+      float t3 = fr * g->dr[k];
+      dir[k] = t2 + t3;
+      float u1 = fc * g->ec[k];
+      float u2 = g->e0[k] + u1;
+      float u3 = fr * g->er[k];
+      v[k] = u2 + u3;
+    }
+    /* RayRectIntersect, limited to the segment (xregSpatialPrimitives.cpp:176-221) */
+    int hit = 1;
+    float t0 = 0.0f, t1 = 1.0f;
+    for (int k = 0; k < 3; ++k) {
+      if ((double)fabsf(dir[k]) > 1.0e-8) {
+        const float inv = 1.0f / dir[k];
+        float ta = (0.0f - g->src[k]) * inv;
+        float tb = (maxb[k] - g->src[k]) * inv;
+        if (tb < ta) { float tmp = ta; ta = tb; tb = tmp; }
+        t0 = (t0 < ta) ? ta : t0;
+        t1 = (tb < t1) ? tb : t1;
+        if (t0 > t1) { hit = 0; break; }
+      } else if (g->src[k] < 0.0f || g->src[k] > maxb[k]) {
+        hit = 0; break;
+      }
+    }
+    float sum = (c->kernel == XO_KERNEL_MAX) ? -FLT_MAX : 0.0f;
+    uint64_t ns = 0;
+    if (hit && ((t1 - t0) > 2.0e-3f)) {
+      t0 = t0 + 1.0e-3f;
+      t1 = t1 - 1.0e-3f;
+      float pos[3];
+      for (int k = 0; k < 3; ++k) {
+        float a = t0 * dir[k];
+        pos[k] = g->src[k] + a;
+      }
+      const float vv0 = v[0] * v[0];
+      const float vv1 = v[1] * v[1];
+      const float vv2 = v[2] * v[2];
+      const float lc = sqrtf((vv0 + vv1) + vv2);
+      const float dt = t1 - t0;
+      const float len = dt * lc;
+      const uint64_t nsteps = (uint64_t)(len / c->step);
+      const float sc = c->step / lc;
+      float stepv[3] = {dir[0] * sc, dir[1] * sc, dir[2] * sc};
+      for (uint64_t s = 0; s <= nsteps; ++s) {
+        const float val = (float)xo_trilinear(c->vol, c->n[0], c->n[1], c->n[2], pos[0], pos[1], pos[2]);
+        if (c->kernel == XO_KERNEL_MAX) sum = (sum < val) ? val : sum;
+        else sum = sum + val;
+        pos[0] = pos[0] + stepv[0];
+        pos[1] = pos[1] + stepv[1];
+        pos[2] = pos[2] + stepv[2];
+      }
+      sum = sum * c->step;
+      ns = nsteps + 1;
+    }
+    /* aa_sum = 0 + sum * 1 (xregRayCastLineIntCPU.cpp:189,282) */
+    const float aa = 0.0f + sum;
+    const float prev = c->out[idx];
+    c->out[idx] = (c->kernel == XO_KERNEL_MAX) ? ((prev < aa) ? aa : prev) : (prev + aa);
+    if (c->nsamples) c->nsamples[idx] = ns;
+  }
+}
+
+/* FP64 twin: the same algorithm with every quantity in double; geometry from
+ * double set-up vectors.  It is the error reference, not the parity target. */
+static void xo_drr_f64_range(void* vctx, int64_t b, int64_t e) {
+  xo_drr_ctx* c = (xo_drr_ctx*)vctx;
+  const int64_t npix = c->rows * c->cols;
+  const double maxb[3] = {(double)(c->n[0] - 1), (double)(c->n[1] - 1), (double)(c->n[2] - 1)};
+  const double step = (double)c->step;
+  for (int64_t idx = b; idx < e; ++idx) {
+    const int64_t p = idx / npix;
+    const int64_t off = idx - p * npix;
+    const int64_t row = off / c->cols;
+    const int64_t col = off - row * c->cols;
+    const double* g = c->geo64 + p * 21;
+    const double* src = g;
+    const double* d0 = g + 3; const double* dc = g + 6; const double* dr = g + 9;
+    const double* e0 = g + 12; const double* ec = g + 15; const double* er = g + 18;
+    double dir[3], v[3];
+    for (int k = 0; k < 3; ++k) {
+      dir[k] = (d0[k] + (double)col * dc[k]) + (double)row * dr[k];
+      v[k] = (e0[k] + (double)col * ec[k]) + (double)row * er[k];
+    }
+    int hit = 1;
+    double t0 = 0.0, t1 = 1.0;
+    for (int k = 0; k < 3; ++k) {
+      if (fabs(dir[k]) > 1.0e-8) {
+        const double inv = 1.0 / dir[k];
+        double ta = (0.0 - src[k]) * inv, tb = (maxb[k] - src[k]) * inv;
+        if (tb < ta) { double tmp = ta; ta = tb; tb = tmp; }
+        t0 = (t0 < ta) ? ta : t0;
+        t1 = (tb < t1) ? tb : t1;
+        if (t0 > t1) { hit = 0; break; }
+      } else if (src[k] < 0.0 || src[k] > maxb[k]) {
+        hit = 0; break;
+      }
+    }
+    double sum = (c->kernel == XO_KERNEL_MAX) ? -DBL_MAX : 0.0;
+    uint64_t ns = 0;
+    if (hit && ((t1 - t0) > 2.0e-3)) {
+      t0 += 1.0e-3;
+      t1 -= 1.0e-3;
+      double pos[3] = {src[0] + t0 * dir[0], src[1] + t0 * dir[1], src[2] + t0 * dir[2]};
+      const double lc = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      const uint64_t nsteps = (uint64_t)(((t1 - t0) * lc) / step);
+      const double sc = step / lc;
+      const double stepv[3] = {dir[0] * sc, dir[1] * sc, dir[2] * sc};
+      for (uint64_t s = 0; s <= nsteps; ++s) {
+        const double val = xo_trilinear(c->vol, c->n[0], c->n[1], c->n[2], pos[0], pos[1], pos[2]);
+        if (c->kernel == XO_KERNEL_MAX) sum = (sum < val) ? val : sum;
+        else sum += val;
+        pos[0] += stepv[0]; pos[1] += stepv[1]; pos[2] += stepv[2];
+      }
+      sum *= step;
+      ns = nsteps + 1;
+    }
+    const double prev = c->out64[idx];
+    c->out64[idx] = (c->kernel == XO_KERNEL_MAX) ? ((prev < sum) ? sum : prev) : (prev + sum);
+    if (c->nsamples) c->nsamples[idx] = ns;
+  }
+}
+
+/* Double set-up vectors for the FP64 twin (no float rounding). */
+static void xo_proj_geom_one_f64(const xo_vol_geom* vg, const xo_camera* cam,
+                                 const double pose[16], double out[21]) {
+  double A[9], Ai[9], ti[3], Ki[9], ER[9], Et[3], pin[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A[i * 3 + j] = vg->direction[i * 3 + j] * vg->spacing[j];
+  m3_inverse(A, Ai);
+  m3_vec(Ai, vg->origin, ti);
+  for (int k = 0; k < 3; ++k) ti[k] = -ti[k];
+  m3_inverse(cam->intrins, Ki);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) ER[i * 3 + j] = cam->extrins[j * 4 + i];
+  {
+    double t[3] = {cam->extrins[3], cam->extrins[7], cam->extrins[11]};
+    m3_vec(ER, t, Et);
+    for (int k = 0; k < 3; ++k) Et[k] = -Et[k];
+  }
+  const double f = cam->focal_len;
+  if (cam->coord_frame_type == 2) {
+    double pz[3] = {0.0, 0.0, f}, tmp[3];
+    m3_vec(ER, pz, tmp);
+    for (int k = 0; k < 3; ++k) pin[k] = tmp[k] + Et[k];
+  } else {
+    for (int k = 0; k < 3; ++k) pin[k] = Et[k];
+  }
+  const double dz = (cam->coord_frame_type == 1) ? -f : f;
+  const double zadj = (cam->coord_frame_type == 2) ? -f : 0.0;
+  double kc[3] = {Ki[0] * dz, Ki[3] * dz, Ki[6] * dz};
+  double kr[3] = {Ki[1] * dz, Ki[4] * dz, Ki[7] * dz};
+  double k0[3] = {Ki[2] * dz, Ki[5] * dz, Ki[8] * dz + zadj};
+  double dcol[3], drow[3], det0[3], e0[3];
+  m3_vec(ER, kc, dcol);
+  m3_vec(ER, kr, drow);
+  m3_vec(ER, k0, det0);
+  for (int k = 0; k < 3; ++k) { det0[k] += Et[k]; e0[k] = det0[k] - pin[k]; }
+  double TR[9], Tt[3], MR[9], Mt[3];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) TR[i * 3 + j] = pose[i * 4 + j];
+    Tt[i] = pose[i * 4 + 3];
+  }
+  m3_mul(Ai, TR, MR);
+  m3_vec(Ai, Tt, Mt);
+  for (int k = 0; k < 3; ++k) Mt[k] += ti[k];
+  double src[3];
+  m3_vec(MR, pin, src);
+  for (int k = 0; k < 3; ++k) src[k] += Mt[k];
+  m3_vec(MR, e0, out + 3);
+  m3_vec(MR, dcol, out + 6);
+  m3_vec(MR, drow, out + 9);
+  for (int k = 0; k < 3; ++k) {
+    out[k] = src[k];
+    out[12 + k] = e0[k];
+    out[15 + k] = dcol[k];
+    out[18 + k] = drow[k];
+  }
+}
+
+static int xo_check_cams(const xo_camera* cams, int64_t ncams) {
+  for (int64_t i = 1; i < ncams; ++i)
+    if (cams[i].num_det_rows != cams[0].num_det_rows || cams[i].num_det_cols != cams[0].num_det_cols) return -1;
+  return 0;
+}
+
+/* Pre-compute of the projection buffer (xregRayCastBaseCPU.cpp:128-158).
+ * bg_projs (optional): one image per camera, used when use_bg_projs. */
+static void xo_pre_compute_f32(float* out, int64_t nproj, int64_t npix, int store, float default_bg,
+                               const float* bg_projs, const int32_t* cam_idx) {
+  if (bg_projs)
+    for (int64_t p = 0; p < nproj; ++p)
+      memcpy(out + p * npix, bg_projs + (int64_t)cam_idx[p] * npix, sizeof(float) * (size_t)npix);
+  if (store == XO_STORE_REPLACE && !bg_projs)
+    for (int64_t i = 0; i < nproj * npix; ++i) out[i] = default_bg;
+}
+
+/* Line-integral DRRs, FP32 xReg-CPU semantics.
+ * poses: [nproj][16] row-major cam -> ITK physical; cam_idx: [nproj].
+ * out: [nproj][rows][cols]; nsamples (optional): per-ray sample counts. */
+XO_EXPORT int xo_drr_f32(const float* vol, const xo_vol_geom* vg,
+                         const xo_camera* cams, int64_t ncams,
+                         const double* poses, const int32_t* cam_idx, int64_t nproj,
+                         float step, int kernel, int store, float default_bg,
+                         const float* bg_projs, float* out, uint64_t* nsamples) {
+  if (xo_check_cams(cams, ncams)) return -1;
+  xo_proj_geom* geo = (xo_proj_geom*)malloc(sizeof(xo_proj_geom) * (size_t)nproj);
+  for (int64_t p = 0; p < nproj; ++p) xo_proj_geom_one(vg, &cams[cam_idx[p]], poses + 16 * p, &geo[p]);
+  const int64_t rows = cams[0].num_det_rows, cols = cams[0].num_det_cols;
+  xo_pre_compute_f32(out, nproj, rows * cols, store, default_bg, bg_projs, cam_idx);
+  xo_drr_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.vol = vol; c.n[0] = vg->n[0]; c.n[1] = vg->n[1]; c.n[2] = vg->n[2];
+  c.geo = geo; c.rows = rows; c.cols = cols; c.step = step; c.kernel = kernel;
+  c.out = out; c.nsamples = nsamples;
+  xo_parallel_for(xo_drr_f32_range, &c, nproj * rows * cols, 256);
+  free(geo);
+  return 0;
+}
+
+/* FP64 twin.  out: double[nproj][rows][cols]; replace mode with default_bg. */
+XO_EXPORT int xo_drr_f64(const float* vol, const xo_vol_geom* vg,
+                         const xo_camera* cams, int64_t ncams,
+                         const double* poses, const int32_t* cam_idx, int64_t nproj,
+                         float step, int kernel, double default_bg,
+                         double* out, uint64_t* nsamples) {
+  if (xo_check_cams(cams, ncams)) return -1;
+  double* geo = (double*)malloc(sizeof(double) * 21 * (size_t)nproj);
+  for (int64_t p = 0; p < nproj; ++p) xo_proj_geom_one_f64(vg, &cams[cam_idx[p]], poses + 16 * p, geo + 21 * p);
+  const int64_t rows = cams[0].num_det_rows, cols = cams[0].num_det_cols;
+  for (int64_t i = 0; i < nproj * rows * cols; ++i) out[i] = default_bg;
+  xo_drr_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.vol = vol; c.n[0] = vg->n[0]; c.n[1] = vg->n[1]; c.n[2] = vg->n[2];
+  c.geo64 = geo; c.rows = rows; c.cols = cols; c.step = step; c.kernel = kernel;
+  c.out64 = out; c.nsamples = nsamples;
+  xo_parallel_for(xo_drr_f64_range, &c, nproj * rows * cols, 256);
+  free(geo);
+  return 0;
+}
+
+/* Exposes the float set-up vectors (for tests of the geometry contract). */
+XO_EXPORT void xo_proj_geoms(const xo_vol_geom* vg, const xo_camera* cams, const double* poses,
+                             const int32_t* cam_idx, int64_t nproj, xo_proj_geom* out) {
+  for (int64_t p = 0; p < nproj; ++p) xo_proj_geom_one(vg, &cams[cam_idx[p]], poses + 16 * p, &out[p]);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Camera model helpers                                                       */
+/* ------------------------------------------------------------------------- */
+/* CameraModel::setup(f, nr, nc, rs, cs) with MakeNaiveIntrins
+ * (xregPerspectiveXform.cpp:200-254); frame type 1 (-z) by default. */
+XO_EXPORT void xo_camera_setup_naive(double f, int64_t nr, int64_t nc, double rs, double cs,
+                                     int32_t frame_type, xo_camera* cam) {
+  memset(cam, 0, sizeof(*cam));
+  cam->coord_frame_type = frame_type;
+  cam->focal_len = f;
+  cam->num_det_rows = nr; cam->num_det_cols = nc;
+  cam->det_row_spacing = rs; cam->det_col_spacing = cs;
+  double K[9] = {f / cs, 0, 0, 0, f / rs, 0, 0, 0, 1};
+  if (frame_type == 1) { K[0] = -K[0]; K[4] = -K[4]; }
+  K[2] = (double)(nc - 1) * 0.5;
+  K[5] = (double)(nr - 1) * 0.5;
+  memcpy(cam->intrins, K, sizeof(K));
+  for (int i = 0; i < 16; ++i) cam->extrins[i] = (i % 5 == 0) ? 1.0 : 0.0;
+}
+
+/* DownsampleCameraModel (xregPerspectiveXform.cpp:654-689). */
+XO_EXPORT void xo_camera_downsample(const xo_camera* src, double ds, int force_even, xo_camera* dst) {
+  *dst = *src;
+  dst->intrins[0] *= ds; dst->intrins[4] *= ds; dst->intrins[2] *= ds; dst->intrins[5] *= ds;
+  long nr = lround((double)src->num_det_rows * ds);
+  long nc = lround((double)src->num_det_cols * ds);
+  if (force_even) { if (nr % 2) --nr; if (nc % 2) --nc; }
+  dst->num_det_rows = nr; dst->num_det_cols = nc;
+  dst->det_row_spacing = src->det_row_spacing / ds;
+  dst->det_col_spacing = src->det_col_spacing / ds;
+  /* FocalLenFromIntrins (xregPerspectiveXform.cpp:186-190) */
+  const double xps = dst->det_col_spacing, yps = dst->det_row_spacing;
+  dst->focal_len = (fabs(dst->intrins[0] * xps) + fabs(dst->intrins[4] * ((yps < 0) ? xps : yps))) / 2.0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* 2D metrics (double arithmetic; float images in, double values out)         */
+/* ------------------------------------------------------------------------- */
+static inline int64_t xo_reflect101(int64_t i, int64_t n) {
+  if (n == 1) return 0;
+  while (i < 0 || i >= n) {
+    if (i < 0) i = -i;
+    if (i >= n) i = 2 * (n - 1) - i;
+  }
+  return i;
+}
+
+/* cv::GaussianBlur(5x5, sigma 0) then cv::Sobel dx / dy, reflect-101 borders
+ * (xregImgSimMetric2DGradImgCPU.cpp:48-65,86-101).  smooth_ksize 0 disables the
+ * blur; only 5 (kernel [1 4 6 4 1]/16) and 3 ([1 2 1]/4) are supported. */
+XO_EXPORT int xo_grad_images(const float* img, int64_t rows, int64_t cols, int smooth_ksize,
+                             double* gx, double* gy) {
+  const double k5[5] = {0.0625, 0.25, 0.375, 0.25, 0.0625};
+  const double k3[3] = {0.25, 0.5, 0.25};
+  const double* k = NULL;
+  int kr = 0;
+  if (smooth_ksize == 5) { k = k5; kr = 2; }
+  else if (smooth_ksize == 3) { k = k3; kr = 1; }
+  else if (smooth_ksize != 0) return -1;
+  const int64_t n = rows * cols;
+  double* src = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int64_t i = 0; i < n; ++i) src[i] = img[i];
+  if (k) {
+    double* tmp = (double*)malloc(sizeof(double) * (size_t)n);
+    for (int64_t r = 0; r < rows; ++r)
+      for (int64_t c = 0; c < cols; ++c) {
+        double s = 0;
+        for (int t = -kr; t <= kr; ++t) s += k[t + kr] * src[r * cols + xo_reflect101(c + t, cols)];
+        tmp[r * cols + c] = s;
+      }
+    for (int64_t r = 0; r < rows; ++r)
+      for (int64_t c = 0; c < cols; ++c) {
+        double s = 0;
+        for (int t = -kr; t <= kr; ++t) s += k[t + kr] * tmp[xo_reflect101(r + t, rows) * cols + c];
+        src[r * cols + c] = s;
+      }
+    free(tmp);
+  }
+  for (int64_t r = 0; r < rows; ++r) {
+    const int64_t ru = xo_reflect101(r - 1, rows), rd = xo_reflect101(r + 1, rows);
+    for (int64_t c = 0; c < cols; ++c) {
+      const int64_t cl = xo_reflect101(c - 1, cols), cr = xo_reflect101(c + 1, cols);
+      const double a = src[ru * cols + cl], b = src[ru * cols + c], cc = src[ru * cols + cr];
+      const double d = src[r * cols + cl], f = src[r * cols + cr];
+      const double g = src[rd * cols + cl], h = src[rd * cols + c], ii = src[rd * cols + cr];
+      gx[r * cols + c] = ((cc - a) + 2.0 * (f - d)) + (ii - g);
+      gy[r * cols + c] = ((g - a) + 2.0 * (h - b)) + (ii - cc);
+    }
+  }
+  free(src);
+  return 0;
+}
+
+/* NCC sim value (1 - ncc)/2 of one moving image against one fixed image
+ * (xregImgSimMetric2DNCCCPU.cpp:53-63,164-209): sample std dev (n-1) clamped at
+ * 1e-6, dot product divided by n.  mask (optional, nonzero = use). */
+static double xo_ncc_one_d(const double* f, const double* m, int64_t n, const uint8_t* mask) {
+  int64_t len = 0;
+  double sf = 0, sm = 0;
+  for (int64_t i = 0; i < n; ++i)
+    if (!mask || mask[i]) { sf += f[i]; sm += m[i]; ++len; }
+  const double mf = sf / (double)len, mm = sm / (double)len;
+  double vf = 0, vm = 0, cov = 0;
+  for (int64_t i = 0; i < n; ++i)
+    if (!mask || mask[i]) {
+      const double a = f[i] - mf, b = m[i] - mm;
+      vf += a * a; vm += b * b; cov += a * b;
+    }
+  double sdf = sqrt(vf / (double)(len - 1)); if (sdf < 1.0e-6) sdf = 1.0e-6;
+  double sdm = sqrt(vm / (double)(len - 1)); if (sdm < 1.0e-6) sdm = 1.0e-6;
+  const double ncc = cov / ((double)len * sdf * sdm);
+  return (1.0 - ncc) * 0.5;
+}
+
+XO_EXPORT void xo_ncc(const float* fixed, const float* mov, int64_t npix, int64_t nimgs,
+                      const uint8_t* mask, double* out) {
+  double* f = (double*)malloc(sizeof(double) * (size_t)npix);
+  double* m = (double*)malloc(sizeof(double) * (size_t)npix);
+  for (int64_t i = 0; i < npix; ++i) f[i] = fixed[i];
+  for (int64_t k = 0; k < nimgs; ++k) {
+    for (int64_t i = 0; i < npix; ++i) m[i] = mov[k * npix + i];
+    out[k] = xo_ncc_one_d(f, m, npix, mask);
+  }
+  free(f); free(m);
+}
+
+/* Grad-NCC: 0.5 * (NCC(gx_f, gx_m) + NCC(gy_f, gy_m)) (xregImgSimMetric2DGradNCCCPU.cpp:51-65). */
+XO_EXPORT int xo_grad_ncc(const float* fixed, const float* mov, int64_t rows, int64_t cols, int64_t nimgs,
+                          int smooth_ksize, const uint8_t* mask, double* out) {
+  const int64_t n = rows * cols;
+  double* fgx = (double*)malloc(sizeof(double) * (size_t)n);
+  double* fgy = (double*)malloc(sizeof(double) * (size_t)n);
+  double* mgx = (double*)malloc(sizeof(double) * (size_t)n);
+  double* mgy = (double*)malloc(sizeof(double) * (size_t)n);
+  int rc = xo_grad_images(fixed, rows, cols, smooth_ksize, fgx, fgy);
+  for (int64_t k = 0; rc == 0 && k < nimgs; ++k) {
+    rc = xo_grad_images(mov + k * n, rows, cols, smooth_ksize, mgx, mgy);
+    if (rc) break;
+    out[k] = 0.5 * (xo_ncc_one_d(fgx, mgx, n, mask) + xo_ncc_one_d(fgy, mgy, n, mask));
+  }
+  free(fgx); free(fgy); free(mgx); free(mgy);
+  return rc;
+}
+
+/* Mean and sample std dev of one patch, two passes, std dev clamped at 1e-6
+ * (xregImgSimMetric2DPatchNCCCPU.cpp:558-619, no mask). */
+static void xo_patch_stats(const double* img, int64_t cols, int64_t r0, int64_t c0, int64_t diam,
+                           double* mean, double* sd) {
+  const int64_t np = diam * diam;
+  double s = 0;
+  for (int64_t r = 0; r < diam; ++r)
+    for (int64_t c = 0; c < diam; ++c) s += img[(r0 + r) * cols + c0 + c];
+  const double mu = s / (double)np;
+  double v = 0;
+  for (int64_t r = 0; r < diam; ++r)
+    for (int64_t c = 0; c < diam; ++c) { const double t = img[(r0 + r) * cols + c0 + c] - mu; v += t * t; }
+  v /= (double)(np - 1);
+  double d = sqrt(v);
+  *mean = mu;
+  *sd = d < 1.0e-6 ? 1.0e-6 : d;
+}
+
+/* Patch NCC of one moving image: patch centres radius..n-1-radius with stride
+ * (xregImgSimMetric2DPatchCommon.cpp:256-300); per patch score 1 - sum(((m-mu_m)/sd_m) * fhat)
+ * with fhat = (f - mu_f)/(sd_f * n_patch); unit weights, so the combined value is
+ * the mean score (xregImgSimMetric2DPatchNCCCPU.cpp:205-287). */
+static double xo_patch_ncc_one(const double* f, const double* m, int64_t rows, int64_t cols,
+                               int64_t radius, int64_t stride) {
+  const int64_t diam = 2 * radius + 1, np = diam * diam;
+  double total = 0;
+  int64_t count = 0;
+  for (int64_t cr = radius; cr + radius <= rows - 1; cr += stride)
+    for (int64_t cc = radius; cc + radius <= cols - 1; cc += stride) {
+      double mf, sf, mm, sm;
+      xo_patch_stats(f, cols, cr - radius, cc - radius, diam, &mf, &sf);
+      xo_patch_stats(m, cols, cr - radius, cc - radius, diam, &mm, &sm);
+      double acc = 0;
+      for (int64_t r = 0; r < diam; ++r)
+        for (int64_t c = 0; c < diam; ++c) {
+          const int64_t i = (cr - radius + r) * cols + cc - radius + c;
+          const double fh = (f[i] - mf) / (sf * (double)np);
+          acc += ((m[i] - mm) / sm) * fh;
+        }
+      total += 1.0 - acc;
+      ++count;
+    }
+  return total / (double)count;
+}
+
+XO_EXPORT void xo_patch_ncc(const float* fixed, const float* mov, int64_t rows, int64_t cols, int64_t nimgs,
+                            int64_t radius, int64_t stride, double* out) {
+  const int64_t n = rows * cols;
+  double* f = (double*)malloc(sizeof(double) * (size_t)n);
+  double* m = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int64_t i = 0; i < n; ++i) f[i] = fixed[i];
+  for (int64_t k = 0; k < nimgs; ++k) {
+    for (int64_t i = 0; i < n; ++i) m[i] = mov[k * n + i];
+    out[k] = xo_patch_ncc_one(f, m, rows, cols, radius, stride);
+  }
+  free(f); free(m);
+}
+
+typedef struct {
+  const double *fgx, *fgy;
+  const float* mov;
+  int64_t rows, cols, radius, stride;
+  int smooth;
+  double* out;
+} xo_pgncc_ctx;
+
+static void xo_pgncc_range(void* vctx, int64_t b, int64_t e) {
+  xo_pgncc_ctx* c = (xo_pgncc_ctx*)vctx;
+  const int64_t n = c->rows * c->cols;
+  double* mgx = (double*)malloc(sizeof(double) * (size_t)n);
+  double* mgy = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int64_t k = b; k < e; ++k) {
+    xo_grad_images(c->mov + k * n, c->rows, c->cols, c->smooth, mgx, mgy);
+    c->out[k] = 0.5 * (xo_patch_ncc_one(c->fgx, mgx, c->rows, c->cols, c->radius, c->stride) +
+                       xo_patch_ncc_one(c->fgy, mgy, c->rows, c->cols, c->radius, c->stride));
+  }
+  free(mgx); free(mgy);
+}
+
+/* Patch grad-NCC (xregImgSimMetric2DPatchGradNCCCPU.cpp:104-230): blur + Sobel,
+ * patch NCC on gx and on gy with the same patches, 0.5 * (s_x + s_y).
+ * Parallel over moving images. */
+XO_EXPORT int xo_patch_grad_ncc(const float* fixed, const float* mov, int64_t rows, int64_t cols, int64_t nimgs,
+                                int smooth_ksize, int64_t radius, int64_t stride, double* out) {
+  const int64_t n = rows * cols;
+  double* fgx = (double*)malloc(sizeof(double) * (size_t)n);
+  double* fgy = (double*)malloc(sizeof(double) * (size_t)n);
+  int rc = xo_grad_images(fixed, rows, cols, smooth_ksize, fgx, fgy);
+  if (rc == 0) {
+    xo_pgncc_ctx c = {fgx, fgy, mov, rows, cols, radius, stride, smooth_ksize, out};
+    xo_parallel_for(xo_pgncc_range, &c, nimgs, 1);
+  }
+  free(fgx); free(fgy);
+  return rc;
+}
+
+typedef struct {
+  const float* fixed;
+  const float* mov;
+  int64_t rows, cols;
+  int smooth;
+  double* out;
+} xo_gncc_ctx;
+
+static void xo_gncc_range(void* vctx, int64_t b, int64_t e) {
+  xo_gncc_ctx* c = (xo_gncc_ctx*)vctx;
+  xo_grad_ncc(c->fixed, c->mov + b * c->rows * c->cols, c->rows, c->cols, e - b, c->smooth, NULL, c->out + b);
+}
+
+/* Grad-NCC parallel over moving images (CPU baseline timing path). */
+XO_EXPORT void xo_grad_ncc_par(const float* fixed, const float* mov, int64_t rows, int64_t cols, int64_t nimgs,
+                               int smooth_ksize, double* out) {
+  xo_gncc_ctx c = {fixed, mov, rows, cols, smooth_ksize, out};
+  xo_parallel_for(xo_gncc_range, &c, nimgs, 1);
+}
+
+/* HU -> linear attenuation (xregHUToLinAtt.cpp:45-69, mu_water 0.02683,
+ * mu_air 0.02485e-4, hu_lower -1000), double math, float result. */
+XO_EXPORT void xo_hu_to_lin_att(const float* hu, int64_t n, float* out) {
+  const double mu_w = 0.02683 * 1.0, mu_a = 0.02485 * 0.0001, hu_lower = -1000.0;
+  const double hu_scale = (mu_w - mu_a) * 1.0e-3;
+  const double mu_lower = (hu_lower * hu_scale) + mu_w;
+  for (int64_t i = 0; i < n; ++i) {
+    const double v = ((double)hu[i] * hu_scale) + mu_w - mu_lower;
+    out[i] = (float)(v > 0.0 ? v : 0.0);
+  }
+}

@@ -1,0 +1,201 @@
+"""GPU DRR parity against the CPU oracle, through the C ABI.
+
+Tolerances (stated in the workload definitions): DRR max relative error <= 1e-4
+with a float32 volume and <= 2e-3 with a half-precision (FP16 or BF16) volume,
+measured against the oracle's FP32 xReg-CPU semantics on the same float32
+volume.  Rays that the oracle leaves at the background must be exactly the
+background on the GPU, and the per-ray sample counts must agree exactly.
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import drr_rel_err, oracle_cams, oracle_geom, small_camera, small_volume
+from xreg_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-4
+TOL16 = 2e-3
+
+
+def _rc(xr, vol, cams, step, voxel_type=0):
+    rc = xr.RayCasterLineIntCUDA()
+    rc.set_volume(vol, voxel_type)
+    rc.set_camera_models(cams)
+    rc.set_ray_step_size(step)
+    return rc
+
+
+def _gpu_drr(xr, vol, cams, poses, step, voxel_type=0, count=False):
+    rc = _rc(xr, vol, cams, step, voxel_type)
+    rc.set_num_projs(len(poses) * len(cams))
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(poses)
+    rc.set_count_samples(count)
+    rc.compute(0)
+    out = rc.projs()
+    ns = rc.last_num_samples() if count else None
+    return out, ns
+
+
+def test_plain_workload_fp32(xr, oracle):
+    w = synth.plain_small(0)
+    pose = synth.fixed_pose(w)
+    g, ns_gpu = _gpu_drr(xr, w.vol, w.cams, pose[None], w.step, count=True)
+    o, ns = oracle.drr_f32(w.vol.voxels, oracle_geom(w.vol), oracle_cams(w.cams), pose[None], step=w.step,
+                           count=True)
+    rel, zero = drr_rel_err(g, o)
+    assert zero == 0.0
+    assert rel <= TOL32, rel
+    assert ns_gpu == int(ns.sum())
+
+
+def test_population_of_poses_fp32(xr, oracle):
+    vol = small_volume(1, (48, 44, 40), (1.5, 1.5, 1.5))
+    cam = small_camera((40, 56), 3.0)
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 12, 10.0, 20.0, seed=4)
+    g, ns_gpu = _gpu_drr(xr, vol, [cam], poses, 0.5, count=True)
+    o, ns = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=0.5, count=True)
+    rel, zero = drr_rel_err(g, o)
+    assert zero == 0.0 and rel <= TOL32, rel
+    assert ns_gpu == int(ns.sum())
+
+
+def test_two_views_distribute(xr, oracle):
+    vol = small_volume(2)
+    cams = [small_camera((32, 36), 4.0), small_camera((32, 36), 4.0)]
+    # the second camera orbits 30 degrees about the volume centre, which sits at
+    # camera-world (0, 0, -700): world -> camera extrinsic fixing that point
+    from xreg_gb300.se3 import rigid, euler_xyz
+    R = euler_xyz(0.0, np.radians(30.0), 0.0)
+    c = np.array([0.0, 0.0, -synth.SOURCE_TO_CENTRE_MM])
+    cams[1].set_extrins(rigid(R, c - R @ c))
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 5, 5.0, 10.0, seed=8)
+    g, _ = _gpu_drr(xr, vol, cams, poses, 0.7)
+    ci = np.repeat(np.arange(2, dtype=np.int32), len(poses))
+    o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams(cams), np.concatenate([poses, poses]),
+                       cam_idx=ci, step=0.7)
+    rel, zero = drr_rel_err(g, o)
+    assert zero == 0.0 and rel <= TOL32, rel
+    assert not np.allclose(g[0], g[len(poses)])  # the views differ
+
+
+@pytest.mark.parametrize("vt,tol", [(1, TOL16), (2, TOL16)])
+def test_half_precision_volumes(xr, oracle, vt, tol):
+    w = synth.plain_small(5)
+    pose = synth.fixed_pose(w)
+    g, _ = _gpu_drr(xr, w.vol, w.cams, pose[None], w.step, voxel_type=vt)
+    o = oracle.drr_f32(w.vol.voxels, oracle_geom(w.vol), oracle_cams(w.cams), pose[None], step=w.step)
+    rel, zero = drr_rel_err(g, o)
+    assert zero == 0.0 and rel <= tol, rel
+
+
+def test_anisotropic_oriented_volume(xr, oracle):
+    vol = small_volume(3, (40, 32, 28), (0.8, 1.1, 1.7))
+    from xreg_gb300.se3 import euler_xyz
+    vol.direction = euler_xyz(0.1, -0.2, 0.3)
+    vol.origin = (-12.0, 30.0, 5.5)
+    cam = small_camera((36, 44), 3.5)
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 4, 8.0, 5.0, seed=2)
+    g, ns_gpu = _gpu_drr(xr, vol, [cam], poses, 0.33, count=True)
+    o, ns = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=0.33, count=True)
+    rel, zero = drr_rel_err(g, o)
+    assert zero == 0.0 and rel <= TOL32, rel
+    assert ns_gpu == int(ns.sum())
+
+
+@pytest.mark.parametrize("frame", [0, 1, 2])
+def test_camera_frames(xr, oracle, frame):
+    vol = small_volume(4)
+    cam = xr.CameraModel.naive(synth.SDD_MM, 30, 34, 4.0, 4.0, coord_frame_type=frame)
+    pose = synth.gt_pose(vol)
+    from xreg_gb300.se3 import rigid
+    if frame == 0:
+        # +z towards the detector: the volume centre must sit at camera (0, 0, +700)
+        pose = pose @ rigid(np.diag([1.0, -1.0, -1.0]), [0.0, 0.0, 0.0])
+    elif frame == 2:
+        # origin on the detector, source at z = +f: volume centre at z = f - 700
+        pose = pose @ rigid(np.eye(3), [0.0, 0.0, -synth.SDD_MM])
+    g, _ = _gpu_drr(xr, vol, [cam], pose[None], 0.5)
+    o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), pose[None], step=0.5)
+    assert o.max() > 0
+    rel, zero = drr_rel_err(g, o)
+    assert zero == 0.0 and rel <= TOL32, rel
+
+
+def test_store_methods_max_kernel_and_background(xr, oracle):
+    vol = small_volume(6)
+    cam = small_camera((33, 37), 4.0)
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 3, 5.0, 5.0, seed=1)
+    G, cams = oracle_geom(vol), oracle_cams([cam])
+    rc = _rc(xr, vol, [cam], 0.5)
+    rc.set_num_projs(3)
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(poses)
+    # replace with a default background
+    rc.set_default_bg_pixel_val(1.25)
+    rc.compute()
+    base = oracle.drr_f32(vol.voxels, G, cams, poses, step=0.5, default_bg=1.25)
+    assert drr_rel_err(rc.projs(), base)[0] <= TOL32
+    # accumulate: a second compute adds the line integrals again
+    rc.use_proj_store_accum_method()
+    rc.compute()
+    acc = oracle.drr_f32(vol.voxels, G, cams, poses, step=0.5, store=1, out=base.copy())
+    assert drr_rel_err(rc.projs(), acc)[0] <= TOL32
+    # background images replace the buffer before the sum (even in accumulate mode)
+    bgimg = np.random.default_rng(0).random((33, 37)).astype(np.float32)
+    rc.set_bg_projs([bgimg], True)
+    rc.compute()
+    bgref = oracle.drr_f32(vol.voxels, G, cams, poses, step=0.5, store=1, bg_projs=bgimg[None],
+                           out=np.zeros_like(base))
+    assert drr_rel_err(rc.projs(), bgref)[0] <= TOL32
+    rc.set_use_bg_projs(False)
+    # max kernel
+    rc.use_proj_store_replace_method()
+    rc.set_default_bg_pixel_val(-1.0)
+    rc.set_kernel_id(1)
+    rc.compute()
+    mx = oracle.drr_f32(vol.voxels, G, cams, poses, step=0.5, kernel=1, default_bg=-1.0)
+    np.testing.assert_allclose(rc.projs(), mx, rtol=1e-6, atol=0)
+
+
+def test_edge_cases(xr, oracle):
+    vol = small_volume(7, (16, 16, 16), (2.0, 2.0, 2.0))
+    # 1x1 detector, odd detector, a pose that misses the volume entirely
+    for det in [(1, 1), (17, 5)]:
+        cam = small_camera(det, 6.0)
+        pose = synth.gt_pose(vol)
+        g, _ = _gpu_drr(xr, vol, [cam], pose[None], 0.5)
+        o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), pose[None], step=0.5)
+        rel, zero = drr_rel_err(g, o)
+        assert zero == 0.0 and rel <= TOL32
+    cam = small_camera((8, 8), 1.0)
+    away = synth.perturb(vol, synth.gt_pose(vol), [0, 0, 0], [500.0, 0.0, 0.0])
+    g, ns = _gpu_drr(xr, vol, [cam], away[None], 0.5, count=True)
+    assert ns == 0 and (g == 0).all()
+
+
+def test_errors_are_reported(xr):
+    from xreg_gb300 import _lib
+    vol = small_volume(8, (8, 8, 8))
+    cam = small_camera((4, 4), 4.0)
+    rc = _rc(xr, vol, [cam], 0.5)
+    rc.set_num_projs(1)
+    with pytest.raises(_lib.XRegError) as e:
+        rc.compute()
+    assert e.value.status == _lib.XR_ERR_NOT_ALLOCATED
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(synth.gt_pose(vol)[None])
+    rc.set_interp_method(_lib.XR_INTERP_NN)
+    with pytest.raises(_lib.XRegError) as e:
+        rc.compute()
+    assert e.value.status == _lib.XR_ERR_UNSUPPORTED
+    rc.use_linear_interp()
+    with pytest.raises(_lib.XRegError):
+        rc.compute(3)
+    with pytest.raises(_lib.XRegError):
+        rc.distribute_xforms_among_cam_models(np.full((1, 4, 4), np.nan))
+    with pytest.raises(_lib.XRegError):
+        rc.set_num_projs(2)  # beyond what allocate_resources reserved
+    rc.compute()
+    assert rc.proj(0).shape == (4, 4)

@@ -1,0 +1,140 @@
+"""ctypes binding of libxreg_gb300.so (the C ABI declared in include/xreg_gb300.h).
+
+The library is built in-tree by xreg_gb300.build; importing this module never
+falls back to any other implementation: if the shared library is missing the
+import raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from .build import LIB_PATH
+
+XR_OK = 0
+XR_ERR_INVALID_ARG = -1
+XR_ERR_CUDA = -2
+XR_ERR_OUT_OF_MEMORY = -3
+XR_ERR_UNSUPPORTED = -4
+XR_ERR_NOT_ALLOCATED = -5
+XR_ERR_DEVICE_CHECK = -6
+
+XR_VOXEL_F32, XR_VOXEL_F16, XR_VOXEL_BF16 = 0, 1, 2
+XR_LINE_INT_SUM, XR_LINE_INT_MAX = 0, 1
+XR_PROJ_STORE_REPLACE, XR_PROJ_STORE_ACCUM = 0, 1
+XR_INTERP_LINEAR, XR_INTERP_NN, XR_INTERP_SINC, XR_INTERP_BSPLINE = 0, 1, 2, 3
+XR_CAM_FOCAL_POS_Z, XR_CAM_FOCAL_NEG_Z, XR_CAM_ON_DETECTOR = 0, 1, 2
+XR_SIM_NCC, XR_SIM_GRAD_NCC, XR_SIM_PATCH_NCC, XR_SIM_PATCH_GRAD_NCC = 0, 1, 2, 3
+
+
+class xr_volume_desc(C.Structure):
+    _fields_ = [("n", C.c_int64 * 3), ("spacing", C.c_double * 3), ("origin", C.c_double * 3),
+                ("direction", C.c_double * 9)]
+
+
+class xr_camera_desc(C.Structure):
+    _fields_ = [("intrins", C.c_double * 9), ("extrins", C.c_double * 16), ("num_det_rows", C.c_int64),
+                ("num_det_cols", C.c_int64), ("det_row_spacing", C.c_double), ("det_col_spacing", C.c_double),
+                ("focal_len", C.c_double), ("coord_frame_type", C.c_int32), ("reserved", C.c_int32)]
+
+
+class XRegError(RuntimeError):
+    """A C-ABI call returned a non-zero xr_status."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[xr_status {status}] {msg}")
+        self.status = status
+
+
+H = C.c_void_p
+P = C.c_void_p
+i32, i64, u64, f32, f64 = C.c_int32, C.c_int64, C.c_uint64, C.c_float, C.c_double
+
+# name -> argtypes (restype is xr_status unless listed in _RESTYPES)
+_SIGS = {
+    "xr_last_error": [],
+    "xr_version": [],
+    "xr_camera_setup_naive": [f64, i64, i64, f64, f64, i32, C.POINTER(xr_camera_desc)],
+    "xr_camera_downsample": [C.POINTER(xr_camera_desc), f64, i32, C.POINTER(xr_camera_desc)],
+    "xr_rc_create": [i32, C.POINTER(H)],
+    "xr_rc_destroy": [H],
+    "xr_rc_set_stream": [H, P],
+    "xr_rc_synchronize": [H],
+    "xr_rc_set_volumes": [H, i32, C.POINTER(xr_volume_desc), C.POINTER(P), i32, f32],
+    "xr_rc_set_volumes_device": [H, i32, C.POINTER(xr_volume_desc), C.POINTER(P), i32, f32],
+    "xr_rc_set_camera_models": [H, i32, C.POINTER(xr_camera_desc)],
+    "xr_rc_set_num_projs": [H, i64],
+    "xr_rc_num_projs": [H, C.POINTER(i64)],
+    "xr_rc_set_ray_step_size": [H, f32],
+    "xr_rc_set_interp_method": [H, i32],
+    "xr_rc_set_proj_store_method": [H, i32],
+    "xr_rc_set_default_bg_pixel_val": [H, f32],
+    "xr_rc_set_kernel_id": [H, i32],
+    "xr_rc_set_bg_projs": [H, C.POINTER(P), i32],
+    "xr_rc_set_use_bg_projs": [H, i32],
+    "xr_rc_set_xforms_cam_to_itk_phys": [H, i64, P],
+    "xr_rc_distribute_xforms_among_cam_models": [H, i64, P],
+    "xr_rc_distribute_xforms_device": [H, i64, P],
+    "xr_rc_set_camera_model_proj_associations": [H, i64, P],
+    "xr_rc_allocate_resources": [H],
+    "xr_rc_max_num_projs_possible": [H, C.POINTER(i64)],
+    "xr_rc_compute": [H, i32],
+    "xr_rc_proj": [H, i64, P],
+    "xr_rc_copy_projs_to_host": [H, P],
+    "xr_rc_device_pixel_buf": [H, C.POINTER(P)],
+    "xr_rc_last_num_samples": [H, C.POINTER(u64)],
+    "xr_rc_set_count_samples": [H, i32],
+    "xr_sm_create": [i32, i32, C.POINTER(H)],
+    "xr_sm_destroy": [H],
+    "xr_sm_set_stream": [H, P],
+    "xr_sm_set_fixed_image": [H, P, i64, i64],
+    "xr_sm_set_mask": [H, P],
+    "xr_sm_set_num_moving_images": [H, i64],
+    "xr_sm_set_mov_imgs_buf_from_ray_caster": [H, H, i64],
+    "xr_sm_set_mov_imgs_device_buf": [H, P, i64],
+    "xr_sm_set_smooth_img_before_sobel_kernel_radius": [H, i32],
+    "xr_sm_set_patch_radius": [H, i32],
+    "xr_sm_set_patch_stride": [H, i32],
+    "xr_sm_allocate_resources": [H],
+    "xr_sm_compute": [H],
+    "xr_sm_sim_vals": [H, P],
+    "xr_sm_device_sim_vals": [H, C.POINTER(P)],
+    "xr_obj_create": [H, i32, i32, C.POINTER(H), i64, C.POINTER(H)],
+    "xr_obj_destroy": [H],
+    "xr_obj_eval": [H, i64, P, P],
+    "xr_obj_eval_device": [H, i64, P, P],
+}
+_RESTYPES = {"xr_last_error": C.c_char_p, "xr_version": C.c_char_p}
+
+EXPORTED = tuple(_SIGS)
+
+_lib = None
+
+
+def lib_path() -> Path:
+    return LIB_PATH
+
+
+def load() -> C.CDLL:
+    """Loads the in-tree shared library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run `python -m xreg_gb300.build` (or __graft_entry__.build())")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPES.get(name, C.c_int32)
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != XR_OK:
+        raise XRegError(status, load().xr_last_error().decode(errors="replace"))
+
+
+def call(name: str, *args) -> None:
+    check(getattr(load(), name)(*args))

@@ -1,0 +1,420 @@
+"""Python mirror of xReg's ray caster / similarity-metric operator surface over
+the C ABI.  Method names follow xReg (lib/ray_cast/xregRayCastInterface.h,
+lib/regi/sim_metrics_2d/xregImgSimMetric2D.h) so code written against xReg's
+objects reads the same; every call goes to libxreg_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import call, load
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+# --------------------------------------------------------------------- camera
+class CameraModel:
+    """xreg::CameraModel (xregPerspectiveXform.h:108-273) as an xr_camera_desc."""
+
+    def __init__(self, desc: L.xr_camera_desc | None = None):
+        self.desc = desc if desc is not None else L.xr_camera_desc()
+
+    @classmethod
+    def naive(cls, focal_len: float, num_rows: int, num_cols: int, row_spacing: float, col_spacing: float,
+              coord_frame_type: int = L.XR_CAM_FOCAL_NEG_Z) -> "CameraModel":
+        """CameraModel::setup(f, nr, nc, rs, cs) (xregPerspectiveXform.cpp:230-254)."""
+        d = L.xr_camera_desc()
+        call("xr_camera_setup_naive", float(focal_len), int(num_rows), int(num_cols), float(row_spacing),
+             float(col_spacing), int(coord_frame_type), C.byref(d))
+        return cls(d)
+
+    def downsample(self, ds_factor: float, force_even_dims: bool = False) -> "CameraModel":
+        """DownsampleCameraModel (xregPerspectiveXform.cpp:654-689)."""
+        d = L.xr_camera_desc()
+        call("xr_camera_downsample", C.byref(self.desc), float(ds_factor), int(force_even_dims), C.byref(d))
+        return CameraModel(d)
+
+    @property
+    def num_det_rows(self) -> int:
+        return int(self.desc.num_det_rows)
+
+    @property
+    def num_det_cols(self) -> int:
+        return int(self.desc.num_det_cols)
+
+    @property
+    def focal_len(self) -> float:
+        return float(self.desc.focal_len)
+
+    @property
+    def intrins(self) -> np.ndarray:
+        return np.array(self.desc.intrins[:], dtype=np.float64).reshape(3, 3)
+
+    @property
+    def extrins(self) -> np.ndarray:
+        return np.array(self.desc.extrins[:], dtype=np.float64).reshape(4, 4)
+
+    def set_extrins(self, extrins: np.ndarray) -> None:
+        e = np.asarray(extrins, dtype=np.float64).reshape(16)
+        for i in range(16):
+            self.desc.extrins[i] = float(e[i])
+
+    def as_tuple(self):
+        d = self.desc
+        return (tuple(d.intrins), tuple(d.extrins), d.num_det_rows, d.num_det_cols, d.det_row_spacing,
+                d.det_col_spacing, d.focal_len, d.coord_frame_type)
+
+
+# --------------------------------------------------------------------- volume
+@dataclass
+class Volume:
+    """A float32 attenuation volume in ITK conventions: voxels[z, y, x] (x fastest),
+    physical = origin + direction @ diag(spacing) @ index."""
+
+    voxels: np.ndarray
+    spacing: tuple = (1.0, 1.0, 1.0)
+    origin: tuple = (0.0, 0.0, 0.0)
+    direction: np.ndarray = field(default_factory=lambda: np.eye(3))
+
+    def __post_init__(self):
+        self.voxels = np.ascontiguousarray(self.voxels, dtype=np.float32)
+        assert self.voxels.ndim == 3
+
+    @property
+    def size(self) -> tuple:
+        nz, ny, nx = self.voxels.shape
+        return (nx, ny, nz)
+
+    def desc(self) -> L.xr_volume_desc:
+        d = L.xr_volume_desc()
+        nx, ny, nz = self.size
+        d.n[0], d.n[1], d.n[2] = nx, ny, nz
+        for i in range(3):
+            d.spacing[i] = float(self.spacing[i])
+            d.origin[i] = float(self.origin[i])
+        dirm = np.asarray(self.direction, dtype=np.float64).reshape(9)
+        for i in range(9):
+            d.direction[i] = float(dirm[i])
+        return d
+
+    def index_to_phys(self) -> np.ndarray:
+        """ITKImagePhysicalPointTransformsAsEigen (xregITKBasicImageUtils.h:133-165)."""
+        T = np.eye(4)
+        T[:3, :3] = np.asarray(self.direction, dtype=np.float64) @ np.diag(np.asarray(self.spacing, dtype=np.float64))
+        T[:3, 3] = np.asarray(self.origin, dtype=np.float64)
+        return T
+
+    def xform_img_center_to_itk_phys(self) -> np.ndarray:
+        """RayCaster::xform_img_center_to_itk_phys (xregRayCastInterface.cpp:200-224):
+        translation to the physical point of continuous index size/2."""
+        c = np.array(self.size, dtype=np.float64) / 2.0
+        T = np.eye(4)
+        T[:3, 3] = (self.index_to_phys() @ np.append(c, 1.0))[:3]
+        return T
+
+
+# ----------------------------------------------------------------- ray caster
+class RayCasterLineIntCUDA:
+    """Line-integral DRR ray caster on the GPU with RayCaster's method names."""
+
+    def __init__(self, device: int = -1):
+        load()
+        h = C.c_void_p()
+        call("xr_rc_create", int(device), C.byref(h))
+        self._h = h
+        self._cams: list[CameraModel] = []
+        self._num_projs = 0
+        self._vols: list[Volume] = []
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                load().xr_rc_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    # state
+    def set_stream(self, cuda_stream: int | None) -> None:
+        call("xr_rc_set_stream", self._h, C.c_void_p(cuda_stream or 0))
+
+    def synchronize(self) -> None:
+        call("xr_rc_synchronize", self._h)
+
+    def set_volume(self, vol: Volume, voxel_type: int = L.XR_VOXEL_F32, scale: float = 0.0) -> None:
+        self.set_volumes([vol], voxel_type, scale)
+
+    def set_volumes(self, vols, voxel_type: int = L.XR_VOXEL_F32, scale: float = 0.0) -> None:
+        descs = (L.xr_volume_desc * len(vols))(*[v.desc() for v in vols])
+        ptrs = (C.c_void_p * len(vols))(*[v.voxels.ctypes.data for v in vols])
+        call("xr_rc_set_volumes", self._h, len(vols), descs, ptrs, int(voxel_type), float(scale))
+        self._vols = list(vols)
+
+    def set_volumes_device(self, vols, device_ptrs, voxel_type: int = L.XR_VOXEL_F32, scale: float = 0.0):
+        descs = (L.xr_volume_desc * len(vols))(*[v.desc() for v in vols])
+        ptrs = (C.c_void_p * len(vols))(*[int(p) for p in device_ptrs])
+        call("xr_rc_set_volumes_device", self._h, len(vols), descs, ptrs, int(voxel_type), float(scale))
+        self._vols = list(vols)
+
+    def set_camera_model(self, cam: CameraModel) -> None:
+        self.set_camera_models([cam])
+
+    def set_camera_models(self, cams) -> None:
+        arr = (L.xr_camera_desc * len(cams))(*[c.desc for c in cams])
+        call("xr_rc_set_camera_models", self._h, len(cams), arr)
+        self._cams = list(cams)
+
+    def camera_models(self):
+        return list(self._cams)
+
+    def num_camera_models(self) -> int:
+        return len(self._cams)
+
+    def set_num_projs(self, n: int) -> None:
+        call("xr_rc_set_num_projs", self._h, int(n))
+        self._num_projs = int(n)
+
+    def num_projs(self) -> int:
+        v = C.c_int64()
+        call("xr_rc_num_projs", self._h, C.byref(v))
+        return int(v.value)
+
+    def set_ray_step_size(self, step: float) -> None:
+        call("xr_rc_set_ray_step_size", self._h, float(step))
+
+    def set_interp_method(self, m: int) -> None:
+        call("xr_rc_set_interp_method", self._h, int(m))
+
+    def use_linear_interp(self) -> None:
+        self.set_interp_method(L.XR_INTERP_LINEAR)
+
+    def use_proj_store_replace_method(self) -> None:
+        call("xr_rc_set_proj_store_method", self._h, L.XR_PROJ_STORE_REPLACE)
+
+    def use_proj_store_accum_method(self) -> None:
+        call("xr_rc_set_proj_store_method", self._h, L.XR_PROJ_STORE_ACCUM)
+
+    def set_default_bg_pixel_val(self, v: float) -> None:
+        call("xr_rc_set_default_bg_pixel_val", self._h, float(v))
+
+    def set_kernel_id(self, k: int) -> None:
+        call("xr_rc_set_kernel_id", self._h, int(k))
+
+    def set_bg_projs(self, imgs, use_bg_projs: bool = True) -> None:
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in imgs]
+        ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        call("xr_rc_set_bg_projs", self._h, ptrs, int(bool(use_bg_projs)))
+
+    def set_use_bg_projs(self, use: bool) -> None:
+        call("xr_rc_set_use_bg_projs", self._h, int(bool(use)))
+
+    def set_xforms_cam_to_itk_phys(self, xforms) -> None:
+        x = np.ascontiguousarray(np.asarray(xforms, dtype=np.float64).reshape(-1, 16))
+        call("xr_rc_set_xforms_cam_to_itk_phys", self._h, x.shape[0], _ptr(x))
+        self._num_projs = x.shape[0]
+
+    def distribute_xforms_among_cam_models(self, xforms) -> None:
+        x = np.ascontiguousarray(np.asarray(xforms, dtype=np.float64).reshape(-1, 16))
+        call("xr_rc_distribute_xforms_among_cam_models", self._h, x.shape[0], _ptr(x))
+
+    def distribute_xforms_device(self, n: int, d_xforms: int) -> None:
+        call("xr_rc_distribute_xforms_device", self._h, int(n), C.c_void_p(int(d_xforms)))
+
+    def set_camera_model_proj_associations(self, cam_idx) -> None:
+        a = np.ascontiguousarray(np.asarray(cam_idx, dtype=np.int32))
+        call("xr_rc_set_camera_model_proj_associations", self._h, a.shape[0], _ptr(a))
+
+    def allocate_resources(self) -> None:
+        call("xr_rc_allocate_resources", self._h)
+
+    def max_num_projs_possible(self) -> int:
+        v = C.c_int64()
+        call("xr_rc_max_num_projs_possible", self._h, C.byref(v))
+        return int(v.value)
+
+    def set_count_samples(self, enable: bool) -> None:
+        call("xr_rc_set_count_samples", self._h, int(bool(enable)))
+
+    def compute(self, vol_idx: int = 0) -> None:
+        call("xr_rc_compute", self._h, int(vol_idx))
+
+    def _shape(self):
+        c = self._cams[0]
+        return c.num_det_rows, c.num_det_cols
+
+    def proj(self, idx: int) -> np.ndarray:
+        r, c = self._shape()
+        out = np.empty((r, c), dtype=np.float32)
+        call("xr_rc_proj", self._h, int(idx), _ptr(out))
+        return out
+
+    def projs(self) -> np.ndarray:
+        r, c = self._shape()
+        out = np.empty((self.num_projs(), r, c), dtype=np.float32)
+        call("xr_rc_copy_projs_to_host", self._h, _ptr(out))
+        return out
+
+    def device_pixel_buf(self) -> int:
+        p = C.c_void_p()
+        call("xr_rc_device_pixel_buf", self._h, C.byref(p))
+        return int(p.value or 0)
+
+    def last_num_samples(self) -> int:
+        v = C.c_uint64()
+        call("xr_rc_last_num_samples", self._h, C.byref(v))
+        return int(v.value)
+
+
+# -------------------------------------------------------------------- metrics
+class ImgSimMetric2DCUDA:
+    """Base of the GPU similarity metrics (ImgSimMetric2D, xregImgSimMetric2D.h:42-159)."""
+
+    KIND = -1
+
+    def __init__(self, device: int = -1):
+        load()
+        h = C.c_void_p()
+        call("xr_sm_create", int(self.KIND), int(device), C.byref(h))
+        self._h = h
+        self._n = 0
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                load().xr_sm_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        call("xr_sm_set_stream", self._h, C.c_void_p(cuda_stream or 0))
+
+    def set_fixed_image(self, img: np.ndarray) -> None:
+        a = np.ascontiguousarray(img, dtype=np.float32)
+        call("xr_sm_set_fixed_image", self._h, _ptr(a), a.shape[0], a.shape[1])
+
+    def set_mask(self, mask: np.ndarray | None) -> None:
+        if mask is None:
+            call("xr_sm_set_mask", self._h, C.c_void_p(0))
+        else:
+            m = np.ascontiguousarray(mask, dtype=np.uint8)
+            call("xr_sm_set_mask", self._h, _ptr(m))
+
+    def set_num_moving_images(self, n: int) -> None:
+        call("xr_sm_set_num_moving_images", self._h, int(n))
+        self._n = int(n)
+
+    def num_moving_images(self) -> int:
+        return self._n
+
+    def set_mov_imgs_buf_from_ray_caster(self, rc: RayCasterLineIntCUDA, proj_offset: int = 0) -> None:
+        call("xr_sm_set_mov_imgs_buf_from_ray_caster", self._h, rc.handle, int(proj_offset))
+
+    def set_mov_imgs_device_buf(self, d_ptr: int, proj_offset: int = 0) -> None:
+        call("xr_sm_set_mov_imgs_device_buf", self._h, C.c_void_p(int(d_ptr)), int(proj_offset))
+
+    def allocate_resources(self) -> None:
+        call("xr_sm_allocate_resources", self._h)
+
+    def compute(self) -> None:
+        call("xr_sm_compute", self._h)
+
+    def sim_vals(self) -> np.ndarray:
+        out = np.empty(self._n, dtype=np.float32)
+        call("xr_sm_sim_vals", self._h, _ptr(out))
+        return out
+
+    def sim_val(self, i: int) -> float:
+        return float(self.sim_vals()[i])
+
+    def device_sim_vals(self) -> int:
+        p = C.c_void_p()
+        call("xr_sm_device_sim_vals", self._h, C.byref(p))
+        return int(p.value or 0)
+
+
+class _GradParams:
+    def set_smooth_img_before_sobel_kernel_radius(self, r: int) -> None:
+        call("xr_sm_set_smooth_img_before_sobel_kernel_radius", self._h, int(r))
+
+
+class _PatchParams:
+    def set_patch_radius(self, r: int) -> None:
+        call("xr_sm_set_patch_radius", self._h, int(r))
+
+    def set_patch_stride(self, s: int) -> None:
+        call("xr_sm_set_patch_stride", self._h, int(s))
+
+
+class ImgSimMetric2DNCCCUDA(ImgSimMetric2DCUDA):
+    KIND = L.XR_SIM_NCC
+
+
+class ImgSimMetric2DGradNCCCUDA(ImgSimMetric2DCUDA, _GradParams):
+    KIND = L.XR_SIM_GRAD_NCC
+
+
+class ImgSimMetric2DPatchNCCCUDA(ImgSimMetric2DCUDA, _PatchParams):
+    KIND = L.XR_SIM_PATCH_NCC
+
+
+class ImgSimMetric2DPatchGradNCCCUDA(ImgSimMetric2DCUDA, _GradParams, _PatchParams):
+    KIND = L.XR_SIM_PATCH_GRAD_NCC
+
+
+# ------------------------------------------------------ population objective
+class PopulationObjective:
+    """Intensity2D3DRegi::obj_fn for one object (xregIntensity2D3DRegi.cpp:571-742):
+    poses -> DRR per (view, pose) -> metric per view -> mean over views."""
+
+    def __init__(self, rc: RayCasterLineIntCUDA, metrics, max_pop: int, vol_idx: int = 0):
+        hs = (C.c_void_p * len(metrics))(*[m.handle.value for m in metrics])
+        h = C.c_void_p()
+        call("xr_obj_create", rc.handle, int(vol_idx), len(metrics), hs, int(max_pop), C.byref(h))
+        self._h = h
+        self.rc = rc
+        self.metrics = list(metrics)
+        self.max_pop = int(max_pop)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                load().xr_obj_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    def eval(self, xforms) -> np.ndarray:
+        x = np.ascontiguousarray(np.asarray(xforms, dtype=np.float64).reshape(-1, 16))
+        out = np.empty(x.shape[0], dtype=np.float32)
+        call("xr_obj_eval", self._h, x.shape[0], _ptr(x), _ptr(out))
+        return out
+
+    def eval_device(self, pop: int, d_xforms: int, d_sims: int) -> None:
+        call("xr_obj_eval_device", self._h, int(pop), C.c_void_p(int(d_xforms)), C.c_void_p(int(d_sims)))

@@ -1,0 +1,1139 @@
+// xr_capi.cu -- the extern "C" boundary: handles, validation, device buffers,
+// stream ordering and CUDA-graph capture of the population objective.
+// Nothing here throws across the ABI; every entry point returns an xr_status.
+#include "xr_internal.h"
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace xr {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+xr_status fail(xr_status code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+xr_status cuda_fail(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return e == cudaErrorMemoryAllocation ? XR_ERR_OUT_OF_MEMORY : XR_ERR_CUDA;
+}
+
+namespace {
+
+// Owning device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // Grows (never shrinks) to at least n bytes; contents are not preserved.
+  cudaError_t reserve(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) { p = nullptr; return e; }
+    bytes = n;
+    return cudaSuccess;
+  }
+  template <typename T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (dev >= 0) {
+      cudaGetDevice(&prev);
+      if (prev != dev) cudaSetDevice(dev);
+      else prev = -1;
+    }
+  }
+  ~DeviceGuard() { if (prev >= 0) cudaSetDevice(prev); }
+};
+
+__global__ void convert_voxels_kernel(const float* __restrict__ in, int64_t n, float scale, int vt, void* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = in[i] * scale;
+    if (vt == XR_VOXEL_F16) static_cast<__half*>(out)[i] = __float2half_rn(v);
+    else static_cast<__nv_bfloat16*>(out)[i] = __float2bfloat16_rn(v);
+  }
+}
+
+__global__ void max_abs_kernel(const float* __restrict__ in, int64_t n, unsigned int* out) {
+  unsigned int m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float a = fabsf(in[i]);
+    if (a == a) m = max(m, __float_as_uint(a));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void cam_idx_distribute_kernel(int32_t* out, int64_t n, int64_t per_cam) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int32_t)(i / per_cam);
+}
+
+bool finite_all(const double* v, int64_t n) {
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+}  // namespace
+}  // namespace xr
+
+using namespace xr;
+
+// ===================================================================== handles
+struct xr_raycaster_s {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t ext_stream = nullptr;
+  bool has_ext_stream = false;
+
+  struct Vol {
+    xr_volume_desc desc;
+    DevBuf voxels;
+    int32_t type = XR_VOXEL_F32;
+    float inv_scale = 1.0f;
+  };
+  std::vector<std::unique_ptr<Vol>> vols;
+  std::vector<xr_camera_desc> cams;
+  DevBuf d_cams;
+  bool cams_dirty = true;
+
+  int64_t num_projs = 0;
+  int64_t capacity = 0;   // projections allocated
+  float step = 1.0f;
+  int32_t interp = XR_INTERP_LINEAR;
+  int32_t store = XR_PROJ_STORE_REPLACE;
+  float default_bg = 0.0f;
+  int32_t kernel_id = XR_LINE_INT_SUM;
+  DevBuf d_bg;
+  bool has_bg = false;
+  bool use_bg = false;
+
+  std::vector<double> xforms;      // pose_count * 16
+  int64_t pose_count = 0;          // projection p uses pose (p % pose_count)
+  bool xforms_dirty = true;
+  bool xforms_on_device = false;   // last set through a device pointer
+  std::vector<int32_t> cam_idx;    // num_projs
+  bool cam_idx_dirty = true;
+
+  DevBuf d_xforms, d_cam_idx, d_geo, d_proj, d_counters;
+  bool allocated = false;
+  bool count_samples = false;
+  uint64_t generation = 1;         // bumps on every change that affects launches
+
+  cudaStream_t stream() const { return has_ext_stream ? ext_stream : own_stream; }
+  int64_t rows() const { return cams.empty() ? 0 : cams[0].num_det_rows; }
+  int64_t cols() const { return cams.empty() ? 0 : cams[0].num_det_cols; }
+};
+
+struct xr_simmetric_s {
+  int32_t kind = XR_SIM_NCC;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t ext_stream = nullptr;
+  bool has_ext_stream = false;
+
+  int64_t rows = 0, cols = 0;
+  DevBuf d_fixed;
+  bool has_fixed = false;
+  DevBuf d_mask;
+  bool has_mask = false;
+  int64_t num_mov = 0;
+  xr_raycaster rc = nullptr;
+  const float* mov_dev = nullptr;
+  int64_t proj_offset = 0;
+  int32_t smooth_ksize = 5;
+  int32_t patch_radius = 5;
+  int32_t patch_stride = 1;
+
+  bool allocated = false;
+  int64_t capacity = 0;            // moving images the partials buffer holds
+  int64_t n_used = 0;              // pixels used by NCC (mask count or all)
+  FixedNCC fx{}, fy{};
+  DevBuf d_fhat_x, d_fhat_y, d_gx, d_gy, d_pmean_x, d_pscale_x, d_pmean_y, d_pscale_y;
+  DevBuf d_partials, d_sims, d_scratch;
+  int nblk = 0;
+  int ncr = 0, ncc = 0;            // patch centre grid
+  uint64_t generation = 1;
+
+  cudaStream_t stream() const {
+    if (has_ext_stream) return ext_stream;
+    if (rc) return rc->stream();
+    return own_stream;
+  }
+};
+
+struct xr_objective_s {
+  xr_raycaster rc = nullptr;
+  int32_t vol_idx = 0;
+  std::vector<xr_simmetric> metrics;
+  int64_t max_pop = 0;
+  DevBuf d_poses, d_sims, d_view_sims_ptrs;
+  DevBuf h_pinned_poses;  // unused placeholder for symmetry (host copies use pageable memory)
+  // captured launch sequence
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_pop = -1;
+  uint64_t graph_rc_gen = 0;
+  std::vector<uint64_t> graph_sm_gen;
+  cudaStream_t graph_stream = nullptr;
+  ~xr_objective_s() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  }
+};
+
+// ===================================================================== misc
+extern "C" XR_API const char* xr_last_error(void) { return g_last_error.c_str(); }
+extern "C" XR_API const char* xr_version(void) { return "xreg_gb300 0.1.0 (sm_103a)"; }
+
+#define XR_CHECK_ARG(cond, msg) \
+  do {                          \
+    if (!(cond)) return fail(XR_ERR_INVALID_ARG, msg); \
+  } while (0)
+
+// ============================================================ camera helpers
+extern "C" XR_API xr_status xr_camera_setup_naive(double f, int64_t nr, int64_t nc, double rs, double cs,
+                                                  int32_t frame, xr_camera_desc* out) {
+  XR_CHECK_ARG(out, "xr_camera_setup_naive: out is NULL");
+  XR_CHECK_ARG(f > 1.0e-8, "xr_camera_setup_naive: focal length must be > 1e-8");
+  XR_CHECK_ARG(nr > 0 && nc > 0, "xr_camera_setup_naive: rows and cols must be positive");
+  XR_CHECK_ARG(rs > 1.0e-8 && cs > 1.0e-8, "xr_camera_setup_naive: spacings must be > 1e-8");
+  XR_CHECK_ARG(frame >= 0 && frame <= 2, "xr_camera_setup_naive: bad coord_frame_type");
+  std::memset(out, 0, sizeof(*out));
+  out->coord_frame_type = frame;
+  out->focal_len = f;
+  out->num_det_rows = nr;
+  out->num_det_cols = nc;
+  out->det_row_spacing = rs;
+  out->det_col_spacing = cs;
+  double K[9] = {f / cs, 0, 0, 0, f / rs, 0, 0, 0, 1};
+  if (frame == XR_CAM_FOCAL_NEG_Z) { K[0] = -K[0]; K[4] = -K[4]; }
+  K[2] = (double)(nc - 1) * 0.5;
+  K[5] = (double)(nr - 1) * 0.5;
+  std::memcpy(out->intrins, K, sizeof(K));
+  for (int i = 0; i < 16; ++i) out->extrins[i] = (i % 5 == 0) ? 1.0 : 0.0;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_camera_downsample(const xr_camera_desc* src, double ds, int32_t force_even,
+                                                 xr_camera_desc* dst) {
+  XR_CHECK_ARG(src && dst, "xr_camera_downsample: NULL argument");
+  XR_CHECK_ARG(ds > 0.0, "xr_camera_downsample: factor must be positive");
+  xr_camera_desc d = *src;
+  d.intrins[0] *= ds; d.intrins[4] *= ds; d.intrins[2] *= ds; d.intrins[5] *= ds;
+  long nr = std::lround((double)src->num_det_rows * ds);
+  long nc = std::lround((double)src->num_det_cols * ds);
+  if (force_even) { if (nr % 2) --nr; if (nc % 2) --nc; }
+  XR_CHECK_ARG(nr > 0 && nc > 0, "xr_camera_downsample: result has no pixels");
+  d.num_det_rows = nr;
+  d.num_det_cols = nc;
+  d.det_row_spacing = src->det_row_spacing / ds;
+  d.det_col_spacing = src->det_col_spacing / ds;
+  const double xps = d.det_col_spacing, yps = d.det_row_spacing;
+  d.focal_len = (std::fabs(d.intrins[0] * xps) + std::fabs(d.intrins[4] * ((yps < 0) ? xps : yps))) / 2.0;
+  *dst = d;
+  return XR_OK;
+}
+
+// ================================================================ ray caster
+extern "C" XR_API xr_status xr_rc_create(int32_t device, xr_raycaster* out) {
+  XR_CHECK_ARG(out, "xr_rc_create: out is NULL");
+  *out = nullptr;
+  int dev = device;
+  if (dev < 0) XR_CUDA_TRY(cudaGetDevice(&dev));
+  int ndev = 0;
+  XR_CUDA_TRY(cudaGetDeviceCount(&ndev));
+  XR_CHECK_ARG(dev < ndev, "xr_rc_create: no such device");
+  DeviceGuard g(dev);
+  auto* rc = new (std::nothrow) xr_raycaster_s();
+  if (!rc) return fail(XR_ERR_OUT_OF_MEMORY, "xr_rc_create: host allocation failed");
+  rc->device = dev;
+  cudaError_t e = cudaStreamCreateWithFlags(&rc->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete rc; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
+  e = rc->d_counters.reserve(64);
+  if (e != cudaSuccess) { cudaStreamDestroy(rc->own_stream); delete rc; return cuda_fail(e, "cudaMalloc"); }
+  cudaMemset(rc->d_counters.p, 0, 64);
+  *out = rc;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_destroy(xr_raycaster rc) {
+  if (!rc) return XR_OK;
+  DeviceGuard g(rc->device);
+  cudaStreamSynchronize(rc->stream());
+  cudaStreamDestroy(rc->own_stream);
+  delete rc;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_stream(xr_raycaster rc, void* s) {
+  XR_CHECK_ARG(rc, "xr_rc_set_stream: NULL handle");
+  rc->ext_stream = static_cast<cudaStream_t>(s);
+  rc->has_ext_stream = s != nullptr;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_synchronize(xr_raycaster rc) {
+  XR_CHECK_ARG(rc, "xr_rc_synchronize: NULL handle");
+  DeviceGuard g(rc->device);
+  XR_CUDA_TRY(cudaStreamSynchronize(rc->stream()));
+  unsigned int err = 0;
+  XR_CUDA_TRY(cudaMemcpy(&err, rc->d_counters.as<char>() + 8, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err) {
+    cudaMemset(rc->d_counters.as<char>() + 8, 0, sizeof(err));
+    return fail(XR_ERR_DEVICE_CHECK, "ray caster: " + std::to_string(err) +
+                                         " rays exceeded the step-count guard (non-finite or degenerate pose)");
+  }
+  return XR_OK;
+}
+
+static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume_desc* descs,
+                                     const float* const* voxels, int32_t vt, float scale, bool on_device) {
+  XR_CHECK_ARG(rc && descs && voxels && n > 0, "set_volumes: NULL argument or no volumes");
+  XR_CHECK_ARG(vt == XR_VOXEL_F32 || vt == XR_VOXEL_F16 || vt == XR_VOXEL_BF16, "set_volumes: bad voxel type");
+  DeviceGuard g(rc->device);
+  cudaStream_t s = rc->stream();
+  std::vector<std::unique_ptr<xr_raycaster_s::Vol>> vols;
+  for (int32_t i = 0; i < n; ++i) {
+    const xr_volume_desc& d = descs[i];
+    XR_CHECK_ARG(voxels[i], "set_volumes: NULL voxel pointer");
+    XR_CHECK_ARG(d.n[0] >= 2 && d.n[1] >= 2 && d.n[2] >= 2, "set_volumes: every dimension must be >= 2");
+    const int64_t nv = d.n[0] * d.n[1] * d.n[2];
+    XR_CHECK_ARG(nv < (int64_t(1) << 31), "set_volumes: volumes above 2^31 voxels are not supported");
+    XR_CHECK_ARG(d.spacing[0] > 0 && d.spacing[1] > 0 && d.spacing[2] > 0, "set_volumes: spacing must be > 0");
+    XR_CHECK_ARG(finite_all(d.spacing, 3) && finite_all(d.origin, 3) && finite_all(d.direction, 9),
+                 "set_volumes: non-finite geometry");
+    auto v = std::make_unique<xr_raycaster_s::Vol>();
+    v->desc = d;
+    v->type = vt;
+    const size_t esz = vt == XR_VOXEL_F32 ? 4 : 2;
+    XR_CUDA_TRY(v->voxels.reserve((size_t)nv * esz));
+    if (vt == XR_VOXEL_F32) {
+      XR_CUDA_TRY(cudaMemcpyAsync(v->voxels.p, voxels[i], (size_t)nv * 4,
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+      v->inv_scale = 1.0f;
+    } else {
+      DevBuf tmp;
+      const float* src = voxels[i];
+      if (!on_device) {
+        XR_CUDA_TRY(tmp.reserve((size_t)nv * 4));
+        XR_CUDA_TRY(cudaMemcpyAsync(tmp.p, voxels[i], (size_t)nv * 4, cudaMemcpyHostToDevice, s));
+        src = tmp.as<float>();
+      }
+      float sc = scale;
+      if (!(sc > 0.0f)) {
+        sc = 1.0f;
+        if (vt == XR_VOXEL_F16) {
+          XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.as<char>() + 16, 0, 4, s));
+          max_abs_kernel<<<1024, 256, 0, s>>>(src, nv, reinterpret_cast<unsigned int*>(rc->d_counters.as<char>() + 16));
+          XR_CUDA_TRY(cudaGetLastError());
+          unsigned int bits = 0;
+          XR_CUDA_TRY(cudaMemcpyAsync(&bits, rc->d_counters.as<char>() + 16, 4, cudaMemcpyDeviceToHost, s));
+          XR_CUDA_TRY(cudaStreamSynchronize(s));
+          float mx;
+          std::memcpy(&mx, &bits, 4);
+          if (mx > 0.0f && std::isfinite(mx)) {
+            // largest power of two with max * scale < 2^15 (FP16 max is 65504)
+            const int e = (int)std::floor(std::log2(32768.0 / (double)mx));
+            sc = (float)std::ldexp(1.0, e);
+          }
+        }
+      }
+      v->inv_scale = 1.0f / sc;
+      convert_voxels_kernel<<<2048, 256, 0, s>>>(src, nv, sc, vt, v->voxels.p);
+      XR_CUDA_TRY(cudaGetLastError());
+      XR_CUDA_TRY(cudaStreamSynchronize(s));  // tmp is released at scope exit
+    }
+    vols.push_back(std::move(v));
+  }
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
+  rc->vols = std::move(vols);
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_volumes(xr_raycaster rc, int32_t n, const xr_volume_desc* descs,
+                                              const float* const* host_voxels, int32_t vt, float scale) {
+  return rc_set_volumes_impl(rc, n, descs, host_voxels, vt, scale, false);
+}
+
+extern "C" XR_API xr_status xr_rc_set_volumes_device(xr_raycaster rc, int32_t n, const xr_volume_desc* descs,
+                                                     const float* const* dev_voxels, int32_t vt, float scale) {
+  return rc_set_volumes_impl(rc, n, descs, dev_voxels, vt, scale, true);
+}
+
+extern "C" XR_API xr_status xr_rc_set_camera_models(xr_raycaster rc, int32_t n, const xr_camera_desc* cams) {
+  XR_CHECK_ARG(rc && cams && n > 0, "set_camera_models: NULL argument or no cameras");
+  for (int32_t i = 0; i < n; ++i) {
+    XR_CHECK_ARG(cams[i].num_det_rows > 0 && cams[i].num_det_cols > 0, "set_camera_models: empty detector");
+    XR_CHECK_ARG(cams[i].coord_frame_type >= 0 && cams[i].coord_frame_type <= 2, "set_camera_models: bad frame");
+    XR_CHECK_ARG(finite_all(cams[i].intrins, 9) && finite_all(cams[i].extrins, 16), "set_camera_models: non-finite");
+    XR_CHECK_ARG(cams[i].num_det_rows < (1 << 30) && cams[i].num_det_cols < (1 << 30), "set_camera_models: too big");
+  }
+  rc->cams.assign(cams, cams + n);
+  rc->cams_dirty = true;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_num_projs(xr_raycaster rc, int64_t n) {
+  XR_CHECK_ARG(rc && n > 0, "set_num_projs: NULL handle or non-positive count");
+  XR_CHECK_ARG(!rc->allocated || n <= rc->capacity,
+               "set_num_projs: more projections than allocate_resources reserved; call allocate_resources again");
+  if (n != rc->num_projs) {
+    rc->num_projs = n;
+    rc->cam_idx.resize((size_t)n, 0);
+    rc->cam_idx_dirty = true;
+    rc->generation++;
+  }
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_num_projs(xr_raycaster rc, int64_t* out) {
+  XR_CHECK_ARG(rc && out, "num_projs: NULL argument");
+  *out = rc->num_projs;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_ray_step_size(xr_raycaster rc, float step) {
+  XR_CHECK_ARG(rc && step > 0.0f && std::isfinite(step), "set_ray_step_size: step must be positive and finite");
+  rc->step = step;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_interp_method(xr_raycaster rc, int32_t m) {
+  XR_CHECK_ARG(rc && m >= 0 && m <= 3, "set_interp_method: bad method");
+  rc->interp = m;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_proj_store_method(xr_raycaster rc, int32_t m) {
+  XR_CHECK_ARG(rc && (m == XR_PROJ_STORE_REPLACE || m == XR_PROJ_STORE_ACCUM), "set_proj_store_method: bad method");
+  rc->store = m;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_default_bg_pixel_val(xr_raycaster rc, float bg) {
+  XR_CHECK_ARG(rc, "set_default_bg_pixel_val: NULL handle");
+  rc->default_bg = bg;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_kernel_id(xr_raycaster rc, int32_t k) {
+  XR_CHECK_ARG(rc && (k == XR_LINE_INT_SUM || k == XR_LINE_INT_MAX), "set_kernel_id: bad kernel id");
+  rc->kernel_id = k;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_bg_projs(xr_raycaster rc, const float* const* imgs, int32_t use) {
+  XR_CHECK_ARG(rc && imgs, "set_bg_projs: NULL argument");
+  XR_CHECK_ARG(!rc->cams.empty(), "set_bg_projs: set the camera models first");
+  DeviceGuard g(rc->device);
+  const size_t npix = (size_t)(rc->rows() * rc->cols());
+  XR_CUDA_TRY(rc->d_bg.reserve(npix * 4 * rc->cams.size()));
+  for (size_t c = 0; c < rc->cams.size(); ++c) {
+    XR_CHECK_ARG(imgs[c], "set_bg_projs: NULL image");
+    XR_CUDA_TRY(cudaMemcpyAsync(rc->d_bg.as<float>() + c * npix, imgs[c], npix * 4, cudaMemcpyHostToDevice,
+                                rc->stream()));
+  }
+  XR_CUDA_TRY(cudaStreamSynchronize(rc->stream()));
+  rc->has_bg = true;
+  rc->use_bg = use != 0;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_use_bg_projs(xr_raycaster rc, int32_t use) {
+  XR_CHECK_ARG(rc, "set_use_bg_projs: NULL handle");
+  XR_CHECK_ARG(!use || rc->has_bg, "set_use_bg_projs: no background projections were set");
+  rc->use_bg = use != 0;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_xforms_cam_to_itk_phys(xr_raycaster rc, int64_t n, const double* xf) {
+  XR_CHECK_ARG(rc && xf && n > 0, "set_xforms_cam_to_itk_phys: NULL argument");
+  XR_CHECK_ARG(finite_all(xf, 16 * n), "set_xforms_cam_to_itk_phys: non-finite transform");
+  xr_status st = xr_rc_set_num_projs(rc, n);
+  if (st != XR_OK) return st;
+  rc->xforms.assign(xf, xf + 16 * n);
+  rc->pose_count = n;
+  rc->xforms_dirty = true;
+  rc->xforms_on_device = false;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_distribute_xforms_among_cam_models(xr_raycaster rc, int64_t n, const double* xf) {
+  XR_CHECK_ARG(rc && xf && n > 0, "distribute_xforms_among_cam_models: NULL argument");
+  XR_CHECK_ARG(!rc->cams.empty(), "distribute_xforms_among_cam_models: no camera models");
+  XR_CHECK_ARG(n * (int64_t)rc->cams.size() == rc->num_projs,
+               "distribute_xforms_among_cam_models: num_xforms * num_cams must equal num_projs");
+  XR_CHECK_ARG(finite_all(xf, 16 * n), "distribute_xforms_among_cam_models: non-finite transform");
+  rc->xforms.assign(xf, xf + 16 * n);
+  rc->pose_count = n;
+  rc->xforms_dirty = true;
+  rc->xforms_on_device = false;
+  for (int64_t p = 0; p < rc->num_projs; ++p) {
+    const int32_t c = (int32_t)(p / n);
+    if (rc->cam_idx[(size_t)p] != c) { rc->cam_idx[(size_t)p] = c; rc->cam_idx_dirty = true; }
+  }
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_camera_model_proj_associations(xr_raycaster rc, int64_t n, const int32_t* ci) {
+  XR_CHECK_ARG(rc && ci, "set_camera_model_proj_associations: NULL argument");
+  XR_CHECK_ARG(n == rc->num_projs, "set_camera_model_proj_associations: size must equal num_projs");
+  for (int64_t i = 0; i < n; ++i)
+    XR_CHECK_ARG(ci[i] >= 0 && ci[i] < (int32_t)rc->cams.size(), "set_camera_model_proj_associations: bad camera");
+  rc->cam_idx.assign(ci, ci + n);
+  rc->cam_idx_dirty = true;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_allocate_resources(xr_raycaster rc) {
+  XR_CHECK_ARG(rc, "allocate_resources: NULL handle");
+  XR_CHECK_ARG(rc->num_projs > 0, "allocate_resources: num_projs is 0");
+  XR_CHECK_ARG(!rc->cams.empty(), "allocate_resources: no camera models");
+  for (size_t c = 1; c < rc->cams.size(); ++c) {
+    if (rc->cams[c].num_det_rows != rc->rows()) return fail(XR_ERR_INVALID_ARG, "Inconsistent number rows in camera model images!");
+    if (rc->cams[c].num_det_cols != rc->cols()) return fail(XR_ERR_INVALID_ARG, "Inconsistent number columns in camera model images!");
+  }
+  DeviceGuard g(rc->device);
+  const size_t n = (size_t)rc->num_projs;
+  XR_CUDA_TRY(rc->d_proj.reserve(n * (size_t)(rc->rows() * rc->cols()) * 4));
+  XR_CUDA_TRY(rc->d_geo.reserve(n * sizeof(ProjGeom)));
+  XR_CUDA_TRY(rc->d_cam_idx.reserve(n * 4));
+  XR_CUDA_TRY(rc->d_xforms.reserve(n * 16 * 8));
+  XR_CUDA_TRY(rc->d_cams.reserve(rc->cams.size() * sizeof(xr_camera_desc)));
+  rc->capacity = rc->num_projs;
+  rc->cams_dirty = rc->cam_idx_dirty = rc->xforms_dirty = true;
+  if (rc->xforms_on_device) rc->xforms_dirty = false;  // device-side poses already live in d_xforms? re-set required
+  rc->allocated = true;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_max_num_projs_possible(xr_raycaster rc, int64_t* out) {
+  XR_CHECK_ARG(rc && out, "max_num_projs_possible: NULL argument");
+  XR_CHECK_ARG(!rc->cams.empty(), "max_num_projs_possible: no camera models");
+  DeviceGuard g(rc->device);
+  size_t fr = 0, tot = 0;
+  XR_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+  const double per = (double)(rc->rows() * rc->cols()) * 4.0 + sizeof(ProjGeom) + 16 * 8 + 4;
+  *out = (int64_t)(0.9 * (double)fr / per);
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable) {
+  XR_CHECK_ARG(rc, "set_count_samples: NULL handle");
+  rc->count_samples = enable != 0;
+  rc->generation++;
+  return XR_OK;
+}
+
+// Uploads dirty host state and enqueues geometry + DRR kernels on the stream.
+static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
+  XR_CHECK_ARG(rc, "compute: NULL handle");
+  if (!rc->allocated) return fail(XR_ERR_NOT_ALLOCATED, "compute: allocate_resources has not been called");
+  if (rc->interp != XR_INTERP_LINEAR)
+    return fail(XR_ERR_UNSUPPORTED, "compute: only linear interpolation is implemented (as RayCasterOCL)");
+  XR_CHECK_ARG(vol_idx >= 0 && vol_idx < (int32_t)rc->vols.size(), "compute: bad volume index");
+  XR_CHECK_ARG(rc->pose_count > 0, "compute: no projection transforms were set");
+  XR_CHECK_ARG(!rc->use_bg || rc->has_bg, "compute: background projections requested but not set");
+  cudaStream_t s = rc->stream();
+  const int64_t n = rc->num_projs;
+  if (rc->cams_dirty) {
+    XR_CUDA_TRY(cudaMemcpyAsync(rc->d_cams.p, rc->cams.data(), rc->cams.size() * sizeof(xr_camera_desc),
+                                cudaMemcpyHostToDevice, s));
+    rc->cams_dirty = false;
+  }
+  if (rc->cam_idx_dirty) {
+    XR_CUDA_TRY(cudaMemcpyAsync(rc->d_cam_idx.p, rc->cam_idx.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    rc->cam_idx_dirty = false;
+  }
+  if (rc->xforms_dirty) {
+    XR_CHECK_ARG(rc->pose_count <= rc->capacity, "compute: more transforms than allocated projections");
+    XR_CUDA_TRY(cudaMemcpyAsync(rc->d_xforms.p, rc->xforms.data(), (size_t)rc->pose_count * 16 * 8,
+                                cudaMemcpyHostToDevice, s));
+    rc->xforms_dirty = false;
+  }
+  const auto& vol = *rc->vols[(size_t)vol_idx];
+  XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
+                               rc->d_cam_idx.as<int32_t>(), n, rc->pose_count, rc->d_geo.as<ProjGeom>(), s));
+  DrrParams p{};
+  p.vol.voxels = vol.voxels.p;
+  p.vol.nx = (int32_t)vol.desc.n[0];
+  p.vol.ny = (int32_t)vol.desc.n[1];
+  p.vol.nz = (int32_t)vol.desc.n[2];
+  p.vol.voxel_type = vol.type;
+  p.vol.inv_scale = vol.inv_scale;
+  p.geo = rc->d_geo.as<ProjGeom>();
+  p.cam_idx = rc->d_cam_idx.as<int32_t>();
+  p.bg_projs = rc->use_bg ? rc->d_bg.as<float>() : nullptr;
+  p.out = rc->d_proj.as<float>();
+  p.sample_counter = rc->count_samples ? reinterpret_cast<unsigned long long*>(rc->d_counters.p) : nullptr;
+  p.err_counter = reinterpret_cast<unsigned int*>(rc->d_counters.as<char>() + 8);
+  {
+    // Longest possible chord: the index-box diagonal scaled to mm by the largest
+    // spacing; 64x margin covers scaled (non-rigid) poses.
+    const double dx = (double)(vol.desc.n[0] - 1), dy = (double)(vol.desc.n[1] - 1), dz = (double)(vol.desc.n[2] - 1);
+    const double sp = std::fmax(vol.desc.spacing[0], std::fmax(vol.desc.spacing[1], vol.desc.spacing[2]));
+    p.max_steps = (unsigned long long)(64.0 * std::sqrt(dx * dx + dy * dy + dz * dz) * sp / (double)rc->step) + 64;
+  }
+  p.num_projs = n;
+  p.rows = (int32_t)rc->rows();
+  p.cols = (int32_t)rc->cols();
+  p.step = rc->step;
+  p.default_bg = rc->default_bg;
+  p.kernel_id = rc->kernel_id;
+  p.store = rc->store;
+  XR_CUDA_TRY(launch_drr(p, s));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_compute(xr_raycaster rc, int32_t vol_idx) {
+  XR_CHECK_ARG(rc, "compute: NULL handle");
+  DeviceGuard g(rc->device);
+  if (rc->count_samples) XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.p, 0, 8, rc->stream()));
+  return rc_enqueue_compute(rc, vol_idx);
+}
+
+extern "C" XR_API xr_status xr_rc_proj(xr_raycaster rc, int64_t idx, float* dst) {
+  XR_CHECK_ARG(rc && dst, "proj: NULL argument");
+  XR_CHECK_ARG(rc->allocated, "proj: resources not allocated");
+  XR_CHECK_ARG(idx >= 0 && idx < rc->num_projs, "proj: index out of range");
+  xr_status st = xr_rc_synchronize(rc);
+  if (st != XR_OK) return st;
+  DeviceGuard g(rc->device);
+  const size_t npix = (size_t)(rc->rows() * rc->cols());
+  XR_CUDA_TRY(cudaMemcpy(dst, rc->d_proj.as<float>() + (size_t)idx * npix, npix * 4, cudaMemcpyDeviceToHost));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_copy_projs_to_host(xr_raycaster rc, float* dst) {
+  XR_CHECK_ARG(rc && dst, "copy_projs_to_host: NULL argument");
+  XR_CHECK_ARG(rc->allocated, "copy_projs_to_host: resources not allocated");
+  xr_status st = xr_rc_synchronize(rc);
+  if (st != XR_OK) return st;
+  DeviceGuard g(rc->device);
+  const size_t n = (size_t)(rc->rows() * rc->cols()) * (size_t)rc->num_projs;
+  XR_CUDA_TRY(cudaMemcpy(dst, rc->d_proj.p, n * 4, cudaMemcpyDeviceToHost));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_device_pixel_buf(xr_raycaster rc, float** out) {
+  XR_CHECK_ARG(rc && out, "device_pixel_buf: NULL argument");
+  XR_CHECK_ARG(rc->allocated, "device_pixel_buf: resources not allocated");
+  *out = rc->d_proj.as<float>();
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* out) {
+  XR_CHECK_ARG(rc && out, "last_num_samples: NULL argument");
+  XR_CHECK_ARG(rc->count_samples, "last_num_samples: counting is disabled (xr_rc_set_count_samples)");
+  xr_status st = xr_rc_synchronize(rc);
+  if (st != XR_OK) return st;
+  DeviceGuard g(rc->device);
+  unsigned long long v = 0;
+  XR_CUDA_TRY(cudaMemcpy(&v, rc->d_counters.p, 8, cudaMemcpyDeviceToHost));
+  *out = v;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_distribute_xforms_device(xr_raycaster rc, int64_t n, const double* d_xf) {
+  XR_CHECK_ARG(rc && d_xf && n > 0, "distribute_xforms_device: NULL argument");
+  XR_CHECK_ARG(!rc->cams.empty(), "distribute_xforms_device: no camera models");
+  XR_CHECK_ARG(rc->allocated, "distribute_xforms_device: allocate_resources first");
+  XR_CHECK_ARG(n * (int64_t)rc->cams.size() == rc->num_projs,
+               "distribute_xforms_device: num_xforms * num_cams must equal num_projs");
+  DeviceGuard g(rc->device);
+  cudaStream_t s = rc->stream();
+  XR_CUDA_TRY(cudaMemcpyAsync(rc->d_xforms.p, d_xf, (size_t)n * 16 * 8, cudaMemcpyDeviceToDevice, s));
+  rc->pose_count = n;
+  rc->xforms_dirty = false;
+  rc->xforms_on_device = true;
+  bool changed = false;
+  for (int64_t p = 0; p < rc->num_projs; ++p) {
+    const int32_t c = (int32_t)(p / n);
+    if (rc->cam_idx[(size_t)p] != c) { rc->cam_idx[(size_t)p] = c; changed = true; }
+  }
+  if (changed || rc->cam_idx_dirty) {
+    cam_idx_distribute_kernel<<<(unsigned)((rc->num_projs + 255) / 256), 256, 0, s>>>(
+        rc->d_cam_idx.as<int32_t>(), rc->num_projs, n);
+    XR_CUDA_TRY(cudaGetLastError());
+    rc->cam_idx_dirty = false;
+  }
+  return XR_OK;
+}
+
+// ======================================================== similarity metric
+extern "C" XR_API xr_status xr_sm_create(int32_t kind, int32_t device, xr_simmetric* out) {
+  XR_CHECK_ARG(out, "xr_sm_create: out is NULL");
+  *out = nullptr;
+  XR_CHECK_ARG(kind >= XR_SIM_NCC && kind <= XR_SIM_PATCH_GRAD_NCC, "xr_sm_create: unknown metric kind");
+  int dev = device;
+  if (dev < 0) XR_CUDA_TRY(cudaGetDevice(&dev));
+  DeviceGuard g(dev);
+  auto* sm = new (std::nothrow) xr_simmetric_s();
+  if (!sm) return fail(XR_ERR_OUT_OF_MEMORY, "xr_sm_create: host allocation failed");
+  sm->kind = kind;
+  sm->device = dev;
+  cudaError_t e = cudaStreamCreateWithFlags(&sm->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete sm; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
+  *out = sm;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_destroy(xr_simmetric sm) {
+  if (!sm) return XR_OK;
+  DeviceGuard g(sm->device);
+  cudaStreamSynchronize(sm->stream());
+  cudaStreamDestroy(sm->own_stream);
+  delete sm;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_stream(xr_simmetric sm, void* s) {
+  XR_CHECK_ARG(sm, "xr_sm_set_stream: NULL handle");
+  sm->ext_stream = static_cast<cudaStream_t>(s);
+  sm->has_ext_stream = s != nullptr;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_fixed_image(xr_simmetric sm, const float* img, int64_t rows, int64_t cols) {
+  XR_CHECK_ARG(sm && img, "set_fixed_image: NULL argument");
+  XR_CHECK_ARG(rows >= 2 && cols >= 2 && rows < (1 << 28) && cols < (1 << 28), "set_fixed_image: bad size");
+  DeviceGuard g(sm->device);
+  const size_t n = (size_t)(rows * cols);
+  XR_CUDA_TRY(sm->d_fixed.reserve(n * 4));
+  XR_CUDA_TRY(cudaMemcpy(sm->d_fixed.p, img, n * 4, cudaMemcpyHostToDevice));
+  if (sm->rows != rows || sm->cols != cols) {
+    sm->has_mask = false;
+    sm->d_mask.release();
+  }
+  sm->rows = rows;
+  sm->cols = cols;
+  sm->has_fixed = true;
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_mask(xr_simmetric sm, const uint8_t* mask) {
+  XR_CHECK_ARG(sm, "set_mask: NULL handle");
+  if (!mask) {
+    sm->has_mask = false;
+    sm->allocated = false;
+    sm->generation++;
+    return XR_OK;
+  }
+  XR_CHECK_ARG(sm->has_fixed, "set_mask: set the fixed image first");
+  if (sm->kind != XR_SIM_NCC && sm->kind != XR_SIM_GRAD_NCC)
+    return fail(XR_ERR_UNSUPPORTED, "set_mask: masks are implemented for NCC and grad-NCC only");
+  DeviceGuard g(sm->device);
+  const size_t n = (size_t)(sm->rows * sm->cols);
+  XR_CUDA_TRY(sm->d_mask.reserve(n));
+  XR_CUDA_TRY(cudaMemcpy(sm->d_mask.p, mask, n, cudaMemcpyHostToDevice));
+  sm->has_mask = true;
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_num_moving_images(xr_simmetric sm, int64_t n) {
+  XR_CHECK_ARG(sm && n > 0, "set_num_moving_images: NULL handle or non-positive count");
+  XR_CHECK_ARG(!sm->allocated || n <= sm->capacity,
+               "set_num_moving_images: more images than allocate_resources reserved; allocate again");
+  if (n != sm->num_mov) { sm->num_mov = n; sm->generation++; }
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_mov_imgs_buf_from_ray_caster(xr_simmetric sm, xr_raycaster rc, int64_t off) {
+  XR_CHECK_ARG(sm && rc && off >= 0, "set_mov_imgs_buf_from_ray_caster: NULL argument or negative offset");
+  sm->rc = rc;
+  sm->mov_dev = nullptr;
+  sm->proj_offset = off;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_mov_imgs_device_buf(xr_simmetric sm, const float* d, int64_t off) {
+  XR_CHECK_ARG(sm && d && off >= 0, "set_mov_imgs_device_buf: NULL argument or negative offset");
+  sm->rc = nullptr;
+  sm->mov_dev = d;
+  sm->proj_offset = off;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_smooth_img_before_sobel_kernel_radius(xr_simmetric sm, int32_t r) {
+  XR_CHECK_ARG(sm, "set_smooth_img_before_sobel_kernel_radius: NULL handle");
+  if (r != 0 && r != 3 && r != 5)
+    return fail(XR_ERR_UNSUPPORTED, "set_smooth_img_before_sobel_kernel_radius: only 0, 3 and 5 are implemented");
+  sm->smooth_ksize = r;
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_patch_radius(xr_simmetric sm, int32_t r) {
+  XR_CHECK_ARG(sm && r > 0 && r <= 16, "set_patch_radius: radius must be in [1, 16]");
+  sm->patch_radius = r;
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_patch_stride(xr_simmetric sm, int32_t s) {
+  XR_CHECK_ARG(sm && s > 0 && s <= 4, "set_patch_stride: stride must be in [1, 4]");
+  sm->patch_stride = s;
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
+// Zero-mean fixed image and its statistics for one NCC direction.
+static xr_status sm_prepare_ncc_fixed(xr_simmetric sm, const float* img, DevBuf& fhat, FixedNCC& fx,
+                                      cudaStream_t s) {
+  const int64_t n = sm->rows * sm->cols;
+  const uint8_t* mask = sm->has_mask ? sm->d_mask.as<uint8_t>() : nullptr;
+  XR_CUDA_TRY(sm->d_scratch.reserve(64));
+  double h[3];
+  XR_CUDA_TRY(launch_image_stats(img, n, mask, sm->d_scratch.as<double>(), s));
+  XR_CUDA_TRY(cudaMemcpyAsync(h, sm->d_scratch.p, 24, cudaMemcpyDeviceToHost, s));
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
+  const double cnt = h[2];
+  if (!(cnt >= 2.0)) return fail(XR_ERR_INVALID_ARG, "allocate_resources: fewer than 2 usable pixels");
+  const double mean = h[0] / cnt;
+  double sd = std::sqrt(h[1] / (cnt - 1.0));
+  if (sd < 1.0e-6) sd = 1.0e-6;
+  XR_CUDA_TRY(fhat.reserve((size_t)n * 4));
+  XR_CUDA_TRY(launch_sub_scalar(img, n, mean, fhat.as<float>(), s));
+  XR_CUDA_TRY(launch_sum_f(fhat.as<float>(), n, mask, sm->d_scratch.as<double>(), s));
+  XR_CUDA_TRY(cudaMemcpyAsync(h, sm->d_scratch.p, 24, cudaMemcpyDeviceToHost, s));
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
+  fx.fhat = fhat.as<float>();
+  fx.sd = sd;
+  fx.sum_fhat = h[0];
+  sm->n_used = (int64_t)cnt;
+  return XR_OK;
+}
+
+static xr_status sm_prepare_patch_fixed(xr_simmetric sm, const float* img, DevBuf& mean, DevBuf& scale,
+                                        PatchFixed& pf, cudaStream_t s) {
+  const size_t np = (size_t)sm->ncr * (size_t)sm->ncc;
+  XR_CUDA_TRY(mean.reserve(np * 4));
+  XR_CUDA_TRY(scale.reserve(np * 4));
+  XR_CUDA_TRY(launch_patch_fixed_stats(img, (int)sm->rows, (int)sm->cols, sm->patch_radius, sm->patch_stride,
+                                       sm->ncr, sm->ncc, mean.as<float>(), scale.as<float>(), s));
+  pf.img = img;
+  pf.mean = mean.as<float>();
+  pf.scale = scale.as<float>();
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm) {
+  XR_CHECK_ARG(sm, "allocate_resources: NULL handle");
+  XR_CHECK_ARG(sm->has_fixed, "allocate_resources: no fixed image");
+  XR_CHECK_ARG(sm->num_mov > 0, "allocate_resources: num_moving_images is 0");
+  XR_CHECK_ARG(sm->rc || sm->mov_dev, "allocate_resources: no moving image buffer");
+  DeviceGuard g(sm->device);
+  cudaStream_t s = sm->stream();
+  const int64_t n = sm->rows * sm->cols;
+  const int rows = (int)sm->rows, cols = (int)sm->cols;
+  sm->capacity = sm->num_mov;
+  if (sm->kind == XR_SIM_NCC) {
+    xr_status st = sm_prepare_ncc_fixed(sm, sm->d_fixed.as<float>(), sm->d_fhat_x, sm->fx, s);
+    if (st != XR_OK) return st;
+    sm->nblk = (int)std::min<int64_t>(128, (n + 255) / 256);
+    XR_CUDA_TRY(sm->d_partials.reserve((size_t)sm->capacity * sm->nblk * 3 * 8));
+  } else if (sm->kind == XR_SIM_GRAD_NCC) {
+    XR_CHECK_ARG(rows >= 8 && cols >= 8, "allocate_resources: gradient metrics need images of at least 8x8");
+    XR_CUDA_TRY(sm->d_gx.reserve((size_t)n * 4));
+    XR_CUDA_TRY(sm->d_gy.reserve((size_t)n * 4));
+    XR_CUDA_TRY(launch_grad_images(sm->d_fixed.as<float>(), rows, cols, 1, sm->smooth_ksize, sm->d_gx.as<float>(),
+                                   sm->d_gy.as<float>(), s));
+    xr_status st = sm_prepare_ncc_fixed(sm, sm->d_gx.as<float>(), sm->d_fhat_x, sm->fx, s);
+    if (st != XR_OK) return st;
+    st = sm_prepare_ncc_fixed(sm, sm->d_gy.as<float>(), sm->d_fhat_y, sm->fy, s);
+    if (st != XR_OK) return st;
+    XR_CUDA_TRY(launch_grad_moments(nullptr, rows, cols, 0, sm->smooth_ksize, nullptr, nullptr, nullptr, nullptr, s,
+                                    &sm->nblk));
+    XR_CUDA_TRY(sm->d_partials.reserve((size_t)sm->capacity * sm->nblk * 6 * 8));
+  } else {
+    const int d = 2 * sm->patch_radius + 1;
+    XR_CHECK_ARG(d <= rows && d <= cols, "allocate_resources: patch larger than the image");
+    const int grad = sm->kind == XR_SIM_PATCH_GRAD_NCC;
+    XR_CHECK_ARG(!grad || (rows >= 8 && cols >= 8), "allocate_resources: gradient metrics need images of at least 8x8");
+    sm->ncr = (rows - 1 - 2 * sm->patch_radius) / sm->patch_stride + 1;
+    sm->ncc = (cols - 1 - 2 * sm->patch_radius) / sm->patch_stride + 1;
+    PatchFixed px{}, py{};
+    if (grad) {
+      XR_CUDA_TRY(sm->d_gx.reserve((size_t)n * 4));
+      XR_CUDA_TRY(sm->d_gy.reserve((size_t)n * 4));
+      XR_CUDA_TRY(launch_grad_images(sm->d_fixed.as<float>(), rows, cols, 1, sm->smooth_ksize,
+                                     sm->d_gx.as<float>(), sm->d_gy.as<float>(), s));
+      xr_status st = sm_prepare_patch_fixed(sm, sm->d_gx.as<float>(), sm->d_pmean_x, sm->d_pscale_x, px, s);
+      if (st != XR_OK) return st;
+      st = sm_prepare_patch_fixed(sm, sm->d_gy.as<float>(), sm->d_pmean_y, sm->d_pscale_y, py, s);
+      if (st != XR_OK) return st;
+    } else {
+      xr_status st = sm_prepare_patch_fixed(sm, sm->d_fixed.as<float>(), sm->d_pmean_x, sm->d_pscale_x, px, s);
+      if (st != XR_OK) return st;
+    }
+    XR_CUDA_TRY(launch_patch_ncc(nullptr, rows, cols, 0, grad, sm->smooth_ksize, sm->patch_radius,
+                                 sm->patch_stride, sm->ncr, sm->ncc, px, py, nullptr, s, &sm->nblk));
+    XR_CUDA_TRY(sm->d_partials.reserve((size_t)sm->capacity * sm->nblk * 2 * 8));
+  }
+  XR_CUDA_TRY(sm->d_sims.reserve((size_t)sm->capacity * 4));
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
+  sm->allocated = true;
+  sm->generation++;
+  return XR_OK;
+}
+
+static xr_status sm_enqueue_compute(xr_simmetric sm) {
+  XR_CHECK_ARG(sm, "compute: NULL handle");
+  if (!sm->allocated) return fail(XR_ERR_NOT_ALLOCATED, "compute: allocate_resources has not been called");
+  const int64_t npix = sm->rows * sm->cols;
+  const float* mov = nullptr;
+  if (sm->rc) {
+    XR_CHECK_ARG(sm->rc->allocated, "compute: the bound ray caster has no buffer");
+    XR_CHECK_ARG(sm->rc->rows() == sm->rows && sm->rc->cols() == sm->cols,
+                 "compute: ray caster image size differs from the fixed image");
+    XR_CHECK_ARG(sm->proj_offset + sm->num_mov <= sm->rc->capacity,
+                 "compute: moving images run past the ray caster's buffer");
+    mov = sm->rc->d_proj.as<float>() + sm->proj_offset * npix;
+  } else {
+    mov = sm->mov_dev + sm->proj_offset * npix;
+  }
+  cudaStream_t s = sm->stream();
+  const int rows = (int)sm->rows, cols = (int)sm->cols;
+  const uint8_t* mask = sm->has_mask ? sm->d_mask.as<uint8_t>() : nullptr;
+  switch (sm->kind) {
+    case XR_SIM_NCC:
+      XR_CUDA_TRY(launch_ncc_moments(mov, npix, sm->num_mov, sm->fx.fhat, mask, sm->d_partials.as<double>(),
+                                     sm->nblk, s));
+      XR_CUDA_TRY(launch_ncc_finalize(sm->d_partials.as<double>(), sm->nblk, sm->num_mov, sm->n_used, sm->fx,
+                                      sm->d_sims.as<float>(), s));
+      break;
+    case XR_SIM_GRAD_NCC:
+      XR_CUDA_TRY(launch_grad_moments(mov, rows, cols, sm->num_mov, sm->smooth_ksize, sm->fx.fhat, sm->fy.fhat, mask,
+                                      sm->d_partials.as<double>(), s, nullptr));
+      XR_CUDA_TRY(launch_grad_finalize(sm->d_partials.as<double>(), sm->nblk, sm->num_mov, sm->n_used, sm->fx,
+                                       sm->fy, sm->d_sims.as<float>(), s));
+      break;
+    default: {
+      const int grad = sm->kind == XR_SIM_PATCH_GRAD_NCC;
+      PatchFixed px{grad ? sm->d_gx.as<float>() : sm->d_fixed.as<float>(), sm->d_pmean_x.as<float>(),
+                    sm->d_pscale_x.as<float>()};
+      PatchFixed py{sm->d_gy.as<float>(), sm->d_pmean_y.as<float>(), sm->d_pscale_y.as<float>()};
+      XR_CUDA_TRY(launch_patch_ncc(mov, rows, cols, sm->num_mov, grad, sm->smooth_ksize, sm->patch_radius,
+                                   sm->patch_stride, sm->ncr, sm->ncc, px, py, sm->d_partials.as<double>(), s,
+                                   nullptr));
+      XR_CUDA_TRY(launch_patch_finalize(sm->d_partials.as<double>(), sm->nblk, sm->num_mov,
+                                        (int64_t)sm->ncr * sm->ncc, grad, sm->d_sims.as<float>(), s));
+      break;
+    }
+  }
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_compute(xr_simmetric sm) {
+  XR_CHECK_ARG(sm, "compute: NULL handle");
+  DeviceGuard g(sm->device);
+  // A metric reading a ray caster's buffer on another stream waits for it.
+  if (sm->rc && sm->stream() != sm->rc->stream()) {
+    cudaEvent_t ev;
+    XR_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, sm->rc->stream());
+    cudaStreamWaitEvent(sm->stream(), ev, 0);
+    cudaEventDestroy(ev);
+  }
+  return sm_enqueue_compute(sm);
+}
+
+extern "C" XR_API xr_status xr_sm_sim_vals(xr_simmetric sm, float* dst) {
+  XR_CHECK_ARG(sm && dst, "sim_vals: NULL argument");
+  XR_CHECK_ARG(sm->allocated, "sim_vals: resources not allocated");
+  DeviceGuard g(sm->device);
+  XR_CUDA_TRY(cudaStreamSynchronize(sm->stream()));
+  if (sm->rc) {
+    xr_status st = xr_rc_synchronize(sm->rc);
+    if (st != XR_OK) return st;
+  }
+  XR_CUDA_TRY(cudaMemcpy(dst, sm->d_sims.p, (size_t)sm->num_mov * 4, cudaMemcpyDeviceToHost));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_device_sim_vals(xr_simmetric sm, float** out) {
+  XR_CHECK_ARG(sm && out, "device_sim_vals: NULL argument");
+  XR_CHECK_ARG(sm->allocated, "device_sim_vals: resources not allocated");
+  *out = sm->d_sims.as<float>();
+  return XR_OK;
+}
+
+// ======================================================= population objective
+extern "C" XR_API xr_status xr_obj_create(xr_raycaster rc, int32_t vol_idx, int32_t nviews, const xr_simmetric* ms,
+                                          int64_t max_pop, xr_objective* out) {
+  XR_CHECK_ARG(out, "xr_obj_create: out is NULL");
+  *out = nullptr;
+  XR_CHECK_ARG(rc && ms && nviews > 0 && nviews <= 16 && max_pop > 0, "xr_obj_create: bad argument");
+  XR_CHECK_ARG((int32_t)rc->cams.size() == nviews, "xr_obj_create: the ray caster needs one camera model per view");
+  XR_CHECK_ARG(vol_idx >= 0 && vol_idx < (int32_t)rc->vols.size(), "xr_obj_create: bad volume index");
+  for (int32_t v = 0; v < nviews; ++v) {
+    XR_CHECK_ARG(ms[v] && ms[v]->has_fixed, "xr_obj_create: every view needs a metric with a fixed image");
+    XR_CHECK_ARG(ms[v]->rows == rc->rows() && ms[v]->cols == rc->cols(),
+                 "xr_obj_create: fixed image size differs from the detector");
+  }
+  DeviceGuard g(rc->device);
+  auto* obj = new (std::nothrow) xr_objective_s();
+  if (!obj) return fail(XR_ERR_OUT_OF_MEMORY, "xr_obj_create: host allocation failed");
+  obj->rc = rc;
+  obj->vol_idx = vol_idx;
+  obj->metrics.assign(ms, ms + nviews);
+  obj->max_pop = max_pop;
+  std::unique_ptr<xr_objective_s> guard(obj);
+  // ray caster: views * max_pop projections, poses distributed over cameras
+  xr_status st = xr_rc_set_num_projs(rc, (int64_t)nviews * max_pop);
+  if (st == XR_ERR_INVALID_ARG && rc->allocated) {
+    rc->allocated = false;
+    st = xr_rc_set_num_projs(rc, (int64_t)nviews * max_pop);
+  }
+  if (st != XR_OK) return st;
+  st = xr_rc_allocate_resources(rc);
+  if (st != XR_OK) return st;
+  for (int32_t v = 0; v < nviews; ++v) {
+    xr_simmetric m = ms[v];
+    m->allocated = false;
+    if ((st = xr_sm_set_num_moving_images(m, max_pop)) != XR_OK) return st;
+    if ((st = xr_sm_set_mov_imgs_buf_from_ray_caster(m, rc, (int64_t)v * max_pop)) != XR_OK) return st;
+    m->has_ext_stream = false;  // metrics follow the ray caster's stream inside the objective
+    if ((st = xr_sm_allocate_resources(m)) != XR_OK) return st;
+  }
+  XR_CUDA_TRY(obj->d_poses.reserve((size_t)max_pop * 16 * 8));
+  XR_CUDA_TRY(obj->d_sims.reserve((size_t)max_pop * 4));
+  *out = guard.release();
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_obj_destroy(xr_objective obj) {
+  if (!obj) return XR_OK;
+  DeviceGuard g(obj->rc->device);
+  cudaStreamSynchronize(obj->rc->stream());
+  delete obj;
+  return XR_OK;
+}
+
+// Enqueues the whole objective for obj->d_poses (pop poses) on the rc stream.
+static xr_status obj_enqueue(xr_objective obj, int64_t pop) {
+  xr_raycaster rc = obj->rc;
+  const int32_t nv = (int32_t)obj->metrics.size();
+  xr_status st = xr_rc_set_num_projs(rc, (int64_t)nv * pop);
+  if (st != XR_OK) return st;
+  if ((st = xr_rc_distribute_xforms_device(rc, pop, obj->d_poses.as<double>())) != XR_OK) return st;
+  rc->store = XR_PROJ_STORE_REPLACE;  // use_proj_store_replace_method (xregIntensity2D3DRegi.cpp:598)
+  if ((st = rc_enqueue_compute(rc, obj->vol_idx)) != XR_OK) return st;
+  const float* view_sims[16];
+  for (int32_t v = 0; v < nv; ++v) {
+    xr_simmetric m = obj->metrics[(size_t)v];
+    m->num_mov = pop;
+    m->rc = rc;
+    m->proj_offset = (int64_t)v * pop;
+    if ((st = sm_enqueue_compute(m)) != XR_OK) return st;
+    view_sims[v] = m->d_sims.as<float>();
+  }
+  XR_CUDA_TRY(launch_combine_mean(view_sims, nv, pop, obj->d_sims.as<float>(), rc->stream()));
+  return XR_OK;
+}
+
+static bool obj_graph_valid(xr_objective obj, int64_t pop) {
+  if (!obj->graph_exec || obj->graph_pop != pop || obj->graph_rc_gen != obj->rc->generation ||
+      obj->graph_stream != obj->rc->stream())
+    return false;
+  for (size_t v = 0; v < obj->metrics.size(); ++v)
+    if (obj->graph_sm_gen[v] != obj->metrics[v]->generation) return false;
+  return true;
+}
+
+static xr_status obj_run(xr_objective obj, int64_t pop) {
+  xr_raycaster rc = obj->rc;
+  cudaStream_t s = rc->stream();
+  // Host state that the captured kernels read must be current before capture;
+  // a first direct run uploads it and settles generations.
+  if (obj_graph_valid(obj, pop)) {
+    XR_CUDA_TRY(cudaGraphLaunch(obj->graph_exec, s));
+    return XR_OK;
+  }
+  xr_status st = obj_enqueue(obj, pop);
+  if (st != XR_OK || s == nullptr) return st;  // the legacy default stream cannot be captured
+  // Capture the steady-state sequence for the next calls.
+  if (obj->graph_exec) { cudaGraphExecDestroy(obj->graph_exec); obj->graph_exec = nullptr; }
+  cudaGraph_t graph = nullptr;
+  XR_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  st = obj_enqueue(obj, pop);
+  cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (st != XR_OK) { if (graph) cudaGraphDestroy(graph); return st; }
+  if (ce != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail(ce, "cudaStreamEndCapture"); }
+  ce = cudaGraphInstantiate(&obj->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) { obj->graph_exec = nullptr; return cuda_fail(ce, "cudaGraphInstantiate"); }
+  obj->graph_pop = pop;
+  obj->graph_rc_gen = rc->generation;
+  obj->graph_stream = s;
+  obj->graph_sm_gen.resize(obj->metrics.size());
+  for (size_t v = 0; v < obj->metrics.size(); ++v) obj->graph_sm_gen[v] = obj->metrics[v]->generation;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_obj_eval_device(xr_objective obj, int64_t pop, const double* d_xforms,
+                                               float* d_sims) {
+  XR_CHECK_ARG(obj && d_xforms && d_sims, "xr_obj_eval_device: NULL argument");
+  XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "xr_obj_eval_device: population outside [1, max_pop]");
+  DeviceGuard g(obj->rc->device);
+  cudaStream_t s = obj->rc->stream();
+  XR_CUDA_TRY(cudaMemcpyAsync(obj->d_poses.p, d_xforms, (size_t)pop * 16 * 8, cudaMemcpyDeviceToDevice, s));
+  xr_status st = obj_run(obj, pop);
+  if (st != XR_OK) return st;
+  XR_CUDA_TRY(cudaMemcpyAsync(d_sims, obj->d_sims.p, (size_t)pop * 4, cudaMemcpyDeviceToDevice, s));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_obj_eval(xr_objective obj, int64_t pop, const double* h_xforms, float* h_sims) {
+  XR_CHECK_ARG(obj && h_xforms && h_sims, "xr_obj_eval: NULL argument");
+  XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "xr_obj_eval: population outside [1, max_pop]");
+  XR_CHECK_ARG(finite_all(h_xforms, 16 * pop), "xr_obj_eval: non-finite transform");
+  DeviceGuard g(obj->rc->device);
+  cudaStream_t s = obj->rc->stream();
+  XR_CUDA_TRY(cudaMemcpyAsync(obj->d_poses.p, h_xforms, (size_t)pop * 16 * 8, cudaMemcpyHostToDevice, s));
+  xr_status st = obj_run(obj, pop);
+  if (st != XR_OK) return st;
+  XR_CUDA_TRY(cudaMemcpyAsync(h_sims, obj->d_sims.p, (size_t)pop * 4, cudaMemcpyDeviceToHost, s));
+  return xr_rc_synchronize(obj->rc);
+}

@@ -1,0 +1,122 @@
+// xr_internal.h -- device data layouts and launcher declarations shared by the
+// translation units of libxreg_gb300.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <string>
+
+#include "xreg_gb300.h"
+
+namespace xr {
+
+// Per-projection ray set-up in volume index coordinates (96 bytes).  Produced by
+// the FP64 geometry kernel, consumed by every ray-marching kernel.
+//   ray direction for pixel (c, r):   d0 + c*dc + r*dr   (pinhole -> pixel)
+//   same vector in camera-world mm:   e0 + c*ec + r*er   (gives the step count)
+struct ProjGeom {
+  float src[3];
+  float d0[3];
+  float dc[3];
+  float dr[3];
+  float e0[3];
+  float ec[3];
+  float er[3];
+  float pad[3];
+};
+static_assert(sizeof(ProjGeom) == 96, "ProjGeom layout");
+
+// Volume as the kernels see it.
+struct VolView {
+  const void* voxels;  // F32 / F16 / BF16, x fastest
+  int32_t nx, ny, nz;
+  int32_t voxel_type;
+  float inv_scale;     // multiplies the ray sum (1 for F32)
+};
+
+// Launch parameters of a DRR kernel.
+struct DrrParams {
+  VolView vol;
+  const ProjGeom* geo;    // [num_projs]
+  const int32_t* cam_idx; // [num_projs]
+  const float* bg_projs;  // [num_cams][rows*cols] or nullptr
+  float* out;             // [num_projs][rows][cols]
+  unsigned long long* sample_counter;  // nullptr = no counting
+  unsigned int* err_counter;          // rays whose step count exceeded max_steps
+  unsigned long long max_steps;       // guard against non-finite / absurd poses
+  int64_t num_projs;
+  int32_t rows, cols;
+  float step;
+  float default_bg;
+  int32_t kernel_id;      // XR_LINE_INT_SUM / MAX
+  int32_t store;          // XR_PROJ_STORE_REPLACE / ACCUM
+};
+
+// ---- launchers (xr_geom.cu) ----
+// One thread per projection: FP64 composition phys_to_idx * pose, camera
+// inverses, rounded to float ProjGeom.
+cudaError_t launch_proj_geom(const xr_volume_desc& vol, const xr_camera_desc* d_cams,
+                             const double* d_poses, const int32_t* d_cam_idx, int64_t num_projs,
+                             int64_t pose_stride_projs, ProjGeom* d_out, cudaStream_t s);
+
+// ---- launchers (xr_raycast.cu) ----
+cudaError_t launch_drr(const DrrParams& p, cudaStream_t s);
+
+// ---- launchers (xr_metrics.cu) ----
+struct FixedNCC {           // per direction (one for NCC, x and y for grad-NCC)
+  const float* fhat;        // zero-mean fixed image (float)
+  double sd;                // sample std dev, clamped at 1e-6
+  double sum_fhat;          // sum of fhat over used pixels (exact decomposition)
+};
+
+struct PatchFixed {         // per direction
+  const float* img;         // fixed image (or its gradient), rows*cols
+  const float* mean;        // per patch mean
+  const float* scale;       // per patch 1 / (sd * n_patch)
+};
+
+// Moments of moving images for (grad-)NCC: partials[img][block][k] in double.
+cudaError_t launch_ncc_moments(const float* mov, int64_t npix, int64_t nimgs, const float* fhat,
+                               const uint8_t* mask, double* partials, int nblk, cudaStream_t s);
+cudaError_t launch_ncc_finalize(const double* partials, int nblk, int64_t nimgs, int64_t n_used,
+                                FixedNCC fx, float* sims, cudaStream_t s);
+cudaError_t launch_grad_moments(const float* mov, int rows, int cols, int64_t nimgs, int smooth_ksize,
+                                const float* fhat_x, const float* fhat_y, const uint8_t* mask,
+                                double* partials, cudaStream_t s, int* nblk_out);
+cudaError_t launch_grad_finalize(const double* partials, int nblk, int64_t nimgs, int64_t n_used,
+                                 FixedNCC fx, FixedNCC fy, float* sims, cudaStream_t s);
+// Gradient images (blur + Sobel) of nimgs images; used for the fixed image.
+cudaError_t launch_grad_images(const float* img, int rows, int cols, int64_t nimgs, int smooth_ksize,
+                               float* gx, float* gy, cudaStream_t s);
+// Mean / sum-of-squares of an image in double (setup); out[0]=sum, out[1]=sum of (x-mean)^2 computed
+// in a second pass, out[2]=count.
+cudaError_t launch_image_stats(const float* img, int64_t npix, const uint8_t* mask, double* d_out,
+                               cudaStream_t s);
+cudaError_t launch_sub_scalar(const float* in, int64_t n, double value, float* out, cudaStream_t s);
+cudaError_t launch_sum_f(const float* in, int64_t n, const uint8_t* mask, double* d_out, cudaStream_t s);
+// Per-patch statistics of a fixed image for patch NCC.
+cudaError_t launch_patch_fixed_stats(const float* img, int rows, int cols, int radius, int stride,
+                                     int ncr, int ncc, float* mean, float* scale, cudaStream_t s);
+cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs, int grad, int smooth_ksize,
+                             int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py,
+                             double* partials, cudaStream_t s, int* nblk_out);
+cudaError_t launch_patch_finalize(const double* partials, int nblk, int64_t nimgs, int64_t npatch, int grad,
+                                  float* sims, cudaStream_t s);
+// Mean over views of per-view similarity values: sims[v][pop] -> out[pop].
+cudaError_t launch_combine_mean(const float* const* view_sims, int nviews, int64_t pop, float* out,
+                                cudaStream_t s);
+
+// ---- error plumbing (xr_capi.cu) ----
+void set_error(const std::string& msg);
+xr_status fail(xr_status code, const std::string& msg);
+xr_status cuda_fail(cudaError_t e, const char* what);
+
+}  // namespace xr
+
+#define XR_CUDA_TRY(expr)                                                        \
+  do {                                                                           \
+    cudaError_t xr_e_ = (expr);                                                  \
+    if (xr_e_ != cudaSuccess) return ::xr::cuda_fail(xr_e_, #expr);              \
+  } while (0)

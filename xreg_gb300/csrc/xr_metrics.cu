@@ -1,0 +1,598 @@
+// xr_metrics.cu -- 2D similarity metric kernels.
+//
+// NCC (xregImgSimMetric2DNCCCPU.cpp:53-63,164-209): per moving image the sums
+// S_m, S_mm, S_mf (f = zero-mean fixed image) are accumulated per thread in
+// compensated (Kahan) float, reduced per block in double, and combined per image
+// in double:  mean_m = S_m/n, var_m = (S_mm - n mean_m^2)/(n-1), sd = max(1e-6, sqrt),
+// cov = S_mf - mean_m * sum(f), ncc = cov / (n sd_f sd_m), sim = (1 - ncc)/2.
+//
+// Gradient images (xregImgSimMetric2DGradImgCPU.cpp:48-65,86-101): 5x5 Gaussian
+// with OpenCV's fixed sigma-0 kernel [1 4 6 4 1]/16 (3x3: [1 2 1]/4), then 3x3
+// Sobel in x and y, BORDER_REFLECT_101 everywhere.  A block stages a 32x32 tile
+// plus halo in shared memory; the blurred tile is computed over the
+// reflect-extended input, which equals the reflect-extended blurred image because
+// the kernels are symmetric.
+//
+// Patch NCC (xregImgSimMetric2DPatchNCCCPU.cpp:205-287,558-619): one thread per
+// patch centre, two-pass mean / sample std dev over the (2r+1)^2 window from a
+// shared-memory tile, score 1 - sum((m - mu_m)/sd_m * fhat), unit weights, mean
+// over patches.  The fixed side (per-patch mean and 1/(sd n)) is pre-computed once.
+#include "xr_internal.h"
+
+namespace xr {
+namespace {
+
+constexpr int kT = 32;          // output tile edge for gradient kernels
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int reflect101(int i, int n) {
+  if (i < 0) i = -i;
+  if (i >= n) i = 2 * (n - 1) - i;
+  return i;
+}
+
+struct Kahan {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of K doubles per thread; result valid in thread 0.
+template <int K>
+__device__ __forceinline__ void block_sum_d(double (&v)[K], double* red /* [K][32] */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const double w = warp_sum_d(v[k]);
+    if (lane == 0) red[k * 32 + warp] = w;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double w = (lane < nw) ? red[k * 32 + lane] : 0.0;
+      w = warp_sum_d(w);
+      v[k] = w;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ setup --
+__global__ void image_sum_kernel(const float* __restrict__ img, int64_t n, const uint8_t* __restrict__ mask,
+                                 double* __restrict__ out) {
+  __shared__ double red[2 * 32];
+  double v[2] = {0.0, 0.0};
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+    if (!mask || mask[i]) { v[0] += (double)img[i]; v[1] += 1.0; }
+  block_sum_d<2>(v, red);
+  if (threadIdx.x == 0) { out[0] = v[0]; out[2] = v[1]; }
+}
+
+__global__ void image_var_kernel(const float* __restrict__ img, int64_t n, const uint8_t* __restrict__ mask,
+                                 double* __restrict__ out) {
+  __shared__ double red[1 * 32];
+  const double mean = out[0] / out[2];
+  double v[1] = {0.0};
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+    if (!mask || mask[i]) { const double d = (double)img[i] - mean; v[0] += d * d; }
+  block_sum_d<1>(v, red);
+  if (threadIdx.x == 0) out[1] = v[0];
+}
+
+__global__ void sub_scalar_kernel(const float* __restrict__ in, int64_t n, float value, float* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = in[i] - value;
+}
+
+// ---------------------------------------------------------------- NCC -----
+__global__ void __launch_bounds__(kThreads) ncc_moments_kernel(const float* __restrict__ mov, int64_t npix,
+                                                               const float* __restrict__ fhat,
+                                                               const uint8_t* __restrict__ mask,
+                                                               double* __restrict__ partials) {
+  __shared__ double red[3 * 32];
+  const int64_t img = blockIdx.y;
+  const float* m = mov + img * npix;
+  Kahan s0, s1, s2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+    if (mask && !mask[i]) continue;
+    const float x = m[i];
+    s0.add(x);
+    s1.add(x * x);
+    s2.add(x * fhat[i]);
+  }
+  double v[3] = {s0.value(), s1.value(), s2.value()};
+  block_sum_d<3>(v, red);
+  if (threadIdx.x == 0) {
+    double* o = partials + (img * gridDim.x + blockIdx.x) * 3;
+    o[0] = v[0]; o[1] = v[1]; o[2] = v[2];
+  }
+}
+
+__device__ __forceinline__ double ncc_sim_from_moments(double sm, double smm, double smf, double n,
+                                                       const FixedNCC& fx) {
+  const double mean = sm / n;
+  double var = (smm - n * mean * mean) / (n - 1.0);
+  if (var < 0.0) var = 0.0;
+  double sd = sqrt(var);
+  if (sd < 1.0e-6) sd = 1.0e-6;
+  const double cov = smf - mean * fx.sum_fhat;
+  const double ncc = cov / (n * fx.sd * sd);
+  return (1.0 - ncc) * 0.5;
+}
+
+__global__ void ncc_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double n,
+                                    FixedNCC fx, float* __restrict__ sims) {
+  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (img >= nimgs) return;
+  double a = 0, b = 0, c = 0;
+  const double* p = partials + img * nblk * 3;
+  for (int k = 0; k < nblk; ++k) { a += p[3 * k]; b += p[3 * k + 1]; c += p[3 * k + 2]; }
+  sims[img] = (float)ncc_sim_from_moments(a, b, c, n, fx);
+}
+
+// ------------------------------------------------------ gradient images ---
+// Stages rows [y0-H, y0+kT+H) x cols [x0-H, x0+kT+H) of an image (reflected at
+// the borders), blurs with radius KR and applies Sobel on the kT x kT tile.
+template <int KR>
+struct GradTile {
+  static constexpr int H = KR + 1;            // total halo
+  static constexpr int WI = kT + 2 * H;       // staged input edge
+  static constexpr int WB = kT + 2;           // blurred region edge
+  float in[WI][WI + 1];
+  float hb[WI][WB + 1];
+  float bl[WB][WB + 1];
+
+  __device__ void load(const float* __restrict__ img, int rows, int cols, int y0, int x0) {
+    for (int i = threadIdx.x; i < WI * WI; i += blockDim.x) {
+      const int r = i / WI, c = i - r * WI;
+      // Rows/cols past the last tile pixel only feed pixels that are skipped;
+      // clamping before the reflection keeps every read inside the image.
+      const int gr = reflect101(min(y0 - H + r, rows - 1 + H), rows);
+      const int gc = reflect101(min(x0 - H + c, cols - 1 + H), cols);
+      in[r][c] = img[(int64_t)gr * cols + gc];
+    }
+    __syncthreads();
+  }
+
+  __device__ void blur() {
+    if constexpr (KR == 0) {
+      for (int i = threadIdx.x; i < WB * WB; i += blockDim.x) {
+        const int r = i / WB, c = i - r * WB;
+        bl[r][c] = in[r][c];
+      }
+      __syncthreads();
+    } else {
+    // horizontal pass over all staged rows, blurred columns [x0-1, x0+kT+1)
+    for (int i = threadIdx.x; i < WI * WB; i += blockDim.x) {
+      const int r = i / WB, c = i - r * WB;
+      float s;
+      if (KR == 2) {
+        s = 0.0625f * in[r][c] + 0.25f * in[r][c + 1] + 0.375f * in[r][c + 2] + 0.25f * in[r][c + 3] +
+            0.0625f * in[r][c + 4];
+      } else {
+        s = 0.25f * in[r][c] + 0.5f * in[r][c + 1] + 0.25f * in[r][c + 2];
+      }
+      hb[r][c] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < WB * WB; i += blockDim.x) {
+      const int r = i / WB, c = i - r * WB;
+      float s;
+      if (KR == 2) {
+        s = 0.0625f * hb[r][c] + 0.25f * hb[r + 1][c] + 0.375f * hb[r + 2][c] + 0.25f * hb[r + 3][c] +
+            0.0625f * hb[r + 4][c];
+      } else {
+        s = 0.25f * hb[r][c] + 0.5f * hb[r + 1][c] + 0.25f * hb[r + 2][c];
+      }
+      bl[r][c] = s;
+    }
+    __syncthreads();
+    }
+  }
+
+  // Sobel at tile pixel (ty, tx) in [0, kT).
+  __device__ __forceinline__ void sobel(int ty, int tx, float& gx, float& gy) const {
+    const int r = ty + 1, c = tx + 1;
+    const float a = bl[r - 1][c - 1], b = bl[r - 1][c], cc = bl[r - 1][c + 1];
+    const float d = bl[r][c - 1], f = bl[r][c + 1];
+    const float g = bl[r + 1][c - 1], h = bl[r + 1][c], ii = bl[r + 1][c + 1];
+    gx = ((cc - a) + 2.0f * (f - d)) + (ii - g);
+    gy = ((g - a) + 2.0f * (h - b)) + (ii - cc);
+  }
+};
+
+template <int KR>
+__global__ void __launch_bounds__(kThreads) grad_images_kernel(const float* __restrict__ imgs, int rows, int cols,
+                                                               float* __restrict__ gx, float* __restrict__ gy) {
+  __shared__ GradTile<KR> t;
+  const int tiles_x = (cols + kT - 1) / kT;
+  const int y0 = (blockIdx.x / tiles_x) * kT, x0 = (blockIdx.x % tiles_x) * kT;
+  const int64_t npix = (int64_t)rows * cols;
+  const int64_t img = blockIdx.y;
+  t.load(imgs + img * npix, rows, cols, y0, x0);
+  t.blur();
+  for (int i = threadIdx.x; i < kT * kT; i += blockDim.x) {
+    const int ty = i / kT, tx = i - ty * kT;
+    if (y0 + ty >= rows || x0 + tx >= cols) continue;
+    float a, b;
+    t.sobel(ty, tx, a, b);
+    const int64_t o = img * npix + (int64_t)(y0 + ty) * cols + x0 + tx;
+    gx[o] = a;
+    gy[o] = b;
+  }
+}
+
+template <int KR>
+__global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __restrict__ imgs, int rows, int cols,
+                                                                const float* __restrict__ fhx,
+                                                                const float* __restrict__ fhy,
+                                                                const uint8_t* __restrict__ mask,
+                                                                double* __restrict__ partials) {
+  __shared__ GradTile<KR> t;
+  __shared__ double red[6 * 32];
+  const int tiles_x = (cols + kT - 1) / kT;
+  const int y0 = (blockIdx.x / tiles_x) * kT, x0 = (blockIdx.x % tiles_x) * kT;
+  const int64_t npix = (int64_t)rows * cols;
+  const int64_t img = blockIdx.y;
+  t.load(imgs + img * npix, rows, cols, y0, x0);
+  t.blur();
+  Kahan s[6];
+  for (int i = threadIdx.x; i < kT * kT; i += blockDim.x) {
+    const int ty = i / kT, tx = i - ty * kT;
+    if (y0 + ty >= rows || x0 + tx >= cols) continue;
+    const int64_t pix = (int64_t)(y0 + ty) * cols + x0 + tx;
+    if (mask && !mask[pix]) continue;
+    float a, b;
+    t.sobel(ty, tx, a, b);
+    s[0].add(a); s[1].add(a * a); s[2].add(a * fhx[pix]);
+    s[3].add(b); s[4].add(b * b); s[5].add(b * fhy[pix]);
+  }
+  double v[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) v[k] = s[k].value();
+  block_sum_d<6>(v, red);
+  if (threadIdx.x == 0) {
+    double* o = partials + (img * gridDim.x + blockIdx.x) * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = v[k];
+  }
+}
+
+__global__ void grad_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double n,
+                                     FixedNCC fx, FixedNCC fy, float* __restrict__ sims) {
+  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (img >= nimgs) return;
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  const double* p = partials + img * nblk * 6;
+  for (int k = 0; k < nblk; ++k)
+    for (int j = 0; j < 6; ++j) a[j] += p[6 * k + j];
+  const double sx = ncc_sim_from_moments(a[0], a[1], a[2], n, fx);
+  const double sy = ncc_sim_from_moments(a[3], a[4], a[5], n, fy);
+  // 0.5 * (float(s_x) + float(s_y)) as in ImgSimMetric2DGradNCCCPU::compute
+  sims[img] = 0.5f * ((float)sx + (float)sy);
+}
+
+// ------------------------------------------------------------ patch NCC ---
+constexpr int kPC = 16;  // patch centres per tile edge
+
+__global__ void patch_fixed_stats_kernel(const float* __restrict__ img, int cols, int radius, int stride,
+                                         int ncr, int ncc, float* __restrict__ mean, float* __restrict__ scale) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (int64_t)ncr * ncc) return;
+  const int pr = (int)(p / ncc), pc = (int)(p - (int64_t)pr * ncc);
+  const int r0 = pr * stride, c0 = pc * stride, d = 2 * radius + 1;
+  const double np = (double)d * d;
+  double s = 0;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) s += img[(int64_t)(r0 + r) * cols + c0 + c];
+  const double mu = s / np;
+  double v = 0;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      const double t = img[(int64_t)(r0 + r) * cols + c0 + c] - mu;
+      v += t * t;
+    }
+  double sd = sqrt(v / (np - 1.0));
+  if (sd < 1.0e-6) sd = 1.0e-6;
+  mean[p] = (float)mu;
+  scale[p] = (float)(1.0 / (sd * np));
+}
+
+// Shared-memory layout for one tile of kPC x kPC patch centres (dynamic).
+struct PatchLayout {
+  int W;    // edge of the patch-window region (moving gradient / fixed tiles)
+  int WI;   // staged input edge
+  int WB;   // blurred edge
+  size_t bytes;
+  __host__ __device__ static PatchLayout make(int radius, int stride, int grad, int kr) {
+    PatchLayout L;
+    L.W = (kPC - 1) * stride + 2 * radius + 1;
+    L.WB = grad ? L.W + 2 : L.W;
+    L.WI = grad ? L.WB + 2 * kr : L.W;
+    const size_t fl = grad ? ((size_t)L.WI * L.WI + (size_t)L.WI * L.WB + (size_t)L.WB * L.WB +
+                              4 * (size_t)L.W * L.W)
+                           : ((size_t)L.WI * L.WI + (size_t)L.W * L.W);
+    L.bytes = fl * sizeof(float);
+    return L;
+  }
+};
+
+__device__ __forceinline__ float patch_score(const float* __restrict__ m, const float* __restrict__ f, int W,
+                                             int r0, int c0, int d, float fmean, float fscale) {
+  float s = 0.0f;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) s += m[(r0 + r) * W + c0 + c];
+  const float n = (float)(d * d);
+  const float mu = s / n;
+  float v = 0.0f, cov = 0.0f;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      const float dm = m[(r0 + r) * W + c0 + c] - mu;
+      v = fmaf(dm, dm, v);
+      cov = fmaf(dm, f[(r0 + r) * W + c0 + c] - fmean, cov);
+    }
+  float sd = sqrtf(v / (n - 1.0f));
+  sd = fmaxf(sd, 1.0e-6f);
+  return 1.0f - (cov / sd) * fscale;
+}
+
+template <int GRAD, int KR>
+__global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __restrict__ imgs, int rows, int cols,
+                                                             int radius, int stride, int ncr, int ncc,
+                                                             PatchFixed px, PatchFixed py,
+                                                             double* __restrict__ partials) {
+  extern __shared__ float sm[];
+  __shared__ double red[2 * 32];
+  const PatchLayout L = PatchLayout::make(radius, stride, GRAD, KR);
+  const int W = L.W, WI = L.WI, WB = L.WB;
+  float* s_in = sm;                         // WI x WI
+  float* s_hb = s_in + WI * WI;             // WI x WB (GRAD)
+  float* s_bl = s_hb + WI * WB;             // WB x WB (GRAD)
+  float* s_mx = GRAD ? s_bl + WB * WB : s_in;   // W x W moving (gx or raw)
+  float* s_my = s_mx + W * W;               // W x W moving gy
+  float* s_fx = GRAD ? s_my + W * W : s_in + WI * WI;  // W x W fixed (gx or raw)
+  float* s_fy = s_fx + W * W;
+
+  const int tiles_x = (ncc + kPC - 1) / kPC;
+  const int tpr = blockIdx.x / tiles_x, tpc = blockIdx.x - tpr * tiles_x;
+  const int pr0 = tpr * kPC, pc0 = tpc * kPC;
+  const int y0 = pr0 * stride, x0 = pc0 * stride;  // top-left pixel of the window region
+  const int64_t npix = (int64_t)rows * cols;
+  const int64_t img = blockIdx.y;
+  const float* src = imgs + img * npix;
+  const int H = GRAD ? (KR + 1) : 0;
+
+  for (int i = threadIdx.x; i < WI * WI; i += blockDim.x) {
+    const int r = i / WI, c = i - r * WI;
+    const int gr = reflect101(min(y0 - H + r, rows - 1 + H), rows);
+    const int gc = reflect101(min(x0 - H + c, cols - 1 + H), cols);
+    s_in[i] = src[(int64_t)gr * cols + gc];
+  }
+  for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
+    const int r = i / W, c = i - r * W;
+    const int gr = min(y0 + r, rows - 1), gc = min(x0 + c, cols - 1);
+    s_fx[i] = px.img[(int64_t)gr * cols + gc];
+    if (GRAD) s_fy[i] = py.img[(int64_t)gr * cols + gc];
+  }
+  __syncthreads();
+  if (GRAD) {
+    if (KR == 0) {
+      for (int i = threadIdx.x; i < WB * WB; i += blockDim.x) {
+        const int r = i / WB, c = i - r * WB;
+        s_bl[i] = s_in[r * WI + c];
+      }
+    } else {
+      for (int i = threadIdx.x; i < WI * WB; i += blockDim.x) {
+        const int r = i / WB, c = i - r * WB;
+        const float* q = s_in + r * WI + c;
+        s_hb[i] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[1] + 0.375f * q[2] + 0.25f * q[3] + 0.0625f * q[4])
+                            : (0.25f * q[0] + 0.5f * q[1] + 0.25f * q[2]);
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < WB * WB; i += blockDim.x) {
+        const int r = i / WB, c = i - r * WB;
+        const float* q = s_hb + r * WB + c;
+        s_bl[i] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[WB] + 0.375f * q[2 * WB] + 0.25f * q[3 * WB] +
+                               0.0625f * q[4 * WB])
+                            : (0.25f * q[0] + 0.5f * q[WB] + 0.25f * q[2 * WB]);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
+      const int r = i / W + 1, c = i % W + 1;
+      const float* q = s_bl;
+      const float a = q[(r - 1) * WB + c - 1], b = q[(r - 1) * WB + c], cc = q[(r - 1) * WB + c + 1];
+      const float d = q[r * WB + c - 1], f = q[r * WB + c + 1];
+      const float g = q[(r + 1) * WB + c - 1], h = q[(r + 1) * WB + c], ii = q[(r + 1) * WB + c + 1];
+      s_mx[i] = ((cc - a) + 2.0f * (f - d)) + (ii - g);
+      s_my[i] = ((g - a) + 2.0f * (h - b)) + (ii - cc);
+    }
+  }
+  __syncthreads();
+
+  double v[2] = {0.0, 0.0};
+  const int lr = threadIdx.x / kPC, lc = threadIdx.x % kPC;
+  const int pr = pr0 + lr, pc = pc0 + lc;
+  if (pr < ncr && pc < ncc) {
+    const int64_t pidx = (int64_t)pr * ncc + pc;
+    const int d = 2 * radius + 1;
+    v[0] = patch_score(s_mx, s_fx, W, lr * stride, lc * stride, d, px.mean[pidx], px.scale[pidx]);
+    if (GRAD) v[1] = patch_score(s_my, s_fy, W, lr * stride, lc * stride, d, py.mean[pidx], py.scale[pidx]);
+  }
+  block_sum_d<2>(v, red);
+  if (threadIdx.x == 0) {
+    double* o = partials + (img * gridDim.x + blockIdx.x) * 2;
+    o[0] = v[0];
+    o[1] = v[1];
+  }
+}
+
+__global__ void patch_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs,
+                                      double npatch, int grad, float* __restrict__ sims) {
+  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (img >= nimgs) return;
+  double a = 0, b = 0;
+  const double* p = partials + img * nblk * 2;
+  for (int k = 0; k < nblk; ++k) { a += p[2 * k]; b += p[2 * k + 1]; }
+  const float sx = (float)(a / npatch);
+  if (grad) sims[img] = 0.5f * (sx + (float)(b / npatch));
+  else sims[img] = sx;
+}
+
+struct ViewPtrs {
+  const float* p[16];
+};
+
+__global__ void combine_mean_kernel(ViewPtrs vp, int nviews, int64_t pop, float* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= pop) return;
+  float s = 0.0f;
+  for (int v = 0; v < nviews; ++v) s += vp.p[v][i];
+  out[i] = s / (float)nviews;
+}
+
+template <typename K>
+cudaError_t set_smem(K kern, size_t bytes) {
+  if (bytes > 48 * 1024) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_image_stats(const float* img, int64_t npix, const uint8_t* mask, double* d_out, cudaStream_t s) {
+  image_sum_kernel<<<1, 1024, 0, s>>>(img, npix, mask, d_out);
+  image_var_kernel<<<1, 1024, 0, s>>>(img, npix, mask, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_f(const float* in, int64_t n, const uint8_t* mask, double* d_out, cudaStream_t s) {
+  image_sum_kernel<<<1, 1024, 0, s>>>(in, n, mask, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sub_scalar(const float* in, int64_t n, double value, float* out, cudaStream_t s) {
+  const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  sub_scalar_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(in, n, (float)value, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ncc_moments(const float* mov, int64_t npix, int64_t nimgs, const float* fhat,
+                               const uint8_t* mask, double* partials, int nblk, cudaStream_t s) {
+  if (nimgs <= 0) return cudaSuccess;
+  const dim3 grid(nblk, (unsigned)nimgs);
+  ncc_moments_kernel<<<grid, kThreads, 0, s>>>(mov, npix, fhat, mask, partials);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ncc_finalize(const double* partials, int nblk, int64_t nimgs, int64_t n_used, FixedNCC fx,
+                                float* sims, cudaStream_t s) {
+  if (nimgs <= 0) return cudaSuccess;
+  ncc_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, (double)n_used, fx,
+                                                                      sims);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_images(const float* img, int rows, int cols, int64_t nimgs, int smooth_ksize, float* gx,
+                               float* gy, cudaStream_t s) {
+  const int tiles = ((rows + kT - 1) / kT) * ((cols + kT - 1) / kT);
+  const dim3 grid(tiles, (unsigned)nimgs);
+  switch (smooth_ksize) {
+    case 0: grad_images_kernel<0><<<grid, kThreads, 0, s>>>(img, rows, cols, gx, gy); break;
+    case 3: grad_images_kernel<1><<<grid, kThreads, 0, s>>>(img, rows, cols, gx, gy); break;
+    case 5: grad_images_kernel<2><<<grid, kThreads, 0, s>>>(img, rows, cols, gx, gy); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_moments(const float* mov, int rows, int cols, int64_t nimgs, int smooth_ksize,
+                                const float* fhat_x, const float* fhat_y, const uint8_t* mask, double* partials,
+                                cudaStream_t s, int* nblk_out) {
+  const int tiles = ((rows + kT - 1) / kT) * ((cols + kT - 1) / kT);
+  if (nblk_out) *nblk_out = tiles;
+  if (nimgs <= 0 || !partials) return cudaSuccess;
+  const dim3 grid(tiles, (unsigned)nimgs);
+  switch (smooth_ksize) {
+    case 0: grad_moments_kernel<0><<<grid, kThreads, 0, s>>>(mov, rows, cols, fhat_x, fhat_y, mask, partials); break;
+    case 3: grad_moments_kernel<1><<<grid, kThreads, 0, s>>>(mov, rows, cols, fhat_x, fhat_y, mask, partials); break;
+    case 5: grad_moments_kernel<2><<<grid, kThreads, 0, s>>>(mov, rows, cols, fhat_x, fhat_y, mask, partials); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_finalize(const double* partials, int nblk, int64_t nimgs, int64_t n_used, FixedNCC fx,
+                                 FixedNCC fy, float* sims, cudaStream_t s) {
+  if (nimgs <= 0) return cudaSuccess;
+  grad_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, (double)n_used, fx,
+                                                                       fy, sims);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_patch_fixed_stats(const float* img, int rows, int cols, int radius, int stride, int ncr, int ncc,
+                                     float* mean, float* scale, cudaStream_t s) {
+  (void)rows;
+  const int64_t n = (int64_t)ncr * ncc;
+  if (n <= 0) return cudaSuccess;
+  patch_fixed_stats_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(img, cols, radius, stride, ncr, ncc, mean,
+                                                                       scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs, int grad, int smooth_ksize,
+                             int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py,
+                             double* partials, cudaStream_t s, int* nblk_out) {
+  const int tiles = ((ncr + kPC - 1) / kPC) * ((ncc + kPC - 1) / kPC);
+  if (nblk_out) *nblk_out = tiles;
+  if (nimgs <= 0 || !partials) return cudaSuccess;
+  const int kr = smooth_ksize == 5 ? 2 : (smooth_ksize == 3 ? 1 : 0);
+  if (smooth_ksize != 0 && smooth_ksize != 3 && smooth_ksize != 5) return cudaErrorInvalidValue;
+  const PatchLayout L = PatchLayout::make(radius, stride, grad, kr);
+  if (L.bytes > 200 * 1024) return cudaErrorInvalidValue;
+  const dim3 grid(tiles, (unsigned)nimgs);
+  cudaError_t e = cudaSuccess;
+#define XR_PATCH_LAUNCH(G, K)                                                                           \
+  e = set_smem(patch_ncc_kernel<G, K>, L.bytes);                                                       \
+  if (e != cudaSuccess) return e;                                                                       \
+  patch_ncc_kernel<G, K><<<grid, kThreads, L.bytes, s>>>(mov, rows, cols, radius, stride, ncr, ncc, px, py, \
+                                                         partials);
+  if (!grad) {
+    XR_PATCH_LAUNCH(0, 0)
+  } else if (kr == 0) {
+    XR_PATCH_LAUNCH(1, 0)
+  } else if (kr == 1) {
+    XR_PATCH_LAUNCH(1, 1)
+  } else {
+    XR_PATCH_LAUNCH(1, 2)
+  }
+#undef XR_PATCH_LAUNCH
+  return cudaGetLastError();
+}
+
+cudaError_t launch_patch_finalize(const double* partials, int nblk, int64_t nimgs, int64_t npatch, int grad,
+                                  float* sims, cudaStream_t s) {
+  if (nimgs <= 0) return cudaSuccess;
+  patch_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, (double)npatch, grad,
+                                                                        sims);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_combine_mean(const float* const* view_sims, int nviews, int64_t pop, float* out, cudaStream_t s) {
+  if (nviews < 1 || nviews > 16) return cudaErrorInvalidValue;
+  ViewPtrs vp;
+  for (int v = 0; v < 16; ++v) vp.p[v] = v < nviews ? view_sims[v] : nullptr;
+  combine_mean_kernel<<<(unsigned)((pop + 127) / 128), 128, 0, s>>>(vp, nviews, pop, out);
+  return cudaGetLastError();
+}
+
+}  // namespace xr
