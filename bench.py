@@ -23,6 +23,7 @@ Multi-GPU: replicas only (each rank evaluates its own populations; no collective
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -454,6 +455,7 @@ def run_reference(a, rank, world):
 
 
 def main():
+    faulthandler.enable()
     a = _args()
     rank, world, local = _dist()
     if world > 1:

@@ -1,0 +1,211 @@
+// xreg_gb300.hpp -- header-only C++ host classes over the C ABI (xreg_gb300.h)
+// with the method names of xReg's RayCaster (lib/ray_cast/xregRayCastInterface.h)
+// and ImgSimMetric2D (lib/regi/sim_metrics_2d/xregImgSimMetric2D.h).  Errors come
+// back as xreg_gb300::Error (status + message); nothing else is thrown.  The
+// classes hold plain arrays instead of ITK/Eigen types; the adapter that derives
+// from xreg::RayCaster inside an xReg build converts at its boundary.
+#ifndef XREG_GB300_HPP_
+#define XREG_GB300_HPP_
+
+#include <array>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../xreg_gb300.h"
+
+namespace xreg_gb300 {
+
+class Error : public std::runtime_error {
+ public:
+  Error(xr_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+  xr_status status;
+};
+
+class UnsupportedOperationException : public Error {
+ public:
+  using Error::Error;
+};
+
+inline void check(xr_status s) {
+  if (s == XR_OK) return;
+  const std::string msg = xr_last_error();
+  if (s == XR_ERR_UNSUPPORTED) throw UnsupportedOperationException(s, msg);
+  throw Error(s, msg);
+}
+
+using Mat4 = std::array<double, 16>;  // row-major 4x4
+
+struct CameraModel {
+  xr_camera_desc desc{};
+  void setup(double focal_len, int64_t nr, int64_t nc, double rs, double cs,
+             int32_t frame = XR_CAM_FOCAL_NEG_Z) {
+    check(xr_camera_setup_naive(focal_len, nr, nc, rs, cs, frame, &desc));
+  }
+  int64_t num_det_rows() const { return desc.num_det_rows; }
+  int64_t num_det_cols() const { return desc.num_det_cols; }
+};
+
+inline CameraModel DownsampleCameraModel(const CameraModel& src, double ds, bool force_even_dims = false) {
+  CameraModel d;
+  check(xr_camera_downsample(&src.desc, ds, force_even_dims ? 1 : 0, &d.desc));
+  return d;
+}
+
+struct Volume {
+  xr_volume_desc desc{};
+  const float* voxels = nullptr;  // host, x fastest; borrowed until set_volumes returns
+};
+
+class RayCasterLineIntCUDA {
+ public:
+  explicit RayCasterLineIntCUDA(int device = -1) { check(xr_rc_create(device, &h_)); }
+  ~RayCasterLineIntCUDA() { xr_rc_destroy(h_); }
+  RayCasterLineIntCUDA(const RayCasterLineIntCUDA&) = delete;
+  RayCasterLineIntCUDA& operator=(const RayCasterLineIntCUDA&) = delete;
+
+  xr_raycaster handle() const { return h_; }
+
+  void set_volume(const Volume& v, int32_t voxel_type = XR_VOXEL_F32) { set_volumes({v}, voxel_type); }
+  void set_volumes(const std::vector<Volume>& vols, int32_t voxel_type = XR_VOXEL_F32, float scale = 0.0f) {
+    std::vector<xr_volume_desc> d;
+    std::vector<const float*> p;
+    for (const auto& v : vols) { d.push_back(v.desc); p.push_back(v.voxels); }
+    check(xr_rc_set_volumes(h_, (int32_t)vols.size(), d.data(), p.data(), voxel_type, scale));
+  }
+  void set_camera_model(const CameraModel& c) { set_camera_models({c}); }
+  void set_camera_models(const std::vector<CameraModel>& cams) {
+    std::vector<xr_camera_desc> d;
+    for (const auto& c : cams) d.push_back(c.desc);
+    check(xr_rc_set_camera_models(h_, (int32_t)d.size(), d.data()));
+    num_cams_ = d.size();
+    if (!d.empty()) { rows_ = d[0].num_det_rows; cols_ = d[0].num_det_cols; }
+  }
+  size_t num_camera_models() const { return num_cams_; }
+  void set_num_projs(int64_t n) { check(xr_rc_set_num_projs(h_, n)); }
+  int64_t num_projs() const { int64_t n = 0; check(xr_rc_num_projs(h_, &n)); return n; }
+  void set_ray_step_size(float s) { check(xr_rc_set_ray_step_size(h_, s)); }
+  void set_interp_method(int32_t m) { check(xr_rc_set_interp_method(h_, m)); }
+  void use_linear_interp() { set_interp_method(XR_INTERP_LINEAR); }
+  void use_proj_store_replace_method() { check(xr_rc_set_proj_store_method(h_, XR_PROJ_STORE_REPLACE)); }
+  void use_proj_store_accum_method() { check(xr_rc_set_proj_store_method(h_, XR_PROJ_STORE_ACCUM)); }
+  void set_default_bg_pixel_val(float v) { check(xr_rc_set_default_bg_pixel_val(h_, v)); }
+  void set_kernel_id(int32_t k) { check(xr_rc_set_kernel_id(h_, k)); }
+  void set_bg_projs(const std::vector<const float*>& imgs, bool use = true) {
+    check(xr_rc_set_bg_projs(h_, imgs.data(), use ? 1 : 0));
+  }
+  void set_use_bg_projs(bool use) { check(xr_rc_set_use_bg_projs(h_, use ? 1 : 0)); }
+  void set_xforms_cam_to_itk_phys(const std::vector<Mat4>& x) {
+    check(xr_rc_set_xforms_cam_to_itk_phys(h_, (int64_t)x.size(), x.empty() ? nullptr : x[0].data()));
+  }
+  void distribute_xforms_among_cam_models(const std::vector<Mat4>& x) {
+    check(xr_rc_distribute_xforms_among_cam_models(h_, (int64_t)x.size(), x.empty() ? nullptr : x[0].data()));
+  }
+  void distribute_xform_among_cam_models(const Mat4& x) { distribute_xforms_among_cam_models({x}); }
+  void set_camera_model_proj_associations(const std::vector<int32_t>& a) {
+    check(xr_rc_set_camera_model_proj_associations(h_, (int64_t)a.size(), a.data()));
+  }
+  void allocate_resources() { check(xr_rc_allocate_resources(h_)); }
+  int64_t max_num_projs_possible() const { int64_t n = 0; check(xr_rc_max_num_projs_possible(h_, &n)); return n; }
+  void compute(int32_t vol_idx = 0) { check(xr_rc_compute(h_, vol_idx)); }
+  // proj(idx): host copy (xReg returns a shallow view invalidated by the next compute)
+  std::vector<float> proj(int64_t idx) const {
+    std::vector<float> out((size_t)(rows_ * cols_));
+    check(xr_rc_proj(h_, idx, out.data()));
+    return out;
+  }
+  std::vector<float> raw_host_pixel_buf() const {
+    std::vector<float> out((size_t)(rows_ * cols_ * num_projs()));
+    check(xr_rc_copy_projs_to_host(h_, out.data()));
+    return out;
+  }
+  float* to_cuda_buf() const { float* p = nullptr; check(xr_rc_device_pixel_buf(h_, &p)); return p; }
+  // RayCasterCPU::use_other_proj_buf is unsupported in xReg's CPU caster as well.
+  void use_other_proj_buf(RayCasterLineIntCUDA*) {
+    throw UnsupportedOperationException(XR_ERR_UNSUPPORTED, "use_other_proj_buf is not supported");
+  }
+
+ private:
+  xr_raycaster h_ = nullptr;
+  size_t num_cams_ = 0;
+  int64_t rows_ = 0, cols_ = 0;
+};
+
+class ImgSimMetric2DCUDA {
+ public:
+  explicit ImgSimMetric2DCUDA(int32_t kind, int device = -1) { check(xr_sm_create(kind, device, &h_)); }
+  virtual ~ImgSimMetric2DCUDA() { xr_sm_destroy(h_); }
+  ImgSimMetric2DCUDA(const ImgSimMetric2DCUDA&) = delete;
+  ImgSimMetric2DCUDA& operator=(const ImgSimMetric2DCUDA&) = delete;
+
+  xr_simmetric handle() const { return h_; }
+  void set_fixed_image(const float* img, int64_t rows, int64_t cols) {
+    check(xr_sm_set_fixed_image(h_, img, rows, cols));
+  }
+  void set_mask(const uint8_t* mask) { check(xr_sm_set_mask(h_, mask)); }
+  void set_num_moving_images(int64_t n) { check(xr_sm_set_num_moving_images(h_, n)); n_ = n; }
+  int64_t num_moving_images() const { return n_; }
+  void set_mov_imgs_buf_from_ray_caster(RayCasterLineIntCUDA* rc, int64_t proj_offset = 0) {
+    check(xr_sm_set_mov_imgs_buf_from_ray_caster(h_, rc->handle(), proj_offset));
+  }
+  void allocate_resources() { check(xr_sm_allocate_resources(h_)); }
+  void compute() { check(xr_sm_compute(h_)); }
+  std::vector<float> sim_vals() const {
+    std::vector<float> out((size_t)n_);
+    check(xr_sm_sim_vals(h_, out.data()));
+    return out;
+  }
+  float sim_val(int64_t i) const { return sim_vals().at((size_t)i); }
+
+ protected:
+  xr_simmetric h_ = nullptr;
+  int64_t n_ = 0;
+};
+
+struct ImgSimMetric2DNCCCUDA : ImgSimMetric2DCUDA {
+  explicit ImgSimMetric2DNCCCUDA(int device = -1) : ImgSimMetric2DCUDA(XR_SIM_NCC, device) {}
+};
+
+struct ImgSimMetric2DGradNCCCUDA : ImgSimMetric2DCUDA {
+  explicit ImgSimMetric2DGradNCCCUDA(int device = -1) : ImgSimMetric2DCUDA(XR_SIM_GRAD_NCC, device) {}
+  void set_smooth_img_before_sobel_kernel_radius(int32_t r) {
+    check(xr_sm_set_smooth_img_before_sobel_kernel_radius(h_, r));
+  }
+};
+
+struct ImgSimMetric2DPatchGradNCCCUDA : ImgSimMetric2DCUDA {
+  explicit ImgSimMetric2DPatchGradNCCCUDA(int device = -1) : ImgSimMetric2DCUDA(XR_SIM_PATCH_GRAD_NCC, device) {}
+  void set_smooth_img_before_sobel_kernel_radius(int32_t r) {
+    check(xr_sm_set_smooth_img_before_sobel_kernel_radius(h_, r));
+  }
+  void set_patch_radius(int32_t r) { check(xr_sm_set_patch_radius(h_, r)); }
+  void set_patch_stride(int32_t s) { check(xr_sm_set_patch_stride(h_, s)); }
+};
+
+// Intensity2D3DRegi::obj_fn for one object over a population of poses.
+class PopulationObjective {
+ public:
+  PopulationObjective(RayCasterLineIntCUDA& rc, const std::vector<ImgSimMetric2DCUDA*>& metrics, int64_t max_pop,
+                      int32_t vol_idx = 0) {
+    std::vector<xr_simmetric> hs;
+    for (auto* m : metrics) hs.push_back(m->handle());
+    check(xr_obj_create(rc.handle(), vol_idx, (int32_t)hs.size(), hs.data(), max_pop, &h_));
+  }
+  ~PopulationObjective() { xr_obj_destroy(h_); }
+  PopulationObjective(const PopulationObjective&) = delete;
+  PopulationObjective& operator=(const PopulationObjective&) = delete;
+  std::vector<float> operator()(const std::vector<Mat4>& poses) {
+    std::vector<float> out(poses.size());
+    check(xr_obj_eval(h_, (int64_t)poses.size(), poses.empty() ? nullptr : poses[0].data(), out.data()));
+    return out;
+  }
+
+ private:
+  xr_objective h_ = nullptr;
+};
+
+}  // namespace xreg_gb300
+
+#endif

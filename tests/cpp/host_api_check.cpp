@@ -1,0 +1,103 @@
+// Drives the header-only C++ host classes (include/xreg_gb300/xreg_gb300.hpp)
+// the way xReg's Intensity2D3DRegi::setup / obj_fn drive a ray caster and its
+// metrics.  Reads raw inputs written by tests/test_gpu_cpp_host.py, writes the
+// DRRs and similarity values for comparison with the oracle.
+//   usage: host_api_check <dir>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "xreg_gb300/xreg_gb300.hpp"
+
+template <typename T>
+static std::vector<T> read_all(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  f.seekg(0, std::ios::end);
+  const size_t n = (size_t)f.tellg() / sizeof(T);
+  f.seekg(0);
+  std::vector<T> v(n);
+  f.read(reinterpret_cast<char*>(v.data()), (std::streamsize)(n * sizeof(T)));
+  return v;
+}
+
+template <typename T>
+static void write_all(const std::string& path, const std::vector<T>& v) {
+  std::ofstream f(path, std::ios::binary);
+  f.write(reinterpret_cast<const char*>(v.data()), (std::streamsize)(v.size() * sizeof(T)));
+}
+
+int main(int argc, char** argv) {
+  if (argc < 2) return 2;
+  const std::string dir = argv[1];
+  const auto meta = read_all<double>(dir + "/meta.f64");  // nx ny nz sp rows cols px step npose
+  const int64_t nx = (int64_t)meta[0], ny = (int64_t)meta[1], nz = (int64_t)meta[2];
+  const double sp = meta[3];
+  const int64_t rows = (int64_t)meta[4], cols = (int64_t)meta[5];
+  const double px = meta[6];
+  const float step = (float)meta[7];
+  const int64_t npose = (int64_t)meta[8];
+  auto vox = read_all<float>(dir + "/vol.f32");
+  auto poses_raw = read_all<double>(dir + "/poses.f64");
+  auto fixed = read_all<float>(dir + "/fixed.f32");
+  try {
+    using namespace xreg_gb300;
+    Volume vol;
+    vol.desc.n[0] = nx; vol.desc.n[1] = ny; vol.desc.n[2] = nz;
+    for (int i = 0; i < 3; ++i) { vol.desc.spacing[i] = sp; vol.desc.origin[i] = 0.0; }
+    for (int i = 0; i < 9; ++i) vol.desc.direction[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    vol.voxels = vox.data();
+    CameraModel cam;
+    cam.setup(1020.0, rows, cols, px, px);
+    std::vector<Mat4> poses((size_t)npose);
+    for (int64_t p = 0; p < npose; ++p)
+      for (int k = 0; k < 16; ++k) poses[(size_t)p][(size_t)k] = poses_raw[(size_t)(p * 16 + k)];
+
+    // ray caster used directly (RayCaster API)
+    RayCasterLineIntCUDA rc;
+    rc.set_volume(vol);
+    rc.set_camera_model(cam);
+    rc.set_ray_step_size(step);
+    rc.set_num_projs(npose);
+    rc.allocate_resources();
+    rc.use_proj_store_replace_method();
+    rc.distribute_xforms_among_cam_models(poses);
+    rc.compute(0);
+    write_all(dir + "/drr.f32", rc.raw_host_pixel_buf());
+
+    // metric reading the ray caster's buffer in place
+    ImgSimMetric2DGradNCCCUDA m;
+    m.set_fixed_image(fixed.data(), rows, cols);
+    m.set_num_moving_images(npose);
+    m.set_mov_imgs_buf_from_ray_caster(&rc, 0);
+    m.allocate_resources();
+    m.compute();
+    write_all(dir + "/sims.f32", m.sim_vals());
+
+    // the population objective over a second ray caster
+    RayCasterLineIntCUDA rc2;
+    rc2.set_volume(vol);
+    rc2.set_camera_model(cam);
+    rc2.set_ray_step_size(step);
+    ImgSimMetric2DGradNCCCUDA m2;
+    m2.set_fixed_image(fixed.data(), rows, cols);
+    PopulationObjective obj(rc2, {&m2}, npose);
+    write_all(dir + "/obj.f32", obj(poses));
+
+    // error path: unsupported interpolation surfaces as UnsupportedOperationException
+    rc.set_interp_method(XR_INTERP_SINC);
+    try {
+      rc.compute(0);
+      std::cerr << "expected UnsupportedOperationException\n";
+      return 3;
+    } catch (const UnsupportedOperationException&) {
+    }
+  } catch (const std::exception& e) {
+    std::cerr << "error: " << e.what() << "\n";
+    return 1;
+  }
+  std::cout << "ok\n";
+  return 0;
+}

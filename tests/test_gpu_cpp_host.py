@@ -1,0 +1,58 @@
+"""The header-only C++ host classes (include/xreg_gb300/xreg_gb300.hpp) compile
+against the C ABI and give the oracle's results when driven like xReg drives its
+ray caster and metrics."""
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tests.helpers import drr_rel_err, oracle_cams, oracle_geom
+from xreg_gb300 import synth
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _compile(tmp: Path) -> Path:
+    from xreg_gb300.build import LIB_PATH
+    exe = tmp / "host_api_check"
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    subprocess.run([cxx, "-std=c++17", "-O1", f"-I{ROOT / 'include'}", str(ROOT / "tests/cpp/host_api_check.cpp"),
+                    "-o", str(exe), f"-L{LIB_PATH.parent}", "-lxreg_gb300", f"-Wl,-rpath,{LIB_PATH.parent}"],
+                   check=True)
+    return exe
+
+
+def test_cpp_header_compiles(xr, tmp_path):
+    _compile(tmp_path)
+
+
+@pytest.mark.gpu
+def test_cpp_host_classes_match_oracle(xr, oracle, tmp_path):
+    exe = _compile(tmp_path)
+    vol = synth.phantom_volume((36, 40, 32), (2.0, 2.0, 2.0), 4)
+    rows, cols, px, step = 30, 34, 4.0, 0.5
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 4, 6.0, 8.0, seed=3)
+    cam = xr.CameraModel.naive(synth.SDD_MM, rows, cols, px, px)
+    fixed = synth.add_noise(oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]),
+                                           synth.gt_pose(vol)[None], step=step)[0], 0.01, 1)
+    nz, ny, nx = vol.voxels.shape
+    np.array([nx, ny, nz, 2.0, rows, cols, px, step, len(poses)], np.float64).tofile(tmp_path / "meta.f64")
+    vol.voxels.tofile(tmp_path / "vol.f32")
+    poses.astype(np.float64).tofile(tmp_path / "poses.f64")
+    fixed.tofile(tmp_path / "fixed.f32")
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    drr = np.fromfile(tmp_path / "drr.f32", np.float32).reshape(len(poses), rows, cols)
+    sims = np.fromfile(tmp_path / "sims.f32", np.float32)
+    obj = np.fromfile(tmp_path / "obj.f32", np.float32)
+    ref = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=step)
+    rel, zero = drr_rel_err(drr, ref)
+    assert zero == 0.0 and rel <= 1e-4
+    ref_sims = oracle.grad_ncc(fixed, ref)
+    np.testing.assert_allclose(sims, ref_sims, atol=1e-5, rtol=0)
+    np.testing.assert_array_equal(obj, sims)

@@ -105,3 +105,25 @@ def test_population_errors(xr):
     rc2.set_camera_models(cams[:1])
     with pytest.raises(_lib.XRegError):
         xr.PopulationObjective(rc2, ms, 4)  # two metrics, one camera
+
+
+def test_destroy_in_any_order(xr):
+    """Destroying a ray caster before the metric or objective bound to it must not
+    crash; the dependent handles report an error instead."""
+    from xreg_gb300 import _lib
+    lib = _lib.load()
+    vol, cams = _two_view_setup(4)
+    fixed = [np.zeros((48, 52), np.float32)] * 2
+    obj, rc, ms = _objective(xr, vol, cams, fixed, xr.ImgSimMetric2DGradNCCCUDA, 2)
+    poses = np.tile(synth.gt_pose(vol), (2, 1, 1))
+    obj.eval(poses)
+    h_rc = rc.handle
+    assert lib.xr_rc_destroy(h_rc) == 0
+    rc._h = None  # already destroyed through the C ABI
+    with pytest.raises(_lib.XRegError):
+        obj.eval(poses)
+    with pytest.raises(_lib.XRegError):
+        ms[0].compute()
+    obj.close()
+    for m in ms:
+        m.close()

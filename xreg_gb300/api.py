@@ -331,6 +331,7 @@ class ImgSimMetric2DCUDA:
 
     def set_mov_imgs_buf_from_ray_caster(self, rc: RayCasterLineIntCUDA, proj_offset: int = 0) -> None:
         call("xr_sm_set_mov_imgs_buf_from_ray_caster", self._h, rc.handle, int(proj_offset))
+        self._rc_ref = rc  # keep the ray caster alive at least as long as this metric
 
     def set_mov_imgs_device_buf(self, d_ptr: int, proj_offset: int = 0) -> None:
         call("xr_sm_set_mov_imgs_device_buf", self._h, C.c_void_p(int(d_ptr)), int(proj_offset))
@@ -396,6 +397,8 @@ class PopulationObjective:
         self._h = h
         self.rc = rc
         self.metrics = list(metrics)
+        for m in self.metrics:
+            m._rc_ref = rc
         self.max_pop = int(max_pop)
 
     def __del__(self):

@@ -6,7 +6,9 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
+#include <unordered_map>
 #include <string>
 #include <vector>
 
@@ -90,6 +92,33 @@ __global__ void cam_idx_distribute_kernel(int32_t* out, int64_t n, int64_t per_c
   if (i < n) out[i] = (int32_t)(i / per_cam);
 }
 
+// Live-handle registry: handles that refer to other handles (a metric bound to
+// a ray caster, an objective over both) store the peer's id and look it up
+// before every use, so destroying handles in any order never dereferences a
+// freed object.
+std::mutex g_reg_mu;
+std::unordered_map<const void*, uint64_t> g_live;
+uint64_t g_next_id = 1;
+
+uint64_t reg_add(const void* p) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  const uint64_t id = g_next_id++;
+  g_live[p] = id;
+  return id;
+}
+
+void reg_remove(const void* p) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  g_live.erase(p);
+}
+
+bool reg_alive(const void* p, uint64_t id) {
+  if (!p) return false;
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_live.find(p);
+  return it != g_live.end() && it->second == id;
+}
+
 bool finite_all(const double* v, int64_t n) {
   for (int64_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return false;
@@ -103,6 +132,7 @@ using namespace xr;
 
 // ===================================================================== handles
 struct xr_raycaster_s {
+  uint64_t id = 0;
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t ext_stream = nullptr;
@@ -148,6 +178,7 @@ struct xr_raycaster_s {
 };
 
 struct xr_simmetric_s {
+  uint64_t id = 0;
   int32_t kind = XR_SIM_NCC;
   int device = 0;
   cudaStream_t own_stream = nullptr;
@@ -160,7 +191,8 @@ struct xr_simmetric_s {
   DevBuf d_mask;
   bool has_mask = false;
   int64_t num_mov = 0;
-  xr_raycaster rc = nullptr;
+  xr_raycaster rc = nullptr;       // bound ray caster (checked with rc_id before use)
+  uint64_t rc_id = 0;
   const float* mov_dev = nullptr;
   int64_t proj_offset = 0;
   int32_t smooth_ksize = 5;
@@ -177,17 +209,30 @@ struct xr_simmetric_s {
   int ncr = 0, ncc = 0;            // patch centre grid
   uint64_t generation = 1;
 
-  cudaStream_t stream() const {
+  // The bound ray caster if it is still alive; forgets it otherwise.
+  xr_raycaster live_rc() {
+    if (rc && !reg_alive(rc, rc_id)) { rc = nullptr; rc_id = 0; }
+    return rc;
+  }
+  cudaStream_t stream() {
     if (has_ext_stream) return ext_stream;
-    if (rc) return rc->stream();
+    if (xr_raycaster r = live_rc()) return r->stream();
     return own_stream;
   }
 };
 
 struct xr_objective_s {
   xr_raycaster rc = nullptr;
+  uint64_t rc_id = 0;
   int32_t vol_idx = 0;
   std::vector<xr_simmetric> metrics;
+  std::vector<uint64_t> metric_ids;
+  bool peers_alive() const {
+    if (!reg_alive(rc, rc_id)) return false;
+    for (size_t i = 0; i < metrics.size(); ++i)
+      if (!reg_alive(metrics[i], metric_ids[i])) return false;
+    return true;
+  }
   int64_t max_pop = 0;
   DevBuf d_poses, d_sims, d_view_sims_ptrs;
   DevBuf h_pinned_poses;  // unused placeholder for symmetry (host copies use pageable memory)
@@ -268,10 +313,16 @@ extern "C" XR_API xr_status xr_rc_create(int32_t device, xr_raycaster* out) {
   auto* rc = new (std::nothrow) xr_raycaster_s();
   if (!rc) return fail(XR_ERR_OUT_OF_MEMORY, "xr_rc_create: host allocation failed");
   rc->device = dev;
+  rc->id = reg_add(rc);
   cudaError_t e = cudaStreamCreateWithFlags(&rc->own_stream, cudaStreamNonBlocking);
-  if (e != cudaSuccess) { delete rc; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
+  if (e != cudaSuccess) { reg_remove(rc); delete rc; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
   e = rc->d_counters.reserve(64);
-  if (e != cudaSuccess) { cudaStreamDestroy(rc->own_stream); delete rc; return cuda_fail(e, "cudaMalloc"); }
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(rc->own_stream);
+    reg_remove(rc);
+    delete rc;
+    return cuda_fail(e, "cudaMalloc");
+  }
   cudaMemset(rc->d_counters.p, 0, 64);
   *out = rc;
   return XR_OK;
@@ -279,6 +330,7 @@ extern "C" XR_API xr_status xr_rc_create(int32_t device, xr_raycaster* out) {
 
 extern "C" XR_API xr_status xr_rc_destroy(xr_raycaster rc) {
   if (!rc) return XR_OK;
+  reg_remove(rc);
   DeviceGuard g(rc->device);
   cudaStreamSynchronize(rc->stream());
   cudaStreamDestroy(rc->own_stream);
@@ -705,12 +757,14 @@ extern "C" XR_API xr_status xr_sm_create(int32_t kind, int32_t device, xr_simmet
   sm->device = dev;
   cudaError_t e = cudaStreamCreateWithFlags(&sm->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete sm; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
+  sm->id = reg_add(sm);
   *out = sm;
   return XR_OK;
 }
 
 extern "C" XR_API xr_status xr_sm_destroy(xr_simmetric sm) {
   if (!sm) return XR_OK;
+  reg_remove(sm);
   DeviceGuard g(sm->device);
   cudaStreamSynchronize(sm->stream());
   cudaStreamDestroy(sm->own_stream);
@@ -777,6 +831,7 @@ extern "C" XR_API xr_status xr_sm_set_num_moving_images(xr_simmetric sm, int64_t
 extern "C" XR_API xr_status xr_sm_set_mov_imgs_buf_from_ray_caster(xr_simmetric sm, xr_raycaster rc, int64_t off) {
   XR_CHECK_ARG(sm && rc && off >= 0, "set_mov_imgs_buf_from_ray_caster: NULL argument or negative offset");
   sm->rc = rc;
+  sm->rc_id = rc->id;
   sm->mov_dev = nullptr;
   sm->proj_offset = off;
   sm->generation++;
@@ -786,6 +841,7 @@ extern "C" XR_API xr_status xr_sm_set_mov_imgs_buf_from_ray_caster(xr_simmetric 
 extern "C" XR_API xr_status xr_sm_set_mov_imgs_device_buf(xr_simmetric sm, const float* d, int64_t off) {
   XR_CHECK_ARG(sm && d && off >= 0, "set_mov_imgs_device_buf: NULL argument or negative offset");
   sm->rc = nullptr;
+  sm->rc_id = 0;
   sm->mov_dev = d;
   sm->proj_offset = off;
   sm->generation++;
@@ -862,7 +918,7 @@ extern "C" XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm) {
   XR_CHECK_ARG(sm, "allocate_resources: NULL handle");
   XR_CHECK_ARG(sm->has_fixed, "allocate_resources: no fixed image");
   XR_CHECK_ARG(sm->num_mov > 0, "allocate_resources: num_moving_images is 0");
-  XR_CHECK_ARG(sm->rc || sm->mov_dev, "allocate_resources: no moving image buffer");
+  XR_CHECK_ARG(sm->live_rc() || sm->mov_dev, "allocate_resources: no moving image buffer");
   DeviceGuard g(sm->device);
   cudaStream_t s = sm->stream();
   const int64_t n = sm->rows * sm->cols;
@@ -923,14 +979,15 @@ static xr_status sm_enqueue_compute(xr_simmetric sm) {
   if (!sm->allocated) return fail(XR_ERR_NOT_ALLOCATED, "compute: allocate_resources has not been called");
   const int64_t npix = sm->rows * sm->cols;
   const float* mov = nullptr;
-  if (sm->rc) {
-    XR_CHECK_ARG(sm->rc->allocated, "compute: the bound ray caster has no buffer");
-    XR_CHECK_ARG(sm->rc->rows() == sm->rows && sm->rc->cols() == sm->cols,
+  if (xr_raycaster rc = sm->live_rc()) {
+    XR_CHECK_ARG(rc->allocated, "compute: the bound ray caster has no buffer");
+    XR_CHECK_ARG(rc->rows() == sm->rows && rc->cols() == sm->cols,
                  "compute: ray caster image size differs from the fixed image");
-    XR_CHECK_ARG(sm->proj_offset + sm->num_mov <= sm->rc->capacity,
+    XR_CHECK_ARG(sm->proj_offset + sm->num_mov <= rc->capacity,
                  "compute: moving images run past the ray caster's buffer");
-    mov = sm->rc->d_proj.as<float>() + sm->proj_offset * npix;
+    mov = rc->d_proj.as<float>() + sm->proj_offset * npix;
   } else {
+    XR_CHECK_ARG(sm->mov_dev, "compute: no moving image buffer (was the bound ray caster destroyed?)");
     mov = sm->mov_dev + sm->proj_offset * npix;
   }
   cudaStream_t s = sm->stream();
@@ -969,10 +1026,11 @@ extern "C" XR_API xr_status xr_sm_compute(xr_simmetric sm) {
   XR_CHECK_ARG(sm, "compute: NULL handle");
   DeviceGuard g(sm->device);
   // A metric reading a ray caster's buffer on another stream waits for it.
-  if (sm->rc && sm->stream() != sm->rc->stream()) {
+  xr_raycaster brc = sm->live_rc();
+  if (brc && sm->stream() != brc->stream()) {
     cudaEvent_t ev;
     XR_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    cudaEventRecord(ev, sm->rc->stream());
+    cudaEventRecord(ev, brc->stream());
     cudaStreamWaitEvent(sm->stream(), ev, 0);
     cudaEventDestroy(ev);
   }
@@ -984,8 +1042,8 @@ extern "C" XR_API xr_status xr_sm_sim_vals(xr_simmetric sm, float* dst) {
   XR_CHECK_ARG(sm->allocated, "sim_vals: resources not allocated");
   DeviceGuard g(sm->device);
   XR_CUDA_TRY(cudaStreamSynchronize(sm->stream()));
-  if (sm->rc) {
-    xr_status st = xr_rc_synchronize(sm->rc);
+  if (xr_raycaster brc2 = sm->live_rc()) {
+    xr_status st = xr_rc_synchronize(brc2);
     if (st != XR_OK) return st;
   }
   XR_CUDA_TRY(cudaMemcpy(dst, sm->d_sims.p, (size_t)sm->num_mov * 4, cudaMemcpyDeviceToHost));
@@ -1016,8 +1074,10 @@ extern "C" XR_API xr_status xr_obj_create(xr_raycaster rc, int32_t vol_idx, int3
   auto* obj = new (std::nothrow) xr_objective_s();
   if (!obj) return fail(XR_ERR_OUT_OF_MEMORY, "xr_obj_create: host allocation failed");
   obj->rc = rc;
+  obj->rc_id = rc->id;
   obj->vol_idx = vol_idx;
   obj->metrics.assign(ms, ms + nviews);
+  for (int32_t v = 0; v < nviews; ++v) obj->metric_ids.push_back(ms[v]->id);
   obj->max_pop = max_pop;
   std::unique_ptr<xr_objective_s> guard(obj);
   // ray caster: views * max_pop projections, poses distributed over cameras
@@ -1045,9 +1105,15 @@ extern "C" XR_API xr_status xr_obj_create(xr_raycaster rc, int32_t vol_idx, int3
 
 extern "C" XR_API xr_status xr_obj_destroy(xr_objective obj) {
   if (!obj) return XR_OK;
-  DeviceGuard g(obj->rc->device);
-  cudaStreamSynchronize(obj->rc->stream());
-  delete obj;
+  if (reg_alive(obj->rc, obj->rc_id)) {
+    DeviceGuard g(obj->rc->device);
+    cudaStreamSynchronize(obj->rc->stream());
+    delete obj;
+  } else {
+    // the ray caster (and its stream) is gone; wait for all device work instead
+    cudaDeviceSynchronize();
+    delete obj;
+  }
   return XR_OK;
 }
 
@@ -1065,6 +1131,7 @@ static xr_status obj_enqueue(xr_objective obj, int64_t pop) {
     xr_simmetric m = obj->metrics[(size_t)v];
     m->num_mov = pop;
     m->rc = rc;
+    m->rc_id = rc->id;
     m->proj_offset = (int64_t)v * pop;
     if ((st = sm_enqueue_compute(m)) != XR_OK) return st;
     view_sims[v] = m->d_sims.as<float>();
@@ -1115,6 +1182,7 @@ static xr_status obj_run(xr_objective obj, int64_t pop) {
 extern "C" XR_API xr_status xr_obj_eval_device(xr_objective obj, int64_t pop, const double* d_xforms,
                                                float* d_sims) {
   XR_CHECK_ARG(obj && d_xforms && d_sims, "xr_obj_eval_device: NULL argument");
+  XR_CHECK_ARG(obj->peers_alive(), "xr_obj_eval_device: a ray caster or metric of this objective was destroyed");
   XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "xr_obj_eval_device: population outside [1, max_pop]");
   DeviceGuard g(obj->rc->device);
   cudaStream_t s = obj->rc->stream();
@@ -1127,6 +1195,7 @@ extern "C" XR_API xr_status xr_obj_eval_device(xr_objective obj, int64_t pop, co
 
 extern "C" XR_API xr_status xr_obj_eval(xr_objective obj, int64_t pop, const double* h_xforms, float* h_sims) {
   XR_CHECK_ARG(obj && h_xforms && h_sims, "xr_obj_eval: NULL argument");
+  XR_CHECK_ARG(obj->peers_alive(), "xr_obj_eval: a ray caster or metric of this objective was destroyed");
   XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "xr_obj_eval: population outside [1, max_pop]");
   XR_CHECK_ARG(finite_all(h_xforms, 16 * pop), "xr_obj_eval: non-finite transform");
   DeviceGuard g(obj->rc->device);
