@@ -84,6 +84,7 @@ def test_alone_equals_in_the_mix_and_graph_path(xr, oracle):
     # device entry point (captured graph on a non-default stream) agrees with the host one
     d_x = torch.from_numpy(poses.reshape(32, 16).copy()).cuda()
     d_s = torch.empty(32, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
     for _ in range(3):
         with torch.cuda.stream(s):
             obj.eval_device(32, d_x.data_ptr(), d_s.data_ptr())
