@@ -16,6 +16,10 @@ pytestmark = pytest.mark.gpu
 
 TOL32 = 1e-4
 TOL16 = 2e-3
+# BF16 keeps 8 significand bits: a voxel's relative rounding error reaches
+# 2^-8 ~ 3.9e-3, so a ray dominated by a few voxels can exceed 2e-3.  The 2e-3
+# half-precision bound is met by FP16 (2^-11); BF16 is held to its own unit roundoff.
+TOLBF16 = 2.0 ** -8
 
 
 def _rc(xr, vol, cams, step, voxel_type=0):
@@ -80,7 +84,7 @@ def test_two_views_distribute(xr, oracle):
     assert not np.allclose(g[0], g[len(poses)])  # the views differ
 
 
-@pytest.mark.parametrize("vt,tol", [(1, TOL16), (2, TOL16)])
+@pytest.mark.parametrize("vt,tol", [(1, TOL16), (2, TOLBF16)])
 def test_half_precision_volumes(xr, oracle, vt, tol):
     w = synth.plain_small(5)
     pose = synth.fixed_pose(w)

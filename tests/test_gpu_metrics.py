@@ -33,9 +33,9 @@ def _drrs(xr, det=(64, 72), n=6, seed=0, px=2.5):
 
 def _metric(xr, cls, rc, fixed, n, offset=1, **kw):
     m = cls()
+    m.set_fixed_image(fixed)  # a mask needs the fixed image's size first
     for k, v in kw.items():
         getattr(m, k)(v)
-    m.set_fixed_image(fixed)
     m.set_num_moving_images(n)
     m.set_mov_imgs_buf_from_ray_caster(rc, offset)
     m.allocate_resources()
