@@ -81,6 +81,10 @@ enum { XR_LINE_INT_SUM = 0, XR_LINE_INT_MAX = 1 };          /* RayCastLineIntKer
 enum { XR_PROJ_STORE_REPLACE = 0, XR_PROJ_STORE_ACCUM = 1 }; /* ProjPixelStoreMethod */
 enum { XR_INTERP_LINEAR = 0, XR_INTERP_NN = 1, XR_INTERP_SINC = 2, XR_INTERP_BSPLINE = 3 };
 enum { XR_CAM_FOCAL_POS_Z = 0, XR_CAM_FOCAL_NEG_Z = 1, XR_CAM_ON_DETECTOR = 2 };
+/* Device layouts of a volume (results are identical; speed differs):
+ * LINEAR = voxels x-fastest; CELL8 = the 8 corners of every trilinear cell stored
+ * together (8x the voxel bytes, one or two vector loads per sample). */
+enum { XR_LAYOUT_AUTO = -1, XR_LAYOUT_LINEAR = 0, XR_LAYOUT_CELL8 = 1 };
 
 /* ------------------------------------------------------- camera helpers -- */
 /* CameraModel::setup(focal_len, nr, nc, rs, cs) with MakeNaiveIntrins
@@ -165,6 +169,17 @@ XR_API xr_status xr_rc_device_pixel_buf(xr_raycaster rc, float** out);
 XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* out);
 /* Enables (1) or disables (0) per-compute sample counting (default off). */
 XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
+/* Launch configuration of the DRR kernel: volume layout (XR_LAYOUT_*), warps
+ * across a 256-thread block (1, 2, 4 or 8; each warp covers 8x4 pixels) and
+ * samples per loop iteration (1 or 2).  layout XR_LAYOUT_AUTO (the default) lets
+ * the autotuner time the candidates on the first compute of each shape (volume
+ * size, voxel type, detector, projection count) and cache the fastest for the
+ * process.  No xReg counterpart (xReg's OpenCL caster has a fixed NDRange). */
+XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t layout, int32_t block_warps_x, int32_t unroll);
+/* The configuration the last compute used. */
+XR_API xr_status xr_rc_get_launch_config(xr_raycaster rc, int32_t* layout, int32_t* block_warps_x, int32_t* unroll);
+/* Whether set_volumes also builds the CELL8 copy (default 1).  Set before set_volumes. */
+XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable);
 
 /* ------------------------------------------------------ similarity metric -- */
 /* Replaces ImgSimMetric2D{NCC,GradNCC,PatchNCC,PatchGradNCC}{CPU,OCL}

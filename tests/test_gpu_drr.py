@@ -203,3 +203,47 @@ def test_errors_are_reported(xr):
         rc.set_num_projs(2)  # beyond what allocate_resources reserved
     rc.compute()
     assert rc.proj(0).shape == (4, 4)
+
+
+@pytest.mark.parametrize("vt", [0, 1, 2])
+def test_launch_configs_are_bit_identical(xr, oracle, vt):
+    """Every layout / block shape / unroll gives the same bits; the autotuned
+    configuration is one of them and matches the oracle."""
+    vol = small_volume(9, (40, 36, 44), (1.5, 1.5, 1.5))
+    cam = small_camera((36, 40), 3.0)
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 3, 10.0, 10.0, seed=6)
+    rc = _rc(xr, vol, [cam], 0.5, vt)
+    rc.set_num_projs(3)
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(poses)
+    rc.compute()
+    auto = rc.projs()
+    lay, bw, un = rc.launch_config()
+    assert lay in (0, 1) and bw in (1, 2, 4) and un in (1, 2)
+    for layout in (0, 1):
+        for bw in (1, 2, 4, 8):
+            for un in (1, 2):
+                rc.set_launch_config(layout, bw, un)
+                rc.compute()
+                assert rc.launch_config() == (layout, bw, un)
+                np.testing.assert_array_equal(rc.projs(), auto)
+    o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=0.5)
+    rel, zero = drr_rel_err(auto, o)
+    assert zero == 0.0 and rel <= (TOL32 if vt == 0 else (TOL16 if vt == 1 else TOLBF16))
+
+
+def test_cell_layout_can_be_disabled(xr):
+    from xreg_gb300 import _lib
+    vol = small_volume(10, (16, 16, 16))
+    rc = xr.RayCasterLineIntCUDA()
+    rc.set_build_cell_layout(False)
+    rc.set_volume(vol)
+    rc.set_camera_model(small_camera((8, 8), 8.0))
+    rc.set_num_projs(1)
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(synth.gt_pose(vol)[None])
+    rc.compute()
+    assert rc.launch_config()[0] == 0
+    rc.set_launch_config(1, 2, 1)
+    with pytest.raises(_lib.XRegError):
+        rc.compute()

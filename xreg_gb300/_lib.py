@@ -24,6 +24,7 @@ XR_LINE_INT_SUM, XR_LINE_INT_MAX = 0, 1
 XR_PROJ_STORE_REPLACE, XR_PROJ_STORE_ACCUM = 0, 1
 XR_INTERP_LINEAR, XR_INTERP_NN, XR_INTERP_SINC, XR_INTERP_BSPLINE = 0, 1, 2, 3
 XR_CAM_FOCAL_POS_Z, XR_CAM_FOCAL_NEG_Z, XR_CAM_ON_DETECTOR = 0, 1, 2
+XR_LAYOUT_AUTO, XR_LAYOUT_LINEAR, XR_LAYOUT_CELL8 = -1, 0, 1
 XR_SIM_NCC, XR_SIM_GRAD_NCC, XR_SIM_PATCH_NCC, XR_SIM_PATCH_GRAD_NCC = 0, 1, 2, 3
 
 
@@ -84,6 +85,9 @@ _SIGS = {
     "xr_rc_device_pixel_buf": [H, C.POINTER(P)],
     "xr_rc_last_num_samples": [H, C.POINTER(u64)],
     "xr_rc_set_count_samples": [H, i32],
+    "xr_rc_set_launch_config": [H, i32, i32, i32],
+    "xr_rc_get_launch_config": [H, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],
+    "xr_rc_set_build_cell_layout": [H, i32],
     "xr_sm_create": [i32, i32, C.POINTER(H)],
     "xr_sm_destroy": [H],
     "xr_sm_set_stream": [H, P],

@@ -249,6 +249,17 @@ class RayCasterLineIntCUDA:
     def set_count_samples(self, enable: bool) -> None:
         call("xr_rc_set_count_samples", self._h, int(bool(enable)))
 
+    def set_launch_config(self, layout: int = L.XR_LAYOUT_AUTO, block_warps_x: int = 2, unroll: int = 1) -> None:
+        call("xr_rc_set_launch_config", self._h, int(layout), int(block_warps_x), int(unroll))
+
+    def launch_config(self) -> tuple:
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        call("xr_rc_get_launch_config", self._h, C.byref(a), C.byref(b), C.byref(c))
+        return (a.value, b.value, c.value)
+
+    def set_build_cell_layout(self, enable: bool) -> None:
+        call("xr_rc_set_build_cell_layout", self._h, int(bool(enable)))
+
     def compute(self, vol_idx: int = 0) -> None:
         call("xr_rc_compute", self._h, int(vol_idx))
 

@@ -141,9 +141,13 @@ struct xr_raycaster_s {
   struct Vol {
     xr_volume_desc desc;
     DevBuf voxels;
+    DevBuf cells;            // CELL8 copy (empty when not built)
     int32_t type = XR_VOXEL_F32;
     float inv_scale = 1.0f;
   };
+  bool build_cells = true;
+  int32_t cfg_layout = XR_LAYOUT_AUTO, cfg_bw = 2, cfg_unroll = 1;   // requested
+  int32_t last_layout = -1, last_bw = 0, last_unroll = 0;            // used by the last compute
   std::vector<std::unique_ptr<Vol>> vols;
   std::vector<xr_camera_desc> cams;
   DevBuf d_cams;
@@ -385,6 +389,11 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
       XR_CUDA_TRY(cudaMemcpyAsync(v->voxels.p, voxels[i], (size_t)nv * 4,
                                   on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
       v->inv_scale = 1.0f;
+      if (rc->build_cells) {
+        XR_CUDA_TRY(v->cells.reserve(cell_layout_bytes(d.n[0], d.n[1], d.n[2], vt)));
+        XR_CUDA_TRY(launch_build_cells(v->voxels.as<float>(), (int)d.n[0], (int)d.n[1], (int)d.n[2], vt, 1.0f,
+                                       v->cells.p, s));
+      }
     } else {
       DevBuf tmp;
       const float* src = voxels[i];
@@ -415,6 +424,10 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
       v->inv_scale = 1.0f / sc;
       convert_voxels_kernel<<<2048, 256, 0, s>>>(src, nv, sc, vt, v->voxels.p);
       XR_CUDA_TRY(cudaGetLastError());
+      if (rc->build_cells) {
+        XR_CUDA_TRY(v->cells.reserve(cell_layout_bytes(d.n[0], d.n[1], d.n[2], vt)));
+        XR_CUDA_TRY(launch_build_cells(src, (int)d.n[0], (int)d.n[1], (int)d.n[2], vt, sc, v->cells.p, s));
+      }
       XR_CUDA_TRY(cudaStreamSynchronize(s));  // tmp is released at scope exit
     }
     vols.push_back(std::move(v));
@@ -608,6 +621,119 @@ extern "C" XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t ena
   return XR_OK;
 }
 
+// ------------------------------------------------------------- autotuner
+// Candidates differ only in speed (layout, block shape, unroll give bit-identical
+// results), so the fastest measured one is cached per shape for the process.
+namespace {
+struct TuneKey {
+  int64_t nx, ny, nz, rows, cols, projs_pow2;
+  int32_t vt, kernel, has_cells;
+  bool operator==(const TuneKey& o) const {
+    return nx == o.nx && ny == o.ny && nz == o.nz && rows == o.rows && cols == o.cols &&
+           projs_pow2 == o.projs_pow2 && vt == o.vt && kernel == o.kernel && has_cells == o.has_cells;
+  }
+};
+struct TuneKeyHash {
+  size_t operator()(const TuneKey& k) const {
+    size_t h = 1469598103934665603ull;
+    const int64_t v[9] = {k.nx, k.ny, k.nz, k.rows, k.cols, k.projs_pow2, k.vt, k.kernel, k.has_cells};
+    for (int64_t x : v) h = (h ^ (size_t)x) * 1099511628211ull;
+    return h;
+  }
+};
+struct TuneCfg {
+  int32_t layout, bw, unroll;
+  float ms;
+};
+std::mutex g_tune_mu;
+std::unordered_map<TuneKey, TuneCfg, TuneKeyHash> g_tune;
+
+int64_t pow2_bucket(int64_t n) {
+  int64_t b = 1;
+  while (b < n) b <<= 1;
+  return b;
+}
+
+xr_status time_config(DrrParams p, cudaStream_t s, float* ms_out) {
+  cudaEvent_t a, b;
+  XR_CUDA_TRY(cudaEventCreate(&a));
+  XR_CUDA_TRY(cudaEventCreate(&b));
+  cudaError_t e = launch_drr(p, s);  // warm-up
+  if (e == cudaSuccess) e = cudaEventRecord(a, s);
+  for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch_drr(p, s);
+  if (e == cudaSuccess) e = cudaEventRecord(b, s);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (e != cudaSuccess) return cuda_fail(e, "autotune launch");
+  *ms_out = ms * 0.5f;
+  return XR_OK;
+}
+}  // namespace
+
+// Picks the launch configuration for p (layout, block_warps_x, unroll).
+static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vol, DrrParams& p, cudaStream_t s) {
+  const bool has_cells = vol.cells.p != nullptr;
+  if (rc->cfg_layout != XR_LAYOUT_AUTO) {
+    if (rc->cfg_layout == XR_LAYOUT_CELL8 && !has_cells)
+      return fail(XR_ERR_INVALID_ARG, "compute: CELL8 layout requested but the volume has no cell copy");
+    p.vol.layout = rc->cfg_layout;
+    p.block_warps_x = rc->cfg_bw;
+    p.unroll = rc->cfg_unroll;
+    return XR_OK;
+  }
+  const TuneKey key{vol.desc.n[0], vol.desc.n[1], vol.desc.n[2], rc->rows(), rc->cols(), pow2_bucket(p.num_projs),
+                    vol.type, p.kernel_id, has_cells ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      p.vol.layout = it->second.layout;
+      p.block_warps_x = it->second.bw;
+      p.unroll = it->second.unroll;
+      return XR_OK;
+    }
+  }
+  // default when tuning is not possible right now
+  p.vol.layout = has_cells ? XR_LAYOUT_CELL8 : XR_LAYOUT_LINEAR;
+  p.block_warps_x = 2;
+  p.unroll = 1;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  XR_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+  // Tuning re-runs the kernel; it needs a stream that is not being captured and an
+  // output that the final launch overwrites (replace mode, no background images).
+  if (cap != cudaStreamCaptureStatusNone || p.store != XR_PROJ_STORE_REPLACE || p.bg_projs) return XR_OK;
+  DrrParams t = p;
+  t.sample_counter = nullptr;
+  TuneCfg best{p.vol.layout, p.block_warps_x, p.unroll, 1e30f};
+  const int32_t layouts[2] = {XR_LAYOUT_LINEAR, XR_LAYOUT_CELL8};
+  const int32_t bws[3] = {1, 2, 4};
+  const int32_t unrolls[2] = {1, 2};
+  for (int32_t lay : layouts) {
+    if (lay == XR_LAYOUT_CELL8 && !has_cells) continue;
+    for (int32_t bw : bws)
+      for (int32_t un : unrolls) {
+        t.vol.layout = lay;
+        t.block_warps_x = bw;
+        t.unroll = un;
+        float ms = 0.0f;
+        xr_status st = time_config(t, s, &ms);
+        if (st != XR_OK) return st;
+        if (ms < best.ms) best = TuneCfg{lay, bw, un, ms};
+      }
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = best;
+  }
+  p.vol.layout = best.layout;
+  p.block_warps_x = best.bw;
+  p.unroll = best.unroll;
+  return XR_OK;
+}
+
 // Uploads dirty host state and enqueues geometry + DRR kernels on the stream.
 static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
   XR_CHECK_ARG(rc, "compute: NULL handle");
@@ -639,6 +765,7 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
                                rc->d_cam_idx.as<int32_t>(), n, rc->pose_count, rc->d_geo.as<ProjGeom>(), s));
   DrrParams p{};
   p.vol.voxels = vol.voxels.p;
+  p.vol.cells = vol.cells.p;
   p.vol.nx = (int32_t)vol.desc.n[0];
   p.vol.ny = (int32_t)vol.desc.n[1];
   p.vol.nz = (int32_t)vol.desc.n[2];
@@ -655,7 +782,8 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
     // spacing; 64x margin covers scaled (non-rigid) poses.
     const double dx = (double)(vol.desc.n[0] - 1), dy = (double)(vol.desc.n[1] - 1), dz = (double)(vol.desc.n[2] - 1);
     const double sp = std::fmax(vol.desc.spacing[0], std::fmax(vol.desc.spacing[1], vol.desc.spacing[2]));
-    p.max_steps = (unsigned long long)(64.0 * std::sqrt(dx * dx + dy * dy + dz * dz) * sp / (double)rc->step) + 64;
+    const double ms = 64.0 * std::sqrt(dx * dx + dy * dy + dz * dz) * sp / (double)rc->step + 64.0;
+    p.max_steps = (unsigned long long)std::fmin(ms, 2147483647.0);
   }
   p.num_projs = n;
   p.rows = (int32_t)rc->rows();
@@ -664,7 +792,39 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
   p.default_bg = rc->default_bg;
   p.kernel_id = rc->kernel_id;
   p.store = rc->store;
+  xr_status st = rc_choose_config(rc, vol, p, s);
+  if (st != XR_OK) return st;
+  rc->last_layout = p.vol.layout;
+  rc->last_bw = p.block_warps_x;
+  rc->last_unroll = p.unroll;
   XR_CUDA_TRY(launch_drr(p, s));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t layout, int32_t bw, int32_t unroll) {
+  XR_CHECK_ARG(rc, "set_launch_config: NULL handle");
+  XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= XR_LAYOUT_CELL8, "set_launch_config: bad layout");
+  XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || bw == 1 || bw == 2 || bw == 4 || bw == 8,
+               "set_launch_config: block_warps_x must be 1, 2, 4 or 8");
+  XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || unroll == 1 || unroll == 2, "set_launch_config: unroll must be 1 or 2");
+  rc->cfg_layout = layout;
+  rc->cfg_bw = bw;
+  rc->cfg_unroll = unroll;
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_get_launch_config(xr_raycaster rc, int32_t* layout, int32_t* bw, int32_t* unroll) {
+  XR_CHECK_ARG(rc && layout && bw && unroll, "get_launch_config: NULL argument");
+  *layout = rc->last_layout;
+  *bw = rc->last_bw;
+  *unroll = rc->last_unroll;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable) {
+  XR_CHECK_ARG(rc, "set_build_cell_layout: NULL handle");
+  rc->build_cells = enable != 0;
   return XR_OK;
 }
 

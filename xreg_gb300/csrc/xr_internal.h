@@ -31,8 +31,10 @@ static_assert(sizeof(ProjGeom) == 96, "ProjGeom layout");
 // Volume as the kernels see it.
 struct VolView {
   const void* voxels;  // F32 / F16 / BF16, x fastest
+  const void* cells;   // CELL8 layout: 8 corners per trilinear cell (or nullptr)
   int32_t nx, ny, nz;
   int32_t voxel_type;
+  int32_t layout;      // XR_LAYOUT_LINEAR / XR_LAYOUT_CELL8
   float inv_scale;     // multiplies the ray sum (1 for F32)
 };
 
@@ -52,6 +54,8 @@ struct DrrParams {
   float default_bg;
   int32_t kernel_id;      // XR_LINE_INT_SUM / MAX
   int32_t store;          // XR_PROJ_STORE_REPLACE / ACCUM
+  int32_t block_warps_x;  // warps across a block (1, 2, 4, 8); 8x4-pixel warps
+  int32_t unroll;         // samples per loop iteration (1 or 2)
 };
 
 // ---- launchers (xr_geom.cu) ----
@@ -63,6 +67,10 @@ cudaError_t launch_proj_geom(const xr_volume_desc& vol, const xr_camera_desc* d_
 
 // ---- launchers (xr_raycast.cu) ----
 cudaError_t launch_drr(const DrrParams& p, cudaStream_t s);
+// Bytes of the CELL8 copy of a volume, and the kernel that builds it from float32 voxels.
+size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type);
+cudaError_t launch_build_cells(const float* vox_f32, int nx, int ny, int nz, int32_t voxel_type, float scale,
+                               void* out, cudaStream_t s);
 
 // ---- launchers (xr_metrics.cu) ----
 struct FixedNCC {           // per direction (one for NCC, x and y for grad-NCC)

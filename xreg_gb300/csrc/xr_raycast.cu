@@ -15,8 +15,16 @@
 //
 // The per-ray geometry (direction, slab test, nudge, step count, start point,
 // step vector) uses explicitly rounded float intrinsics in the same order as the
-// CPU oracle, so sample counts are bit-identical.  The interpolation and the sum
-// use ordinary float arithmetic (FMA allowed).
+// CPU oracle, so sample counts and sample positions are bit-identical.  The
+// interpolation and the sum use ordinary float arithmetic.
+//
+// Volume layouts (same values, same arithmetic, bit-identical results):
+//   LINEAR  voxels x-fastest; a sample issues 8 scalar loads.
+//   CELL8   for every trilinear cell (ix, iy, iz) in [0, n-2]^3 the 8 corner
+//           values are stored contiguously (v000 v100 v010 v110 v001 v101 v011
+//           v111): one 16-byte load per sample for FP16/BF16, two for FP32.
+//           It spends 8x the voxel bytes of HBM to cut L1 requests per sample
+//           from 8 to 1-2; the linear kernel is bound by exactly those requests.
 #include "xr_internal.h"
 
 #include <cfloat>
@@ -31,11 +39,26 @@ struct Vox<XR_VOXEL_F32> {
   __device__ __forceinline__ static float ld(const void* b, int i) {
     return __ldg(static_cast<const float*>(b) + i);
   }
+  // 8 corners of cell c (CELL8 layout)
+  __device__ __forceinline__ static void cell(const void* b, int c, float v[8]) {
+    const float4* p = static_cast<const float4*>(b) + 2 * (size_t)c;
+    const float4 lo = __ldg(p), hi = __ldg(p + 1);
+    v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
+    v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
+  }
 };
 template <>
 struct Vox<XR_VOXEL_F16> {
   __device__ __forceinline__ static float ld(const void* b, int i) {
     return __half2float(__ldg(static_cast<const __half*>(b) + i));
+  }
+  __device__ __forceinline__ static void cell(const void* b, int c, float v[8]) {
+    const uint4 q = __ldg(static_cast<const uint4*>(b) + c);
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+    const float2 bb = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
+    const float2 cc = __half22float2(*reinterpret_cast<const __half2*>(&q.z));
+    const float2 d = __half22float2(*reinterpret_cast<const __half2*>(&q.w));
+    v[0] = a.x; v[1] = a.y; v[2] = bb.x; v[3] = bb.y; v[4] = cc.x; v[5] = cc.y; v[6] = d.x; v[7] = d.y;
   }
 };
 template <>
@@ -43,19 +66,67 @@ struct Vox<XR_VOXEL_BF16> {
   __device__ __forceinline__ static float ld(const void* b, int i) {
     return __bfloat162float(__ldg(static_cast<const __nv_bfloat16*>(b) + i));
   }
+  __device__ __forceinline__ static void cell(const void* b, int c, float v[8]) {
+    const uint4 q = __ldg(static_cast<const uint4*>(b) + c);
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.x));
+    const float2 bb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.y));
+    const float2 cc = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.z));
+    const float2 d = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.w));
+    v[0] = a.x; v[1] = a.y; v[2] = bb.x; v[3] = bb.y; v[4] = cc.x; v[5] = cc.y; v[6] = d.x; v[7] = d.y;
+  }
 };
 
-constexpr int kTileX = 16;
-constexpr int kTileY = 16;
 constexpr int kThreads = 256;
 
-template <int VT, int KERNEL>
+// Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
+// the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
+// the last index gets weight 0 (weight 1 on the last voxel).  The weighted form
+// w0*a + w1*b keeps every term >= 0 for non-negative attenuation, so the
+// relative error stays at a few ulps even where the value is tiny.
+template <int VT, int LAYOUT>
+__device__ __forceinline__ float sample(const VolView& vol, const void* data, float px, float py, float pz,
+                                        float bx, float by, float bz) {
+  const int nx = vol.nx, ny = vol.ny;
+  const float x = fminf(fmaxf(px, 0.0f), bx);
+  const float y = fminf(fmaxf(py, 0.0f), by);
+  const float z = fminf(fmaxf(pz, 0.0f), bz);
+  const int ix = min(__float2int_rd(x), nx - 2);
+  const int iy = min(__float2int_rd(y), ny - 2);
+  const int iz = min(__float2int_rd(z), vol.nz - 2);
+  const float fx = x - (float)ix, fy = y - (float)iy, fz = z - (float)iz;
+  float v[8];
+  if (LAYOUT == XR_LAYOUT_CELL8) {
+    Vox<VT>::cell(data, (iz * (ny - 1) + iy) * (nx - 1) + ix, v);
+  } else {
+    const int sy = nx, sz = nx * ny;
+    const int b = (iz * ny + iy) * nx + ix;
+    v[0] = Vox<VT>::ld(data, b);
+    v[1] = Vox<VT>::ld(data, b + 1);
+    v[2] = Vox<VT>::ld(data, b + sy);
+    v[3] = Vox<VT>::ld(data, b + sy + 1);
+    v[4] = Vox<VT>::ld(data, b + sz);
+    v[5] = Vox<VT>::ld(data, b + sz + 1);
+    v[6] = Vox<VT>::ld(data, b + sz + sy);
+    v[7] = Vox<VT>::ld(data, b + sz + sy + 1);
+  }
+  const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+  const float a00 = fmaf(v[1], fx, v[0] * gx);
+  const float a10 = fmaf(v[3], fx, v[2] * gx);
+  const float a01 = fmaf(v[5], fx, v[4] * gx);
+  const float a11 = fmaf(v[7], fx, v[6] * gx);
+  const float b0 = fmaf(a10, fy, a00 * gy);
+  const float b1 = fmaf(a11, fy, a01 * gy);
+  return fmaf(b1, fz, b0 * gz);
+}
+
+template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 __global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const int64_t proj_base) {
-  // 16 x 16 pixels per block; each warp covers an 8 x 4 patch so the 32 rays of
-  // a warp stay close together inside the volume.
+  // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
+  // the volume; a block is bw x (8 / bw) warps.
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int col = blockIdx.x * kTileX + (warp & 1) * 8 + (lane & 7);
-  const int row = blockIdx.y * kTileY + (warp >> 1) * 4 + (lane >> 3);
+  const int bw = p.block_warps_x;
+  const int col = blockIdx.x * (8 * bw) + (warp % bw) * 8 + (lane & 7);
+  const int row = blockIdx.y * (32 / bw) + (warp / bw) * 4 + (lane >> 3);
   const int64_t proj = proj_base + blockIdx.z;
   const bool active = (col < p.cols) && (row < p.rows);
 
@@ -109,42 +180,31 @@ __global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const 
       }
       const float sc = __fdiv_rn(p.step, lc);
       const float sx = __fmul_rn(dir[0], sc), sy = __fmul_rn(dir[1], sc), sz = __fmul_rn(dir[2], sc);
-
-      const int nx = p.vol.nx, ny = p.vol.ny, nz = p.vol.nz;
-      const int sy_ = nx, sz_ = nx * ny;
+      const void* data = (LAYOUT == XR_LAYOUT_CELL8) ? p.vol.cells : p.vol.voxels;
       const float bx = maxb[0], by = maxb[1], bz = maxb[2];
-      const void* vox = p.vol.voxels;
-      for (unsigned long long s = 0; hit && s <= nsteps; ++s) {
-        const float x = fminf(fmaxf(px, 0.0f), bx);
-        const float y = fminf(fmaxf(py, 0.0f), by);
-        const float z = fminf(fmaxf(pz, 0.0f), bz);
-        const int ix = min(__float2int_rd(x), nx - 2);
-        const int iy = min(__float2int_rd(y), ny - 2);
-        const int iz = min(__float2int_rd(z), nz - 2);
-        const float fx = x - (float)ix, fy = y - (float)iy, fz = z - (float)iz;
-        const int b = (iz * ny + iy) * nx + ix;
-        const float v000 = Vox<VT>::ld(vox, b), v100 = Vox<VT>::ld(vox, b + 1);
-        const float v010 = Vox<VT>::ld(vox, b + sy_), v110 = Vox<VT>::ld(vox, b + sy_ + 1);
-        const float v001 = Vox<VT>::ld(vox, b + sz_), v101 = Vox<VT>::ld(vox, b + sz_ + 1);
-        const float v011 = Vox<VT>::ld(vox, b + sz_ + sy_), v111 = Vox<VT>::ld(vox, b + sz_ + sy_ + 1);
-        // Weighted form w0*a + w1*b rather than a + (b - a)*w: with non-negative
-        // attenuation every term is >= 0, so the relative error stays at a few
-        // ulps even where a ray grazes the body edge and the value is tiny.
-        const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-        const float a00 = fmaf(v100, fx, v000 * gx);
-        const float a10 = fmaf(v110, fx, v010 * gx);
-        const float a01 = fmaf(v101, fx, v001 * gx);
-        const float a11 = fmaf(v111, fx, v011 * gx);
-        const float b0 = fmaf(a10, fy, a00 * gy);
-        const float b1 = fmaf(a11, fy, a01 * gy);
-        const float val = fmaf(b1, fz, b0 * gz);
-        if (KERNEL == XR_LINE_INT_MAX) sum = (sum < val) ? val : sum;
-        else sum = __fadd_rn(sum, val);
-        px = __fadd_rn(px, sx);
-        py = __fadd_rn(py, sy);
-        pz = __fadd_rn(pz, sz);
-      }
       if (hit) {
+        // samples 0..nsteps in order; the sum order never changes with UNROLL
+        unsigned int n = (unsigned int)nsteps + 1u;
+        if (UNROLL == 2) {
+          for (; n >= 2; n -= 2) {
+            const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            const float v1 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            if (KERNEL == XR_LINE_INT_MAX) {
+              sum = (sum < v0) ? v0 : sum;
+              sum = (sum < v1) ? v1 : sum;
+            } else {
+              sum = __fadd_rn(__fadd_rn(sum, v0), v1);
+            }
+          }
+        }
+        for (; n > 0; --n) {
+          const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+          if (KERNEL == XR_LINE_INT_MAX) sum = (sum < v0) ? v0 : sum;
+          else sum = __fadd_rn(sum, v0);
+        }
         sum = __fmul_rn(sum, p.step);
         if (VT != XR_VOXEL_F32) sum = __fmul_rn(sum, p.vol.inv_scale);
         ns = nsteps + 1;
@@ -167,33 +227,94 @@ __global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const 
   }
 }
 
-template <int VT, int KERNEL>
+template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
-  const dim3 block(kThreads);
+  const int bw = p.block_warps_x;
+  const int tx = 8 * bw, ty = 32 / bw;
   const int64_t max_z = 65535;
   for (int64_t base = 0; base < p.num_projs; base += max_z) {
     const int64_t n = (p.num_projs - base) < max_z ? (p.num_projs - base) : max_z;
-    const dim3 grid((p.cols + kTileX - 1) / kTileX, (p.rows + kTileY - 1) / kTileY, (unsigned)n);
-    drr_kernel<VT, KERNEL><<<grid, block, 0, s>>>(p, base);
+    const dim3 grid((p.cols + tx - 1) / tx, (p.rows + ty - 1) / ty, (unsigned)n);
+    drr_kernel<VT, KERNEL, LAYOUT, UNROLL><<<grid, kThreads, 0, s>>>(p, base);
   }
   return cudaGetLastError();
+}
+
+template <int VT, int KERNEL>
+cudaError_t launch_layout(const DrrParams& p, cudaStream_t s) {
+  const bool cell = p.vol.layout == XR_LAYOUT_CELL8;
+  if (cell) return p.unroll == 2 ? launch_t<VT, KERNEL, XR_LAYOUT_CELL8, 2>(p, s)
+                                 : launch_t<VT, KERNEL, XR_LAYOUT_CELL8, 1>(p, s);
+  return p.unroll == 2 ? launch_t<VT, KERNEL, XR_LAYOUT_LINEAR, 2>(p, s)
+                       : launch_t<VT, KERNEL, XR_LAYOUT_LINEAR, 1>(p, s);
+}
+
+template <int VT>
+cudaError_t launch_kernel_id(const DrrParams& p, cudaStream_t s) {
+  return p.kernel_id == XR_LINE_INT_MAX ? launch_layout<VT, XR_LINE_INT_MAX>(p, s)
+                                        : launch_layout<VT, XR_LINE_INT_SUM>(p, s);
+}
+
+// One thread per cell: gathers the 8 corners from the float32 voxels.
+template <int VT>
+__global__ void build_cells_kernel(const float* __restrict__ vox, int nx, int ny, int nz, float scale, void* out) {
+  const int64_t ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+  const int64_t ncell = ncx * ncy * ncz;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ix = c % ncx, iy = (c / ncx) % ncy, iz = c / (ncx * ncy);
+    const int64_t b = (iz * ny + iy) * nx + ix, sy = nx, sz = (int64_t)nx * ny;
+    const float v[8] = {vox[b], vox[b + 1], vox[b + sy], vox[b + sy + 1],
+                        vox[b + sz], vox[b + sz + 1], vox[b + sz + sy], vox[b + sz + sy + 1]};
+    if (VT == XR_VOXEL_F32) {
+      float4* o = static_cast<float4*>(out) + 2 * c;
+      o[0] = make_float4(v[0], v[1], v[2], v[3]);
+      o[1] = make_float4(v[4], v[5], v[6], v[7]);
+    } else {
+      uint4 q;
+      unsigned int* w = &q.x;
+      for (int k = 0; k < 4; ++k) {
+        if (VT == XR_VOXEL_F16) {
+          __half2 h = __floats2half2_rn(v[2 * k] * scale, v[2 * k + 1] * scale);
+          w[k] = *reinterpret_cast<unsigned int*>(&h);
+        } else {
+          __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k] * scale, v[2 * k + 1] * scale);
+          w[k] = *reinterpret_cast<unsigned int*>(&h);
+        }
+      }
+      static_cast<uint4*>(out)[c] = q;
+    }
+  }
 }
 
 }  // namespace
 
 cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
   if (p.num_projs <= 0) return cudaSuccess;
-  const bool mx = p.kernel_id == XR_LINE_INT_MAX;
+  if (!(p.block_warps_x == 1 || p.block_warps_x == 2 || p.block_warps_x == 4 || p.block_warps_x == 8))
+    return cudaErrorInvalidValue;
+  if (p.vol.layout == XR_LAYOUT_CELL8 && !p.vol.cells) return cudaErrorInvalidValue;
   switch (p.vol.voxel_type) {
-    case XR_VOXEL_F32:
-      return mx ? launch_t<XR_VOXEL_F32, XR_LINE_INT_MAX>(p, s) : launch_t<XR_VOXEL_F32, XR_LINE_INT_SUM>(p, s);
-    case XR_VOXEL_F16:
-      return mx ? launch_t<XR_VOXEL_F16, XR_LINE_INT_MAX>(p, s) : launch_t<XR_VOXEL_F16, XR_LINE_INT_SUM>(p, s);
-    case XR_VOXEL_BF16:
-      return mx ? launch_t<XR_VOXEL_BF16, XR_LINE_INT_MAX>(p, s) : launch_t<XR_VOXEL_BF16, XR_LINE_INT_SUM>(p, s);
-    default:
-      return cudaErrorInvalidValue;
+    case XR_VOXEL_F32: return launch_kernel_id<XR_VOXEL_F32>(p, s);
+    case XR_VOXEL_F16: return launch_kernel_id<XR_VOXEL_F16>(p, s);
+    case XR_VOXEL_BF16: return launch_kernel_id<XR_VOXEL_BF16>(p, s);
+    default: return cudaErrorInvalidValue;
   }
+}
+
+size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type) {
+  const size_t ncell = (size_t)(nx - 1) * (size_t)(ny - 1) * (size_t)(nz - 1);
+  return ncell * (voxel_type == XR_VOXEL_F32 ? 32 : 16);
+}
+
+cudaError_t launch_build_cells(const float* vox_f32, int nx, int ny, int nz, int32_t voxel_type, float scale,
+                               void* out, cudaStream_t s) {
+  switch (voxel_type) {
+    case XR_VOXEL_F32: build_cells_kernel<XR_VOXEL_F32><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, 1.0f, out); break;
+    case XR_VOXEL_F16: build_cells_kernel<XR_VOXEL_F16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, out); break;
+    case XR_VOXEL_BF16: build_cells_kernel<XR_VOXEL_BF16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace xr
