@@ -49,6 +49,9 @@ def _args():
     p.add_argument("--voxel", default="f32", choices=["f32", "f16", "bf16"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true")
+    p.add_argument("--launch-config", default="auto",
+                   help="DRR kernel configuration 'layout,block_warps_x,unroll' (layout 0 linear, 1 cell8) "
+                        "instead of the autotuner's choice")
     return p.parse_args()
 
 
@@ -198,7 +201,10 @@ def run_ours(a, rank, world, local):
     stream = torch.cuda.Stream(device=dev)
 
     # fixed image: DRR at the ground-truth pose + 1% noise (computed on the GPU)
+    forced = None if a.launch_config == "auto" else tuple(int(v) for v in a.launch_config.split(","))
     rc0 = xr.RayCasterLineIntCUDA(dev)
+    if forced:
+        rc0.set_launch_config(*forced)
     rc0.set_volume(w.vol)
     rc0.set_camera_model(w.cams[0])
     rc0.set_ray_step_size(w.step)
@@ -210,6 +216,8 @@ def run_ours(a, rank, world, local):
     rc0.close()
 
     rc = xr.RayCasterLineIntCUDA(dev)
+    if forced:
+        rc.set_launch_config(*forced)
     rc.set_stream(stream.cuda_stream)
     rc.set_volume(w.vol, vt)
     rc.set_camera_model(w.cams[0])
@@ -271,6 +279,8 @@ def run_ours(a, rank, world, local):
     rc.distribute_xforms_device(POP, d_pops[a.warmup].data_ptr())
     rc.compute()
     samples = rc.last_num_samples()
+    layout, bw, unroll = rc.launch_config()
+    lname = {0: "linear", 1: "cell8"}.get(layout, str(layout))
     rc.set_count_samples(False)
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
     with torch.cuda.stream(stream):
@@ -286,7 +296,7 @@ def run_ours(a, rank, world, local):
     alg_bytes = 8.0 * bvox * samples
     achieved = alg_bytes / (drr_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
-    tag = f"batched-256^3-384^2-pop100-{a.voxel}"
+    tag = f"batched-256^3-384^2-pop100-{a.voxel}-{lname}"
     traffic = _ncu_traffic(tag)
 
     extras = {}
@@ -316,7 +326,7 @@ def run_ours(a, rank, world, local):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": None if traffic is None else traffic,
-                     "kernel": "drr_kernel<f32,sum>" if vt == 0 else f"drr_kernel<{a.voxel},sum>",
+                     "kernel": f"drr_kernel<{a.voxel},sum,{lname},unroll{unroll}> block {8 * bw}x{32 // bw}",
                      "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
                      "alg_bytes_per_launch": alg_bytes, "samples_per_launch": samples,
