@@ -280,7 +280,7 @@ def run_ours(a, rank, world, local):
     rc.compute()
     samples = rc.last_num_samples()
     layout, bw, unroll = rc.launch_config()
-    lname = {0: "linear", 1: "cell8"}.get(layout, str(layout))
+    lname = {0: "linear", 1: "cell8", 2: "cell8-256bit"}.get(layout, str(layout))
     rc.set_count_samples(False)
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
     with torch.cuda.stream(stream):

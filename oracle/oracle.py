@@ -227,3 +227,55 @@ def hu_to_lin_att(hu) -> np.ndarray:
     out = np.empty_like(h)
     lib().xo_hu_to_lin_att(_p(h), h.size, _p(out))
     return out
+
+
+class RefCMAES:
+    """The reference's vendored CMA-ES (cmaes.c) through oracle/_ref (checker only)."""
+
+    _lib = None
+
+    def __init__(self, xstart, stddevs, lam, seed, tol_fun=1e-12, tol_x=1e-11, max_iter=1e6):
+        if RefCMAES._lib is None:
+            p = build_ref()
+            if p is None:
+                raise FileNotFoundError("the reference CMA-ES library is not available")
+            L = C.CDLL(str(p))
+            L.xo_cmaes_new.restype = C.c_void_p
+            L.xo_cmaes_new.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_double, C.c_double,
+                                       C.c_double]
+            for n in ("xo_cmaes_sample", "xo_cmaes_update", "xo_cmaes_mean"):
+                getattr(L, n).argtypes = [C.c_void_p, C.c_void_p]
+            L.xo_cmaes_stop.argtypes = [C.c_void_p]
+            L.xo_cmaes_generation.argtypes = [C.c_void_p]
+            L.xo_cmaes_generation.restype = C.c_double
+            L.xo_cmaes_free.argtypes = [C.c_void_p]
+            RefCMAES._lib = L
+        x0 = np.ascontiguousarray(xstart, dtype=np.float64)
+        sd = np.ascontiguousarray(stddevs, dtype=np.float64)
+        self.n, self.lam = x0.size, int(lam)
+        self.h = RefCMAES._lib.xo_cmaes_new(self.n, _p(x0), _p(sd), int(seed), self.lam, tol_fun, tol_x, max_iter)
+        self.pop = np.zeros((self.lam, self.n))
+
+    def sample(self):
+        RefCMAES._lib.xo_cmaes_sample(self.h, _p(self.pop))
+        return self.pop
+
+    def update(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        RefCMAES._lib.xo_cmaes_update(self.h, _p(f))
+
+    def stop(self) -> bool:
+        return bool(RefCMAES._lib.xo_cmaes_stop(self.h))
+
+    def mean(self):
+        m = np.zeros(self.n)
+        RefCMAES._lib.xo_cmaes_mean(self.h, _p(m))
+        return m
+
+    def generation(self) -> int:
+        return int(RefCMAES._lib.xo_cmaes_generation(self.h))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            RefCMAES._lib.xo_cmaes_free(self.h)
+            self.h = None

@@ -107,6 +107,14 @@ _SIGS = {
     "xr_obj_destroy": [H],
     "xr_obj_eval": [H, i64, P, P],
     "xr_obj_eval_device": [H, i64, P, P],
+    "xr_cmaes_create": [i32, P, P, i32, u64, C.POINTER(H)],
+    "xr_cmaes_destroy": [H],
+    "xr_cmaes_set_stop": [H, f64, f64, i64],
+    "xr_cmaes_sample_population": [H, P],
+    "xr_cmaes_resample_single": [H, i32, P],
+    "xr_cmaes_update_distribution": [H, P],
+    "xr_cmaes_test_termination": [H, C.POINTER(i32)],
+    "xr_cmaes_get": [H, P, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
 }
 _RESTYPES = {"xr_last_error": C.c_char_p, "xr_version": C.c_char_p}
 

@@ -17,7 +17,7 @@ REPO_DIR = PKG_DIR.parent
 CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_PATH = BUILD_DIR / "libxreg_gb300.so"
-SOURCES = ["xr_capi.cu", "xr_geom.cu", "xr_raycast.cu", "xr_metrics.cu"]
+SOURCES = ["xr_capi.cu", "xr_geom.cu", "xr_raycast.cu", "xr_metrics.cu", "xr_cmaes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -43,7 +43,7 @@ def _stale(target: Path, deps) -> bool:
 def build(verbose: bool = False, force: bool = False) -> Path:
     nvcc = nvcc_path()
     BUILD_DIR.mkdir(exist_ok=True)
-    headers = [REPO_DIR / "include" / "xreg_gb300.h", CSRC / "xr_internal.h"]
+    headers = [*sorted((REPO_DIR / "include").glob("*.h")), CSRC / "xr_internal.h"]
     objs = []
     jobs = []
     for src in SOURCES:

@@ -1,0 +1,78 @@
+"""CMA-ES optimizer (libxreg_gb300, xr_cmaes_*) with the call sequence of xReg's
+vendored cmaes.c: sample a population, (re)sample out-of-bounds candidates,
+update with the objective values, test for termination."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import call, load
+
+STOP_REASONS = {0: None, 1: "tol_fun", 2: "tol_x", 3: "max_iter", 4: "numerical"}
+
+
+class CMAES:
+    def __init__(self, xstart, stddevs, lam: int, seed: int = 0):
+        load()
+        x0 = np.ascontiguousarray(xstart, dtype=np.float64)
+        sd = np.ascontiguousarray(stddevs, dtype=np.float64)
+        assert x0.shape == sd.shape and x0.ndim == 1
+        h = C.c_void_p()
+        call("xr_cmaes_create", int(x0.size), x0.ctypes.data_as(C.c_void_p), sd.ctypes.data_as(C.c_void_p), int(lam),
+             C.c_uint64(int(seed) & 0xFFFFFFFFFFFFFFFF), C.byref(h))
+        self._h = h
+        self.n = int(x0.size)
+        self.lam = int(lam)
+        self._pop = np.zeros((self.lam, self.n))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load().xr_cmaes_destroy(h)
+            self._h = None
+
+    def set_stop(self, tol_fun: float = 1e-12, tol_x: float = 1e-11, max_iter: int = 1_000_000) -> None:
+        call("xr_cmaes_set_stop", self._h, float(tol_fun), float(tol_x), int(max_iter))
+
+    def sample_population(self) -> np.ndarray:
+        call("xr_cmaes_sample_population", self._h, self._pop.ctypes.data_as(C.c_void_p))
+        return self._pop
+
+    def resample_single(self, k: int) -> np.ndarray:
+        call("xr_cmaes_resample_single", self._h, int(k), self._pop.ctypes.data_as(C.c_void_p))
+        return self._pop[k]
+
+    def sample_within_bounds(self, bounds) -> np.ndarray:
+        """Samples, then redraws every candidate outside [-b, b] until it is inside
+        (Intensity2D3DRegiCMAES::run, xregIntensity2D3DRegiCMAES.cpp:162-191)."""
+        pop = self.sample_population()
+        if bounds is None:
+            return pop
+        b = np.asarray(bounds, dtype=np.float64)
+        for k in range(self.lam):
+            tries = 0
+            while np.any(np.abs(pop[k]) > b):
+                self.resample_single(k)
+                tries += 1
+                if tries > 100000:
+                    raise RuntimeError("CMA-ES: could not sample a candidate inside the bounds")
+        return pop
+
+    def update_distribution(self, fvals) -> None:
+        f = np.ascontiguousarray(fvals, dtype=np.float64)
+        assert f.size == self.lam
+        call("xr_cmaes_update_distribution", self._h, f.ctypes.data_as(C.c_void_p))
+
+    def test_for_termination(self):
+        r = C.c_int32()
+        call("xr_cmaes_test_termination", self._h, C.byref(r))
+        return STOP_REASONS.get(r.value, "unknown")
+
+    def state(self) -> dict:
+        mean = np.zeros(self.n)
+        best = np.zeros(self.n)
+        bf, sg, gen = C.c_double(), C.c_double(), C.c_int64()
+        call("xr_cmaes_get", self._h, mean.ctypes.data_as(C.c_void_p), best.ctypes.data_as(C.c_void_p), C.byref(bf),
+             C.byref(sg), C.byref(gen))
+        return {"mean": mean, "best_x": best, "best_f": bf.value, "sigma": sg.value, "generation": gen.value}

@@ -677,8 +677,10 @@ xr_status time_config(DrrParams p, cudaStream_t s, float* ms_out) {
 static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vol, DrrParams& p, cudaStream_t s) {
   const bool has_cells = vol.cells.p != nullptr;
   if (rc->cfg_layout != XR_LAYOUT_AUTO) {
-    if (rc->cfg_layout == XR_LAYOUT_CELL8 && !has_cells)
+    if (rc->cfg_layout != XR_LAYOUT_LINEAR && !has_cells)
       return fail(XR_ERR_INVALID_ARG, "compute: CELL8 layout requested but the volume has no cell copy");
+    if (rc->cfg_layout == 2 && vol.type != XR_VOXEL_F32)
+      return fail(XR_ERR_INVALID_ARG, "compute: the 256-bit CELL8 read needs a float32 volume");
     p.vol.layout = rc->cfg_layout;
     p.block_warps_x = rc->cfg_bw;
     p.unroll = rc->cfg_unroll;
@@ -708,11 +710,13 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   DrrParams t = p;
   t.sample_counter = nullptr;
   TuneCfg best{p.vol.layout, p.block_warps_x, p.unroll, 1e30f};
-  const int32_t layouts[2] = {XR_LAYOUT_LINEAR, XR_LAYOUT_CELL8};
+  // layout 2 = CELL8 read with one 256-bit load per sample (float32 only)
+  const int32_t layouts[3] = {XR_LAYOUT_LINEAR, XR_LAYOUT_CELL8, 2};
   const int32_t bws[3] = {1, 2, 4};
   const int32_t unrolls[2] = {1, 2};
   for (int32_t lay : layouts) {
-    if (lay == XR_LAYOUT_CELL8 && !has_cells) continue;
+    if (lay != XR_LAYOUT_LINEAR && !has_cells) continue;
+    if (lay == 2 && vol.type != XR_VOXEL_F32) continue;
     for (int32_t bw : bws)
       for (int32_t un : unrolls) {
         t.vol.layout = lay;
@@ -803,7 +807,7 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
 
 extern "C" XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t layout, int32_t bw, int32_t unroll) {
   XR_CHECK_ARG(rc, "set_launch_config: NULL handle");
-  XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= XR_LAYOUT_CELL8, "set_launch_config: bad layout");
+  XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= 2, "set_launch_config: bad layout");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || bw == 1 || bw == 2 || bw == 4 || bw == 8,
                "set_launch_config: block_warps_x must be 1, 2, 4 or 8");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || unroll == 1 || unroll == 2, "set_launch_config: unroll must be 1 or 2");

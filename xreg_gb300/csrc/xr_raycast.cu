@@ -46,6 +46,14 @@ struct Vox<XR_VOXEL_F32> {
     v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
     v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
   }
+  // The same 32-byte cell with one 256-bit load (sm_100+ .v8 form); cells are
+  // 32-byte aligned because the buffer is and every cell is 32 bytes.
+  __device__ __forceinline__ static void cell_wide(const void* b, int c, float v[8]) {
+    const float* p = static_cast<const float*>(b) + 8 * (size_t)c;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p));
+  }
 };
 template <>
 struct Vox<XR_VOXEL_F16> {
@@ -77,6 +85,8 @@ struct Vox<XR_VOXEL_BF16> {
 };
 
 constexpr int kThreads = 256;
+// CELL8 data read with one 256-bit load per sample (float32 volumes only).
+constexpr int kLayoutCell8Wide = 2;
 
 // Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
 // the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
@@ -95,7 +105,9 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
   const int iz = min(__float2int_rd(z), vol.nz - 2);
   const float fx = x - (float)ix, fy = y - (float)iy, fz = z - (float)iz;
   float v[8];
-  if (LAYOUT == XR_LAYOUT_CELL8) {
+  if (LAYOUT == kLayoutCell8Wide) {
+    if constexpr (VT == XR_VOXEL_F32) Vox<VT>::cell_wide(data, (iz * (ny - 1) + iy) * (nx - 1) + ix, v);
+  } else if (LAYOUT == XR_LAYOUT_CELL8) {
     Vox<VT>::cell(data, (iz * (ny - 1) + iy) * (nx - 1) + ix, v);
   } else {
     const int sy = nx, sz = nx * ny;
@@ -122,12 +134,14 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 __global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const int64_t proj_base) {
   // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
-  // the volume; a block is bw x (8 / bw) warps.
+  // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
+  // grid index: blocks resident at the same time trace the same detector tile
+  // for many nearby poses, whose footprints overlap in L2.
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int bw = p.block_warps_x;
-  const int col = blockIdx.x * (8 * bw) + (warp % bw) * 8 + (lane & 7);
-  const int row = blockIdx.y * (32 / bw) + (warp / bw) * 4 + (lane >> 3);
-  const int64_t proj = proj_base + blockIdx.z;
+  const int col = blockIdx.y * (8 * bw) + (warp % bw) * 8 + (lane & 7);
+  const int row = blockIdx.z * (32 / bw) + (warp / bw) * 4 + (lane >> 3);
+  const int64_t proj = proj_base + blockIdx.x;
   const bool active = (col < p.cols) && (row < p.rows);
 
   float sum = (KERNEL == XR_LINE_INT_MAX) ? -FLT_MAX : 0.0f;
@@ -180,7 +194,7 @@ __global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const 
       }
       const float sc = __fdiv_rn(p.step, lc);
       const float sx = __fmul_rn(dir[0], sc), sy = __fmul_rn(dir[1], sc), sz = __fmul_rn(dir[2], sc);
-      const void* data = (LAYOUT == XR_LAYOUT_CELL8) ? p.vol.cells : p.vol.voxels;
+      const void* data = (LAYOUT != XR_LAYOUT_LINEAR) ? p.vol.cells : p.vol.voxels;
       const float bx = maxb[0], by = maxb[1], bz = maxb[2];
       if (hit) {
         // samples 0..nsteps in order; the sum order never changes with UNROLL
@@ -231,10 +245,10 @@ template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
   const int bw = p.block_warps_x;
   const int tx = 8 * bw, ty = 32 / bw;
-  const int64_t max_z = 65535;
-  for (int64_t base = 0; base < p.num_projs; base += max_z) {
-    const int64_t n = (p.num_projs - base) < max_z ? (p.num_projs - base) : max_z;
-    const dim3 grid((p.cols + tx - 1) / tx, (p.rows + ty - 1) / ty, (unsigned)n);
+  const int64_t max_x = 0x7fffffff;
+  for (int64_t base = 0; base < p.num_projs; base += max_x) {
+    const int64_t n = (p.num_projs - base) < max_x ? (p.num_projs - base) : max_x;
+    const dim3 grid((unsigned)n, (p.cols + tx - 1) / tx, (p.rows + ty - 1) / ty);
     drr_kernel<VT, KERNEL, LAYOUT, UNROLL><<<grid, kThreads, 0, s>>>(p, base);
   }
   return cudaGetLastError();
@@ -242,6 +256,12 @@ cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
 
 template <int VT, int KERNEL>
 cudaError_t launch_layout(const DrrParams& p, cudaStream_t s) {
+  if (p.vol.layout == kLayoutCell8Wide) {
+    if constexpr (VT == XR_VOXEL_F32)
+      return p.unroll == 2 ? launch_t<VT, KERNEL, kLayoutCell8Wide, 2>(p, s)
+                           : launch_t<VT, KERNEL, kLayoutCell8Wide, 1>(p, s);
+    return cudaErrorInvalidValue;
+  }
   const bool cell = p.vol.layout == XR_LAYOUT_CELL8;
   if (cell) return p.unroll == 2 ? launch_t<VT, KERNEL, XR_LAYOUT_CELL8, 2>(p, s)
                                  : launch_t<VT, KERNEL, XR_LAYOUT_CELL8, 1>(p, s);
@@ -292,7 +312,8 @@ cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
   if (p.num_projs <= 0) return cudaSuccess;
   if (!(p.block_warps_x == 1 || p.block_warps_x == 2 || p.block_warps_x == 4 || p.block_warps_x == 8))
     return cudaErrorInvalidValue;
-  if (p.vol.layout == XR_LAYOUT_CELL8 && !p.vol.cells) return cudaErrorInvalidValue;
+  if (p.vol.layout != XR_LAYOUT_LINEAR && !p.vol.cells) return cudaErrorInvalidValue;
+  if (p.vol.layout == kLayoutCell8Wide && p.vol.voxel_type != XR_VOXEL_F32) return cudaErrorInvalidValue;
   switch (p.vol.voxel_type) {
     case XR_VOXEL_F32: return launch_kernel_id<XR_VOXEL_F32>(p, s);
     case XR_VOXEL_F16: return launch_kernel_id<XR_VOXEL_F16>(p, s);
