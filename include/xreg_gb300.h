@@ -240,6 +240,22 @@ XR_API xr_status xr_obj_eval(xr_objective obj, int64_t pop, const double* host_x
 /* Same with device pointers; asynchronous on the ray caster's stream. */
 XR_API xr_status xr_obj_eval_device(xr_objective obj, int64_t pop, const double* d_xforms, float* d_sims);
 
+/* -------------------------------------------------- allocation-free metric -- */
+/* Grad-NCC of num_moving moving images (device, rows*cols floats each, back to
+ * back) against a fixed image (device), written to d_sims (device, num_moving
+ * floats), asynchronously on cuda_stream, without allocating any device memory.
+ * It is for callers that cannot call cudaMalloc on this path: hosts whose device
+ * memory belongs to another allocator, or that hand the library only device
+ * pointers.  Every intermediate lives in one fixed 16 MiB array inside the
+ * library (held on each GPU that loads it until the process exits); requests
+ * that need more are refused with XR_ERR_INVALID_ARG.  The first call on a device
+ * looks up that array's address (once per device); make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race: keep
+ * them on one stream.  smooth_ksize is 5, 3 or 0 as for XR_SIM_GRAD_NCC; no mask.
+ * No counterpart in the reference (xReg's metrics always allocate their buffers). */
+XR_API xr_status xr_grad_ncc_noalloc(const float* d_fixed, const float* d_moving, int64_t rows, int64_t cols,
+                                     int64_t num_moving, int32_t smooth_ksize, float* d_sims, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,7 @@ _SIGS = {
     "xr_obj_destroy": [H],
     "xr_obj_eval": [H, i64, P, P],
     "xr_obj_eval_device": [H, i64, P, P],
+    "xr_grad_ncc_noalloc": [P, P, i64, i64, i64, i32, P, P],
     "xr_cmaes_create": [i32, P, P, i32, u64, C.POINTER(H)],
     "xr_cmaes_destroy": [H],
     "xr_cmaes_set_stop": [H, f64, f64, i64],
