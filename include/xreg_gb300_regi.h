@@ -43,6 +43,29 @@ XR_API xr_status xr_cmaes_test_termination(xr_cmaes e, int32_t* reason);
 XR_API xr_status xr_cmaes_get(xr_cmaes e, double* mean, double* best_x, double* best_f, double* sigma,
                               int64_t* generation);
 
+/* Job set: evaluates one population for each of several registrations (each an
+ * xr_objective with its own volume, cameras, fixed images and population size)
+ * with ONE persistent DRR launch over all their (tile, projection) work items,
+ * followed by each job's metrics.  This is the multi-job batching of many
+ * concurrent Intensity2D3DRegiCMAES runs (each calls obj_fn per iteration,
+ * xregIntensity2D3DRegi.cpp:571-742); xReg itself has no counterpart and runs
+ * them one after another.  Values are identical to evaluating each objective
+ * alone.  Objectives passed in one call must be distinct and live on the job
+ * set's device; any subset may be passed on any call (continuous batching). */
+typedef struct xr_jobset_s* xr_jobset;
+XR_API xr_status xr_jobset_create(int32_t device, xr_jobset* out);
+XR_API xr_status xr_jobset_destroy(xr_jobset js);
+XR_API xr_status xr_jobset_set_stream(xr_jobset js, void* cuda_stream);
+/* pops[i] poses (row-major 4x4 doubles, camera -> ITK physical) for objs[i]
+ * from host memory, values to host memory; synchronises. */
+XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t num_jobs, const xr_objective* objs, const int64_t* pops,
+                                const double* const* host_xforms, float* const* host_sims);
+/* Same with device pointers; asynchronous on the job set's stream. */
+XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t num_jobs, const xr_objective* objs,
+                                       const int64_t* pops, const double* const* d_xforms, float* const* d_sims);
+/* Work items and persistent blocks of the last launch. */
+XR_API xr_status xr_jobset_last_launch(xr_jobset js, int64_t* work_items, int32_t* blocks);
+
 #ifdef __cplusplus
 }
 #endif

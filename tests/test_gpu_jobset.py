@@ -1,0 +1,101 @@
+"""Job sets: several registrations' populations in one persistent DRR launch.
+
+Uneven jobs (volume sizes, voxel types, layouts, views, detectors, metrics,
+population sizes) evaluated together must give exactly the values each gives
+alone ("alone vs in the mix"), on any subset and order of jobs, through host and
+device entry points."""
+import numpy as np
+import pytest
+
+from tests.helpers import oracle_cams, oracle_geom, small_camera, small_volume
+from xreg_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _job(xr, seed, size, vt, det, nviews, kind, max_pop, cells=True):
+    vol = small_volume(seed, size, (1.5, 1.5, 1.5))
+    cams = [small_camera(det, 3.0)]
+    if nviews > 1:
+        from xreg_gb300.se3 import euler_xyz, rigid
+        for k in range(1, nviews):
+            R = euler_xyz(0.0, np.radians(15.0 + 10.0 * k), 0.0)
+            c = np.array([0.0, 0.0, -synth.SOURCE_TO_CENTRE_MM])
+            cam = small_camera(det, 3.0)
+            cam.set_extrins(rigid(R, c - R @ c))
+            cams.append(cam)
+    rc = xr.RayCasterLineIntCUDA()
+    rc.set_build_cell_layout(cells)
+    rc.set_volume(vol, vt)
+    rc.set_camera_models(cams)
+    rc.set_ray_step_size(0.5)
+    rng = np.random.default_rng(seed)
+    ms = []
+    for v in range(nviews):
+        m = kind()
+        m.set_fixed_image(rng.random(det).astype(np.float32))
+        ms.append(m)
+    obj = xr.PopulationObjective(rc, ms, max_pop)
+    return obj, vol, cams, ms
+
+
+def test_jobset_equals_alone(xr, oracle):
+    jobs = [
+        _job(xr, 1, (48, 44, 40), 0, (48, 52), 1, xr.ImgSimMetric2DGradNCCCUDA, 8),
+        _job(xr, 2, (40, 36, 44), 1, (32, 36), 2, xr.ImgSimMetric2DNCCCUDA, 6),
+        _job(xr, 3, (32, 32, 32), 2, (40, 40), 1, xr.ImgSimMetric2DPatchGradNCCCUDA, 4, cells=False),
+        _job(xr, 4, (36, 40, 30), 0, (24, 28), 3, xr.ImgSimMetric2DGradNCCCUDA, 5, cells=False),
+    ]
+    pops = [7, 5, 3, 4]
+    poses = [synth.sample_poses(j[1], synth.gt_pose(j[1]), p, 8.0, 10.0, seed=10 + i)
+             for i, (j, p) in enumerate(zip(jobs, pops))]
+    alone = [j[0].eval(p) for j, p in zip(jobs, poses)]
+    js = xr.JobSet()
+    mixed = js.eval([j[0] for j in jobs], poses)
+    for a, m in zip(alone, mixed):
+        np.testing.assert_array_equal(m, a)
+    items, blocks = js.last_launch()
+    assert blocks >= 152 and items > 0
+    # subsets in another order, other population sizes
+    sub = [jobs[2], jobs[0]]
+    p2 = [poses[2][:2], poses[0][:5]]
+    mixed2 = js.eval([j[0] for j in sub], p2)
+    np.testing.assert_array_equal(mixed2[0], jobs[2][0].eval(p2[0]))
+    np.testing.assert_array_equal(mixed2[1], jobs[0][0].eval(p2[1]))
+    # job 0 against the oracle (FP32 DRR semantics + double grad-NCC)
+    obj, vol, cams, ms = jobs[0]
+    drr = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams(cams), poses[0], step=0.5)
+    fixed = np.random.default_rng(1).random((48, 52)).astype(np.float32)
+    np.testing.assert_allclose(mixed[0], oracle.grad_ncc(fixed, drr), atol=1e-5, rtol=0)
+
+
+def test_jobset_device_entry(xr):
+    import torch
+    jobs = [_job(xr, 5, (40, 40, 40), 0, (40, 44), 1, xr.ImgSimMetric2DGradNCCCUDA, 6),
+            _job(xr, 6, (44, 40, 36), 1, (36, 40), 2, xr.ImgSimMetric2DGradNCCCUDA, 6)]
+    poses = [synth.sample_poses(j[1], synth.gt_pose(j[1]), 6, 8.0, 10.0, seed=20 + i) for i, j in enumerate(jobs)]
+    host = xr.JobSet().eval([j[0] for j in jobs], poses)
+    js = xr.JobSet()
+    s = torch.cuda.Stream()
+    js.set_stream(s.cuda_stream)
+    dx = [torch.from_numpy(p.reshape(-1, 16).copy()).cuda() for p in poses]
+    ds = [torch.empty(6, dtype=torch.float32, device="cuda") for _ in jobs]
+    torch.cuda.synchronize()
+    js.eval_device([j[0] for j in jobs], [6, 6], [t.data_ptr() for t in dx], [t.data_ptr() for t in ds])
+    s.synchronize()
+    for h, d in zip(host, ds):
+        np.testing.assert_array_equal(d.cpu().numpy(), h)
+
+
+def test_jobset_errors(xr):
+    from xreg_gb300 import _lib
+    obj, vol, cams, ms = _job(xr, 7, (32, 32, 32), 0, (24, 24), 1, xr.ImgSimMetric2DGradNCCCUDA, 3)
+    js = xr.JobSet()
+    p = synth.sample_poses(vol, synth.gt_pose(vol), 4, 5.0, 5.0, seed=1)
+    with pytest.raises(_lib.XRegError):
+        js.eval([obj], [p])  # population above max_pop
+    with pytest.raises(_lib.XRegError):
+        js.eval([obj, obj], [p[:2], p[:2]])  # listed twice
+    obj.close()
+    with pytest.raises(_lib.XRegError):
+        js.eval([obj], [p[:2]]) if obj._h else (_ for _ in ()).throw(_lib.XRegError(-1, "closed"))

@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     ImgSimMetric2DNCCCUDA,
     ImgSimMetric2DPatchGradNCCCUDA,
     ImgSimMetric2DPatchNCCCUDA,
+    JobSet,
     PopulationObjective,
     RayCasterLineIntCUDA,
     Volume,

@@ -116,6 +116,12 @@ _SIGS = {
     "xr_cmaes_update_distribution": [H, P],
     "xr_cmaes_test_termination": [H, C.POINTER(i32)],
     "xr_cmaes_get": [H, P, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
+    "xr_jobset_create": [i32, C.POINTER(H)],
+    "xr_jobset_destroy": [H],
+    "xr_jobset_set_stream": [H, P],
+    "xr_jobset_eval": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
+    "xr_jobset_eval_device": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
+    "xr_jobset_last_launch": [H, C.POINTER(i64), C.POINTER(i32)],
 }
 _RESTYPES = {"xr_last_error": C.c_char_p, "xr_version": C.c_char_p}
 

@@ -432,3 +432,55 @@ class PopulationObjective:
 
     def eval_device(self, pop: int, d_xforms: int, d_sims: int) -> None:
         call("xr_obj_eval_device", self._h, int(pop), C.c_void_p(int(d_xforms)), C.c_void_p(int(d_sims)))
+
+
+# ------------------------------------------------------------------ job sets
+class JobSet:
+    """One step of several registrations at once: one persistent DRR launch over
+    every listed objective's work, then each objective's metrics (xr_jobset_*)."""
+
+    def __init__(self, device: int = -1):
+        load()
+        h = C.c_void_p()
+        call("xr_jobset_create", int(device), C.byref(h))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                load().xr_jobset_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        call("xr_jobset_set_stream", self._h, C.c_void_p(cuda_stream or 0))
+
+    def eval(self, objectives, poses_per_job):
+        """poses_per_job[i]: [pop_i, 4, 4] for objectives[i]; returns a list of value arrays."""
+        n = len(objectives)
+        xs = [np.ascontiguousarray(np.asarray(p, dtype=np.float64).reshape(-1, 16)) for p in poses_per_job]
+        outs = [np.empty(x.shape[0], dtype=np.float32) for x in xs]
+        objs = (C.c_void_p * n)(*[o._h.value for o in objectives])
+        pops = (C.c_int64 * n)(*[x.shape[0] for x in xs])
+        xp = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
+        op = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+        call("xr_jobset_eval", self._h, n, objs, pops, xp, op)
+        return outs
+
+    def eval_device(self, objectives, pops, d_xforms, d_sims) -> None:
+        n = len(objectives)
+        objs = (C.c_void_p * n)(*[o._h.value for o in objectives])
+        pp = (C.c_int64 * n)(*[int(p) for p in pops])
+        xp = (C.c_void_p * n)(*[int(p) for p in d_xforms])
+        sp = (C.c_void_p * n)(*[int(p) for p in d_sims])
+        call("xr_jobset_eval_device", self._h, n, objs, pp, xp, sp)
+
+    def last_launch(self):
+        a, b = C.c_int64(), C.c_int32()
+        call("xr_jobset_last_launch", self._h, C.byref(a), C.byref(b))
+        return a.value, b.value

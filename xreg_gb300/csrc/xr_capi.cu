@@ -2,6 +2,7 @@
 // stream ordering and CUDA-graph capture of the population objective.
 // Nothing here throws across the ABI; every entry point returns an xr_status.
 #include "xr_internal.h"
+#include "xreg_gb300_regi.h"
 
 #include <cmath>
 #include <cstring>
@@ -238,8 +239,8 @@ struct xr_objective_s {
     return true;
   }
   int64_t max_pop = 0;
-  DevBuf d_poses, d_sims, d_view_sims_ptrs;
-  DevBuf h_pinned_poses;  // unused placeholder for symmetry (host copies use pageable memory)
+  uint64_t id = 0;
+  DevBuf d_poses, d_sims;
   // captured launch sequence
   cudaGraphExec_t graph_exec = nullptr;
   int64_t graph_pop = -1;
@@ -738,8 +739,11 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   return XR_OK;
 }
 
-// Uploads dirty host state and enqueues geometry + DRR kernels on the stream.
-static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
+static xr_status rc_distribute_device_on(xr_raycaster rc, int64_t n, const double* d_xf, cudaStream_t s);
+
+// Uploads dirty host state, enqueues the geometry kernel on stream s and fills
+// the DRR launch parameters (without choosing a launch configuration).
+static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, DrrParams& p) {
   XR_CHECK_ARG(rc, "compute: NULL handle");
   if (!rc->allocated) return fail(XR_ERR_NOT_ALLOCATED, "compute: allocate_resources has not been called");
   if (rc->interp != XR_INTERP_LINEAR)
@@ -747,7 +751,6 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
   XR_CHECK_ARG(vol_idx >= 0 && vol_idx < (int32_t)rc->vols.size(), "compute: bad volume index");
   XR_CHECK_ARG(rc->pose_count > 0, "compute: no projection transforms were set");
   XR_CHECK_ARG(!rc->use_bg || rc->has_bg, "compute: background projections requested but not set");
-  cudaStream_t s = rc->stream();
   const int64_t n = rc->num_projs;
   if (rc->cams_dirty) {
     XR_CUDA_TRY(cudaMemcpyAsync(rc->d_cams.p, rc->cams.data(), rc->cams.size() * sizeof(xr_camera_desc),
@@ -767,7 +770,7 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
   const auto& vol = *rc->vols[(size_t)vol_idx];
   XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
                                rc->d_cam_idx.as<int32_t>(), n, rc->pose_count, rc->d_geo.as<ProjGeom>(), s));
-  DrrParams p{};
+  p = DrrParams{};
   p.vol.voxels = vol.voxels.p;
   p.vol.cells = vol.cells.p;
   p.vol.nx = (int32_t)vol.desc.n[0];
@@ -796,7 +799,18 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
   p.default_bg = rc->default_bg;
   p.kernel_id = rc->kernel_id;
   p.store = rc->store;
-  xr_status st = rc_choose_config(rc, vol, p, s);
+  return XR_OK;
+}
+
+// Uploads dirty host state and enqueues geometry + DRR kernels on the stream.
+static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
+  XR_CHECK_ARG(rc, "compute: NULL handle");
+  cudaStream_t s = rc->stream();
+  DrrParams p{};
+  xr_status st = rc_prepare(rc, vol_idx, s, p);
+  if (st != XR_OK) return st;
+  const auto& vol = *rc->vols[(size_t)vol_idx];
+  st = rc_choose_config(rc, vol, p, s);
   if (st != XR_OK) return st;
   rc->last_layout = p.vol.layout;
   rc->last_bw = p.block_warps_x;
@@ -882,13 +896,18 @@ extern "C" XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* ou
 }
 
 extern "C" XR_API xr_status xr_rc_distribute_xforms_device(xr_raycaster rc, int64_t n, const double* d_xf) {
+  XR_CHECK_ARG(rc, "distribute_xforms_device: NULL handle");
+  DeviceGuard g(rc->device);
+  return rc_distribute_device_on(rc, n, d_xf, rc->stream());
+}
+
+// distribute_xforms_among_cam_models with device poses, enqueued on stream s.
+static xr_status rc_distribute_device_on(xr_raycaster rc, int64_t n, const double* d_xf, cudaStream_t s) {
   XR_CHECK_ARG(rc && d_xf && n > 0, "distribute_xforms_device: NULL argument");
   XR_CHECK_ARG(!rc->cams.empty(), "distribute_xforms_device: no camera models");
   XR_CHECK_ARG(rc->allocated, "distribute_xforms_device: allocate_resources first");
   XR_CHECK_ARG(n * (int64_t)rc->cams.size() == rc->num_projs,
                "distribute_xforms_device: num_xforms * num_cams must equal num_projs");
-  DeviceGuard g(rc->device);
-  cudaStream_t s = rc->stream();
   XR_CUDA_TRY(cudaMemcpyAsync(rc->d_xforms.p, d_xf, (size_t)n * 16 * 8, cudaMemcpyDeviceToDevice, s));
   rc->pose_count = n;
   rc->xforms_dirty = false;
@@ -1138,7 +1157,15 @@ extern "C" XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm) {
   return XR_OK;
 }
 
+static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s);
+
 static xr_status sm_enqueue_compute(xr_simmetric sm) {
+  XR_CHECK_ARG(sm, "compute: NULL handle");
+  return sm_enqueue_compute_on(sm, sm->stream());
+}
+
+// Enqueues the metric's kernels on stream s.
+static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
   XR_CHECK_ARG(sm, "compute: NULL handle");
   if (!sm->allocated) return fail(XR_ERR_NOT_ALLOCATED, "compute: allocate_resources has not been called");
   const int64_t npix = sm->rows * sm->cols;
@@ -1154,7 +1181,6 @@ static xr_status sm_enqueue_compute(xr_simmetric sm) {
     XR_CHECK_ARG(sm->mov_dev, "compute: no moving image buffer (was the bound ray caster destroyed?)");
     mov = sm->mov_dev + sm->proj_offset * npix;
   }
-  cudaStream_t s = sm->stream();
   const int rows = (int)sm->rows, cols = (int)sm->cols;
   const uint8_t* mask = sm->has_mask ? sm->d_mask.as<uint8_t>() : nullptr;
   switch (sm->kind) {
@@ -1263,12 +1289,14 @@ extern "C" XR_API xr_status xr_obj_create(xr_raycaster rc, int32_t vol_idx, int3
   }
   XR_CUDA_TRY(obj->d_poses.reserve((size_t)max_pop * 16 * 8));
   XR_CUDA_TRY(obj->d_sims.reserve((size_t)max_pop * 4));
+  obj->id = reg_add(obj);
   *out = guard.release();
   return XR_OK;
 }
 
 extern "C" XR_API xr_status xr_obj_destroy(xr_objective obj) {
   if (!obj) return XR_OK;
+  reg_remove(obj);
   if (reg_alive(obj->rc, obj->rc_id)) {
     DeviceGuard g(obj->rc->device);
     cudaStreamSynchronize(obj->rc->stream());
@@ -1369,4 +1397,163 @@ extern "C" XR_API xr_status xr_obj_eval(xr_objective obj, int64_t pop, const dou
   if (st != XR_OK) return st;
   XR_CUDA_TRY(cudaMemcpyAsync(h_sims, obj->d_sims.p, (size_t)pop * 4, cudaMemcpyDeviceToHost, s));
   return xr_rc_synchronize(obj->rc);
+}
+
+// ================================================================== job sets
+// Several registration objectives evaluated in one step: per job the poses are
+// copied in and its geometry kernel runs, then ONE persistent DRR launch covers
+// every job's (tile, projection) work items, then each job's metrics and mean
+// over views run and the values are copied out.  Everything is ordered on the
+// job set's stream.
+struct xr_jobset_s {
+  int device = 0;
+  cudaStream_t own_stream = nullptr, ext_stream = nullptr;
+  bool has_ext = false;
+  DevBuf d_jobs, d_counter;
+  std::vector<MultiJobDrr> h_jobs;
+  int blocks = 0;
+  long long last_items = 0;
+  cudaStream_t stream() const { return has_ext ? ext_stream : own_stream; }
+};
+
+namespace {
+bool reg_contains(const void* p) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  return g_live.count(p) != 0;
+}
+}  // namespace
+
+extern "C" XR_API xr_status xr_jobset_create(int32_t device, xr_jobset* out) {
+  XR_CHECK_ARG(out, "xr_jobset_create: out is NULL");
+  *out = nullptr;
+  int dev = device;
+  if (dev < 0) XR_CUDA_TRY(cudaGetDevice(&dev));
+  DeviceGuard g(dev);
+  auto js = std::make_unique<xr_jobset_s>();
+  js->device = dev;
+  XR_CUDA_TRY(cudaStreamCreateWithFlags(&js->own_stream, cudaStreamNonBlocking));
+  XR_CUDA_TRY(js->d_counter.reserve(256));
+  js->blocks = drr_multi_blocks();
+  if (js->blocks <= 0) {
+    cudaStreamDestroy(js->own_stream);
+    return fail(XR_ERR_CUDA, "xr_jobset_create: could not size the persistent grid");
+  }
+  *out = js.release();
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_jobset_destroy(xr_jobset js) {
+  if (!js) return XR_OK;
+  DeviceGuard g(js->device);
+  cudaStreamSynchronize(js->stream());
+  cudaStreamDestroy(js->own_stream);
+  delete js;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_jobset_set_stream(xr_jobset js, void* s) {
+  XR_CHECK_ARG(js, "xr_jobset_set_stream: NULL handle");
+  js->ext_stream = static_cast<cudaStream_t>(s);
+  js->has_ext = s != nullptr;
+  return XR_OK;
+}
+
+static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
+                                const double* const* xforms, bool host_in, float* const* sims, bool host_out) {
+  XR_CHECK_ARG(js && objs && pops && xforms && sims && n > 0, "xr_jobset_eval: NULL argument or no jobs");
+  DeviceGuard g(js->device);
+  cudaStream_t s = js->stream();
+  js->h_jobs.clear();
+  long long items = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    xr_objective obj = objs[i];
+    XR_CHECK_ARG(obj && reg_contains(obj), "xr_jobset_eval: unknown or destroyed objective");
+    XR_CHECK_ARG(obj->peers_alive(), "xr_jobset_eval: a ray caster or metric of an objective was destroyed");
+    XR_CHECK_ARG(obj->rc->device == js->device, "xr_jobset_eval: objective lives on another device");
+    for (int32_t k = 0; k < i; ++k) XR_CHECK_ARG(objs[k] != obj, "xr_jobset_eval: an objective is listed twice");
+    const int64_t pop = pops[i];
+    XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "xr_jobset_eval: population outside [1, max_pop]");
+    XR_CHECK_ARG(xforms[i] && sims[i], "xr_jobset_eval: NULL pose or value pointer");
+    if (host_in) XR_CHECK_ARG(finite_all(xforms[i], 16 * pop), "xr_jobset_eval: non-finite transform");
+    XR_CUDA_TRY(cudaMemcpyAsync(obj->d_poses.p, xforms[i], (size_t)pop * 16 * 8,
+                                host_in ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    xr_raycaster rc = obj->rc;
+    const int32_t nv = (int32_t)obj->metrics.size();
+    xr_status st = xr_rc_set_num_projs(rc, (int64_t)nv * pop);
+    if (st != XR_OK) return st;
+    if ((st = rc_distribute_device_on(rc, pop, obj->d_poses.as<double>(), s)) != XR_OK) return st;
+    rc->store = XR_PROJ_STORE_REPLACE;
+    MultiJobDrr J{};
+    if ((st = rc_prepare(rc, obj->vol_idx, s, J.p)) != XR_OK) return st;
+    XR_CHECK_ARG(J.p.kernel_id == XR_LINE_INT_SUM, "xr_jobset_eval: job sets use the line-integral sum kernel");
+    const auto& vol = *rc->vols[(size_t)obj->vol_idx];
+    // float32 volumes read their cell copy with one 256-bit load; half volumes with one 128-bit load
+    J.p.vol.layout = vol.cells.p ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
+    J.p.block_warps_x = 2;
+    J.p.unroll = 2;
+    J.tiles_x = (int32_t)((J.p.cols + 15) / 16);
+    J.tiles_y = (int32_t)((J.p.rows + 15) / 16);
+    J.item_begin = items;
+    items += (long long)J.p.num_projs * J.tiles_x * J.tiles_y;
+    rc->last_layout = J.p.vol.layout;
+    rc->last_bw = 2;
+    rc->last_unroll = 2;
+    js->h_jobs.push_back(J);
+  }
+  XR_CUDA_TRY(js->d_jobs.reserve(js->h_jobs.size() * sizeof(MultiJobDrr)));
+  XR_CUDA_TRY(cudaMemcpyAsync(js->d_jobs.p, js->h_jobs.data(), js->h_jobs.size() * sizeof(MultiJobDrr),
+                              cudaMemcpyHostToDevice, s));
+  XR_CUDA_TRY(launch_drr_multi(js->d_jobs.as<MultiJobDrr>(), (int)js->h_jobs.size(), items,
+                               js->d_counter.as<unsigned long long>(), js->blocks, s));
+  js->last_items = items;
+  for (int32_t i = 0; i < n; ++i) {
+    xr_objective obj = objs[i];
+    const int64_t pop = pops[i];
+    const int32_t nv = (int32_t)obj->metrics.size();
+    const float* view_sims[16];
+    for (int32_t v = 0; v < nv; ++v) {
+      xr_simmetric m = obj->metrics[(size_t)v];
+      m->num_mov = pop;
+      m->rc = obj->rc;
+      m->rc_id = obj->rc->id;
+      m->proj_offset = (int64_t)v * pop;
+      xr_status st = sm_enqueue_compute_on(m, s);
+      if (st != XR_OK) return st;
+      view_sims[v] = m->d_sims.as<float>();
+    }
+    XR_CUDA_TRY(launch_combine_mean(view_sims, nv, pop, obj->d_sims.as<float>(), s));
+    XR_CUDA_TRY(cudaMemcpyAsync(sims[i], obj->d_sims.p, (size_t)pop * 4,
+                                host_out ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  }
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
+                                           const double* const* host_xforms, float* const* host_sims) {
+  xr_status st = jobset_enqueue(js, n, objs, pops, host_xforms, true, host_sims, true);
+  if (st != XR_OK) return st;
+  XR_CUDA_TRY(cudaStreamSynchronize(js->stream()));
+  for (int32_t i = 0; i < n; ++i) {
+    unsigned int err = 0;
+    xr_raycaster rc = objs[i]->rc;
+    XR_CUDA_TRY(cudaMemcpy(&err, rc->d_counters.as<char>() + 8, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) {
+      cudaMemset(rc->d_counters.as<char>() + 8, 0, sizeof(err));
+      return fail(XR_ERR_DEVICE_CHECK, "xr_jobset_eval: a job's rays exceeded the step-count guard");
+    }
+  }
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t n, const xr_objective* objs,
+                                                  const int64_t* pops, const double* const* d_xforms,
+                                                  float* const* d_sims) {
+  return jobset_enqueue(js, n, objs, pops, d_xforms, false, d_sims, false);
+}
+
+extern "C" XR_API xr_status xr_jobset_last_launch(xr_jobset js, int64_t* work_items, int32_t* blocks) {
+  XR_CHECK_ARG(js && work_items && blocks, "xr_jobset_last_launch: NULL argument");
+  *work_items = js->last_items;
+  *blocks = js->blocks;
+  return XR_OK;
 }

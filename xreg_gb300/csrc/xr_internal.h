@@ -67,6 +67,19 @@ cudaError_t launch_proj_geom(const xr_volume_desc& vol, const xr_camera_desc* d_
 
 // ---- launchers (xr_raycast.cu) ----
 cudaError_t launch_drr(const DrrParams& p, cudaStream_t s);
+
+// One job of a multi-job DRR launch: its parameters (sum kernel; any store
+// rule), where its work items start, and its 16x16-pixel tile grid.
+struct MultiJobDrr {
+  DrrParams p;
+  long long item_begin;  // items of this job: [item_begin, item_begin + num_projs * tiles_x * tiles_y)
+  int32_t tiles_x, tiles_y;
+};
+// Persistent kernel over all jobs' (tile, projection) items; d_counter is reset here.
+cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long total_items,
+                             unsigned long long* d_counter, int blocks, cudaStream_t s);
+// Blocks that fill the current device once (SMs x resident blocks per SM).
+int drr_multi_blocks();
 // Bytes of the CELL8 copy of a volume, and the kernel that builds it from float32 voxels.
 size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type);
 cudaError_t launch_build_cells(const float* vox_f32, int nx, int ny, int nz, int32_t voxel_type, float scale,

@@ -131,22 +131,14 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
   return fmaf(b1, fz, b0 * gz);
 }
 
+// Traces the ray of pixel (row, col) of projection proj and stores the result
+// (the caller checks that the pixel exists).  Returns the number of samples.
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const int64_t proj_base) {
-  // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
-  // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
-  // grid index: blocks resident at the same time trace the same detector tile
-  // for many nearby poses, whose footprints overlap in L2.
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int bw = p.block_warps_x;
-  const int col = blockIdx.y * (8 * bw) + (warp % bw) * 8 + (lane & 7);
-  const int row = blockIdx.z * (32 / bw) + (warp / bw) * 4 + (lane >> 3);
-  const int64_t proj = proj_base + blockIdx.x;
-  const bool active = (col < p.cols) && (row < p.rows);
-
+__device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, const int64_t proj, const int row,
+                                                          const int col) {
   float sum = (KERNEL == XR_LINE_INT_MAX) ? -FLT_MAX : 0.0f;
   unsigned long long ns = 0;
-  if (active) {
+  {
     const ProjGeom& g = p.geo[proj];
     const float fc = (float)col, fr = (float)row;
     float dir[3], v[3], src[3];
@@ -235,9 +227,74 @@ __global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const 
     else prev = p.out[oidx];
     p.out[oidx] = (KERNEL == XR_LINE_INT_MAX) ? ((prev < aa) ? aa : prev) : __fadd_rn(prev, aa);
   }
+  return ns;
+}
+
+template <int VT, int KERNEL, int LAYOUT, int UNROLL>
+__global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const int64_t proj_base) {
+  // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
+  // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
+  // grid index: blocks resident at the same time trace the same detector tile
+  // for many nearby poses, whose footprints overlap in L2.
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int bw = p.block_warps_x;
+  const int col = blockIdx.y * (8 * bw) + (warp % bw) * 8 + (lane & 7);
+  const int row = blockIdx.z * (32 / bw) + (warp / bw) * 4 + (lane >> 3);
+  const int64_t proj = proj_base + blockIdx.x;
+  unsigned long long ns = 0;
+  if (col < p.cols && row < p.rows) ns = trace_pixel<VT, KERNEL, LAYOUT, UNROLL>(p, proj, row, col);
   if (p.sample_counter) {
     for (int o = 16; o > 0; o >>= 1) ns += __shfl_down_sync(0xffffffffu, ns, o);
     if (lane == 0 && ns) atomicAdd(p.sample_counter, ns);
+  }
+}
+
+// Persistent multi-job kernel: every block repeatedly takes the next work item
+// (job, tile, projection) from a global counter until all are done; projections
+// are the fastest index within a job for L2 reuse across nearby poses.  Blocks
+// never wait on one another (the counter is only incremented), so a block that
+// finds no work simply exits.  Line-integral sum kernel, 16x16-pixel tiles,
+// unroll 2; the layout and voxel type are per job.
+__global__ void __launch_bounds__(kThreads) drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs,
+                                                             long long total, unsigned long long* counter) {
+  __shared__ long long s_item;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= total) break;
+    int j = 0;
+    while (j + 1 < njobs && jobs[j + 1].item_begin <= item) ++j;
+    const MultiJobDrr& J = jobs[j];
+    const long long local = item - J.item_begin;
+    const long long nproj = J.p.num_projs;
+    const int64_t proj = (int64_t)(local % nproj);
+    const int tile = (int)(local / nproj);
+    const int ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
+    const int col = tx * 16 + (warp & 1) * 8 + (lane & 7);
+    const int row = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
+    if (col < J.p.cols && row < J.p.rows) {
+      const int sel = J.p.vol.voxel_type * 4 + J.p.vol.layout;
+      switch (sel) {
+        case XR_VOXEL_F32 * 4 + XR_LAYOUT_LINEAR:
+          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, 2>(J.p, proj, row, col); break;
+        case XR_VOXEL_F32 * 4 + XR_LAYOUT_CELL8:
+          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, 2>(J.p, proj, row, col); break;
+        case XR_VOXEL_F32 * 4 + kLayoutCell8Wide:
+          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, kLayoutCell8Wide, 2>(J.p, proj, row, col); break;
+        case XR_VOXEL_F16 * 4 + XR_LAYOUT_LINEAR:
+          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, 2>(J.p, proj, row, col); break;
+        case XR_VOXEL_F16 * 4 + XR_LAYOUT_CELL8:
+          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, 2>(J.p, proj, row, col); break;
+        case XR_VOXEL_BF16 * 4 + XR_LAYOUT_LINEAR:
+          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, 2>(J.p, proj, row, col); break;
+        case XR_VOXEL_BF16 * 4 + XR_LAYOUT_CELL8:
+          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, 2>(J.p, proj, row, col); break;
+        default: break;
+      }
+    }
   }
 }
 
@@ -320,6 +377,23 @@ cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
     case XR_VOXEL_BF16: return launch_kernel_id<XR_VOXEL_BF16>(p, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+int drr_multi_blocks() {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drr_multi_kernel, kThreads, 0) != cudaSuccess) return 0;
+  return sms * (per_sm > 0 ? per_sm : 1);
+}
+
+cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long total_items,
+                             unsigned long long* d_counter, int blocks, cudaStream_t s) {
+  if (total_items <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  drr_multi_kernel<<<blocks, kThreads, 0, s>>>(d_jobs, njobs, total_items, d_counter);
+  return cudaGetLastError();
 }
 
 size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type) {
