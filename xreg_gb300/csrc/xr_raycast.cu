@@ -85,6 +85,9 @@ struct Vox<XR_VOXEL_BF16> {
 };
 
 constexpr int kThreads = 256;
+// Resident blocks per SM the DRR kernel is compiled for (caps registers at 40:
+// 48 warps per SM instead of 40 at 48 registers).
+constexpr int kMinBlocksPerSM = 6;
 // CELL8 data read with one 256-bit load per sample (float32 volumes only).
 constexpr int kLayoutCell8Wide = 2;
 
@@ -96,14 +99,16 @@ constexpr int kLayoutCell8Wide = 2;
 template <int VT, int LAYOUT>
 __device__ __forceinline__ float sample(const VolView& vol, const void* data, float px, float py, float pz,
                                         float bx, float by, float bz) {
+  // Cell = floor(position) clamped to [0, n-2]; fraction = position - cell
+  // saturated to [0, 1].  Equal to clamping the position to [0, n-1] first: below
+  // 0 the cell is 0 and the fraction 0, above n-1 the cell is n-2 and the
+  // fraction 1, and a NaN position reads cell 0 with fraction 0.
+  (void)bx; (void)by; (void)bz;
   const int nx = vol.nx, ny = vol.ny;
-  const float x = fminf(fmaxf(px, 0.0f), bx);
-  const float y = fminf(fmaxf(py, 0.0f), by);
-  const float z = fminf(fmaxf(pz, 0.0f), bz);
-  const int ix = min(__float2int_rd(x), nx - 2);
-  const int iy = min(__float2int_rd(y), ny - 2);
-  const int iz = min(__float2int_rd(z), vol.nz - 2);
-  const float fx = x - (float)ix, fy = y - (float)iy, fz = z - (float)iz;
+  const int ix = max(min(__float2int_rd(px), nx - 2), 0);
+  const int iy = max(min(__float2int_rd(py), ny - 2), 0);
+  const int iz = max(min(__float2int_rd(pz), vol.nz - 2), 0);
+  const float fx = __saturatef(px - (float)ix), fy = __saturatef(py - (float)iy), fz = __saturatef(pz - (float)iz);
   float v[8];
   if (LAYOUT == kLayoutCell8Wide) {
     if constexpr (VT == XR_VOXEL_F32) Vox<VT>::cell_wide(data, (iz * (ny - 1) + iy) * (nx - 1) + ix, v);
@@ -231,7 +236,7 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 }
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads) drr_kernel(const DrrParams p, const int64_t proj_base) {
+__global__ void __launch_bounds__(kThreads, kMinBlocksPerSM) drr_kernel(const DrrParams p, const int64_t proj_base) {
   // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
   // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
   // grid index: blocks resident at the same time trace the same detector tile

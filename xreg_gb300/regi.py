@@ -1,0 +1,184 @@
+"""Intensity-based 2D/3D registration driven by the GPU population objective.
+
+A `Registration` is one job of xReg's MultiLevelMultiObjRegi for a single object
+(lib/regi/interfaces_2d_3d/xregMultiObjMultiLevel2D3DRegi.cpp:164-531): a list of
+levels (camera models, fixed images, metric, optimizer schedule); at each level a
+CMA-ES (Intensity2D3DRegiCMAES::run, xregIntensity2D3DRegiCMAES.cpp:76-247)
+searches SE(3) Lie-algebra offsets x (SE3OptVarsLieAlg, xregSE3OptVars.cpp:128-137)
+applied about an intermediate frame at the volume centre, so a candidate pose is
+
+    pose(x) = C @ ExpSE3(x) @ inv(C) @ start_pose        (C = volume centre frame),
+
+the objective is the mean over views of the metric (one GPU population
+evaluation per generation), out-of-bounds candidates are resampled, and the next
+level starts from the previous level's result.
+
+The job exposes a step interface (propose / tell) so a server can evaluate the
+populations of many jobs in one GPU launch (continuous batching); `run()` drives
+one job alone.  The volume is uploaded once per job and stays on the device.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api
+from .cmaes import CMAES
+from .se3 import exp_se3
+
+METRICS = {
+    "ncc": api.ImgSimMetric2DNCCCUDA,
+    "grad_ncc": api.ImgSimMetric2DGradNCCCUDA,
+    "patch_ncc": api.ImgSimMetric2DPatchNCCCUDA,
+    "patch_grad_ncc": api.ImgSimMetric2DPatchGradNCCCUDA,
+}
+
+# xReg's single-view pelvis registration uses sigma (15, 15, 30 deg, 50, 50, 100 mm)
+# for its first level; these are milder defaults for perturbations of ~10 deg / 20 mm.
+DEFAULT_SIGMA = np.array([np.radians(10.0)] * 3 + [20.0] * 3)
+
+
+@dataclass
+class RegiLevel:
+    cams: list                      # CameraModel per view
+    fixed: list                     # fixed image per view (rows x cols float32)
+    metric: str = "grad_ncc"
+    pop: int = 50
+    sigma: np.ndarray = field(default_factory=lambda: DEFAULT_SIGMA.copy())
+    bounds: np.ndarray | None = None
+    max_iters: int = 100
+    tol_fun: float = 1e-6
+    tol_x: float = 1e-6
+
+
+@dataclass
+class LevelResult:
+    pose: np.ndarray
+    x: np.ndarray
+    best_value: float
+    generations: int
+    stop: str | None
+
+
+class Registration:
+    def __init__(self, vol: api.Volume, levels: list, init_pose: np.ndarray, step: float = 0.5,
+                 voxel_type: int = 0, seed: int = 0, device: int = -1, name: str = ""):
+        self.vol = vol
+        self.levels = list(levels)
+        self.init_pose = np.asarray(init_pose, dtype=np.float64)
+        self.step = float(step)
+        self.voxel_type = int(voxel_type)
+        self.seed = int(seed)
+        self.device = device
+        self.name = name
+        self.C = vol.xform_img_center_to_itk_phys()
+        self.Ci = np.linalg.inv(self.C)
+        self.rc = None
+        self.level = -1
+        self.obj = None
+        self.es = None
+        self.start_pose = self.init_pose.copy()
+        self.results: list = []
+        self.done = False
+        self.started = False
+        self.t_submit = None
+        self.t_start = None
+        self.t_done = None
+        self._pop_x = None
+
+    # ---------------------------------------------------------- resources
+    def footprint_bytes(self) -> int:
+        """Device memory the job holds while active (volume copies + the largest level's buffers)."""
+        nx, ny, nz = self.vol.size
+        bvox = 4 if self.voxel_type == 0 else 2
+        vol = nx * ny * nz * bvox + (nx - 1) * (ny - 1) * (nz - 1) * bvox * 8
+        lev = 0
+        for L in self.levels:
+            r, c = L.cams[0].num_det_rows, L.cams[0].num_det_cols
+            per = len(L.cams) * L.pop * r * c * 4 + len(L.cams) * r * c * 4 * 6 + len(L.cams) * L.pop * 2048 * 8
+            lev = max(lev, per)
+        return int(vol + lev + (16 << 20))
+
+    def start(self) -> None:
+        self.rc = api.RayCasterLineIntCUDA(self.device)
+        self.rc.set_volume(self.vol, self.voxel_type)
+        self.rc.set_ray_step_size(self.step)
+        self.started = True
+        self.t_start = time.perf_counter()
+        self._enter_level(0)
+
+    def _enter_level(self, k: int) -> None:
+        L = self.levels[k]
+        self.level = k
+        self.rc.set_camera_models(L.cams)
+        ms = []
+        for f in L.fixed:
+            m = METRICS[L.metric](self.device)
+            m.set_fixed_image(f)
+            ms.append(m)
+        if self.obj is not None:
+            self.obj.close()
+        self.obj = api.PopulationObjective(self.rc, ms, L.pop)
+        self.es = CMAES(np.zeros(6), L.sigma, L.pop, seed=self.seed * 1009 + k)
+        self.es.set_stop(tol_fun=L.tol_fun, tol_x=L.tol_x, max_iter=L.max_iters)
+
+    def poses_of(self, xs: np.ndarray) -> np.ndarray:
+        A = self.C
+        B = self.Ci @ self.start_pose
+        return np.stack([A @ exp_se3(x) @ B for x in xs])
+
+    # ---------------------------------------------------------- stepping
+    def propose(self) -> np.ndarray:
+        """Samples the current level's population; returns its poses [pop, 4, 4]."""
+        L = self.levels[self.level]
+        self._pop_x = self.es.sample_within_bounds(L.bounds).copy()
+        return self.poses_of(self._pop_x)
+
+    def tell(self, values) -> None:
+        self.es.update_distribution(np.asarray(values, dtype=np.float64))
+        stop = self.es.test_for_termination()
+        if stop is not None:
+            st = self.es.state()
+            x = st["best_x"]
+            pose = self.poses_of(x[None])[0]
+            self.results.append(LevelResult(pose, x, st["best_f"], st["generation"], stop))
+            self.start_pose = pose
+            if self.level + 1 < len(self.levels):
+                self._enter_level(self.level + 1)
+            else:
+                self.finish()
+
+    def finish(self) -> None:
+        self.done = True
+        self.t_done = time.perf_counter()
+        if self.obj is not None:
+            self.obj.close()
+            self.obj = None
+        if self.rc is not None:
+            self.rc.close()
+            self.rc = None
+
+    @property
+    def final_pose(self) -> np.ndarray:
+        return self.results[-1].pose if self.results else self.init_pose
+
+    def run(self) -> np.ndarray:
+        """Runs the job alone to completion."""
+        if not self.started:
+            self.start()
+        while not self.done:
+            poses = self.propose()
+            self.tell(self.obj.eval(poses))
+        return self.final_pose
+
+
+def pose_error(a: np.ndarray, b: np.ndarray, vol: api.Volume) -> tuple:
+    """Difference of two cam -> ITK physical poses as (rotation angle in degrees,
+    displacement in mm of the volume centre in camera coordinates)."""
+    c = vol.xform_img_center_to_itk_phys()[:, 3]
+    ai, bi = np.linalg.inv(a), np.linalg.inv(b)
+    R = ai[:3, :3] @ bi[:3, :3].T
+    ang = float(np.degrees(np.arccos(np.clip((np.trace(R) - 1.0) * 0.5, -1.0, 1.0))))
+    return ang, float(np.linalg.norm((ai @ c)[:3] - (bi @ c)[:3]))

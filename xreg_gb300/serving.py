@@ -1,0 +1,121 @@
+"""Continuous-batching registration server.
+
+Requests (a `Registration`: volume, cameras, fixed images per level, initial
+pose, optimizer schedule) arrive at any time.  Each server step:
+
+  1. admits queued jobs in arrival order while the summed device footprint of
+     the active jobs stays within the HBM budget (their volumes are uploaded
+     once and stay resident, as do fixed-image gradients and optimizer state);
+  2. asks every active job for its current population (CMA-ES sample);
+  3. evaluates all populations with ONE job-set call: one persistent DRR launch
+     over every job's (tile, pose) work, then each job's metrics;
+  4. hands each job its values (CMA-ES update, level change, completion) and
+     retires finished jobs, recording their latency from arrival.
+
+Because each job's optimizer has its own random stream and the job-set values
+equal the values each job gets alone, a job's result does not depend on which
+other jobs share its steps.
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api
+from .regi import Registration
+
+
+@dataclass
+class ServerStats:
+    completed: int = 0
+    latencies_s: list = field(default_factory=list)
+    steps: int = 0
+    poses_evaluated: int = 0
+    busy_s: float = 0.0
+    max_active: int = 0
+    max_footprint: int = 0
+
+    def summary(self) -> dict:
+        lat = np.array(self.latencies_s) if self.latencies_s else np.zeros(1)
+        return {"completed": self.completed, "p50_s": float(np.percentile(lat, 50)),
+                "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "steps": self.steps,
+                "poses_evaluated": self.poses_evaluated, "busy_s": self.busy_s, "max_active": self.max_active,
+                "max_footprint_gb": self.max_footprint / 1e9}
+
+
+class RegistrationServer:
+    def __init__(self, device: int = -1, hbm_budget_bytes: float = 180e9, max_active: int = 64):
+        self.device = device
+        self.budget = float(hbm_budget_bytes)
+        self.max_active = int(max_active)
+        self.queue: collections.deque = collections.deque()
+        self.active: list = []
+        self.finished: list = []
+        self.jobset = api.JobSet(device)
+        self.stats = ServerStats()
+
+    def submit(self, job: Registration, t_arrival: float | None = None) -> None:
+        job.t_submit = time.perf_counter() if t_arrival is None else t_arrival
+        self.queue.append(job)
+
+    def footprint(self) -> int:
+        return sum(j.footprint_bytes() for j in self.active)
+
+    def _admit(self) -> None:
+        used = self.footprint()
+        while self.queue and len(self.active) < self.max_active:
+            need = self.queue[0].footprint_bytes()
+            if self.active and used + need > self.budget:
+                break
+            job = self.queue.popleft()
+            job.start()
+            self.active.append(job)
+            used += need
+        self.stats.max_active = max(self.stats.max_active, len(self.active))
+        self.stats.max_footprint = max(self.stats.max_footprint, used)
+
+    def step(self) -> int:
+        """One optimizer generation for every active job; returns the number of jobs stepped."""
+        self._admit()
+        if not self.active:
+            return 0
+        t0 = time.perf_counter()
+        jobs = list(self.active)
+        poses = [j.propose() for j in jobs]
+        values = self.jobset.eval([j.obj for j in jobs], poses)
+        for j, v in zip(jobs, values):
+            j.tell(v)
+        now = time.perf_counter()
+        self.stats.busy_s += now - t0
+        self.stats.steps += 1
+        self.stats.poses_evaluated += sum(len(p) for p in poses)
+        still = []
+        for j in jobs:
+            if j.done:
+                self.finished.append(j)
+                self.stats.completed += 1
+                self.stats.latencies_s.append(j.t_done - j.t_submit)
+            else:
+                still.append(j)
+        self.active = still
+        return len(jobs)
+
+    def run(self, arrivals=None) -> ServerStats:
+        """Runs until every submitted job is done.  arrivals: optional list of
+        (offset_seconds, Registration) released when the wall clock passes them."""
+        pending = sorted(arrivals or [], key=lambda a: a[0])
+        t0 = time.perf_counter()
+        i = 0
+        while i < len(pending) or self.queue or self.active:
+            now = time.perf_counter() - t0
+            while i < len(pending) and pending[i][0] <= now:
+                self.submit(pending[i][1], t0 + pending[i][0])
+                i += 1
+            if not self.queue and not self.active:
+                time.sleep(max(0.0, min(0.01, pending[i][0] - now)) if i < len(pending) else 0.0)
+                continue
+            self.step()
+        return self.stats

@@ -164,3 +164,92 @@ def fixed_pose(w: Workload) -> np.ndarray:
     """Ground-truth pose: the nominal view perturbed by rot ~ N(0, 5 deg), trans ~ N(0, 10 mm)."""
     rng = np.random.default_rng(w.seed + 1)
     return perturb(w.vol, w.gt, rng.normal(0.0, 5.0, 3), rng.normal(0.0, 10.0, 3))
+
+
+# ------------------------------------------------------------ uneven jobs
+@dataclass
+class JobSpec:
+    """One registration request of the uneven multi-job / serving workloads."""
+    seed: int
+    size: tuple            # volume (nx, ny, nz)
+    spacing: tuple
+    view_angles: list      # degrees about the volume's z axis, one per view
+    ds_first: float        # detector downsample factor of the first level (0.125 = 8x)
+    pop: int
+
+
+def uneven_job_specs(n: int, seed: int) -> list:
+    """n requests with volumes from 192^3 to 512x512x300 (each its own seed), 1-3
+    views 15-40 degrees apart, detector 1536^2 @ 0.194 mm downsampled 4x or 8x,
+    CMA-ES lambda in [20, 100]."""
+    rng = np.random.default_rng(seed)
+    sizes = [(192, 192, 192), (256, 256, 200), (256, 256, 256), (320, 320, 256), (384, 384, 280),
+             (448, 448, 300), (512, 512, 300)]
+    out = []
+    for k in range(n):
+        size = sizes[int(rng.integers(len(sizes)))]
+        sp = 300.0 / size[0]
+        nv = int(rng.integers(1, 4))
+        angles = [0.0]
+        for _ in range(nv - 1):
+            angles.append(angles[-1] + float(rng.uniform(15.0, 40.0)))
+        out.append(JobSpec(seed=seed * 1000 + k, size=size, spacing=(sp, sp, sp), view_angles=angles,
+                           ds_first=float(rng.choice([0.25, 0.125])), pop=int(rng.integers(20, 101))))
+    return out
+
+
+def job_registration(spec: JobSpec, levels=None, iters=(150, 100), level2_pop: int = 8, voxel_type: int = 1,
+                     step: float = 0.5, device: int = -1):
+    """A two-level registration request from a JobSpec: level 1 at the spec's
+    downsampling (or 8x) with CMA-ES lambda = spec.pop, level 2 at 4x with a small
+    population; fixed images rendered at a ground-truth pose, start pose perturbed
+    from it by N(0, 5 deg) / N(0, 10 mm).  Returns (Registration, ground truth)."""
+    from .regi import Registration, RegiLevel
+    vol = phantom_volume(spec.size, spec.spacing, spec.seed)
+    rng = np.random.default_rng(spec.seed + 1)
+    gt = perturb(vol, gt_pose(vol), rng.normal(0.0, 3.0, 3), rng.normal(0.0, 5.0, 3))
+    init = perturb(vol, gt, rng.normal(0.0, 5.0, 3), rng.normal(0.0, 10.0, 3))
+    ds = levels or [spec.ds_first, 0.25]
+    lv = []
+    for k, d in enumerate(ds):
+        cams = view_cameras(spec.view_angles, d)
+        fixed = render_fixed(vol, cams, gt, step, spec.seed + 17 * (k + 1), device)
+        if k == 0:
+            lv.append(RegiLevel(cams, fixed, "grad_ncc", pop=spec.pop, max_iters=iters[0]))
+        else:
+            sig = np.array([np.radians(1.5)] * 3 + [3.0] * 3)
+            lv.append(RegiLevel(cams, fixed, "grad_ncc", pop=level2_pop, sigma=sig,
+                                max_iters=iters[min(k, len(iters) - 1)]))
+    return Registration(vol, lv, init, step=step, voxel_type=voxel_type, seed=spec.seed, device=device,
+                        name=f"job{spec.seed}"), gt
+
+
+def view_cameras(angles, ds: float) -> list:
+    """One naive camera per view; view k orbits angles[k] degrees about the volume centre."""
+    from .se3 import rigid
+    cams = []
+    for a in angles:
+        cam = camera_for(1536, 0.194, ds)
+        if a != 0.0:
+            R = np.array([[np.cos(np.radians(a)), 0.0, np.sin(np.radians(a))], [0.0, 1.0, 0.0],
+                          [-np.sin(np.radians(a)), 0.0, np.cos(np.radians(a))]])
+            c = np.array([0.0, 0.0, -SOURCE_TO_CENTRE_MM])
+            cam.set_extrins(rigid(R, c - R @ c))
+        cams.append(cam)
+    return cams
+
+
+def render_fixed(vol: Volume, cams: list, pose: np.ndarray, step: float, noise_seed: int, device: int = -1):
+    """Fixed images: DRR of each view at the ground-truth pose (GPU ray caster) plus 1 % noise."""
+    from .api import RayCasterLineIntCUDA
+    rc = RayCasterLineIntCUDA(device)
+    rc.set_volume(vol)
+    rc.set_camera_models(cams)
+    rc.set_ray_step_size(step)
+    rc.set_num_projs(len(cams))
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(pose[None])
+    rc.compute()
+    imgs = rc.projs()
+    rc.close()
+    return [add_noise(imgs[v], 0.01, noise_seed + v) for v in range(len(cams))]
