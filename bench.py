@@ -49,6 +49,8 @@ def _args():
     p.add_argument("--voxel", default="f32", choices=["f32", "f16", "bf16"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true")
+    p.add_argument("--serving-requests", type=int, default=10, help="requests in the serving measurement (0 = off)")
+    p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving measurement")
     p.add_argument("--launch-config", default="auto",
                    help="DRR kernel configuration 'layout,block_warps_x,unroll' (layout 0 linear, 1 cell8) "
                         "instead of the autotuner's choice")
@@ -402,7 +404,96 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
                                           "max_abs_sim_diff_vs_f32": float(
                                               np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
         objh.close()
+    for key, fn in (("uneven_multi_job", lambda: _multi_job(xr, dev)),
+                    ("serving", lambda: _serving(dev, a.serving_requests, a.serving_rate))):
+        if key == "serving" and a.serving_requests <= 0:
+            continue
+        try:
+            out[key] = fn()
+        except Exception as e:  # reported, never fatal to the headline line
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
     return out
+
+
+def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
+    """8 concurrent registrations of uneven size (volumes 192^3 .. 512x512x300,
+    1-3 views, detector 4x or 8x downsampled, lambda 20-100; FP16 volumes), one
+    population per job per optimizer step: one job-set call (one persistent DRR
+    launch) per step versus the same populations evaluated job by job."""
+    from xreg_gb300 import synth
+    specs = synth.uneven_job_specs(njobs, seed=4)
+    objs, poses_sets, total = [], [], 0
+    for sp in specs:
+        vol = synth.phantom_volume(sp.size, sp.spacing, sp.seed)
+        cams = synth.view_cameras(sp.view_angles, sp.ds_first)
+        gt = synth.gt_pose(vol)
+        fixed = synth.render_fixed(vol, cams, gt, 0.5, sp.seed, dev)
+        rc = xr.RayCasterLineIntCUDA(dev)
+        rc.set_volume(vol, 1)
+        rc.set_camera_models(cams)
+        rc.set_ray_step_size(0.5)
+        ms = []
+        for f in fixed:
+            m = xr.ImgSimMetric2DGradNCCCUDA(dev)
+            m.set_fixed_image(f)
+            ms.append(m)
+        objs.append(xr.PopulationObjective(rc, ms, sp.pop))
+        poses_sets.append([synth.sample_poses(vol, gt, sp.pop, 10.0, 20.0, seed=sp.seed + 100 + k)
+                           for k in range(steps + 1)])
+        total += sp.pop
+    js = xr.JobSet(dev)
+    js.eval(objs, [p[0] for p in poses_sets])  # warm-up
+    for o, p in zip(objs, poses_sets):
+        o.eval(p[0])
+    t0 = time.perf_counter()
+    for k in range(1, steps + 1):
+        mixed = js.eval(objs, [p[k] for p in poses_sets])
+    t_mixed = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for k in range(1, steps + 1):
+        alone = [o.eval(p[k]) for o, p in zip(objs, poses_sets)]
+    t_alone = time.perf_counter() - t0
+    same = all(np.array_equal(x, y) for x, y in zip(mixed, alone))
+    return {"value": round(steps * total / t_mixed, 2), "unit": "poses/s",
+            "one_job_at_a_time": round(steps * total / t_alone, 2),
+            "ms_per_step": round(1e3 * t_mixed / steps, 3), "jobs": njobs, "poses_per_step": total,
+            "identical_to_alone": bool(same),
+            "job_shapes": [f"{s.size[0]}x{s.size[1]}x{s.size[2]} v{len(s.view_angles)} "
+                           f"ds{int(round(1 / s.ds_first))} pop{s.pop}" for s in specs],
+            "how": "host poses in, host values out, one job-set call per step (wall clock)"}
+
+
+def _serving(dev, n_req: int, rate: float):
+    """Poisson arrivals of n_req two-level registrations (8x CMA-ES 150 iterations,
+    then 4x 100 iterations with lambda 8; grad-NCC; FP16 volumes; sizes as the
+    uneven multi-job workload).  Requests are prepared before the clock starts;
+    latency runs from arrival to completion and includes the volume upload."""
+    from xreg_gb300 import synth
+    from xreg_gb300.regi import pose_error
+    from xreg_gb300.serving import RegistrationServer
+    specs = synth.uneven_job_specs(n_req, seed=5)
+    jobs, gts = [], []
+    for sp in specs:
+        sp.ds_first = 0.125
+        job, gt = synth.job_registration(sp, iters=(150, 100), level2_pop=8, voxel_type=1, device=dev)
+        jobs.append(job)
+        gts.append(gt)
+    rng = np.random.default_rng(6)
+    offsets = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    srv = RegistrationServer(dev, hbm_budget_bytes=180e9)
+    t0 = time.perf_counter()
+    st = srv.run(arrivals=list(zip(offsets.tolist(), jobs)))
+    makespan = time.perf_counter() - t0
+    errs = [pose_error(j.final_pose, g, j.vol) for j, g in zip(jobs, gts)]
+    s = st.summary()
+    return {"p50_latency_s": round(s["p50_s"], 3), "p99_latency_s": round(s["p99_s"], 3),
+            "registrations_per_s": round(n_req / makespan, 3), "arrival_rate_per_s": rate, "requests": n_req,
+            "poses_evaluated": s["poses_evaluated"], "server_steps": s["steps"], "max_active": s["max_active"],
+            "max_footprint_gb": round(s["max_footprint_gb"], 2),
+            "pose_error_deg_median": round(float(np.median([e[0] for e in errs])), 4),
+            "pose_error_mm_median": round(float(np.median([e[1] for e in errs])), 4),
+            "pose_error_deg_max": round(float(np.max([e[0] for e in errs])), 4),
+            "pose_error_mm_max": round(float(np.max([e[1] for e in errs])), 4)}
 
 
 def _barrier(world):

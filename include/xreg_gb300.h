@@ -180,6 +180,12 @@ XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t layout, int32_
 XR_API xr_status xr_rc_get_launch_config(xr_raycaster rc, int32_t* layout, int32_t* block_warps_x, int32_t* unroll);
 /* Whether set_volumes also builds the CELL8 copy (default 1).  Set before set_volumes. */
 XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable);
+/* Empty-space skipping for the line-integral sum (default 1): samples whose
+ * trilinear cell lies outside the bounding box of the volume's non-zero voxels
+ * add exactly zero, so they are not loaded; positions still advance by the same
+ * float additions, so the DRR is bit-identical with skipping on or off and equal
+ * to xReg's sample-by-sample sum.  The max kernel never skips. */
+XR_API xr_status xr_rc_set_empty_space_skipping(xr_raycaster rc, int32_t enable);
 
 /* ------------------------------------------------------ similarity metric -- */
 /* Replaces ImgSimMetric2D{NCC,GradNCC,PatchNCC,PatchGradNCC}{CPU,OCL}

@@ -248,3 +248,41 @@ def test_cell_layout_can_be_disabled(xr):
     rc.set_launch_config(1, 2, 1)
     with pytest.raises(_lib.XRegError):
         rc.compute()
+
+
+@pytest.mark.parametrize("vt", [0, 1])
+def test_empty_space_skipping_is_exact(xr, oracle, vt):
+    """Skipping samples outside the non-zero voxels' bounding box changes no bit,
+    for every layout; the body is padded with air on every side, rays cross the
+    air, graze the body edge and miss it."""
+    vol = synth.phantom_volume((56, 60, 52), (1.5, 1.5, 1.5), 12)
+    big = np.zeros((72, 80, 76), np.float32)  # extra air around the phantom
+    big[10:62, 8:68, 12:68] = vol.voxels
+    vol = xr.Volume(big, spacing=(1.5, 1.5, 1.5))
+    cam = small_camera((48, 56), 3.0)
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 4, 15.0, 25.0, seed=3)
+    rc = _rc(xr, vol, [cam], 0.5, vt)
+    rc.set_num_projs(4)
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(poses)
+    rc.set_count_samples(True)
+    outs = []
+    for skip in (False, True):
+        rc.set_empty_space_skipping(skip)
+        for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
+            rc.set_launch_config(layout, 2, 2)
+            rc.compute()
+            outs.append((rc.projs(), rc.last_num_samples()))
+    for img, ns in outs[1:]:
+        np.testing.assert_array_equal(img, outs[0][0])
+        assert ns == outs[0][1]
+    o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=0.5)
+    rel, zero = drr_rel_err(outs[-1][0], o)
+    assert zero == 0.0 and rel <= (TOL32 if vt == 0 else TOL16)
+    # an all-zero volume: every ray sums to exactly zero
+    rz = _rc(xr, xr.Volume(np.zeros((20, 20, 20), np.float32)), [cam], 0.5, vt)
+    rz.set_num_projs(1)
+    rz.allocate_resources()
+    rz.distribute_xforms_among_cam_models(synth.gt_pose(vol)[None])
+    rz.compute()
+    assert (rz.projs() == 0).all()

@@ -260,6 +260,9 @@ class RayCasterLineIntCUDA:
     def set_build_cell_layout(self, enable: bool) -> None:
         call("xr_rc_set_build_cell_layout", self._h, int(bool(enable)))
 
+    def set_empty_space_skipping(self, enable: bool) -> None:
+        call("xr_rc_set_empty_space_skipping", self._h, int(bool(enable)))
+
     def compute(self, vol_idx: int = 0) -> None:
         call("xr_rc_compute", self._h, int(vol_idx))
 

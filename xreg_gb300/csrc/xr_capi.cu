@@ -145,7 +145,10 @@ struct xr_raycaster_s {
     DevBuf cells;            // CELL8 copy (empty when not built)
     int32_t type = XR_VOXEL_F32;
     float inv_scale = 1.0f;
+    bool has_support = false;   // support box of the non-zero voxels (empty-space skipping)
+    float sup_lo[3] = {0, 0, 0}, sup_hi[3] = {0, 0, 0};
   };
+  bool skip_empty = true;
   bool build_cells = true;
   int32_t cfg_layout = XR_LAYOUT_AUTO, cfg_bw = 2, cfg_unroll = 1;   // requested
   int32_t last_layout = -1, last_bw = 0, last_unroll = 0;            // used by the last compute
@@ -365,6 +368,28 @@ extern "C" XR_API xr_status xr_rc_synchronize(xr_raycaster rc) {
   return XR_OK;
 }
 
+// Support box of a volume's non-zero voxels for empty-space skipping: in
+// continuous index coordinates every sample outside (min - 1 - m, max + 1 + m)
+// on some axis interpolates only zero voxels.  The margin m = 0.5 voxel covers
+// the drift of positions advanced by repeated float addition.
+static xr_status vol_support(xr_raycaster rc, xr_raycaster_s::Vol& v, const float* vox_f32, cudaStream_t s) {
+  int* d_box = reinterpret_cast<int*>(rc->d_counters.as<char>() + 32);
+  XR_CUDA_TRY(launch_support_box(vox_f32, (int)v.desc.n[0], (int)v.desc.n[1], (int)v.desc.n[2], d_box, s));
+  int box[6];
+  XR_CUDA_TRY(cudaMemcpyAsync(box, d_box, sizeof(box), cudaMemcpyDeviceToHost, s));
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
+  v.has_support = true;
+  if (box[3] < box[0]) {  // no non-zero voxel
+    for (int k = 0; k < 3; ++k) { v.sup_lo[k] = 1.0f; v.sup_hi[k] = 0.0f; }
+  } else {
+    for (int k = 0; k < 3; ++k) {
+      v.sup_lo[k] = (float)box[k] - 1.5f;
+      v.sup_hi[k] = (float)box[3 + k] + 1.5f;
+    }
+  }
+  return XR_OK;
+}
+
 static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume_desc* descs,
                                      const float* const* voxels, int32_t vt, float scale, bool on_device) {
   XR_CHECK_ARG(rc && descs && voxels && n > 0, "set_volumes: NULL argument or no volumes");
@@ -395,6 +420,8 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
         XR_CUDA_TRY(launch_build_cells(v->voxels.as<float>(), (int)d.n[0], (int)d.n[1], (int)d.n[2], vt, 1.0f,
                                        v->cells.p, s));
       }
+      xr_status st = vol_support(rc, *v, v->voxels.as<float>(), s);
+      if (st != XR_OK) return st;
     } else {
       DevBuf tmp;
       const float* src = voxels[i];
@@ -429,6 +456,8 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
         XR_CUDA_TRY(v->cells.reserve(cell_layout_bytes(d.n[0], d.n[1], d.n[2], vt)));
         XR_CUDA_TRY(launch_build_cells(src, (int)d.n[0], (int)d.n[1], (int)d.n[2], vt, sc, v->cells.p, s));
       }
+      xr_status st = vol_support(rc, *v, src, s);
+      if (st != XR_OK) return st;
       XR_CUDA_TRY(cudaStreamSynchronize(s));  // tmp is released at scope exit
     }
     vols.push_back(std::move(v));
@@ -778,6 +807,11 @@ static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, Dr
   p.vol.nz = (int32_t)vol.desc.n[2];
   p.vol.voxel_type = vol.type;
   p.vol.inv_scale = vol.inv_scale;
+  p.vol.has_support = (rc->skip_empty && vol.has_support) ? 1 : 0;
+  for (int k = 0; k < 3; ++k) {
+    p.vol.sup_lo[k] = vol.sup_lo[k];
+    p.vol.sup_hi[k] = vol.sup_hi[k];
+  }
   p.geo = rc->d_geo.as<ProjGeom>();
   p.cam_idx = rc->d_cam_idx.as<int32_t>();
   p.bg_projs = rc->use_bg ? rc->d_bg.as<float>() : nullptr;
@@ -837,6 +871,13 @@ extern "C" XR_API xr_status xr_rc_get_launch_config(xr_raycaster rc, int32_t* la
   *layout = rc->last_layout;
   *bw = rc->last_bw;
   *unroll = rc->last_unroll;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_empty_space_skipping(xr_raycaster rc, int32_t enable) {
+  XR_CHECK_ARG(rc, "set_empty_space_skipping: NULL handle");
+  rc->skip_empty = enable != 0;
+  rc->generation++;
   return XR_OK;
 }
 

@@ -36,6 +36,11 @@ struct VolView {
   int32_t voxel_type;
   int32_t layout;      // XR_LAYOUT_LINEAR / XR_LAYOUT_CELL8
   float inv_scale;     // multiplies the ray sum (1 for F32)
+  // Support box: every sample whose continuous index lies outside
+  // (sup_lo, sup_hi) on some axis interpolates only zero voxels.  has_support 0
+  // disables sample skipping; an all-zero volume has an empty box (lo > hi).
+  int32_t has_support;
+  float sup_lo[3], sup_hi[3];
 };
 
 // Launch parameters of a DRR kernel.
@@ -80,6 +85,8 @@ cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long tot
                              unsigned long long* d_counter, int blocks, cudaStream_t s);
 // Blocks that fill the current device once (SMs x resident blocks per SM).
 int drr_multi_blocks();
+// Index bounds of the non-zero voxels into d_box[6] (min xyz, max xyz; max < min if none).
+cudaError_t launch_support_box(const float* vox_f32, int nx, int ny, int nz, int* d_box, cudaStream_t s);
 // Bytes of the CELL8 copy of a volume, and the kernel that builds it from float32 voxels.
 size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type);
 cudaError_t launch_build_cells(const float* vox_f32, int nx, int ny, int nz, int32_t voxel_type, float scale,

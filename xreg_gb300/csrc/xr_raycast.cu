@@ -193,9 +193,41 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
       const float sx = __fmul_rn(dir[0], sc), sy = __fmul_rn(dir[1], sc), sz = __fmul_rn(dir[2], sc);
       const void* data = (LAYOUT != XR_LAYOUT_LINEAR) ? p.vol.cells : p.vol.voxels;
       const float bx = maxb[0], by = maxb[1], bz = maxb[2];
+      // Samples [first, last] may touch non-zero voxels; the others interpolate
+      // only zeros, so for the sum they add exactly +0 and need no load.  The
+      // samples before `first` still advance the position by the same float
+      // additions, so every sampled position is the one the reference uses.
+      unsigned int first = 0, last = (unsigned int)nsteps;
+      if (KERNEL == XR_LINE_INT_SUM && p.vol.has_support && hit) {
+        float lo = 0.0f, hi = (float)nsteps;
+        if (p.vol.sup_lo[0] > p.vol.sup_hi[0]) hi = -1.0f;  // all-zero volume
+        const float st[3] = {sx, sy, sz}, p0[3] = {px, py, pz};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (fabsf(st[k]) > 1.0e-20f) {
+            float a = (p.vol.sup_lo[k] - p0[k]) / st[k], b = (p.vol.sup_hi[k] - p0[k]) / st[k];
+            if (a > b) { const float t = a; a = b; b = t; }
+            lo = fmaxf(lo, a);
+            hi = fminf(hi, b);
+          } else if (!(p0[k] > p.vol.sup_lo[k] && p0[k] < p.vol.sup_hi[k])) {
+            hi = -1.0f;
+          }
+        }
+        if (!(lo <= hi)) {
+          last = 0;
+          first = 1;  // no sample can be non-zero
+        } else {
+          const float f0 = floorf(lo) - 1.0f, f1 = ceilf(hi) + 1.0f;
+          first = f0 > 0.0f ? (unsigned int)f0 : 0u;
+          last = f1 < (float)nsteps ? (unsigned int)f1 : (unsigned int)nsteps;
+        }
+      }
       if (hit) {
-        // samples 0..nsteps in order; the sum order never changes with UNROLL
-        unsigned int n = (unsigned int)nsteps + 1u;
+        for (unsigned int s = 0; s < first && s <= last; ++s) {
+          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+        }
+        // samples first..last in order; the sum order never changes with UNROLL
+        unsigned int n = first <= last ? last - first + 1u : 0u;
         if (UNROLL == 2) {
           for (; n >= 2; n -= 2) {
             const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
@@ -382,6 +414,42 @@ cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
     case XR_VOXEL_BF16: return launch_kernel_id<XR_VOXEL_BF16>(p, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+__global__ void support_init_kernel(int* box) {
+  if (threadIdx.x < 3) box[threadIdx.x] = 0x7fffffff;
+  else if (threadIdx.x < 6) box[threadIdx.x] = -1;
+}
+
+// Index bounds of the non-zero voxels: box = (min x, min y, min z, max x, max y, max z).
+__global__ void support_box_kernel(const float* __restrict__ vox, int nx, int ny, int nz, int* box) {
+  int mn[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, mx[3] = {-1, -1, -1};
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (vox[i] != 0.0f) {
+      const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
+      mn[0] = min(mn[0], x); mn[1] = min(mn[1], y); mn[2] = min(mn[2], z);
+      mx[0] = max(mx[0], x); mx[1] = max(mx[1], y); mx[2] = max(mx[2], z);
+    }
+  }
+  for (int k = 0; k < 3; ++k) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[k] = min(mn[k], __shfl_down_sync(0xffffffffu, mn[k], o));
+      mx[k] = max(mx[k], __shfl_down_sync(0xffffffffu, mx[k], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int k = 0; k < 3; ++k) {
+      atomicMin(&box[k], mn[k]);
+      atomicMax(&box[3 + k], mx[k]);
+    }
+  }
+}
+
+cudaError_t launch_support_box(const float* vox_f32, int nx, int ny, int nz, int* d_box, cudaStream_t s) {
+  support_init_kernel<<<1, 32, 0, s>>>(d_box);
+  support_box_kernel<<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, d_box);
+  return cudaGetLastError();
 }
 
 int drr_multi_blocks() {

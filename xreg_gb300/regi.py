@@ -26,7 +26,7 @@ import numpy as np
 
 from . import api
 from .cmaes import CMAES
-from .se3 import exp_se3
+from .se3 import exp_se3_batch
 
 METRICS = {
     "ncc": api.ImgSimMetric2DNCCCUDA,
@@ -125,9 +125,8 @@ class Registration:
         self.es.set_stop(tol_fun=L.tol_fun, tol_x=L.tol_x, max_iter=L.max_iters)
 
     def poses_of(self, xs: np.ndarray) -> np.ndarray:
-        A = self.C
         B = self.Ci @ self.start_pose
-        return np.stack([A @ exp_se3(x) @ B for x in xs])
+        return np.einsum("ij,njk,kl->nil", self.C, exp_se3_batch(xs), B)
 
     # ---------------------------------------------------------- stepping
     def propose(self) -> np.ndarray:

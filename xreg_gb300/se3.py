@@ -65,3 +65,29 @@ def rigid_inv(T: np.ndarray) -> np.ndarray:
 def rot_angle_deg(R: np.ndarray) -> float:
     c = (np.trace(R) - 1.0) * 0.5
     return float(np.degrees(np.arccos(np.clip(c, -1.0, 1.0))))
+
+
+def exp_se3_batch(xs) -> np.ndarray:
+    """exp_se3 of every row of xs ([n, 6]) at once -> [n, 4, 4]."""
+    xs = np.asarray(xs, dtype=np.float64).reshape(-1, 6)
+    n = xs.shape[0]
+    w, v = xs[:, :3], xs[:, 3:]
+    th = np.linalg.norm(w, axis=1)
+    W = np.zeros((n, 3, 3))
+    W[:, 0, 1], W[:, 0, 2] = -w[:, 2], w[:, 1]
+    W[:, 1, 0], W[:, 1, 2] = w[:, 2], -w[:, 0]
+    W[:, 2, 0], W[:, 2, 1] = -w[:, 1], w[:, 0]
+    WW = W @ W
+    big = th > 1.0e-14
+    ths = np.where(big, th, 1.0)
+    a = np.where(big, np.sin(ths) / ths, 1.0)
+    b = np.where(big, (1.0 - np.cos(ths)) / ths ** 2, 0.0)
+    c = np.where(big, (ths - np.sin(ths)) / ths ** 3, 0.0)
+    I = np.eye(3)[None]
+    R = np.where(big[:, None, None], I + a[:, None, None] * W + b[:, None, None] * WW, I)
+    A = np.where(big[:, None, None], I + b[:, None, None] * W + c[:, None, None] * WW, I)
+    T = np.zeros((n, 4, 4))
+    T[:, :3, :3] = R
+    T[:, :3, 3] = np.einsum("nij,nj->ni", A, v)
+    T[:, 3, 3] = 1.0
+    return T
