@@ -43,6 +43,24 @@ XR_API xr_status xr_cmaes_test_termination(xr_cmaes e, int32_t* reason);
 XR_API xr_status xr_cmaes_get(xr_cmaes e, double* mean, double* best_x, double* best_f, double* sigma,
                               int64_t* generation);
 
+/* Bound-constrained model-based trust-region optimizer for a final level, in
+ * place of NLopt's LN_BOBYQA (Intensity2D3DRegiBOBYQA, xregIntensity2D3DRegiBOBYQA.cpp:28-39;
+ * Intensity2D3DRegiNLOptInterface::run, xregIntensity2D3DRegiNLOptInterface.cpp:83-188):
+ * 2n+1-point quadratic models around the best point, box-constrained trust-region
+ * steps, rho halved on stalls, stop at rho_end or max_iter.  Each iteration asks
+ * for one batch of up to 2*dim+2 points (evaluate them together) and is told
+ * their values in the same order. */
+typedef struct xr_dfo_s* xr_dfo;
+XR_API xr_status xr_dfo_create(int32_t dim, const double* x0, const double* lower, const double* upper,
+                               double rho_beg, double rho_end, int64_t max_iter, xr_dfo* out);
+XR_API xr_status xr_dfo_destroy(xr_dfo d);
+/* Writes the batch (rows of dim doubles) into pts, room for 2*dim+2 rows; *count = rows. */
+XR_API xr_status xr_dfo_ask(xr_dfo d, double* pts, int32_t* count);
+XR_API xr_status xr_dfo_tell(xr_dfo d, const double* fvals);
+/* *reason: 0 continue, 2 rho below rho_end, 3 iteration limit. */
+XR_API xr_status xr_dfo_test_termination(xr_dfo d, int32_t* reason);
+XR_API xr_status xr_dfo_get(xr_dfo d, double* best_x, double* best_f, double* rho, int64_t* iterations);
+
 /* Job set: evaluates one population for each of several registrations (each an
  * xr_objective with its own volume, cameras, fixed images and population size)
  * with ONE persistent DRR launch over all their (tile, projection) work items,

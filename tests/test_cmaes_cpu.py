@@ -86,3 +86,33 @@ def test_reproducible_and_validated(xr):
         CMAES(np.ones(3), np.array([1.0, 0.0, 1.0]), 8)
     with pytest.raises(_lib.XRegError):
         CMAES(np.ones(3), np.ones(3), 1)
+
+
+def _run_dfo(f, x0, lo, hi, rho_beg, rho_end, max_iter=500):
+    from xreg_gb300.cmaes import TrustRegionDFO
+    d = TrustRegionDFO(x0, lo, hi, rho_beg, rho_end, max_iter)
+    n_eval = 0
+    while d.test_for_termination() is None:
+        pts = d.ask()
+        assert np.all(pts >= lo - 1e-12) and np.all(pts <= hi + 1e-12)
+        d.tell([f(p) for p in pts])
+        n_eval += len(pts)
+    return d.state(), n_eval
+
+
+def test_trust_region_dfo_on_quadratics_and_rosenbrock(xr):
+    scale = np.array([0.1, 0.1, 0.1, 10.0, 10.0, 10.0])
+    target = np.array([0.02, -0.03, 0.01, 2.0, -3.0, 4.0])
+    lo, hi = -2.5 * scale, 2.5 * scale
+    f = lambda x: float(np.sum(((x - target) / scale) ** 2) + 0.3 * ((x[0] - target[0]) / scale[0]) *
+                        ((x[4] - target[4]) / scale[4]))
+    st, ne = _run_dfo(f, np.zeros(6), lo, hi, 0.2, 1e-6)
+    np.testing.assert_allclose(st["best_x"], target, atol=1e-4 * 10)
+    assert st["best_f"] < f(np.zeros(6)) * 1e-6
+    # a bound-active optimum: the solution sits on the box
+    g = lambda x: float(np.sum((x - 3.0) ** 2))
+    st2, _ = _run_dfo(g, np.zeros(3), -np.ones(3), np.ones(3), 0.5, 1e-7)
+    np.testing.assert_allclose(st2["best_x"], np.ones(3), atol=1e-9)
+    # Rosenbrock in 4-D from a bounded start
+    st3, _ = _run_dfo(rosenbrock, np.full(4, -0.5), -2 * np.ones(4), 2 * np.ones(4), 0.5, 1e-9, max_iter=4000)
+    assert st3["best_f"] < 1e-3, st3

@@ -117,6 +117,12 @@ _SIGS = {
     "xr_cmaes_update_distribution": [H, P],
     "xr_cmaes_test_termination": [H, C.POINTER(i32)],
     "xr_cmaes_get": [H, P, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
+    "xr_dfo_create": [i32, P, P, P, f64, f64, i64, C.POINTER(H)],
+    "xr_dfo_destroy": [H],
+    "xr_dfo_ask": [H, P, C.POINTER(i32)],
+    "xr_dfo_tell": [H, P],
+    "xr_dfo_test_termination": [H, C.POINTER(i32)],
+    "xr_dfo_get": [H, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
     "xr_jobset_create": [i32, C.POINTER(H)],
     "xr_jobset_destroy": [H],
     "xr_jobset_set_stream": [H, P],

@@ -76,3 +76,46 @@ class CMAES:
         call("xr_cmaes_get", self._h, mean.ctypes.data_as(C.c_void_p), best.ctypes.data_as(C.c_void_p), C.byref(bf),
              C.byref(sg), C.byref(gen))
         return {"mean": mean, "best_x": best, "best_f": bf.value, "sigma": sg.value, "generation": gen.value}
+
+
+class TrustRegionDFO:
+    """Bound-constrained model-based trust-region optimizer (xr_dfo_*), the
+    final-level optimizer in place of xReg's NLopt LN_BOBYQA; batch ask / tell."""
+
+    def __init__(self, x0, lower, upper, rho_beg: float, rho_end: float, max_iter: int):
+        load()
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        lo = np.ascontiguousarray(lower, dtype=np.float64)
+        hi = np.ascontiguousarray(upper, dtype=np.float64)
+        h = C.c_void_p()
+        call("xr_dfo_create", int(x0.size), x0.ctypes.data_as(C.c_void_p), lo.ctypes.data_as(C.c_void_p),
+             hi.ctypes.data_as(C.c_void_p), float(rho_beg), float(rho_end), int(max_iter), C.byref(h))
+        self._h = h
+        self.n = int(x0.size)
+        self._buf = np.zeros((2 * self.n + 2, self.n))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load().xr_dfo_destroy(h)
+            self._h = None
+
+    def ask(self) -> np.ndarray:
+        cnt = C.c_int32()
+        call("xr_dfo_ask", self._h, self._buf.ctypes.data_as(C.c_void_p), C.byref(cnt))
+        return self._buf[:cnt.value].copy()
+
+    def tell(self, fvals) -> None:
+        f = np.ascontiguousarray(fvals, dtype=np.float64)
+        call("xr_dfo_tell", self._h, f.ctypes.data_as(C.c_void_p))
+
+    def test_for_termination(self):
+        r = C.c_int32()
+        call("xr_dfo_test_termination", self._h, C.byref(r))
+        return {0: None, 2: "rho_end", 3: "max_iter"}.get(r.value, "unknown")
+
+    def state(self) -> dict:
+        x = np.zeros(self.n)
+        bf, rho, it = C.c_double(), C.c_double(), C.c_int64()
+        call("xr_dfo_get", self._h, x.ctypes.data_as(C.c_void_p), C.byref(bf), C.byref(rho), C.byref(it))
+        return {"best_x": x, "best_f": bf.value, "rho": rho.value, "iterations": it.value}

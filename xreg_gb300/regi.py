@@ -25,8 +25,11 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import api
-from .cmaes import CMAES
+from .cmaes import CMAES, TrustRegionDFO
 from .se3 import exp_se3_batch
+
+# Bounds of xReg's single-view BOBYQA level (+-2.5 deg rotations, +-5, 5, 10 mm).
+DFO_BOUNDS = np.array([np.radians(2.5)] * 3 + [5.0, 5.0, 10.0])
 
 METRICS = {
     "ncc": api.ImgSimMetric2DNCCCUDA,
@@ -51,6 +54,12 @@ class RegiLevel:
     max_iters: int = 100
     tol_fun: float = 1e-6
     tol_x: float = 1e-6
+    # "cmaes" (Intensity2D3DRegiCMAES) or "dfo": the bound-constrained model
+    # trust region used where xReg runs NLopt's BOBYQA; for "dfo" the bounds
+    # default to xReg's single-view app (+-2.5 deg, +-5/5/10 mm) and rho is in mm
+    optimizer: str = "cmaes"
+    rho_beg: float = 2.0
+    rho_end: float = 0.01
 
 
 @dataclass
@@ -97,7 +106,8 @@ class Registration:
         lev = 0
         for L in self.levels:
             r, c = L.cams[0].num_det_rows, L.cams[0].num_det_cols
-            per = len(L.cams) * L.pop * r * c * 4 + len(L.cams) * r * c * 4 * 6 + len(L.cams) * L.pop * 2048 * 8
+            pop = 14 if L.optimizer == "dfo" else L.pop
+            per = len(L.cams) * pop * r * c * 4 + len(L.cams) * r * c * 4 * 6 + len(L.cams) * pop * 2048 * 8
             lev = max(lev, per)
         return int(vol + lev + (16 << 20))
 
@@ -120,9 +130,14 @@ class Registration:
             ms.append(m)
         if self.obj is not None:
             self.obj.close()
-        self.obj = api.PopulationObjective(self.rc, ms, L.pop)
-        self.es = CMAES(np.zeros(6), L.sigma, L.pop, seed=self.seed * 1009 + k)
-        self.es.set_stop(tol_fun=L.tol_fun, tol_x=L.tol_x, max_iter=L.max_iters)
+        if L.optimizer == "dfo":
+            b = DFO_BOUNDS if L.bounds is None else np.asarray(L.bounds, dtype=np.float64)
+            self.obj = api.PopulationObjective(self.rc, ms, 2 * 6 + 2)
+            self.es = TrustRegionDFO(np.zeros(6), -b, b, L.rho_beg, L.rho_end, L.max_iters)
+        else:
+            self.obj = api.PopulationObjective(self.rc, ms, L.pop)
+            self.es = CMAES(np.zeros(6), L.sigma, L.pop, seed=self.seed * 1009 + k)
+            self.es.set_stop(tol_fun=L.tol_fun, tol_x=L.tol_x, max_iter=L.max_iters)
 
     def poses_of(self, xs: np.ndarray) -> np.ndarray:
         B = self.Ci @ self.start_pose
@@ -132,17 +147,25 @@ class Registration:
     def propose(self) -> np.ndarray:
         """Samples the current level's population; returns its poses [pop, 4, 4]."""
         L = self.levels[self.level]
-        self._pop_x = self.es.sample_within_bounds(L.bounds).copy()
+        if L.optimizer == "dfo":
+            self._pop_x = self.es.ask()
+        else:
+            self._pop_x = self.es.sample_within_bounds(L.bounds).copy()
         return self.poses_of(self._pop_x)
 
     def tell(self, values) -> None:
-        self.es.update_distribution(np.asarray(values, dtype=np.float64))
+        L = self.levels[self.level]
+        if L.optimizer == "dfo":
+            self.es.tell(np.asarray(values, dtype=np.float64))
+        else:
+            self.es.update_distribution(np.asarray(values, dtype=np.float64))
         stop = self.es.test_for_termination()
         if stop is not None:
             st = self.es.state()
             x = st["best_x"]
             pose = self.poses_of(x[None])[0]
-            self.results.append(LevelResult(pose, x, st["best_f"], st["generation"], stop))
+            gens = st.get("generation", st.get("iterations", 0))
+            self.results.append(LevelResult(pose, x, st["best_f"], gens, stop))
             self.start_pose = pose
             if self.level + 1 < len(self.levels):
                 self._enter_level(self.level + 1)

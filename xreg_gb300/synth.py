@@ -199,11 +199,13 @@ def uneven_job_specs(n: int, seed: int) -> list:
 
 
 def job_registration(spec: JobSpec, levels=None, iters=(150, 100), level2_pop: int = 8, voxel_type: int = 1,
-                     step: float = 0.5, device: int = -1):
+                     step: float = 0.5, device: int = -1, level2: str = "dfo"):
     """A two-level registration request from a JobSpec: level 1 at the spec's
-    downsampling (or 8x) with CMA-ES lambda = spec.pop, level 2 at 4x with a small
-    population; fixed images rendered at a ground-truth pose, start pose perturbed
-    from it by N(0, 5 deg) / N(0, 10 mm).  Returns (Registration, ground truth)."""
+    downsampling (or 8x) with CMA-ES lambda = spec.pop, level 2 at 4x with the
+    bound-constrained trust-region optimizer (level2 "dfo", xReg's BOBYQA level)
+    or a small CMA-ES (level2 "cmaes", lambda = level2_pop); fixed images rendered
+    at a ground-truth pose, start pose perturbed from it by N(0, 5 deg) /
+    N(0, 10 mm).  Returns (Registration, ground truth)."""
     from .regi import Registration, RegiLevel
     vol = phantom_volume(spec.size, spec.spacing, spec.seed)
     rng = np.random.default_rng(spec.seed + 1)
@@ -216,6 +218,8 @@ def job_registration(spec: JobSpec, levels=None, iters=(150, 100), level2_pop: i
         fixed = render_fixed(vol, cams, gt, step, spec.seed + 17 * (k + 1), device)
         if k == 0:
             lv.append(RegiLevel(cams, fixed, "grad_ncc", pop=spec.pop, max_iters=iters[0]))
+        elif level2 == "dfo":
+            lv.append(RegiLevel(cams, fixed, "grad_ncc", optimizer="dfo", max_iters=iters[min(k, len(iters) - 1)]))
         else:
             sig = np.array([np.radians(1.5)] * 3 + [3.0] * 3)
             lv.append(RegiLevel(cams, fixed, "grad_ncc", pop=level2_pop, sigma=sig,
