@@ -61,6 +61,23 @@ XR_API xr_status xr_dfo_tell(xr_dfo d, const double* fvals);
 XR_API xr_status xr_dfo_test_termination(xr_dfo d, int32_t* reason);
 XR_API xr_status xr_dfo_get(xr_dfo d, double* best_x, double* best_f, double* rho, int64_t* iterations);
 
+/* ---------------------------------------------------- data preparation -- */
+/* HUToLinAttFilter (lib/image/xregHUToLinAtt.cpp:45-69): device float HU ->
+ * device float attenuation (1/mm), mu_water 0.02683, mu_air 0.02485e-4,
+ * hu_lower -1000, computed in double; asynchronous on cuda_stream. */
+XR_API xr_status xr_hu_to_lin_att(const float* d_hu, int64_t n, float* d_mu, void* cuda_stream);
+/* Output size of DownsampleImage: floor(n * factor + 0.5) per axis, 0 < factor <= 1. */
+XR_API xr_status xr_downsample_image_size(int64_t rows, int64_t cols, double factor, int64_t* out_rows,
+                                          int64_t* out_cols);
+/* DownsampleProjData's image part (lib/image/xregProjData.cpp:40-53 ->
+ * DownsampleImage, lib/itk/xregITKResampleUtils.h:51-131): discrete Gaussian of
+ * variance (0.5/factor)^2 pixels (max error 0.01, replicated edges) when
+ * factor < 1, then bilinear resampling at continuous index i / factor onto the
+ * xr_downsample_image_size grid.  d_scratch: 2 * rows * cols doubles.  The camera
+ * model of the level comes from xr_camera_downsample.  Asynchronous. */
+XR_API xr_status xr_downsample_image(const float* d_src, int64_t rows, int64_t cols, double factor,
+                                     double* d_scratch, float* d_dst, void* cuda_stream);
+
 /* Job set: evaluates one population for each of several registrations (each an
  * xr_objective with its own volume, cameras, fixed images and population size)
  * with ONE persistent DRR launch over all their (tile, projection) work items,

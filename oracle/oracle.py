@@ -279,3 +279,22 @@ class RefCMAES:
         if getattr(self, "h", None):
             RefCMAES._lib.xo_cmaes_free(self.h)
             self.h = None
+
+
+def discrete_gaussian_taps(variance, max_error=0.01, max_width=32):
+    out = np.zeros(64)
+    L = lib()
+    L.xo_discrete_gaussian_taps.argtypes = [C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_int]
+    L.xo_discrete_gaussian_taps.restype = C.c_int
+    r = L.xo_discrete_gaussian_taps(variance, max_error, max_width, _p(out), 64)
+    return out[:r + 1].copy()
+
+
+def downsample_image(img, factor):
+    src = np.ascontiguousarray(img, dtype=np.float32)
+    orows, ocols = int(src.shape[0] * factor + 0.5), int(src.shape[1] * factor + 0.5)
+    dst = np.zeros((orows, ocols), np.float32)
+    L = lib()
+    L.xo_downsample_image.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p]
+    assert L.xo_downsample_image(_p(src), src.shape[0], src.shape[1], factor, _p(dst)) == 0
+    return dst

@@ -831,3 +831,90 @@ XO_EXPORT void xo_hu_to_lin_att(const float* hu, int64_t n, float* out) {
     out[i] = (float)(v > 0.0 ? v : 0.0);
   }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Fixed-image downsampling (DownsampleImage, lib/itk/xregITKResampleUtils.h:51-131) */
+/* ------------------------------------------------------------------------- */
+/* Discrete Gaussian taps as ITK's GaussianOperator builds them: e^{-t} I0(t),
+ * e^{-t} I1(t), then the Bessel recurrence c_k = c_{k-2} - 2 (k-1) / t c_{k-1},
+ * accumulated until c_0 + 2 sum c_k >= 1 - max_error (or max_width one-sided taps),
+ * normalised to sum one.  I0 and I1 are summed from their power series here. */
+static double xo_bessel_i_series(int k, double t) {
+  double term = 1.0;
+  for (int j = 1; j <= k; ++j) term *= (0.5 * t) / j;
+  double s = term;
+  const double q = 0.25 * t * t;
+  for (int m = 1; m < 500; ++m) {
+    term *= q / ((double)m * (double)(m + k));
+    s += term;
+    if (term < 1e-18 * s) break;
+  }
+  return s;
+}
+
+XO_EXPORT int xo_discrete_gaussian_taps(double variance, double max_error, int max_width, double* out, int cap_len) {
+  const double et = exp(-variance);
+  int n = 0;
+  out[n++] = et * xo_bessel_i_series(0, variance);
+  double sum = out[0];
+  out[n++] = et * xo_bessel_i_series(1, variance);
+  sum += 2.0 * out[1];
+  for (int i = 2; sum < 1.0 - max_error && n < cap_len; ++i) {
+    out[n] = out[i - 2] - 2.0 * (i - 1) / variance * out[i - 1];
+    sum += 2.0 * out[n];
+    ++n;
+    if (n > max_width) break;
+  }
+  for (int i = 0; i < n; ++i) out[i] /= sum;
+  return n - 1;  /* radius */
+}
+
+/* dst: floor(rows*factor+0.5) x floor(cols*factor+0.5) floats. */
+XO_EXPORT int xo_downsample_image(const float* src, int64_t rows, int64_t cols, double factor, float* dst) {
+  const int64_t orows = (int64_t)((double)rows * factor + 0.5), ocols = (int64_t)((double)cols * factor + 0.5);
+  const int64_t n = rows * cols;
+  double* a = (double*)malloc(sizeof(double) * (size_t)n);
+  double* b = (double*)malloc(sizeof(double) * (size_t)n);
+  double taps[64];
+  int radius = 0;
+  taps[0] = 1.0;
+  if (factor < 1.0) {
+    const double sigma = 0.5 / factor;
+    radius = xo_discrete_gaussian_taps(sigma * sigma, 0.01, 32, taps, 64);
+  }
+  for (int64_t r = 0; r < rows; ++r)
+    for (int64_t c = 0; c < cols; ++c) {
+      double s = taps[0] * src[r * cols + c];
+      for (int t = 1; t <= radius; ++t) {
+        const int64_t l = c - t < 0 ? 0 : c - t, h = c + t > cols - 1 ? cols - 1 : c + t;
+        s += taps[t] * ((double)src[r * cols + l] + (double)src[r * cols + h]);
+      }
+      a[r * cols + c] = s;
+    }
+  for (int64_t r = 0; r < rows; ++r)
+    for (int64_t c = 0; c < cols; ++c) {
+      double s = taps[0] * a[r * cols + c];
+      for (int t = 1; t <= radius; ++t) {
+        const int64_t l = r - t < 0 ? 0 : r - t, h = r + t > rows - 1 ? rows - 1 : r + t;
+        s += taps[t] * (a[l * cols + c] + a[h * cols + c]);
+      }
+      b[r * cols + c] = s;
+    }
+  for (int64_t r = 0; r < orows; ++r)
+    for (int64_t c = 0; c < ocols; ++c) {
+      const double y = r / factor, x = c / factor;
+      if (x > cols - 0.5 || y > rows - 0.5) { dst[r * ocols + c] = 0.0f; continue; }
+      int64_t x0 = (int64_t)floor(x), y0 = (int64_t)floor(y), x1 = x0 + 1, y1 = y0 + 1;
+      double fx = x - x0, fy = y - y0;
+      if (x1 > cols - 1) { x1 = x0; fx = 0.0; }
+      if (y1 > rows - 1) { y1 = y0; fy = 0.0; }
+      if (x0 > cols - 1) x0 = x1 = cols - 1;
+      if (y0 > rows - 1) y0 = y1 = rows - 1;
+      const double v00 = b[y0 * cols + x0], v01 = b[y0 * cols + x1], v10 = b[y1 * cols + x0], v11 = b[y1 * cols + x1];
+      const double p = v00 + (v01 - v00) * fx, q = v10 + (v11 - v10) * fx;
+      dst[r * ocols + c] = (float)(p + (q - p) * fy);
+    }
+  free(a);
+  free(b);
+  return 0;
+}

@@ -123,6 +123,9 @@ _SIGS = {
     "xr_dfo_tell": [H, P],
     "xr_dfo_test_termination": [H, C.POINTER(i32)],
     "xr_dfo_get": [H, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
+    "xr_hu_to_lin_att": [P, i64, P, P],
+    "xr_downsample_image_size": [i64, i64, f64, C.POINTER(i64), C.POINTER(i64)],
+    "xr_downsample_image": [P, i64, i64, f64, P, P, P],
     "xr_jobset_create": [i32, C.POINTER(H)],
     "xr_jobset_destroy": [H],
     "xr_jobset_set_stream": [H, P],

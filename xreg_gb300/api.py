@@ -487,3 +487,31 @@ class JobSet:
         a, b = C.c_int64(), C.c_int32()
         call("xr_jobset_last_launch", self._h, C.byref(a), C.byref(b))
         return a.value, b.value
+
+
+# --------------------------------------------------------- data preparation
+def hu_to_lin_att_device(d_hu: int, n: int, d_mu: int, stream: int = 0) -> None:
+    """HUToLinAtt on device buffers (xr_hu_to_lin_att); asynchronous on `stream`."""
+    call("xr_hu_to_lin_att", C.c_void_p(int(d_hu)), int(n), C.c_void_p(int(d_mu)), C.c_void_p(int(stream)))
+
+
+def downsample_size(rows: int, cols: int, factor: float) -> tuple:
+    r, c = C.c_int64(), C.c_int64()
+    call("xr_downsample_image_size", int(rows), int(cols), float(factor), C.byref(r), C.byref(c))
+    return r.value, c.value
+
+
+def downsample_image(img: np.ndarray, factor: float, device: int = -1) -> np.ndarray:
+    """DownsampleProjData's image part on the GPU (discrete Gaussian + resampling)."""
+    import torch
+    dev = torch.device("cuda", device if device >= 0 else torch.cuda.current_device())
+    src = torch.from_numpy(np.ascontiguousarray(img, dtype=np.float32)).to(dev)
+    rows, cols = src.shape
+    orows, ocols = downsample_size(rows, cols, factor)
+    scratch = torch.empty(2 * rows * cols, dtype=torch.float64, device=dev)
+    dst = torch.empty((orows, ocols), dtype=torch.float32, device=dev)
+    s = torch.cuda.current_stream(dev)
+    call("xr_downsample_image", C.c_void_p(src.data_ptr()), rows, cols, float(factor),
+         C.c_void_p(scratch.data_ptr()), C.c_void_p(dst.data_ptr()), C.c_void_p(s.cuda_stream))
+    s.synchronize()
+    return dst.cpu().numpy()
