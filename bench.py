@@ -298,7 +298,7 @@ def run_ours(a, rank, world, local):
     alg_bytes = 8.0 * bvox * samples
     achieved = alg_bytes / (drr_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
-    tag = f"batched-256^3-384^2-pop100-{a.voxel}-{lname}"
+    tag = f"batched-256^3-384^2-pop100-{a.voxel}-{lname}-loop{unroll}"
     traffic = _ncu_traffic(tag)
 
     extras = {}

@@ -219,11 +219,12 @@ def test_launch_configs_are_bit_identical(xr, oracle, vt):
     rc.compute()
     auto = rc.projs()
     lay, bw, un = rc.launch_config()
-    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2)
-    # layout 2: the float32 cell copy read with one 256-bit load per sample
+    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2, 3)
+    # layout 2: the float32 cell copy read with one 256-bit load per sample;
+    # loop 3: one sample per iteration with macro-cell skipping
     for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
         for bw in (1, 2, 4, 8):
-            for un in (1, 2):
+            for un in (1, 2, 3):
                 rc.set_launch_config(layout, bw, un)
                 rc.compute()
                 assert rc.launch_config() == (layout, bw, un)
@@ -270,9 +271,10 @@ def test_empty_space_skipping_is_exact(xr, oracle, vt):
     for skip in (False, True):
         rc.set_empty_space_skipping(skip)
         for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
-            rc.set_launch_config(layout, 2, 2)
-            rc.compute()
-            outs.append((rc.projs(), rc.last_num_samples()))
+            for un in (2, 3):
+                rc.set_launch_config(layout, 2, un)
+                rc.compute()
+                outs.append((rc.projs(), rc.last_num_samples()))
     for img, ns in outs[1:]:
         np.testing.assert_array_equal(img, outs[0][0])
         assert ns == outs[0][1]
@@ -286,3 +288,42 @@ def test_empty_space_skipping_is_exact(xr, oracle, vt):
     rz.distribute_xforms_among_cam_models(synth.gt_pose(vol)[None])
     rz.compute()
     assert (rz.projs() == 0).all()
+
+
+@pytest.mark.parametrize("vt", [0, 1])
+def test_macro_cell_skipping_is_exact(xr, oracle, vt):
+    """Macro-cell skipping (loop 3) changes no bit where the bounding box does
+    not help: two blobs in opposite corners and a one-voxel sheet in between
+    leave empty macro cells inside the support box.  Covers an unperturbed
+    (axis-aligned central ray) pose, a step far below the voxel size (long jumps
+    through empty macro cells) and the oracle."""
+    ph = synth.phantom_volume((40, 36, 32), (1.5, 1.5, 1.5), 21).voxels
+    big = np.zeros((96, 88, 80), np.float32)
+    big[3:43, 4:40, 2:34] = ph
+    big[54:94, 50:86, 46:78] = ph[::-1, :, ::-1]
+    big[47, 30:60, 20:60] = 0.02  # a sheet one voxel thick
+    vol = xr.Volume(big, spacing=(1.5, 1.5, 1.5))
+    cam = small_camera((48, 56), 3.5)
+    gt = synth.gt_pose(vol)
+    poses = np.concatenate([gt[None], synth.sample_poses(vol, gt, 3, 20.0, 20.0, seed=8)])
+    for step in (0.5, 0.04):
+        rc = _rc(xr, vol, [cam], step, vt)
+        rc.set_num_projs(len(poses))
+        rc.allocate_resources()
+        rc.distribute_xforms_among_cam_models(poses)
+        rc.set_count_samples(True)
+        outs = []
+        for skip, un in ((False, 1), (True, 1), (True, 3)):
+            rc.set_empty_space_skipping(skip)
+            for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
+                rc.set_launch_config(layout, 2, un)
+                rc.compute()
+                outs.append((rc.projs(), rc.last_num_samples()))
+        assert outs[0][0].max() > 0
+        for img, ns in outs[1:]:
+            np.testing.assert_array_equal(img, outs[0][0])
+            assert ns == outs[0][1]
+        if step == 0.5:
+            o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=step)
+            rel, zero = drr_rel_err(outs[-1][0], o)
+            assert zero == 0.0 and rel <= (TOL32 if vt == 0 else TOL16)

@@ -147,6 +147,8 @@ struct xr_raycaster_s {
     float inv_scale = 1.0f;
     bool has_support = false;   // support box of the non-zero voxels (empty-space skipping)
     float sup_lo[3] = {0, 0, 0}, sup_hi[3] = {0, 0, 0};
+    DevBuf occ;                 // macro-cell occupancy bitmask
+    int32_t nmx = 0, nmy = 0, nmz = 0;
   };
   bool skip_empty = true;
   bool build_cells = true;
@@ -378,6 +380,13 @@ static xr_status vol_support(xr_raycaster rc, xr_raycaster_s::Vol& v, const floa
   int box[6];
   XR_CUDA_TRY(cudaMemcpyAsync(box, d_box, sizeof(box), cudaMemcpyDeviceToHost, s));
   XR_CUDA_TRY(cudaStreamSynchronize(s));
+  v.nmx = (int32_t)(((v.desc.n[0] - 1) + (1 << kMacroShift) - 1) >> kMacroShift);
+  v.nmy = (int32_t)(((v.desc.n[1] - 1) + (1 << kMacroShift) - 1) >> kMacroShift);
+  v.nmz = (int32_t)(((v.desc.n[2] - 1) + (1 << kMacroShift) - 1) >> kMacroShift);
+  const size_t words = ((size_t)v.nmx * v.nmy * v.nmz + 31) / 32;
+  XR_CUDA_TRY(v.occ.reserve(words * 4));
+  XR_CUDA_TRY(launch_build_occupancy(vox_f32, (int)v.desc.n[0], (int)v.desc.n[1], (int)v.desc.n[2],
+                                     v.occ.as<uint32_t>(), v.nmx, v.nmy, v.nmz, s));
   v.has_support = true;
   if (box[3] < box[0]) {  // no non-zero voxel
     for (int k = 0; k < 3; ++k) { v.sup_lo[k] = 1.0f; v.sup_hi[k] = 0.0f; }
@@ -717,7 +726,7 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
     return XR_OK;
   }
   const TuneKey key{vol.desc.n[0], vol.desc.n[1], vol.desc.n[2], rc->rows(), rc->cols(), pow2_bucket(p.num_projs),
-                    vol.type, p.kernel_id, has_cells ? 1 : 0};
+                    vol.type, p.kernel_id, (has_cells ? 1 : 0) | (p.vol.occ ? 2 : 0)};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -743,12 +752,14 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   // layout 2 = CELL8 read with one 256-bit load per sample (float32 only)
   const int32_t layouts[3] = {XR_LAYOUT_LINEAR, XR_LAYOUT_CELL8, 2};
   const int32_t bws[3] = {1, 2, 4};
-  const int32_t unrolls[2] = {1, 2};
+  // unroll 3 = one sample per iteration with macro-cell skipping (sum kernel)
+  const int32_t unrolls[3] = {1, 2, 3};
   for (int32_t lay : layouts) {
     if (lay != XR_LAYOUT_LINEAR && !has_cells) continue;
     if (lay == 2 && vol.type != XR_VOXEL_F32) continue;
     for (int32_t bw : bws)
       for (int32_t un : unrolls) {
+        if (un == 3 && !(p.vol.occ && p.kernel_id == XR_LINE_INT_SUM)) continue;
         t.vol.layout = lay;
         t.block_warps_x = bw;
         t.unroll = un;
@@ -808,6 +819,10 @@ static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, Dr
   p.vol.voxel_type = vol.type;
   p.vol.inv_scale = vol.inv_scale;
   p.vol.has_support = (rc->skip_empty && vol.has_support) ? 1 : 0;
+  p.vol.occ = rc->skip_empty ? vol.occ.as<uint32_t>() : nullptr;
+  p.vol.nmx = vol.nmx;
+  p.vol.nmy = vol.nmy;
+  p.vol.nmz = vol.nmz;
   for (int k = 0; k < 3; ++k) {
     p.vol.sup_lo[k] = vol.sup_lo[k];
     p.vol.sup_hi[k] = vol.sup_hi[k];
@@ -858,7 +873,8 @@ extern "C" XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t lay
   XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= 2, "set_launch_config: bad layout");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || bw == 1 || bw == 2 || bw == 4 || bw == 8,
                "set_launch_config: block_warps_x must be 1, 2, 4 or 8");
-  XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || unroll == 1 || unroll == 2, "set_launch_config: unroll must be 1 or 2");
+  XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || unroll == 1 || unroll == 2 || unroll == 3,
+               "set_launch_config: unroll must be 1, 2 or 3");
   rc->cfg_layout = layout;
   rc->cfg_bw = bw;
   rc->cfg_unroll = unroll;

@@ -41,7 +41,12 @@ struct VolView {
   // disables sample skipping; an all-zero volume has an empty box (lo > hi).
   int32_t has_support;
   float sup_lo[3], sup_hi[3];
+  // Macro-cell occupancy: bit m of occ is 0 when every trilinear cell of macro
+  // cell m (kMacroCells^3 cells) has only zero corners.  occ may be nullptr.
+  const uint32_t* occ;
+  int32_t nmx, nmy, nmz;
 };
+constexpr int kMacroShift = 3;  // macro cells of 8 x 8 x 8 trilinear cells
 
 // Launch parameters of a DRR kernel.
 struct DrrParams {
@@ -85,6 +90,10 @@ cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long tot
                              unsigned long long* d_counter, int blocks, cudaStream_t s);
 // Blocks that fill the current device once (SMs x resident blocks per SM).
 int drr_multi_blocks();
+// Macro-cell occupancy bitmask of a volume (see VolView::occ); d_occ holds
+// ceil(nmx * nmy * nmz / 32) words and is cleared here.
+cudaError_t launch_build_occupancy(const float* vox_f32, int nx, int ny, int nz, uint32_t* d_occ, int nmx, int nmy,
+                                   int nmz, cudaStream_t s);
 // Index bounds of the non-zero voxels into d_box[6] (min xyz, max xyz; max < min if none).
 cudaError_t launch_support_box(const float* vox_f32, int nx, int ny, int nz, int* d_box, cudaStream_t s);
 // Bytes of the CELL8 copy of a volume, and the kernel that builds it from float32 voxels.

@@ -90,6 +90,8 @@ constexpr int kThreads = 256;
 constexpr int kMinBlocksPerSM = 6;
 // CELL8 data read with one 256-bit load per sample (float32 volumes only).
 constexpr int kLayoutCell8Wide = 2;
+// Sample-loop variant 3: macro-cell empty-space skipping (sum kernel).
+constexpr int kUnrollMacroSkip = 3;
 
 // Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
 // the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
@@ -228,6 +230,72 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
         }
         // samples first..last in order; the sum order never changes with UNROLL
         unsigned int n = first <= last ? last - first + 1u : 0u;
+        if (UNROLL == kUnrollMacroSkip && KERNEL == XR_LINE_INT_SUM && p.vol.occ) {
+          // Macro-cell skipping.  The ray is walked one macro cell (8^3 trilinear
+          // cells) at a time.  In an occupied macro cell the samples whose
+          // positions stay inside its box are taken with the plain two-sample
+          // loop.  In an empty one every sample whose cell lies inside is exactly
+          // 0, so the samples whose positions provably stay inside are passed
+          // with position updates only: "provably" = inside the box shrunk by half
+          // a voxel.  Rounding is monotonic, so along each axis positions never
+          // move against the step; towards the step each addition errs by at
+          // most half an ulp of a coordinate below 2^e, and capping a jump at
+          // 2^(22-e) samples keeps that drift under a quarter voxel.  Samples are
+          // visited in order, so the sum and every sampled position equal the
+          // sample-by-sample loop.
+          const int nmx = p.vol.nmx, nmy = p.vol.nmy;
+          const int nx2 = p.vol.nx - 2, ny2 = p.vol.ny - 2, nz2 = p.vol.nz - 2;
+          const int ebits = 32 - __clz(max(p.vol.nx, max(p.vol.ny, p.vol.nz)));
+          const float kcap = ebits <= 22 ? (float)(1u << (22 - ebits)) : 0.0f;
+          const float ss[3] = {sx, sy, sz};
+          float inv[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) inv[k] = fabsf(ss[k]) > 1.0e-20f ? 1.0f / ss[k] : 0.0f;
+          while (n > 0) {
+            const int ix = max(min(__float2int_rd(px), nx2), 0);
+            const int iy = max(min(__float2int_rd(py), ny2), 0);
+            const int iz = max(min(__float2int_rd(pz), nz2), 0);
+            const int m = ((iz >> kMacroShift) * nmy + (iy >> kMacroShift)) * nmx + (ix >> kMacroShift);
+            const bool occupied = (__ldg(p.vol.occ + (m >> 5)) >> (m & 31)) & 1u;
+            // samples after this one that stay inside the (shrunk) macro box
+            const float margin = occupied ? 0.0f : 0.5f;
+            float kmax = fminf((float)(n - 1), occupied ? 4.0e9f : kcap);
+            const float mb[3] = {(float)((ix >> kMacroShift) << kMacroShift), (float)((iy >> kMacroShift) << kMacroShift),
+                                 (float)((iz >> kMacroShift) << kMacroShift)};
+            const float pp[3] = {px, py, pz};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              const float lo = mb[k] + margin, hi = mb[k] + (float)(1 << kMacroShift) - margin;
+              float kk;
+              if (ss[k] > 1.0e-20f) kk = (hi - pp[k]) * inv[k];
+              else if (ss[k] < -1.0e-20f) kk = (lo - pp[k]) * inv[k];
+              else kk = (pp[k] >= lo && pp[k] <= hi) ? kmax : 0.0f;
+              kmax = fminf(kmax, kk);
+            }
+            unsigned int c = 1;  // this sample
+            if (kmax >= 1.0f) c += (unsigned int)kmax;
+            if (c > n) c = n;
+            n -= c;
+            if (occupied) {
+              for (; c >= 2; c -= 2) {
+                const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+                const float v1 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+                sum = __fadd_rn(__fadd_rn(sum, v0), v1);
+              }
+              if (c) {
+                const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+                sum = __fadd_rn(sum, v0);
+              }
+            } else {
+              for (; c > 0; --c) {
+                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+              }
+            }
+          }
+        }
         if (UNROLL == 2) {
           for (; n >= 2; n -= 2) {
             const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
@@ -268,7 +336,8 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 }
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, kMinBlocksPerSM) drr_kernel(const DrrParams p, const int64_t proj_base) {
+__global__ void __launch_bounds__(kThreads, UNROLL == kUnrollMacroSkip ? kMinBlocksPerSM - 1 : kMinBlocksPerSM)
+drr_kernel(const DrrParams p, const int64_t proj_base) {
   // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
   // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
   // grid index: blocks resident at the same time trace the same detector tile
@@ -348,19 +417,25 @@ cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <int VT, int KERNEL, int LAYOUT>
+cudaError_t launch_unroll(const DrrParams& p, cudaStream_t s) {
+  if (p.unroll == kUnrollMacroSkip) {
+    // macro-cell skipping exists for the sum kernel; the maximum kernel runs the
+    // plain loop, which gives the same image
+    if constexpr (KERNEL == XR_LINE_INT_SUM) return launch_t<VT, KERNEL, LAYOUT, kUnrollMacroSkip>(p, s);
+    return launch_t<VT, KERNEL, LAYOUT, 1>(p, s);
+  }
+  return p.unroll == 2 ? launch_t<VT, KERNEL, LAYOUT, 2>(p, s) : launch_t<VT, KERNEL, LAYOUT, 1>(p, s);
+}
+
 template <int VT, int KERNEL>
 cudaError_t launch_layout(const DrrParams& p, cudaStream_t s) {
   if (p.vol.layout == kLayoutCell8Wide) {
-    if constexpr (VT == XR_VOXEL_F32)
-      return p.unroll == 2 ? launch_t<VT, KERNEL, kLayoutCell8Wide, 2>(p, s)
-                           : launch_t<VT, KERNEL, kLayoutCell8Wide, 1>(p, s);
+    if constexpr (VT == XR_VOXEL_F32) return launch_unroll<VT, KERNEL, kLayoutCell8Wide>(p, s);
     return cudaErrorInvalidValue;
   }
-  const bool cell = p.vol.layout == XR_LAYOUT_CELL8;
-  if (cell) return p.unroll == 2 ? launch_t<VT, KERNEL, XR_LAYOUT_CELL8, 2>(p, s)
-                                 : launch_t<VT, KERNEL, XR_LAYOUT_CELL8, 1>(p, s);
-  return p.unroll == 2 ? launch_t<VT, KERNEL, XR_LAYOUT_LINEAR, 2>(p, s)
-                       : launch_t<VT, KERNEL, XR_LAYOUT_LINEAR, 1>(p, s);
+  if (p.vol.layout == XR_LAYOUT_CELL8) return launch_unroll<VT, KERNEL, XR_LAYOUT_CELL8>(p, s);
+  return launch_unroll<VT, KERNEL, XR_LAYOUT_LINEAR>(p, s);
 }
 
 template <int VT>
@@ -416,6 +491,26 @@ cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
   }
 }
 
+// Marks macro cell m occupied when any trilinear cell in it has a non-zero
+// corner: voxel (x, y, z) is a corner of cells x-1..x, y-1..y, z-1..z.
+__global__ void occupancy_kernel(const float* __restrict__ vox, int nx, int ny, int nz, uint32_t* occ, int nmx,
+                                 int nmy) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (vox[i] == 0.0f) continue;
+    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
+    for (int dz = -1; dz <= 0; ++dz)
+      for (int dy = -1; dy <= 0; ++dy)
+        for (int dx = -1; dx <= 0; ++dx) {
+          const int cx = x + dx, cy = y + dy, cz = z + dz;
+          if (cx < 0 || cy < 0 || cz < 0 || cx > nx - 2 || cy > ny - 2 || cz > nz - 2) continue;
+          const int m = ((cz >> kMacroShift) * nmy + (cy >> kMacroShift)) * nmx + (cx >> kMacroShift);
+          const uint32_t bit = 1u << (m & 31);
+          if (!(occ[m >> 5] & bit)) atomicOr(&occ[m >> 5], bit);
+        }
+  }
+}
+
 __global__ void support_init_kernel(int* box) {
   if (threadIdx.x < 3) box[threadIdx.x] = 0x7fffffff;
   else if (threadIdx.x < 6) box[threadIdx.x] = -1;
@@ -444,6 +539,15 @@ __global__ void support_box_kernel(const float* __restrict__ vox, int nx, int ny
       atomicMax(&box[3 + k], mx[k]);
     }
   }
+}
+
+cudaError_t launch_build_occupancy(const float* vox_f32, int nx, int ny, int nz, uint32_t* d_occ, int nmx, int nmy,
+                                   int nmz, cudaStream_t s) {
+  const size_t words = ((size_t)nmx * nmy * nmz + 31) / 32;
+  cudaError_t e = cudaMemsetAsync(d_occ, 0, words * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  occupancy_kernel<<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, d_occ, nmx, nmy);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_support_box(const float* vox_f32, int nx, int ny, int nz, int* d_box, cudaStream_t s) {
