@@ -171,9 +171,10 @@ XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* out);
 XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
 /* Launch configuration of the DRR kernel: volume layout (XR_LAYOUT_*), warps
  * across a 256-thread block (1, 2, 4 or 8; each warp covers 8x4 pixels) and
- * the sample loop: 1 or 2 samples per iteration, or 3 = one sample per
- * iteration with macro-cell skipping (sum kernel with empty-space skipping on;
- * otherwise the same as 1).  layout XR_LAYOUT_AUTO (the default) lets
+ * the sample loop: 1 or 2 samples per iteration, or 3 = 2 per iteration after
+ * each ray is trimmed to its first and last occupied macro cell (sum kernel
+ * with empty-space skipping on; otherwise the same as 2).  layout
+ * XR_LAYOUT_AUTO (the default) lets
  * the autotuner time the candidates on the first compute of each shape (volume
  * size, voxel type, detector, projection count) and cache the fastest for the
  * process.  No xReg counterpart (xReg's OpenCL caster has a fixed NDRange). */
@@ -186,9 +187,10 @@ XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable);
  * trilinear cell lies outside the bounding box of the volume's non-zero voxels
  * add exactly zero, so they are not loaded; positions still advance by the same
  * float additions, so the DRR is bit-identical with skipping on or off and equal
- * to xReg's sample-by-sample sum.  Loop variant 3 also skips the samples inside
- * empty macro cells (8x8x8 trilinear cells whose corners are all zero), with the
- * same guarantee.  The max kernel never skips. */
+ * to xReg's sample-by-sample sum.  Loop variant 3 also trims each ray's leading
+ * and trailing samples that lie in empty macro cells (8x8x8 trilinear cells with
+ * no non-zero corner within one cell), with the same guarantee.  The max kernel
+ * never skips. */
 XR_API xr_status xr_rc_set_empty_space_skipping(xr_raycaster rc, int32_t enable);
 
 /* ------------------------------------------------------ similarity metric -- */

@@ -70,13 +70,33 @@ XR_API xr_status xr_hu_to_lin_att(const float* d_hu, int64_t n, float* d_mu, voi
 XR_API xr_status xr_downsample_image_size(int64_t rows, int64_t cols, double factor, int64_t* out_rows,
                                           int64_t* out_cols);
 /* DownsampleProjData's image part (lib/image/xregProjData.cpp:40-53 ->
- * DownsampleImage, lib/itk/xregITKResampleUtils.h:51-131): discrete Gaussian of
- * variance (0.5/factor)^2 pixels (max error 0.01, replicated edges) when
- * factor < 1, then bilinear resampling at continuous index i / factor onto the
- * xr_downsample_image_size grid.  d_scratch: 2 * rows * cols doubles.  The camera
- * model of the level comes from xr_camera_downsample.  Asynchronous. */
+ * DownsampleImage, lib/itk/xregITKResampleUtils.h:51-131,183-187): discrete
+ * Gaussian of variance (0.5/factor)^2 pixels (max error 0.01, replicated edges,
+ * rounded to float) when factor < 1, then cubic B-spline resampling (the default
+ * interpolator: mirror-boundary prefilter, 4 x 4 weights) at continuous index
+ * i / factor onto the xr_downsample_image_size grid; points outside
+ * [-0.5, n - 0.5) are 0.  d_scratch: 2 * rows * cols doubles.  The camera model
+ * of the level comes from xr_camera_downsample.  Asynchronous. */
 XR_API xr_status xr_downsample_image(const float* d_src, int64_t rows, int64_t cols, double factor,
                                      double* d_scratch, float* d_dst, void* cuda_stream);
+/* ProjPreProc (lib/image/xregProjPreProc.cpp:31-139), boundary crop:
+ * CropBoundaryPixels (lib/image/xregProjData.cpp:543-567) ->
+ * UpdateCameraModelFor2DROI (lib/transforms/xregPerspectiveXform.cpp:482-503):
+ * the principal point moves by -width on both axes, width pixels go from
+ * every side. */
+XR_API xr_status xr_camera_crop_boundary(const xr_camera_desc* src, int64_t width, xr_camera_desc* out);
+/* CropImage2DBoundary (lib/itk/xregITKCropPadUtils.h:89-114): d_dst receives the
+ * (rows - 2 width) x (cols - 2 width) interior.  Asynchronous. */
+XR_API xr_status xr_crop_image_boundary(const float* d_src, int64_t rows, int64_t cols, int64_t width,
+                                        float* d_dst, void* cuda_stream);
+/* ProjPreProc's log remap, ImageIntensLogTransFilter (lib/image/xregImageIntensLogTrans.cpp:52-146):
+ * use_max_as_i0 1 (ProjPreProc's setting) takes I0 = maximum of the image
+ * smoothed by a discrete Gaussian of variance 2 pixels, else I0 = i0;
+ * out = -log(x / I0) for x > 1e-6, else -log(min_pos / I0) with min_pos the
+ * smallest value above 1e-6; float arithmetic.  d_scratch: rows * cols + 1025
+ * doubles.  Asynchronous. */
+XR_API xr_status xr_log_remap(const float* d_src, int64_t rows, int64_t cols, int32_t use_max_as_i0, float i0,
+                              double* d_scratch, float* d_dst, void* cuda_stream);
 
 /* Job set: evaluates one population for each of several registrations (each an
  * xr_objective with its own volume, cameras, fixed images and population size)

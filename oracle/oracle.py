@@ -298,3 +298,12 @@ def downsample_image(img, factor):
     L.xo_downsample_image.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p]
     assert L.xo_downsample_image(_p(src), src.shape[0], src.shape[1], factor, _p(dst)) == 0
     return dst
+
+
+def log_remap(img, use_max=True, i0=1.0):
+    src = np.ascontiguousarray(img, dtype=np.float32)
+    dst = np.zeros_like(src)
+    L = lib()
+    L.xo_log_remap.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int, C.c_float, C.c_void_p]
+    assert L.xo_log_remap(_p(src), src.shape[0], src.shape[1], int(use_max), float(i0), _p(dst)) == 0
+    return dst

@@ -860,7 +860,7 @@ XO_EXPORT int xo_discrete_gaussian_taps(double variance, double max_error, int m
   out[n++] = et * xo_bessel_i_series(1, variance);
   sum += 2.0 * out[1];
   for (int i = 2; sum < 1.0 - max_error && n < cap_len; ++i) {
-    out[n] = out[i - 2] - 2.0 * (i - 1) / variance * out[i - 1];
+    out[n] = out[i - 2] - 2.0 * (i - 1) * out[i - 1] / variance;
     sum += 2.0 * out[n];
     ++n;
     if (n > max_width) break;
@@ -869,19 +869,10 @@ XO_EXPORT int xo_discrete_gaussian_taps(double variance, double max_error, int m
   return n - 1;  /* radius */
 }
 
-/* dst: floor(rows*factor+0.5) x floor(cols*factor+0.5) floats. */
-XO_EXPORT int xo_downsample_image(const float* src, int64_t rows, int64_t cols, double factor, float* dst) {
-  const int64_t orows = (int64_t)((double)rows * factor + 0.5), ocols = (int64_t)((double)cols * factor + 0.5);
-  const int64_t n = rows * cols;
-  double* a = (double*)malloc(sizeof(double) * (size_t)n);
-  double* b = (double*)malloc(sizeof(double) * (size_t)n);
-  double taps[64];
-  int radius = 0;
-  taps[0] = 1.0;
-  if (factor < 1.0) {
-    const double sigma = 0.5 / factor;
-    radius = xo_discrete_gaussian_taps(sigma * sigma, 0.01, 32, taps, 64);
-  }
+/* Separable discrete Gaussian, edges replicated, in double: src (float) along x
+ * into a, then along y into b. */
+static void xo_gauss2d(const float* src, int64_t rows, int64_t cols, const double* taps, int radius, double* a,
+                       double* b) {
   for (int64_t r = 0; r < rows; ++r)
     for (int64_t c = 0; c < cols; ++c) {
       double s = taps[0] * src[r * cols + c];
@@ -900,21 +891,139 @@ XO_EXPORT int xo_downsample_image(const float* src, int64_t rows, int64_t cols, 
       }
       b[r * cols + c] = s;
     }
+}
+
+/* Cubic B-spline prefilter of one line in place (ITK BSplineDecompositionImageFilter
+ * with spline order 3, after Unser, "Splines: a perfect fit for signal and image
+ * processing", 1999, Box 2): gain (1 - z)(1 - 1/z), causal start with mirror
+ * boundaries (summed to the horizon ceil(log 1e-10 / log|z|) when the line is
+ * longer, else the closed full sum), causal recursion, anti-causal start
+ * z / (z^2 - 1) (z v[N-2] + v[N-1]), anti-causal recursion. */
+static void xo_bspline_line(double* v, int64_t len, int64_t stride) {
+  if (len < 2) return;
+  const double z = sqrt(3.0) - 2.0;
+  double c0 = 1.0;
+  c0 = c0 * (1.0 - z) * (1.0 - 1.0 / z);
+  for (int64_t n = 0; n < len; ++n) v[n * stride] *= c0;
+  const int64_t horizon = (int64_t)ceil(log(1.0e-10) / log(fabs(z)));
+  double zn = z, sum;
+  if (horizon < len) {
+    sum = v[0];
+    for (int64_t n = 1; n < horizon; ++n) {
+      sum += zn * v[n * stride];
+      zn *= z;
+    }
+    v[0] = sum;
+  } else {
+    const double iz = 1.0 / z;
+    double z2n = pow(z, (double)(len - 1));
+    sum = v[0] + z2n * v[(len - 1) * stride];
+    z2n *= z2n * iz;
+    for (int64_t n = 1; n <= len - 2; ++n) {
+      sum += (zn + z2n) * v[n * stride];
+      zn *= z;
+      z2n *= iz;
+    }
+    v[0] = sum / (1.0 - zn * zn);
+  }
+  for (int64_t n = 1; n < len; ++n) v[n * stride] += z * v[(n - 1) * stride];
+  v[(len - 1) * stride] = (z / (z * z - 1.0)) * (z * v[(len - 2) * stride] + v[(len - 1) * stride]);
+  for (int64_t n = len - 2; n >= 0; --n) v[n * stride] = z * (v[(n + 1) * stride] - v[n * stride]);
+}
+
+static int64_t xo_mirror(int64_t k, int64_t n) {
+  if (n == 1) return 0;
+  if (k < 0) k = -k;
+  if (k > n - 1) k = (n - 1) - (k - (n - 1));
+  return k;
+}
+
+/* ITK BSplineInterpolateImageFunction (order 3) at continuous index (x, y):
+ * support starts at floor((float)x) - 1, weights of t = x - floor((float)x),
+ * indices mirrored, sum over the 4 x 4 points with x fastest. */
+static double xo_bspline_eval(const double* coef, int64_t rows, int64_t cols, double x, double y) {
+  const double xy[2] = {x, y};
+  const int64_t len[2] = {cols, rows};
+  double w[2][4];
+  int64_t idx[2][4];
+  for (int d = 0; d < 2; ++d) {
+    const int64_t i1 = (int64_t)floor((float)xy[d]);
+    const double t = xy[d] - (double)i1;
+    w[d][3] = (1.0 / 6.0) * t * t * t;
+    w[d][0] = (1.0 / 6.0) + 0.5 * t * (t - 1.0) - w[d][3];
+    w[d][2] = t + w[d][0] - 2.0 * w[d][3];
+    w[d][1] = 1.0 - w[d][0] - w[d][2] - w[d][3];
+    for (int k = 0; k < 4; ++k) idx[d][k] = xo_mirror(i1 - 1 + k, len[d]);
+  }
+  double acc = 0.0;
+  for (int p = 0; p < 16; ++p) {
+    const int a = p % 4, b = p / 4;
+    const double wt = w[0][a] * w[1][b];
+    acc += wt * coef[idx[1][b] * cols + idx[0][a]];
+  }
+  return acc;
+}
+
+/* DownsampleImage (lib/itk/xregITKResampleUtils.h:51-131, default cubic B-spline
+ * interpolator :183-187) as used by DownsampleProjData (lib/image/xregProjData.cpp:40-53).
+ * dst: floor(rows*factor+0.5) x floor(cols*factor+0.5) floats. */
+XO_EXPORT int xo_downsample_image(const float* src, int64_t rows, int64_t cols, double factor, float* dst) {
+  const int64_t orows = (int64_t)((double)rows * factor + 0.5), ocols = (int64_t)((double)cols * factor + 0.5);
+  const int64_t n = rows * cols;
+  double* a = (double*)malloc(sizeof(double) * (size_t)n);
+  double* b = (double*)malloc(sizeof(double) * (size_t)n);
+  if (factor < 1.0) {
+    double taps[64];
+    const double sigma = 0.5 / factor;
+    const int radius = xo_discrete_gaussian_taps(sigma * sigma, 0.01, 32, taps, 64);
+    xo_gauss2d(src, rows, cols, taps, radius, a, b);
+    for (int64_t i = 0; i < n; ++i) b[i] = (double)(float)b[i];  /* the smoothed float image */
+  } else {
+    for (int64_t i = 0; i < n; ++i) b[i] = (double)src[i];
+  }
+  for (int64_t r = 0; r < rows; ++r) xo_bspline_line(b + r * cols, cols, 1);
+  for (int64_t c = 0; c < cols; ++c) xo_bspline_line(b + c, rows, cols);
   for (int64_t r = 0; r < orows; ++r)
     for (int64_t c = 0; c < ocols; ++c) {
-      const double y = r / factor, x = c / factor;
-      if (x > cols - 0.5 || y > rows - 0.5) { dst[r * ocols + c] = 0.0f; continue; }
-      int64_t x0 = (int64_t)floor(x), y0 = (int64_t)floor(y), x1 = x0 + 1, y1 = y0 + 1;
-      double fx = x - x0, fy = y - y0;
-      if (x1 > cols - 1) { x1 = x0; fx = 0.0; }
-      if (y1 > rows - 1) { y1 = y0; fy = 0.0; }
-      if (x0 > cols - 1) x0 = x1 = cols - 1;
-      if (y0 > rows - 1) y0 = y1 = rows - 1;
-      const double v00 = b[y0 * cols + x0], v01 = b[y0 * cols + x1], v10 = b[y1 * cols + x0], v11 = b[y1 * cols + x1];
-      const double p = v00 + (v01 - v00) * fx, q = v10 + (v11 - v10) * fx;
-      dst[r * ocols + c] = (float)(p + (q - p) * fy);
+      const double y = (double)r / factor, x = (double)c / factor;
+      const int inside = x >= -0.5 && x < cols - 0.5 && y >= -0.5 && y < rows - 0.5;
+      dst[r * ocols + c] = inside ? (float)xo_bspline_eval(b, rows, cols, x, y) : 0.0f;
     }
   free(a);
   free(b);
+  return 0;
+}
+
+/* ImageIntensLogTransFilter::GenerateData with UseMaxIntensityAsI0
+ * (lib/image/xregImageIntensLogTrans.cpp:52-146): I0 = max of the image smoothed
+ * by a discrete Gaussian of variance 2 (pixel units, max error 0.01, width 32,
+ * rounded to float); min_pos = smallest value above 1e-6 (0 if none);
+ * out = x > 1e-6 ? -log(x / I0) : -log(min_pos / I0), in float.
+ * use_max 0 takes I0 = i0. */
+XO_EXPORT int xo_log_remap(const float* src, int64_t rows, int64_t cols, int use_max, float i0, float* dst) {
+  const int64_t n = rows * cols;
+  const float eps = 1.0e-6f;
+  float I0 = i0;
+  if (use_max) {
+    double* a = (double*)malloc(sizeof(double) * (size_t)n);
+    double* b = (double*)malloc(sizeof(double) * (size_t)n);
+    double taps[64];
+    const int radius = xo_discrete_gaussian_taps(2.0, 0.01, 32, taps, 64);
+    xo_gauss2d(src, rows, cols, taps, radius, a, b);
+    I0 = (float)b[0];
+    for (int64_t i = 1; i < n; ++i)
+      if ((float)b[i] > I0) I0 = (float)b[i];
+    free(a);
+    free(b);
+  }
+  float min_pos = 0.0f;
+  int found = 0;
+  for (int64_t i = 0; i < n; ++i)
+    if (src[i] > eps) {
+      if (!found || min_pos > src[i]) min_pos = src[i];
+      found = 1;
+    }
+  const float out_max = -logf(min_pos / I0);
+  for (int64_t i = 0; i < n; ++i) dst[i] = (src[i] > eps) ? -logf(src[i] / I0) : out_max;
   return 0;
 }

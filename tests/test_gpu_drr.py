@@ -292,16 +292,16 @@ def test_empty_space_skipping_is_exact(xr, oracle, vt):
 
 @pytest.mark.parametrize("vt", [0, 1])
 def test_macro_cell_skipping_is_exact(xr, oracle, vt):
-    """Macro-cell skipping (loop 3) changes no bit where the bounding box does
+    """The macro-cell trim (loop 3) changes no bit where the bounding box does
     not help: two blobs in opposite corners and a one-voxel sheet in between
     leave empty macro cells inside the support box.  Covers an unperturbed
-    (axis-aligned central ray) pose, a step far below the voxel size (long jumps
-    through empty macro cells) and the oracle."""
-    ph = synth.phantom_volume((40, 36, 32), (1.5, 1.5, 1.5), 21).voxels
-    big = np.zeros((96, 88, 80), np.float32)
-    big[3:43, 4:40, 2:34] = ph
-    big[54:94, 50:86, 46:78] = ph[::-1, :, ::-1]
-    big[47, 30:60, 20:60] = 0.02  # a sheet one voxel thick
+    (axis-aligned central ray) pose, a step far below the voxel size (many
+    samples per macro cell) and the oracle."""
+    ph = synth.phantom_volume((40, 36, 32), (1.5, 1.5, 1.5), 21).voxels  # (z, y, x)
+    big = np.zeros((80, 88, 96), np.float32)
+    big[2:34, 4:40, 3:43] = ph
+    big[46:78, 50:86, 54:94] = ph[::-1, :, ::-1]
+    big[20:60, 30:60, 47] = 0.02  # a sheet one voxel thick
     vol = xr.Volume(big, spacing=(1.5, 1.5, 1.5))
     cam = small_camera((48, 56), 3.5)
     gt = synth.gt_pose(vol)

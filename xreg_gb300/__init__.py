@@ -18,6 +18,12 @@ from .api import (  # noqa: F401
     PopulationObjective,
     RayCasterLineIntCUDA,
     Volume,
+    crop_image_boundary,
+    downsample_image,
+    downsample_size,
+    hu_to_lin_att_device,
+    log_remap,
+    proj_preproc,
 )
 
 __version__ = "0.1.0"

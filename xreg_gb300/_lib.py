@@ -126,6 +126,9 @@ _SIGS = {
     "xr_hu_to_lin_att": [P, i64, P, P],
     "xr_downsample_image_size": [i64, i64, f64, C.POINTER(i64), C.POINTER(i64)],
     "xr_downsample_image": [P, i64, i64, f64, P, P, P],
+    "xr_camera_crop_boundary": [P, i64, P],
+    "xr_crop_image_boundary": [P, i64, i64, i64, P, P],
+    "xr_log_remap": [P, i64, i64, i32, f32, P, P, P],
     "xr_jobset_create": [i32, C.POINTER(H)],
     "xr_jobset_destroy": [H],
     "xr_jobset_set_stream": [H, P],

@@ -40,6 +40,13 @@ class CameraModel:
         call("xr_camera_downsample", C.byref(self.desc), float(ds_factor), int(force_even_dims), C.byref(d))
         return CameraModel(d)
 
+    def crop_boundary(self, width: int) -> "CameraModel":
+        """The camera of CropBoundaryPixels (xregProjData.cpp:543-567 ->
+        UpdateCameraModelFor2DROI, xregPerspectiveXform.cpp:482-503)."""
+        d = L.xr_camera_desc()
+        call("xr_camera_crop_boundary", C.byref(self.desc), int(width), C.byref(d))
+        return CameraModel(d)
+
     @property
     def num_det_rows(self) -> int:
         return int(self.desc.num_det_rows)
@@ -515,3 +522,47 @@ def downsample_image(img: np.ndarray, factor: float, device: int = -1) -> np.nda
          C.c_void_p(scratch.data_ptr()), C.c_void_p(dst.data_ptr()), C.c_void_p(s.cuda_stream))
     s.synchronize()
     return dst.cpu().numpy()
+
+
+def crop_image_boundary(img: np.ndarray, width: int, device: int = -1) -> np.ndarray:
+    """CropImage2DBoundary on the GPU (xr_crop_image_boundary)."""
+    import torch
+    dev = torch.device("cuda", device if device >= 0 else torch.cuda.current_device())
+    src = torch.from_numpy(np.ascontiguousarray(img, dtype=np.float32)).to(dev)
+    rows, cols = src.shape
+    dst = torch.empty((max(rows - 2 * width, 0), max(cols - 2 * width, 0)), dtype=torch.float32, device=dev)
+    s = torch.cuda.current_stream(dev)
+    call("xr_crop_image_boundary", C.c_void_p(src.data_ptr()), rows, cols, int(width), C.c_void_p(dst.data_ptr()),
+         C.c_void_p(s.cuda_stream))
+    s.synchronize()
+    return dst.cpu().numpy()
+
+
+def log_remap(img: np.ndarray, use_max_as_i0: bool = True, i0: float = 1.0, device: int = -1) -> np.ndarray:
+    """ImageIntensLogTransFilter as ProjPreProc runs it, on the GPU (xr_log_remap)."""
+    import torch
+    dev = torch.device("cuda", device if device >= 0 else torch.cuda.current_device())
+    src = torch.from_numpy(np.ascontiguousarray(img, dtype=np.float32)).to(dev)
+    rows, cols = src.shape
+    scratch = torch.empty(rows * cols + 1025, dtype=torch.float64, device=dev)
+    dst = torch.empty_like(src)
+    s = torch.cuda.current_stream(dev)
+    call("xr_log_remap", C.c_void_p(src.data_ptr()), rows, cols, int(bool(use_max_as_i0)), float(i0),
+         C.c_void_p(scratch.data_ptr()), C.c_void_p(dst.data_ptr()), C.c_void_p(s.cuda_stream))
+    s.synchronize()
+    return dst.cpu().numpy()
+
+
+def proj_preproc(img: np.ndarray, cam: CameraModel, crop_width: int = 50, no_log_remap: bool = False,
+                 device: int = -1):
+    """ProjPreProc::operator() (xregProjPreProc.cpp:31-139) for one projection with
+    its defaults (crop 50 pixels from every side, then the log remap with I0 from
+    the smoothed maximum; metal auto-masking is not part of it here).  Returns
+    (image, camera)."""
+    out, c = np.ascontiguousarray(img, dtype=np.float32), cam
+    if crop_width > 0:
+        c = cam.crop_boundary(crop_width)
+        out = crop_image_boundary(out, crop_width, device)
+    if not no_log_remap:
+        out = log_remap(out, True, 1.0, device)
+    return out, c

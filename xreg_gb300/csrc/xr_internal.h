@@ -41,8 +41,9 @@ struct VolView {
   // disables sample skipping; an all-zero volume has an empty box (lo > hi).
   int32_t has_support;
   float sup_lo[3], sup_hi[3];
-  // Macro-cell occupancy: bit m of occ is 0 when every trilinear cell of macro
-  // cell m (kMacroCells^3 cells) has only zero corners.  occ may be nullptr.
+  // Dilated macro-cell occupancy: bit m of occ is 0 when every trilinear cell
+  // with base index in [8m - 1, 8m + 8] on each axis has only zero corners
+  // (macro cell m spans cells [8m, 8m + 7]).  occ may be nullptr.
   const uint32_t* occ;
   int32_t nmx, nmy, nmz;
 };
@@ -65,7 +66,7 @@ struct DrrParams {
   int32_t kernel_id;      // XR_LINE_INT_SUM / MAX
   int32_t store;          // XR_PROJ_STORE_REPLACE / ACCUM
   int32_t block_warps_x;  // warps across a block (1, 2, 4, 8); 8x4-pixel warps
-  int32_t unroll;         // samples per loop iteration (1 or 2)
+  int32_t unroll;         // samples per loop iteration (1 or 2); 3 = 2 after the macro-cell trim
 };
 
 // ---- launchers (xr_geom.cu) ----

@@ -140,6 +140,57 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
 
 // Traces the ray of pixel (row, col) of projection proj and stores the result
 // (the caller checks that the pixel exists).  Returns the number of samples.
+// Walks the macro cells of the ray p0 + k st from k = kstart towards kend
+// (dir +1 forward, -1 backward) and returns the ray parameter at which it
+// enters the first macro cell whose (dilated) occupancy bit is set, or +inf
+// (-inf backward) when none is met before kend.  Macro cell m spans continuous
+// index [8m, 8m + 8) on each axis; positions are clamped to cells as the
+// sampler does.  The walk is bounded by the number of macro cells on a line.
+__device__ __forceinline__ float macro_march(const VolView& v, const float p0[3], const float st[3], float kstart,
+                                             float kend, int dir) {
+  const int nm[3] = {v.nmx, v.nmy, v.nmz};
+  const int n2[3] = {v.nx - 2, v.ny - 2, v.nz - 2};
+  int m[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float q = p0[a] + kstart * st[a];
+    m[a] = max(min(__float2int_rd(q), n2[a]), 0) >> kMacroShift;
+  }
+  float k = kstart;
+  const int cap = nm[0] + nm[1] + nm[2] + 3;
+  for (int it = 0; it < cap; ++it) {
+    const int idx = (m[2] * nm[1] + m[1]) * nm[0] + m[0];
+    if ((__ldg(v.occ + (idx >> 5)) >> (idx & 31)) & 1u) return k;
+    float best = INFINITY, knext = 0.0f;
+    int ax = -1, dm = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float d = dir > 0 ? st[a] : -st[a];
+      float bound;
+      int step;
+      if (d > 1.0e-20f) {
+        if (m[a] >= nm[a] - 1) continue;  // the last macro cell on this axis runs to the volume's end
+        bound = (float)((m[a] + 1) << kMacroShift);
+        step = 1;
+      } else if (d < -1.0e-20f) {
+        if (m[a] <= 0) continue;
+        bound = (float)(m[a] << kMacroShift);
+        step = -1;
+      } else {
+        continue;
+      }
+      const float kk = (bound - p0[a]) / st[a];
+      const float tt = dir > 0 ? kk : -kk;  // increases along the walk
+      if (tt < best) { best = tt; knext = kk; ax = a; dm = step; }
+    }
+    if (ax < 0) return dir > 0 ? INFINITY : -INFINITY;  // stays in this empty macro cell
+    if (dir > 0 ? (knext > kend) : (knext < kend)) return dir > 0 ? INFINITY : -INFINITY;
+    if (dir > 0 ? (knext > k) : (knext < k)) k = knext;
+    m[ax] += dm;
+  }
+  return k;  // walk limit: treat the rest as occupied
+}
+
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, const int64_t proj, const int row,
                                                           const int col) {
@@ -224,79 +275,42 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
           last = f1 < (float)nsteps ? (unsigned int)f1 : (unsigned int)nsteps;
         }
       }
+      if (UNROLL == kUnrollMacroSkip && KERNEL == XR_LINE_INT_SUM && p.vol.occ && hit && first <= last) {
+        // Macro-cell trim: walk the macro grid from each end of [first, last]
+        // to the first occupied macro cell; the samples before (after) it lie in
+        // empty macro cells and add exactly 0.  The occupancy is dilated by one
+        // trilinear cell, so a sample whose float position strays less than a
+        // voxel from the exact ray still reads only zero corners; repeated
+        // addition drifts by at most (last + 1) half-ulps of a coordinate below
+        // 2^e, kept under a voxel by the 2^(22-e) sample limit.
+        const int ebits = 32 - __clz(max(p.vol.nx, max(p.vol.ny, p.vol.nz)));
+        if (ebits <= 22 && last < (1u << (22 - ebits))) {
+          const float p0[3] = {px, py, pz}, st[3] = {sx, sy, sz};
+          const float kf = macro_march(p.vol, p0, st, (float)first, (float)last, 1);
+          if (kf == INFINITY) {
+            first = 1u;
+            last = 0u;  // every sample is zero
+          } else {
+            const float f = floorf(kf) - 1.0f;
+            if (f > (float)first) first = (unsigned int)f;
+            const float kl = macro_march(p.vol, p0, st, (float)last, (float)first, -1);
+            if (kl == -INFINITY) {
+              first = 1u;
+              last = 0u;
+            } else {
+              const float l = ceilf(kl) + 1.0f;
+              if (l < (float)last) last = (unsigned int)l;
+            }
+          }
+        }
+      }
       if (hit) {
         for (unsigned int s = 0; s < first && s <= last; ++s) {
           px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
         }
         // samples first..last in order; the sum order never changes with UNROLL
         unsigned int n = first <= last ? last - first + 1u : 0u;
-        if (UNROLL == kUnrollMacroSkip && KERNEL == XR_LINE_INT_SUM && p.vol.occ) {
-          // Macro-cell skipping.  The ray is walked one macro cell (8^3 trilinear
-          // cells) at a time.  In an occupied macro cell the samples whose
-          // positions stay inside its box are taken with the plain two-sample
-          // loop.  In an empty one every sample whose cell lies inside is exactly
-          // 0, so the samples whose positions provably stay inside are passed
-          // with position updates only: "provably" = inside the box shrunk by half
-          // a voxel.  Rounding is monotonic, so along each axis positions never
-          // move against the step; towards the step each addition errs by at
-          // most half an ulp of a coordinate below 2^e, and capping a jump at
-          // 2^(22-e) samples keeps that drift under a quarter voxel.  Samples are
-          // visited in order, so the sum and every sampled position equal the
-          // sample-by-sample loop.
-          const int nmx = p.vol.nmx, nmy = p.vol.nmy;
-          const int nx2 = p.vol.nx - 2, ny2 = p.vol.ny - 2, nz2 = p.vol.nz - 2;
-          const int ebits = 32 - __clz(max(p.vol.nx, max(p.vol.ny, p.vol.nz)));
-          const float kcap = ebits <= 22 ? (float)(1u << (22 - ebits)) : 0.0f;
-          const float ss[3] = {sx, sy, sz};
-          float inv[3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) inv[k] = fabsf(ss[k]) > 1.0e-20f ? 1.0f / ss[k] : 0.0f;
-          while (n > 0) {
-            const int ix = max(min(__float2int_rd(px), nx2), 0);
-            const int iy = max(min(__float2int_rd(py), ny2), 0);
-            const int iz = max(min(__float2int_rd(pz), nz2), 0);
-            const int m = ((iz >> kMacroShift) * nmy + (iy >> kMacroShift)) * nmx + (ix >> kMacroShift);
-            const bool occupied = (__ldg(p.vol.occ + (m >> 5)) >> (m & 31)) & 1u;
-            // samples after this one that stay inside the (shrunk) macro box
-            const float margin = occupied ? 0.0f : 0.5f;
-            float kmax = fminf((float)(n - 1), occupied ? 4.0e9f : kcap);
-            const float mb[3] = {(float)((ix >> kMacroShift) << kMacroShift), (float)((iy >> kMacroShift) << kMacroShift),
-                                 (float)((iz >> kMacroShift) << kMacroShift)};
-            const float pp[3] = {px, py, pz};
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              const float lo = mb[k] + margin, hi = mb[k] + (float)(1 << kMacroShift) - margin;
-              float kk;
-              if (ss[k] > 1.0e-20f) kk = (hi - pp[k]) * inv[k];
-              else if (ss[k] < -1.0e-20f) kk = (lo - pp[k]) * inv[k];
-              else kk = (pp[k] >= lo && pp[k] <= hi) ? kmax : 0.0f;
-              kmax = fminf(kmax, kk);
-            }
-            unsigned int c = 1;  // this sample
-            if (kmax >= 1.0f) c += (unsigned int)kmax;
-            if (c > n) c = n;
-            n -= c;
-            if (occupied) {
-              for (; c >= 2; c -= 2) {
-                const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-                const float v1 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-                sum = __fadd_rn(__fadd_rn(sum, v0), v1);
-              }
-              if (c) {
-                const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-                sum = __fadd_rn(sum, v0);
-              }
-            } else {
-              for (; c > 0; --c) {
-                px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-              }
-            }
-          }
-        }
-        if (UNROLL == 2) {
+        if (UNROLL >= 2) {  // loop 3 = loop 2 after the macro-cell trim
           for (; n >= 2; n -= 2) {
             const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
             px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
@@ -336,8 +350,7 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 }
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, UNROLL == kUnrollMacroSkip ? kMinBlocksPerSM - 1 : kMinBlocksPerSM)
-drr_kernel(const DrrParams p, const int64_t proj_base) {
+__global__ void __launch_bounds__(kThreads, kMinBlocksPerSM) drr_kernel(const DrrParams p, const int64_t proj_base) {
   // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
   // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
   // grid index: blocks resident at the same time trace the same detector tile
@@ -420,10 +433,10 @@ cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
 template <int VT, int KERNEL, int LAYOUT>
 cudaError_t launch_unroll(const DrrParams& p, cudaStream_t s) {
   if (p.unroll == kUnrollMacroSkip) {
-    // macro-cell skipping exists for the sum kernel; the maximum kernel runs the
-    // plain loop, which gives the same image
+    // the macro-cell trim exists for the sum kernel; the maximum kernel runs the
+    // plain two-sample loop, which gives the same image
     if constexpr (KERNEL == XR_LINE_INT_SUM) return launch_t<VT, KERNEL, LAYOUT, kUnrollMacroSkip>(p, s);
-    return launch_t<VT, KERNEL, LAYOUT, 1>(p, s);
+    return launch_t<VT, KERNEL, LAYOUT, 2>(p, s);
   }
   return p.unroll == 2 ? launch_t<VT, KERNEL, LAYOUT, 2>(p, s) : launch_t<VT, KERNEL, LAYOUT, 1>(p, s);
 }
@@ -493,18 +506,22 @@ cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
 
 // Marks macro cell m occupied when any trilinear cell in it has a non-zero
 // corner: voxel (x, y, z) is a corner of cells x-1..x, y-1..y, z-1..z.
+// Dilated macro-cell occupancy: bit m is set when some trilinear cell with base
+// index in [8m - 1, 8m + 8] on every axis has a non-zero corner, i.e. some
+// non-zero voxel lies in [8m - 1, 8m + 9].
 __global__ void occupancy_kernel(const float* __restrict__ vox, int nx, int ny, int nz, uint32_t* occ, int nmx,
-                                 int nmy) {
+                                 int nmy, int nmz) {
   const int64_t n = (int64_t)nx * ny * nz;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if (vox[i] == 0.0f) continue;
     const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
-    for (int dz = -1; dz <= 0; ++dz)
-      for (int dy = -1; dy <= 0; ++dy)
-        for (int dx = -1; dx <= 0; ++dx) {
-          const int cx = x + dx, cy = y + dy, cz = z + dz;
-          if (cx < 0 || cy < 0 || cz < 0 || cx > nx - 2 || cy > ny - 2 || cz > nz - 2) continue;
-          const int m = ((cz >> kMacroShift) * nmy + (cy >> kMacroShift)) * nmx + (cx >> kMacroShift);
+    const int x0 = max(x - 2, 0) >> kMacroShift, x1 = min((x + 1) >> kMacroShift, nmx - 1);
+    const int y0 = max(y - 2, 0) >> kMacroShift, y1 = min((y + 1) >> kMacroShift, nmy - 1);
+    const int z0 = max(z - 2, 0) >> kMacroShift, z1 = min((z + 1) >> kMacroShift, nmz - 1);
+    for (int mz = z0; mz <= z1; ++mz)
+      for (int my = y0; my <= y1; ++my)
+        for (int mx = x0; mx <= x1; ++mx) {
+          const int m = (mz * nmy + my) * nmx + mx;
           const uint32_t bit = 1u << (m & 31);
           if (!(occ[m >> 5] & bit)) atomicOr(&occ[m >> 5], bit);
         }
@@ -546,7 +563,7 @@ cudaError_t launch_build_occupancy(const float* vox_f32, int nx, int ny, int nz,
   const size_t words = ((size_t)nmx * nmy * nmz + 31) / 32;
   cudaError_t e = cudaMemsetAsync(d_occ, 0, words * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
-  occupancy_kernel<<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, d_occ, nmx, nmy);
+  occupancy_kernel<<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, d_occ, nmx, nmy, nmz);
   return cudaGetLastError();
 }
 
