@@ -91,7 +91,8 @@ constexpr int kMinBlocksPerSM = 6;
 // CELL8 data read with one 256-bit load per sample (float32 volumes only).
 constexpr int kLayoutCell8Wide = 2;
 // Sample-loop variant 3: macro-cell empty-space skipping (sum kernel).
-constexpr int kUnrollMacroSkip = 3;
+constexpr int kUnrollMacroSkip = 3;  // loop 2 after the macro-cell trim
+constexpr int kUnrollTrim4 = 4;      // four samples per iteration after the macro-cell trim
 
 // Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
 // the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
@@ -275,7 +276,7 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
           last = f1 < (float)nsteps ? (unsigned int)f1 : (unsigned int)nsteps;
         }
       }
-      if (UNROLL == kUnrollMacroSkip && KERNEL == XR_LINE_INT_SUM && p.vol.occ && hit && first <= last) {
+      if (UNROLL >= kUnrollMacroSkip && KERNEL == XR_LINE_INT_SUM && p.vol.occ && hit && first <= last) {
         // Macro-cell trim: walk the macro grid from each end of [first, last]
         // to the first occupied macro cell; the samples before (after) it lie in
         // empty macro cells and add exactly 0.  The occupancy is dilated by one
@@ -310,7 +311,27 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
         }
         // samples first..last in order; the sum order never changes with UNROLL
         unsigned int n = first <= last ? last - first + 1u : 0u;
-        if (UNROLL >= 2) {  // loop 3 = loop 2 after the macro-cell trim
+        if (UNROLL == kUnrollTrim4) {  // four loads in flight per thread
+          for (; n >= 4; n -= 4) {
+            const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            const float v1 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            const float v2 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            const float v3 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            if (KERNEL == XR_LINE_INT_MAX) {
+              sum = (sum < v0) ? v0 : sum;
+              sum = (sum < v1) ? v1 : sum;
+              sum = (sum < v2) ? v2 : sum;
+              sum = (sum < v3) ? v3 : sum;
+            } else {
+              sum = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(sum, v0), v1), v2), v3);
+            }
+          }
+        }
+        if (UNROLL >= 2) {  // loops 3 and 4 finish with the two-sample loop
           for (; n >= 2; n -= 2) {
             const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
             px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
@@ -350,7 +371,8 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 }
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, kMinBlocksPerSM) drr_kernel(const DrrParams p, const int64_t proj_base) {
+__global__ void __launch_bounds__(kThreads, UNROLL == kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
+drr_kernel(const DrrParams p, const int64_t proj_base) {
   // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
   // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
   // grid index: blocks resident at the same time trace the same detector tile
@@ -432,10 +454,13 @@ cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
 
 template <int VT, int KERNEL, int LAYOUT>
 cudaError_t launch_unroll(const DrrParams& p, cudaStream_t s) {
-  if (p.unroll == kUnrollMacroSkip) {
+  if (p.unroll == kUnrollMacroSkip || p.unroll == kUnrollTrim4) {
     // the macro-cell trim exists for the sum kernel; the maximum kernel runs the
     // plain two-sample loop, which gives the same image
-    if constexpr (KERNEL == XR_LINE_INT_SUM) return launch_t<VT, KERNEL, LAYOUT, kUnrollMacroSkip>(p, s);
+    if constexpr (KERNEL == XR_LINE_INT_SUM) {
+      if (p.unroll == kUnrollTrim4) return launch_t<VT, KERNEL, LAYOUT, kUnrollTrim4>(p, s);
+      return launch_t<VT, KERNEL, LAYOUT, kUnrollMacroSkip>(p, s);
+    }
     return launch_t<VT, KERNEL, LAYOUT, 2>(p, s);
   }
   return p.unroll == 2 ? launch_t<VT, KERNEL, LAYOUT, 2>(p, s) : launch_t<VT, KERNEL, LAYOUT, 1>(p, s);

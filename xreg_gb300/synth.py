@@ -199,23 +199,33 @@ def uneven_job_specs(n: int, seed: int) -> list:
 
 
 def job_registration(spec: JobSpec, levels=None, iters=(150, 100), level2_pop: int = 8, voxel_type: int = 1,
-                     step: float = 0.5, device: int = -1, level2: str = "dfo"):
+                     step: float = 0.5, device: int = -1, level2: str = "dfo", fixed_from: str = "downsample"):
     """A two-level registration request from a JobSpec: level 1 at the spec's
     downsampling (or 8x) with CMA-ES lambda = spec.pop, level 2 at 4x with the
     bound-constrained trust-region optimizer (level2 "dfo", xReg's BOBYQA level)
-    or a small CMA-ES (level2 "cmaes", lambda = level2_pop); fixed images rendered
-    at a ground-truth pose, start pose perturbed from it by N(0, 5 deg) /
-    N(0, 10 mm).  Returns (Registration, ground truth)."""
+    or a small CMA-ES (level2 "cmaes", lambda = level2_pop).  The fixed images are
+    full-resolution (1536^2) DRRs at a ground-truth pose plus 1 % noise, brought
+    to each level by DownsampleProjData as MultiLevelMultiObjRegi does
+    (xregMultiObjMultiLevel2D3DRegi.cpp:254; fixed_from "render" instead renders
+    each level directly).  Start pose perturbed from the ground truth by
+    N(0, 5 deg) / N(0, 10 mm).  Returns (Registration, ground truth)."""
     from .regi import Registration, RegiLevel
     vol = phantom_volume(spec.size, spec.spacing, spec.seed)
     rng = np.random.default_rng(spec.seed + 1)
     gt = perturb(vol, gt_pose(vol), rng.normal(0.0, 3.0, 3), rng.normal(0.0, 5.0, 3))
     init = perturb(vol, gt, rng.normal(0.0, 5.0, 3), rng.normal(0.0, 10.0, 3))
     ds = levels or [spec.ds_first, 0.25]
+    full = None
+    if fixed_from == "downsample":
+        full = render_fixed(vol, view_cameras(spec.view_angles, 1.0), gt, step, spec.seed + 17, device)
     lv = []
     for k, d in enumerate(ds):
         cams = view_cameras(spec.view_angles, d)
-        fixed = render_fixed(vol, cams, gt, step, spec.seed + 17 * (k + 1), device)
+        if full is not None:
+            from .api import downsample_image
+            fixed = [downsample_image(f, d, device) for f in full]
+        else:
+            fixed = render_fixed(vol, cams, gt, step, spec.seed + 17 * (k + 1), device)
         if k == 0:
             lv.append(RegiLevel(cams, fixed, "grad_ncc", pop=spec.pop, max_iters=iters[0]))
         elif level2 == "dfo":
