@@ -60,6 +60,28 @@ def test_converges_like_reference(xr, fn, opt, tolx):
     assert 0.5 < r < 2.0, (gens_ours, gens_ref)
 
 
+def test_against_reference_golden_runs(xr):
+    """The same comparison against committed runs of the reference's cmaes.c
+    (tests/golden/cmaes_reference_runs.json, made by make_cmaes_golden.py), so it
+    also holds where the xReg sources are absent: every run of ours reaches the
+    optimum the reference reached, in a comparable number of generations."""
+    import json
+    from pathlib import Path
+    d = json.loads((Path(__file__).parent / "golden" / "cmaes_reference_runs.json").read_text())
+    fns = {"sphere": (sphere, 0.0, 1e-6), "ellipsoid": (ellipsoid, 0.0, 1e-5), "rosenbrock": (rosenbrock, 1.0, 1e-4)}
+    for name, (fn, opt, tolx) in fns.items():
+        runs = [r for r in d["runs"] if r["function"] == name]
+        assert len(runs) == 3
+        ours = []
+        for r in runs:
+            assert np.max(np.abs(np.array(r["final_mean"]) - opt)) < tolx
+            m, g = _run_ours(fn, np.array(r["x0"]), np.full(r["dim"], 1.0), r["lambda"], r["seed"], 1e-14)
+            assert np.max(np.abs(m - opt)) < tolx, (name, m)
+            ours.append(g)
+        ratio = np.mean(ours) / np.mean([r["generations"] for r in runs])
+        assert 0.5 < ratio < 2.0, (name, ours, [r["generations"] for r in runs])
+
+
 def test_registration_like_objective(xr):
     """6 parameters with xReg's per-coordinate scales (radians vs mm) and bounds."""
     target = np.array([0.05, -0.03, 0.08, 4.0, -6.0, 9.0])

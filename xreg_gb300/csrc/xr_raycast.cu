@@ -395,7 +395,8 @@ drr_kernel(const DrrParams p, const int64_t proj_base) {
 // are the fastest index within a job for L2 reuse across nearby poses.  Blocks
 // never wait on one another (the counter is only incremented), so a block that
 // finds no work simply exits.  Line-integral sum kernel, 16x16-pixel tiles,
-// unroll 2; the layout and voxel type are per job.
+// loop 3 (macro-cell trim when the job's occupancy is set, then two samples
+// per iteration); the layout and voxel type are per job.
 __global__ void __launch_bounds__(kThreads) drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs,
                                                              long long total, unsigned long long* counter) {
   __shared__ long long s_item;
@@ -420,19 +421,19 @@ __global__ void __launch_bounds__(kThreads) drr_multi_kernel(const MultiJobDrr* 
       const int sel = J.p.vol.voxel_type * 4 + J.p.vol.layout;
       switch (sel) {
         case XR_VOXEL_F32 * 4 + XR_LAYOUT_LINEAR:
-          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, 2>(J.p, proj, row, col); break;
+          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, kUnrollMacroSkip>(J.p, proj, row, col); break;
         case XR_VOXEL_F32 * 4 + XR_LAYOUT_CELL8:
-          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, 2>(J.p, proj, row, col); break;
+          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, kUnrollMacroSkip>(J.p, proj, row, col); break;
         case XR_VOXEL_F32 * 4 + kLayoutCell8Wide:
-          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, kLayoutCell8Wide, 2>(J.p, proj, row, col); break;
+          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, kLayoutCell8Wide, kUnrollMacroSkip>(J.p, proj, row, col); break;
         case XR_VOXEL_F16 * 4 + XR_LAYOUT_LINEAR:
-          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, 2>(J.p, proj, row, col); break;
+          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, kUnrollMacroSkip>(J.p, proj, row, col); break;
         case XR_VOXEL_F16 * 4 + XR_LAYOUT_CELL8:
-          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, 2>(J.p, proj, row, col); break;
+          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, kUnrollMacroSkip>(J.p, proj, row, col); break;
         case XR_VOXEL_BF16 * 4 + XR_LAYOUT_LINEAR:
-          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, 2>(J.p, proj, row, col); break;
+          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, kUnrollMacroSkip>(J.p, proj, row, col); break;
         case XR_VOXEL_BF16 * 4 + XR_LAYOUT_CELL8:
-          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, 2>(J.p, proj, row, col); break;
+          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, kUnrollMacroSkip>(J.p, proj, row, col); break;
         default: break;
       }
     }
