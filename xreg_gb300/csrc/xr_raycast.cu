@@ -139,8 +139,6 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
   return fmaf(b1, fz, b0 * gz);
 }
 
-// Traces the ray of pixel (row, col) of projection proj and stores the result
-// (the caller checks that the pixel exists).  Returns the number of samples.
 // Walks the macro cells of the ray p0 + k st from k = kstart towards kend
 // (dir +1 forward, -1 backward) and returns the ray parameter at which it
 // enters the first macro cell whose (dilated) occupancy bit is set, or +inf
@@ -192,6 +190,8 @@ __device__ __forceinline__ float macro_march(const VolView& v, const float p0[3]
   return k;  // walk limit: treat the rest as occupied
 }
 
+// Traces the ray of pixel (row, col) of projection proj and stores the result
+// (the caller checks that the pixel exists).  Returns the number of samples.
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, const int64_t proj, const int row,
                                                           const int col) {
