@@ -404,7 +404,8 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
                                           "max_abs_sim_diff_vs_f32": float(
                                               np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
         objh.close()
-    for key, fn in (("uneven_multi_job", lambda: _multi_job(xr, dev)),
+    for key, fn in (("precision_large", lambda: _precision(xr, dev, stream)),
+                    ("uneven_multi_job", lambda: _multi_job(xr, dev)),
                     ("serving", lambda: _serving(dev, a.serving_requests, a.serving_rate))):
         if key == "serving" and a.serving_requests <= 0:
             continue
@@ -412,6 +413,66 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
             out[key] = fn()
         except Exception as e:  # reported, never fatal to the headline line
             out[key] = {"error": f"{type(e).__name__}: {e}"}
+    return out
+
+
+def _precision(xr, dev, stream, pop: int = 20, reps: int = 5):
+    """The precision workload (512x512x400 phantom at 0.8x0.8x1 mm, 1536^2 detector
+    downsampled 2x to 768^2, patch grad-NCC 11x11 stride 1): population throughput
+    for float32, FP16 and BF16 volumes, and the FP16 / BF16 DRR and similarity
+    differences against the float32-volume path (errors against the FP64 oracle
+    are checked by the full-size GPU tests)."""
+    import torch
+    from xreg_gb300 import synth
+    w = synth.precision_large(0)
+    rc = xr.RayCasterLineIntCUDA(dev)
+    rc.set_volume(w.vol)
+    rc.set_camera_models(w.cams)
+    rc.set_ray_step_size(w.step)
+    rc.set_num_projs(1)
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(w.gt[None])
+    rc.compute()
+    fixed = synth.add_noise(rc.proj(0), 0.01, 3)
+    rc.close()
+    poses = synth.sample_poses(w.vol, w.gt, pop, 5.0, 10.0, seed=5)
+    dp = torch.from_numpy(poses.reshape(pop, 16).copy()).to(f"cuda:{dev}")
+    out = {"volume": "512x512x400 @0.8x0.8x1 mm", "detector": "768x768", "metric": "patch grad-NCC 11x11 stride 1",
+           "pop": pop}
+    ref_drr = ref_sims = None
+    for vname, vt in (("f32", 0), ("f16", 1), ("bf16", 2)):
+        rcv = xr.RayCasterLineIntCUDA(dev)
+        rcv.set_stream(stream.cuda_stream)
+        rcv.set_volume(w.vol, vt)
+        rcv.set_camera_models(w.cams)
+        rcv.set_ray_step_size(w.step)
+        m = xr.ImgSimMetric2DPatchGradNCCCUDA(dev)
+        m.set_fixed_image(fixed)
+        obj = xr.PopulationObjective(rcv, [m], pop)
+        ds = torch.empty(pop, dtype=torch.float32, device=f"cuda:{dev}")
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                obj.eval_device(pop, dp.data_ptr(), ds.data_ptr())
+        stream.synchronize()
+        drr = rcv.projs()[0].copy()
+        sims = ds.cpu().numpy().copy()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        with torch.cuda.stream(stream):
+            for s0, e0 in evs:
+                s0.record(stream)
+                obj.eval_device(pop, dp.data_ptr(), ds.data_ptr())
+                e0.record(stream)
+        torch.cuda.synchronize()
+        t = float(np.mean([s0.elapsed_time(e0) for s0, e0 in evs])) / 1e3
+        entry = {"poses_per_s": round(pop / t, 2)}
+        if ref_drr is None:
+            ref_drr, ref_sims = drr, sims
+        else:
+            body = ref_drr > 0.1 * ref_drr.max()
+            entry["drr_max_rel_diff_vs_f32_over_body"] = float(np.max(np.abs(drr[body] - ref_drr[body]) / ref_drr[body]))
+            entry["sim_max_abs_diff_vs_f32"] = float(np.max(np.abs(sims - ref_sims)))
+        out[vname] = entry
+        obj.close()
     return out
 
 

@@ -173,7 +173,9 @@ XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
  * across a 256-thread block (1, 2, 4 or 8; each warp covers 8x4 pixels) and
  * the sample loop: 1 or 2 samples per iteration, or 3 / 4 = 2 / 4 per iteration
  * after each ray is trimmed to its first and last occupied macro cell (sum
- * kernel with empty-space skipping on; otherwise 3 runs as 2).  layout
+ * kernel with empty-space skipping on; otherwise 3 and 4 run as 2), or 5 = 3
+ * with the second sample of a pair reusing the first's corners when both lie in
+ * one cell (256-bit float32 CELL8 read; elsewhere 5 runs as 3).  layout
  * XR_LAYOUT_AUTO (the default) lets
  * the autotuner time the candidates on the first compute of each shape (volume
  * size, voxel type, detector, projection count) and cache the fastest for the

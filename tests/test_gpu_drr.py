@@ -163,7 +163,7 @@ def test_store_methods_max_kernel_and_background(xr, oracle):
     np.testing.assert_allclose(rc.projs(), mx, rtol=1e-6, atol=0)
     # every loop variant gives the same maximum image (loops 3 and 4 run as 2 for the maximum)
     first = rc.projs()
-    for un in (1, 2, 3, 4):
+    for un in (1, 2, 3, 4, 5):
         rc.set_launch_config(1, 2, un)
         rc.compute()
         np.testing.assert_array_equal(rc.projs(), first)
@@ -225,12 +225,12 @@ def test_launch_configs_are_bit_identical(xr, oracle, vt):
     rc.compute()
     auto = rc.projs()
     lay, bw, un = rc.launch_config()
-    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2, 3, 4)
+    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2, 3, 4, 5)
     # layout 2: the float32 cell copy read with one 256-bit load per sample;
     # loops 3 / 4: two / four samples per iteration after the macro-cell trim
     for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
         for bw in (1, 2, 4, 8):
-            for un in (1, 2, 3, 4):
+            for un in (1, 2, 3, 4, 5):
                 rc.set_launch_config(layout, bw, un)
                 rc.compute()
                 assert rc.launch_config() == (layout, bw, un)
@@ -277,7 +277,7 @@ def test_empty_space_skipping_is_exact(xr, oracle, vt):
     for skip in (False, True):
         rc.set_empty_space_skipping(skip)
         for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
-            for un in (2, 3, 4):
+            for un in (2, 3, 4, 5):
                 rc.set_launch_config(layout, 2, un)
                 rc.compute()
                 outs.append((rc.projs(), rc.last_num_samples()))
@@ -319,7 +319,7 @@ def test_macro_cell_skipping_is_exact(xr, oracle, vt):
         rc.distribute_xforms_among_cam_models(poses)
         rc.set_count_samples(True)
         outs = []
-        for skip, un in ((False, 1), (True, 1), (True, 3), (True, 4)):
+        for skip, un in ((False, 1), (True, 1), (True, 3), (True, 4), (True, 5)):
             rc.set_empty_space_skipping(skip)
             for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
                 rc.set_launch_config(layout, 2, un)

@@ -54,6 +54,15 @@ struct Vox<XR_VOXEL_F32> {
         : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
         : "l"(p));
   }
+  // cell_wide when pred is true; otherwise v is left unwritten (no memory request).
+  __device__ __forceinline__ static void cell_wide_if(const void* b, int c, bool pred, float v[8]) {
+    const float* p = static_cast<const float*>(b) + 8 * (size_t)c;
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %9, 0;\n\t"
+        "@q ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t}"
+        : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7])
+        : "l"(p), "r"((unsigned)pred));
+  }
 };
 template <>
 struct Vox<XR_VOXEL_F16> {
@@ -93,6 +102,38 @@ constexpr int kLayoutCell8Wide = 2;
 // Sample-loop variant 3: macro-cell empty-space skipping (sum kernel).
 constexpr int kUnrollMacroSkip = 3;  // loop 2 after the macro-cell trim
 constexpr int kUnrollTrim4 = 4;      // four samples per iteration after the macro-cell trim
+constexpr int kUnrollPairShare = 5;  // loop 3 whose second sample of a pair reuses the first's cell
+
+// Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
+// the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
+// the last index gets weight 0 (weight 1 on the last voxel).  The weighted form
+// w0*a + w1*b keeps every term >= 0 for non-negative attenuation, so the
+// relative error stays at a few ulps even where the value is tiny.
+// Cell of a position for the CELL8 layouts, with its fractions (the clamping
+// rule of sample() below).
+__device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, float pz, float& fx, float& fy,
+                                       float& fz) {
+  const int nx = vol.nx, ny = vol.ny;
+  const int ix = max(min(__float2int_rd(px), nx - 2), 0);
+  const int iy = max(min(__float2int_rd(py), ny - 2), 0);
+  const int iz = max(min(__float2int_rd(pz), vol.nz - 2), 0);
+  fx = __saturatef(px - (float)ix);
+  fy = __saturatef(py - (float)iy);
+  fz = __saturatef(pz - (float)iz);
+  return (iz * (ny - 1) + iy) * (nx - 1) + ix;
+}
+
+// Weighted-form trilinear of the 8 corners v000 v100 v010 v110 v001 v101 v011 v111.
+__device__ __forceinline__ float interp8(const float v[8], float fx, float fy, float fz) {
+  const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+  const float a00 = fmaf(v[1], fx, v[0] * gx);
+  const float a10 = fmaf(v[3], fx, v[2] * gx);
+  const float a01 = fmaf(v[5], fx, v[4] * gx);
+  const float a11 = fmaf(v[7], fx, v[6] * gx);
+  const float b0 = fmaf(a10, fy, a00 * gy);
+  const float b1 = fmaf(a11, fy, a01 * gy);
+  return fmaf(b1, fz, b0 * gz);
+}
 
 // Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
 // the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
@@ -107,17 +148,21 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
   // 0 the cell is 0 and the fraction 0, above n-1 the cell is n-2 and the
   // fraction 1, and a NaN position reads cell 0 with fraction 0.
   (void)bx; (void)by; (void)bz;
-  const int nx = vol.nx, ny = vol.ny;
-  const int ix = max(min(__float2int_rd(px), nx - 2), 0);
-  const int iy = max(min(__float2int_rd(py), ny - 2), 0);
-  const int iz = max(min(__float2int_rd(pz), vol.nz - 2), 0);
-  const float fx = __saturatef(px - (float)ix), fy = __saturatef(py - (float)iy), fz = __saturatef(pz - (float)iz);
-  float v[8];
+  float v[8], fx, fy, fz;
   if (LAYOUT == kLayoutCell8Wide) {
-    if constexpr (VT == XR_VOXEL_F32) Vox<VT>::cell_wide(data, (iz * (ny - 1) + iy) * (nx - 1) + ix, v);
+    const int c = cell_of(vol, px, py, pz, fx, fy, fz);
+    if constexpr (VT == XR_VOXEL_F32) Vox<VT>::cell_wide(data, c, v);
   } else if (LAYOUT == XR_LAYOUT_CELL8) {
-    Vox<VT>::cell(data, (iz * (ny - 1) + iy) * (nx - 1) + ix, v);
+    const int c = cell_of(vol, px, py, pz, fx, fy, fz);
+    Vox<VT>::cell(data, c, v);
   } else {
+    const int nx = vol.nx, ny = vol.ny;
+    const int ix = max(min(__float2int_rd(px), nx - 2), 0);
+    const int iy = max(min(__float2int_rd(py), ny - 2), 0);
+    const int iz = max(min(__float2int_rd(pz), vol.nz - 2), 0);
+    fx = __saturatef(px - (float)ix);
+    fy = __saturatef(py - (float)iy);
+    fz = __saturatef(pz - (float)iz);
     const int sy = nx, sz = nx * ny;
     const int b = (iz * ny + iy) * nx + ix;
     v[0] = Vox<VT>::ld(data, b);
@@ -129,14 +174,7 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
     v[6] = Vox<VT>::ld(data, b + sz + sy);
     v[7] = Vox<VT>::ld(data, b + sz + sy + 1);
   }
-  const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-  const float a00 = fmaf(v[1], fx, v[0] * gx);
-  const float a10 = fmaf(v[3], fx, v[2] * gx);
-  const float a01 = fmaf(v[5], fx, v[4] * gx);
-  const float a11 = fmaf(v[7], fx, v[6] * gx);
-  const float b0 = fmaf(a10, fy, a00 * gy);
-  const float b1 = fmaf(a11, fy, a01 * gy);
-  return fmaf(b1, fz, b0 * gz);
+  return interp8(v, fx, fy, fz);
 }
 
 // Walks the macro cells of the ray p0 + k st from k = kstart towards kend
@@ -331,7 +369,30 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
             }
           }
         }
-        if (UNROLL >= 2) {  // loops 3 and 4 finish with the two-sample loop
+        if (UNROLL == kUnrollPairShare && LAYOUT == kLayoutCell8Wide && KERNEL == XR_LINE_INT_SUM) {
+          // Two samples per iteration; at a step below the voxel size both often
+          // fall in one cell, and then the second load is not issued (its lane
+          // makes no memory request) and the first sample's corners are reused.
+          for (; n >= 2; n -= 2) {
+            float f0x, f0y, f0z, f1x, f1y, f1z;
+            const int c0 = cell_of(p.vol, px, py, pz, f0x, f0y, f0z);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            const int c1 = cell_of(p.vol, px, py, pz, f1x, f1y, f1z);
+            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+            float v0[8], v1[8];
+            if constexpr (VT == XR_VOXEL_F32) {
+              Vox<VT>::cell_wide(data, c0, v0);
+#pragma unroll
+              for (int i = 0; i < 8; ++i) v1[i] = 0.0f;
+              Vox<VT>::cell_wide_if(data, c1, c1 != c0, v1);
+            }
+            const bool same = c1 == c0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v1[i] = same ? v0[i] : v1[i];
+            sum = __fadd_rn(__fadd_rn(sum, interp8(v0, f0x, f0y, f0z)), interp8(v1, f1x, f1y, f1z));
+          }
+        }
+        if (UNROLL >= 2) {  // loops 3, 4 and 5 finish with the two-sample loop
           for (; n >= 2; n -= 2) {
             const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
             px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
@@ -455,11 +516,14 @@ cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
 
 template <int VT, int KERNEL, int LAYOUT>
 cudaError_t launch_unroll(const DrrParams& p, cudaStream_t s) {
-  if (p.unroll == kUnrollMacroSkip || p.unroll == kUnrollTrim4) {
+  if (p.unroll >= kUnrollMacroSkip) {
     // the macro-cell trim exists for the sum kernel; the maximum kernel runs the
-    // plain two-sample loop, which gives the same image
+    // plain two-sample loop, which gives the same image; the shared-cell pair
+    // loop exists for the 256-bit float32 CELL8 read (elsewhere loop 3 runs)
     if constexpr (KERNEL == XR_LINE_INT_SUM) {
       if (p.unroll == kUnrollTrim4) return launch_t<VT, KERNEL, LAYOUT, kUnrollTrim4>(p, s);
+      if constexpr (LAYOUT == kLayoutCell8Wide && VT == XR_VOXEL_F32)
+        if (p.unroll == kUnrollPairShare) return launch_t<VT, KERNEL, LAYOUT, kUnrollPairShare>(p, s);
       return launch_t<VT, KERNEL, LAYOUT, kUnrollMacroSkip>(p, s);
     }
     return launch_t<VT, KERNEL, LAYOUT, 2>(p, s);
