@@ -4,6 +4,7 @@
 #include "xr_internal.h"
 #include "xreg_gb300_regi.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -1493,11 +1494,7 @@ extern "C" XR_API xr_status xr_jobset_create(int32_t device, xr_jobset* out) {
   js->device = dev;
   XR_CUDA_TRY(cudaStreamCreateWithFlags(&js->own_stream, cudaStreamNonBlocking));
   XR_CUDA_TRY(js->d_counter.reserve(256));
-  js->blocks = drr_multi_blocks();
-  if (js->blocks <= 0) {
-    cudaStreamDestroy(js->own_stream);
-    return fail(XR_ERR_CUDA, "xr_jobset_create: could not size the persistent grid");
-  }
+  js->blocks = 0;  // sized per launch from the kernel's occupancy
   *out = js.release();
   return XR_OK;
 }
@@ -1518,13 +1515,17 @@ extern "C" XR_API xr_status xr_jobset_set_stream(xr_jobset js, void* s) {
   return XR_OK;
 }
 
+// Sample loop of the job-set kernel: the macro-cell trim, then four samples per
+// iteration (the fastest loop measured on the batched workload).
+constexpr int32_t kJobSetLoop = 4;
+
 static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
                                 const double* const* xforms, bool host_in, float* const* sims, bool host_out) {
   XR_CHECK_ARG(js && objs && pops && xforms && sims && n > 0, "xr_jobset_eval: NULL argument or no jobs");
   DeviceGuard g(js->device);
   cudaStream_t s = js->stream();
   js->h_jobs.clear();
-  long long items = 0;
+  std::vector<int32_t> group;  // voxel type * 4 + layout of each job
   for (int32_t i = 0; i < n; ++i) {
     xr_objective obj = objs[i];
     XR_CHECK_ARG(obj && reg_contains(obj), "xr_jobset_eval: unknown or destroyed objective");
@@ -1550,22 +1551,53 @@ static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* obj
     // float32 volumes read their cell copy with one 256-bit load; half volumes with one 128-bit load
     J.p.vol.layout = vol.cells.p ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
     J.p.block_warps_x = 2;
-    J.p.unroll = 2;
+    J.p.unroll = kJobSetLoop;
     J.tiles_x = (int32_t)((J.p.cols + 15) / 16);
     J.tiles_y = (int32_t)((J.p.rows + 15) / 16);
-    J.item_begin = items;
-    items += (long long)J.p.num_projs * J.tiles_x * J.tiles_y;
     rc->last_layout = J.p.vol.layout;
     rc->last_bw = 2;
-    rc->last_unroll = 2;
+    rc->last_unroll = kJobSetLoop;
     js->h_jobs.push_back(J);
+    group.push_back(vol.type * 4 + J.p.vol.layout);
   }
-  XR_CUDA_TRY(js->d_jobs.reserve(js->h_jobs.size() * sizeof(MultiJobDrr)));
-  XR_CUDA_TRY(cudaMemcpyAsync(js->d_jobs.p, js->h_jobs.data(), js->h_jobs.size() * sizeof(MultiJobDrr),
+  // One persistent launch per (voxel type, layout) group, jobs of a group
+  // contiguous; item numbering restarts in each group.
+  std::vector<MultiJobDrr> ordered;
+  std::vector<std::pair<size_t, size_t>> ranges;  // [begin, end) of each group in `ordered`
+  std::vector<long long> group_items;
+  {
+    std::vector<int32_t> keys(group);
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    for (int32_t k : keys) {
+      const size_t b = ordered.size();
+      long long items = 0;
+      for (size_t i = 0; i < js->h_jobs.size(); ++i)
+        if (group[i] == k) {
+          MultiJobDrr J = js->h_jobs[i];
+          J.item_begin = items;
+          items += (long long)J.p.num_projs * J.tiles_x * J.tiles_y;
+          ordered.push_back(J);
+        }
+      ranges.emplace_back(b, ordered.size());
+      group_items.push_back(items);
+    }
+  }
+  XR_CUDA_TRY(js->d_jobs.reserve(ordered.size() * sizeof(MultiJobDrr)));
+  XR_CUDA_TRY(cudaMemcpyAsync(js->d_jobs.p, ordered.data(), ordered.size() * sizeof(MultiJobDrr),
                               cudaMemcpyHostToDevice, s));
-  XR_CUDA_TRY(launch_drr_multi(js->d_jobs.as<MultiJobDrr>(), (int)js->h_jobs.size(), items,
-                               js->d_counter.as<unsigned long long>(), js->blocks, s));
-  js->last_items = items;
+  js->last_items = 0;
+  js->blocks = 0;
+  for (size_t gi = 0; gi < ranges.size(); ++gi) {
+    const MultiJobDrr& first = ordered[ranges[gi].first];
+    int blocks = 0;
+    XR_CUDA_TRY(launch_drr_multi(js->d_jobs.as<MultiJobDrr>() + ranges[gi].first,
+                                 (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
+                                 first.p.vol.voxel_type, first.p.vol.layout, kJobSetLoop,
+                                 js->d_counter.as<unsigned long long>(), &blocks, s));
+    js->last_items += group_items[gi];
+    js->blocks = std::max(js->blocks, blocks);
+  }
   for (int32_t i = 0; i < n; ++i) {
     xr_objective obj = objs[i];
     const int64_t pop = pops[i];

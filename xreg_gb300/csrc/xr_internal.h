@@ -86,11 +86,13 @@ struct MultiJobDrr {
   long long item_begin;  // items of this job: [item_begin, item_begin + num_projs * tiles_x * tiles_y)
   int32_t tiles_x, tiles_y;
 };
-// Persistent kernel over all jobs' (tile, projection) items; d_counter is reset here.
-cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long total_items,
-                             unsigned long long* d_counter, int blocks, cudaStream_t s);
-// Blocks that fill the current device once (SMs x resident blocks per SM).
-int drr_multi_blocks();
+// Persistent kernel over the (tile, projection) items of jobs that share a voxel
+// type and layout, one grid filling the current device once; unroll 3 or 4 is
+// the sample loop (macro-cell trim, 2 or 4 samples per iteration); d_counter is
+// reset here.
+cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long total_items, int32_t voxel_type,
+                             int32_t layout, int32_t unroll, unsigned long long* d_counter, int* blocks_out,
+                             cudaStream_t s);
 // Macro-cell occupancy bitmask of a volume (see VolView::occ); d_occ holds
 // ceil(nmx * nmy * nmz / 32) words and is cleared here.
 cudaError_t launch_build_occupancy(const float* vox_f32, int nx, int ny, int nz, uint32_t* d_occ, int nmx, int nmy,

@@ -455,11 +455,12 @@ drr_kernel(const DrrParams p, const int64_t proj_base) {
 // (job, tile, projection) from a global counter until all are done; projections
 // are the fastest index within a job for L2 reuse across nearby poses.  Blocks
 // never wait on one another (the counter is only incremented), so a block that
-// finds no work simply exits.  Line-integral sum kernel, 16x16-pixel tiles,
-// loop 3 (macro-cell trim when the job's occupancy is set, then two samples
-// per iteration); the layout and voxel type are per job.
-__global__ void __launch_bounds__(kThreads) drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs,
-                                                             long long total, unsigned long long* counter) {
+// finds no work simply exits.  Line-integral sum kernel, 16x16-pixel tiles; one
+// instantiation per voxel type, layout and sample loop, so the jobs of one
+// launch share those (the host groups them).
+template <int VT, int LAYOUT, int UNROLL>
+__global__ void __launch_bounds__(kThreads, UNROLL == kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
+drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long total, unsigned long long* counter) {
   __shared__ long long s_item;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
@@ -478,27 +479,42 @@ __global__ void __launch_bounds__(kThreads) drr_multi_kernel(const MultiJobDrr* 
     const int ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
     const int col = tx * 16 + (warp & 1) * 8 + (lane & 7);
     const int row = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
-    if (col < J.p.cols && row < J.p.rows) {
-      const int sel = J.p.vol.voxel_type * 4 + J.p.vol.layout;
-      switch (sel) {
-        case XR_VOXEL_F32 * 4 + XR_LAYOUT_LINEAR:
-          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, kUnrollMacroSkip>(J.p, proj, row, col); break;
-        case XR_VOXEL_F32 * 4 + XR_LAYOUT_CELL8:
-          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, kUnrollMacroSkip>(J.p, proj, row, col); break;
-        case XR_VOXEL_F32 * 4 + kLayoutCell8Wide:
-          trace_pixel<XR_VOXEL_F32, XR_LINE_INT_SUM, kLayoutCell8Wide, kUnrollMacroSkip>(J.p, proj, row, col); break;
-        case XR_VOXEL_F16 * 4 + XR_LAYOUT_LINEAR:
-          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, kUnrollMacroSkip>(J.p, proj, row, col); break;
-        case XR_VOXEL_F16 * 4 + XR_LAYOUT_CELL8:
-          trace_pixel<XR_VOXEL_F16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, kUnrollMacroSkip>(J.p, proj, row, col); break;
-        case XR_VOXEL_BF16 * 4 + XR_LAYOUT_LINEAR:
-          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_LINEAR, kUnrollMacroSkip>(J.p, proj, row, col); break;
-        case XR_VOXEL_BF16 * 4 + XR_LAYOUT_CELL8:
-          trace_pixel<XR_VOXEL_BF16, XR_LINE_INT_SUM, XR_LAYOUT_CELL8, kUnrollMacroSkip>(J.p, proj, row, col); break;
-        default: break;
-      }
-    }
+    if (col < J.p.cols && row < J.p.rows) trace_pixel<VT, XR_LINE_INT_SUM, LAYOUT, UNROLL>(J.p, proj, row, col);
   }
+}
+
+template <int VT, int LAYOUT, int UNROLL>
+int multi_blocks_t() {
+  static int cached[64] = {0};  // per device
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (cached[dev]) return cached[dev];
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drr_multi_kernel<VT, LAYOUT, UNROLL>, kThreads, 0) !=
+      cudaSuccess)
+    return 0;
+  cached[dev] = sms * (per_sm > 0 ? per_sm : 1);
+  return cached[dev];
+}
+
+template <int VT, int LAYOUT, int UNROLL>
+cudaError_t launch_multi_t(const MultiJobDrr* d_jobs, int njobs, long long total, unsigned long long* d_counter,
+                           int* blocks_out, cudaStream_t s) {
+  const int blocks = multi_blocks_t<VT, LAYOUT, UNROLL>();
+  if (blocks <= 0) return cudaErrorInvalidConfiguration;
+  *blocks_out = blocks;
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  drr_multi_kernel<VT, LAYOUT, UNROLL><<<blocks, kThreads, 0, s>>>(d_jobs, njobs, total, d_counter);
+  return cudaGetLastError();
+}
+
+template <int VT, int LAYOUT>
+cudaError_t launch_multi_unroll(const MultiJobDrr* d_jobs, int njobs, long long total, unsigned long long* d_counter,
+                                int unroll, int* blocks_out, cudaStream_t s) {
+  if (unroll == kUnrollTrim4)
+    return launch_multi_t<VT, LAYOUT, kUnrollTrim4>(d_jobs, njobs, total, d_counter, blocks_out, s);
+  return launch_multi_t<VT, LAYOUT, kUnrollMacroSkip>(d_jobs, njobs, total, d_counter, blocks_out, s);
 }
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
@@ -663,21 +679,29 @@ cudaError_t launch_support_box(const float* vox_f32, int nx, int ny, int nz, int
   return cudaGetLastError();
 }
 
-int drr_multi_blocks() {
-  int dev = 0, sms = 0, per_sm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drr_multi_kernel, kThreads, 0) != cudaSuccess) return 0;
-  return sms * (per_sm > 0 ? per_sm : 1);
-}
-
-cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long total_items,
-                             unsigned long long* d_counter, int blocks, cudaStream_t s) {
+cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long total_items, int32_t voxel_type,
+                             int32_t layout, int32_t unroll, unsigned long long* d_counter, int* blocks_out,
+                             cudaStream_t s) {
+  *blocks_out = 0;
   if (total_items <= 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return e;
-  drr_multi_kernel<<<blocks, kThreads, 0, s>>>(d_jobs, njobs, total_items, d_counter);
-  return cudaGetLastError();
+  switch (voxel_type * 4 + layout) {
+    case XR_VOXEL_F32 * 4 + XR_LAYOUT_LINEAR:
+      return launch_multi_unroll<XR_VOXEL_F32, XR_LAYOUT_LINEAR>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    case XR_VOXEL_F32 * 4 + XR_LAYOUT_CELL8:
+      return launch_multi_unroll<XR_VOXEL_F32, XR_LAYOUT_CELL8>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    case XR_VOXEL_F32 * 4 + kLayoutCell8Wide:
+      return launch_multi_unroll<XR_VOXEL_F32, kLayoutCell8Wide>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    case XR_VOXEL_F16 * 4 + XR_LAYOUT_LINEAR:
+      return launch_multi_unroll<XR_VOXEL_F16, XR_LAYOUT_LINEAR>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    case XR_VOXEL_F16 * 4 + XR_LAYOUT_CELL8:
+      return launch_multi_unroll<XR_VOXEL_F16, XR_LAYOUT_CELL8>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    case XR_VOXEL_BF16 * 4 + XR_LAYOUT_LINEAR:
+      return launch_multi_unroll<XR_VOXEL_BF16, XR_LAYOUT_LINEAR>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    case XR_VOXEL_BF16 * 4 + XR_LAYOUT_CELL8:
+      return launch_multi_unroll<XR_VOXEL_BF16, XR_LAYOUT_CELL8>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    default:
+      return cudaErrorInvalidValue;
+  }
 }
 
 size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type) {
