@@ -110,16 +110,26 @@ constexpr int kUnrollPairShare = 5;  // loop 3 whose second sample of a pair reu
 // w0*a + w1*b keeps every term >= 0 for non-negative attenuation, so the
 // relative error stays at a few ulps even where the value is tiny.
 // Cell of a position for the CELL8 layouts, with its fractions (the clamping
-// rule of sample() below).
+// rule of sample() below).  INSIDE: the caller has shown that the position lies
+// in [0, n-1) on every axis, where the clamps and the saturation change
+// nothing, so they are left out (same cell, same fractions).
+template <bool INSIDE = false>
 __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, float pz, float& fx, float& fy,
                                        float& fz) {
   const int nx = vol.nx, ny = vol.ny;
-  const int ix = max(min(__float2int_rd(px), nx - 2), 0);
-  const int iy = max(min(__float2int_rd(py), ny - 2), 0);
-  const int iz = max(min(__float2int_rd(pz), vol.nz - 2), 0);
-  fx = __saturatef(px - (float)ix);
-  fy = __saturatef(py - (float)iy);
-  fz = __saturatef(pz - (float)iz);
+  int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
+  if (INSIDE) {
+    fx = px - (float)ix;
+    fy = py - (float)iy;
+    fz = pz - (float)iz;
+  } else {
+    ix = max(min(ix, nx - 2), 0);
+    iy = max(min(iy, ny - 2), 0);
+    iz = max(min(iz, vol.nz - 2), 0);
+    fx = __saturatef(px - (float)ix);
+    fy = __saturatef(py - (float)iy);
+    fz = __saturatef(pz - (float)iz);
+  }
   return (iz * (ny - 1) + iy) * (nx - 1) + ix;
 }
 
@@ -140,29 +150,34 @@ __device__ __forceinline__ float interp8(const float v[8], float fx, float fy, f
 // the last index gets weight 0 (weight 1 on the last voxel).  The weighted form
 // w0*a + w1*b keeps every term >= 0 for non-negative attenuation, so the
 // relative error stays at a few ulps even where the value is tiny.
-template <int VT, int LAYOUT>
-__device__ __forceinline__ float sample(const VolView& vol, const void* data, float px, float py, float pz,
-                                        float bx, float by, float bz) {
+template <int VT, int LAYOUT, bool INSIDE = false>
+__device__ __forceinline__ float sample(const VolView& vol, const void* data, float px, float py, float pz) {
   // Cell = floor(position) clamped to [0, n-2]; fraction = position - cell
   // saturated to [0, 1].  Equal to clamping the position to [0, n-1] first: below
   // 0 the cell is 0 and the fraction 0, above n-1 the cell is n-2 and the
   // fraction 1, and a NaN position reads cell 0 with fraction 0.
-  (void)bx; (void)by; (void)bz;
   float v[8], fx, fy, fz;
   if (LAYOUT == kLayoutCell8Wide) {
-    const int c = cell_of(vol, px, py, pz, fx, fy, fz);
+    const int c = cell_of<INSIDE>(vol, px, py, pz, fx, fy, fz);
     if constexpr (VT == XR_VOXEL_F32) Vox<VT>::cell_wide(data, c, v);
   } else if (LAYOUT == XR_LAYOUT_CELL8) {
-    const int c = cell_of(vol, px, py, pz, fx, fy, fz);
+    const int c = cell_of<INSIDE>(vol, px, py, pz, fx, fy, fz);
     Vox<VT>::cell(data, c, v);
   } else {
     const int nx = vol.nx, ny = vol.ny;
-    const int ix = max(min(__float2int_rd(px), nx - 2), 0);
-    const int iy = max(min(__float2int_rd(py), ny - 2), 0);
-    const int iz = max(min(__float2int_rd(pz), vol.nz - 2), 0);
-    fx = __saturatef(px - (float)ix);
-    fy = __saturatef(py - (float)iy);
-    fz = __saturatef(pz - (float)iz);
+    int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
+    if (INSIDE) {
+      fx = px - (float)ix;
+      fy = py - (float)iy;
+      fz = pz - (float)iz;
+    } else {
+      ix = max(min(ix, nx - 2), 0);
+      iy = max(min(iy, ny - 2), 0);
+      iz = max(min(iz, vol.nz - 2), 0);
+      fx = __saturatef(px - (float)ix);
+      fy = __saturatef(py - (float)iy);
+      fz = __saturatef(pz - (float)iz);
+    }
     const int sy = nx, sz = nx * ny;
     const int b = (iz * ny + iy) * nx + ix;
     v[0] = Vox<VT>::ld(data, b);
@@ -228,6 +243,79 @@ __device__ __forceinline__ float macro_march(const VolView& v, const float p0[3]
   return k;  // walk limit: treat the rest as occupied
 }
 
+// The samples of one ray from the current position on, n of them, in order
+// (the sum order never changes with UNROLL).  INSIDE: every position stays in
+// [0, n-1) on every axis (see sample()).
+template <int VT, int KERNEL, int LAYOUT, int UNROLL, bool INSIDE>
+__device__ __forceinline__ float march_samples(const DrrParams& p, const void* data, float px, float py, float pz,
+                                               const float sx, const float sy, const float sz, unsigned int n,
+                                               float sum) {
+  if (UNROLL == kUnrollTrim4) {  // four loads in flight per thread
+    for (; n >= 4; n -= 4) {
+      const float v0 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      const float v1 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      const float v2 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      const float v3 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      if (KERNEL == XR_LINE_INT_MAX) {
+        sum = (sum < v0) ? v0 : sum;
+        sum = (sum < v1) ? v1 : sum;
+        sum = (sum < v2) ? v2 : sum;
+        sum = (sum < v3) ? v3 : sum;
+      } else {
+        sum = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(sum, v0), v1), v2), v3);
+      }
+    }
+  }
+  if (UNROLL == kUnrollPairShare && LAYOUT == kLayoutCell8Wide && KERNEL == XR_LINE_INT_SUM) {
+    // Two samples per iteration; at a step below the voxel size both often
+    // fall in one cell, and then the second load is not issued (its lane
+    // makes no memory request) and the first sample's corners are reused.
+    for (; n >= 2; n -= 2) {
+      float f0x, f0y, f0z, f1x, f1y, f1z;
+      const int c0 = cell_of<INSIDE>(p.vol, px, py, pz, f0x, f0y, f0z);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      const int c1 = cell_of<INSIDE>(p.vol, px, py, pz, f1x, f1y, f1z);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      float v0[8], v1[8];
+      if constexpr (VT == XR_VOXEL_F32) {
+        Vox<VT>::cell_wide(data, c0, v0);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v1[i] = 0.0f;
+        Vox<VT>::cell_wide_if(data, c1, c1 != c0, v1);
+      }
+      const bool same = c1 == c0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v1[i] = same ? v0[i] : v1[i];
+      sum = __fadd_rn(__fadd_rn(sum, interp8(v0, f0x, f0y, f0z)), interp8(v1, f1x, f1y, f1z));
+    }
+  }
+  if (UNROLL >= 2) {  // loops 3, 4 and 5 finish with the two-sample loop
+    for (; n >= 2; n -= 2) {
+      const float v0 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      const float v1 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
+      px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+      if (KERNEL == XR_LINE_INT_MAX) {
+        sum = (sum < v0) ? v0 : sum;
+        sum = (sum < v1) ? v1 : sum;
+      } else {
+        sum = __fadd_rn(__fadd_rn(sum, v0), v1);
+      }
+    }
+  }
+  for (; n > 0; --n) {
+    const float v0 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
+    px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+    if (KERNEL == XR_LINE_INT_MAX) sum = (sum < v0) ? v0 : sum;
+    else sum = __fadd_rn(sum, v0);
+  }
+  return sum;
+}
+
 // Traces the ray of pixel (row, col) of projection proj and stores the result
 // (the caller checks that the pixel exists).  Returns the number of samples.
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
@@ -284,7 +372,6 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
       const float sc = __fdiv_rn(p.step, lc);
       const float sx = __fmul_rn(dir[0], sc), sy = __fmul_rn(dir[1], sc), sz = __fmul_rn(dir[2], sc);
       const void* data = (LAYOUT != XR_LAYOUT_LINEAR) ? p.vol.cells : p.vol.voxels;
-      const float bx = maxb[0], by = maxb[1], bz = maxb[2];
       // Samples [first, last] may touch non-zero voxels; the others interpolate
       // only zeros, so for the sum they add exactly +0 and need no load.  The
       // samples before `first` still advance the position by the same float
@@ -314,6 +401,7 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
           last = f1 < (float)nsteps ? (unsigned int)f1 : (unsigned int)nsteps;
         }
       }
+      bool trim_ok = false;  // positions drift by less than an eighth of a voxel
       if (UNROLL >= kUnrollMacroSkip && KERNEL == XR_LINE_INT_SUM && p.vol.occ && hit && first <= last) {
         // Macro-cell trim: walk the macro grid from each end of [first, last]
         // to the first occupied macro cell; the samples before (after) it lie in
@@ -324,6 +412,7 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
         // 2^e, kept under a voxel by the 2^(22-e) sample limit.
         const int ebits = 32 - __clz(max(p.vol.nx, max(p.vol.ny, p.vol.nz)));
         if (ebits <= 22 && last < (1u << (22 - ebits))) {
+          trim_ok = true;
           const float p0[3] = {px, py, pz}, st[3] = {sx, sy, sz};
           const float kf = macro_march(p.vol, p0, st, (float)first, (float)last, 1);
           if (kf == INFINITY) {
@@ -343,75 +432,30 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
           }
         }
       }
+      // Rays whose first and last loaded samples lie at least a quarter voxel
+      // inside [0, n-1] on every axis keep every sample there (the segment is
+      // straight and the drift stays under an eighth of a voxel), so they run
+      // the sampler without clamps.
+      bool inside = false;
+      if (UNROLL >= kUnrollMacroSkip && trim_ok && first <= last) {
+        const float p0[3] = {px, py, pz}, st[3] = {sx, sy, sz};
+        inside = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float a = p0[k] + (float)first * st[k], b = p0[k] + (float)last * st[k];
+          inside = inside && fminf(a, b) >= 0.25f && fmaxf(a, b) <= maxb[k] - 0.25f;
+        }
+      }
       if (hit) {
         for (unsigned int s = 0; s < first && s <= last; ++s) {
           px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
         }
         // samples first..last in order; the sum order never changes with UNROLL
         unsigned int n = first <= last ? last - first + 1u : 0u;
-        if (UNROLL == kUnrollTrim4) {  // four loads in flight per thread
-          for (; n >= 4; n -= 4) {
-            const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            const float v1 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            const float v2 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            const float v3 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            if (KERNEL == XR_LINE_INT_MAX) {
-              sum = (sum < v0) ? v0 : sum;
-              sum = (sum < v1) ? v1 : sum;
-              sum = (sum < v2) ? v2 : sum;
-              sum = (sum < v3) ? v3 : sum;
-            } else {
-              sum = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(sum, v0), v1), v2), v3);
-            }
-          }
-        }
-        if (UNROLL == kUnrollPairShare && LAYOUT == kLayoutCell8Wide && KERNEL == XR_LINE_INT_SUM) {
-          // Two samples per iteration; at a step below the voxel size both often
-          // fall in one cell, and then the second load is not issued (its lane
-          // makes no memory request) and the first sample's corners are reused.
-          for (; n >= 2; n -= 2) {
-            float f0x, f0y, f0z, f1x, f1y, f1z;
-            const int c0 = cell_of(p.vol, px, py, pz, f0x, f0y, f0z);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            const int c1 = cell_of(p.vol, px, py, pz, f1x, f1y, f1z);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            float v0[8], v1[8];
-            if constexpr (VT == XR_VOXEL_F32) {
-              Vox<VT>::cell_wide(data, c0, v0);
-#pragma unroll
-              for (int i = 0; i < 8; ++i) v1[i] = 0.0f;
-              Vox<VT>::cell_wide_if(data, c1, c1 != c0, v1);
-            }
-            const bool same = c1 == c0;
-#pragma unroll
-            for (int i = 0; i < 8; ++i) v1[i] = same ? v0[i] : v1[i];
-            sum = __fadd_rn(__fadd_rn(sum, interp8(v0, f0x, f0y, f0z)), interp8(v1, f1x, f1y, f1z));
-          }
-        }
-        if (UNROLL >= 2) {  // loops 3, 4 and 5 finish with the two-sample loop
-          for (; n >= 2; n -= 2) {
-            const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            const float v1 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-            px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-            if (KERNEL == XR_LINE_INT_MAX) {
-              sum = (sum < v0) ? v0 : sum;
-              sum = (sum < v1) ? v1 : sum;
-            } else {
-              sum = __fadd_rn(__fadd_rn(sum, v0), v1);
-            }
-          }
-        }
-        for (; n > 0; --n) {
-          const float v0 = sample<VT, LAYOUT>(p.vol, data, px, py, pz, bx, by, bz);
-          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-          if (KERNEL == XR_LINE_INT_MAX) sum = (sum < v0) ? v0 : sum;
-          else sum = __fadd_rn(sum, v0);
-        }
+        if (inside)
+          sum = march_samples<VT, KERNEL, LAYOUT, UNROLL, true>(p, data, px, py, pz, sx, sy, sz, n, sum);
+        else
+          sum = march_samples<VT, KERNEL, LAYOUT, UNROLL, false>(p, data, px, py, pz, sx, sy, sz, n, sum);
         sum = __fmul_rn(sum, p.step);
         if (VT != XR_VOXEL_F32) sum = __fmul_rn(sum, p.vol.inv_scale);
         ns = nsteps + 1;
