@@ -475,8 +475,10 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
   return ns;
 }
 
+// Loop 4 keeps four cells (32 floats) in flight per thread: capped at 48
+// registers (5 blocks per SM), measured faster than 40 (small spills) or 64.
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, UNROLL == kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
+__global__ void __launch_bounds__(kThreads, UNROLL == kUnrollTrim4 ? kMinBlocksPerSM - 1 : kMinBlocksPerSM)
 drr_kernel(const DrrParams p, const int64_t proj_base) {
   // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
   // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
