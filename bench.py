@@ -145,13 +145,14 @@ def _peaks():
         return PEAK_FALLBACK_GBS, "fallback"
 
 
-def _ncu_traffic(workload_tag: str):
-    """Per-launch DRAM traffic of the DRR kernel from a committed ncu summary
-    (profiles/*.md line 'traffic_bytes_per_launch[<tag>]: N'), else None."""
+def _ncu_traffic(workload_tag: str, what: str = "traffic_bytes_per_launch"):
+    """A figure of the DRR kernel from a committed ncu summary (profiles/*.md line
+    '<what>[<tag>]: N', or '<what>: N' when workload_tag is empty), else None:
+    per-launch DRAM traffic, per-launch L2 traffic, the L2 sector peak."""
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return None
-    key = f"traffic_bytes_per_launch[{workload_tag}]:"
+    key = f"{what}[{workload_tag}]:" if workload_tag else f"{what}:"
     for fn in sorted(os.listdir(d)):
         if not fn.endswith(".md"):
             continue
@@ -300,6 +301,15 @@ def run_ours(a, rank, world, local):
     peak, peak_kind = _peaks()
     tag = f"batched-256^3-384^2-pop100-{a.voxel}-{lname}-loop{unroll}"
     traffic = _ncu_traffic(tag)
+    l2_bytes = _ncu_traffic(tag, "l2_bytes_per_launch")
+    l2_peak = _ncu_traffic("", "l2_sector_peak_gbs")
+    l2 = None
+    if l2_peak:
+        l2 = {"peak": l2_peak, "unit": "GB/s",
+              "peak_source": "ncu: lts__t_sectors per second / its pct_of_peak_sustained_elapsed (profiles/)",
+              "algorithmic_frac": round(achieved / l2_peak, 4),
+              "traffic": l2_bytes,
+              "traffic_frac": None if l2_bytes is None else round(l2_bytes / (drr_ms / 1e3) / 1e9 / l2_peak, 4)}
 
     extras = {}
     if not a.no_extras and rank == 0:
@@ -333,6 +343,7 @@ def run_ours(a, rank, world, local):
                      else "fallback 6.8 TB/s",
                      "alg_bytes_per_launch": alg_bytes, "samples_per_launch": samples,
                      "kernel_ms": round(drr_ms, 4),
+                     "l2": l2,
                      "note": "algorithmic bytes count 8 neighbour reads per trilinear sample; they are served "
                              "mostly from L1/L2, so frac compares gather throughput with the HBM copy peak"},
         "clocks": clk.summary(),

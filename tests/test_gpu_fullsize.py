@@ -11,6 +11,9 @@
   permuting the population permutes the values, FP16 stays within the metric
   tolerance of FP32.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -61,6 +64,17 @@ def test_precision_workload_drr(xr, oracle, precision):
     body = ref64 > 0.1 * ref64.max()
     for g in (g32, g16):
         assert np.median(np.abs(g[body] - ref64[body]) / ref64[body]) < 1e-3
+    report = {"workload": "512x512x400 @0.8x0.8x1 mm, 768^2, step %.2f mm, one pose" % w.step,
+              "samples": int(ns.sum())}
+    for name, g, rel in (("f32", g32, rel32), ("f16", g16, rel16), ("bf16", gbf, relbf)):
+        r64 = np.abs(g[body] - ref64[body]) / ref64[body]
+        report[name] = {"max_rel_vs_fp32_oracle": float(rel), "max_rel_vs_fp64_oracle_body": float(r64.max()),
+                        "median_rel_vs_fp64_oracle_body": float(np.median(r64)),
+                        "max_rel_vs_f32_volume_body": float(np.max(np.abs(g[body] - g32[body]) / g32[body]))}
+    r = np.abs(ref[body] - ref64[body]) / ref64[body]
+    report["fp32_oracle_itself"] = {"max_rel_vs_fp64_oracle_body": float(r.max()),
+                                    "median_rel_vs_fp64_oracle_body": float(np.median(r))}
+    _report("precision_drr", report)
 
 
 def test_precision_workload_patch_grad_ncc(xr, oracle, precision):
@@ -80,6 +94,18 @@ def test_precision_workload_patch_grad_ncc(xr, oracle, precision):
     ref = oracle.patch_grad_ncc(fixed, drr, smooth_ksize=5, radius=5, stride=1)
     np.testing.assert_allclose(got, ref, atol=1e-5, rtol=0)
     assert got[1] < got[0]  # the ground-truth pose scores better
+    _report("precision_patch_grad_ncc", {"gpu": got.tolist(), "oracle_fp64_on_same_drrs": ref.tolist(),
+                                         "max_abs_diff": float(np.max(np.abs(got - ref)))})
+
+
+def _report(name, d):
+    """Prints an error summary; also writes it as JSON into XREG_GB300_REPORT_DIR when set."""
+    print(name, json.dumps(d))
+    out = os.environ.get("XREG_GB300_REPORT_DIR")
+    if out:
+        os.makedirs(out, exist_ok=True)
+        with open(os.path.join(out, name + ".json"), "w") as f:
+            json.dump(d, f, indent=1)
 
 
 def test_batched_population_properties(xr):

@@ -1,7 +1,9 @@
 """Registration and serving on the GPU.
 
-* A two-level registration (CMA-ES at 8x then 4x downsampling, grad-NCC) of a
-  seeded phantom recovers the ground-truth pose.
+* A two-level registration (CMA-ES at 8x, then the bound-constrained trust
+  region at 4x, grad-NCC, fixed images downsampled from full-resolution DRRs)
+  of a seeded two-view phantom recovers the ground-truth pose within
+  0.05 deg / 0.1 mm.
 * The continuous-batching server gives every job exactly the result it gets
   when run alone (its optimizer has its own random stream and the job-set values
   equal the single-job values), while several jobs share each GPU step.
@@ -26,7 +28,9 @@ def test_two_level_registration_recovers_pose(xr):
     pose = job.run()
     rot, trans = pose_error(pose, gt, job.vol)
     assert err0[0] > 2.0 or err0[1] > 5.0  # it started away from the truth
-    assert rot < 0.5 and trans < 1.0, (rot, trans, err0)
+    print(f"start error {err0[0]:.3f} deg / {err0[1]:.3f} mm -> final {rot:.4f} deg / {trans:.4f} mm")
+    # the registration tolerance the path is specified with: 0.05 deg / 0.1 mm
+    assert rot < 0.05 and trans < 0.1, (rot, trans, err0)
     assert len(job.results) == 2 and job.results[1].best_value <= job.results[0].best_value + 0.05
 
 
