@@ -109,6 +109,17 @@ constexpr int kUnrollPairShare = 5;  // loop 3 whose second sample of a pair reu
 // the last index gets weight 0 (weight 1 on the last voxel).  The weighted form
 // w0*a + w1*b keeps every term >= 0 for non-negative attenuation, so the
 // relative error stays at a few ulps even where the value is tiny.
+// floor(x) as an integer and x - floor(x), for 0 <= x < 2^22, with float
+// additions only: x + 2^23 rounded down is 2^23 + floor(x) exactly, its bit
+// pattern minus that of 2^23 is floor(x), and subtracting 2^23 back and then
+// the result from x are exact.  Equal to the conversion-based floor and
+// fraction on that range.
+__device__ __forceinline__ void floor_split(float x, int& i, float& f) {
+  const float t = __fadd_rd(x, 8388608.0f);
+  i = __float_as_int(t) - 0x4B000000;
+  f = __fsub_rn(x, __fsub_rn(t, 8388608.0f));
+}
+
 // Cell of a position for the CELL8 layouts, with its fractions (the clamping
 // rule of sample() below).  INSIDE: the caller has shown that the position lies
 // in [0, n-1) on every axis, where the clamps and the saturation change
@@ -117,12 +128,15 @@ template <bool INSIDE = false>
 __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, float pz, float& fx, float& fy,
                                        float& fz) {
   const int nx = vol.nx, ny = vol.ny;
-  int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
+  int ix, iy, iz;
   if (INSIDE) {
-    fx = px - (float)ix;
-    fy = py - (float)iy;
-    fz = pz - (float)iz;
+    floor_split(px, ix, fx);
+    floor_split(py, iy, fy);
+    floor_split(pz, iz, fz);
   } else {
+    ix = __float2int_rd(px);
+    iy = __float2int_rd(py);
+    iz = __float2int_rd(pz);
     ix = max(min(ix, nx - 2), 0);
     iy = max(min(iy, ny - 2), 0);
     iz = max(min(iz, vol.nz - 2), 0);
@@ -165,12 +179,15 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
     Vox<VT>::cell(data, c, v);
   } else {
     const int nx = vol.nx, ny = vol.ny;
-    int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
+    int ix, iy, iz;
     if (INSIDE) {
-      fx = px - (float)ix;
-      fy = py - (float)iy;
-      fz = pz - (float)iz;
+      floor_split(px, ix, fx);
+      floor_split(py, iy, fy);
+      floor_split(pz, iz, fz);
     } else {
+      ix = __float2int_rd(px);
+      iy = __float2int_rd(py);
+      iz = __float2int_rd(pz);
       ix = max(min(ix, nx - 2), 0);
       iy = max(min(iy, ny - 2), 0);
       iz = max(min(iz, vol.nz - 2), 0);
@@ -447,7 +464,16 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
         }
       }
       if (hit) {
-        for (unsigned int s = 0; s < first && s <= last; ++s) {
+        // advance to sample `first` (four additions per trip: the skipped samples
+        // are a large part of a trimmed ray)
+        unsigned int skip = first <= last ? first : last + 1u;
+        for (; skip >= 4; skip -= 4) {
+          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+        }
+        for (; skip > 0; --skip) {
           px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
         }
         // samples first..last in order; the sum order never changes with UNROLL
