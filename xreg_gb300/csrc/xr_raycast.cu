@@ -109,17 +109,6 @@ constexpr int kUnrollPairShare = 5;  // loop 3 whose second sample of a pair reu
 // the last index gets weight 0 (weight 1 on the last voxel).  The weighted form
 // w0*a + w1*b keeps every term >= 0 for non-negative attenuation, so the
 // relative error stays at a few ulps even where the value is tiny.
-// floor(x) as an integer and x - floor(x), for 0 <= x < 2^22, with float
-// additions only: x + 2^23 rounded down is 2^23 + floor(x) exactly, its bit
-// pattern minus that of 2^23 is floor(x), and subtracting 2^23 back and then
-// the result from x are exact.  Equal to the conversion-based floor and
-// fraction on that range.
-__device__ __forceinline__ void floor_split(float x, int& i, float& f) {
-  const float t = __fadd_rd(x, 8388608.0f);
-  i = __float_as_int(t) - 0x4B000000;
-  f = __fsub_rn(x, __fsub_rn(t, 8388608.0f));
-}
-
 // Cell of a position for the CELL8 layouts, with its fractions (the clamping
 // rule of sample() below).  INSIDE: the caller has shown that the position lies
 // in [0, n-1) on every axis, where the clamps and the saturation change
@@ -128,15 +117,12 @@ template <bool INSIDE = false>
 __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, float pz, float& fx, float& fy,
                                        float& fz) {
   const int nx = vol.nx, ny = vol.ny;
-  int ix, iy, iz;
+  int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
   if (INSIDE) {
-    floor_split(px, ix, fx);
-    floor_split(py, iy, fy);
-    floor_split(pz, iz, fz);
+    fx = px - (float)ix;
+    fy = py - (float)iy;
+    fz = pz - (float)iz;
   } else {
-    ix = __float2int_rd(px);
-    iy = __float2int_rd(py);
-    iz = __float2int_rd(pz);
     ix = max(min(ix, nx - 2), 0);
     iy = max(min(iy, ny - 2), 0);
     iz = max(min(iz, vol.nz - 2), 0);
@@ -179,15 +165,12 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
     Vox<VT>::cell(data, c, v);
   } else {
     const int nx = vol.nx, ny = vol.ny;
-    int ix, iy, iz;
+    int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
     if (INSIDE) {
-      floor_split(px, ix, fx);
-      floor_split(py, iy, fy);
-      floor_split(pz, iz, fz);
+      fx = px - (float)ix;
+      fy = py - (float)iy;
+      fz = pz - (float)iz;
     } else {
-      ix = __float2int_rd(px);
-      iy = __float2int_rd(py);
-      iz = __float2int_rd(pz);
       ix = max(min(ix, nx - 2), 0);
       iy = max(min(iy, ny - 2), 0);
       iz = max(min(iz, vol.nz - 2), 0);
