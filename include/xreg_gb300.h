@@ -207,7 +207,9 @@ XR_API xr_status xr_sm_set_stream(xr_simmetric sm, void* cuda_stream);
 /* set_fixed_image (xregImgSimMetric2D.h:69): host float image, copied. */
 XR_API xr_status xr_sm_set_fixed_image(xr_simmetric sm, const float* host_img, int64_t rows, int64_t cols);
 /* set_mask (xregImgSimMetric2D.h:130): host uint8 image (nonzero = use), NULL clears.
- * Supported for XR_SIM_NCC and XR_SIM_GRAD_NCC. */
+ * NCC / grad-NCC: only masked-in pixels enter the statistics.  Patch metrics: the
+ * mask weights the patches and limits each patch's correlation sum, as the
+ * xr_patch_options below say. */
 XR_API xr_status xr_sm_set_mask(xr_simmetric sm, const uint8_t* host_mask);
 /* set_num_moving_images (xregImgSimMetric2D.h:93). */
 XR_API xr_status xr_sm_set_num_moving_images(xr_simmetric sm, int64_t n);
@@ -222,6 +224,54 @@ XR_API xr_status xr_sm_set_smooth_img_before_sobel_kernel_radius(xr_simmetric sm
 /* ImgSimMetric2DPatchCommon::set_patch_radius / set_patch_stride (defaults 5 and 1). */
 XR_API xr_status xr_sm_set_patch_radius(xr_simmetric sm, int32_t r);
 XR_API xr_status xr_sm_set_patch_stride(xr_simmetric sm, int32_t s);
+/* Options of the patch metrics, xReg's defaults in brackets:
+ * ImgSimMetric2DPatchCommon (xregImgSimMetric2DPatchCommon.h:140-180),
+ * ImgSimMetric2DPatchNCCCPU (xregImgSimMetric2DPatchNCCCPU.h:92-94),
+ * ImgSimMetric2DPatchGradNCCCPU (xregImgSimMetric2DPatchGradNCCCPU.h:100-104).
+ * Patch weights (xregImgSimMetric2DPatchCommon.cpp:306-410): the weight image
+ * (user-set, or the fixed-image patch variances) at each patch centre, zero at
+ * masked centres when use_mask_for_weighting; else, with a mask and
+ * use_mask_for_weighting, the patch's unmasked fraction; normalised to sum 1
+ * when normalize_weights_as_prob; otherwise 1.  Moving-image patch variances
+ * replace the weight per image (0 at masked centres, normalised; a total at or
+ * below 1e-6 gives the value FLT_MAX).  Per patch (xregImgSimMetric2DPatchNCCCPU.cpp:200-287):
+ * statistics over all pixels (over masked-in pixels when
+ * use_mask_for_patch_stats), correlation sum over masked-in pixels, score
+ * 1 - sum; a patch whose weight is at or below 1e-6 is left out when
+ * weight_patch_sims_in_combine.  Value: sum of weight x score over the patches
+ * used, divided by the patch count (compute_mean_of_patch_sims) or by the sum of
+ * their weights (weight_patch_sims_in_combine).  Random subsets
+ * (xregImgSimMetric2DPatchCommon.cpp:412-493): each compute draws
+ * num_rand_patches patches with probability proportional to the weights,
+ * rejecting those closer than rand_patch_min_pixels_sep to one already drawn;
+ * xReg seeds that draw from std::random_device, here from rand_seed. */
+typedef struct {
+  int32_t use_mask_for_weighting;                /* [1] */
+  int32_t use_mask_for_patch_stats;              /* [0] */
+  int32_t normalize_weights_as_prob;             /* [1] */
+  int32_t weight_patch_sims_in_combine;          /* [1] */
+  int32_t compute_mean_of_patch_sims;            /* [0] */
+  int32_t use_fixed_img_patch_variances_as_wgts; /* [0] */
+  int32_t use_mov_img_patch_variances_as_wgts;   /* [0] */
+  int32_t use_variances_in_grad_imgs_as_wgts;    /* [0] patch grad-NCC: variances of the gradient images */
+  int32_t choose_rand_patches;                   /* [0] */
+  int32_t reserved;
+  int64_t num_rand_patches;                      /* [100] */
+  double rand_patch_min_pixels_sep;              /* [-1] = sqrt(2) radius; 0 = no check */
+  uint64_t rand_seed;
+} xr_patch_options;
+/* xReg's defaults. */
+XR_API xr_status xr_patch_options_default(xr_patch_options* out);
+/* Takes effect at the next allocate_resources. */
+XR_API xr_status xr_sm_set_patch_options(xr_simmetric sm, const xr_patch_options* o);
+XR_API xr_status xr_sm_get_patch_options(xr_simmetric sm, xr_patch_options* o);
+/* set_wgt_img (xregImgSimMetric2DPatchCommon.h): host float image of the fixed
+ * image's size, read at patch centres; NULL clears.  Takes effect at the next
+ * allocate_resources. */
+XR_API xr_status xr_sm_set_patch_wgt_img(xr_simmetric sm, const float* host_img);
+/* Patches the last compute used, in draw order (row-major patch-centre grid
+ * indices); *count receives the number, at most cap are written. */
+XR_API xr_status xr_sm_patch_indices_used(xr_simmetric sm, int64_t cap, int64_t* idx, int64_t* count);
 /* allocate_resources (xregImgSimMetric2D.h:81): fixed-image statistics, gradients
  * and patch statistics are computed once here and stay on the device. */
 XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm);

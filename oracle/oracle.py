@@ -222,6 +222,63 @@ def patch_grad_ncc(fixed, movs, smooth_ksize=5, radius=5, stride=1) -> np.ndarra
     return out
 
 
+class patch_opts(C.Structure):
+    """Options of the masked / weighted patch metrics (xReg's defaults)."""
+    _fields_ = [("use_mask_for_weighting", C.c_int), ("use_mask_for_patch_stats", C.c_int),
+                ("normalize_weights_as_prob", C.c_int), ("weight_patch_sims_in_combine", C.c_int),
+                ("compute_mean_of_patch_sims", C.c_int), ("use_fixed_var_wgts", C.c_int),
+                ("use_mov_var_wgts", C.c_int), ("use_grad_var_wgts", C.c_int),
+                ("wgt_img", C.c_void_p), ("patch_count", C.c_void_p)]
+
+
+def _patch_opts(opts, shape, keep):
+    o = patch_opts(1, 0, 1, 1, 0, 0, 0, 0, None, None)
+    for k, v in (opts or {}).items():
+        if k == "wgt_img":
+            a = np.ascontiguousarray(v, dtype=np.float32).reshape(shape)
+            keep.append(a)
+            o.wgt_img = a.ctypes.data
+        elif k == "patch_count":
+            a = np.ascontiguousarray(v, dtype=np.int32)
+            keep.append(a)
+            o.patch_count = a.ctypes.data
+        else:
+            setattr(o, k, int(v))
+    return o
+
+
+def patch_ncc_ex(fixed, movs, radius=5, stride=1, mask=None, **opts) -> np.ndarray:
+    """Patch NCC with an optional mask and xReg's weighting options (double arithmetic)."""
+    f = np.ascontiguousarray(fixed, dtype=np.float32)
+    m = np.ascontiguousarray(movs, dtype=np.float32).reshape(-1, *f.shape)
+    keep = []
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).reshape(f.shape)
+    o = _patch_opts(opts, f.shape, keep)
+    out = np.zeros(m.shape[0], dtype=np.float64)
+    L = lib()
+    L.xo_patch_ncc_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                  C.c_void_p, C.POINTER(patch_opts), C.c_void_p]
+    assert L.xo_patch_ncc_ex(_p(f), _p(m), f.shape[0], f.shape[1], m.shape[0], radius, stride,
+                             None if mk is None else _p(mk), C.byref(o), _p(out)) == 0
+    return out
+
+
+def patch_grad_ncc_ex(fixed, movs, smooth_ksize=5, radius=5, stride=1, mask=None, **opts) -> np.ndarray:
+    """Patch grad-NCC with an optional mask and xReg's weighting options (double arithmetic)."""
+    f = np.ascontiguousarray(fixed, dtype=np.float32)
+    m = np.ascontiguousarray(movs, dtype=np.float32).reshape(-1, *f.shape)
+    keep = []
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).reshape(f.shape)
+    o = _patch_opts(opts, f.shape, keep)
+    out = np.zeros(m.shape[0], dtype=np.float64)
+    L = lib()
+    L.xo_patch_grad_ncc_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int,
+                                       C.c_int64, C.c_int64, C.c_void_p, C.POINTER(patch_opts), C.c_void_p]
+    assert L.xo_patch_grad_ncc_ex(_p(f), _p(m), f.shape[0], f.shape[1], m.shape[0], smooth_ksize, radius, stride,
+                                  None if mk is None else _p(mk), C.byref(o), _p(out)) == 0
+    return out
+
+
 def hu_to_lin_att(hu) -> np.ndarray:
     h = np.ascontiguousarray(hu, dtype=np.float32)
     out = np.empty_like(h)

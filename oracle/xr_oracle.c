@@ -800,6 +800,294 @@ XO_EXPORT int xo_patch_grad_ncc(const float* fixed, const float* mov, int64_t ro
   return rc;
 }
 
+/* ------------------------------------------------------------------------- */
+/* Patch NCC with masks, weights and patch subsets                            */
+/* (xregImgSimMetric2DPatchCommon.cpp:256-493, xregImgSimMetric2DPatchNCCCPU.cpp:34-441,558-619,
+ *  xregImgSimMetric2DPatchGradNCCCPU.cpp:34-400).  Double arithmetic.          */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int use_mask_for_weighting;      /* default 1 */
+  int use_mask_for_patch_stats;    /* default 0 */
+  int normalize_weights_as_prob;   /* default 1 */
+  int weight_patch_sims_in_combine;/* default 1 */
+  int compute_mean_of_patch_sims;  /* default 0 */
+  int use_fixed_var_wgts;          /* fixed-image patch variances as weights */
+  int use_mov_var_wgts;            /* moving-image patch variances as weights */
+  int use_grad_var_wgts;           /* patch grad-NCC: variances of the gradient images */
+  const float* wgt_img;            /* weight image (rows x cols) or NULL */
+  const int32_t* patch_count;      /* times each patch is used (npatch) or NULL = every patch once */
+} xo_patch_opts;
+
+/* ComputePatchMeanStdDev (xregImgSimMetric2DPatchNCCCPU.cpp:558-619): pixels with
+ * (!use_mask_for_stats || !mask || mask) count; the mean is divided and the
+ * variance formed only when more than one pixel counts; sd clamped at 1e-6. */
+static void xo_patch_stats_m(const double* img, int64_t cols, int64_t r0, int64_t c0, int64_t diam,
+                             const uint8_t* mask, int use_mask_for_stats, double* mean, double* sd, int64_t* cnt) {
+  int64_t n = 0;
+  double mu = 0;
+  for (int64_t r = 0; r < diam; ++r)
+    for (int64_t c = 0; c < diam; ++c) {
+      const int64_t i = (r0 + r) * cols + c0 + c;
+      if (!use_mask_for_stats || !mask || mask[i]) { mu += img[i]; ++n; }
+    }
+  double var = 0;
+  if (n > 1) {
+    mu /= (double)n;
+    for (int64_t r = 0; r < diam; ++r)
+      for (int64_t c = 0; c < diam; ++c) {
+        const int64_t i = (r0 + r) * cols + c0 + c;
+        if (!use_mask_for_stats || !mask || mask[i]) { const double t = img[i] - mu; var += t * t; }
+      }
+    var /= (double)(n - 1);
+  }
+  const double d = sqrt(var);
+  *mean = mu;
+  *sd = d < 1.0e-6 ? 1.0e-6 : d;
+  *cnt = n;
+}
+
+typedef struct {
+  int64_t rows, cols, radius, stride, diam, ncr, ncc, np;
+  const uint8_t* mask;
+  xo_patch_opts o;
+  double* fhat;       /* np * diam * diam scaled fixed patches */
+  double* w;          /* np static patch weights */
+  int32_t* cnt;       /* np multiplicities */
+  int64_t nused;      /* sum of multiplicities */
+} xo_pncc;
+
+static int64_t xo_pncc_centre(const xo_pncc* P, int64_t p, int64_t* cr, int64_t* cc) {
+  *cr = P->radius + (p / P->ncc) * P->stride;
+  *cc = P->radius + (p % P->ncc) * P->stride;
+  return *cr * P->cols + *cc;
+}
+
+/* compute_weights (xregImgSimMetric2DPatchCommon.cpp:306-410) given a weight image or none. */
+static void xo_pncc_weights(xo_pncc* P, const double* wimg) {
+  const int use_img = wimg != NULL;
+  const int use_mask = P->o.use_mask_for_weighting && P->mask;
+  for (int64_t p = 0; p < P->np; ++p) {
+    int64_t cr, cc;
+    const int64_t ci = xo_pncc_centre(P, p, &cr, &cc);
+    double w = 1.0;
+    if (use_img) {
+      w = wimg[ci];
+      if (use_mask && !P->mask[ci]) w = 0.0;
+    } else if (use_mask) {
+      int64_t k = 0;
+      for (int64_t r = 0; r < P->diam; ++r)
+        for (int64_t c = 0; c < P->diam; ++c)
+          if (P->mask[(cr - P->radius + r) * P->cols + cc - P->radius + c]) ++k;
+      w = (double)k / (double)(P->diam * P->diam);
+    }
+    P->w[p] = w;
+  }
+  if ((use_img || use_mask) && P->o.normalize_weights_as_prob) {
+    double s = 0;
+    for (int64_t p = 0; p < P->np; ++p) s += P->w[p];
+    for (int64_t p = 0; p < P->np; ++p) P->w[p] /= s;
+  }
+}
+
+/* Patch grid and fixed side; wimg_override: weight image handed down (patch grad-NCC). */
+static void xo_pncc_setup(xo_pncc* P, const double* f, int64_t rows, int64_t cols, int64_t radius, int64_t stride,
+                          const uint8_t* mask, const xo_patch_opts* o, const double* wimg_override) {
+  P->rows = rows; P->cols = cols; P->radius = radius; P->stride = stride; P->diam = 2 * radius + 1;
+  P->ncr = (rows - 1 - 2 * radius) / stride + 1;
+  P->ncc = (cols - 1 - 2 * radius) / stride + 1;
+  P->np = P->ncr * P->ncc;
+  P->mask = mask;
+  P->o = *o;
+  const int64_t dd = P->diam * P->diam;
+  P->fhat = (double*)malloc(sizeof(double) * (size_t)(P->np * dd));
+  P->w = (double*)malloc(sizeof(double) * (size_t)P->np);
+  P->cnt = (int32_t*)malloc(sizeof(int32_t) * (size_t)P->np);
+  double* wimg = NULL;
+  if (o->use_fixed_var_wgts && !wimg_override) wimg = (double*)calloc((size_t)(rows * cols), sizeof(double));
+  for (int64_t p = 0; p < P->np; ++p) {
+    int64_t cr, cc;
+    const int64_t ci = xo_pncc_centre(P, p, &cr, &cc);
+    double mu, sd;
+    int64_t n;
+    xo_patch_stats_m(f, cols, cr - radius, cc - radius, P->diam, mask, o->use_mask_for_patch_stats, &mu, &sd, &n);
+    for (int64_t r = 0; r < P->diam; ++r)
+      for (int64_t c = 0; c < P->diam; ++c)
+        P->fhat[p * dd + r * P->diam + c] = (f[(cr - radius + r) * cols + cc - radius + c] - mu) / (sd * (double)n);
+    if (wimg) {
+      if (mask && !o->use_mask_for_patch_stats)
+        xo_patch_stats_m(f, cols, cr - radius, cc - radius, P->diam, mask, 1, &mu, &sd, &n);
+      wimg[ci] = sd * sd;
+    }
+  }
+  const double* wsrc = wimg_override ? wimg_override : (wimg ? wimg : NULL);
+  if (!wsrc && o->wgt_img) {
+    wimg = (double*)malloc(sizeof(double) * (size_t)(rows * cols));
+    for (int64_t i = 0; i < rows * cols; ++i) wimg[i] = o->wgt_img[i];
+    wsrc = wimg;
+  }
+  xo_pncc_weights(P, wsrc);
+  free(wimg);
+  P->nused = 0;
+  for (int64_t p = 0; p < P->np; ++p) {
+    P->cnt[p] = o->patch_count ? o->patch_count[p] : 1;
+    P->nused += P->cnt[p];
+  }
+}
+
+static void xo_pncc_free(xo_pncc* P) { free(P->fhat); free(P->w); free(P->cnt); }
+
+/* Moving-image patch variances (all pixels, no mask) at unmasked centres, 0
+ * elsewhere, for every used patch (with multiplicity); normalised as a
+ * probability when asked.  Returns 0 when that normalisation finds a total at
+ * or below 1e-6 (the value is then FLT_MAX). */
+static int xo_pncc_mov_vars(const xo_pncc* P, const double* m, double* var) {
+  double s = 0;
+  for (int64_t p = 0; p < P->np; ++p) {
+    int64_t cr, cc;
+    const int64_t ci = xo_pncc_centre(P, p, &cr, &cc);
+    var[p] = 0.0;
+    if (!P->cnt[p]) continue;
+    if (!P->mask || P->mask[ci]) {
+      double mu, sd;
+      int64_t n;
+      xo_patch_stats_m(m, P->cols, cr - P->radius, cc - P->radius, P->diam, NULL, 0, &mu, &sd, &n);
+      var[p] = sd * sd;
+    }
+    s += P->cnt[p] * var[p];
+  }
+  if (P->o.normalize_weights_as_prob) {
+    if (!(s > 1.0e-6)) return 0;
+    for (int64_t p = 0; p < P->np; ++p) var[p] /= s;
+  }
+  return 1;
+}
+
+/* One moving image (ImgSimMetric2DPatchNCCCPU::compute, :74-287); mvar: per patch
+ * moving-variance weights (already normalised) or NULL. */
+static double xo_pncc_eval(const xo_pncc* P, const double* m, const double* mvar) {
+  const int64_t dd = P->diam * P->diam;
+  double total = 0;
+  for (int64_t p = 0; p < P->np; ++p) {
+    if (!P->cnt[p]) continue;
+    int64_t cr, cc;
+    xo_pncc_centre(P, p, &cr, &cc);
+    const double wgt = mvar ? mvar[p] : P->w[p];
+    double val = 0.0;
+    if (!P->o.weight_patch_sims_in_combine || fabs(wgt) > 1.0e-6) {
+      double mu, sd;
+      int64_t n;
+      xo_patch_stats_m(m, P->cols, cr - P->radius, cc - P->radius, P->diam, P->mask, P->o.use_mask_for_patch_stats,
+                       &mu, &sd, &n);
+      double acc = 0;
+      for (int64_t r = 0; r < P->diam; ++r)
+        for (int64_t c = 0; c < P->diam; ++c) {
+          const int64_t i = (cr - P->radius + r) * P->cols + cc - P->radius + c;
+          if (!P->mask || P->mask[i]) acc += ((m[i] - mu) / sd) * P->fhat[p * dd + r * P->diam + c];
+        }
+      val = (P->o.weight_patch_sims_in_combine ? wgt : 1.0) * (1.0 - acc);
+    }
+    total += P->cnt[p] * val;
+  }
+  if (P->o.compute_mean_of_patch_sims) {
+    total /= (double)P->nused;
+  } else if (P->o.weight_patch_sims_in_combine) {
+    double tw = 0;
+    for (int64_t p = 0; p < P->np; ++p) tw += P->cnt[p] * P->w[p];
+    total /= tw;
+  }
+  return total;
+}
+
+#define XO_FLT_MAX 3.4028234663852886e38
+
+XO_EXPORT int xo_patch_ncc_ex(const float* fixed, const float* mov, int64_t rows, int64_t cols, int64_t nimgs,
+                              int64_t radius, int64_t stride, const uint8_t* mask, const xo_patch_opts* o,
+                              double* out) {
+  const int64_t n = rows * cols;
+  double* f = (double*)malloc(sizeof(double) * (size_t)n);
+  double* m = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int64_t i = 0; i < n; ++i) f[i] = fixed[i];
+  xo_pncc P;
+  xo_pncc_setup(&P, f, rows, cols, radius, stride, mask, o, NULL);
+  double* var = (double*)malloc(sizeof(double) * (size_t)P.np);
+  for (int64_t k = 0; k < nimgs; ++k) {
+    for (int64_t i = 0; i < n; ++i) m[i] = mov[k * n + i];
+    if (o->use_mov_var_wgts) {
+      out[k] = xo_pncc_mov_vars(&P, m, var) ? xo_pncc_eval(&P, m, var) : XO_FLT_MAX;
+    } else {
+      out[k] = xo_pncc_eval(&P, m, NULL);
+    }
+  }
+  free(var);
+  xo_pncc_free(&P);
+  free(f); free(m);
+  return 0;
+}
+
+/* Patch grad-NCC with the same options (xregImgSimMetric2DPatchGradNCCCPU.cpp:34-400):
+ * patch NCC on gx and on gy, 0.5 (s_x + s_y).  Without use_grad_var_wgts the
+ * variance weights come from the (fixed / moving) images themselves and are
+ * shared by both directions; with it each direction uses its gradient image. */
+XO_EXPORT int xo_patch_grad_ncc_ex(const float* fixed, const float* mov, int64_t rows, int64_t cols, int64_t nimgs,
+                                   int smooth_ksize, int64_t radius, int64_t stride, const uint8_t* mask,
+                                   const xo_patch_opts* o, double* out) {
+  const int64_t n = rows * cols;
+  double* fgx = (double*)malloc(sizeof(double) * (size_t)n);
+  double* fgy = (double*)malloc(sizeof(double) * (size_t)n);
+  double* mgx = (double*)malloc(sizeof(double) * (size_t)n);
+  double* mgy = (double*)malloc(sizeof(double) * (size_t)n);
+  double* mimg = (double*)malloc(sizeof(double) * (size_t)n);
+  int rc = xo_grad_images(fixed, rows, cols, smooth_ksize, fgx, fgy);
+  if (rc) { free(fgx); free(fgy); free(mgx); free(mgy); free(mimg); return rc; }
+  xo_patch_opts so = *o;
+  double* wimg = NULL;
+  if (!o->use_grad_var_wgts) {
+    so.use_fixed_var_wgts = 0;
+    so.use_mov_var_wgts = 0;
+    if (o->use_fixed_var_wgts) {
+      /* variances of the fixed image's patches (mask-aware stats when masked) */
+      double* f = (double*)malloc(sizeof(double) * (size_t)n);
+      for (int64_t i = 0; i < n; ++i) f[i] = fixed[i];
+      wimg = (double*)calloc((size_t)n, sizeof(double));
+      const int64_t diam = 2 * radius + 1;
+      for (int64_t cr = radius; cr + radius <= rows - 1; cr += stride)
+        for (int64_t cc = radius; cc + radius <= cols - 1; cc += stride) {
+          double mu, sd;
+          int64_t k;
+          xo_patch_stats_m(f, cols, cr - radius, cc - radius, diam, mask, mask != NULL, &mu, &sd, &k);
+          wimg[cr * cols + cc] = sd * sd;
+        }
+      free(f);
+    }
+  }
+  xo_pncc X, Y;
+  xo_pncc_setup(&X, fgx, rows, cols, radius, stride, mask, &so, wimg);
+  xo_pncc_setup(&Y, fgy, rows, cols, radius, stride, mask, &so, wimg);
+  free(wimg);
+  double* vx = (double*)malloc(sizeof(double) * (size_t)X.np);
+  double* vy = (double*)malloc(sizeof(double) * (size_t)X.np);
+  for (int64_t k = 0; k < nimgs; ++k) {
+    xo_grad_images(mov + k * n, rows, cols, smooth_ksize, mgx, mgy);
+    if (o->use_mov_var_wgts && !o->use_grad_var_wgts) {
+      for (int64_t i = 0; i < n; ++i) mimg[i] = mov[k * n + i];
+      xo_pncc Pm = X;  /* same grid, mask, counts and normalisation flag */
+      if (!xo_pncc_mov_vars(&Pm, mimg, vx)) { out[k] = XO_FLT_MAX; continue; }
+      out[k] = 0.5 * (xo_pncc_eval(&X, mgx, vx) + xo_pncc_eval(&Y, mgy, vx));
+    } else if (o->use_mov_var_wgts) {
+      const double sx = xo_pncc_mov_vars(&X, mgx, vx) ? xo_pncc_eval(&X, mgx, vx) : XO_FLT_MAX;
+      const double sy = xo_pncc_mov_vars(&Y, mgy, vy) ? xo_pncc_eval(&Y, mgy, vy) : XO_FLT_MAX;
+      out[k] = 0.5 * (sx + sy);
+    } else {
+      out[k] = 0.5 * (xo_pncc_eval(&X, mgx, NULL) + xo_pncc_eval(&Y, mgy, NULL));
+    }
+  }
+  free(vx); free(vy);
+  xo_pncc_free(&X);
+  xo_pncc_free(&Y);
+  free(fgx); free(fgy); free(mgx); free(mgy); free(mimg);
+  return 0;
+}
+
 typedef struct {
   const float* fixed;
   const float* mov;

@@ -1,0 +1,191 @@
+"""Patch metrics with masks, weights and patch subsets against the oracle's
+restatement of ImgSimMetric2DPatchCommon / PatchNCCCPU / PatchGradNCCCPU
+(double arithmetic): mask-derived weights, masked correlation sums, statistics
+over masked-in pixels, a user weight image, fixed- and moving-image patch
+variances as weights (with the FLT_MAX value of flat moving images), the
+combine rules (weighted, unweighted, mean) and random patch subsets.
+Tolerance: absolute difference of each value <= 1e-5."""
+import numpy as np
+import pytest
+
+from tests.test_gpu_metrics import _drrs
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+FLT_MAX = np.finfo(np.float32).max
+
+
+def _eval(xr, cls, rc, fixed, n, radius, stride, mask=None, wgt=None, offset=1, **opts):
+    m = cls()
+    m.set_fixed_image(fixed)
+    if mask is not None:
+        m.set_mask(mask)
+    if wgt is not None:
+        m.set_wgt_img(wgt)
+    m.set_patch_radius(radius)
+    m.set_patch_stride(stride)
+    if opts:
+        m.set_patch_options(**opts)
+    m.set_num_moving_images(n)
+    m.set_mov_imgs_buf_from_ray_caster(rc, offset)
+    m.allocate_resources()
+    m.compute()
+    return m, m.sim_vals()
+
+
+def _mask(shape, seed, frac=0.35):
+    rng = np.random.default_rng(seed)
+    mk = (rng.random(shape) > frac).astype(np.uint8)
+    mk[: shape[0] // 4, : shape[1] // 3] = 0  # a masked-out block: patches with weight 0
+    return mk
+
+
+CASES = [
+    dict(),
+    dict(use_mask_for_patch_stats=1),
+    dict(use_mask_for_weighting=0),
+    dict(normalize_weights_as_prob=0),
+    dict(weight_patch_sims_in_combine=0),
+    dict(compute_mean_of_patch_sims=1),
+    dict(use_fixed_img_patch_variances_as_wgts=1),
+    dict(use_mov_img_patch_variances_as_wgts=1),
+    dict(use_mov_img_patch_variances_as_wgts=1, normalize_weights_as_prob=0),
+]
+
+ORACLE_KEYS = {"use_fixed_img_patch_variances_as_wgts": "use_fixed_var_wgts",
+               "use_mov_img_patch_variances_as_wgts": "use_mov_var_wgts",
+               "use_variances_in_grad_imgs_as_wgts": "use_grad_var_wgts"}
+
+
+def _okw(opts):
+    return {ORACLE_KEYS.get(k, k): v for k, v in opts.items()}
+
+
+@pytest.mark.parametrize("opts", CASES)
+def test_patch_ncc_options(xr, oracle, opts):
+    rc, imgs, fixed = _drrs(xr, seed=11)
+    mask = _mask(fixed.shape, 5)
+    _, got = _eval(xr, xr.ImgSimMetric2DPatchNCCCUDA, rc, fixed, 6, 3, 2, mask=mask, **opts)
+    ref = oracle.patch_ncc_ex(fixed, imgs[1:], radius=3, stride=2, mask=mask, **_okw(opts))
+    np.testing.assert_allclose(got, ref, atol=TOL, rtol=2e-6)
+
+
+@pytest.mark.parametrize("opts", CASES + [dict(use_fixed_img_patch_variances_as_wgts=1,
+                                               use_variances_in_grad_imgs_as_wgts=1),
+                                          dict(use_mov_img_patch_variances_as_wgts=1,
+                                               use_variances_in_grad_imgs_as_wgts=1)])
+def test_patch_grad_ncc_options(xr, oracle, opts):
+    rc, imgs, fixed = _drrs(xr, seed=12)
+    mask = _mask(fixed.shape, 6)
+    _, got = _eval(xr, xr.ImgSimMetric2DPatchGradNCCCUDA, rc, fixed, 6, 3, 2, mask=mask, **opts)
+    ref = oracle.patch_grad_ncc_ex(fixed, imgs[1:], smooth_ksize=5, radius=3, stride=2, mask=mask, **_okw(opts))
+    np.testing.assert_allclose(got, ref, atol=TOL, rtol=2e-6)
+
+
+def test_weight_image_and_no_mask(xr, oracle):
+    rc, imgs, fixed = _drrs(xr, seed=13)
+    wgt = np.random.default_rng(2).random(fixed.shape).astype(np.float32)
+    for cls, fn in ((xr.ImgSimMetric2DPatchNCCCUDA, oracle.patch_ncc_ex),
+                    (xr.ImgSimMetric2DPatchGradNCCCUDA, oracle.patch_grad_ncc_ex)):
+        _, got = _eval(xr, cls, rc, fixed, 6, 5, 1, wgt=wgt)
+        np.testing.assert_allclose(got, fn(fixed, imgs[1:], radius=5, stride=1, wgt_img=wgt), atol=TOL, rtol=0)
+        # with a mask too: masked centres get weight 0
+        mask = _mask(fixed.shape, 7)
+        _, got = _eval(xr, cls, rc, fixed, 6, 5, 1, wgt=wgt, mask=mask)
+        np.testing.assert_allclose(got, fn(fixed, imgs[1:], radius=5, stride=1, wgt_img=wgt, mask=mask),
+                                   atol=TOL, rtol=0)
+    # no mask and no options: the plain metric
+    _, got = _eval(xr, xr.ImgSimMetric2DPatchNCCCUDA, rc, fixed, 6, 3, 2)
+    np.testing.assert_allclose(got, oracle.patch_ncc(fixed, imgs[1:], radius=3, stride=2), atol=TOL, rtol=0)
+
+
+def test_flat_moving_images_give_flt_max(xr, oracle):
+    """Normalised moving-variance weights of an image whose patches are all flat
+    sum to at most 1e-6: the value is FLT_MAX, as in xReg."""
+    import torch
+    rng = np.random.default_rng(4)
+    fixed = rng.random((40, 44)).astype(np.float32)
+    movs = np.stack([np.full((40, 44), 2.0, np.float32), rng.random((40, 44)).astype(np.float32)])
+    d = torch.from_numpy(movs).cuda()
+    for cls, fn in ((xr.ImgSimMetric2DPatchNCCCUDA, oracle.patch_ncc_ex),
+                    (xr.ImgSimMetric2DPatchGradNCCCUDA, oracle.patch_grad_ncc_ex)):
+        m = cls()
+        m.set_fixed_image(fixed)
+        m.set_patch_radius(3)
+        m.set_patch_stride(2)
+        m.set_patch_options(use_mov_img_patch_variances_as_wgts=1)
+        m.set_num_moving_images(2)
+        m.set_mov_imgs_device_buf(d.data_ptr(), 0)
+        m.allocate_resources()
+        torch.cuda.synchronize()
+        m.compute()
+        got = m.sim_vals()
+        ref = fn(fixed, movs, radius=3, stride=2, use_mov_var_wgts=1)
+        assert got[0] == FLT_MAX and ref[0] > 1e38
+        assert abs(got[1] - ref[1]) <= TOL
+
+
+@pytest.mark.parametrize("grad", [0, 1])
+def test_random_patch_subsets(xr, oracle, grad):
+    rc, imgs, fixed = _drrs(xr, seed=14)
+    mask = _mask(fixed.shape, 8)
+    cls = xr.ImgSimMetric2DPatchGradNCCCUDA if grad else xr.ImgSimMetric2DPatchNCCCUDA
+    fn = oracle.patch_grad_ncc_ex if grad else oracle.patch_ncc_ex
+    m, got = _eval(xr, cls, rc, fixed, 6, 3, 1, mask=mask, choose_rand_patches=1, num_rand_patches=40,
+                   rand_seed=123)
+    idx = m.patch_indices_used()
+    assert idx.size == 40
+    ncc = fixed.shape[1] - 6
+    centres = np.stack([3 + idx // ncc, 3 + idx % ncc], axis=1).astype(np.float64)
+    dist = np.sqrt(((centres[:, None, :] - centres[None, :, :]) ** 2).sum(-1)) + np.eye(40) * 1e9
+    assert dist.min() >= np.sqrt(2.0 * 9.0) - 1e-9  # the default minimum separation
+    count = np.bincount(idx, minlength=(fixed.shape[0] - 6) * ncc).astype(np.int32)
+    ref = fn(fixed, imgs[1:], radius=3, stride=1, mask=mask, patch_count=count)
+    np.testing.assert_allclose(got, ref, atol=TOL, rtol=2e-6)
+    # each compute draws anew; the same seed repeats the draws
+    m.compute()
+    idx2 = m.patch_indices_used()
+    assert not np.array_equal(idx, idx2)
+    m2, _ = _eval(xr, cls, rc, fixed, 6, 3, 1, mask=mask, choose_rand_patches=1, num_rand_patches=40,
+                  rand_seed=123)
+    np.testing.assert_array_equal(m2.patch_indices_used(), idx)
+    # zero-weight (fully masked) patches are never drawn
+    w_zero = np.array([mask[int(r) - 3:int(r) + 4, int(c) - 3:int(c) + 4].sum() == 0 for r, c in centres])
+    assert not w_zero.any()
+
+
+def test_objective_with_masked_random_patch_metric(xr, oracle):
+    """A masked, randomly sampled patch grad-NCC with moving-variance weights
+    inside the population objective (run directly, without the captured graph):
+    every evaluation equals the oracle on the objective's own DRRs and the
+    patches that evaluation drew."""
+    from tests.helpers import small_camera, small_volume
+    from xreg_gb300 import synth
+    vol = small_volume(15, (48, 44, 40), (1.5, 1.5, 1.5))
+    cam = small_camera((64, 72), 2.5)
+    rc = xr.RayCasterLineIntCUDA()
+    rc.set_volume(vol)
+    rc.set_camera_model(cam)
+    rc.set_ray_step_size(0.5)
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 5, 8.0, 10.0, seed=2)
+    fixed = np.random.default_rng(3).random((64, 72)).astype(np.float32)
+    mask = _mask((64, 72), 9)
+    m = xr.ImgSimMetric2DPatchGradNCCCUDA()
+    m.set_fixed_image(fixed)
+    m.set_mask(mask)
+    m.set_patch_radius(3)
+    m.set_patch_options(choose_rand_patches=1, num_rand_patches=30, rand_seed=7,
+                        use_mov_img_patch_variances_as_wgts=1)
+    obj = xr.PopulationObjective(rc, [m], 5)
+    seen = []
+    for _ in range(3):
+        vals = obj.eval(poses)
+        drr = rc.projs()
+        idx = m.patch_indices_used()
+        seen.append(idx.copy())
+        count = np.bincount(idx, minlength=(64 - 6) * (72 - 6)).astype(np.int32)
+        ref = oracle.patch_grad_ncc_ex(fixed, drr, radius=3, stride=1, mask=mask, patch_count=count,
+                                       use_mov_var_wgts=1)
+        np.testing.assert_allclose(vals, ref, atol=TOL, rtol=0)
+    assert not np.array_equal(seen[0], seen[1])

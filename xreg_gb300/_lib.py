@@ -39,6 +39,16 @@ class xr_camera_desc(C.Structure):
                 ("focal_len", C.c_double), ("coord_frame_type", C.c_int32), ("reserved", C.c_int32)]
 
 
+class xr_patch_options(C.Structure):
+    _fields_ = [("use_mask_for_weighting", C.c_int32), ("use_mask_for_patch_stats", C.c_int32),
+                ("normalize_weights_as_prob", C.c_int32), ("weight_patch_sims_in_combine", C.c_int32),
+                ("compute_mean_of_patch_sims", C.c_int32), ("use_fixed_img_patch_variances_as_wgts", C.c_int32),
+                ("use_mov_img_patch_variances_as_wgts", C.c_int32),
+                ("use_variances_in_grad_imgs_as_wgts", C.c_int32), ("choose_rand_patches", C.c_int32),
+                ("reserved", C.c_int32), ("num_rand_patches", C.c_int64), ("rand_patch_min_pixels_sep", C.c_double),
+                ("rand_seed", C.c_uint64)]
+
+
 class XRegError(RuntimeError):
     """A C-ABI call returned a non-zero xr_status."""
 
@@ -100,6 +110,11 @@ _SIGS = {
     "xr_sm_set_smooth_img_before_sobel_kernel_radius": [H, i32],
     "xr_sm_set_patch_radius": [H, i32],
     "xr_sm_set_patch_stride": [H, i32],
+    "xr_patch_options_default": [C.POINTER(xr_patch_options)],
+    "xr_sm_set_patch_options": [H, C.POINTER(xr_patch_options)],
+    "xr_sm_get_patch_options": [H, C.POINTER(xr_patch_options)],
+    "xr_sm_set_patch_wgt_img": [H, P],
+    "xr_sm_patch_indices_used": [H, i64, P, C.POINTER(i64)],
     "xr_sm_allocate_resources": [H],
     "xr_sm_compute": [H],
     "xr_sm_sim_vals": [H, P],

@@ -389,6 +389,40 @@ class _PatchParams:
     def set_patch_stride(self, s: int) -> None:
         call("xr_sm_set_patch_stride", self._h, int(s))
 
+    def patch_options(self) -> dict:
+        o = L.xr_patch_options()
+        call("xr_sm_get_patch_options", self._h, C.byref(o))
+        return {k: getattr(o, k) for k, _ in L.xr_patch_options._fields_ if k != "reserved"}
+
+    def set_patch_options(self, **kw) -> None:
+        """ImgSimMetric2DPatchCommon / PatchNCC / PatchGradNCC setters by name
+        (use_mask_for_weighting, use_mask_for_patch_stats, normalize_weights_as_prob,
+        weight_patch_sims_in_combine, compute_mean_of_patch_sims,
+        use_fixed_img_patch_variances_as_wgts, use_mov_img_patch_variances_as_wgts,
+        use_variances_in_grad_imgs_as_wgts, choose_rand_patches, num_rand_patches,
+        rand_patch_min_pixels_sep, rand_seed); unnamed ones keep their values."""
+        o = L.xr_patch_options()
+        call("xr_sm_get_patch_options", self._h, C.byref(o))
+        for k, v in kw.items():
+            if k not in dict(L.xr_patch_options._fields_) or k == "reserved":
+                raise TypeError(f"unknown patch option {k!r}")
+            setattr(o, k, type(getattr(o, k))(v) if not isinstance(getattr(o, k), float) else float(v))
+        call("xr_sm_set_patch_options", self._h, C.byref(o))
+
+    def set_wgt_img(self, img: np.ndarray | None) -> None:
+        if img is None:
+            call("xr_sm_set_patch_wgt_img", self._h, None)
+        else:
+            a = np.ascontiguousarray(img, dtype=np.float32)
+            call("xr_sm_set_patch_wgt_img", self._h, _ptr(a))
+
+    def patch_indices_used(self) -> np.ndarray:
+        n = C.c_int64()
+        call("xr_sm_patch_indices_used", self._h, 0, None, C.byref(n))
+        out = np.empty(n.value, dtype=np.int64)
+        call("xr_sm_patch_indices_used", self._h, n.value, _ptr(out), C.byref(n))
+        return out
+
 
 class ImgSimMetric2DNCCCUDA(ImgSimMetric2DCUDA):
     KIND = L.XR_SIM_NCC

@@ -10,6 +10,7 @@
 #include <memory>
 #include <mutex>
 #include <new>
+#include <random>
 #include <unordered_map>
 #include <string>
 #include <vector>
@@ -219,6 +220,19 @@ struct xr_simmetric_s {
   int nblk = 0;
   int ncr = 0, ncc = 0;            // patch centre grid
   uint64_t generation = 1;
+  // patch metrics: options, weights and patch subsets
+  xr_patch_options popt{};
+  std::vector<uint8_t> h_mask;     // host copy of the mask (patch weights)
+  std::vector<float> wgt_img;      // user weight image (rows * cols) or empty
+  DevBuf d_pw_x, d_pw_y, d_pcnt, d_pidx, d_mvar_sum;
+  bool has_pw = false;             // per-patch weights on the device (else 1)
+  std::vector<double> w_x, w_y;    // static patch weights per direction
+  std::vector<double> w_draw;      // weights the random subsets are drawn with
+  double tot_w_x = 0, tot_w_y = 0; // sums of the weights of the patches in use
+  int64_t nused = 0;               // patches in use (with multiplicity)
+  int mvar_mode = 0;               // moving-variance weights (PatchRun::mvar)
+  std::mt19937 rng;
+  std::vector<int32_t> last_idx;   // the last drawn subset
 
   // The bound ray caster if it is still alive; forgets it otherwise.
   xr_raycaster live_rc() {
@@ -999,6 +1013,7 @@ extern "C" XR_API xr_status xr_sm_create(int32_t kind, int32_t device, xr_simmet
   if (!sm) return fail(XR_ERR_OUT_OF_MEMORY, "xr_sm_create: host allocation failed");
   sm->kind = kind;
   sm->device = dev;
+  xr_patch_options_default(&sm->popt);
   cudaError_t e = cudaStreamCreateWithFlags(&sm->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete sm; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
   sm->id = reg_add(sm);
@@ -1034,6 +1049,8 @@ extern "C" XR_API xr_status xr_sm_set_fixed_image(xr_simmetric sm, const float* 
   if (sm->rows != rows || sm->cols != cols) {
     sm->has_mask = false;
     sm->d_mask.release();
+    sm->h_mask.clear();
+    sm->wgt_img.clear();
   }
   sm->rows = rows;
   sm->cols = cols;
@@ -1047,17 +1064,17 @@ extern "C" XR_API xr_status xr_sm_set_mask(xr_simmetric sm, const uint8_t* mask)
   XR_CHECK_ARG(sm, "set_mask: NULL handle");
   if (!mask) {
     sm->has_mask = false;
+    sm->h_mask.clear();
     sm->allocated = false;
     sm->generation++;
     return XR_OK;
   }
   XR_CHECK_ARG(sm->has_fixed, "set_mask: set the fixed image first");
-  if (sm->kind != XR_SIM_NCC && sm->kind != XR_SIM_GRAD_NCC)
-    return fail(XR_ERR_UNSUPPORTED, "set_mask: masks are implemented for NCC and grad-NCC only");
   DeviceGuard g(sm->device);
   const size_t n = (size_t)(sm->rows * sm->cols);
   XR_CUDA_TRY(sm->d_mask.reserve(n));
   XR_CUDA_TRY(cudaMemcpy(sm->d_mask.p, mask, n, cudaMemcpyHostToDevice));
+  sm->h_mask.assign(mask, mask + n);
   sm->has_mask = true;
   sm->allocated = false;
   sm->generation++;
@@ -1118,6 +1135,68 @@ extern "C" XR_API xr_status xr_sm_set_patch_stride(xr_simmetric sm, int32_t s) {
   return XR_OK;
 }
 
+extern "C" XR_API xr_status xr_patch_options_default(xr_patch_options* o) {
+  XR_CHECK_ARG(o, "xr_patch_options_default: NULL argument");
+  *o = xr_patch_options{};
+  o->use_mask_for_weighting = 1;
+  o->use_mask_for_patch_stats = 0;
+  o->normalize_weights_as_prob = 1;
+  o->weight_patch_sims_in_combine = 1;
+  o->compute_mean_of_patch_sims = 0;
+  o->num_rand_patches = 100;
+  o->rand_patch_min_pixels_sep = -1.0;
+  o->rand_seed = 0;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_patch_options(xr_simmetric sm, const xr_patch_options* o) {
+  XR_CHECK_ARG(sm && o, "set_patch_options: NULL argument");
+  XR_CHECK_ARG(sm->kind == XR_SIM_PATCH_NCC || sm->kind == XR_SIM_PATCH_GRAD_NCC,
+               "set_patch_options: not a patch metric");
+  XR_CHECK_ARG(!(o->use_fixed_img_patch_variances_as_wgts && o->use_mov_img_patch_variances_as_wgts),
+               "set_patch_options: fixed and moving patch variances cannot both be the weights");
+  XR_CHECK_ARG(!o->choose_rand_patches || o->num_rand_patches > 0,
+               "set_patch_options: num_rand_patches must be positive");
+  sm->popt = *o;
+  sm->rng.seed((std::mt19937::result_type)o->rand_seed);
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_get_patch_options(xr_simmetric sm, xr_patch_options* o) {
+  XR_CHECK_ARG(sm && o, "get_patch_options: NULL argument");
+  *o = sm->popt;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_patch_wgt_img(xr_simmetric sm, const float* img) {
+  XR_CHECK_ARG(sm, "set_patch_wgt_img: NULL handle");
+  if (!img) {
+    sm->wgt_img.clear();
+  } else {
+    XR_CHECK_ARG(sm->has_fixed, "set_patch_wgt_img: set the fixed image first");
+    sm->wgt_img.assign(img, img + sm->rows * sm->cols);
+  }
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_patch_indices_used(xr_simmetric sm, int64_t cap, int64_t* idx, int64_t* count) {
+  XR_CHECK_ARG(sm && count && (idx || cap == 0), "patch_indices_used: NULL argument");
+  XR_CHECK_ARG(sm->kind == XR_SIM_PATCH_NCC || sm->kind == XR_SIM_PATCH_GRAD_NCC,
+               "patch_indices_used: not a patch metric");
+  if (sm->popt.choose_rand_patches) {
+    *count = (int64_t)sm->last_idx.size();
+    for (int64_t k = 0; k < std::min<int64_t>(cap, *count); ++k) idx[k] = sm->last_idx[(size_t)k];
+  } else {
+    *count = (int64_t)sm->ncr * sm->ncc;
+    for (int64_t k = 0; k < std::min<int64_t>(cap, *count); ++k) idx[k] = k;
+  }
+  return XR_OK;
+}
+
 // Zero-mean fixed image and its statistics for one NCC direction.
 static xr_status sm_prepare_ncc_fixed(xr_simmetric sm, const float* img, DevBuf& fhat, FixedNCC& fx,
                                       cudaStream_t s) {
@@ -1145,16 +1224,180 @@ static xr_status sm_prepare_ncc_fixed(xr_simmetric sm, const float* img, DevBuf&
   return XR_OK;
 }
 
-static xr_status sm_prepare_patch_fixed(xr_simmetric sm, const float* img, DevBuf& mean, DevBuf& scale,
-                                        PatchFixed& pf, cudaStream_t s) {
+// compute_weights (xregImgSimMetric2DPatchCommon.cpp:306-410): the weight image
+// at each patch centre (zero at masked centres when the mask weights), else the
+// unmasked fraction of the patch when the mask weights, normalised to sum 1;
+// otherwise 1.  wimg: weight image values at the patch centres, or nullptr.
+static bool patch_weights(const xr_simmetric_s* sm, const std::vector<float>* wimg, const std::vector<int>& ucount,
+                          std::vector<double>& w) {
+  const int64_t np = (int64_t)sm->ncr * sm->ncc;
+  const int d = 2 * sm->patch_radius + 1;
+  const bool use_img = wimg != nullptr;
+  const bool use_mask = sm->popt.use_mask_for_weighting && sm->has_mask;
+  w.assign((size_t)np, 1.0);
+  if (!use_img && !use_mask) return false;
+  for (int64_t p = 0; p < np; ++p) {
+    const int64_t cr = sm->patch_radius + (p / sm->ncc) * sm->patch_stride;
+    const int64_t cc = sm->patch_radius + (p % sm->ncc) * sm->patch_stride;
+    if (use_img) {
+      double v = (*wimg)[(size_t)p];
+      if (use_mask && !sm->h_mask[(size_t)(cr * sm->cols + cc)]) v = 0.0;
+      w[(size_t)p] = v;
+    } else {
+      w[(size_t)p] = (double)ucount[(size_t)p] / (double)(d * d);
+    }
+  }
+  if (sm->popt.normalize_weights_as_prob) {
+    double t = 0;
+    for (double v : w) t += v;
+    for (double& v : w) v /= t;
+  }
+  return true;
+}
+
+// Fixed side of a patch metric: per-patch statistics of the fixed image (or its
+// gradients), the static patch weights and what the moving-variance weights need.
+static xr_status sm_prepare_patches(xr_simmetric sm, cudaStream_t s) {
+  const xr_patch_options& o = sm->popt;
+  const bool grad = sm->kind == XR_SIM_PATCH_GRAD_NCC;
+  const int rows = (int)sm->rows, cols = (int)sm->cols;
+  const int64_t np = (int64_t)sm->ncr * sm->ncc;
+  const uint8_t* dmask = sm->has_mask ? sm->d_mask.as<uint8_t>() : nullptr;
+  const int ums = o.use_mask_for_patch_stats ? 1 : 0;
+  // fixed-variance weights of each direction's own image (patch NCC, or patch
+  // grad-NCC with gradient-image variances), or of the fixed image for both
+  const bool fv_dir = o.use_fixed_img_patch_variances_as_wgts && (!grad || o.use_variances_in_grad_imgs_as_wgts);
+  const bool fv_img = o.use_fixed_img_patch_variances_as_wgts && grad && !o.use_variances_in_grad_imgs_as_wgts;
+  const bool want_ucount = o.use_mask_for_weighting && sm->has_mask;
+  DevBuf wv_x, wv_y, wv_img, ucnt;
+  const float* img_x = grad ? sm->d_gx.as<float>() : sm->d_fixed.as<float>();
+  XR_CUDA_TRY(sm->d_pmean_x.reserve((size_t)np * 4));
+  XR_CUDA_TRY(sm->d_pscale_x.reserve((size_t)np * 4));
+  if (fv_dir) XR_CUDA_TRY(wv_x.reserve((size_t)np * 4));
+  XR_CUDA_TRY(launch_patch_fixed_stats(img_x, rows, cols, sm->patch_radius, sm->patch_stride, sm->ncr, sm->ncc,
+                                       dmask, ums, sm->d_pmean_x.as<float>(), sm->d_pscale_x.as<float>(),
+                                       fv_dir ? wv_x.as<float>() : nullptr, nullptr, s));
+  if (grad) {
+    XR_CUDA_TRY(sm->d_pmean_y.reserve((size_t)np * 4));
+    XR_CUDA_TRY(sm->d_pscale_y.reserve((size_t)np * 4));
+    if (fv_dir) XR_CUDA_TRY(wv_y.reserve((size_t)np * 4));
+    XR_CUDA_TRY(launch_patch_fixed_stats(sm->d_gy.as<float>(), rows, cols, sm->patch_radius, sm->patch_stride,
+                                         sm->ncr, sm->ncc, dmask, ums, sm->d_pmean_y.as<float>(),
+                                         sm->d_pscale_y.as<float>(), fv_dir ? wv_y.as<float>() : nullptr, nullptr,
+                                         s));
+  }
+  if (fv_img) {
+    XR_CUDA_TRY(wv_img.reserve((size_t)np * 4));
+    XR_CUDA_TRY(launch_patch_fixed_stats(sm->d_fixed.as<float>(), rows, cols, sm->patch_radius, sm->patch_stride,
+                                         sm->ncr, sm->ncc, dmask, dmask ? 1 : 0, nullptr, nullptr,
+                                         wv_img.as<float>(), nullptr, s));
+  }
+  if (want_ucount) {
+    XR_CUDA_TRY(ucnt.reserve((size_t)np * 4));
+    XR_CUDA_TRY(launch_patch_fixed_stats(sm->d_fixed.as<float>(), rows, cols, sm->patch_radius, sm->patch_stride,
+                                         sm->ncr, sm->ncc, dmask, 0, nullptr, nullptr, nullptr, ucnt.as<int>(), s));
+  }
+  std::vector<float> h_wv_x, h_wv_y, h_wv_img, h_user;
+  std::vector<int> h_ucnt;
+  auto fetch = [&](DevBuf& b, auto& v) -> cudaError_t {
+    v.resize((size_t)np);
+    return cudaMemcpyAsync(v.data(), b.p, (size_t)np * sizeof(v[0]), cudaMemcpyDeviceToHost, s);
+  };
+  if (fv_dir) { XR_CUDA_TRY(fetch(wv_x, h_wv_x)); if (grad) XR_CUDA_TRY(fetch(wv_y, h_wv_y)); }
+  if (fv_img) XR_CUDA_TRY(fetch(wv_img, h_wv_img));
+  if (want_ucount) XR_CUDA_TRY(fetch(ucnt, h_ucnt));
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
+  if (!sm->wgt_img.empty()) {
+    h_user.resize((size_t)np);
+    for (int64_t p = 0; p < np; ++p) {
+      const int64_t cr = sm->patch_radius + (p / sm->ncc) * sm->patch_stride;
+      const int64_t cc = sm->patch_radius + (p % sm->ncc) * sm->patch_stride;
+      h_user[(size_t)p] = sm->wgt_img[(size_t)(cr * sm->cols + cc)];
+    }
+  }
+  const std::vector<float>* user = sm->wgt_img.empty() ? nullptr : &h_user;
+  bool any = false;
+  if (fv_dir) {
+    any |= patch_weights(sm, &h_wv_x, h_ucnt, sm->w_x);
+    if (grad) any |= patch_weights(sm, &h_wv_y, h_ucnt, sm->w_y);
+  } else if (fv_img) {
+    any |= patch_weights(sm, &h_wv_img, h_ucnt, sm->w_x);
+    sm->w_y = sm->w_x;
+  } else {
+    any |= patch_weights(sm, user, h_ucnt, sm->w_x);
+    sm->w_y = sm->w_x;
+  }
+  if (!grad) sm->w_y = sm->w_x;
+  // random subsets are drawn with the metric's own weights (patch grad-NCC: the
+  // ones its mask / weight image give, ImgSimMetric2DPatchGradNCCCPU::compute)
+  if (grad && (fv_dir || fv_img)) patch_weights(sm, user, h_ucnt, sm->w_draw);
+  else sm->w_draw = sm->w_x;
+  sm->has_pw = any;
+  if (any) {
+    std::vector<float> f((size_t)np);
+    for (int64_t p = 0; p < np; ++p) f[(size_t)p] = (float)sm->w_x[(size_t)p];
+    XR_CUDA_TRY(sm->d_pw_x.reserve((size_t)np * 4));
+    XR_CUDA_TRY(cudaMemcpy(sm->d_pw_x.p, f.data(), (size_t)np * 4, cudaMemcpyHostToDevice));
+    for (int64_t p = 0; p < np; ++p) f[(size_t)p] = (float)sm->w_y[(size_t)p];
+    XR_CUDA_TRY(sm->d_pw_y.reserve((size_t)np * 4));
+    XR_CUDA_TRY(cudaMemcpy(sm->d_pw_y.p, f.data(), (size_t)np * 4, cudaMemcpyHostToDevice));
+  }
+  sm->mvar_mode = o.use_mov_img_patch_variances_as_wgts ? ((grad && o.use_variances_in_grad_imgs_as_wgts) ? 2 : 1) : 0;
+  if (o.choose_rand_patches) {
+    XR_CHECK_ARG(o.num_rand_patches < np, "allocate_resources: num_rand_patches must be below the patch count");
+    double t = 0;
+    for (double v : sm->w_draw) t += v;
+    XR_CHECK_ARG(t > 0.0, "allocate_resources: random patches need a positive total weight");
+    XR_CUDA_TRY(sm->d_pcnt.reserve((size_t)np * 4));
+    XR_CUDA_TRY(sm->d_pidx.reserve((size_t)o.num_rand_patches * 4));
+  } else {
+    sm->tot_w_x = 0;
+    sm->tot_w_y = 0;
+    for (int64_t p = 0; p < np; ++p) { sm->tot_w_x += sm->w_x[(size_t)p]; sm->tot_w_y += sm->w_y[(size_t)p]; }
+    sm->nused = np;
+  }
+  return XR_OK;
+}
+
+// patch_indices_to_use (xregImgSimMetric2DPatchCommon.cpp:412-493): draws
+// num_rand_patches patch indices with probability proportional to the weights,
+// rejecting candidates closer than the minimum separation to an accepted one;
+// then uploads their multiplicities.
+static xr_status sm_draw_patches(xr_simmetric sm, cudaStream_t s) {
+  const xr_patch_options& o = sm->popt;
+  std::discrete_distribution<size_t> dist(sm->w_draw.begin(), sm->w_draw.end());
+  const double r = (double)sm->patch_radius;
+  const double min_sep = o.rand_patch_min_pixels_sep < 0 ? std::sqrt(2.0 * r * r) : o.rand_patch_min_pixels_sep;
+  const bool check = min_sep > 1.0e-8;
+  std::vector<std::pair<double, double>> centres;
+  sm->last_idx.clear();
+  const int64_t limit = 1000 * o.num_rand_patches + 100000;
+  for (int64_t attempts = 0; (int64_t)sm->last_idx.size() < o.num_rand_patches; ++attempts) {
+    if (attempts >= limit) return fail(XR_ERR_INVALID_ARG, "compute: could not place the random patches apart");
+    const size_t cand = dist(sm->rng);
+    if (check) {
+      const double cr = r + (double)((int64_t)cand / sm->ncc) * sm->patch_stride;
+      const double cc = r + (double)((int64_t)cand % sm->ncc) * sm->patch_stride;
+      bool ok = true;
+      for (const auto& e : centres)
+        if (std::sqrt((e.first - cr) * (e.first - cr) + (e.second - cc) * (e.second - cc)) < min_sep) {
+          ok = false;
+          break;
+        }
+      if (!ok) continue;
+      centres.emplace_back(cr, cc);
+    }
+    sm->last_idx.push_back((int32_t)cand);
+  }
+  sm->tot_w_x = 0;
+  sm->tot_w_y = 0;
+  for (int32_t i : sm->last_idx) { sm->tot_w_x += sm->w_x[(size_t)i]; sm->tot_w_y += sm->w_y[(size_t)i]; }
+  sm->nused = (int64_t)sm->last_idx.size();
   const size_t np = (size_t)sm->ncr * (size_t)sm->ncc;
-  XR_CUDA_TRY(mean.reserve(np * 4));
-  XR_CUDA_TRY(scale.reserve(np * 4));
-  XR_CUDA_TRY(launch_patch_fixed_stats(img, (int)sm->rows, (int)sm->cols, sm->patch_radius, sm->patch_stride,
-                                       sm->ncr, sm->ncc, mean.as<float>(), scale.as<float>(), s));
-  pf.img = img;
-  pf.mean = mean.as<float>();
-  pf.scale = scale.as<float>();
+  XR_CUDA_TRY(cudaMemcpyAsync(sm->d_pidx.p, sm->last_idx.data(), sm->last_idx.size() * 4, cudaMemcpyHostToDevice, s));
+  XR_CUDA_TRY(cudaMemsetAsync(sm->d_pcnt.p, 0, np * 4, s));
+  XR_CUDA_TRY(launch_patch_scatter_counts(sm->d_pidx.as<int32_t>(), (int64_t)sm->last_idx.size(),
+                                          sm->d_pcnt.as<int32_t>(), s));
   return XR_OK;
 }
 
@@ -1193,23 +1436,19 @@ extern "C" XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm) {
     XR_CHECK_ARG(!grad || (rows >= 8 && cols >= 8), "allocate_resources: gradient metrics need images of at least 8x8");
     sm->ncr = (rows - 1 - 2 * sm->patch_radius) / sm->patch_stride + 1;
     sm->ncc = (cols - 1 - 2 * sm->patch_radius) / sm->patch_stride + 1;
-    PatchFixed px{}, py{};
     if (grad) {
       XR_CUDA_TRY(sm->d_gx.reserve((size_t)n * 4));
       XR_CUDA_TRY(sm->d_gy.reserve((size_t)n * 4));
       XR_CUDA_TRY(launch_grad_images(sm->d_fixed.as<float>(), rows, cols, 1, sm->smooth_ksize,
                                      sm->d_gx.as<float>(), sm->d_gy.as<float>(), s));
-      xr_status st = sm_prepare_patch_fixed(sm, sm->d_gx.as<float>(), sm->d_pmean_x, sm->d_pscale_x, px, s);
-      if (st != XR_OK) return st;
-      st = sm_prepare_patch_fixed(sm, sm->d_gy.as<float>(), sm->d_pmean_y, sm->d_pscale_y, py, s);
-      if (st != XR_OK) return st;
-    } else {
-      xr_status st = sm_prepare_patch_fixed(sm, sm->d_fixed.as<float>(), sm->d_pmean_x, sm->d_pscale_x, px, s);
-      if (st != XR_OK) return st;
     }
+    xr_status st = sm_prepare_patches(sm, s);
+    if (st != XR_OK) return st;
+    PatchFixed px{}, py{};
     XR_CUDA_TRY(launch_patch_ncc(nullptr, rows, cols, 0, grad, sm->smooth_ksize, sm->patch_radius,
-                                 sm->patch_stride, sm->ncr, sm->ncc, px, py, nullptr, s, &sm->nblk));
+                                 sm->patch_stride, sm->ncr, sm->ncc, px, py, PatchRun{}, 1, nullptr, s, &sm->nblk));
     XR_CUDA_TRY(sm->d_partials.reserve((size_t)sm->capacity * sm->nblk * 2 * 8));
+    if (sm->mvar_mode) XR_CUDA_TRY(sm->d_mvar_sum.reserve((size_t)sm->capacity * 2 * 8));
   }
   XR_CUDA_TRY(sm->d_sims.reserve((size_t)sm->capacity * 4));
   XR_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1259,14 +1498,37 @@ static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
       break;
     default: {
       const int grad = sm->kind == XR_SIM_PATCH_GRAD_NCC;
+      const xr_patch_options& o = sm->popt;
       PatchFixed px{grad ? sm->d_gx.as<float>() : sm->d_fixed.as<float>(), sm->d_pmean_x.as<float>(),
-                    sm->d_pscale_x.as<float>()};
-      PatchFixed py{sm->d_gy.as<float>(), sm->d_pmean_y.as<float>(), sm->d_pscale_y.as<float>()};
+                    sm->d_pscale_x.as<float>(), sm->has_pw ? sm->d_pw_x.as<float>() : nullptr};
+      PatchFixed py{sm->d_gy.as<float>(), sm->d_pmean_y.as<float>(), sm->d_pscale_y.as<float>(),
+                    sm->has_pw ? sm->d_pw_y.as<float>() : nullptr};
+      PatchRun run{mask, nullptr, o.use_mask_for_patch_stats ? 1 : 0, o.weight_patch_sims_in_combine ? 1 : 0,
+                   sm->mvar_mode, o.normalize_weights_as_prob ? 1 : 0,
+                   sm->mvar_mode ? sm->d_mvar_sum.as<double>() : nullptr};
+      if (o.choose_rand_patches) {
+        xr_status st = sm_draw_patches(sm, s);
+        if (st != XR_OK) return st;
+        run.cnt = sm->d_pcnt.as<int32_t>();
+      }
+      if (sm->mvar_mode) {
+        XR_CUDA_TRY(launch_patch_ncc(mov, rows, cols, sm->num_mov, grad, sm->smooth_ksize, sm->patch_radius,
+                                     sm->patch_stride, sm->ncr, sm->ncc, px, py, run, 0,
+                                     sm->d_partials.as<double>(), s, nullptr));
+        XR_CUDA_TRY(launch_patch_sum_partials(sm->d_partials.as<double>(), sm->nblk, sm->num_mov,
+                                              sm->d_mvar_sum.as<double>(), s));
+      }
       XR_CUDA_TRY(launch_patch_ncc(mov, rows, cols, sm->num_mov, grad, sm->smooth_ksize, sm->patch_radius,
-                                   sm->patch_stride, sm->ncr, sm->ncc, px, py, sm->d_partials.as<double>(), s,
-                                   nullptr));
-      XR_CUDA_TRY(launch_patch_finalize(sm->d_partials.as<double>(), sm->nblk, sm->num_mov,
-                                        (int64_t)sm->ncr * sm->ncc, grad, sm->d_sims.as<float>(), s));
+                                   sm->patch_stride, sm->ncr, sm->ncc, px, py, run, 1, sm->d_partials.as<double>(),
+                                   s, nullptr));
+      const double den_x = o.compute_mean_of_patch_sims ? (double)sm->nused
+                                                        : (o.weight_patch_sims_in_combine ? sm->tot_w_x : 1.0);
+      const double den_y = o.compute_mean_of_patch_sims ? (double)sm->nused
+                                                        : (o.weight_patch_sims_in_combine ? sm->tot_w_y : 1.0);
+      XR_CUDA_TRY(launch_patch_finalize(sm->d_partials.as<double>(), sm->nblk, sm->num_mov, den_x, den_y, grad,
+                                        sm->mvar_mode, o.normalize_weights_as_prob ? 1 : 0,
+                                        sm->mvar_mode ? sm->d_mvar_sum.as<double>() : nullptr,
+                                        sm->d_sims.as<float>(), s));
       break;
     }
   }
@@ -1405,6 +1667,11 @@ static bool obj_graph_valid(xr_objective obj, int64_t pop) {
 static xr_status obj_run(xr_objective obj, int64_t pop) {
   xr_raycaster rc = obj->rc;
   cudaStream_t s = rc->stream();
+  // A metric that draws random patches on the host at every compute is run
+  // directly (a captured graph would replay one draw).
+  for (xr_simmetric m : obj->metrics)
+    if ((m->kind == XR_SIM_PATCH_NCC || m->kind == XR_SIM_PATCH_GRAD_NCC) && m->popt.choose_rand_patches)
+      return obj_enqueue(obj, pop);
   // Host state that the captured kernels read must be current before capture;
   // a first direct run uploads it and settles generations.
   if (obj_graph_valid(obj, pop)) {

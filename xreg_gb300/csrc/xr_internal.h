@@ -114,7 +114,18 @@ struct FixedNCC {           // per direction (one for NCC, x and y for grad-NCC)
 struct PatchFixed {         // per direction
   const float* img;         // fixed image (or its gradient), rows*cols
   const float* mean;        // per patch mean
-  const float* scale;       // per patch 1 / (sd * n_patch)
+  const float* scale;       // per patch 1 / (sd * n used for the statistics)
+  const float* w;           // per patch weight, nullptr = 1
+};
+
+struct PatchRun {           // per compute
+  const uint8_t* mask;      // image mask or nullptr
+  const int32_t* cnt;       // times each patch is used, nullptr = once
+  int use_mask_stats;       // statistics over masked-in pixels only
+  int weighted;             // weight_patch_sims_in_combine
+  int mvar;                 // moving-variance weights: 0 none, 1 of the image, 2 of each gradient image
+  int normalize;            // normalise moving variances by their sum
+  const double* mvar_sum;   // [image][direction] sums of count x variance (pass 0), for pass 1
 };
 
 // Moments of moving images for (grad-)NCC: partials[img][block][k] in double.
@@ -136,14 +147,20 @@ cudaError_t launch_image_stats(const float* img, int64_t npix, const uint8_t* ma
                                cudaStream_t s);
 cudaError_t launch_sub_scalar(const float* in, int64_t n, double value, float* out, cudaStream_t s);
 cudaError_t launch_sum_f(const float* in, int64_t n, const uint8_t* mask, double* d_out, cudaStream_t s);
-// Per-patch statistics of a fixed image for patch NCC.
-cudaError_t launch_patch_fixed_stats(const float* img, int rows, int cols, int radius, int stride,
-                                     int ncr, int ncc, float* mean, float* scale, cudaStream_t s);
+// Per-patch statistics of a fixed image for patch NCC (mean / scale may be
+// nullptr; wvar: variance weight; ucount: masked-in pixel count; both optional).
+cudaError_t launch_patch_fixed_stats(const float* img, int rows, int cols, int radius, int stride, int ncr, int ncc,
+                                     const uint8_t* mask, int use_mask_stats, float* mean, float* scale, float* wvar,
+                                     int* ucount, cudaStream_t s);
+// pass 0: moving-variance sums; pass 1: weighted score sums.  partials [image][block][2].
 cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs, int grad, int smooth_ksize,
-                             int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py,
-                             double* partials, cudaStream_t s, int* nblk_out);
-cudaError_t launch_patch_finalize(const double* partials, int nblk, int64_t nimgs, int64_t npatch, int grad,
-                                  float* sims, cudaStream_t s);
+                             int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py, PatchRun run,
+                             int pass, double* partials, cudaStream_t s, int* nblk_out);
+cudaError_t launch_patch_sum_partials(const double* partials, int nblk, int64_t nimgs, double* out, cudaStream_t s);
+cudaError_t launch_patch_finalize(const double* partials, int nblk, int64_t nimgs, double den_x, double den_y,
+                                  int grad, int mvar, int normalize, const double* mvar_sum, float* sims,
+                                  cudaStream_t s);
+cudaError_t launch_patch_scatter_counts(const int32_t* idx, int64_t n, int32_t* cnt, cudaStream_t s);
 // Mean over views of per-view similarity values: sims[v][pop] -> out[pop].
 cudaError_t launch_combine_mean(const float* const* view_sims, int nviews, int64_t pop, float* out,
                                 cudaStream_t s);

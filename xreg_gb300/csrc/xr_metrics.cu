@@ -19,6 +19,8 @@
 // over patches.  The fixed side (per-patch mean and 1/(sd n)) is pre-computed once.
 #include "xr_internal.h"
 
+#include <cfloat>
+
 namespace xr {
 namespace {
 
@@ -285,27 +287,66 @@ __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nb
 // ------------------------------------------------------------ patch NCC ---
 constexpr int kPC = 16;  // patch centres per tile edge
 
-__global__ void patch_fixed_stats_kernel(const float* __restrict__ img, int cols, int radius, int stride,
-                                         int ncr, int ncc, float* __restrict__ mean, float* __restrict__ scale) {
+// Per-patch statistics of a fixed image (ComputePatchMeanStdDev,
+// xregImgSimMetric2DPatchNCCCPU.cpp:558-619, in double): pixels that count are
+// all of them, or the masked-in ones when use_mask_stats; the mean is divided
+// and the variance formed only when more than one pixel counts; sd >= 1e-6.
+// mean / scale = 1 / (sd n) give the scaled fixed patch (f - mean) scale.
+// wvar (optional): the squared sd used as a patch weight (with the mask when
+// there is one, xregImgSimMetric2DPatchNCCCPU.cpp:402-411); ucount (optional):
+// masked-in pixels of the patch.
+__device__ void patch_stats_d(const float* __restrict__ img, int cols, int r0, int c0, int d,
+                              const uint8_t* __restrict__ mask, int use_mask, double* mu_out, double* sd_out,
+                              int* n_out) {
+  int n = 0;
+  double s = 0;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      const int64_t i = (int64_t)(r0 + r) * cols + c0 + c;
+      if (!use_mask || !mask || mask[i]) { s += img[i]; ++n; }
+    }
+  double var = 0;
+  if (n > 1) {
+    s /= (double)n;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) {
+        const int64_t i = (int64_t)(r0 + r) * cols + c0 + c;
+        if (!use_mask || !mask || mask[i]) { const double t = img[i] - s; var += t * t; }
+      }
+    var /= (double)(n - 1);
+  }
+  double sd = sqrt(var);
+  if (sd < 1.0e-6) sd = 1.0e-6;
+  *mu_out = s;
+  *sd_out = sd;
+  *n_out = n;
+}
+
+__global__ void patch_fixed_stats_kernel(const float* __restrict__ img, int cols, int radius, int stride, int ncr,
+                                         int ncc, const uint8_t* __restrict__ mask, int use_mask_stats,
+                                         float* __restrict__ mean, float* __restrict__ scale,
+                                         float* __restrict__ wvar, int* __restrict__ ucount) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= (int64_t)ncr * ncc) return;
   const int pr = (int)(p / ncc), pc = (int)(p - (int64_t)pr * ncc);
   const int r0 = pr * stride, c0 = pc * stride, d = 2 * radius + 1;
-  const double np = (double)d * d;
-  double s = 0;
-  for (int r = 0; r < d; ++r)
-    for (int c = 0; c < d; ++c) s += img[(int64_t)(r0 + r) * cols + c0 + c];
-  const double mu = s / np;
-  double v = 0;
-  for (int r = 0; r < d; ++r)
-    for (int c = 0; c < d; ++c) {
-      const double t = img[(int64_t)(r0 + r) * cols + c0 + c] - mu;
-      v += t * t;
-    }
-  double sd = sqrt(v / (np - 1.0));
-  if (sd < 1.0e-6) sd = 1.0e-6;
-  mean[p] = (float)mu;
-  scale[p] = (float)(1.0 / (sd * np));
+  double mu, sd;
+  int n;
+  patch_stats_d(img, cols, r0, c0, d, mask, use_mask_stats, &mu, &sd, &n);
+  if (mean) {
+    mean[p] = (float)mu;
+    scale[p] = (float)(1.0 / (sd * (double)n));
+  }
+  if (wvar) {
+    if (mask && !use_mask_stats) patch_stats_d(img, cols, r0, c0, d, mask, 1, &mu, &sd, &n);
+    wvar[p] = (float)(sd * sd);
+  }
+  if (ucount) {
+    int k = 0;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) k += (!mask || mask[(int64_t)(r0 + r) * cols + c0 + c]) ? 1 : 0;
+    ucount[p] = k;
+  }
 }
 
 // Shared-memory layout for one tile of kPC x kPC patch centres (dynamic).
@@ -313,7 +354,8 @@ struct PatchLayout {
   int W;    // edge of the patch-window region (moving gradient / fixed tiles)
   int WI;   // staged input edge
   int WB;   // blurred edge
-  size_t bytes;
+  size_t fbytes;  // float part
+  size_t bytes;   // plus the W x W mask tile
   __host__ __device__ static PatchLayout make(int radius, int stride, int grad, int kr) {
     PatchLayout L;
     L.W = (kPC - 1) * stride + 2 * radius + 1;
@@ -322,34 +364,62 @@ struct PatchLayout {
     const size_t fl = grad ? ((size_t)L.WI * L.WI + (size_t)L.WI * L.WB + (size_t)L.WB * L.WB +
                               4 * (size_t)L.W * L.W)
                            : ((size_t)L.WI * L.WI + (size_t)L.W * L.W);
-    L.bytes = fl * sizeof(float);
+    L.fbytes = fl * sizeof(float);
+    L.bytes = L.fbytes + (((size_t)L.W * L.W + 15) & ~(size_t)15);
     return L;
   }
 };
 
-__device__ __forceinline__ float patch_score(const float* __restrict__ m, const float* __restrict__ f, int W,
-                                             int r0, int c0, int d, float fmean, float fscale) {
+// Score 1 - sum over masked-in pixels of (m - mu_m) / sd_m * (f - fmean) fscale,
+// moving statistics over all pixels (masked-in ones when use_mask_stats); the
+// unmasked case is the plain patch NCC.  *var = sd_m^2.
+__device__ __forceinline__ float patch_score(const float* __restrict__ m, const float* __restrict__ f,
+                                             const uint8_t* __restrict__ mk, int W, int r0, int c0, int d,
+                                             float fmean, float fscale, int use_mask_stats) {
   float s = 0.0f;
+  int n = 0;
   for (int r = 0; r < d; ++r)
-    for (int c = 0; c < d; ++c) s += m[(r0 + r) * W + c0 + c];
-  const float n = (float)(d * d);
-  const float mu = s / n;
+    for (int c = 0; c < d; ++c)
+      if (!use_mask_stats || !mk || mk[(r0 + r) * W + c0 + c]) { s += m[(r0 + r) * W + c0 + c]; ++n; }
+  const float mu = n > 1 ? s / (float)n : s;
   float v = 0.0f, cov = 0.0f;
   for (int r = 0; r < d; ++r)
     for (int c = 0; c < d; ++c) {
-      const float dm = m[(r0 + r) * W + c0 + c] - mu;
-      v = fmaf(dm, dm, v);
-      cov = fmaf(dm, f[(r0 + r) * W + c0 + c] - fmean, cov);
+      const int i = (r0 + r) * W + c0 + c;
+      const float dm = m[i] - mu;
+      if (!use_mask_stats || !mk || mk[i]) v = fmaf(dm, dm, v);
+      if (!mk || mk[i]) cov = fmaf(dm, f[i] - fmean, cov);
     }
-  float sd = sqrtf(v / (n - 1.0f));
+  float sd = n > 1 ? sqrtf(v / (float)(n - 1)) : 0.0f;
   sd = fmaxf(sd, 1.0e-6f);
   return 1.0f - (cov / sd) * fscale;
 }
 
-template <int GRAD, int KR>
+// Sample variance (sd clamped at 1e-6, squared) of a d x d window with row pitch P.
+__device__ __forceinline__ float patch_var(const float* __restrict__ m, int P, int r0, int c0, int d) {
+  float s = 0.0f;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) s += m[(r0 + r) * P + c0 + c];
+  const float n = (float)(d * d);
+  const float mu = s / n;
+  float v = 0.0f;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      const float dm = m[(r0 + r) * P + c0 + c] - mu;
+      v = fmaf(dm, dm, v);
+    }
+  const float sd = fmaxf(sqrtf(v / (n - 1.0f)), 1.0e-6f);
+  return sd * sd;
+}
+
+// PASS 0: per image and direction, the sum over used patches with an unmasked
+// centre of count x moving-patch variance (the normaliser of variance weights).
+// PASS 1: per image and direction, the sum over used patches of
+// count x weight x score (weight 1 when not weighting in the combine).
+template <int GRAD, int KR, int PASS>
 __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __restrict__ imgs, int rows, int cols,
                                                              int radius, int stride, int ncr, int ncc,
-                                                             PatchFixed px, PatchFixed py,
+                                                             PatchFixed px, PatchFixed py, PatchRun run,
                                                              double* __restrict__ partials) {
   extern __shared__ float sm[];
   __shared__ double red[2 * 32];
@@ -362,6 +432,7 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   float* s_my = s_mx + W * W;               // W x W moving gy
   float* s_fx = GRAD ? s_my + W * W : s_in + WI * WI;  // W x W fixed (gx or raw)
   float* s_fy = s_fx + W * W;
+  uint8_t* s_mk = reinterpret_cast<uint8_t*>(reinterpret_cast<char*>(sm) + L.fbytes);  // W x W mask
 
   const int tiles_x = (ncc + kPC - 1) / kPC;
   const int tpr = blockIdx.x / tiles_x, tpc = blockIdx.x - tpr * tiles_x;
@@ -371,6 +442,7 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   const int64_t img = blockIdx.y;
   const float* src = imgs + img * npix;
   const int H = GRAD ? (KR + 1) : 0;
+  const uint8_t* mk = run.mask ? s_mk : nullptr;
 
   for (int i = threadIdx.x; i < WI * WI; i += blockDim.x) {
     const int r = i / WI, c = i - r * WI;
@@ -381,11 +453,15 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
     const int r = i / W, c = i - r * W;
     const int gr = min(y0 + r, rows - 1), gc = min(x0 + c, cols - 1);
-    s_fx[i] = px.img[(int64_t)gr * cols + gc];
-    if (GRAD) s_fy[i] = py.img[(int64_t)gr * cols + gc];
+    if (PASS == 1) {
+      s_fx[i] = px.img[(int64_t)gr * cols + gc];
+      if (GRAD) s_fy[i] = py.img[(int64_t)gr * cols + gc];
+    }
+    if (run.mask) s_mk[i] = run.mask[(int64_t)gr * cols + gc];
   }
   __syncthreads();
-  if (GRAD) {
+  const bool need_grads = GRAD && (PASS == 1 || run.mvar == 2);
+  if (need_grads) {
     if (KR == 0) {
       for (int i = threadIdx.x; i < WB * WB; i += blockDim.x) {
         const int r = i / WB, c = i - r * WB;
@@ -425,9 +501,53 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   const int pr = pr0 + lr, pc = pc0 + lc;
   if (pr < ncr && pc < ncc) {
     const int64_t pidx = (int64_t)pr * ncc + pc;
+    const int cnt = run.cnt ? run.cnt[pidx] : 1;
     const int d = 2 * radius + 1;
-    v[0] = patch_score(s_mx, s_fx, W, lr * stride, lc * stride, d, px.mean[pidx], px.scale[pidx]);
-    if (GRAD) v[1] = patch_score(s_my, s_fy, W, lr * stride, lc * stride, d, py.mean[pidx], py.scale[pidx]);
+    const int r0 = lr * stride, c0 = lc * stride;
+    const bool centre = !mk || mk[(r0 + radius) * W + c0 + radius];
+    if (cnt > 0) {
+      // moving-patch variances used as weights: of the moving image itself
+      // (mvar 1, shared by both directions) or of each gradient image (mvar 2)
+      float var0 = 0.0f, var1 = 0.0f;
+      if (run.mvar && centre) {
+        if (run.mvar == 1) {
+          var0 = GRAD ? patch_var(s_in + H * WI + H, WI, r0, c0, d) : patch_var(s_mx, W, r0, c0, d);
+          var1 = var0;
+        } else {
+          var0 = patch_var(s_mx, W, r0, c0, d);
+          if (GRAD) var1 = patch_var(s_my, W, r0, c0, d);
+        }
+      }
+      if (PASS == 0) {
+        v[0] = (double)cnt * var0;
+        v[1] = (double)cnt * var1;
+      } else {
+        float w[2];
+        for (int k = 0; k < 2; ++k) {
+          const PatchFixed& P = k == 0 ? px : py;
+          if (run.mvar) {
+            float vk = k == 0 ? var0 : var1;
+            if (run.normalize) {
+              const float S = (float)run.mvar_sum[img * 2 + k];
+              vk = S > 1.0e-6f ? vk / S : 0.0f;
+            }
+            w[k] = vk;
+          } else {
+            w[k] = P.w ? P.w[pidx] : 1.0f;
+          }
+        }
+        if (!run.weighted || fabsf(w[0]) > 1.0e-6f) {
+          const float sc = patch_score(s_mx, s_fx, mk, W, r0, c0, d, px.mean[pidx], px.scale[pidx],
+                                       run.use_mask_stats);
+          v[0] = (double)cnt * (double)((run.weighted ? w[0] : 1.0f) * sc);
+        }
+        if (GRAD && (!run.weighted || fabsf(w[1]) > 1.0e-6f)) {
+          const float sc = patch_score(s_my, s_fy, mk, W, r0, c0, d, py.mean[pidx], py.scale[pidx],
+                                       run.use_mask_stats);
+          v[1] = (double)cnt * (double)((run.weighted ? w[1] : 1.0f) * sc);
+        }
+      }
+    }
   }
   block_sum_d<2>(v, red);
   if (threadIdx.x == 0) {
@@ -437,16 +557,46 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   }
 }
 
-__global__ void patch_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs,
-                                      double npatch, int grad, float* __restrict__ sims) {
+// Per image: out[img][2] = the two sums over blocks of the partials.
+__global__ void patch_sum_partials_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs,
+                                          double* __restrict__ out) {
   const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (img >= nimgs) return;
   double a = 0, b = 0;
   const double* p = partials + img * nblk * 2;
   for (int k = 0; k < nblk; ++k) { a += p[2 * k]; b += p[2 * k + 1]; }
-  const float sx = (float)(a / npatch);
-  if (grad) sims[img] = 0.5f * (sx + (float)(b / npatch));
-  else sims[img] = sx;
+  out[img * 2] = a;
+  out[img * 2 + 1] = b;
+}
+
+// Value per image: sum / denominator per direction; FLT_MAX where normalised
+// moving variances sum to at most 1e-6; patch grad-NCC 0.5 (s_x + s_y) in float.
+__global__ void patch_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double den_x,
+                                      double den_y, int grad, int mvar, int normalize,
+                                      const double* __restrict__ mvar_sum, float* __restrict__ sims) {
+  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (img >= nimgs) return;
+  double a = 0, b = 0;
+  const double* p = partials + img * nblk * 2;
+  for (int k = 0; k < nblk; ++k) { a += p[2 * k]; b += p[2 * k + 1]; }
+  const bool chk = mvar && normalize;
+  if (chk && mvar == 1 && !((float)mvar_sum[img * 2] > 1.0e-6f)) {
+    sims[img] = FLT_MAX;
+    return;
+  }
+  const float sx = (chk && !((float)mvar_sum[img * 2] > 1.0e-6f)) ? FLT_MAX : (float)(a / den_x);
+  if (grad) {
+    const float sy = (chk && !((float)mvar_sum[img * 2 + 1] > 1.0e-6f)) ? FLT_MAX : (float)(b / den_y);
+    sims[img] = 0.5f * (sx + sy);
+  } else {
+    sims[img] = sx;
+  }
+}
+
+// cnt[idx[k]] += 1 for k < n (patch multiplicities of a drawn subset).
+__global__ void patch_scatter_counts_kernel(const int32_t* __restrict__ idx, int64_t n, int32_t* __restrict__ cnt) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) atomicAdd(cnt + idx[k], 1);
 }
 
 struct ViewPtrs {
@@ -540,18 +690,19 @@ cudaError_t launch_grad_finalize(const double* partials, int nblk, int64_t nimgs
 }
 
 cudaError_t launch_patch_fixed_stats(const float* img, int rows, int cols, int radius, int stride, int ncr, int ncc,
-                                     float* mean, float* scale, cudaStream_t s) {
+                                     const uint8_t* mask, int use_mask_stats, float* mean, float* scale, float* wvar,
+                                     int* ucount, cudaStream_t s) {
   (void)rows;
   const int64_t n = (int64_t)ncr * ncc;
   if (n <= 0) return cudaSuccess;
-  patch_fixed_stats_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(img, cols, radius, stride, ncr, ncc, mean,
-                                                                       scale);
+  patch_fixed_stats_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(img, cols, radius, stride, ncr, ncc, mask,
+                                                                       use_mask_stats, mean, scale, wvar, ucount);
   return cudaGetLastError();
 }
 
 cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs, int grad, int smooth_ksize,
-                             int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py,
-                             double* partials, cudaStream_t s, int* nblk_out) {
+                             int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py, PatchRun run,
+                             int pass, double* partials, cudaStream_t s, int* nblk_out) {
   const int tiles = ((ncr + kPC - 1) / kPC) * ((ncc + kPC - 1) / kPC);
   if (nblk_out) *nblk_out = tiles;
   if (nimgs <= 0 || !partials) return cudaSuccess;
@@ -561,29 +712,49 @@ cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs
   if (L.bytes > 200 * 1024) return cudaErrorInvalidValue;
   const dim3 grid(tiles, (unsigned)nimgs);
   cudaError_t e = cudaSuccess;
-#define XR_PATCH_LAUNCH(G, K)                                                                           \
-  e = set_smem(patch_ncc_kernel<G, K>, L.bytes);                                                       \
-  if (e != cudaSuccess) return e;                                                                       \
-  patch_ncc_kernel<G, K><<<grid, kThreads, L.bytes, s>>>(mov, rows, cols, radius, stride, ncr, ncc, px, py, \
-                                                         partials);
-  if (!grad) {
-    XR_PATCH_LAUNCH(0, 0)
-  } else if (kr == 0) {
-    XR_PATCH_LAUNCH(1, 0)
-  } else if (kr == 1) {
-    XR_PATCH_LAUNCH(1, 1)
-  } else {
-    XR_PATCH_LAUNCH(1, 2)
+#define XR_PATCH_LAUNCH(G, K, P)                                                                           \
+  e = set_smem(patch_ncc_kernel<G, K, P>, L.bytes);                                                       \
+  if (e != cudaSuccess) return e;                                                                          \
+  patch_ncc_kernel<G, K, P><<<grid, kThreads, L.bytes, s>>>(mov, rows, cols, radius, stride, ncr, ncc, px, py, \
+                                                            run, partials);
+#define XR_PATCH_PASS(G, K) \
+  if (pass == 0) {          \
+    XR_PATCH_LAUNCH(G, K, 0) \
+  } else {                  \
+    XR_PATCH_LAUNCH(G, K, 1) \
   }
+  if (!grad) {
+    XR_PATCH_PASS(0, 0)
+  } else if (kr == 0) {
+    XR_PATCH_PASS(1, 0)
+  } else if (kr == 1) {
+    XR_PATCH_PASS(1, 1)
+  } else {
+    XR_PATCH_PASS(1, 2)
+  }
+#undef XR_PATCH_PASS
 #undef XR_PATCH_LAUNCH
   return cudaGetLastError();
 }
 
-cudaError_t launch_patch_finalize(const double* partials, int nblk, int64_t nimgs, int64_t npatch, int grad,
-                                  float* sims, cudaStream_t s) {
+cudaError_t launch_patch_sum_partials(const double* partials, int nblk, int64_t nimgs, double* out, cudaStream_t s) {
   if (nimgs <= 0) return cudaSuccess;
-  patch_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, (double)npatch, grad,
-                                                                        sims);
+  patch_sum_partials_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_patch_finalize(const double* partials, int nblk, int64_t nimgs, double den_x, double den_y,
+                                  int grad, int mvar, int normalize, const double* mvar_sum, float* sims,
+                                  cudaStream_t s) {
+  if (nimgs <= 0) return cudaSuccess;
+  patch_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, den_x, den_y, grad,
+                                                                        mvar, normalize, mvar_sum, sims);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_patch_scatter_counts(const int32_t* idx, int64_t n, int32_t* cnt, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  patch_scatter_counts_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(idx, n, cnt);
   return cudaGetLastError();
 }
 
