@@ -118,9 +118,17 @@ def test_metric_errors(xr):
     with pytest.raises(_lib.XRegError):
         m.allocate_resources()  # no fixed image
     m.set_fixed_image(np.zeros((20, 20), np.float32))
-    with pytest.raises(_lib.XRegError) as e:
-        m.set_mask(np.ones((20, 20), np.uint8))
-    assert e.value.status == _lib.XR_ERR_UNSUPPORTED
+    m.set_mask(np.ones((20, 20), np.uint8))  # patch metrics take masks (weights, masked sums)
+    with pytest.raises(_lib.XRegError):
+        m.set_patch_options(use_fixed_img_patch_variances_as_wgts=1, use_mov_img_patch_variances_as_wgts=1)
+    with pytest.raises(TypeError):
+        m.set_patch_options(no_such_option=1)
+    import ctypes
+    o = _lib.xr_patch_options()
+    _lib.call("xr_patch_options_default", ctypes.byref(o))
+    plain = xr.ImgSimMetric2DNCCCUDA()
+    with pytest.raises(_lib.XRegError):  # not a patch metric
+        _lib.call("xr_sm_set_patch_options", plain.handle, ctypes.byref(o))
     with pytest.raises(_lib.XRegError):
         m.set_smooth_img_before_sobel_kernel_radius(7)
     with pytest.raises(_lib.XRegError):
