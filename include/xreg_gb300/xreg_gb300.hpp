@@ -168,6 +168,57 @@ struct ImgSimMetric2DNCCCUDA : ImgSimMetric2DCUDA {
   explicit ImgSimMetric2DNCCCUDA(int device = -1) : ImgSimMetric2DCUDA(XR_SIM_NCC, device) {}
 };
 
+// ImgSimMetric2DPatchCommon (xregImgSimMetric2DPatchCommon.h) setters over xr_patch_options.
+class ImgSimMetric2DPatchCUDA : public ImgSimMetric2DCUDA {
+ public:
+  ImgSimMetric2DPatchCUDA(int32_t kind, int device) : ImgSimMetric2DCUDA(kind, device) {}
+  void set_patch_radius(int32_t r) { check(xr_sm_set_patch_radius(h_, r)); }
+  void set_patch_stride(int32_t s) { check(xr_sm_set_patch_stride(h_, s)); }
+  void set_wgt_img(const float* img) { check(xr_sm_set_patch_wgt_img(h_, img)); }
+  void set_use_mask_for_weighting(bool v) { set([&](xr_patch_options& o) { o.use_mask_for_weighting = v; }); }
+  void set_use_mask_for_patch_stats(bool v) { set([&](xr_patch_options& o) { o.use_mask_for_patch_stats = v; }); }
+  void set_normalize_weights_as_prob(bool v) { set([&](xr_patch_options& o) { o.normalize_weights_as_prob = v; }); }
+  void set_weight_patch_sims_in_combine(bool v) {
+    set([&](xr_patch_options& o) { o.weight_patch_sims_in_combine = v; });
+  }
+  void set_compute_mean_of_patch_sims(bool v) { set([&](xr_patch_options& o) { o.compute_mean_of_patch_sims = v; }); }
+  void set_use_fixed_img_patch_variances_as_wgts(bool v) {
+    set([&](xr_patch_options& o) { o.use_fixed_img_patch_variances_as_wgts = v; });
+  }
+  void set_use_mov_img_patch_variances_as_wgts(bool v) {
+    set([&](xr_patch_options& o) { o.use_mov_img_patch_variances_as_wgts = v; });
+  }
+  // random patch subsets; xReg seeds the draw from std::random_device, here from seed
+  void set_choose_rand_patches(bool v, int64_t num = 100, double min_sep = -1.0, uint64_t seed = 0) {
+    set([&](xr_patch_options& o) {
+      o.choose_rand_patches = v;
+      o.num_rand_patches = num;
+      o.rand_patch_min_pixels_sep = min_sep;
+      o.rand_seed = seed;
+    });
+  }
+  std::vector<int64_t> patch_indices_used() const {
+    int64_t n = 0;
+    check(xr_sm_patch_indices_used(h_, 0, nullptr, &n));
+    std::vector<int64_t> out((size_t)n);
+    check(xr_sm_patch_indices_used(h_, n, out.data(), &n));
+    return out;
+  }
+
+ protected:
+  template <typename F>
+  void set(F f) {
+    xr_patch_options o;
+    check(xr_sm_get_patch_options(h_, &o));
+    f(o);
+    check(xr_sm_set_patch_options(h_, &o));
+  }
+};
+
+struct ImgSimMetric2DPatchNCCCUDA : ImgSimMetric2DPatchCUDA {
+  explicit ImgSimMetric2DPatchNCCCUDA(int device = -1) : ImgSimMetric2DPatchCUDA(XR_SIM_PATCH_NCC, device) {}
+};
+
 struct ImgSimMetric2DGradNCCCUDA : ImgSimMetric2DCUDA {
   explicit ImgSimMetric2DGradNCCCUDA(int device = -1) : ImgSimMetric2DCUDA(XR_SIM_GRAD_NCC, device) {}
   void set_smooth_img_before_sobel_kernel_radius(int32_t r) {
@@ -175,13 +226,13 @@ struct ImgSimMetric2DGradNCCCUDA : ImgSimMetric2DCUDA {
   }
 };
 
-struct ImgSimMetric2DPatchGradNCCCUDA : ImgSimMetric2DCUDA {
-  explicit ImgSimMetric2DPatchGradNCCCUDA(int device = -1) : ImgSimMetric2DCUDA(XR_SIM_PATCH_GRAD_NCC, device) {}
+struct ImgSimMetric2DPatchGradNCCCUDA : ImgSimMetric2DPatchCUDA {
+  explicit ImgSimMetric2DPatchGradNCCCUDA(int device = -1) : ImgSimMetric2DPatchCUDA(XR_SIM_PATCH_GRAD_NCC, device) {}
   void set_smooth_img_before_sobel_kernel_radius(int32_t r) {
     check(xr_sm_set_smooth_img_before_sobel_kernel_radius(h_, r));
   }
-  void set_patch_radius(int32_t r) { check(xr_sm_set_patch_radius(h_, r)); }
-  void set_patch_stride(int32_t s) { check(xr_sm_set_patch_stride(h_, s)); }
+  // ImgSimMetric2DPatchGradNCCCPU::set_use_variances_in_grad_imgs_as_wgts
+  void set_use_variances_in_grad_imgs_as_wgts(bool v) { set([&](xr_patch_options& o) { o.use_variances_in_grad_imgs_as_wgts = v; }); }
 };
 
 // Intensity2D3DRegi::obj_fn for one object over a population of poses.

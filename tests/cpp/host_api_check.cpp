@@ -76,6 +76,20 @@ int main(int argc, char** argv) {
     m.compute();
     write_all(dir + "/sims.f32", m.sim_vals());
 
+    // masked patch NCC with moving-image patch variances as weights
+    auto mask = read_all<uint8_t>(dir + "/mask.u8");
+    ImgSimMetric2DPatchNCCCUDA pm;
+    pm.set_fixed_image(fixed.data(), rows, cols);
+    pm.set_mask(mask.data());
+    pm.set_patch_radius(3);
+    pm.set_patch_stride(2);
+    pm.set_use_mov_img_patch_variances_as_wgts(true);
+    pm.set_num_moving_images(npose);
+    pm.set_mov_imgs_buf_from_ray_caster(&rc, 0);
+    pm.allocate_resources();
+    pm.compute();
+    write_all(dir + "/psims.f32", pm.sim_vals());
+
     // the population objective over a second ray caster
     RayCasterLineIntCUDA rc2;
     rc2.set_volume(vol);

@@ -45,6 +45,8 @@ def test_cpp_host_classes_match_oracle(xr, oracle, tmp_path):
     vol.voxels.tofile(tmp_path / "vol.f32")
     poses.astype(np.float64).tofile(tmp_path / "poses.f64")
     fixed.tofile(tmp_path / "fixed.f32")
+    mask = (np.random.default_rng(7).random((rows, cols)) > 0.3).astype(np.uint8)
+    mask.tofile(tmp_path / "mask.u8")
     r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     drr = np.fromfile(tmp_path / "drr.f32", np.float32).reshape(len(poses), rows, cols)
@@ -56,3 +58,6 @@ def test_cpp_host_classes_match_oracle(xr, oracle, tmp_path):
     ref_sims = oracle.grad_ncc(fixed, ref)
     np.testing.assert_allclose(sims, ref_sims, atol=1e-5, rtol=0)
     np.testing.assert_array_equal(obj, sims)
+    psims = np.fromfile(tmp_path / "psims.f32", np.float32)
+    ref_p = oracle.patch_ncc_ex(fixed, drr, radius=3, stride=2, mask=mask, use_mov_var_wgts=1)
+    np.testing.assert_allclose(psims, ref_p, atol=1e-5, rtol=2e-6)
