@@ -328,10 +328,8 @@ def run_ours(a, rank, world, local):
         "vs_baseline": None,
         "dtype": {"f32": "f32", "f16": "f16-volume/f32-accum", "bf16": "bf16-volume/f32-accum"}[a.voxel],
         "data": "synthetic (seeded ellipsoid phantom, sampled poses, noisy fixed DRR)",
-        "config": {"workload": "batched population: 256^3 phantom @1 mm, 1536^2@0.194 mm detector ds 4x -> 384^2, "
-                               "lambda=100, grad-NCC 5x5 Gaussian + Sobel, CUDA graph",
-                   "volume": "256x256x256 " + a.voxel, "detector": "384x384", "pop": POP, "step_mm": w.step,
-                   "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
+        "config": dict(_config(w, a.voxel), l2="flushed between timed steps (256 MB write)",
+                       parallelism=f"replicas x{world}"),
         "e2e": {"value": round(e2e, 2), "unit": "poses/s", "h2d_bytes_per_step": POP * 16 * 8,
                 "d2h_bytes_per_step": POP * 4},
         "gpu_launches": a.steps * 5,
@@ -584,6 +582,13 @@ def _max_over_ranks(x, world):
     return float(t.item())
 
 
+def _config(w, voxel: str) -> dict:
+    """The workload as both arms name it."""
+    return {"workload": "batched population: 256^3 phantom @1 mm, 1536^2@0.194 mm detector ds 4x -> 384^2, "
+                        "lambda=100, grad-NCC 5x5 Gaussian + Sobel",
+            "volume": "256x256x256 " + voxel, "detector": "384x384", "pop": POP, "step_mm": w.step}
+
+
 def run_reference(a, rank, world):
     """The reference's CPU path (restated: the reference cannot be compiled here)
     timed on the host cores: each step evaluates a bounded sample of poses."""
@@ -617,9 +622,9 @@ def run_reference(a, rank, world):
         "metric": "poses/sec (DRR+grad-NCC pose evaluations, batched population)",
         "value": round(v, 3), "unit": "poses/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": round(t * 1e3 / a.steps, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batched population: 256^3 phantom @1 mm, 384^2 detector, grad-NCC",
-                   "pop_per_step": per_step},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantom, sampled poses, noisy fixed DRR)",
+        "config": dict(_config(w, "f32"), pop_per_step=per_step,
+                       parallelism="rank 0 on the host cores"),
         "cpu_baseline": {"value": round(v, 3), "unit": "poses/s", "cores": cores, "kind": "port",
                          "sample": f"{per_step} poses per step; xReg's CPU ray caster + grad-NCC restated in C "
                                    "(the reference needs ITK/OpenCV/TBB, absent here)"},
