@@ -574,6 +574,13 @@ cudaError_t launch_multi_unroll(const MultiJobDrr* d_jobs, int njobs, long long 
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
+  // The kernel uses no shared memory: ask for the largest L1 (the gathers hit it).
+  static bool carveout_set = false;
+  if (!carveout_set) {
+    cudaFuncSetAttribute(drr_kernel<VT, KERNEL, LAYOUT, UNROLL>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxL1);
+    carveout_set = true;
+  }
   const int bw = p.block_warps_x;
   const int tx = 8 * bw, ty = 32 / bw;
   const int64_t max_x = 0x7fffffff;
