@@ -164,6 +164,16 @@ XR_API xr_status xr_rc_copy_projs_to_host(xr_raycaster rc, float* host_dst);
 /* to_cuda_buf(): device address of the projection buffer (view-major, row-major
  * images, num_projs * rows * cols floats), valid until the next allocate_resources. */
 XR_API xr_status xr_rc_device_pixel_buf(xr_raycaster rc, float** out);
+/* use_other_proj_buf (xregRayCastInterface.h:320): this caster writes its images
+ * into the device buffer of `other` (same detector size, enough allocated
+ * projections), e.g. several objects accumulated into one DRR with the
+ * accumulate store method; NULL restores its own buffer.  A destroyed `other`
+ * is detected at the next compute. */
+XR_API xr_status xr_rc_use_other_proj_buf(xr_raycaster rc, xr_raycaster other);
+/* use_external_host_pixel_buf (xregRayCastInterface.h:287): after every compute
+ * the images are copied into host_buf (num_projs images, row-major), on the
+ * caster's stream; read it after xr_rc_synchronize.  NULL stops the copies. */
+XR_API xr_status xr_rc_use_external_host_pixel_buf(xr_raycaster rc, float* host_buf);
 /* Exact number of trilinear samples the last compute took (algorithmic-bytes
  * accounting); synchronises. */
 XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* out);

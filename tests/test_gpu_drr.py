@@ -333,3 +333,43 @@ def test_macro_cell_skipping_is_exact(xr, oracle, vt):
             o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=step)
             rel, zero = drr_rel_err(outs[-1][0], o)
             assert zero == 0.0 and rel <= (TOL32 if vt == 0 else TOL16)
+
+
+def test_shared_and_external_projection_buffers(xr, oracle):
+    """use_other_proj_buf: a second object's caster accumulates into the first
+    caster's buffer (one DRR of two objects); use_external_host_pixel_buf: the
+    images land in a host array after each compute; a destroyed buffer owner
+    sends the caster back to its own buffer."""
+    vol1 = small_volume(20, (40, 36, 32))
+    vol2 = small_volume(21, (36, 40, 30))
+    cam = small_camera((32, 36), 4.0)
+    poses = synth.sample_poses(vol1, synth.gt_pose(vol1), 3, 5.0, 5.0, seed=4)
+    rcs = []
+    for v in (vol1, vol2):
+        rc = _rc(xr, v, [cam], 0.5)
+        rc.set_num_projs(3)
+        rc.allocate_resources()
+        rc.distribute_xforms_among_cam_models(poses)
+        rcs.append(rc)
+    rc1, rc2 = rcs
+    rc2.use_other_proj_buf(rc1)
+    rc2.use_proj_store_accum_method()
+    host = np.zeros((3, 32, 36), np.float32)
+    rc1.use_external_host_pixel_buf(host)
+    rc1.compute()
+    rc2.compute()
+    rc1.synchronize()
+    rc2.synchronize()
+    o1 = oracle.drr_f32(vol1.voxels, oracle_geom(vol1), oracle_cams([cam]), poses, step=0.5)
+    o2 = oracle.drr_f32(vol2.voxels, oracle_geom(vol2), oracle_cams([cam]), poses, step=0.5)
+    rel, zero = drr_rel_err(host, o1)
+    assert zero == 0.0 and rel <= TOL32
+    both = rc1.projs()
+    rel, zero = drr_rel_err(both, o1 + o2)
+    assert zero == 0.0 and rel <= TOL32
+    np.testing.assert_array_equal(rc2.projs(), both)
+    rc1.close()
+    rc2.use_proj_store_replace_method()
+    rc2.compute()
+    rel, zero = drr_rel_err(rc2.projs(), o2)
+    assert zero == 0.0 and rel <= TOL32

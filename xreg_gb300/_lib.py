@@ -93,6 +93,8 @@ _SIGS = {
     "xr_rc_proj": [H, i64, P],
     "xr_rc_copy_projs_to_host": [H, P],
     "xr_rc_device_pixel_buf": [H, C.POINTER(P)],
+    "xr_rc_use_other_proj_buf": [H, H],
+    "xr_rc_use_external_host_pixel_buf": [H, P],
     "xr_rc_last_num_samples": [H, C.POINTER(u64)],
     "xr_rc_set_count_samples": [H, i32],
     "xr_rc_set_launch_config": [H, i32, i32, i32],

@@ -294,6 +294,22 @@ class RayCasterLineIntCUDA:
         call("xr_rc_device_pixel_buf", self._h, C.byref(p))
         return int(p.value or 0)
 
+    def use_other_proj_buf(self, other: "RayCasterLineIntCUDA | None") -> None:
+        """RayCaster::use_other_proj_buf: write the images into other's buffer."""
+        call("xr_rc_use_other_proj_buf", self._h, other.handle if other is not None else None)
+        self._other_ref = other
+
+    def use_external_host_pixel_buf(self, buf: np.ndarray | None) -> None:
+        """RayCaster::use_external_host_pixel_buf: a float32 array of
+        num_projs x rows x cols that receives the images after each compute
+        (read it after synchronize())."""
+        if buf is None:
+            call("xr_rc_use_external_host_pixel_buf", self._h, None)
+        else:
+            assert buf.dtype == np.float32 and buf.flags["C_CONTIGUOUS"]
+            call("xr_rc_use_external_host_pixel_buf", self._h, _ptr(buf))
+        self._ext_ref = buf
+
     def last_num_samples(self) -> int:
         v = C.c_uint64()
         call("xr_rc_last_num_samples", self._h, C.byref(v))

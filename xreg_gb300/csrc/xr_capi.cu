@@ -122,6 +122,11 @@ bool reg_alive(const void* p, uint64_t id) {
   return it != g_live.end() && it->second == id;
 }
 
+bool reg_contains(const void* p) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  return g_live.count(p) != 0;
+}
+
 bool finite_all(const double* v, int64_t n) {
   for (int64_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return false;
@@ -180,6 +185,9 @@ struct xr_raycaster_s {
   bool cam_idx_dirty = true;
 
   DevBuf d_xforms, d_cam_idx, d_geo, d_proj, d_counters;
+  xr_raycaster other = nullptr;    // use_other_proj_buf: writes into this caster's buffer
+  uint64_t other_id = 0;
+  float* ext_host = nullptr;       // use_external_host_pixel_buf: copy of the images after each compute
   bool allocated = false;
   bool count_samples = false;
   uint64_t generation = 1;         // bumps on every change that affects launches
@@ -801,6 +809,18 @@ static xr_status rc_distribute_device_on(xr_raycaster rc, int64_t n, const doubl
 
 // Uploads dirty host state, enqueues the geometry kernel on stream s and fills
 // the DRR launch parameters (without choosing a launch configuration).
+// The device buffer a caster's images go to: its own, or the one of the caster
+// given to use_other_proj_buf while that one is alive; *cap = images it holds.
+static float* rc_out(xr_raycaster rc, int64_t* cap) {
+  if (rc->other && !reg_alive(rc->other, rc->other_id)) { rc->other = nullptr; rc->other_id = 0; }
+  if (rc->other) {
+    if (cap) *cap = rc->other->allocated ? rc->other->capacity : 0;
+    return rc->other->d_proj.as<float>();
+  }
+  if (cap) *cap = rc->capacity;
+  return rc->d_proj.as<float>();
+}
+
 static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, DrrParams& p) {
   XR_CHECK_ARG(rc, "compute: NULL handle");
   if (!rc->allocated) return fail(XR_ERR_NOT_ALLOCATED, "compute: allocate_resources has not been called");
@@ -848,7 +868,15 @@ static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, Dr
   p.geo = rc->d_geo.as<ProjGeom>();
   p.cam_idx = rc->d_cam_idx.as<int32_t>();
   p.bg_projs = rc->use_bg ? rc->d_bg.as<float>() : nullptr;
-  p.out = rc->d_proj.as<float>();
+  {
+    int64_t cap = 0;
+    p.out = rc_out(rc, &cap);
+    if (rc->other) {
+      XR_CHECK_ARG(rc->other->rows() == rc->rows() && rc->other->cols() == rc->cols(),
+                   "compute: the shared projection buffer has another detector size");
+      XR_CHECK_ARG(n <= cap, "compute: more projections than the shared buffer holds");
+    }
+  }
   p.sample_counter = rc->count_samples ? reinterpret_cast<unsigned long long*>(rc->d_counters.p) : nullptr;
   p.err_counter = reinterpret_cast<unsigned int*>(rc->d_counters.as<char>() + 8);
   {
@@ -883,6 +911,9 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
   rc->last_bw = p.block_warps_x;
   rc->last_unroll = p.unroll;
   XR_CUDA_TRY(launch_drr(p, s));
+  if (rc->ext_host)
+    XR_CUDA_TRY(cudaMemcpyAsync(rc->ext_host, p.out, (size_t)p.num_projs * (size_t)(rc->rows() * rc->cols()) * 4,
+                                cudaMemcpyDeviceToHost, s));
   return XR_OK;
 }
 
@@ -936,7 +967,7 @@ extern "C" XR_API xr_status xr_rc_proj(xr_raycaster rc, int64_t idx, float* dst)
   if (st != XR_OK) return st;
   DeviceGuard g(rc->device);
   const size_t npix = (size_t)(rc->rows() * rc->cols());
-  XR_CUDA_TRY(cudaMemcpy(dst, rc->d_proj.as<float>() + (size_t)idx * npix, npix * 4, cudaMemcpyDeviceToHost));
+  XR_CUDA_TRY(cudaMemcpy(dst, rc_out(rc, nullptr) + (size_t)idx * npix, npix * 4, cudaMemcpyDeviceToHost));
   return XR_OK;
 }
 
@@ -947,14 +978,37 @@ extern "C" XR_API xr_status xr_rc_copy_projs_to_host(xr_raycaster rc, float* dst
   if (st != XR_OK) return st;
   DeviceGuard g(rc->device);
   const size_t n = (size_t)(rc->rows() * rc->cols()) * (size_t)rc->num_projs;
-  XR_CUDA_TRY(cudaMemcpy(dst, rc->d_proj.p, n * 4, cudaMemcpyDeviceToHost));
+  XR_CUDA_TRY(cudaMemcpy(dst, rc_out(rc, nullptr), n * 4, cudaMemcpyDeviceToHost));
   return XR_OK;
 }
 
 extern "C" XR_API xr_status xr_rc_device_pixel_buf(xr_raycaster rc, float** out) {
   XR_CHECK_ARG(rc && out, "device_pixel_buf: NULL argument");
   XR_CHECK_ARG(rc->allocated, "device_pixel_buf: resources not allocated");
-  *out = rc->d_proj.as<float>();
+  *out = rc_out(rc, nullptr);
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_use_other_proj_buf(xr_raycaster rc, xr_raycaster other) {
+  XR_CHECK_ARG(rc, "use_other_proj_buf: NULL handle");
+  if (!other || other == rc) {
+    rc->other = nullptr;
+    rc->other_id = 0;
+  } else {
+    XR_CHECK_ARG(reg_contains(other), "use_other_proj_buf: unknown or destroyed ray caster");
+    XR_CHECK_ARG(other->device == rc->device, "use_other_proj_buf: the ray casters are on different devices");
+    XR_CHECK_ARG(!other->other, "use_other_proj_buf: that ray caster itself writes into another's buffer");
+    rc->other = other;
+    rc->other_id = other->id;
+  }
+  rc->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_use_external_host_pixel_buf(xr_raycaster rc, float* host_buf) {
+  XR_CHECK_ARG(rc, "use_external_host_pixel_buf: NULL handle");
+  rc->ext_host = host_buf;
+  rc->generation++;
   return XR_OK;
 }
 
@@ -1474,9 +1528,10 @@ static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
     XR_CHECK_ARG(rc->allocated, "compute: the bound ray caster has no buffer");
     XR_CHECK_ARG(rc->rows() == sm->rows && rc->cols() == sm->cols,
                  "compute: ray caster image size differs from the fixed image");
-    XR_CHECK_ARG(sm->proj_offset + sm->num_mov <= rc->capacity,
-                 "compute: moving images run past the ray caster's buffer");
-    mov = rc->d_proj.as<float>() + sm->proj_offset * npix;
+    int64_t cap = 0;
+    const float* buf = rc_out(rc, &cap);
+    XR_CHECK_ARG(sm->proj_offset + sm->num_mov <= cap, "compute: moving images run past the ray caster's buffer");
+    mov = buf + sm->proj_offset * npix;
   } else {
     XR_CHECK_ARG(sm->mov_dev, "compute: no moving image buffer (was the bound ray caster destroyed?)");
     mov = sm->mov_dev + sm->proj_offset * npix;
@@ -1667,8 +1722,10 @@ static bool obj_graph_valid(xr_objective obj, int64_t pop) {
 static xr_status obj_run(xr_objective obj, int64_t pop) {
   xr_raycaster rc = obj->rc;
   cudaStream_t s = rc->stream();
-  // A metric that draws random patches on the host at every compute is run
-  // directly (a captured graph would replay one draw).
+  // A metric that draws random patches on the host at every compute, or a copy
+  // into an external host buffer, is run directly (a captured graph would replay
+  // one draw; pageable copies cannot be captured).
+  if (rc->ext_host) return obj_enqueue(obj, pop);
   for (xr_simmetric m : obj->metrics)
     if ((m->kind == XR_SIM_PATCH_NCC || m->kind == XR_SIM_PATCH_GRAD_NCC) && m->popt.choose_rand_patches)
       return obj_enqueue(obj, pop);
@@ -1743,13 +1800,6 @@ struct xr_jobset_s {
   long long last_items = 0;
   cudaStream_t stream() const { return has_ext ? ext_stream : own_stream; }
 };
-
-namespace {
-bool reg_contains(const void* p) {
-  std::lock_guard<std::mutex> lk(g_reg_mu);
-  return g_live.count(p) != 0;
-}
-}  // namespace
 
 extern "C" XR_API xr_status xr_jobset_create(int32_t device, xr_jobset* out) {
   XR_CHECK_ARG(out, "xr_jobset_create: out is NULL");
