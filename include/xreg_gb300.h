@@ -226,6 +226,9 @@ XR_API xr_status xr_sm_set_num_moving_images(xr_simmetric sm, int64_t n);
 /* set_mov_imgs_buf_from_ray_caster (xregImgSimMetric2DCPU.cpp:43-72): the moving
  * images are read in place from the ray caster's device buffer at proj_offset. */
 XR_API xr_status xr_sm_set_mov_imgs_buf_from_ray_caster(xr_simmetric sm, xr_raycaster rc, int64_t proj_offset);
+/* set_mov_imgs_host_buf (xregImgSimMetric2D.h:122): num_moving_images host
+ * images, copied to the device at every compute (the buffer must stay valid). */
+XR_API xr_status xr_sm_set_mov_imgs_host_buf(xr_simmetric sm, const float* host_imgs);
 /* set_mov_imgs_host_buf analogue for device memory (xregImgSimMetric2DCPU.cpp:74-88). */
 XR_API xr_status xr_sm_set_mov_imgs_device_buf(xr_simmetric sm, const float* d_imgs, int64_t proj_offset);
 /* ImgSimMetric2DGradImgParamInterface::set_smooth_img_before_sobel_kernel_radius

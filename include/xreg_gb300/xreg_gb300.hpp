@@ -122,6 +122,9 @@ class RayCasterLineIntCUDA {
     return out;
   }
   float* to_cuda_buf() const { float* p = nullptr; check(xr_rc_device_pixel_buf(h_, &p)); return p; }
+  // RayCaster::use_other_proj_buf / use_external_host_pixel_buf
+  void use_other_proj_buf(RayCasterLineIntCUDA* other) { check(xr_rc_use_other_proj_buf(h_, other ? other->h_ : nullptr)); }
+  void use_external_host_pixel_buf(float* buf) { check(xr_rc_use_external_host_pixel_buf(h_, buf)); }
   // RayCasterCPU::use_other_proj_buf is unsupported in xReg's CPU caster as well.
   void use_other_proj_buf(RayCasterLineIntCUDA*) {
     throw UnsupportedOperationException(XR_ERR_UNSUPPORTED, "use_other_proj_buf is not supported");
@@ -150,6 +153,7 @@ class ImgSimMetric2DCUDA {
   void set_mov_imgs_buf_from_ray_caster(RayCasterLineIntCUDA* rc, int64_t proj_offset = 0) {
     check(xr_sm_set_mov_imgs_buf_from_ray_caster(h_, rc->handle(), proj_offset));
   }
+  void set_mov_imgs_host_buf(const float* imgs) { check(xr_sm_set_mov_imgs_host_buf(h_, imgs)); }
   void allocate_resources() { check(xr_sm_allocate_resources(h_)); }
   void compute() { check(xr_sm_compute(h_)); }
   std::vector<float> sim_vals() const {

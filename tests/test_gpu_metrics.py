@@ -133,3 +133,19 @@ def test_metric_errors(xr):
         m.set_smooth_img_before_sobel_kernel_radius(7)
     with pytest.raises(_lib.XRegError):
         m.compute()
+
+
+def test_host_buffer_input(xr, oracle):
+    """set_mov_imgs_host_buf: host images copied to the device at each compute."""
+    rc, imgs, fixed = _drrs(xr, seed=4)
+    m = xr.ImgSimMetric2DGradNCCCUDA()
+    m.set_fixed_image(fixed)
+    m.set_num_moving_images(5)
+    host = np.ascontiguousarray(imgs[1:6])
+    m.set_mov_imgs_host_buf(host)
+    m.allocate_resources()
+    m.compute()
+    np.testing.assert_allclose(m.sim_vals(), oracle.grad_ncc(fixed, host), atol=TOL, rtol=0)
+    host[:] = imgs[2:7]  # the buffer is read again at every compute
+    m.compute()
+    np.testing.assert_allclose(m.sim_vals(), oracle.grad_ncc(fixed, imgs[2:7]), atol=TOL, rtol=0)

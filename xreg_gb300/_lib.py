@@ -109,6 +109,7 @@ _SIGS = {
     "xr_sm_set_num_moving_images": [H, i64],
     "xr_sm_set_mov_imgs_buf_from_ray_caster": [H, H, i64],
     "xr_sm_set_mov_imgs_device_buf": [H, P, i64],
+    "xr_sm_set_mov_imgs_host_buf": [H, P],
     "xr_sm_set_smooth_img_before_sobel_kernel_radius": [H, i32],
     "xr_sm_set_patch_radius": [H, i32],
     "xr_sm_set_patch_stride": [H, i32],

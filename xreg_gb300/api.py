@@ -370,6 +370,13 @@ class ImgSimMetric2DCUDA:
         call("xr_sm_set_mov_imgs_buf_from_ray_caster", self._h, rc.handle, int(proj_offset))
         self._rc_ref = rc  # keep the ray caster alive at least as long as this metric
 
+    def set_mov_imgs_host_buf(self, imgs: np.ndarray) -> None:
+        """ImgSimMetric2D::set_mov_imgs_host_buf: float32 images (n x rows x cols),
+        copied to the device at every compute."""
+        a = np.ascontiguousarray(imgs, dtype=np.float32)
+        self._host_ref = a
+        call("xr_sm_set_mov_imgs_host_buf", self._h, _ptr(a))
+
     def set_mov_imgs_device_buf(self, d_ptr: int, proj_offset: int = 0) -> None:
         call("xr_sm_set_mov_imgs_device_buf", self._h, C.c_void_p(int(d_ptr)), int(proj_offset))
 

@@ -214,6 +214,8 @@ struct xr_simmetric_s {
   xr_raycaster rc = nullptr;       // bound ray caster (checked with rc_id before use)
   uint64_t rc_id = 0;
   const float* mov_dev = nullptr;
+  const float* mov_host = nullptr; // set_mov_imgs_host_buf: copied to d_mov_stage at each compute
+  DevBuf d_mov_stage;
   int64_t proj_offset = 0;
   int32_t smooth_ksize = 5;
   int32_t patch_radius = 5;
@@ -1148,7 +1150,19 @@ extern "C" XR_API xr_status xr_sm_set_mov_imgs_buf_from_ray_caster(xr_simmetric 
   sm->rc = rc;
   sm->rc_id = rc->id;
   sm->mov_dev = nullptr;
+  sm->mov_host = nullptr;
   sm->proj_offset = off;
+  sm->generation++;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_set_mov_imgs_host_buf(xr_simmetric sm, const float* h) {
+  XR_CHECK_ARG(sm && h, "set_mov_imgs_host_buf: NULL argument");
+  sm->rc = nullptr;
+  sm->rc_id = 0;
+  sm->mov_dev = nullptr;
+  sm->mov_host = h;
+  sm->proj_offset = 0;
   sm->generation++;
   return XR_OK;
 }
@@ -1157,6 +1171,7 @@ extern "C" XR_API xr_status xr_sm_set_mov_imgs_device_buf(xr_simmetric sm, const
   XR_CHECK_ARG(sm && d && off >= 0, "set_mov_imgs_device_buf: NULL argument or negative offset");
   sm->rc = nullptr;
   sm->rc_id = 0;
+  sm->mov_host = nullptr;
   sm->mov_dev = d;
   sm->proj_offset = off;
   sm->generation++;
@@ -1459,7 +1474,7 @@ extern "C" XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm) {
   XR_CHECK_ARG(sm, "allocate_resources: NULL handle");
   XR_CHECK_ARG(sm->has_fixed, "allocate_resources: no fixed image");
   XR_CHECK_ARG(sm->num_mov > 0, "allocate_resources: num_moving_images is 0");
-  XR_CHECK_ARG(sm->live_rc() || sm->mov_dev, "allocate_resources: no moving image buffer");
+  XR_CHECK_ARG(sm->live_rc() || sm->mov_dev || sm->mov_host, "allocate_resources: no moving image buffer");
   DeviceGuard g(sm->device);
   cudaStream_t s = sm->stream();
   const int64_t n = sm->rows * sm->cols;
@@ -1532,6 +1547,12 @@ static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
     const float* buf = rc_out(rc, &cap);
     XR_CHECK_ARG(sm->proj_offset + sm->num_mov <= cap, "compute: moving images run past the ray caster's buffer");
     mov = buf + sm->proj_offset * npix;
+  } else if (sm->mov_host) {
+    // ImgSimMetric2DCPU::set_mov_imgs_host_buf: the host images go to the device first
+    XR_CUDA_TRY(sm->d_mov_stage.reserve((size_t)(sm->num_mov * npix) * 4));
+    XR_CUDA_TRY(cudaMemcpyAsync(sm->d_mov_stage.p, sm->mov_host, (size_t)(sm->num_mov * npix) * 4,
+                                cudaMemcpyHostToDevice, s));
+    mov = sm->d_mov_stage.as<float>();
   } else {
     XR_CHECK_ARG(sm->mov_dev, "compute: no moving image buffer (was the bound ray caster destroyed?)");
     mov = sm->mov_dev + sm->proj_offset * npix;
