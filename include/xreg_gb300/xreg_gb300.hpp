@@ -122,13 +122,10 @@ class RayCasterLineIntCUDA {
     return out;
   }
   float* to_cuda_buf() const { float* p = nullptr; check(xr_rc_device_pixel_buf(h_, &p)); return p; }
-  // RayCaster::use_other_proj_buf / use_external_host_pixel_buf
+  // RayCaster::use_other_proj_buf (as RayCasterOCL: this caster writes into the
+  // other's device buffer) / use_external_host_pixel_buf
   void use_other_proj_buf(RayCasterLineIntCUDA* other) { check(xr_rc_use_other_proj_buf(h_, other ? other->h_ : nullptr)); }
   void use_external_host_pixel_buf(float* buf) { check(xr_rc_use_external_host_pixel_buf(h_, buf)); }
-  // RayCasterCPU::use_other_proj_buf is unsupported in xReg's CPU caster as well.
-  void use_other_proj_buf(RayCasterLineIntCUDA*) {
-    throw UnsupportedOperationException(XR_ERR_UNSUPPORTED, "use_other_proj_buf is not supported");
-  }
 
  private:
   xr_raycaster h_ = nullptr;
