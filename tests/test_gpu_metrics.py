@@ -141,7 +141,7 @@ def test_host_buffer_input(xr, oracle):
     m = xr.ImgSimMetric2DGradNCCCUDA()
     m.set_fixed_image(fixed)
     m.set_num_moving_images(5)
-    host = np.ascontiguousarray(imgs[1:6])
+    host = imgs[1:6].copy()
     m.set_mov_imgs_host_buf(host)
     m.allocate_resources()
     m.compute()
