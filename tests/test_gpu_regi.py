@@ -76,3 +76,11 @@ def test_server_admission_respects_budget(xr):
     while srv.queue or srv.active:
         srv.step()
     assert srv.stats.completed == 3 and srv.stats.max_active == 1
+
+
+def test_reset_repeats_the_registration(xr):
+    job, _ = synth.job_registration(_spec(41, size=(64, 64, 64), pop=8), iters=(6, 4), level2_pop=4)
+    first = job.run().copy()
+    job.reset()
+    assert not job.done and job.results == []
+    np.testing.assert_array_equal(job.run(), first)

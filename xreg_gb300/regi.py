@@ -97,6 +97,21 @@ class Registration:
         self.t_done = None
         self._pop_x = None
 
+    def reset(self) -> None:
+        """Back to the state before start(): the same request can be run again
+        (its optimizers are seeded, so it repeats the same registration)."""
+        if self.obj is not None:
+            self.obj.close()
+        if self.rc is not None:
+            self.rc.close()
+        self.rc = self.obj = self.es = None
+        self.level = -1
+        self.start_pose = self.init_pose.copy()
+        self.results = []
+        self.done = self.started = False
+        self.t_submit = self.t_start = self.t_done = None
+        self._pop_x = None
+
     # ---------------------------------------------------------- resources
     def footprint_bytes(self) -> int:
         """Device memory the job holds while active (volume copies + the largest level's buffers)."""
