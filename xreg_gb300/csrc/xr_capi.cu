@@ -1937,6 +1937,13 @@ static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* obj
     js->blocks = std::max(js->blocks, blocks);
   }
   for (int32_t i = 0; i < n; ++i) {
+    xr_raycaster rc = objs[i]->rc;
+    if (rc->ext_host)
+      XR_CUDA_TRY(cudaMemcpyAsync(rc->ext_host, rc_out(rc, nullptr),
+                                  (size_t)rc->num_projs * (size_t)(rc->rows() * rc->cols()) * 4,
+                                  cudaMemcpyDeviceToHost, s));
+  }
+  for (int32_t i = 0; i < n; ++i) {
     xr_objective obj = objs[i];
     const int64_t pop = pops[i];
     const int32_t nv = (int32_t)obj->metrics.size();
