@@ -557,36 +557,47 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   }
 }
 
-// Per image: out[img][2] = the two sums over blocks of the partials.
-__global__ void patch_sum_partials_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs,
-                                          double* __restrict__ out) {
-  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (img >= nimgs) return;
-  double a = 0, b = 0;
-  const double* p = partials + img * nblk * 2;
-  for (int k = 0; k < nblk; ++k) { a += p[2 * k]; b += p[2 * k + 1]; }
-  out[img * 2] = a;
-  out[img * 2 + 1] = b;
+// Per image (one block each): the two sums over the blocks' partials.
+__device__ __forceinline__ void patch_partials_sum(const double* __restrict__ p, int nblk, double (&v)[2],
+                                                   double* red) {
+  v[0] = 0.0;
+  v[1] = 0.0;
+  for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
+    v[0] += p[2 * k];
+    v[1] += p[2 * k + 1];
+  }
+  block_sum_d<2>(v, red);
+}
+
+__global__ void patch_sum_partials_kernel(const double* __restrict__ partials, int nblk, double* __restrict__ out) {
+  __shared__ double red[2 * 32];
+  const int64_t img = blockIdx.x;
+  double v[2];
+  patch_partials_sum(partials + img * nblk * 2, nblk, v, red);
+  if (threadIdx.x == 0) {
+    out[img * 2] = v[0];
+    out[img * 2 + 1] = v[1];
+  }
 }
 
 // Value per image: sum / denominator per direction; FLT_MAX where normalised
 // moving variances sum to at most 1e-6; patch grad-NCC 0.5 (s_x + s_y) in float.
-__global__ void patch_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double den_x,
-                                      double den_y, int grad, int mvar, int normalize,
-                                      const double* __restrict__ mvar_sum, float* __restrict__ sims) {
-  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (img >= nimgs) return;
-  double a = 0, b = 0;
-  const double* p = partials + img * nblk * 2;
-  for (int k = 0; k < nblk; ++k) { a += p[2 * k]; b += p[2 * k + 1]; }
+__global__ void patch_finalize_kernel(const double* __restrict__ partials, int nblk, double den_x, double den_y,
+                                      int grad, int mvar, int normalize, const double* __restrict__ mvar_sum,
+                                      float* __restrict__ sims) {
+  __shared__ double red[2 * 32];
+  const int64_t img = blockIdx.x;
+  double v[2];
+  patch_partials_sum(partials + img * nblk * 2, nblk, v, red);
+  if (threadIdx.x != 0) return;
   const bool chk = mvar && normalize;
   if (chk && mvar == 1 && !((float)mvar_sum[img * 2] > 1.0e-6f)) {
     sims[img] = FLT_MAX;
     return;
   }
-  const float sx = (chk && !((float)mvar_sum[img * 2] > 1.0e-6f)) ? FLT_MAX : (float)(a / den_x);
+  const float sx = (chk && !((float)mvar_sum[img * 2] > 1.0e-6f)) ? FLT_MAX : (float)(v[0] / den_x);
   if (grad) {
-    const float sy = (chk && !((float)mvar_sum[img * 2 + 1] > 1.0e-6f)) ? FLT_MAX : (float)(b / den_y);
+    const float sy = (chk && !((float)mvar_sum[img * 2 + 1] > 1.0e-6f)) ? FLT_MAX : (float)(v[1] / den_y);
     sims[img] = 0.5f * (sx + sy);
   } else {
     sims[img] = sx;
@@ -739,7 +750,7 @@ cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs
 
 cudaError_t launch_patch_sum_partials(const double* partials, int nblk, int64_t nimgs, double* out, cudaStream_t s) {
   if (nimgs <= 0) return cudaSuccess;
-  patch_sum_partials_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, out);
+  patch_sum_partials_kernel<<<(unsigned)nimgs, 256, 0, s>>>(partials, nblk, out);
   return cudaGetLastError();
 }
 
@@ -747,8 +758,8 @@ cudaError_t launch_patch_finalize(const double* partials, int nblk, int64_t nimg
                                   int grad, int mvar, int normalize, const double* mvar_sum, float* sims,
                                   cudaStream_t s) {
   if (nimgs <= 0) return cudaSuccess;
-  patch_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, den_x, den_y, grad,
-                                                                        mvar, normalize, mvar_sum, sims);
+  patch_finalize_kernel<<<(unsigned)nimgs, 256, 0, s>>>(partials, nblk, den_x, den_y, grad, mvar, normalize,
+                                                       mvar_sum, sims);
   return cudaGetLastError();
 }
 
