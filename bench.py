@@ -49,6 +49,8 @@ def _args():
     p.add_argument("--voxel", default="f32", choices=["f32", "f16", "bf16"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true")
+    p.add_argument("--only", default="", choices=["", "precision", "multi-job", "serving"],
+                   help="run one of the extra measurements alone and print its JSON (for profiling)")
     p.add_argument("--serving-requests", type=int, default=10, help="requests in the serving measurement (0 = off)")
     p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving measurement")
     p.add_argument("--launch-config", default="auto",
@@ -657,7 +659,16 @@ def main():
         if a.impl != "reference":
             torch.cuda.set_device(local)
         dist.init_process_group(backend)
-    if a.impl == "reference":
+    if a.only:
+        import torch
+        import xreg_gb300 as xr
+        torch.cuda.set_device(local)
+        xr.load()
+        fn = {"precision": lambda: _precision(xr, local, torch.cuda.Stream(device=local)),
+              "multi-job": lambda: _multi_job(xr, local),
+              "serving": lambda: _serving(local, a.serving_requests, a.serving_rate)}[a.only]
+        res = {"only": a.only, "result": fn()} if rank == 0 else None
+    elif a.impl == "reference":
         res = run_reference(a, rank, world)
     else:
         res = run_ours(a, rank, world, local)
