@@ -24,8 +24,13 @@
  *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchCommon.cpp:256-300 patch grid
  *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchNCCCPU.cpp:74-300,332-441,
  *        558-619                                    patch NCC
- *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchGradNCCCPU.cpp:104-230
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchGradNCCCPU.cpp:34-400
+ *   lib/regi/sim_metrics_2d/xregImgSimMetric2DPatchCommon.cpp:306-493 patch
+ *        weights (mask / weight image / variances, normalisation), subsets
  *   lib/image/xregHUToLinAtt.cpp:45-69              HU -> linear attenuation
+ *   lib/image/xregProjData.cpp:40-53, lib/itk/xregITKResampleUtils.h:51-187
+ *                                                    DownsampleImage
+ *   lib/image/xregImageIntensLogTrans.cpp:52-146    log remap (ProjPreProc)
  *
  * Third-party arithmetic restated from published descriptions (absent here):
  *   ITK 5.1.1 LinearInterpolateImageFunction: trilinear at a continuous index,
@@ -35,6 +40,13 @@
  *   OpenCV 3.4 GaussianBlur(ksize 5x5, sigma 0): separable, the fixed small
  *     kernel [1 4 6 4 1]/16; Sobel(ksize 3): [-1 0 1] x [1 2 1]; both with the
  *     default border BORDER_REFLECT_101 (gfedcb|abcdefgh|gfedcba).
+ *   ITK DiscreteGaussianImageFilter / GaussianOperator: Lindeberg's discrete
+ *     Gaussian e^-t I_k(t) (I_0, I_1 from their power series; Bessel recurrence
+ *     for k >= 2), cut at 1 - max_error or 32 one-sided taps, replicated edges,
+ *     double passes, float output.
+ *   ITK BSplineDecompositionImageFilter + BSplineInterpolateImageFunction,
+ *     order 3 (Unser, "Splines: a perfect fit for signal and image processing",
+ *     1999, Box 2): mirror-boundary recursive prefilter, 4 x 4 weights.
  *
  * Geometry precision contract (shared with the CUDA kernels on purpose): the
  * per-projection set-up (index<->physical inverse, camera inverse, pose
