@@ -61,6 +61,35 @@ XR_API xr_status xr_dfo_tell(xr_dfo d, const double* fvals);
 XR_API xr_status xr_dfo_test_termination(xr_dfo d, int32_t* reason);
 XR_API xr_status xr_dfo_get(xr_dfo d, double* best_x, double* best_f, double* rho, int64_t* iterations);
 
+/* ------------------------------------------------ one registration level -- */
+/* The level loop of Intensity2D3DRegiCMAES::run (xregIntensity2D3DRegiCMAES.cpp:76-247)
+ * or of the trust-region level in NLopt LN_BOBYQA's place
+ * (xregIntensity2D3DRegiNLOptInterface.cpp:83-188), run natively over a population
+ * objective (every population / batch of points is one xr_obj_eval).  Offsets x
+ * are SE(3) Lie-algebra vectors [w (rad), v (mm)] (SE3OptVarsLieAlg,
+ * xregSE3OptVars.cpp:128-137) and a candidate pose is
+ * centre * ExpSE3(x) * centre^-1 * start_pose (centre: a rigid frame at the volume
+ * centre, xregIntensity2D3DRegi.cpp:1028-1099); 4x4 row-major doubles. */
+enum { XR_REGI_CMAES = 0, XR_REGI_DFO = 1 };
+typedef struct {
+  int32_t optimizer;   /* XR_REGI_CMAES or XR_REGI_DFO */
+  int32_t lambda;      /* CMA-ES population */
+  double sigma[6];     /* CMA-ES initial standard deviations */
+  double bounds[6];    /* half-widths of the box: CMA-ES redraws candidates outside (0 = unbounded);
+                          the trust region needs all six */
+  int64_t max_iters;
+  double tol_fun, tol_x;    /* CMA-ES stopping tolerances */
+  double rho_beg, rho_end;  /* trust-region radii (mm-scaled, as xr_dfo_create) */
+  uint64_t seed;            /* CMA-ES random stream */
+} xr_regi_level_params;
+XR_API xr_status xr_regi_level_params_default(int32_t optimizer, xr_regi_level_params* out);
+/* best_pose: the pose of the best offset found; best_value, iterations (CMA-ES
+ * generations / trust-region iterations) and stop_reason (xr_cmaes_test_termination
+ * or xr_dfo_test_termination codes) may be NULL. */
+XR_API xr_status xr_regi_run_level(xr_objective obj, const double* centre, const double* start_pose,
+                                   const xr_regi_level_params* params, double* best_pose, double* best_value,
+                                   int64_t* iterations, int32_t* stop_reason);
+
 /* ---------------------------------------------------- data preparation -- */
 /* HUToLinAttFilter (lib/image/xregHUToLinAtt.cpp:45-69): device float HU ->
  * device float attenuation (1/mm), mu_water 0.02683, mu_air 0.02485e-4,

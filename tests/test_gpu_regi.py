@@ -84,3 +84,31 @@ def test_reset_repeats_the_registration(xr):
     job.reset()
     assert not job.done and job.results == []
     np.testing.assert_array_equal(job.run(), first)
+
+
+def test_native_level_driver(xr):
+    """xr_regi_run_level runs a CMA-ES level and a trust-region level in the
+    library and lands where the Python level loop lands (both near the truth)."""
+    from xreg_gb300 import api
+    from xreg_gb300.regi import run_level_native
+    job, gt = synth.job_registration(_spec(3, views=(0.0, 30.0)), iters=(80, 40), level2_pop=10)
+    py_pose = job.run()
+    rc = api.RayCasterLineIntCUDA()
+    rc.set_volume(job.vol, job.voxel_type)
+    rc.set_ray_step_size(job.step)
+    start = job.init_pose
+    for k, L in enumerate(job.levels):
+        rc.set_camera_models(L.cams)
+        ms = []
+        for f in L.fixed:
+            m = api.ImgSimMetric2DGradNCCCUDA()
+            m.set_fixed_image(f)
+            ms.append(m)
+        obj = api.PopulationObjective(rc, ms, 14 if L.optimizer == "dfo" else L.pop)
+        res = run_level_native(obj, job.C, start, L, seed=job.seed * 1009 + k)
+        start = res.pose
+        obj.close()
+    rot, trans = pose_error(start, gt, job.vol)
+    assert rot < 0.05 and trans < 0.1, (rot, trans)
+    rot2, trans2 = pose_error(start, py_pose, job.vol)
+    assert rot2 < 0.05 and trans2 < 0.1, (rot2, trans2)

@@ -22,6 +22,7 @@ XR_ERR_DEVICE_CHECK = -6
 XR_VOXEL_F32, XR_VOXEL_F16, XR_VOXEL_BF16 = 0, 1, 2
 XR_LINE_INT_SUM, XR_LINE_INT_MAX = 0, 1
 XR_PROJ_STORE_REPLACE, XR_PROJ_STORE_ACCUM = 0, 1
+XR_REGI_CMAES, XR_REGI_DFO = 0, 1
 XR_INTERP_LINEAR, XR_INTERP_NN, XR_INTERP_SINC, XR_INTERP_BSPLINE = 0, 1, 2, 3
 XR_CAM_FOCAL_POS_Z, XR_CAM_FOCAL_NEG_Z, XR_CAM_ON_DETECTOR = 0, 1, 2
 XR_LAYOUT_AUTO, XR_LAYOUT_LINEAR, XR_LAYOUT_CELL8 = -1, 0, 1
@@ -47,6 +48,12 @@ class xr_patch_options(C.Structure):
                 ("use_variances_in_grad_imgs_as_wgts", C.c_int32), ("choose_rand_patches", C.c_int32),
                 ("reserved", C.c_int32), ("num_rand_patches", C.c_int64), ("rand_patch_min_pixels_sep", C.c_double),
                 ("rand_seed", C.c_uint64)]
+
+
+class xr_regi_level_params(C.Structure):
+    _fields_ = [("optimizer", C.c_int32), ("lambda_", C.c_int32), ("sigma", C.c_double * 6),
+                ("bounds", C.c_double * 6), ("max_iters", C.c_int64), ("tol_fun", C.c_double),
+                ("tol_x", C.c_double), ("rho_beg", C.c_double), ("rho_end", C.c_double), ("seed", C.c_uint64)]
 
 
 class XRegError(RuntimeError):
@@ -147,6 +154,9 @@ _SIGS = {
     "xr_camera_crop_boundary": [P, i64, P],
     "xr_crop_image_boundary": [P, i64, i64, i64, P, P],
     "xr_log_remap": [P, i64, i64, i32, f32, P, P, P],
+    "xr_regi_level_params_default": [i32, C.POINTER(xr_regi_level_params)],
+    "xr_regi_run_level": [H, P, P, C.POINTER(xr_regi_level_params), P, C.POINTER(f64), C.POINTER(i64),
+                          C.POINTER(i32)],
     "xr_jobset_create": [i32, C.POINTER(H)],
     "xr_jobset_destroy": [H],
     "xr_jobset_set_stream": [H, P],

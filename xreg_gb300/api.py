@@ -479,6 +479,10 @@ class PopulationObjective:
             m._rc_ref = rc
         self.max_pop = int(max_pop)
 
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

@@ -1,0 +1,226 @@
+// xr_regi.cpp -- one registration level run natively over a population
+// objective: the loop of Intensity2D3DRegiCMAES::run
+// (xregIntensity2D3DRegiCMAES.cpp:76-247: sample lambda Lie-algebra offsets,
+// redraw the out-of-bounds ones, evaluate the population, update, test for
+// termination) or of the bound-constrained trust-region level that takes NLopt
+// LN_BOBYQA's place (Intensity2D3DRegiNLOptInterface::run,
+// xregIntensity2D3DRegiNLOptInterface.cpp:83-188), with every population
+// evaluated in one xr_obj_eval call.
+//
+// A candidate offset x = [w, v] (SE3OptVarsLieAlg, xregSE3OptVars.cpp:128-137)
+// maps to the pose  centre * ExpSE3(x) * centre^-1 * start  (the intermediate
+// frame about the volume centre that xReg's pre/post transforms apply,
+// xregIntensity2D3DRegi.cpp:1028-1099); ExpSE3 (xregRigidUtils.cpp:40-85):
+// theta = |w|, R = I + a W + b W^2, t = (I + b W + c W^2) v with a = sin(theta)/theta,
+// b = (1 - cos(theta))/theta^2, c = (theta - sin(theta))/theta^3 (R = I, t = v
+// for theta <= 1e-14).
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "xreg_gb300.h"
+#include "xreg_gb300_regi.h"
+
+namespace xr {
+xr_status fail(xr_status code, const std::string& msg);
+}  // namespace xr
+
+namespace {
+
+using M4 = double[16];
+
+void mat_mul(const double* a, const double* b, double* out) {
+  double t[16];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 4; ++k) s += a[i * 4 + k] * b[k * 4 + j];
+      t[i * 4 + j] = s;
+    }
+  std::memcpy(out, t, sizeof(t));
+}
+
+// Inverse of a rigid transform [R t; 0 1]: [R^T, -R^T t].
+void rigid_inverse(const double* m, double* out) {
+  double t[16] = {0};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) t[i * 4 + j] = m[j * 4 + i];
+  for (int i = 0; i < 3; ++i) t[i * 4 + 3] = -(t[i * 4 + 0] * m[3] + t[i * 4 + 1] * m[7] + t[i * 4 + 2] * m[11]);
+  t[15] = 1.0;
+  std::memcpy(out, t, sizeof(t));
+}
+
+void exp_se3(const double* x, double* out) {
+  const double w[3] = {x[0], x[1], x[2]}, v[3] = {x[3], x[4], x[5]};
+  const double th = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  double W[9] = {0.0, -w[2], w[1], w[2], 0.0, -w[0], -w[1], w[0], 0.0};
+  double WW[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += W[i * 3 + k] * W[k * 3 + j];
+      WW[i * 3 + j] = s;
+    }
+  double R[9], A[9];
+  const bool big = th > 1.0e-14;
+  const double a = big ? std::sin(th) / th : 1.0;
+  const double b = big ? (1.0 - std::cos(th)) / (th * th) : 0.0;
+  const double c = big ? (th - std::sin(th)) / (th * th * th) : 0.0;
+  for (int i = 0; i < 9; ++i) {
+    const double id = (i % 4 == 0) ? 1.0 : 0.0;
+    R[i] = big ? id + a * W[i] + b * WW[i] : id;
+    A[i] = big ? id + b * W[i] + c * WW[i] : id;
+  }
+  std::memset(out, 0, 16 * sizeof(double));
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) out[i * 4 + j] = R[i * 3 + j];
+    out[i * 4 + 3] = A[i * 3 + 0] * v[0] + A[i * 3 + 1] * v[1] + A[i * 3 + 2] * v[2];
+  }
+  out[15] = 1.0;
+}
+
+struct PoseMap {
+  double C[16], B[16];  // pose(x) = C * Exp(x) * B,  B = C^-1 * start
+  void operator()(const double* x, double* out) const {
+    double E[16], CE[16];
+    exp_se3(x, E);
+    mat_mul(C, E, CE);
+    mat_mul(CE, B, out);
+  }
+};
+
+bool finite6(const double* v) {
+  for (int i = 0; i < 6; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+}  // namespace
+
+using namespace xr;
+
+extern "C" XR_API xr_status xr_regi_level_params_default(int32_t optimizer, xr_regi_level_params* out) {
+  if (!out) return fail(XR_ERR_INVALID_ARG, "xr_regi_level_params_default: NULL argument");
+  if (optimizer != XR_REGI_CMAES && optimizer != XR_REGI_DFO)
+    return fail(XR_ERR_INVALID_ARG, "xr_regi_level_params_default: unknown optimizer");
+  xr_regi_level_params p{};
+  p.optimizer = optimizer;
+  p.lambda = 50;
+  const double deg = 3.14159265358979323846 / 180.0;
+  for (int i = 0; i < 3; ++i) {
+    p.sigma[i] = 10.0 * deg;
+    p.sigma[i + 3] = 20.0;
+  }
+  if (optimizer == XR_REGI_DFO) {
+    for (int i = 0; i < 3; ++i) p.bounds[i] = 2.5 * deg;
+    p.bounds[3] = 5.0;
+    p.bounds[4] = 5.0;
+    p.bounds[5] = 10.0;
+    p.max_iters = 100;
+  } else {
+    p.max_iters = 100;
+  }
+  p.tol_fun = 1.0e-6;
+  p.tol_x = 1.0e-6;
+  p.rho_beg = 2.0;
+  p.rho_end = 0.01;
+  p.seed = 0;
+  *out = p;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_regi_run_level(xr_objective obj, const double* centre, const double* start_pose,
+                                             const xr_regi_level_params* p, double* best_pose, double* best_value,
+                                             int64_t* iterations, int32_t* stop_reason) {
+  if (!obj || !centre || !start_pose || !p || !best_pose)
+    return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: NULL argument");
+  if (p->max_iters <= 0) return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: max_iters must be positive");
+  PoseMap map;
+  std::memcpy(map.C, centre, sizeof(map.C));
+  {
+    double Ci[16];
+    rigid_inverse(centre, Ci);
+    mat_mul(Ci, start_pose, map.B);
+  }
+  const double zero[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<double> poses, pop;
+  std::vector<float> sims;
+  std::vector<double> f;
+  double bx[6] = {0}, bf = 0.0;
+  int64_t iters = 0;
+  int32_t reason = 0;
+  xr_status st = XR_OK;
+  auto eval = [&](const double* xs, int32_t n) -> xr_status {
+    poses.resize((size_t)n * 16);
+    sims.resize((size_t)n);
+    f.resize((size_t)n);
+    for (int32_t k = 0; k < n; ++k) map(xs + (size_t)k * 6, poses.data() + (size_t)k * 16);
+    xr_status e = xr_obj_eval(obj, n, poses.data(), sims.data());
+    if (e != XR_OK) return e;
+    for (int32_t k = 0; k < n; ++k) f[(size_t)k] = (double)sims[(size_t)k];
+    return XR_OK;
+  };
+  if (p->optimizer == XR_REGI_CMAES) {
+    if (p->lambda < 2) return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: lambda must be at least 2");
+    xr_cmaes es = nullptr;
+    if ((st = xr_cmaes_create(6, zero, p->sigma, p->lambda, p->seed, &es)) != XR_OK) return st;
+    if ((st = xr_cmaes_set_stop(es, p->tol_fun, p->tol_x, p->max_iters)) != XR_OK) { xr_cmaes_destroy(es); return st; }
+    pop.resize((size_t)p->lambda * 6);
+    bool bounded = false;
+    for (int i = 0; i < 6; ++i) bounded = bounded || p->bounds[i] > 0.0;
+    while (st == XR_OK) {
+      if ((st = xr_cmaes_sample_population(es, pop.data())) != XR_OK) break;
+      // redraw candidates outside [-b, b] (xregIntensity2D3DRegiCMAES.cpp:162-191)
+      for (int32_t k = 0; bounded && k < p->lambda && st == XR_OK; ++k) {
+        for (int tries = 0;; ++tries) {
+          bool inside = true;
+          for (int i = 0; i < 6; ++i)
+            if (p->bounds[i] > 0.0 && std::fabs(pop[(size_t)k * 6 + i]) > p->bounds[i]) inside = false;
+          if (inside) break;
+          if (tries > 100000) {
+            st = fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: could not sample a candidate inside the bounds");
+            break;
+          }
+          if ((st = xr_cmaes_resample_single(es, k, pop.data())) != XR_OK) break;
+        }
+      }
+      if (st != XR_OK) break;
+      if ((st = eval(pop.data(), p->lambda)) != XR_OK) break;
+      if ((st = xr_cmaes_update_distribution(es, f.data())) != XR_OK) break;
+      if ((st = xr_cmaes_test_termination(es, &reason)) != XR_OK) break;
+      if (reason != 0) break;
+    }
+    if (st == XR_OK) st = xr_cmaes_get(es, nullptr, bx, &bf, nullptr, &iters);
+    xr_cmaes_destroy(es);
+  } else if (p->optimizer == XR_REGI_DFO) {
+    double lo[6], hi[6];
+    for (int i = 0; i < 6; ++i) {
+      if (!(p->bounds[i] > 0.0)) return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: the trust-region level needs bounds");
+      lo[i] = -p->bounds[i];
+      hi[i] = p->bounds[i];
+    }
+    xr_dfo d = nullptr;
+    if ((st = xr_dfo_create(6, zero, lo, hi, p->rho_beg, p->rho_end, p->max_iters, &d)) != XR_OK) return st;
+    pop.resize((size_t)(2 * 6 + 2) * 6);
+    while (st == XR_OK) {
+      int32_t n = 0;
+      if ((st = xr_dfo_ask(d, pop.data(), &n)) != XR_OK) break;
+      if ((st = eval(pop.data(), n)) != XR_OK) break;
+      if ((st = xr_dfo_tell(d, f.data())) != XR_OK) break;
+      if ((st = xr_dfo_test_termination(d, &reason)) != XR_OK) break;
+      if (reason != 0) break;
+    }
+    if (st == XR_OK) st = xr_dfo_get(d, bx, &bf, nullptr, &iters);
+    xr_dfo_destroy(d);
+  } else {
+    return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: unknown optimizer");
+  }
+  if (st != XR_OK) return st;
+  if (!finite6(bx)) return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: the optimizer returned a non-finite offset");
+  map(bx, best_pose);
+  if (best_value) *best_value = bf;
+  if (iterations) *iterations = iters;
+  if (stop_reason) *stop_reason = reason;
+  return XR_OK;
+}

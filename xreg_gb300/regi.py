@@ -211,6 +211,37 @@ class Registration:
         return self.final_pose
 
 
+def run_level_native(obj: api.PopulationObjective, centre: np.ndarray, start_pose: np.ndarray,
+                     level: RegiLevel, seed: int = 0) -> LevelResult:
+    """One level run entirely in the library (xr_regi_run_level): the same loop as
+    Registration's propose / tell for that level, without Python in between."""
+    import ctypes as C
+    from . import _lib as L
+    opt = L.XR_REGI_DFO if level.optimizer == "dfo" else L.XR_REGI_CMAES
+    p = L.xr_regi_level_params()
+    L.call("xr_regi_level_params_default", opt, C.byref(p))
+    if opt == L.XR_REGI_CMAES:
+        p.lambda_ = int(level.pop)
+        for i in range(6):
+            p.sigma[i] = float(level.sigma[i])
+            p.bounds[i] = 0.0 if level.bounds is None else float(level.bounds[i])
+        p.tol_fun, p.tol_x = float(level.tol_fun), float(level.tol_x)
+    else:
+        b = DFO_BOUNDS if level.bounds is None else np.asarray(level.bounds, dtype=np.float64)
+        for i in range(6):
+            p.bounds[i] = float(b[i])
+        p.rho_beg, p.rho_end = float(level.rho_beg), float(level.rho_end)
+    p.max_iters = int(level.max_iters)
+    p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    c = np.ascontiguousarray(centre, dtype=np.float64)
+    s = np.ascontiguousarray(start_pose, dtype=np.float64)
+    out = np.zeros((4, 4))
+    bf, it, why = C.c_double(), C.c_int64(), C.c_int32()
+    L.call("xr_regi_run_level", obj.handle, c.ctypes.data_as(C.c_void_p), s.ctypes.data_as(C.c_void_p), C.byref(p),
+           out.ctypes.data_as(C.c_void_p), C.byref(bf), C.byref(it), C.byref(why))
+    return LevelResult(out, None, bf.value, it.value, why.value)
+
+
 def pose_error(a: np.ndarray, b: np.ndarray, vol: api.Volume) -> tuple:
     """Difference of two cam -> ITK physical poses as (rotation angle in degrees,
     displacement in mm of the volume centre in camera coordinates)."""
