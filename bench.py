@@ -344,8 +344,10 @@ def run_ours(a, rank, world, local):
                      "alg_bytes_per_launch": alg_bytes, "samples_per_launch": samples,
                      "kernel_ms": round(drr_ms, 4),
                      "l2": l2,
-                     "note": "algorithmic bytes count 8 neighbour reads per trilinear sample; they are served "
-                             "mostly from L1/L2, so frac compares gather throughput with the HBM copy peak"},
+                     "note": "algorithmic bytes = 8 neighbour reads x voxel bytes x every sample of the "
+                             "reference step rule; frac > 1 because those reads hit L1/L2 (HBM carries "
+                             "`traffic`, under 1 % of them) and samples proven zero are not loaded; the kernel "
+                             "is instruction-issue bound (see profiles/)"},
         "clocks": clk.summary(),
     }
     if rank == 0:
