@@ -268,7 +268,9 @@ typedef struct {
   int32_t use_mov_img_patch_variances_as_wgts;   /* [0] */
   int32_t use_variances_in_grad_imgs_as_wgts;    /* [0] patch grad-NCC: variances of the gradient images */
   int32_t choose_rand_patches;                   /* [0] */
-  int32_t reserved;
+  int32_t mask_only_for_weights;                 /* [0] 1 = the OpenCL metric's rule
+                                                    (xregImgSimMetric2DPatchNCCOCL.cpp:240): the mask
+                                                    weights patches but every pixel enters the sums */
   int64_t num_rand_patches;                      /* [100] */
   double rand_patch_min_pixels_sep;              /* [-1] = sqrt(2) radius; 0 = no check */
   uint64_t rand_seed;

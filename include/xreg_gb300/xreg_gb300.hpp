@@ -183,6 +183,8 @@ class ImgSimMetric2DPatchCUDA : public ImgSimMetric2DCUDA {
     set([&](xr_patch_options& o) { o.weight_patch_sims_in_combine = v; });
   }
   void set_compute_mean_of_patch_sims(bool v) { set([&](xr_patch_options& o) { o.compute_mean_of_patch_sims = v; }); }
+  // the OpenCL patch metrics' rule: the mask only weights the patches
+  void set_mask_only_for_weights(bool v) { set([&](xr_patch_options& o) { o.mask_only_for_weights = v; }); }
   void set_use_fixed_img_patch_variances_as_wgts(bool v) {
     set([&](xr_patch_options& o) { o.use_fixed_img_patch_variances_as_wgts = v; });
   }

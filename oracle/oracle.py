@@ -228,11 +228,11 @@ class patch_opts(C.Structure):
                 ("normalize_weights_as_prob", C.c_int), ("weight_patch_sims_in_combine", C.c_int),
                 ("compute_mean_of_patch_sims", C.c_int), ("use_fixed_var_wgts", C.c_int),
                 ("use_mov_var_wgts", C.c_int), ("use_grad_var_wgts", C.c_int),
-                ("wgt_img", C.c_void_p), ("patch_count", C.c_void_p)]
+                ("wgt_img", C.c_void_p), ("patch_count", C.c_void_p), ("mask_only_for_weights", C.c_int)]
 
 
 def _patch_opts(opts, shape, keep):
-    o = patch_opts(1, 0, 1, 1, 0, 0, 0, 0, None, None)
+    o = patch_opts(1, 0, 1, 1, 0, 0, 0, 0, None, None, 0)
     for k, v in (opts or {}).items():
         if k == "wgt_img":
             a = np.ascontiguousarray(v, dtype=np.float32).reshape(shape)

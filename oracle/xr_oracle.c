@@ -828,6 +828,7 @@ typedef struct {
   int use_grad_var_wgts;           /* patch grad-NCC: variances of the gradient images */
   const float* wgt_img;            /* weight image (rows x cols) or NULL */
   const int32_t* patch_count;      /* times each patch is used (npatch) or NULL = every patch once */
+  int mask_only_for_weights;       /* the OpenCL metric: every pixel enters the correlation sums */
 } xo_patch_opts;
 
 /* ComputePatchMeanStdDev (xregImgSimMetric2DPatchNCCCPU.cpp:558-619): pixels with
@@ -994,7 +995,8 @@ static double xo_pncc_eval(const xo_pncc* P, const double* m, const double* mvar
       for (int64_t r = 0; r < P->diam; ++r)
         for (int64_t c = 0; c < P->diam; ++c) {
           const int64_t i = (cr - P->radius + r) * P->cols + cc - P->radius + c;
-          if (!P->mask || P->mask[i]) acc += ((m[i] - mu) / sd) * P->fhat[p * dd + r * P->diam + c];
+          if (!P->mask || P->o.mask_only_for_weights || P->mask[i])
+            acc += ((m[i] - mu) / sd) * P->fhat[p * dd + r * P->diam + c];
         }
       val = (P->o.weight_patch_sims_in_combine ? wgt : 1.0) * (1.0 - acc);
     }

@@ -51,6 +51,7 @@ CASES = [
     dict(use_fixed_img_patch_variances_as_wgts=1),
     dict(use_mov_img_patch_variances_as_wgts=1),
     dict(use_mov_img_patch_variances_as_wgts=1, normalize_weights_as_prob=0),
+    dict(mask_only_for_weights=1),
 ]
 
 ORACLE_KEYS = {"use_fixed_img_patch_variances_as_wgts": "use_fixed_var_wgts",

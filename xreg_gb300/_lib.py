@@ -46,7 +46,7 @@ class xr_patch_options(C.Structure):
                 ("compute_mean_of_patch_sims", C.c_int32), ("use_fixed_img_patch_variances_as_wgts", C.c_int32),
                 ("use_mov_img_patch_variances_as_wgts", C.c_int32),
                 ("use_variances_in_grad_imgs_as_wgts", C.c_int32), ("choose_rand_patches", C.c_int32),
-                ("reserved", C.c_int32), ("num_rand_patches", C.c_int64), ("rand_patch_min_pixels_sep", C.c_double),
+                ("mask_only_for_weights", C.c_int32), ("num_rand_patches", C.c_int64), ("rand_patch_min_pixels_sep", C.c_double),
                 ("rand_seed", C.c_uint64)]
 
 

@@ -415,19 +415,19 @@ class _PatchParams:
     def patch_options(self) -> dict:
         o = L.xr_patch_options()
         call("xr_sm_get_patch_options", self._h, C.byref(o))
-        return {k: getattr(o, k) for k, _ in L.xr_patch_options._fields_ if k != "reserved"}
+        return {k: getattr(o, k) for k, _ in L.xr_patch_options._fields_}
 
     def set_patch_options(self, **kw) -> None:
         """ImgSimMetric2DPatchCommon / PatchNCC / PatchGradNCC setters by name
         (use_mask_for_weighting, use_mask_for_patch_stats, normalize_weights_as_prob,
         weight_patch_sims_in_combine, compute_mean_of_patch_sims,
         use_fixed_img_patch_variances_as_wgts, use_mov_img_patch_variances_as_wgts,
-        use_variances_in_grad_imgs_as_wgts, choose_rand_patches, num_rand_patches,
-        rand_patch_min_pixels_sep, rand_seed); unnamed ones keep their values."""
+        use_variances_in_grad_imgs_as_wgts, choose_rand_patches, mask_only_for_weights,
+        num_rand_patches, rand_patch_min_pixels_sep, rand_seed); unnamed ones keep their values."""
         o = L.xr_patch_options()
         call("xr_sm_get_patch_options", self._h, C.byref(o))
         for k, v in kw.items():
-            if k not in dict(L.xr_patch_options._fields_) or k == "reserved":
+            if k not in dict(L.xr_patch_options._fields_):
                 raise TypeError(f"unknown patch option {k!r}")
             setattr(o, k, type(getattr(o, k))(v) if not isinstance(getattr(o, k), float) else float(v))
         call("xr_sm_set_patch_options", self._h, C.byref(o))

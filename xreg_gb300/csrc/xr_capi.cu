@@ -1226,6 +1226,8 @@ extern "C" XR_API xr_status xr_sm_set_patch_options(xr_simmetric sm, const xr_pa
                "set_patch_options: fixed and moving patch variances cannot both be the weights");
   XR_CHECK_ARG(!o->choose_rand_patches || o->num_rand_patches > 0,
                "set_patch_options: num_rand_patches must be positive");
+  XR_CHECK_ARG(!(o->mask_only_for_weights && o->use_mask_for_patch_stats),
+               "set_patch_options: masked statistics need the mask inside the patches");
   sm->popt = *o;
   sm->rng.seed((std::mt19937::result_type)o->rand_seed);
   sm->allocated = false;
@@ -1579,7 +1581,8 @@ static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
                     sm->d_pscale_x.as<float>(), sm->has_pw ? sm->d_pw_x.as<float>() : nullptr};
       PatchFixed py{sm->d_gy.as<float>(), sm->d_pmean_y.as<float>(), sm->d_pscale_y.as<float>(),
                     sm->has_pw ? sm->d_pw_y.as<float>() : nullptr};
-      PatchRun run{mask, nullptr, o.use_mask_for_patch_stats ? 1 : 0, o.weight_patch_sims_in_combine ? 1 : 0,
+      PatchRun run{mask, nullptr, o.use_mask_for_patch_stats ? 1 : 0, o.mask_only_for_weights ? 0 : 1,
+                   o.weight_patch_sims_in_combine ? 1 : 0,
                    sm->mvar_mode, o.normalize_weights_as_prob ? 1 : 0,
                    sm->mvar_mode ? sm->d_mvar_sum.as<double>() : nullptr};
       if (o.choose_rand_patches) {

@@ -122,6 +122,7 @@ struct PatchRun {           // per compute
   const uint8_t* mask;      // image mask or nullptr
   const int32_t* cnt;       // times each patch is used, nullptr = once
   int use_mask_stats;       // statistics over masked-in pixels only
+  int mask_in_sums;         // correlation sums over masked-in pixels only
   int weighted;             // weight_patch_sims_in_combine
   int mvar;                 // moving-variance weights: 0 none, 1 of the image, 2 of each gradient image
   int normalize;            // normalise moving variances by their sum

@@ -375,7 +375,7 @@ struct PatchLayout {
 // unmasked case is the plain patch NCC.  *var = sd_m^2.
 __device__ __forceinline__ float patch_score(const float* __restrict__ m, const float* __restrict__ f,
                                              const uint8_t* __restrict__ mk, int W, int r0, int c0, int d,
-                                             float fmean, float fscale, int use_mask_stats) {
+                                             float fmean, float fscale, int use_mask_stats, int mask_in_sums) {
   float s = 0.0f;
   int n = 0;
   for (int r = 0; r < d; ++r)
@@ -388,7 +388,7 @@ __device__ __forceinline__ float patch_score(const float* __restrict__ m, const 
       const int i = (r0 + r) * W + c0 + c;
       const float dm = m[i] - mu;
       if (!use_mask_stats || !mk || mk[i]) v = fmaf(dm, dm, v);
-      if (!mk || mk[i]) cov = fmaf(dm, f[i] - fmean, cov);
+      if (!mk || !mask_in_sums || mk[i]) cov = fmaf(dm, f[i] - fmean, cov);
     }
   float sd = n > 1 ? sqrtf(v / (float)(n - 1)) : 0.0f;
   sd = fmaxf(sd, 1.0e-6f);
@@ -538,12 +538,12 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
         }
         if (!run.weighted || fabsf(w[0]) > 1.0e-6f) {
           const float sc = patch_score(s_mx, s_fx, mk, W, r0, c0, d, px.mean[pidx], px.scale[pidx],
-                                       run.use_mask_stats);
+                                       run.use_mask_stats, run.mask_in_sums);
           v[0] = (double)cnt * (double)((run.weighted ? w[0] : 1.0f) * sc);
         }
         if (GRAD && (!run.weighted || fabsf(w[1]) > 1.0e-6f)) {
           const float sc = patch_score(s_my, s_fy, mk, W, r0, c0, d, py.mean[pidx], py.scale[pidx],
-                                       run.use_mask_stats);
+                                       run.use_mask_stats, run.mask_in_sums);
           v[1] = (double)cnt * (double)((run.weighted ? w[1] : 1.0f) * sc);
         }
       }
