@@ -54,8 +54,9 @@ def _args():
     p.add_argument("--serving-requests", type=int, default=10, help="requests in the serving measurement (0 = off)")
     p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving measurement")
     p.add_argument("--launch-config", default="auto",
-                   help="DRR kernel configuration 'layout,block_warps_x,unroll' (layout 0 linear, 1 cell8) "
-                        "instead of the autotuner's choice")
+                   help="DRR kernel configuration 'layout,block_warps_x,unroll[,warp_rows]' (layout 0 linear, "
+                        "1 cell8, 2 cell8 256-bit; warp_rows 4 = 8x4-pixel warps, 8 = 4x8) instead of the "
+                        "autotuner's choice")
     return p.parse_args()
 
 
@@ -284,8 +285,11 @@ def run_ours(a, rank, world, local):
     rc.distribute_xforms_device(POP, d_pops[a.warmup].data_ptr())
     rc.compute()
     samples = rc.last_num_samples()
-    layout, bw, unroll = rc.launch_config()
+    layout, bw, unroll, wrows = rc.launch_config_ex()
     lname = {0: "linear", 1: "cell8", 2: "cell8-256bit"}.get(layout, str(layout))
+    wcols = 32 // wrows
+    wshape = "" if wrows == 4 else f"-warp{wcols}x{wrows}"
+    block = f"{wcols * bw}x{(8 // bw) * wrows}"
     rc.set_count_samples(False)
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
     with torch.cuda.stream(stream):
@@ -301,7 +305,7 @@ def run_ours(a, rank, world, local):
     alg_bytes = 8.0 * bvox * samples
     achieved = alg_bytes / (drr_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
-    tag = f"batched-256^3-384^2-pop100-{a.voxel}-{lname}-loop{unroll}"
+    tag = f"batched-256^3-384^2-pop100-{a.voxel}-{lname}-loop{unroll}{wshape}"
     traffic = _ncu_traffic(tag)
     l2_bytes = _ncu_traffic(tag, "l2_bytes_per_launch")
     l2_peak = _ncu_traffic("", "l2_sector_peak_gbs")
@@ -338,7 +342,7 @@ def run_ours(a, rank, world, local):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": None if traffic is None else traffic,
-                     "kernel": f"drr_kernel<{a.voxel},sum,{lname},unroll{unroll}> block {8 * bw}x{32 // bw}",
+                     "kernel": f"drr_kernel<{a.voxel},sum,{lname},unroll{unroll}> block {block}, warps {wcols}x{wrows}",
                      "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
                      "alg_bytes_per_launch": alg_bytes, "samples_per_launch": samples,

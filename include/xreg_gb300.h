@@ -193,6 +193,13 @@ XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
 XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t layout, int32_t block_warps_x, int32_t unroll);
 /* The configuration the last compute used. */
 XR_API xr_status xr_rc_get_launch_config(xr_raycaster rc, int32_t* layout, int32_t* block_warps_x, int32_t* unroll);
+/* As xr_rc_set_launch_config with the warp shape too: warp_rows 4 = each warp
+ * covers 8x4 pixels (what xr_rc_set_launch_config sets), 8 = 4x8.  The
+ * autotuner also times 4x8 warps for its fastest layout and loop. */
+XR_API xr_status xr_rc_set_launch_config_ex(xr_raycaster rc, int32_t layout, int32_t block_warps_x, int32_t unroll,
+                                            int32_t warp_rows);
+XR_API xr_status xr_rc_get_launch_config_ex(xr_raycaster rc, int32_t* layout, int32_t* block_warps_x,
+                                            int32_t* unroll, int32_t* warp_rows);
 /* Whether set_volumes also builds the CELL8 copy (default 1).  Set before set_volumes. */
 XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable);
 /* Empty-space skipping for the line-integral sum (default 1): samples whose

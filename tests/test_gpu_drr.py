@@ -224,17 +224,19 @@ def test_launch_configs_are_bit_identical(xr, oracle, vt):
     rc.distribute_xforms_among_cam_models(poses)
     rc.compute()
     auto = rc.projs()
-    lay, bw, un = rc.launch_config()
-    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2, 3, 4, 5)
+    lay, bw, un, wr = rc.launch_config_ex()
+    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2, 3, 4, 5) and wr in (4, 8)
     # layout 2: the float32 cell copy read with one 256-bit load per sample;
-    # loops 3 / 4: two / four samples per iteration after the macro-cell trim
+    # loops 3 / 4: two / four samples per iteration after the macro-cell trim;
+    # warps of 8x4 or 4x8 pixels
     for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
         for bw in (1, 2, 4, 8):
             for un in (1, 2, 3, 4, 5):
-                rc.set_launch_config(layout, bw, un)
-                rc.compute()
-                assert rc.launch_config() == (layout, bw, un)
-                np.testing.assert_array_equal(rc.projs(), auto)
+                for wr in (4, 8):
+                    rc.set_launch_config(layout, bw, un, wr)
+                    rc.compute()
+                    assert rc.launch_config_ex() == (layout, bw, un, wr)
+                    np.testing.assert_array_equal(rc.projs(), auto)
     o = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]), poses, step=0.5)
     rel, zero = drr_rel_err(auto, o)
     assert zero == 0.0 and rel <= (TOL32 if vt == 0 else (TOL16 if vt == 1 else TOLBF16))

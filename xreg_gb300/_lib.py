@@ -106,6 +106,8 @@ _SIGS = {
     "xr_rc_set_count_samples": [H, i32],
     "xr_rc_set_launch_config": [H, i32, i32, i32],
     "xr_rc_get_launch_config": [H, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],
+    "xr_rc_set_launch_config_ex": [H, i32, i32, i32, i32],
+    "xr_rc_get_launch_config_ex": [H, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],
     "xr_rc_set_build_cell_layout": [H, i32],
     "xr_rc_set_empty_space_skipping": [H, i32],
     "xr_sm_create": [i32, i32, C.POINTER(H)],

@@ -256,13 +256,20 @@ class RayCasterLineIntCUDA:
     def set_count_samples(self, enable: bool) -> None:
         call("xr_rc_set_count_samples", self._h, int(bool(enable)))
 
-    def set_launch_config(self, layout: int = L.XR_LAYOUT_AUTO, block_warps_x: int = 2, unroll: int = 1) -> None:
-        call("xr_rc_set_launch_config", self._h, int(layout), int(block_warps_x), int(unroll))
+    def set_launch_config(self, layout: int = L.XR_LAYOUT_AUTO, block_warps_x: int = 2, unroll: int = 1,
+                          warp_rows: int = 4) -> None:
+        """DRR launch configuration; warp_rows 4 = 8x4-pixel warps, 8 = 4x8."""
+        call("xr_rc_set_launch_config_ex", self._h, int(layout), int(block_warps_x), int(unroll), int(warp_rows))
 
     def launch_config(self) -> tuple:
-        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
-        call("xr_rc_get_launch_config", self._h, C.byref(a), C.byref(b), C.byref(c))
-        return (a.value, b.value, c.value)
+        """(layout, block_warps_x, unroll) of the last compute."""
+        return self.launch_config_ex()[:3]
+
+    def launch_config_ex(self) -> tuple:
+        """(layout, block_warps_x, unroll, warp_rows) of the last compute."""
+        a, b, c, d = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        call("xr_rc_get_launch_config_ex", self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d))
+        return (a.value, b.value, c.value, d.value)
 
     def set_build_cell_layout(self, enable: bool) -> None:
         call("xr_rc_set_build_cell_layout", self._h, int(bool(enable)))

@@ -159,8 +159,8 @@ struct xr_raycaster_s {
   };
   bool skip_empty = true;
   bool build_cells = true;
-  int32_t cfg_layout = XR_LAYOUT_AUTO, cfg_bw = 2, cfg_unroll = 1;   // requested
-  int32_t last_layout = -1, last_bw = 0, last_unroll = 0;            // used by the last compute
+  int32_t cfg_layout = XR_LAYOUT_AUTO, cfg_bw = 2, cfg_unroll = 1, cfg_warp_rows = 4;  // requested
+  int32_t last_layout = -1, last_bw = 0, last_unroll = 0, last_warp_rows = 0;          // used by the last compute
   std::vector<std::unique_ptr<Vol>> vols;
   std::vector<xr_camera_desc> cams;
   DevBuf d_cams;
@@ -706,7 +706,7 @@ struct TuneKeyHash {
   }
 };
 struct TuneCfg {
-  int32_t layout, bw, unroll;
+  int32_t layout, bw, unroll, tall;
   float ms;
 };
 std::mutex g_tune_mu;
@@ -737,7 +737,7 @@ xr_status time_config(DrrParams p, cudaStream_t s, float* ms_out) {
 }
 }  // namespace
 
-// Picks the launch configuration for p (layout, block_warps_x, unroll).
+// Picks the launch configuration for p (layout, block_warps_x, unroll, warp shape).
 static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vol, DrrParams& p, cudaStream_t s) {
   const bool has_cells = vol.cells.p != nullptr;
   if (rc->cfg_layout != XR_LAYOUT_AUTO) {
@@ -748,6 +748,7 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
     p.vol.layout = rc->cfg_layout;
     p.block_warps_x = rc->cfg_bw;
     p.unroll = rc->cfg_unroll;
+    p.warp_tall = rc->cfg_warp_rows == 8 ? 1 : 0;
     return XR_OK;
   }
   const TuneKey key{vol.desc.n[0], vol.desc.n[1], vol.desc.n[2], rc->rows(), rc->cols(), pow2_bucket(p.num_projs),
@@ -759,6 +760,7 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
       p.vol.layout = it->second.layout;
       p.block_warps_x = it->second.bw;
       p.unroll = it->second.unroll;
+      p.warp_tall = it->second.tall;
       return XR_OK;
     }
   }
@@ -766,6 +768,7 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   p.vol.layout = has_cells ? XR_LAYOUT_CELL8 : XR_LAYOUT_LINEAR;
   p.block_warps_x = 2;
   p.unroll = 1;
+  p.warp_tall = 0;
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   XR_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
   // Tuning re-runs the kernel; it needs a stream that is not being captured and an
@@ -773,7 +776,7 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   if (cap != cudaStreamCaptureStatusNone || p.store != XR_PROJ_STORE_REPLACE || p.bg_projs) return XR_OK;
   DrrParams t = p;
   t.sample_counter = nullptr;
-  TuneCfg best{p.vol.layout, p.block_warps_x, p.unroll, 1e30f};
+  TuneCfg best{p.vol.layout, p.block_warps_x, p.unroll, 0, 1e30f};
   // layout 2 = CELL8 read with one 256-bit load per sample (float32 only)
   const int32_t layouts[3] = {XR_LAYOUT_LINEAR, XR_LAYOUT_CELL8, 2};
   const int32_t bws[3] = {1, 2, 4};
@@ -791,11 +794,27 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
         t.vol.layout = lay;
         t.block_warps_x = bw;
         t.unroll = un;
+        t.warp_tall = 0;
         float ms = 0.0f;
         xr_status st = time_config(t, s, &ms);
         if (st != XR_OK) return st;
-        if (ms < best.ms) best = TuneCfg{lay, bw, un, ms};
+        if (ms < best.ms) best = TuneCfg{lay, bw, un, 0, ms};
       }
+  }
+  // 4x8-pixel warps for the fastest layout and loop (rays of a warp span more
+  // detector rows, which changes how their cells share L1 lines)
+  {
+    const TuneCfg wide = best;
+    for (int32_t bw : bws) {
+      t.vol.layout = wide.layout;
+      t.block_warps_x = bw;
+      t.unroll = wide.unroll;
+      t.warp_tall = 1;
+      float ms = 0.0f;
+      xr_status st = time_config(t, s, &ms);
+      if (st != XR_OK) return st;
+      if (ms < best.ms) best = TuneCfg{wide.layout, bw, wide.unroll, 1, ms};
+    }
   }
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -804,6 +823,7 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   p.vol.layout = best.layout;
   p.block_warps_x = best.bw;
   p.unroll = best.unroll;
+  p.warp_tall = best.tall;
   return XR_OK;
 }
 
@@ -912,6 +932,7 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
   rc->last_layout = p.vol.layout;
   rc->last_bw = p.block_warps_x;
   rc->last_unroll = p.unroll;
+  rc->last_warp_rows = p.warp_tall ? 8 : 4;
   XR_CUDA_TRY(launch_drr(p, s));
   if (rc->ext_host)
     XR_CUDA_TRY(cudaMemcpyAsync(rc->ext_host, p.out, (size_t)p.num_projs * (size_t)(rc->rows() * rc->cols()) * 4,
@@ -920,7 +941,14 @@ static xr_status rc_enqueue_compute(xr_raycaster rc, int32_t vol_idx) {
 }
 
 extern "C" XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t layout, int32_t bw, int32_t unroll) {
+  return xr_rc_set_launch_config_ex(rc, layout, bw, unroll, 4);
+}
+
+extern "C" XR_API xr_status xr_rc_set_launch_config_ex(xr_raycaster rc, int32_t layout, int32_t bw, int32_t unroll,
+                                                      int32_t warp_rows) {
   XR_CHECK_ARG(rc, "set_launch_config: NULL handle");
+  XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || warp_rows == 4 || warp_rows == 8,
+               "set_launch_config: warp_rows must be 4 (8x4-pixel warps) or 8 (4x8)");
   XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= 2, "set_launch_config: bad layout");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || bw == 1 || bw == 2 || bw == 4 || bw == 8,
                "set_launch_config: block_warps_x must be 1, 2, 4 or 8");
@@ -929,6 +957,7 @@ extern "C" XR_API xr_status xr_rc_set_launch_config(xr_raycaster rc, int32_t lay
   rc->cfg_layout = layout;
   rc->cfg_bw = bw;
   rc->cfg_unroll = unroll;
+  rc->cfg_warp_rows = warp_rows;
   rc->generation++;
   return XR_OK;
 }
@@ -938,6 +967,16 @@ extern "C" XR_API xr_status xr_rc_get_launch_config(xr_raycaster rc, int32_t* la
   *layout = rc->last_layout;
   *bw = rc->last_bw;
   *unroll = rc->last_unroll;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_get_launch_config_ex(xr_raycaster rc, int32_t* layout, int32_t* bw, int32_t* unroll,
+                                                      int32_t* warp_rows) {
+  XR_CHECK_ARG(rc && layout && bw && unroll && warp_rows, "get_launch_config: NULL argument");
+  *layout = rc->last_layout;
+  *bw = rc->last_bw;
+  *unroll = rc->last_unroll;
+  *warp_rows = rc->last_warp_rows;
   return XR_OK;
 }
 
@@ -1898,6 +1937,7 @@ static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* obj
     rc->last_layout = J.p.vol.layout;
     rc->last_bw = 2;
     rc->last_unroll = kJobSetLoop;
+    rc->last_warp_rows = 4;
     js->h_jobs.push_back(J);
     group.push_back(vol.type * 4 + J.p.vol.layout);
   }

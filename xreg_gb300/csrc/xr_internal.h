@@ -65,8 +65,9 @@ struct DrrParams {
   float default_bg;
   int32_t kernel_id;      // XR_LINE_INT_SUM / MAX
   int32_t store;          // XR_PROJ_STORE_REPLACE / ACCUM
-  int32_t block_warps_x;  // warps across a block (1, 2, 4, 8); 8x4-pixel warps
-  int32_t unroll;         // samples per loop iteration (1 or 2); 3 = 2 after the macro-cell trim
+  int32_t block_warps_x;  // warps across a block (1, 2, 4, 8)
+  int32_t warp_tall;      // 0: each warp covers 8x4 pixels (cols x rows); 1: 4x8
+  int32_t unroll;         // sample loop 1..5 (xr_rc_set_launch_config)
 };
 
 // ---- launchers (xr_geom.cu) ----

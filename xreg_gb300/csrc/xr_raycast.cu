@@ -489,14 +489,16 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 __global__ void __launch_bounds__(kThreads, UNROLL == kUnrollTrim4 ? kMinBlocksPerSM - 1 : kMinBlocksPerSM)
 drr_kernel(const DrrParams p, const int64_t proj_base) {
-  // Each warp covers an 8 x 4 patch of pixels so its 32 rays stay close inside
-  // the volume; a block is bw x (8 / bw) warps.  The projection is the fastest
-  // grid index: blocks resident at the same time trace the same detector tile
-  // for many nearby poses, whose footprints overlap in L2.
+  // Each warp covers an 8 x 4 (or, tall, 4 x 8) patch of pixels so its 32 rays
+  // stay close inside the volume; a block is bw x (8 / bw) warps.  The
+  // projection is the fastest grid index: blocks resident at the same time trace
+  // the same detector tile for many nearby poses, whose footprints overlap in L2.
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int bw = p.block_warps_x;
-  const int col = blockIdx.y * (8 * bw) + (warp % bw) * 8 + (lane & 7);
-  const int row = blockIdx.z * (32 / bw) + (warp / bw) * 4 + (lane >> 3);
+  const int wl = p.warp_tall ? 2 : 3;  // log2 of the warp's width in pixels
+  const int wc = 1 << wl, wr = 32 >> wl;
+  const int col = blockIdx.y * (wc * bw) + (warp % bw) * wc + (lane & (wc - 1));
+  const int row = blockIdx.z * ((8 / bw) * wr) + (warp / bw) * wr + (lane >> wl);
   const int64_t proj = proj_base + blockIdx.x;
   unsigned long long ns = 0;
   if (col < p.cols && row < p.rows) ns = trace_pixel<VT, KERNEL, LAYOUT, UNROLL>(p, proj, row, col);
@@ -582,7 +584,8 @@ cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
     carveout_set = true;
   }
   const int bw = p.block_warps_x;
-  const int tx = 8 * bw, ty = 32 / bw;
+  const int wc = p.warp_tall ? 4 : 8;
+  const int tx = wc * bw, ty = (8 / bw) * (32 / wc);
   const int64_t max_x = 0x7fffffff;
   for (int64_t base = 0; base < p.num_projs; base += max_x) {
     const int64_t n = (p.num_projs - base) < max_x ? (p.num_projs - base) : max_x;
@@ -662,6 +665,7 @@ cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
   if (p.num_projs <= 0) return cudaSuccess;
   if (!(p.block_warps_x == 1 || p.block_warps_x == 2 || p.block_warps_x == 4 || p.block_warps_x == 8))
     return cudaErrorInvalidValue;
+  if (p.warp_tall != 0 && p.warp_tall != 1) return cudaErrorInvalidValue;
   if (p.vol.layout != XR_LAYOUT_LINEAR && !p.vol.cells) return cudaErrorInvalidValue;
   if (p.vol.layout == kLayoutCell8Wide && p.vol.voxel_type != XR_VOXEL_F32) return cudaErrorInvalidValue;
   switch (p.vol.voxel_type) {
