@@ -113,10 +113,29 @@ constexpr int kUnrollPairShare = 5;  // loop 3 whose second sample of a pair reu
 // rule of sample() below).  INSIDE: the caller has shown that the position lies
 // in [0, n-1) on every axis, where the clamps and the saturation change
 // nothing, so they are left out (same cell, same fractions).
-template <bool INSIDE = false>
+// ADD_FLOOR (inside only): floor(p) comes from one round-down addition: for
+// 0 <= p < 2^23 the floats in [2^23, 2^24) are the integers, so p + 2^23
+// rounded down is exactly 2^23 + floor(p), whose bit pattern is
+// 0x4B000000 + floor(p).  No conversion instructions (the cell index is formed
+// from the biased integers and the bias removed once, in wrapping 32-bit
+// arithmetic), but two more FMA-pipe additions per axis: faster for float32
+// cells, slower for half cells whose conversions already load that pipe.
+template <bool INSIDE = false, bool ADD_FLOOR = false>
 __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, float pz, float& fx, float& fy,
                                        float& fz) {
   const int nx = vol.nx, ny = vol.ny;
+  if (INSIDE && ADD_FLOOR) {
+    constexpr float kTwo23 = 8388608.0f;
+    const float tx = __fadd_rd(px, kTwo23), ty = __fadd_rd(py, kTwo23), tz = __fadd_rd(pz, kTwo23);
+    fx = __fsub_rn(px, __fsub_rn(tx, kTwo23));
+    fy = __fsub_rn(py, __fsub_rn(ty, kTwo23));
+    fz = __fsub_rn(pz, __fsub_rn(tz, kTwo23));
+    const unsigned int ux = (unsigned int)(nx - 1), uy = (unsigned int)(ny - 1), kb = 0x4B000000u;
+    const unsigned int bias = kb * (uy * ux + ux + 1u);
+    const unsigned int bx = (unsigned int)__float_as_int(tx), by = (unsigned int)__float_as_int(ty),
+                       bz = (unsigned int)__float_as_int(tz);
+    return (int)((bz * uy + by) * ux + bx - bias);
+  }
   int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
   if (INSIDE) {
     fx = px - (float)ix;
@@ -158,10 +177,10 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
   // fraction 1, and a NaN position reads cell 0 with fraction 0.
   float v[8], fx, fy, fz;
   if (LAYOUT == kLayoutCell8Wide) {
-    const int c = cell_of<INSIDE>(vol, px, py, pz, fx, fy, fz);
+    const int c = cell_of<INSIDE, true>(vol, px, py, pz, fx, fy, fz);
     if constexpr (VT == XR_VOXEL_F32) Vox<VT>::cell_wide(data, c, v);
   } else if (LAYOUT == XR_LAYOUT_CELL8) {
-    const int c = cell_of<INSIDE>(vol, px, py, pz, fx, fy, fz);
+    const int c = cell_of<INSIDE, VT == XR_VOXEL_F32>(vol, px, py, pz, fx, fy, fz);
     Vox<VT>::cell(data, c, v);
   } else {
     const int nx = vol.nx, ny = vol.ny;
@@ -238,7 +257,8 @@ __device__ __forceinline__ float macro_march(const VolView& v, const float p0[3]
     if (ax < 0) return dir > 0 ? INFINITY : -INFINITY;  // stays in this empty macro cell
     if (dir > 0 ? (knext > kend) : (knext < kend)) return dir > 0 ? INFINITY : -INFINITY;
     if (dir > 0 ? (knext > k) : (knext < k)) k = knext;
-    m[ax] += dm;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) m[a] += (a == ax) ? dm : 0;  // static indices: m stays in registers
   }
   return k;  // walk limit: treat the rest as occupied
 }
@@ -276,9 +296,9 @@ __device__ __forceinline__ float march_samples(const DrrParams& p, const void* d
     // makes no memory request) and the first sample's corners are reused.
     for (; n >= 2; n -= 2) {
       float f0x, f0y, f0z, f1x, f1y, f1z;
-      const int c0 = cell_of<INSIDE>(p.vol, px, py, pz, f0x, f0y, f0z);
+      const int c0 = cell_of<INSIDE, true>(p.vol, px, py, pz, f0x, f0y, f0z);
       px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-      const int c1 = cell_of<INSIDE>(p.vol, px, py, pz, f1x, f1y, f1z);
+      const int c1 = cell_of<INSIDE, true>(p.vol, px, py, pz, f1x, f1y, f1z);
       px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
       float v0[8], v1[8];
       if constexpr (VT == XR_VOXEL_F32) {
@@ -339,7 +359,9 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       if (!hit) break;
-      if ((double)fabsf(dir[k]) > 1.0e-8) {
+      // |v| > 1e-8 compared in double by the reference; 1.0e-8f is the largest
+      // float not above 1e-8, so the float comparison decides the same
+      if (fabsf(dir[k]) > 1.0e-8f) {
         const float inv = __frcp_rn(dir[k]);
         float ta = __fmul_rn(__fsub_rn(0.0f, src[k]), inv);
         float tb = __fmul_rn(__fsub_rn(maxb[k], src[k]), inv);
