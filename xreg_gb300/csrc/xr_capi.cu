@@ -1555,8 +1555,7 @@ extern "C" XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm) {
     xr_status st = sm_prepare_patches(sm, s);
     if (st != XR_OK) return st;
     PatchFixed px{}, py{};
-    XR_CUDA_TRY(launch_patch_ncc(nullptr, rows, cols, 0, grad, sm->smooth_ksize, sm->patch_radius,
-                                 sm->patch_stride, sm->ncr, sm->ncc, px, py, PatchRun{}, 1, nullptr, s, &sm->nblk));
+    sm->nblk = patch_ncc_max_blocks(sm->ncr, sm->ncc);
     XR_CUDA_TRY(sm->d_partials.reserve((size_t)sm->capacity * sm->nblk * 2 * 8));
     if (sm->mvar_mode) XR_CUDA_TRY(sm->d_mvar_sum.reserve((size_t)sm->capacity * 2 * 8));
   }
@@ -1630,20 +1629,24 @@ static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
         run.cnt = sm->d_pcnt.as<int32_t>();
       }
       if (sm->mvar_mode) {
+        int nblk0 = 0;
         XR_CUDA_TRY(launch_patch_ncc(mov, rows, cols, sm->num_mov, grad, sm->smooth_ksize, sm->patch_radius,
                                      sm->patch_stride, sm->ncr, sm->ncc, px, py, run, 0,
-                                     sm->d_partials.as<double>(), s, nullptr));
-        XR_CUDA_TRY(launch_patch_sum_partials(sm->d_partials.as<double>(), sm->nblk, sm->num_mov,
+                                     sm->d_partials.as<double>(), s, &nblk0));
+        XR_CHECK_ARG(nblk0 <= sm->nblk, "compute: patch partials exceed their buffer");
+        XR_CUDA_TRY(launch_patch_sum_partials(sm->d_partials.as<double>(), nblk0, sm->num_mov,
                                               sm->d_mvar_sum.as<double>(), s));
       }
+      int nblk = 0;
       XR_CUDA_TRY(launch_patch_ncc(mov, rows, cols, sm->num_mov, grad, sm->smooth_ksize, sm->patch_radius,
                                    sm->patch_stride, sm->ncr, sm->ncc, px, py, run, 1, sm->d_partials.as<double>(),
-                                   s, nullptr));
+                                   s, &nblk));
+      XR_CHECK_ARG(nblk <= sm->nblk, "compute: patch partials exceed their buffer");
       const double den_x = o.compute_mean_of_patch_sims ? (double)sm->nused
                                                         : (o.weight_patch_sims_in_combine ? sm->tot_w_x : 1.0);
       const double den_y = o.compute_mean_of_patch_sims ? (double)sm->nused
                                                         : (o.weight_patch_sims_in_combine ? sm->tot_w_y : 1.0);
-      XR_CUDA_TRY(launch_patch_finalize(sm->d_partials.as<double>(), sm->nblk, sm->num_mov, den_x, den_y, grad,
+      XR_CUDA_TRY(launch_patch_finalize(sm->d_partials.as<double>(), nblk, sm->num_mov, den_x, den_y, grad,
                                         sm->mvar_mode, o.normalize_weights_as_prob ? 1 : 0,
                                         sm->mvar_mode ? sm->d_mvar_sum.as<double>() : nullptr,
                                         sm->d_sims.as<float>(), s));

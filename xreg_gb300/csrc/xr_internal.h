@@ -154,7 +154,11 @@ cudaError_t launch_sum_f(const float* in, int64_t n, const uint8_t* mask, double
 cudaError_t launch_patch_fixed_stats(const float* img, int rows, int cols, int radius, int stride, int ncr, int ncc,
                                      const uint8_t* mask, int use_mask_stats, float* mean, float* scale, float* wvar,
                                      int* ucount, cudaStream_t s);
-// pass 0: moving-variance sums; pass 1: weighted score sums.  partials [image][block][2].
+// pass 0: moving-variance sums; pass 1: weighted score sums.  partials
+// [image][block][2]; *nblk_out = the blocks per image of this launch (its tile
+// shape depends on the mask and weight options), at most
+// patch_ncc_max_blocks(ncr, ncc).
+int patch_ncc_max_blocks(int ncr, int ncc);
 cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs, int grad, int smooth_ksize,
                              int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py, PatchRun run,
                              int pass, double* partials, cudaStream_t s, int* nblk_out);

@@ -349,23 +349,27 @@ __global__ void patch_fixed_stats_kernel(const float* __restrict__ img, int cols
   }
 }
 
-// Shared-memory layout for one tile of kPC x kPC patch centres (dynamic).
+// Shared-memory layout for one tile of kPC x (kPC rb) patch centres (columns x
+// rows; dynamic): rb = patches scored per thread, stacked in a column.
 struct PatchLayout {
-  int W;    // edge of the patch-window region (moving gradient / fixed tiles)
-  int WI;   // staged input edge
-  int WB;   // blurred edge
+  int Wr, Wc;    // patch-window region (moving gradient / fixed tiles)
+  int WIr, WIc;  // staged input
+  int WBr, WBc;  // blurred
   size_t fbytes;  // float part
-  size_t bytes;   // plus the W x W mask tile
-  __host__ __device__ static PatchLayout make(int radius, int stride, int grad, int kr) {
+  size_t bytes;   // plus the Wr x Wc mask tile
+  __host__ __device__ static PatchLayout make(int radius, int stride, int grad, int kr, int rb) {
     PatchLayout L;
-    L.W = (kPC - 1) * stride + 2 * radius + 1;
-    L.WB = grad ? L.W + 2 : L.W;
-    L.WI = grad ? L.WB + 2 * kr : L.W;
-    const size_t fl = grad ? ((size_t)L.WI * L.WI + (size_t)L.WI * L.WB + (size_t)L.WB * L.WB +
-                              4 * (size_t)L.W * L.W)
-                           : ((size_t)L.WI * L.WI + (size_t)L.W * L.W);
+    L.Wc = (kPC - 1) * stride + 2 * radius + 1;
+    L.Wr = (kPC * rb - 1) * stride + 2 * radius + 1;
+    L.WBc = grad ? L.Wc + 2 : L.Wc;
+    L.WBr = grad ? L.Wr + 2 : L.Wr;
+    L.WIc = grad ? L.WBc + 2 * kr : L.Wc;
+    L.WIr = grad ? L.WBr + 2 * kr : L.Wr;
+    const size_t w = (size_t)L.Wr * L.Wc;
+    const size_t fl = grad ? ((size_t)L.WIr * L.WIc + (size_t)L.WIr * L.WBc + (size_t)L.WBr * L.WBc + 4 * w)
+                           : ((size_t)L.WIr * L.WIc + w);
     L.fbytes = fl * sizeof(float);
-    L.bytes = L.fbytes + (((size_t)L.W * L.W + 15) & ~(size_t)15);
+    L.bytes = L.fbytes + ((w + 15) & ~(size_t)15);
     return L;
   }
 };
@@ -412,31 +416,86 @@ __device__ __forceinline__ float patch_var(const float* __restrict__ m, int P, i
   return sd * sd;
 }
 
+// RB vertically adjacent unmasked patches of one thread (tile-local rows
+// lr RB .. lr RB + RB - 1, column c0): each moving / fixed value is read once
+// from shared memory for every patch whose window holds it.  Per patch the
+// operations and their order are those of patch_score without a mask (sum in
+// row-major order, mean, then variance and covariance in row-major order), so
+// each score has the same bits.
+template <int RB>
+__device__ __forceinline__ void patch_scores_rows(const float* __restrict__ m, const float* __restrict__ f, int Wc,
+                                                  int rbase, int c0, int d, int stride, const float (&fmean)[RB],
+                                                  const float (&fscale)[RB], float (&score)[RB]) {
+  const int span = (RB - 1) * stride + d;
+  float acc[RB], v[RB], cov[RB];
+#pragma unroll
+  for (int j = 0; j < RB; ++j) { acc[j] = 0.0f; v[j] = 0.0f; cov[j] = 0.0f; }
+  for (int rr = 0; rr < span; ++rr) {
+    bool in[RB];
+#pragma unroll
+    for (int j = 0; j < RB; ++j) in[j] = rr >= j * stride && rr < j * stride + d;
+    const float* row = m + (rbase + rr) * Wc + c0;
+    for (int c = 0; c < d; ++c) {
+      const float x = row[c];
+#pragma unroll
+      for (int j = 0; j < RB; ++j)
+        if (in[j]) acc[j] += x;
+    }
+  }
+  const float n = (float)(d * d);
+  float mu[RB];
+#pragma unroll
+  for (int j = 0; j < RB; ++j) mu[j] = d * d > 1 ? acc[j] / n : acc[j];
+  for (int rr = 0; rr < span; ++rr) {
+    bool in[RB];
+#pragma unroll
+    for (int j = 0; j < RB; ++j) in[j] = rr >= j * stride && rr < j * stride + d;
+    const int o = (rbase + rr) * Wc + c0;
+    for (int c = 0; c < d; ++c) {
+      const float x = m[o + c], fx = f[o + c];
+#pragma unroll
+      for (int j = 0; j < RB; ++j)
+        if (in[j]) {
+          const float dm = x - mu[j];
+          v[j] = fmaf(dm, dm, v[j]);
+          cov[j] = fmaf(dm, fx - fmean[j], cov[j]);
+        }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < RB; ++j) {
+    float sd = d * d > 1 ? sqrtf(v[j] / (n - 1.0f)) : 0.0f;
+    sd = fmaxf(sd, 1.0e-6f);
+    score[j] = 1.0f - (cov[j] / sd) * fscale[j];
+  }
+}
+
 // PASS 0: per image and direction, the sum over used patches with an unmasked
 // centre of count x moving-patch variance (the normaliser of variance weights).
 // PASS 1: per image and direction, the sum over used patches of
 // count x weight x score (weight 1 when not weighting in the combine).
-template <int GRAD, int KR, int PASS>
+template <int GRAD, int KR, int PASS, int RB>
 __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __restrict__ imgs, int rows, int cols,
                                                              int radius, int stride, int ncr, int ncc,
                                                              PatchFixed px, PatchFixed py, PatchRun run,
                                                              double* __restrict__ partials) {
   extern __shared__ float sm[];
   __shared__ double red[2 * 32];
-  const PatchLayout L = PatchLayout::make(radius, stride, GRAD, KR);
-  const int W = L.W, WI = L.WI, WB = L.WB;
-  float* s_in = sm;                         // WI x WI
-  float* s_hb = s_in + WI * WI;             // WI x WB (GRAD)
-  float* s_bl = s_hb + WI * WB;             // WB x WB (GRAD)
-  float* s_mx = GRAD ? s_bl + WB * WB : s_in;   // W x W moving (gx or raw)
-  float* s_my = s_mx + W * W;               // W x W moving gy
-  float* s_fx = GRAD ? s_my + W * W : s_in + WI * WI;  // W x W fixed (gx or raw)
-  float* s_fy = s_fx + W * W;
-  uint8_t* s_mk = reinterpret_cast<uint8_t*>(reinterpret_cast<char*>(sm) + L.fbytes);  // W x W mask
+  const PatchLayout L = PatchLayout::make(radius, stride, GRAD, KR, RB);
+  const int Wr = L.Wr, Wc = L.Wc, WIr = L.WIr, WIc = L.WIc, WBr = L.WBr, WBc = L.WBc;
+  const int WW = Wr * Wc;
+  float* s_in = sm;                              // WIr x WIc
+  float* s_hb = s_in + WIr * WIc;                // WIr x WBc (GRAD)
+  float* s_bl = s_hb + WIr * WBc;                // WBr x WBc (GRAD)
+  float* s_mx = GRAD ? s_bl + WBr * WBc : s_in;  // Wr x Wc moving (gx or raw)
+  float* s_my = s_mx + WW;                       // Wr x Wc moving gy
+  float* s_fx = GRAD ? s_my + WW : s_in + WIr * WIc;  // Wr x Wc fixed (gx or raw)
+  float* s_fy = s_fx + WW;
+  uint8_t* s_mk = reinterpret_cast<uint8_t*>(reinterpret_cast<char*>(sm) + L.fbytes);  // Wr x Wc mask
 
   const int tiles_x = (ncc + kPC - 1) / kPC;
   const int tpr = blockIdx.x / tiles_x, tpc = blockIdx.x - tpr * tiles_x;
-  const int pr0 = tpr * kPC, pc0 = tpc * kPC;
+  const int pr0 = tpr * kPC * RB, pc0 = tpc * kPC;
   const int y0 = pr0 * stride, x0 = pc0 * stride;  // top-left pixel of the window region
   const int64_t npix = (int64_t)rows * cols;
   const int64_t img = blockIdx.y;
@@ -444,14 +503,14 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   const int H = GRAD ? (KR + 1) : 0;
   const uint8_t* mk = run.mask ? s_mk : nullptr;
 
-  for (int i = threadIdx.x; i < WI * WI; i += blockDim.x) {
-    const int r = i / WI, c = i - r * WI;
+  for (int i = threadIdx.x; i < WIr * WIc; i += blockDim.x) {
+    const int r = i / WIc, c = i - r * WIc;
     const int gr = reflect101(min(y0 - H + r, rows - 1 + H), rows);
     const int gc = reflect101(min(x0 - H + c, cols - 1 + H), cols);
     s_in[i] = src[(int64_t)gr * cols + gc];
   }
-  for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
-    const int r = i / W, c = i - r * W;
+  for (int i = threadIdx.x; i < WW; i += blockDim.x) {
+    const int r = i / Wc, c = i - r * Wc;
     const int gr = min(y0 + r, rows - 1), gc = min(x0 + c, cols - 1);
     if (PASS == 1) {
       s_fx[i] = px.img[(int64_t)gr * cols + gc];
@@ -463,33 +522,33 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   const bool need_grads = GRAD && (PASS == 1 || run.mvar == 2);
   if (need_grads) {
     if (KR == 0) {
-      for (int i = threadIdx.x; i < WB * WB; i += blockDim.x) {
-        const int r = i / WB, c = i - r * WB;
-        s_bl[i] = s_in[r * WI + c];
+      for (int i = threadIdx.x; i < WBr * WBc; i += blockDim.x) {
+        const int r = i / WBc, c = i - r * WBc;
+        s_bl[i] = s_in[r * WIc + c];
       }
     } else {
-      for (int i = threadIdx.x; i < WI * WB; i += blockDim.x) {
-        const int r = i / WB, c = i - r * WB;
-        const float* q = s_in + r * WI + c;
+      for (int i = threadIdx.x; i < WIr * WBc; i += blockDim.x) {
+        const int r = i / WBc, c = i - r * WBc;
+        const float* q = s_in + r * WIc + c;
         s_hb[i] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[1] + 0.375f * q[2] + 0.25f * q[3] + 0.0625f * q[4])
                             : (0.25f * q[0] + 0.5f * q[1] + 0.25f * q[2]);
       }
       __syncthreads();
-      for (int i = threadIdx.x; i < WB * WB; i += blockDim.x) {
-        const int r = i / WB, c = i - r * WB;
-        const float* q = s_hb + r * WB + c;
-        s_bl[i] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[WB] + 0.375f * q[2 * WB] + 0.25f * q[3 * WB] +
-                               0.0625f * q[4 * WB])
-                            : (0.25f * q[0] + 0.5f * q[WB] + 0.25f * q[2 * WB]);
+      for (int i = threadIdx.x; i < WBr * WBc; i += blockDim.x) {
+        const int r = i / WBc, c = i - r * WBc;
+        const float* q = s_hb + r * WBc + c;
+        s_bl[i] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[WBc] + 0.375f * q[2 * WBc] + 0.25f * q[3 * WBc] +
+                               0.0625f * q[4 * WBc])
+                            : (0.25f * q[0] + 0.5f * q[WBc] + 0.25f * q[2 * WBc]);
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
-      const int r = i / W + 1, c = i % W + 1;
+    for (int i = threadIdx.x; i < WW; i += blockDim.x) {
+      const int r = i / Wc + 1, c = i % Wc + 1;
       const float* q = s_bl;
-      const float a = q[(r - 1) * WB + c - 1], b = q[(r - 1) * WB + c], cc = q[(r - 1) * WB + c + 1];
-      const float d = q[r * WB + c - 1], f = q[r * WB + c + 1];
-      const float g = q[(r + 1) * WB + c - 1], h = q[(r + 1) * WB + c], ii = q[(r + 1) * WB + c + 1];
+      const float a = q[(r - 1) * WBc + c - 1], b = q[(r - 1) * WBc + c], cc = q[(r - 1) * WBc + c + 1];
+      const float d = q[r * WBc + c - 1], f = q[r * WBc + c + 1];
+      const float g = q[(r + 1) * WBc + c - 1], h = q[(r + 1) * WBc + c], ii = q[(r + 1) * WBc + c + 1];
       s_mx[i] = ((cc - a) + 2.0f * (f - d)) + (ii - g);
       s_my[i] = ((g - a) + 2.0f * (h - b)) + (ii - cc);
     }
@@ -498,53 +557,90 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
 
   double v[2] = {0.0, 0.0};
   const int lr = threadIdx.x / kPC, lc = threadIdx.x % kPC;
-  const int pr = pr0 + lr, pc = pc0 + lc;
-  if (pr < ncr && pc < ncc) {
-    const int64_t pidx = (int64_t)pr * ncc + pc;
-    const int cnt = run.cnt ? run.cnt[pidx] : 1;
-    const int d = 2 * radius + 1;
-    const int r0 = lr * stride, c0 = lc * stride;
-    const bool centre = !mk || mk[(r0 + radius) * W + c0 + radius];
-    if (cnt > 0) {
-      // moving-patch variances used as weights: of the moving image itself
-      // (mvar 1, shared by both directions) or of each gradient image (mvar 2)
-      float var0 = 0.0f, var1 = 0.0f;
-      if (run.mvar && centre) {
-        if (run.mvar == 1) {
-          var0 = GRAD ? patch_var(s_in + H * WI + H, WI, r0, c0, d) : patch_var(s_mx, W, r0, c0, d);
-          var1 = var0;
-        } else {
-          var0 = patch_var(s_mx, W, r0, c0, d);
-          if (GRAD) var1 = patch_var(s_my, W, r0, c0, d);
+  const int pc = pc0 + lc;
+  const int d = 2 * radius + 1;
+  const int c0 = lc * stride;
+  if (RB > 1) {
+    // several unmasked patches per thread, no moving-variance weights (the
+    // host picks this form only then); PASS 1 only
+    if (PASS == 1 && pc < ncc) {
+      int64_t pidx[RB];
+      int cnt[RB];
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < RB; ++j) {
+        const int pr = pr0 + lr * RB + j;
+        pidx[j] = (int64_t)pr * ncc + pc;
+        cnt[j] = pr < ncr ? (run.cnt ? run.cnt[pidx[j]] : 1) : 0;
+        any = any || cnt[j] > 0;
+      }
+      if (any) {
+        const int rbase = lr * RB * stride;
+        for (int k = 0; k < (GRAD ? 2 : 1); ++k) {
+          const PatchFixed& P = k == 0 ? px : py;
+          float fm[RB], fs[RB], sc[RB], w[RB];
+#pragma unroll
+          for (int j = 0; j < RB; ++j) {
+            fm[j] = cnt[j] > 0 ? P.mean[pidx[j]] : 0.0f;
+            fs[j] = cnt[j] > 0 ? P.scale[pidx[j]] : 0.0f;
+            w[j] = (cnt[j] > 0 && P.w) ? P.w[pidx[j]] : 1.0f;
+          }
+          patch_scores_rows<RB>(k == 0 ? s_mx : s_my, k == 0 ? s_fx : s_fy, Wc, rbase, c0, d, stride, fm, fs, sc);
+#pragma unroll
+          for (int j = 0; j < RB; ++j)
+            if (cnt[j] > 0 && (!run.weighted || fabsf(w[j]) > 1.0e-6f))
+              v[k] += (double)cnt[j] * (double)((run.weighted ? w[j] : 1.0f) * sc[j]);
         }
       }
-      if (PASS == 0) {
-        v[0] = (double)cnt * var0;
-        v[1] = (double)cnt * var1;
-      } else {
-        float w[2];
-        for (int k = 0; k < 2; ++k) {
-          const PatchFixed& P = k == 0 ? px : py;
-          if (run.mvar) {
-            float vk = k == 0 ? var0 : var1;
-            if (run.normalize) {
-              const float S = (float)run.mvar_sum[img * 2 + k];
-              vk = S > 1.0e-6f ? vk / S : 0.0f;
-            }
-            w[k] = vk;
+    }
+  } else {
+    const int pr = pr0 + lr;
+    if (pr < ncr && pc < ncc) {
+      const int64_t pidx = (int64_t)pr * ncc + pc;
+      const int cnt = run.cnt ? run.cnt[pidx] : 1;
+      const int r0 = lr * stride;
+      const bool centre = !mk || mk[(r0 + radius) * Wc + c0 + radius];
+      if (cnt > 0) {
+        // moving-patch variances used as weights: of the moving image itself
+        // (mvar 1, shared by both directions) or of each gradient image (mvar 2)
+        float var0 = 0.0f, var1 = 0.0f;
+        if (run.mvar && centre) {
+          if (run.mvar == 1) {
+            var0 = GRAD ? patch_var(s_in + H * WIc + H, WIc, r0, c0, d) : patch_var(s_mx, Wc, r0, c0, d);
+            var1 = var0;
           } else {
-            w[k] = P.w ? P.w[pidx] : 1.0f;
+            var0 = patch_var(s_mx, Wc, r0, c0, d);
+            if (GRAD) var1 = patch_var(s_my, Wc, r0, c0, d);
           }
         }
-        if (!run.weighted || fabsf(w[0]) > 1.0e-6f) {
-          const float sc = patch_score(s_mx, s_fx, mk, W, r0, c0, d, px.mean[pidx], px.scale[pidx],
-                                       run.use_mask_stats, run.mask_in_sums);
-          v[0] = (double)cnt * (double)((run.weighted ? w[0] : 1.0f) * sc);
-        }
-        if (GRAD && (!run.weighted || fabsf(w[1]) > 1.0e-6f)) {
-          const float sc = patch_score(s_my, s_fy, mk, W, r0, c0, d, py.mean[pidx], py.scale[pidx],
-                                       run.use_mask_stats, run.mask_in_sums);
-          v[1] = (double)cnt * (double)((run.weighted ? w[1] : 1.0f) * sc);
+        if (PASS == 0) {
+          v[0] = (double)cnt * var0;
+          v[1] = (double)cnt * var1;
+        } else {
+          float w[2];
+          for (int k = 0; k < 2; ++k) {
+            const PatchFixed& P = k == 0 ? px : py;
+            if (run.mvar) {
+              float vk = k == 0 ? var0 : var1;
+              if (run.normalize) {
+                const float S = (float)run.mvar_sum[img * 2 + k];
+                vk = S > 1.0e-6f ? vk / S : 0.0f;
+              }
+              w[k] = vk;
+            } else {
+              w[k] = P.w ? P.w[pidx] : 1.0f;
+            }
+          }
+          if (!run.weighted || fabsf(w[0]) > 1.0e-6f) {
+            const float sc = patch_score(s_mx, s_fx, mk, Wc, r0, c0, d, px.mean[pidx], px.scale[pidx],
+                                         run.use_mask_stats, run.mask_in_sums);
+            v[0] = (double)cnt * (double)((run.weighted ? w[0] : 1.0f) * sc);
+          }
+          if (GRAD && (!run.weighted || fabsf(w[1]) > 1.0e-6f)) {
+            const float sc = patch_score(s_my, s_fy, mk, Wc, r0, c0, d, py.mean[pidx], py.scale[pidx],
+                                         run.use_mask_stats, run.mask_in_sums);
+            v[1] = (double)cnt * (double)((run.weighted ? w[1] : 1.0f) * sc);
+          }
         }
       }
     }
@@ -711,28 +807,46 @@ cudaError_t launch_patch_fixed_stats(const float* img, int rows, int cols, int r
   return cudaGetLastError();
 }
 
+// Patches scored per thread: four stacked in a column when no mask and no
+// moving-variance weight is involved and the taller tile fits, else one.
+constexpr int kPatchRows = 4;
+static int patch_rb(int radius, int stride, int grad, int kr, const PatchRun& run) {
+  if (run.mask || run.mvar) return 1;
+  return PatchLayout::make(radius, stride, grad, kr, kPatchRows).bytes <= 112 * 1024 ? kPatchRows : 1;
+}
+
+static int patch_tiles(int ncr, int ncc, int rb) {
+  return ((ncr + kPC * rb - 1) / (kPC * rb)) * ((ncc + kPC - 1) / kPC);
+}
+
+int patch_ncc_max_blocks(int ncr, int ncc) { return patch_tiles(ncr, ncc, 1); }
+
 cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs, int grad, int smooth_ksize,
                              int radius, int stride, int ncr, int ncc, PatchFixed px, PatchFixed py, PatchRun run,
                              int pass, double* partials, cudaStream_t s, int* nblk_out) {
-  const int tiles = ((ncr + kPC - 1) / kPC) * ((ncc + kPC - 1) / kPC);
-  if (nblk_out) *nblk_out = tiles;
-  if (nimgs <= 0 || !partials) return cudaSuccess;
   const int kr = smooth_ksize == 5 ? 2 : (smooth_ksize == 3 ? 1 : 0);
   if (smooth_ksize != 0 && smooth_ksize != 3 && smooth_ksize != 5) return cudaErrorInvalidValue;
-  const PatchLayout L = PatchLayout::make(radius, stride, grad, kr);
+  const int rb = patch_rb(radius, stride, grad, kr, run);
+  const int tiles = patch_tiles(ncr, ncc, rb);
+  if (nblk_out) *nblk_out = tiles;
+  if (nimgs <= 0 || !partials) return cudaSuccess;
+  if (rb > 1 && pass != 1) return cudaErrorInvalidValue;
+  const PatchLayout L = PatchLayout::make(radius, stride, grad, kr, rb);
   if (L.bytes > 200 * 1024) return cudaErrorInvalidValue;
   const dim3 grid(tiles, (unsigned)nimgs);
   cudaError_t e = cudaSuccess;
-#define XR_PATCH_LAUNCH(G, K, P)                                                                           \
-  e = set_smem(patch_ncc_kernel<G, K, P>, L.bytes);                                                       \
-  if (e != cudaSuccess) return e;                                                                          \
-  patch_ncc_kernel<G, K, P><<<grid, kThreads, L.bytes, s>>>(mov, rows, cols, radius, stride, ncr, ncc, px, py, \
-                                                            run, partials);
-#define XR_PATCH_PASS(G, K) \
-  if (pass == 0) {          \
-    XR_PATCH_LAUNCH(G, K, 0) \
-  } else {                  \
-    XR_PATCH_LAUNCH(G, K, 1) \
+#define XR_PATCH_LAUNCH(G, K, P, R)                                                                          \
+  e = set_smem(patch_ncc_kernel<G, K, P, R>, L.bytes);                                                      \
+  if (e != cudaSuccess) return e;                                                                            \
+  patch_ncc_kernel<G, K, P, R><<<grid, kThreads, L.bytes, s>>>(mov, rows, cols, radius, stride, ncr, ncc, px, py, \
+                                                               run, partials);
+#define XR_PATCH_PASS(G, K)              \
+  if (rb > 1) {                          \
+    XR_PATCH_LAUNCH(G, K, 1, kPatchRows) \
+  } else if (pass == 0) {                \
+    XR_PATCH_LAUNCH(G, K, 0, 1)          \
+  } else {                               \
+    XR_PATCH_LAUNCH(G, K, 1, 1)          \
   }
   if (!grad) {
     XR_PATCH_PASS(0, 0)
