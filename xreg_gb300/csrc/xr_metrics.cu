@@ -33,6 +33,11 @@ __device__ __forceinline__ int reflect101(int i, int n) {
   return i;
 }
 
+// A float-float value hi + lo (about 48 significant bits).
+struct FF {
+  float hi, lo;
+};
+
 struct Kahan {
   float s = 0.0f, c = 0.0f;
   __device__ __forceinline__ void add(float x) {
@@ -42,7 +47,53 @@ struct Kahan {
     s = t;
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  __device__ __forceinline__ FF ff() const { return FF{s, -c}; }
 };
+
+// Knuth's two-sum on the FP32 pipe for float-float values (FF, before Kahan):
+// this GPU's FP64 pipe is slow enough that block reductions in double kept it
+// 82 % busy and bounded the grad-NCC moment kernel.  Explicit _rn intrinsics
+// keep every step unfused.
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));  // s + e = a.hi + b.hi exactly
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  const float hi = __fadd_rn(s, e);
+  return FF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+
+// a b exactly as a float-float (the rounding error of the product from one fma).
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return FF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_shfl_down(FF v, int o) {
+  return FF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+// Block-wide sum of K float-float values per thread, returned in double by
+// thread 0 (the other threads get undefined values).
+template <int K>
+__device__ __forceinline__ void block_sum_ff(FF (&v)[K], double (&out)[K], FF* red /* [K][32] */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    FF w = v[k];
+    for (int o = 16; o > 0; o >>= 1) w = ff_add(w, ff_shfl_down(w, o));
+    if (lane == 0) red[k * 32 + warp] = w;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      FF w = (lane < nw) ? red[k * 32 + lane] : FF{0.0f, 0.0f};
+      for (int o = 16; o > 0; o >>= 1) w = ff_add(w, ff_shfl_down(w, o));
+      out[k] = (double)w.hi + (double)w.lo;
+    }
+  }
+}
 
 __device__ __forceinline__ double warp_sum_d(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -101,7 +152,7 @@ __global__ void __launch_bounds__(kThreads) ncc_moments_kernel(const float* __re
                                                                const float* __restrict__ fhat,
                                                                const uint8_t* __restrict__ mask,
                                                                double* __restrict__ partials) {
-  __shared__ double red[3 * 32];
+  __shared__ FF red[3 * 32];
   const int64_t img = blockIdx.y;
   const float* m = mov + img * npix;
   Kahan s0, s1, s2;
@@ -112,8 +163,9 @@ __global__ void __launch_bounds__(kThreads) ncc_moments_kernel(const float* __re
     s1.add(x * x);
     s2.add(x * fhat[i]);
   }
-  double v[3] = {s0.value(), s1.value(), s2.value()};
-  block_sum_d<3>(v, red);
+  FF f[3] = {s0.ff(), s1.ff(), s2.ff()};
+  double v[3];
+  block_sum_ff<3>(f, v, red);
   if (threadIdx.x == 0) {
     double* o = partials + (img * gridDim.x + blockIdx.x) * 3;
     o[0] = v[0]; o[1] = v[1]; o[2] = v[2];
@@ -132,14 +184,20 @@ __device__ __forceinline__ double ncc_sim_from_moments(double sm, double smm, do
   return (1.0 - ncc) * 0.5;
 }
 
+// One block per image (as grad_finalize_kernel).
 __global__ void ncc_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double n,
                                     FixedNCC fx, float* __restrict__ sims) {
-  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (img >= nimgs) return;
-  double a = 0, b = 0, c = 0;
+  __shared__ double red[3 * 32];
+  const int64_t img = blockIdx.x;
+  double a[3] = {0, 0, 0};
   const double* p = partials + img * nblk * 3;
-  for (int k = 0; k < nblk; ++k) { a += p[3 * k]; b += p[3 * k + 1]; c += p[3 * k + 2]; }
-  sims[img] = (float)ncc_sim_from_moments(a, b, c, n, fx);
+  for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
+    a[0] += p[3 * k];
+    a[1] += p[3 * k + 1];
+    a[2] += p[3 * k + 2];
+  }
+  block_sum_d<3>(a, red);
+  if (threadIdx.x == 0) sims[img] = (float)ncc_sim_from_moments(a[0], a[1], a[2], n, fx);
 }
 
 // ------------------------------------------------------ gradient images ---
@@ -241,7 +299,7 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
                                                                 const uint8_t* __restrict__ mask,
                                                                 double* __restrict__ partials) {
   __shared__ GradTile<KR> t;
-  __shared__ double red[6 * 32];
+  __shared__ FF red[6 * 32];
   const int tiles_x = (cols + kT - 1) / kT;
   const int y0 = (blockIdx.x / tiles_x) * kT, x0 = (blockIdx.x % tiles_x) * kT;
   const int64_t npix = (int64_t)rows * cols;
@@ -259,10 +317,11 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
     s[0].add(a); s[1].add(a * a); s[2].add(a * fhx[pix]);
     s[3].add(b); s[4].add(b * b); s[5].add(b * fhy[pix]);
   }
-  double v[6];
+  FF f[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) v[k] = s[k].value();
-  block_sum_d<6>(v, red);
+  for (int k = 0; k < 6; ++k) f[k] = s[k].ff();
+  double v[6];
+  block_sum_ff<6>(f, v, red);
   if (threadIdx.x == 0) {
     double* o = partials + (img * gridDim.x + blockIdx.x) * 6;
 #pragma unroll
@@ -270,14 +329,18 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
   }
 }
 
+// One block per image: the block partials summed by all threads in double,
+// then across the block.
 __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double n,
                                      FixedNCC fx, FixedNCC fy, float* __restrict__ sims) {
-  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (img >= nimgs) return;
+  __shared__ double red[6 * 32];
+  const int64_t img = blockIdx.x;
   double a[6] = {0, 0, 0, 0, 0, 0};
   const double* p = partials + img * nblk * 6;
-  for (int k = 0; k < nblk; ++k)
+  for (int k = threadIdx.x; k < nblk; k += blockDim.x)
     for (int j = 0; j < 6; ++j) a[j] += p[6 * k + j];
+  block_sum_d<6>(a, red);
+  if (threadIdx.x != 0) return;
   const double sx = ncc_sim_from_moments(a[0], a[1], a[2], n, fx);
   const double sy = ncc_sim_from_moments(a[3], a[4], a[5], n, fy);
   // 0.5 * (float(s_x) + float(s_y)) as in ImgSimMetric2DGradNCCCPU::compute
@@ -480,7 +543,7 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
                                                              PatchFixed px, PatchFixed py, PatchRun run,
                                                              double* __restrict__ partials) {
   extern __shared__ float sm[];
-  __shared__ double red[2 * 32];
+  __shared__ FF red[2 * 32];
   const PatchLayout L = PatchLayout::make(radius, stride, GRAD, KR, RB);
   const int Wr = L.Wr, Wc = L.Wc, WIr = L.WIr, WIc = L.WIc, WBr = L.WBr, WBc = L.WBc;
   const int WW = Wr * Wc;
@@ -555,7 +618,7 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
   }
   __syncthreads();
 
-  double v[2] = {0.0, 0.0};
+  FF v[2] = {FF{0.0f, 0.0f}, FF{0.0f, 0.0f}};
   const int lr = threadIdx.x / kPC, lc = threadIdx.x % kPC;
   const int pc = pc0 + lc;
   const int d = 2 * radius + 1;
@@ -589,7 +652,7 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
 #pragma unroll
           for (int j = 0; j < RB; ++j)
             if (cnt[j] > 0 && (!run.weighted || fabsf(w[j]) > 1.0e-6f))
-              v[k] += (double)cnt[j] * (double)((run.weighted ? w[j] : 1.0f) * sc[j]);
+              v[k] = ff_add(v[k], ff_prod((float)cnt[j], (run.weighted ? w[j] : 1.0f) * sc[j]));
         }
       }
     }
@@ -614,8 +677,8 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
           }
         }
         if (PASS == 0) {
-          v[0] = (double)cnt * var0;
-          v[1] = (double)cnt * var1;
+          v[0] = ff_prod((float)cnt, var0);
+          v[1] = ff_prod((float)cnt, var1);
         } else {
           float w[2];
           for (int k = 0; k < 2; ++k) {
@@ -634,22 +697,23 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
           if (!run.weighted || fabsf(w[0]) > 1.0e-6f) {
             const float sc = patch_score(s_mx, s_fx, mk, Wc, r0, c0, d, px.mean[pidx], px.scale[pidx],
                                          run.use_mask_stats, run.mask_in_sums);
-            v[0] = (double)cnt * (double)((run.weighted ? w[0] : 1.0f) * sc);
+            v[0] = ff_prod((float)cnt, (run.weighted ? w[0] : 1.0f) * sc);
           }
           if (GRAD && (!run.weighted || fabsf(w[1]) > 1.0e-6f)) {
             const float sc = patch_score(s_my, s_fy, mk, Wc, r0, c0, d, py.mean[pidx], py.scale[pidx],
                                          run.use_mask_stats, run.mask_in_sums);
-            v[1] = (double)cnt * (double)((run.weighted ? w[1] : 1.0f) * sc);
+            v[1] = ff_prod((float)cnt, (run.weighted ? w[1] : 1.0f) * sc);
           }
         }
       }
     }
   }
-  block_sum_d<2>(v, red);
+  double t[2];
+  block_sum_ff<2>(v, t, red);
   if (threadIdx.x == 0) {
     double* o = partials + (img * gridDim.x + blockIdx.x) * 2;
-    o[0] = v[0];
-    o[1] = v[1];
+    o[0] = t[0];
+    o[1] = t[1];
   }
 }
 
@@ -754,8 +818,7 @@ cudaError_t launch_ncc_moments(const float* mov, int64_t npix, int64_t nimgs, co
 cudaError_t launch_ncc_finalize(const double* partials, int nblk, int64_t nimgs, int64_t n_used, FixedNCC fx,
                                 float* sims, cudaStream_t s) {
   if (nimgs <= 0) return cudaSuccess;
-  ncc_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, (double)n_used, fx,
-                                                                      sims);
+  ncc_finalize_kernel<<<(unsigned)nimgs, 128, 0, s>>>(partials, nblk, nimgs, (double)n_used, fx, sims);
   return cudaGetLastError();
 }
 
@@ -791,8 +854,7 @@ cudaError_t launch_grad_moments(const float* mov, int rows, int cols, int64_t ni
 cudaError_t launch_grad_finalize(const double* partials, int nblk, int64_t nimgs, int64_t n_used, FixedNCC fx,
                                  FixedNCC fy, float* sims, cudaStream_t s) {
   if (nimgs <= 0) return cudaSuccess;
-  grad_finalize_kernel<<<(unsigned)((nimgs + 127) / 128), 128, 0, s>>>(partials, nblk, nimgs, (double)n_used, fx,
-                                                                       fy, sims);
+  grad_finalize_kernel<<<(unsigned)nimgs, 128, 0, s>>>(partials, nblk, nimgs, (double)n_used, fx, fy, sims);
   return cudaGetLastError();
 }
 
