@@ -382,7 +382,10 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
       const float lc = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(v[0], v[0]), __fmul_rn(v[1], v[1])),
                                             __fmul_rn(v[2], v[2])));
       const float len = __fmul_rn(__fsub_rn(t1, t0), lc);
-      unsigned long long nsteps = (unsigned long long)__fdiv_rn(len, p.step);
+      // floor(len / step) through a saturating 32-bit conversion (a 64-bit one
+      // runs on the slow FP64 pipe): above 2^32 - 1 it saturates and NaN gives
+      // 0, so the max_steps test (max_steps < 2^31) decides as with 64 bits
+      unsigned long long nsteps = __float2uint_rz(__fdiv_rn(len, p.step));
       if (!(nsteps <= p.max_steps)) {
         // A ray longer than the volume diagonal allows can only come from a
         // non-finite or degenerate pose: count it and leave the pixel unsampled
