@@ -49,7 +49,7 @@ def _args():
     p.add_argument("--voxel", default="f32", choices=["f32", "f16", "bf16"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true")
-    p.add_argument("--only", default="", choices=["", "precision", "multi-job", "serving"],
+    p.add_argument("--only", default="", choices=["", "plain-small", "precision", "multi-job", "serving"],
                    help="run one of the extra measurements alone and print its JSON (for profiling)")
     p.add_argument("--serving-requests", type=int, default=10, help="requests in the serving measurement (0 = off)")
     p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrival rate of the serving measurement")
@@ -360,6 +360,70 @@ def run_ours(a, rank, world, local):
     return res
 
 
+def _plain_small(xr, dev, cpu_budget_s: float):
+    """The plain method's own configuration: 128^3 FP32 phantom at 1.5 mm, 256^2
+    detector at 1.55 mm, 0.5 mm step, NCC, one pose per evaluation.  The GPU's
+    plain path (pose upload, DRR launch, NCC launches, host read per pose) and
+    the oracle's FP32 DRR + NCC on the host cores, on the same poses; the largest
+    difference of the NCC values over the poses the oracle ran."""
+    from oracle import oracle as O
+    from tests.helpers import oracle_cams, oracle_geom
+    from xreg_gb300 import synth
+    w = synth.plain_small(0)
+    rc0 = xr.RayCasterLineIntCUDA(dev)
+    rc0.set_volume(w.vol)
+    rc0.set_camera_model(w.cams[0])
+    rc0.set_ray_step_size(w.step)
+    rc0.set_num_projs(1)
+    rc0.allocate_resources()
+    rc0.distribute_xforms_among_cam_models(synth.fixed_pose(w)[None])
+    rc0.compute()
+    fixed = synth.add_noise(rc0.proj(0), 0.01, w.seed + 2)
+    rc0.close()
+    poses = synth.sample_poses(w.vol, w.gt, 200, w.rot_sigma, w.trans_sigma, seed=w.seed + 3)
+    rc = xr.RayCasterLineIntCUDA(dev)
+    rc.set_volume(w.vol)
+    rc.set_camera_model(w.cams[0])
+    rc.set_ray_step_size(w.step)
+    rc.set_num_projs(1)
+    rc.allocate_resources()
+    m = xr.ImgSimMetric2DNCCCUDA(dev)
+    m.set_fixed_image(fixed)
+    m.set_num_moving_images(1)
+    m.set_mov_imgs_buf_from_ray_caster(rc, 0)
+    m.allocate_resources()
+    for i in range(5):
+        rc.distribute_xforms_among_cam_models(poses[i][None])
+        rc.compute()
+        m.compute()
+        m.sim_vals()
+    vals = []
+    t0 = time.perf_counter()
+    for p in poses:
+        rc.distribute_xforms_among_cam_models(p[None])
+        rc.compute()
+        m.compute()
+        vals.append(float(m.sim_vals()[0]))
+    gpu = len(poses) / (time.perf_counter() - t0)
+    rc.close()
+    cores = O.set_threads(os.cpu_count() or 1)
+    geom, cams = oracle_geom(w.vol), oracle_cams(w.cams)
+    done, t_used, diff = 0, 0.0, 0.0
+    while done < len(poses) and (done == 0 or t_used < cpu_budget_s):
+        t1 = time.perf_counter()
+        d = O.drr_f32(w.vol.voxels, geom, cams, poses[done][None], step=w.step)
+        v = float(O.ncc(fixed, d)[0])
+        t_used += time.perf_counter() - t1
+        diff = max(diff, abs(v - vals[done]))
+        done += 1
+    return {"workload": "128^3 FP32 @1.5 mm, 256^2 @1.55 mm, step 0.5 mm, NCC, one pose per evaluation",
+            "gpu_plain_poses_per_s": round(gpu, 1),
+            "how": "per pose: pose upload, DRR launch, NCC launches, host read (200 poses)",
+            "cpu_oracle_poses_per_s": round(done / t_used, 2), "cpu_cores": cores,
+            "cpu_sample": f"{done} poses, {t_used:.1f} s",
+            "max_abs_ncc_diff_vs_oracle": diff}
+
+
 def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
     """Plain single-pose path (one DRR + one metric launch per pose, host sync per
     pose as xReg's OpenCL path does) and half-precision volumes, for context."""
@@ -421,7 +485,8 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
                                           "max_abs_sim_diff_vs_f32": float(
                                               np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
         objh.close()
-    for key, fn in (("precision_large", lambda: _precision(xr, dev, stream)),
+    for key, fn in (("plain_small_config", lambda: _plain_small(xr, dev, min(3.0, a.cpu_seconds))),
+                    ("precision_large", lambda: _precision(xr, dev, stream)),
                     ("uneven_multi_job", lambda: _multi_job(xr, dev)),
                     ("serving", lambda: _serving(dev, a.serving_requests, a.serving_rate))):
         if key == "serving" and a.serving_requests <= 0:
@@ -670,7 +735,8 @@ def main():
         import xreg_gb300 as xr
         torch.cuda.set_device(local)
         xr.load()
-        fn = {"precision": lambda: _precision(xr, local, torch.cuda.Stream(device=local)),
+        fn = {"plain-small": lambda: _plain_small(xr, local, min(3.0, a.cpu_seconds)),
+              "precision": lambda: _precision(xr, local, torch.cuda.Stream(device=local)),
               "multi-job": lambda: _multi_job(xr, local),
               "serving": lambda: _serving(local, a.serving_requests, a.serving_rate)}[a.only]
         res = {"only": a.only, "result": fn()} if rank == 0 else None
