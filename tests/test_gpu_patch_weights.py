@@ -190,3 +190,27 @@ def test_objective_with_masked_random_patch_metric(xr, oracle):
                                        use_mov_var_wgts=1)
         np.testing.assert_allclose(vals, ref, atol=TOL, rtol=2e-6)
     assert not np.array_equal(seen[0], seen[1])
+
+
+def test_unmasked_tiles_and_random_subsets(xr, oracle):
+    """Unmasked patches without variance weights run four vertically adjacent
+    patches per thread over 16x64-centre tiles: a detector with several tile
+    rows and a ragged last one, random subsets (patch counts) through that
+    path, and a radius whose tall tile exceeds the shared-memory budget (one
+    patch per thread again)."""
+    rc, imgs, fixed = _drrs(xr, det=(150, 70), seed=21, px=0.8)
+    for cls, fn in ((xr.ImgSimMetric2DPatchNCCCUDA, oracle.patch_ncc_ex),
+                    (xr.ImgSimMetric2DPatchGradNCCCUDA, oracle.patch_grad_ncc_ex)):
+        _, got = _eval(xr, cls, rc, fixed, 6, 5, 1)
+        np.testing.assert_allclose(got, fn(fixed, imgs[1:], radius=5, stride=1), atol=TOL, rtol=2e-6)
+        _, got = _eval(xr, cls, rc, fixed, 6, 4, 3)
+        np.testing.assert_allclose(got, fn(fixed, imgs[1:], radius=4, stride=3), atol=TOL, rtol=2e-6)
+        m, got = _eval(xr, cls, rc, fixed, 6, 3, 1, choose_rand_patches=1, num_rand_patches=60, rand_seed=5)
+        idx = m.patch_indices_used()
+        ncc = fixed.shape[1] - 6
+        count = np.bincount(idx, minlength=(fixed.shape[0] - 6) * ncc).astype(np.int32)
+        np.testing.assert_allclose(got, fn(fixed, imgs[1:], radius=3, stride=1, patch_count=count),
+                                   atol=TOL, rtol=2e-6)
+    _, got = _eval(xr, xr.ImgSimMetric2DPatchGradNCCCUDA, rc, fixed, 6, 16, 1)  # 136 KB tall tile
+    np.testing.assert_allclose(got, oracle.patch_grad_ncc_ex(fixed, imgs[1:], radius=16, stride=1),
+                               atol=TOL, rtol=2e-6)
