@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../xreg_gb300.h"
+#include "../xreg_gb300_io.h"
 
 namespace xreg_gb300 {
 
@@ -259,6 +260,21 @@ class PopulationObjective {
  private:
   xr_objective h_ = nullptr;
 };
+
+// Poses on disk (lib/itk/xregITKIOUtils.h:46-57), ITK text transform files.
+inline Mat4 ReadITKAffineTransformFromFile(const std::string& path) {
+  Mat4 m{};
+  check(xr_itk_affine_transform_read(path.c_str(), m.data()));
+  return m;
+}
+inline Mat4 ReadSlicerAffineTransformFromFile(const std::string& path) {
+  Mat4 m{};
+  check(xr_itk_slicer_affine_transform_read(path.c_str(), m.data()));
+  return m;
+}
+inline void WriteITKAffineTransform(const std::string& path, const Mat4& xform) {
+  check(xr_itk_affine_transform_write(path.c_str(), xform.data()));
+}
 
 }  // namespace xreg_gb300
 

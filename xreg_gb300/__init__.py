@@ -24,6 +24,9 @@ from .api import (  # noqa: F401
     hu_to_lin_att_device,
     log_remap,
     proj_preproc,
+    read_itk_affine_transform,
+    read_slicer_affine_transform,
+    write_itk_affine_transform,
 )
 
 __version__ = "0.1.0"

@@ -165,6 +165,9 @@ _SIGS = {
     "xr_jobset_eval": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
     "xr_jobset_eval_device": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
     "xr_jobset_last_launch": [H, C.POINTER(i64), C.POINTER(i32)],
+    "xr_itk_affine_transform_read": [C.c_char_p, P],
+    "xr_itk_slicer_affine_transform_read": [C.c_char_p, P],
+    "xr_itk_affine_transform_write": [C.c_char_p, P],
 }
 _RESTYPES = {"xr_last_error": C.c_char_p, "xr_version": C.c_char_p}
 

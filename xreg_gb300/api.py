@@ -6,6 +6,7 @@ objects reads the same; every call goes to libxreg_gb300.so.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -634,3 +635,27 @@ def proj_preproc(img: np.ndarray, cam: CameraModel, crop_width: int = 50, no_log
     if not no_log_remap:
         out = log_remap(out, True, 1.0, device)
     return out, c
+
+
+# ------------------------------------------------------------ poses on disk
+def read_itk_affine_transform(path: str) -> np.ndarray:
+    """ReadITKAffineTransformFromFile: the 4x4 pose in an ITK text transform file
+    (".txt" / ".tfm"; xr_itk_affine_transform_read)."""
+    out = np.empty((4, 4), dtype=np.float64)
+    call("xr_itk_affine_transform_read", os.fsencode(path), out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def read_slicer_affine_transform(path: str) -> np.ndarray:
+    """ReadSlicerAffineTransformFromFile: the inverse of the file's pose
+    (xr_itk_slicer_affine_transform_read)."""
+    out = np.empty((4, 4), dtype=np.float64)
+    call("xr_itk_slicer_affine_transform_read", os.fsencode(path), out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def write_itk_affine_transform(path: str, xform) -> None:
+    """WriteITKAffineTransform: the pose as an AffineTransform_float_3_3 in an ITK
+    text transform file (xr_itk_affine_transform_write)."""
+    x = np.ascontiguousarray(np.asarray(xform, dtype=np.float64).reshape(4, 4))
+    call("xr_itk_affine_transform_write", os.fsencode(path), x.ctypes.data_as(C.c_void_p))
