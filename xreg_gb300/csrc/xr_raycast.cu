@@ -22,11 +22,13 @@
 //   LINEAR  voxels x-fastest; a sample issues 8 scalar loads.
 //   CELL8   for every trilinear cell (ix, iy, iz) in [0, n-2]^3 the 8 corner
 //           values are stored contiguously (v000 v100 v010 v110 v001 v101 v011
-//           v111): one 16-byte load per sample for FP16/BF16, two for FP32.
-//           It spends 8x the voxel bytes of HBM to cut L1 requests per sample
-//           from 8 to 1-2; the linear kernel is bound by exactly those requests.
+//           v111): one 16-byte load per sample for FP16/BF16, two for FP32,
+//           or one 32-byte load for FP32 (the 256-bit read, layout 2).  It
+//           spends 8x the voxel bytes of HBM to cut L1 requests per sample from
+//           8 to 1-2; the linear kernel is bound by exactly those requests.
 #include "xr_internal.h"
 
+#include <atomic>
 #include <cfloat>
 
 namespace xr {
@@ -565,18 +567,22 @@ drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long tota
   }
 }
 
+constexpr int kMaxDevices = 64;
+
 template <int VT, int LAYOUT, int UNROLL>
 int multi_blocks_t() {
-  static int cached[64] = {0};  // per device
+  static std::atomic<int> cached[kMaxDevices];  // per device; zero = not known yet
   int dev = 0, sms = 0, per_sm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  if (cached[dev]) return cached[dev];
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 0;
+  const int known = cached[dev].load(std::memory_order_relaxed);
+  if (known) return known;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drr_multi_kernel<VT, LAYOUT, UNROLL>, kThreads, 0) !=
       cudaSuccess)
     return 0;
-  cached[dev] = sms * (per_sm > 0 ? per_sm : 1);
-  return cached[dev];
+  const int blocks = sms * (per_sm > 0 ? per_sm : 1);
+  cached[dev].store(blocks, std::memory_order_relaxed);  // every thread computes the same value
+  return blocks;
 }
 
 template <int VT, int LAYOUT, int UNROLL>
@@ -601,12 +607,15 @@ cudaError_t launch_multi_unroll(const MultiJobDrr* d_jobs, int njobs, long long 
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 cudaError_t launch_t(const DrrParams& p, cudaStream_t s) {
-  // The kernel uses no shared memory: ask for the largest L1 (the gathers hit it).
-  static bool carveout_set = false;
-  if (!carveout_set) {
+  // The kernel uses no shared memory: ask for the largest L1 (the gathers hit
+  // it), once per device (a preference; setting it twice is harmless).
+  static std::atomic<bool> carveout_set[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices &&
+      !carveout_set[dev].load(std::memory_order_relaxed)) {
     cudaFuncSetAttribute(drr_kernel<VT, KERNEL, LAYOUT, UNROLL>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxL1);
-    carveout_set = true;
+    carveout_set[dev].store(true, std::memory_order_relaxed);
   }
   const int bw = p.block_warps_x;
   const int wc = p.warp_tall ? 4 : 8;
