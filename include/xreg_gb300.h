@@ -278,6 +278,8 @@ typedef struct {
   int32_t mask_only_for_weights;                 /* [0] 1 = the OpenCL metric's rule
                                                     (xregImgSimMetric2DPatchNCCOCL.cpp:240): the mask
                                                     weights patches but every pixel enters the sums */
+  int32_t save_all_per_patch_scores;             /* [0] keep every patch's score (xr_sm_patch_scores) */
+  int32_t reserved0;                             /* 0 */
   int64_t num_rand_patches;                      /* [100] */
   double rand_patch_min_pixels_sep;              /* [-1] = sqrt(2) radius; 0 = no check */
   uint64_t rand_seed;
@@ -294,6 +296,16 @@ XR_API xr_status xr_sm_set_patch_wgt_img(xr_simmetric sm, const float* host_img)
 /* Patches the last compute used, in draw order (row-major patch-centre grid
  * indices); *count receives the number, at most cap are written. */
 XR_API xr_status xr_sm_patch_indices_used(xr_simmetric sm, int64_t cap, int64_t* idx, int64_t* count);
+/* ImgSimMetric2DPatchCommon::sim_vals_for_each_patch (xregImgSimMetric2DPatchCommon.h:91,
+ * filled by xregImgSimMetric2DPatchNCCCPU.cpp:172-180,247-250 and
+ * xregImgSimMetric2DPatchGradNCCCPU.cpp:226-240) for moving image img of the last
+ * compute, with save_all_per_patch_scores set before allocate_resources: *count =
+ * the number of patches; entry i is the score 1 - sum of the i-th patch in use
+ * (the grid order, or the order of the random draw), 0.5 (s_x + s_y) for patch
+ * grad-NCC (0 for a direction left out by a weight at or below 1e-6); entries
+ * past the patches in use and patches left out are 0; every entry is FLT_MAX
+ * when the image's value is FLT_MAX. */
+XR_API xr_status xr_sm_patch_scores(xr_simmetric sm, int64_t img, int64_t cap, float* out, int64_t* count);
 /* allocate_resources (xregImgSimMetric2D.h:81): fixed-image statistics, gradients
  * and patch statistics are computed once here and stay on the device. */
 XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm);

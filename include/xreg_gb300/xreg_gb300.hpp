@@ -186,6 +186,8 @@ class ImgSimMetric2DPatchCUDA : public ImgSimMetric2DCUDA {
   void set_compute_mean_of_patch_sims(bool v) { set([&](xr_patch_options& o) { o.compute_mean_of_patch_sims = v; }); }
   // the OpenCL patch metrics' rule: the mask only weights the patches
   void set_mask_only_for_weights(bool v) { set([&](xr_patch_options& o) { o.mask_only_for_weights = v; }); }
+  // ImgSimMetric2DPatchCommon::set_save_all_per_patch_scores (xregImgSimMetric2DPatchCommon.h:93)
+  void set_save_all_per_patch_scores(bool v) { set([&](xr_patch_options& o) { o.save_all_per_patch_scores = v; }); }
   void set_use_fixed_img_patch_variances_as_wgts(bool v) {
     set([&](xr_patch_options& o) { o.use_fixed_img_patch_variances_as_wgts = v; });
   }
@@ -206,6 +208,18 @@ class ImgSimMetric2DPatchCUDA : public ImgSimMetric2DCUDA {
     check(xr_sm_patch_indices_used(h_, 0, nullptr, &n));
     std::vector<int64_t> out((size_t)n);
     check(xr_sm_patch_indices_used(h_, n, out.data(), &n));
+    return out;
+  }
+  // sim_vals_for_each_patch (xregImgSimMetric2DPatchCommon.h:91), indexed [patch][moving image]
+  std::vector<std::vector<float>> sim_vals_for_each_patch(int64_t num_mov_imgs) const {
+    int64_t n = 0;
+    check(xr_sm_patch_scores(h_, 0, 0, nullptr, &n));
+    std::vector<std::vector<float>> out((size_t)n, std::vector<float>((size_t)num_mov_imgs));
+    std::vector<float> one((size_t)n);
+    for (int64_t m = 0; m < num_mov_imgs; ++m) {
+      check(xr_sm_patch_scores(h_, m, n, one.data(), &n));
+      for (int64_t p = 0; p < n; ++p) out[(size_t)p][(size_t)m] = one[(size_t)p];
+    }
     return out;
   }
 

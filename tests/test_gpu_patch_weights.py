@@ -214,3 +214,85 @@ def test_unmasked_tiles_and_random_subsets(xr, oracle):
     _, got = _eval(xr, xr.ImgSimMetric2DPatchGradNCCCUDA, rc, fixed, 6, 16, 1)  # 136 KB tall tile
     np.testing.assert_allclose(got, oracle.patch_grad_ncc_ex(fixed, imgs[1:], radius=16, stride=1),
                                atol=TOL, rtol=2e-6)
+
+
+def _np_patch_scores(fixed, mov, radius, stride):
+    """Each patch's score 1 - sum(((m - mu_m) / sd_m) (f - mu_f) / (sd_f n)) in
+    double (sample standard deviations, clamped at 1e-6), in grid order."""
+    d = 2 * radius + 1
+    n = d * d
+    rows, cols = fixed.shape
+    out = []
+    for r in range(radius, rows - radius, stride):
+        for c in range(radius, cols - radius, stride):
+            f = fixed[r - radius:r + radius + 1, c - radius:c + radius + 1].astype(np.float64)
+            m = mov[r - radius:r + radius + 1, c - radius:c + radius + 1].astype(np.float64)
+            sf = max(np.sqrt(((f - f.mean()) ** 2).sum() / (n - 1)), 1e-6)
+            sm = max(np.sqrt(((m - m.mean()) ** 2).sum() / (n - 1)), 1e-6)
+            out.append(1.0 - (((m - m.mean()) / sm) * (f - f.mean()) / (sf * n)).sum())
+    return np.array(out)
+
+
+@pytest.mark.parametrize("masked", [0, 1])
+def test_per_patch_scores(xr, oracle, masked):
+    """save_all_per_patch_scores: every patch's score in xReg's order; for patch
+    NCC against a direct double computation, for patch grad-NCC 0.5 (s_x + s_y)
+    against the same computation on the oracle's gradient images; the weighted
+    mean of the kept scores is the metric's value; random subsets list the drawn
+    patches in draw order; flat moving images mark every patch FLT_MAX."""
+    rc, imgs, fixed = _drrs(xr, det=(40, 46), seed=31)
+    mask = _mask(fixed.shape, 12) if masked else None
+    r, st = 3, 2
+    m, vals = _eval(xr, xr.ImgSimMetric2DPatchNCCCUDA, rc, fixed, 4, r, st, mask=mask,
+                    save_all_per_patch_scores=1)
+    ncr, ncc = (fixed.shape[0] - 2 * r + st - 1) // st, (fixed.shape[1] - 2 * r + st - 1) // st
+    for k in range(4):
+        sc = m.patch_scores(k)
+        assert sc.shape == (ncr * ncc,)
+        if not masked:
+            np.testing.assert_allclose(sc, _np_patch_scores(fixed, imgs[1 + k], r, st), atol=2e-5, rtol=0)
+        else:
+            # patches wholly inside the masked-out block have weight 0: left out, kept as 0
+            out = np.array([mask[rr - r:rr + r + 1, cc - r:cc + r + 1].sum() == 0
+                            for rr in range(r, fixed.shape[0] - r, st) for cc in range(r, fixed.shape[1] - r, st)])
+            assert out.any() and np.all(sc[out] == 0.0)
+    if masked:
+        # unweighted mean combine: the value is the mean of the kept scores
+        mm, mvals = _eval(xr, xr.ImgSimMetric2DPatchNCCCUDA, rc, fixed, 4, r, st, mask=mask,
+                          save_all_per_patch_scores=1, weight_patch_sims_in_combine=0, compute_mean_of_patch_sims=1)
+        for k in range(4):
+            np.testing.assert_allclose(mm.patch_scores(k).mean(), mvals[k], atol=2e-5, rtol=0)
+    mg, gvals = _eval(xr, xr.ImgSimMetric2DPatchGradNCCCUDA, rc, fixed, 4, r, st, save_all_per_patch_scores=1)
+    fgx, fgy = oracle.grad_images(fixed)
+    for k in range(4):
+        mgx, mgy = oracle.grad_images(imgs[1 + k])
+        ref = 0.5 * (_np_patch_scores(fgx, mgx, r, st) + _np_patch_scores(fgy, mgy, r, st))
+        np.testing.assert_allclose(mg.patch_scores(k), ref, atol=2e-5, rtol=0)
+        np.testing.assert_allclose(mg.patch_scores(k).mean(), gvals[k], atol=2e-5, rtol=0)
+    # random subsets: the drawn patches in draw order, the rest 0
+    mr, _ = _eval(xr, xr.ImgSimMetric2DPatchNCCCUDA, rc, fixed, 4, r, 1, choose_rand_patches=1,
+                  num_rand_patches=12, rand_seed=3, save_all_per_patch_scores=1)
+    idx = mr.patch_indices_used()
+    full = _np_patch_scores(fixed, imgs[1], r, 1)
+    sc = mr.patch_scores(0)
+    np.testing.assert_allclose(sc[:12], full[idx], atol=2e-5, rtol=0)
+    assert np.all(sc[12:] == 0.0)
+
+
+def test_per_patch_scores_flat_image(xr):
+    import torch
+    rng = np.random.default_rng(4)
+    fixed = rng.random((30, 32)).astype(np.float32)
+    movs = np.stack([np.full((30, 32), 2.0, np.float32), rng.random((30, 32)).astype(np.float32)])
+    d = torch.from_numpy(movs).cuda()
+    m = xr.ImgSimMetric2DPatchNCCCUDA()
+    m.set_fixed_image(fixed)
+    m.set_patch_radius(3)
+    m.set_patch_options(use_mov_img_patch_variances_as_wgts=1, save_all_per_patch_scores=1)
+    m.set_num_moving_images(2)
+    m.set_mov_imgs_device_buf(d.data_ptr(), 0)
+    m.allocate_resources()
+    torch.cuda.synchronize()
+    m.compute()
+    assert np.all(m.patch_scores(0) == FLT_MAX)
+    assert np.all(m.patch_scores(1) < 2.0)

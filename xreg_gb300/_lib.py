@@ -46,7 +46,8 @@ class xr_patch_options(C.Structure):
                 ("compute_mean_of_patch_sims", C.c_int32), ("use_fixed_img_patch_variances_as_wgts", C.c_int32),
                 ("use_mov_img_patch_variances_as_wgts", C.c_int32),
                 ("use_variances_in_grad_imgs_as_wgts", C.c_int32), ("choose_rand_patches", C.c_int32),
-                ("mask_only_for_weights", C.c_int32), ("num_rand_patches", C.c_int64), ("rand_patch_min_pixels_sep", C.c_double),
+                ("mask_only_for_weights", C.c_int32), ("save_all_per_patch_scores", C.c_int32),
+                ("reserved0", C.c_int32), ("num_rand_patches", C.c_int64), ("rand_patch_min_pixels_sep", C.c_double),
                 ("rand_seed", C.c_uint64)]
 
 
@@ -127,6 +128,7 @@ _SIGS = {
     "xr_sm_get_patch_options": [H, C.POINTER(xr_patch_options)],
     "xr_sm_set_patch_wgt_img": [H, P],
     "xr_sm_patch_indices_used": [H, i64, P, C.POINTER(i64)],
+    "xr_sm_patch_scores": [H, i64, i64, P, C.POINTER(i64)],
     "xr_sm_allocate_resources": [H],
     "xr_sm_compute": [H],
     "xr_sm_sim_vals": [H, P],

@@ -454,6 +454,15 @@ class _PatchParams:
         call("xr_sm_patch_indices_used", self._h, n.value, _ptr(out), C.byref(n))
         return out
 
+    def patch_scores(self, img: int) -> np.ndarray:
+        """sim_vals_for_each_patch for moving image img of the last compute (patches
+        in use order; needs save_all_per_patch_scores before allocate_resources)."""
+        n = C.c_int64()
+        call("xr_sm_patch_scores", self._h, int(img), 0, None, C.byref(n))
+        out = np.empty(n.value, dtype=np.float32)
+        call("xr_sm_patch_scores", self._h, int(img), n.value, _ptr(out), C.byref(n))
+        return out
+
 
 class ImgSimMetric2DNCCCUDA(ImgSimMetric2DCUDA):
     KIND = L.XR_SIM_NCC

@@ -5,6 +5,7 @@
 #include "xreg_gb300_regi.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -235,6 +236,7 @@ struct xr_simmetric_s {
   std::vector<uint8_t> h_mask;     // host copy of the mask (patch weights)
   std::vector<float> wgt_img;      // user weight image (rows * cols) or empty
   DevBuf d_pw_x, d_pw_y, d_pcnt, d_pidx, d_mvar_sum;
+  DevBuf d_pscores;                // [image][patch] scores (save_all_per_patch_scores)
   bool has_pw = false;             // per-patch weights on the device (else 1)
   std::vector<double> w_x, w_y;    // static patch weights per direction
   std::vector<double> w_draw;      // weights the random subsets are drawn with
@@ -1293,6 +1295,36 @@ extern "C" XR_API xr_status xr_sm_set_patch_wgt_img(xr_simmetric sm, const float
   return XR_OK;
 }
 
+extern "C" XR_API xr_status xr_sm_patch_scores(xr_simmetric sm, int64_t img, int64_t cap, float* out, int64_t* count) {
+  XR_CHECK_ARG(sm && count && (out || cap == 0), "patch_scores: NULL argument");
+  XR_CHECK_ARG(sm->kind == XR_SIM_PATCH_NCC || sm->kind == XR_SIM_PATCH_GRAD_NCC, "patch_scores: not a patch metric");
+  XR_CHECK_ARG(sm->allocated && sm->popt.save_all_per_patch_scores,
+               "patch_scores: set save_all_per_patch_scores before allocate_resources");
+  XR_CHECK_ARG(img >= 0 && img < sm->num_mov, "patch_scores: bad moving image index");
+  const int64_t np = (int64_t)sm->ncr * sm->ncc;
+  *count = np;
+  if (cap <= 0) return XR_OK;
+  DeviceGuard g(sm->device);
+  cudaStream_t s = sm->stream();
+  std::vector<float> all((size_t)np);
+  float sim = 0.0f;
+  XR_CUDA_TRY(cudaMemcpyAsync(all.data(), sm->d_pscores.as<float>() + img * np, (size_t)np * 4,
+                              cudaMemcpyDeviceToHost, s));
+  XR_CUDA_TRY(cudaMemcpyAsync(&sim, sm->d_sims.as<float>() + img, 4, cudaMemcpyDeviceToHost, s));
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
+  const int64_t n = std::min<int64_t>(cap, np);
+  if (sim == FLT_MAX) {  // flat moving image: xReg marks every patch
+    for (int64_t i = 0; i < n; ++i) out[i] = FLT_MAX;
+    return XR_OK;
+  }
+  // xReg keeps the scores in the order of the patches in use
+  const bool drawn = sm->popt.choose_rand_patches != 0;
+  const int64_t used = drawn ? (int64_t)sm->last_idx.size() : np;
+  for (int64_t i = 0; i < n; ++i)
+    out[i] = i < used ? all[(size_t)(drawn ? (int64_t)sm->last_idx[(size_t)i] : i)] : 0.0f;
+  return XR_OK;
+}
+
 extern "C" XR_API xr_status xr_sm_patch_indices_used(xr_simmetric sm, int64_t cap, int64_t* idx, int64_t* count) {
   XR_CHECK_ARG(sm && count && (idx || cap == 0), "patch_indices_used: NULL argument");
   XR_CHECK_ARG(sm->kind == XR_SIM_PATCH_NCC || sm->kind == XR_SIM_PATCH_GRAD_NCC,
@@ -1557,6 +1589,8 @@ extern "C" XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm) {
     PatchFixed px{}, py{};
     sm->nblk = patch_ncc_max_blocks(sm->ncr, sm->ncc);
     XR_CUDA_TRY(sm->d_partials.reserve((size_t)sm->capacity * sm->nblk * 2 * 8));
+    if (sm->popt.save_all_per_patch_scores)
+      XR_CUDA_TRY(sm->d_pscores.reserve((size_t)sm->capacity * (size_t)sm->ncr * (size_t)sm->ncc * 4));
     if (sm->mvar_mode) XR_CUDA_TRY(sm->d_mvar_sum.reserve((size_t)sm->capacity * 2 * 8));
   }
   XR_CUDA_TRY(sm->d_sims.reserve((size_t)sm->capacity * 4));
@@ -1627,6 +1661,11 @@ static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
         xr_status st = sm_draw_patches(sm, s);
         if (st != XR_OK) return st;
         run.cnt = sm->d_pcnt.as<int32_t>();
+      }
+      if (o.save_all_per_patch_scores) {
+        XR_CUDA_TRY(cudaMemsetAsync(sm->d_pscores.p, 0,
+                                    (size_t)sm->num_mov * (size_t)sm->ncr * (size_t)sm->ncc * 4, s));
+        run.scores = sm->d_pscores.as<float>();
       }
       if (sm->mvar_mode) {
         int nblk0 = 0;

@@ -128,6 +128,7 @@ struct PatchRun {           // per compute
   int mvar;                 // moving-variance weights: 0 none, 1 of the image, 2 of each gradient image
   int normalize;            // normalise moving variances by their sum
   const double* mvar_sum;   // [image][direction] sums of count x variance (pass 0), for pass 1
+  float* scores;            // [image][patch] each patch's score (pass 1), nullptr = not kept
 };
 
 // Moments of moving images for (grad-)NCC: partials[img][block][k] in double.

@@ -639,6 +639,9 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
       }
       if (any) {
         const int rbase = lr * RB * stride;
+        float kept[RB];  // per-patch score as xReg keeps it (0.5 (s_x + s_y) for GRAD)
+#pragma unroll
+        for (int j = 0; j < RB; ++j) kept[j] = 0.0f;
         for (int k = 0; k < (GRAD ? 2 : 1); ++k) {
           const PatchFixed& P = k == 0 ? px : py;
           float fm[RB], fs[RB], sc[RB], w[RB];
@@ -651,9 +654,15 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
           patch_scores_rows<RB>(k == 0 ? s_mx : s_my, k == 0 ? s_fx : s_fy, Wc, rbase, c0, d, stride, fm, fs, sc);
 #pragma unroll
           for (int j = 0; j < RB; ++j)
-            if (cnt[j] > 0 && (!run.weighted || fabsf(w[j]) > 1.0e-6f))
+            if (cnt[j] > 0 && (!run.weighted || fabsf(w[j]) > 1.0e-6f)) {
               v[k] = ff_add(v[k], ff_prod((float)cnt[j], (run.weighted ? w[j] : 1.0f) * sc[j]));
+              kept[j] += GRAD ? 0.5f * sc[j] : sc[j];
+            }
         }
+        if (run.scores)
+#pragma unroll
+          for (int j = 0; j < RB; ++j)
+            if (cnt[j] > 0) run.scores[img * (int64_t)ncr * ncc + pidx[j]] = kept[j];
       }
     }
   } else {
@@ -694,16 +703,20 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
               w[k] = P.w ? P.w[pidx] : 1.0f;
             }
           }
+          float kept = 0.0f;  // per-patch score as xReg keeps it (0.5 (s_x + s_y) for GRAD)
           if (!run.weighted || fabsf(w[0]) > 1.0e-6f) {
             const float sc = patch_score(s_mx, s_fx, mk, Wc, r0, c0, d, px.mean[pidx], px.scale[pidx],
                                          run.use_mask_stats, run.mask_in_sums);
             v[0] = ff_prod((float)cnt, (run.weighted ? w[0] : 1.0f) * sc);
+            kept += GRAD ? 0.5f * sc : sc;
           }
           if (GRAD && (!run.weighted || fabsf(w[1]) > 1.0e-6f)) {
             const float sc = patch_score(s_my, s_fy, mk, Wc, r0, c0, d, py.mean[pidx], py.scale[pidx],
                                          run.use_mask_stats, run.mask_in_sums);
             v[1] = ff_prod((float)cnt, (run.weighted ? w[1] : 1.0f) * sc);
+            kept += 0.5f * sc;
           }
+          if (run.scores) run.scores[img * (int64_t)ncr * ncc + pidx] = kept;
         }
       }
     }
