@@ -300,12 +300,19 @@ XR_API xr_status xr_sm_patch_indices_used(xr_simmetric sm, int64_t cap, int64_t*
  * filled by xregImgSimMetric2DPatchNCCCPU.cpp:172-180,247-250 and
  * xregImgSimMetric2DPatchGradNCCCPU.cpp:226-240) for moving image img of the last
  * compute, with save_all_per_patch_scores set before allocate_resources: *count =
- * the number of patches; entry i is the score 1 - sum of the i-th patch in use
- * (the grid order, or the order of the random draw), 0.5 (s_x + s_y) for patch
- * grad-NCC (0 for a direction left out by a weight at or below 1e-6); entries
- * past the patches in use and patches left out are 0; every entry is FLT_MAX
- * when the image's value is FLT_MAX. */
+ * the number of patches in use (all, num_rand_patches, or the set_patches_to_use
+ * list); entry i is the score 1 - sum of the i-th patch in use (grid order, draw
+ * order or list order), 0.5 (s_x + s_y) for patch grad-NCC (0 for a direction
+ * left out by a weight at or below 1e-6); patches left out are 0; every entry
+ * is FLT_MAX when the image's value is FLT_MAX. */
 XR_API xr_status xr_sm_patch_scores(xr_simmetric sm, int64_t img, int64_t cap, float* out, int64_t* count);
+/* ImgSimMetric2DPatchCommon::set_patches_to_use / reset_patches_to_use
+ * (xregImgSimMetric2DPatchCommon.cpp:231-241): the patches to use, by grid
+ * index, repeats counted (the value sums weight x score over the list and, with
+ * weight_patch_sims_in_combine, divides by the list's weights); it takes the
+ * place of the grid and of random draws.  n = 0 resets.  Takes effect at the
+ * next allocate_resources, which checks the indices against the grid. */
+XR_API xr_status xr_sm_set_patches_to_use(xr_simmetric sm, int64_t n, const int64_t* idx);
 /* allocate_resources (xregImgSimMetric2D.h:81): fixed-image statistics, gradients
  * and patch statistics are computed once here and stay on the device. */
 XR_API xr_status xr_sm_allocate_resources(xr_simmetric sm);

@@ -210,6 +210,11 @@ class ImgSimMetric2DPatchCUDA : public ImgSimMetric2DCUDA {
     check(xr_sm_patch_indices_used(h_, n, out.data(), &n));
     return out;
   }
+  // set_patches_to_use / reset_patches_to_use (xregImgSimMetric2DPatchCommon.h:121-123)
+  void set_patches_to_use(const std::vector<int64_t>& idx) {
+    check(xr_sm_set_patches_to_use(h_, (int64_t)idx.size(), idx.empty() ? nullptr : idx.data()));
+  }
+  void reset_patches_to_use() { check(xr_sm_set_patches_to_use(h_, 0, nullptr)); }
   // sim_vals_for_each_patch (xregImgSimMetric2DPatchCommon.h:91), indexed [patch][moving image]
   std::vector<std::vector<float>> sim_vals_for_each_patch(int64_t num_mov_imgs) const {
     int64_t n = 0;

@@ -269,14 +269,14 @@ def test_per_patch_scores(xr, oracle, masked):
         ref = 0.5 * (_np_patch_scores(fgx, mgx, r, st) + _np_patch_scores(fgy, mgy, r, st))
         np.testing.assert_allclose(mg.patch_scores(k), ref, atol=2e-5, rtol=0)
         np.testing.assert_allclose(mg.patch_scores(k).mean(), gvals[k], atol=2e-5, rtol=0)
-    # random subsets: the drawn patches in draw order, the rest 0
+    # random subsets: the drawn patches in draw order
     mr, _ = _eval(xr, xr.ImgSimMetric2DPatchNCCCUDA, rc, fixed, 4, r, 1, choose_rand_patches=1,
                   num_rand_patches=12, rand_seed=3, save_all_per_patch_scores=1)
     idx = mr.patch_indices_used()
     full = _np_patch_scores(fixed, imgs[1], r, 1)
     sc = mr.patch_scores(0)
-    np.testing.assert_allclose(sc[:12], full[idx], atol=2e-5, rtol=0)
-    assert np.all(sc[12:] == 0.0)
+    assert sc.shape == (12,)
+    np.testing.assert_allclose(sc, full[idx], atol=2e-5, rtol=0)
 
 
 def test_per_patch_scores_flat_image(xr):
@@ -296,3 +296,44 @@ def test_per_patch_scores_flat_image(xr):
     m.compute()
     assert np.all(m.patch_scores(0) == FLT_MAX)
     assert np.all(m.patch_scores(1) < 2.0)
+
+
+@pytest.mark.parametrize("grad", [0, 1])
+def test_patches_to_use(xr, oracle, grad):
+    """set_patches_to_use: a fixed list (repeats counted) instead of the grid or a
+    draw; the value equals the oracle with those counts, the indices and the kept
+    scores follow the list; reset returns to the whole grid."""
+    rc, imgs, fixed = _drrs(xr, det=(44, 50), seed=33)
+    mask = _mask(fixed.shape, 13)
+    cls = xr.ImgSimMetric2DPatchGradNCCCUDA if grad else xr.ImgSimMetric2DPatchNCCCUDA
+    fn = oracle.patch_grad_ncc_ex if grad else oracle.patch_ncc_ex
+    np_all = (44 - 6) * (50 - 6)
+    lst = np.array([5, 77, 77, 300, 1203, 999, 5, 640, 641, 1500], dtype=np.int64)
+    for mk in (None, mask):
+        m = cls()
+        m.set_fixed_image(fixed)
+        if mk is not None:
+            m.set_mask(mk)
+        m.set_patch_radius(3)
+        m.set_patch_options(save_all_per_patch_scores=1, choose_rand_patches=1, num_rand_patches=20)
+        m.set_patches_to_use(lst)  # the list wins over random draws
+        m.set_num_moving_images(5)
+        m.set_mov_imgs_buf_from_ray_caster(rc, 1)
+        m.allocate_resources()
+        m.compute()
+        count = np.bincount(lst, minlength=np_all).astype(np.int32)
+        ref = fn(fixed, imgs[1:6], radius=3, stride=1, mask=mk, patch_count=count)
+        np.testing.assert_allclose(m.sim_vals(), ref, atol=TOL, rtol=2e-6)
+        np.testing.assert_array_equal(m.patch_indices_used(), lst)
+        sc = m.patch_scores(2)
+        assert sc.shape == lst.shape and sc[0] == sc[6] and sc[1] == sc[2]
+        m.reset_patches_to_use()
+        m.set_patch_options(choose_rand_patches=0)
+        m.allocate_resources()
+        m.compute()
+        np.testing.assert_allclose(m.sim_vals(), fn(fixed, imgs[1:6], radius=3, stride=1, mask=mk),
+                                   atol=TOL, rtol=2e-6)
+        assert m.patch_scores(0).shape == (np_all,)
+    with pytest.raises(Exception):
+        m.set_patches_to_use([np_all])  # outside the grid: refused at allocate_resources
+        m.allocate_resources()

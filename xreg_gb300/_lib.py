@@ -129,6 +129,7 @@ _SIGS = {
     "xr_sm_set_patch_wgt_img": [H, P],
     "xr_sm_patch_indices_used": [H, i64, P, C.POINTER(i64)],
     "xr_sm_patch_scores": [H, i64, i64, P, C.POINTER(i64)],
+    "xr_sm_set_patches_to_use": [H, i64, P],
     "xr_sm_allocate_resources": [H],
     "xr_sm_compute": [H],
     "xr_sm_sim_vals": [H, P],

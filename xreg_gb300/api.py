@@ -454,6 +454,14 @@ class _PatchParams:
         call("xr_sm_patch_indices_used", self._h, n.value, _ptr(out), C.byref(n))
         return out
 
+    def set_patches_to_use(self, idx) -> None:
+        """set_patches_to_use (grid indices, repeats counted); empty or None = reset_patches_to_use."""
+        a = np.ascontiguousarray(np.asarray([] if idx is None else idx, dtype=np.int64).ravel())
+        call("xr_sm_set_patches_to_use", self._h, a.size, _ptr(a) if a.size else None)
+
+    def reset_patches_to_use(self) -> None:
+        self.set_patches_to_use(None)
+
     def patch_scores(self, img: int) -> np.ndarray:
         """sim_vals_for_each_patch for moving image img of the last compute (patches
         in use order; needs save_all_per_patch_scores before allocate_resources)."""

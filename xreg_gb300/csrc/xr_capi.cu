@@ -244,7 +244,8 @@ struct xr_simmetric_s {
   int64_t nused = 0;               // patches in use (with multiplicity)
   int mvar_mode = 0;               // moving-variance weights (PatchRun::mvar)
   std::mt19937 rng;
-  std::vector<int32_t> last_idx;   // the last drawn subset
+  std::vector<int32_t> last_idx;   // the patches in use when listed (the last draw, or user_idx)
+  std::vector<int32_t> user_idx;   // set_patches_to_use (empty = not set)
 
   // The bound ray caster if it is still alive; forgets it otherwise.
   xr_raycaster live_rc() {
@@ -1295,6 +1296,22 @@ extern "C" XR_API xr_status xr_sm_set_patch_wgt_img(xr_simmetric sm, const float
   return XR_OK;
 }
 
+extern "C" XR_API xr_status xr_sm_set_patches_to_use(xr_simmetric sm, int64_t n, const int64_t* idx) {
+  XR_CHECK_ARG(sm && (idx || n == 0), "set_patches_to_use: NULL argument");
+  XR_CHECK_ARG(sm->kind == XR_SIM_PATCH_NCC || sm->kind == XR_SIM_PATCH_GRAD_NCC,
+               "set_patches_to_use: not a patch metric");
+  XR_CHECK_ARG(n >= 0 && n <= INT32_MAX, "set_patches_to_use: bad count");
+  std::vector<int32_t> v((size_t)n);
+  for (int64_t k = 0; k < n; ++k) {
+    XR_CHECK_ARG(idx[k] >= 0 && idx[k] <= INT32_MAX, "set_patches_to_use: patch index out of range");
+    v[(size_t)k] = (int32_t)idx[k];
+  }
+  sm->user_idx.swap(v);
+  sm->allocated = false;
+  sm->generation++;
+  return XR_OK;
+}
+
 extern "C" XR_API xr_status xr_sm_patch_scores(xr_simmetric sm, int64_t img, int64_t cap, float* out, int64_t* count) {
   XR_CHECK_ARG(sm && count && (out || cap == 0), "patch_scores: NULL argument");
   XR_CHECK_ARG(sm->kind == XR_SIM_PATCH_NCC || sm->kind == XR_SIM_PATCH_GRAD_NCC, "patch_scores: not a patch metric");
@@ -1302,7 +1319,9 @@ extern "C" XR_API xr_status xr_sm_patch_scores(xr_simmetric sm, int64_t img, int
                "patch_scores: set save_all_per_patch_scores before allocate_resources");
   XR_CHECK_ARG(img >= 0 && img < sm->num_mov, "patch_scores: bad moving image index");
   const int64_t np = (int64_t)sm->ncr * sm->ncc;
-  *count = np;
+  const bool listed = !sm->user_idx.empty() || sm->popt.choose_rand_patches;
+  const int64_t used = listed ? (int64_t)sm->last_idx.size() : np;
+  *count = used;  // xReg sizes the list by num_patches(): the patches in use
   if (cap <= 0) return XR_OK;
   DeviceGuard g(sm->device);
   cudaStream_t s = sm->stream();
@@ -1312,16 +1331,13 @@ extern "C" XR_API xr_status xr_sm_patch_scores(xr_simmetric sm, int64_t img, int
                               cudaMemcpyDeviceToHost, s));
   XR_CUDA_TRY(cudaMemcpyAsync(&sim, sm->d_sims.as<float>() + img, 4, cudaMemcpyDeviceToHost, s));
   XR_CUDA_TRY(cudaStreamSynchronize(s));
-  const int64_t n = std::min<int64_t>(cap, np);
+  const int64_t n = std::min<int64_t>(cap, used);
   if (sim == FLT_MAX) {  // flat moving image: xReg marks every patch
     for (int64_t i = 0; i < n; ++i) out[i] = FLT_MAX;
     return XR_OK;
   }
   // xReg keeps the scores in the order of the patches in use
-  const bool drawn = sm->popt.choose_rand_patches != 0;
-  const int64_t used = drawn ? (int64_t)sm->last_idx.size() : np;
-  for (int64_t i = 0; i < n; ++i)
-    out[i] = i < used ? all[(size_t)(drawn ? (int64_t)sm->last_idx[(size_t)i] : i)] : 0.0f;
+  for (int64_t i = 0; i < n; ++i) out[i] = all[(size_t)(listed ? (int64_t)sm->last_idx[(size_t)i] : i)];
   return XR_OK;
 }
 
@@ -1329,7 +1345,7 @@ extern "C" XR_API xr_status xr_sm_patch_indices_used(xr_simmetric sm, int64_t ca
   XR_CHECK_ARG(sm && count && (idx || cap == 0), "patch_indices_used: NULL argument");
   XR_CHECK_ARG(sm->kind == XR_SIM_PATCH_NCC || sm->kind == XR_SIM_PATCH_GRAD_NCC,
                "patch_indices_used: not a patch metric");
-  if (sm->popt.choose_rand_patches) {
+  if (!sm->user_idx.empty() || sm->popt.choose_rand_patches) {
     *count = (int64_t)sm->last_idx.size();
     for (int64_t k = 0; k < std::min<int64_t>(cap, *count); ++k) idx[k] = sm->last_idx[(size_t)k];
   } else {
@@ -1485,7 +1501,23 @@ static xr_status sm_prepare_patches(xr_simmetric sm, cudaStream_t s) {
     XR_CUDA_TRY(cudaMemcpy(sm->d_pw_y.p, f.data(), (size_t)np * 4, cudaMemcpyHostToDevice));
   }
   sm->mvar_mode = o.use_mov_img_patch_variances_as_wgts ? ((grad && o.use_variances_in_grad_imgs_as_wgts) ? 2 : 1) : 0;
-  if (o.choose_rand_patches) {
+  if (!sm->user_idx.empty()) {
+    // set_patches_to_use: this list, duplicates counted, instead of the grid or a draw
+    for (int32_t i : sm->user_idx)
+      XR_CHECK_ARG(i >= 0 && i < np, "allocate_resources: a patch given to set_patches_to_use is outside the grid");
+    XR_CUDA_TRY(sm->d_pcnt.reserve((size_t)np * 4));
+    XR_CUDA_TRY(sm->d_pidx.reserve(sm->user_idx.size() * 4));
+    sm->last_idx = sm->user_idx;
+    sm->tot_w_x = 0;
+    sm->tot_w_y = 0;
+    for (int32_t i : sm->last_idx) { sm->tot_w_x += sm->w_x[(size_t)i]; sm->tot_w_y += sm->w_y[(size_t)i]; }
+    sm->nused = (int64_t)sm->last_idx.size();
+    XR_CUDA_TRY(cudaMemcpyAsync(sm->d_pidx.p, sm->last_idx.data(), sm->last_idx.size() * 4, cudaMemcpyHostToDevice,
+                                s));
+    XR_CUDA_TRY(cudaMemsetAsync(sm->d_pcnt.p, 0, (size_t)np * 4, s));
+    XR_CUDA_TRY(launch_patch_scatter_counts(sm->d_pidx.as<int32_t>(), sm->nused, sm->d_pcnt.as<int32_t>(), s));
+    XR_CUDA_TRY(cudaStreamSynchronize(s));  // last_idx's host copy is reused by the next prepare
+  } else if (o.choose_rand_patches) {
     XR_CHECK_ARG(o.num_rand_patches < np, "allocate_resources: num_rand_patches must be below the patch count");
     double t = 0;
     for (double v : sm->w_draw) t += v;
@@ -1657,7 +1689,9 @@ static xr_status sm_enqueue_compute_on(xr_simmetric sm, cudaStream_t s) {
                    o.weight_patch_sims_in_combine ? 1 : 0,
                    sm->mvar_mode, o.normalize_weights_as_prob ? 1 : 0,
                    sm->mvar_mode ? sm->d_mvar_sum.as<double>() : nullptr};
-      if (o.choose_rand_patches) {
+      if (!sm->user_idx.empty()) {
+        run.cnt = sm->d_pcnt.as<int32_t>();  // set_patches_to_use: counted at allocate_resources
+      } else if (o.choose_rand_patches) {
         xr_status st = sm_draw_patches(sm, s);
         if (st != XR_OK) return st;
         run.cnt = sm->d_pcnt.as<int32_t>();
