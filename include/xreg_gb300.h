@@ -150,6 +150,28 @@ XR_API xr_status xr_rc_distribute_xforms_among_cam_models(xr_raycaster rc, int64
 XR_API xr_status xr_rc_distribute_xforms_device(xr_raycaster rc, int64_t num_xforms, const double* d_xforms);
 /* set_camera_model_proj_associations (xregRayCastInterface.cpp:73-80). */
 XR_API xr_status xr_rc_set_camera_model_proj_associations(xr_raycaster rc, int64_t n, const int32_t* cam_idx);
+/* camera_model_proj_associations / set_proj_cam_model (xregRayCastInterface.cpp:78-87):
+ * the camera of every projection (*count = num_projs), and one projection's camera. */
+XR_API xr_status xr_rc_camera_model_proj_associations(xr_raycaster rc, int64_t cap, int32_t* cam_idx, int64_t* count);
+XR_API xr_status xr_rc_set_proj_cam_model(xr_raycaster rc, int64_t proj_idx, int32_t cam_idx);
+/* xforms_cam_to_itk_phys (xregRayCastInterface.cpp:182-198): every projection's
+ * pose (row-major 4x4 each; *count = num_projs, 0 before any pose is set);
+ * poses given on the device are copied back first. */
+XR_API xr_status xr_rc_xforms_cam_to_itk_phys(xr_raycaster rc, int64_t cap, double* xforms, int64_t* count);
+/* pre_multiply_all_xforms / post_multiply_all_xforms
+ * (xregRayCastInterface.cpp:235-261): every pose becomes pre * pose, or
+ * pose * post (in double; xReg's FrameTransform is float). */
+XR_API xr_status xr_rc_pre_multiply_all_xforms(xr_raycaster rc, const double* pre_xform);
+XR_API xr_status xr_rc_post_multiply_all_xforms(xr_raycaster rc, const double* post_xform);
+/* num_vols, num_camera_models (xregRayCastInterface.h:93-98). */
+XR_API xr_status xr_rc_num_vols(xr_raycaster rc, int32_t* out);
+XR_API xr_status xr_rc_num_camera_models(xr_raycaster rc, int32_t* out);
+/* xform_img_center_to_itk_phys (xregRayCastInterface.cpp:200-224): translation
+ * by the ITK physical point of the volume's continuous index size / 2.
+ * xform_cam_wrt_carm_center_of_rot (:226-233): translation by -focal_len / 2
+ * along z.  Row-major 4x4 outputs. */
+XR_API xr_status xr_rc_xform_img_center_to_itk_phys(xr_raycaster rc, int32_t vol_idx, double* out);
+XR_API xr_status xr_rc_xform_cam_wrt_carm_center_of_rot(xr_raycaster rc, int32_t cam_idx, double* out);
 /* RayCaster::allocate_resources + RayCasterCPU::allocate_resources
  * (xregRayCastInterface.cpp:248-260, xregRayCastBaseCPU.cpp:50-88). */
 XR_API xr_status xr_rc_allocate_resources(xr_raycaster rc);

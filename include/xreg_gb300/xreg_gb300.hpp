@@ -108,6 +108,34 @@ class RayCasterLineIntCUDA {
   void set_camera_model_proj_associations(const std::vector<int32_t>& a) {
     check(xr_rc_set_camera_model_proj_associations(h_, (int64_t)a.size(), a.data()));
   }
+  std::vector<int32_t> camera_model_proj_associations() const {
+    int64_t n = 0;
+    check(xr_rc_camera_model_proj_associations(h_, 0, nullptr, &n));
+    std::vector<int32_t> out((size_t)n);
+    check(xr_rc_camera_model_proj_associations(h_, n, out.data(), &n));
+    return out;
+  }
+  void set_proj_cam_model(int64_t proj_idx, int32_t cam_idx) { check(xr_rc_set_proj_cam_model(h_, proj_idx, cam_idx)); }
+  std::vector<Mat4> xforms_cam_to_itk_phys() const {
+    int64_t n = 0;
+    check(xr_rc_xforms_cam_to_itk_phys(h_, 0, nullptr, &n));
+    std::vector<Mat4> out((size_t)n);
+    check(xr_rc_xforms_cam_to_itk_phys(h_, n, n ? out[0].data() : nullptr, &n));
+    return out;
+  }
+  void pre_multiply_all_xforms(const Mat4& m) { check(xr_rc_pre_multiply_all_xforms(h_, m.data())); }
+  void post_multiply_all_xforms(const Mat4& m) { check(xr_rc_post_multiply_all_xforms(h_, m.data())); }
+  int32_t num_vols() const { int32_t n = 0; check(xr_rc_num_vols(h_, &n)); return n; }
+  Mat4 xform_img_center_to_itk_phys(int32_t vol_idx = 0) const {
+    Mat4 m{};
+    check(xr_rc_xform_img_center_to_itk_phys(h_, vol_idx, m.data()));
+    return m;
+  }
+  Mat4 xform_cam_wrt_carm_center_of_rot(int32_t cam_idx = 0) const {
+    Mat4 m{};
+    check(xr_rc_xform_cam_wrt_carm_center_of_rot(h_, cam_idx, m.data()));
+    return m;
+  }
   void allocate_resources() { check(xr_rc_allocate_resources(h_)); }
   int64_t max_num_projs_possible() const { int64_t n = 0; check(xr_rc_max_num_projs_possible(h_, &n)); return n; }
   void compute(int32_t vol_idx = 0) { check(xr_rc_compute(h_, vol_idx)); }
@@ -278,6 +306,81 @@ class PopulationObjective {
 
  private:
   xr_objective h_ = nullptr;
+};
+
+// SimpleRayCasterWrapperFn (xregRayCastInterface.h:552-573, xregRayCastInterface.cpp:456-533):
+// one projection per camera of every volume in vols_to_proj (all volumes when
+// empty) at cam_world_to_vols[i], the first replacing and the rest accumulating,
+// optionally about intermediate frames; the ray caster's projection count and
+// camera associations are restored afterwards.
+struct SimpleRayCasterWrapperFn {
+  RayCasterLineIntCUDA* ray_caster = nullptr;
+  std::vector<Mat4> cam_world_to_vols;
+  std::vector<Mat4> inter_frames;
+  std::vector<bool> inter_frames_wrt_vol;
+  std::vector<Mat4> ref_frames_cam_world_to_vol;
+  std::vector<int32_t> vols_to_proj;
+  std::vector<std::vector<float>> projs;
+
+  static Mat4 mul(const Mat4& a, const Mat4& b) {
+    Mat4 t{};
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        double v = 0.0;
+        for (int k = 0; k < 4; ++k) v += a[(size_t)(i * 4 + k)] * b[(size_t)(k * 4 + j)];
+        t[(size_t)(i * 4 + j)] = v;
+      }
+    return t;
+  }
+  static Mat4 affine_inverse(const Mat4& m) {  // [A t; 0 1]^-1 = [A^-1, -A^-1 t]
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], k = m[10];
+    const double A = e * k - f * h, B = -(d * k - f * g), C = d * h - e * g;
+    const double det = a * A + b * B + c * C;
+    if (det == 0.0) throw Error(XR_ERR_INVALID_ARG, "SimpleRayCasterWrapperFn: singular intermediate frame");
+    const double inv[9] = {A / det, -(b * k - c * h) / det, (b * f - c * e) / det,
+                           B / det, (a * k - c * g) / det, -(a * f - c * d) / det,
+                           C / det, -(a * h - b * g) / det, (a * e - b * d) / det};
+    Mat4 t{};
+    for (int i = 0; i < 3; ++i) {
+      for (int j = 0; j < 3; ++j) t[(size_t)(i * 4 + j)] = inv[i * 3 + j];
+      t[(size_t)(i * 4 + 3)] = -(inv[i * 3] * m[3] + inv[i * 3 + 1] * m[7] + inv[i * 3 + 2] * m[11]);
+    }
+    t[15] = 1.0;
+    return t;
+  }
+
+  void operator()() {
+    RayCasterLineIntCUDA& rc = *ray_caster;
+    const bool listed = !vols_to_proj.empty();
+    const size_t nv = listed ? vols_to_proj.size() : (size_t)rc.num_vols();
+    if (cam_world_to_vols.size() != nv) throw Error(XR_ERR_INVALID_ARG, "SimpleRayCasterWrapperFn: one pose per volume");
+    const bool inter = !inter_frames.empty();
+    if (inter && (inter_frames.size() != nv || inter_frames_wrt_vol.size() != nv || ref_frames_cam_world_to_vol.size() != nv))
+      throw Error(XR_ERR_INVALID_ARG, "SimpleRayCasterWrapperFn: one intermediate frame per volume");
+    const int64_t num_cams = (int64_t)rc.num_camera_models();
+    const int64_t prev_num_projs = rc.num_projs();
+    const std::vector<int32_t> cam_assocs = rc.camera_model_proj_associations();
+    rc.set_num_projs(num_cams);
+    for (size_t v = 0; v < nv; ++v) {
+      if (v == 0) rc.use_proj_store_replace_method();
+      else rc.use_proj_store_accum_method();
+      rc.distribute_xform_among_cam_models(cam_world_to_vols[v]);
+      if (inter) {
+        if (inter_frames_wrt_vol[v]) {
+          rc.pre_multiply_all_xforms(inter_frames[v]);
+          rc.post_multiply_all_xforms(mul(affine_inverse(inter_frames[v]), ref_frames_cam_world_to_vol[v]));
+        } else {
+          rc.pre_multiply_all_xforms(mul(ref_frames_cam_world_to_vol[v], inter_frames[v]));
+          rc.post_multiply_all_xforms(affine_inverse(inter_frames[v]));
+        }
+      }
+      rc.compute(listed ? vols_to_proj[v] : (int32_t)v);
+    }
+    projs.assign((size_t)num_cams, {});
+    for (int64_t c = 0; c < num_cams; ++c) projs[(size_t)c] = rc.proj(c);
+    rc.set_num_projs(prev_num_projs);
+    if ((int64_t)cam_assocs.size() == prev_num_projs && prev_num_projs > 0) rc.set_camera_model_proj_associations(cam_assocs);
+  }
 };
 
 // Poses on disk (lib/itk/xregITKIOUtils.h:46-57), ITK text transform files.

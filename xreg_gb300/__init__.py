@@ -26,6 +26,7 @@ from .api import (  # noqa: F401
     proj_preproc,
     read_itk_affine_transform,
     read_slicer_affine_transform,
+    simple_ray_cast,
     write_itk_affine_transform,
 )
 

@@ -95,6 +95,15 @@ _SIGS = {
     "xr_rc_distribute_xforms_among_cam_models": [H, i64, P],
     "xr_rc_distribute_xforms_device": [H, i64, P],
     "xr_rc_set_camera_model_proj_associations": [H, i64, P],
+    "xr_rc_camera_model_proj_associations": [H, i64, P, C.POINTER(i64)],
+    "xr_rc_set_proj_cam_model": [H, i64, i32],
+    "xr_rc_xforms_cam_to_itk_phys": [H, i64, P, C.POINTER(i64)],
+    "xr_rc_pre_multiply_all_xforms": [H, P],
+    "xr_rc_post_multiply_all_xforms": [H, P],
+    "xr_rc_num_vols": [H, C.POINTER(i32)],
+    "xr_rc_num_camera_models": [H, C.POINTER(i32)],
+    "xr_rc_xform_img_center_to_itk_phys": [H, i32, P],
+    "xr_rc_xform_cam_wrt_carm_center_of_rot": [H, i32, P],
     "xr_rc_allocate_resources": [H],
     "xr_rc_max_num_projs_possible": [H, C.POINTER(i64)],
     "xr_rc_compute": [H, i32],

@@ -246,6 +246,52 @@ class RayCasterLineIntCUDA:
         a = np.ascontiguousarray(np.asarray(cam_idx, dtype=np.int32))
         call("xr_rc_set_camera_model_proj_associations", self._h, a.shape[0], _ptr(a))
 
+    def camera_model_proj_associations(self) -> np.ndarray:
+        n = C.c_int64()
+        call("xr_rc_camera_model_proj_associations", self._h, 0, None, C.byref(n))
+        out = np.empty(n.value, dtype=np.int32)
+        call("xr_rc_camera_model_proj_associations", self._h, n.value, _ptr(out), C.byref(n))
+        return out
+
+    def set_proj_cam_model(self, proj_idx: int, cam_idx: int) -> None:
+        call("xr_rc_set_proj_cam_model", self._h, int(proj_idx), int(cam_idx))
+
+    def xforms_cam_to_itk_phys(self) -> np.ndarray:
+        """Every projection's pose, [num_projs, 4, 4]."""
+        n = C.c_int64()
+        call("xr_rc_xforms_cam_to_itk_phys", self._h, 0, None, C.byref(n))
+        out = np.empty((n.value, 4, 4), dtype=np.float64)
+        call("xr_rc_xforms_cam_to_itk_phys", self._h, n.value, _ptr(out), C.byref(n))
+        return out
+
+    def pre_multiply_all_xforms(self, pre_xform) -> None:
+        m = np.ascontiguousarray(np.asarray(pre_xform, dtype=np.float64).reshape(4, 4))
+        call("xr_rc_pre_multiply_all_xforms", self._h, _ptr(m))
+
+    def post_multiply_all_xforms(self, post_xform) -> None:
+        m = np.ascontiguousarray(np.asarray(post_xform, dtype=np.float64).reshape(4, 4))
+        call("xr_rc_post_multiply_all_xforms", self._h, _ptr(m))
+
+    def num_vols(self) -> int:
+        v = C.c_int32()
+        call("xr_rc_num_vols", self._h, C.byref(v))
+        return v.value
+
+    def num_camera_models(self) -> int:
+        v = C.c_int32()
+        call("xr_rc_num_camera_models", self._h, C.byref(v))
+        return v.value
+
+    def xform_img_center_to_itk_phys(self, vol_idx: int = 0) -> np.ndarray:
+        out = np.empty((4, 4), dtype=np.float64)
+        call("xr_rc_xform_img_center_to_itk_phys", self._h, int(vol_idx), _ptr(out))
+        return out
+
+    def xform_cam_wrt_carm_center_of_rot(self, cam_idx: int = 0) -> np.ndarray:
+        out = np.empty((4, 4), dtype=np.float64)
+        call("xr_rc_xform_cam_wrt_carm_center_of_rot", self._h, int(cam_idx), _ptr(out))
+        return out
+
     def allocate_resources(self) -> None:
         call("xr_rc_allocate_resources", self._h)
 
@@ -676,3 +722,44 @@ def write_itk_affine_transform(path: str, xform) -> None:
     text transform file (xr_itk_affine_transform_write)."""
     x = np.ascontiguousarray(np.asarray(xform, dtype=np.float64).reshape(4, 4))
     call("xr_itk_affine_transform_write", os.fsencode(path), x.ctypes.data_as(C.c_void_p))
+
+
+def simple_ray_cast(rc: RayCasterLineIntCUDA, cam_world_to_vols, inter_frames=None, inter_frames_wrt_vol=None,
+                    ref_frames_cam_world_to_vol=None, vols_to_proj=None) -> list:
+    """SimpleRayCasterWrapperFn (xregRayCastInterface.cpp:456-533): one projection
+    per camera of every volume in vols_to_proj (all when None) at
+    cam_world_to_vols[i], the first replacing and the rest accumulating, about
+    optional intermediate frames; returns the projection of each camera and
+    restores the caster's projection count and camera associations."""
+    nv = len(vols_to_proj) if vols_to_proj is not None else rc.num_vols()
+    poses = [np.asarray(x, dtype=np.float64).reshape(4, 4) for x in cam_world_to_vols]
+    if len(poses) != nv:
+        raise ValueError("simple_ray_cast: one pose per volume")
+    inter = inter_frames is not None and len(inter_frames) > 0
+    if inter and not (len(inter_frames) == nv == len(inter_frames_wrt_vol) == len(ref_frames_cam_world_to_vol)):
+        raise ValueError("simple_ray_cast: one intermediate frame per volume")
+    ncam = rc.num_camera_models()
+    prev_n = rc.num_projs()
+    assocs = rc.camera_model_proj_associations()
+    rc.set_num_projs(ncam)
+    for v in range(nv):
+        if v == 0:
+            rc.use_proj_store_replace_method()
+        else:
+            rc.use_proj_store_accum_method()
+        rc.distribute_xforms_among_cam_models(poses[v][None])
+        if inter:
+            F = np.asarray(inter_frames[v], dtype=np.float64).reshape(4, 4)
+            R = np.asarray(ref_frames_cam_world_to_vol[v], dtype=np.float64).reshape(4, 4)
+            if inter_frames_wrt_vol[v]:
+                rc.pre_multiply_all_xforms(F)
+                rc.post_multiply_all_xforms(np.linalg.inv(F) @ R)
+            else:
+                rc.pre_multiply_all_xforms(R @ F)
+                rc.post_multiply_all_xforms(np.linalg.inv(F))
+        rc.compute(int(vols_to_proj[v]) if vols_to_proj is not None else v)
+    projs = [rc.proj(c) for c in range(ncam)]
+    rc.set_num_projs(prev_n)
+    if prev_n > 0 and assocs.size == prev_n:
+        rc.set_camera_model_proj_associations(assocs)
+    return projs

@@ -637,6 +637,123 @@ extern "C" XR_API xr_status xr_rc_distribute_xforms_among_cam_models(xr_raycaste
   return XR_OK;
 }
 
+namespace {
+void mat4_mul(const double* a, const double* b, double* out) {
+  double t[16];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 4; ++k) s += a[i * 4 + k] * b[k * 4 + j];
+      t[i * 4 + j] = s;
+    }
+  std::memcpy(out, t, sizeof(t));
+}
+}  // namespace
+
+// The poses on the host, current (copied back when they were given on the device).
+static xr_status rc_host_xforms(xr_raycaster rc, const char* fn) {
+  if (rc->pose_count <= 0) return fail(XR_ERR_INVALID_ARG, std::string(fn) + ": no projection transforms were set");
+  if (rc->xforms_on_device) {
+    DeviceGuard g(rc->device);
+    rc->xforms.resize((size_t)rc->pose_count * 16);
+    XR_CUDA_TRY(cudaMemcpyAsync(rc->xforms.data(), rc->d_xforms.p, (size_t)rc->pose_count * 16 * 8,
+                                cudaMemcpyDeviceToHost, rc->stream()));
+    XR_CUDA_TRY(cudaStreamSynchronize(rc->stream()));
+    rc->xforms_on_device = false;
+  }
+  return XR_OK;
+}
+
+// RayCaster::pre_multiply_all_xforms / post_multiply_all_xforms
+// (xregRayCastInterface.cpp:235-261), in double.
+static xr_status rc_multiply_all(xr_raycaster rc, const double* m, bool pre, const char* fn) {
+  XR_CHECK_ARG(rc && m, std::string(fn) + ": NULL argument");
+  XR_CHECK_ARG(finite_all(m, 16), std::string(fn) + ": non-finite transform");
+  xr_status st = rc_host_xforms(rc, fn);
+  if (st != XR_OK) return st;
+  for (int64_t k = 0; k < rc->pose_count; ++k) {
+    double* x = rc->xforms.data() + 16 * k;
+    if (pre) mat4_mul(m, x, x);
+    else mat4_mul(x, m, x);
+  }
+  rc->xforms_dirty = true;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_pre_multiply_all_xforms(xr_raycaster rc, const double* pre_xform) {
+  return rc_multiply_all(rc, pre_xform, true, "pre_multiply_all_xforms");
+}
+
+extern "C" XR_API xr_status xr_rc_post_multiply_all_xforms(xr_raycaster rc, const double* post_xform) {
+  return rc_multiply_all(rc, post_xform, false, "post_multiply_all_xforms");
+}
+
+extern "C" XR_API xr_status xr_rc_xforms_cam_to_itk_phys(xr_raycaster rc, int64_t cap, double* out, int64_t* count) {
+  XR_CHECK_ARG(rc && count && (out || cap == 0), "xforms_cam_to_itk_phys: NULL argument");
+  *count = rc->pose_count > 0 ? rc->num_projs : 0;
+  if (cap <= 0 || *count == 0) return XR_OK;
+  xr_status st = rc_host_xforms(rc, "xforms_cam_to_itk_phys");
+  if (st != XR_OK) return st;
+  for (int64_t p = 0; p < std::min(cap, *count); ++p)
+    std::memcpy(out + 16 * p, rc->xforms.data() + 16 * (p % rc->pose_count), 16 * sizeof(double));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_camera_model_proj_associations(xr_raycaster rc, int64_t cap, int32_t* out,
+                                                                int64_t* count) {
+  XR_CHECK_ARG(rc && count && (out || cap == 0), "camera_model_proj_associations: NULL argument");
+  *count = (int64_t)rc->cam_idx.size();
+  for (int64_t p = 0; p < std::min(cap, *count); ++p) out[p] = rc->cam_idx[(size_t)p];
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_set_proj_cam_model(xr_raycaster rc, int64_t proj_idx, int32_t cam_idx) {
+  XR_CHECK_ARG(rc, "set_proj_cam_model: NULL handle");
+  XR_CHECK_ARG(proj_idx >= 0 && proj_idx < (int64_t)rc->cam_idx.size(), "set_proj_cam_model: bad projection");
+  XR_CHECK_ARG(cam_idx >= 0 && cam_idx < (int32_t)rc->cams.size(), "set_proj_cam_model: bad camera");
+  rc->cam_idx[(size_t)proj_idx] = cam_idx;
+  rc->cam_idx_dirty = true;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_num_vols(xr_raycaster rc, int32_t* out) {
+  XR_CHECK_ARG(rc && out, "num_vols: NULL argument");
+  *out = (int32_t)rc->vols.size();
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_num_camera_models(xr_raycaster rc, int32_t* out) {
+  XR_CHECK_ARG(rc && out, "num_camera_models: NULL argument");
+  *out = (int32_t)rc->cams.size();
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_xform_img_center_to_itk_phys(xr_raycaster rc, int32_t vol_idx, double* out) {
+  XR_CHECK_ARG(rc && out, "xform_img_center_to_itk_phys: NULL argument");
+  XR_CHECK_ARG(vol_idx >= 0 && vol_idx < (int32_t)rc->vols.size(), "xform_img_center_to_itk_phys: bad volume index");
+  const xr_volume_desc& d = rc->vols[(size_t)vol_idx]->desc;
+  double c[3];
+  for (int i = 0; i < 3; ++i) {
+    // continuous index size / 2 (not (size - 1) / 2) to ITK physical coordinates
+    double v = d.origin[i];
+    for (int k = 0; k < 3; ++k) v += d.direction[i * 3 + k] * d.spacing[k] * ((double)d.n[k] / 2.0);
+    c[i] = v;
+  }
+  for (int i = 0; i < 16; ++i) out[i] = (i % 5 == 0) ? 1.0 : 0.0;
+  out[3] = c[0];
+  out[7] = c[1];
+  out[11] = c[2];
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_xform_cam_wrt_carm_center_of_rot(xr_raycaster rc, int32_t cam_idx, double* out) {
+  XR_CHECK_ARG(rc && out, "xform_cam_wrt_carm_center_of_rot: NULL argument");
+  XR_CHECK_ARG(cam_idx >= 0 && cam_idx < (int32_t)rc->cams.size(), "xform_cam_wrt_carm_center_of_rot: bad camera");
+  for (int i = 0; i < 16; ++i) out[i] = (i % 5 == 0) ? 1.0 : 0.0;
+  out[11] = -rc->cams[(size_t)cam_idx].focal_len / 2.0;
+  return XR_OK;
+}
+
 extern "C" XR_API xr_status xr_rc_set_camera_model_proj_associations(xr_raycaster rc, int64_t n, const int32_t* ci) {
   XR_CHECK_ARG(rc && ci, "set_camera_model_proj_associations: NULL argument");
   XR_CHECK_ARG(n == rc->num_projs, "set_camera_model_proj_associations: size must equal num_projs");
