@@ -252,6 +252,13 @@ XR_API xr_status xr_sm_set_fixed_image(xr_simmetric sm, const float* host_img, i
 XR_API xr_status xr_sm_set_mask(xr_simmetric sm, const uint8_t* host_mask);
 /* set_num_moving_images (xregImgSimMetric2D.h:93). */
 XR_API xr_status xr_sm_set_num_moving_images(xr_simmetric sm, int64_t n);
+/* fixed_image, mask, num_pix_per_proj (xregImgSimMetric2D.h:72,132,139) and the
+ * moving-image count: the fixed image as set (rows, cols; up to cap values), the
+ * mask (*has_mask = 0 when none) and rows * cols. */
+XR_API xr_status xr_sm_fixed_image(xr_simmetric sm, int64_t cap, float* out, int64_t* rows, int64_t* cols);
+XR_API xr_status xr_sm_mask(xr_simmetric sm, int64_t cap, uint8_t* out, int32_t* has_mask);
+XR_API xr_status xr_sm_num_pix_per_proj(xr_simmetric sm, int64_t* out);
+XR_API xr_status xr_sm_num_moving_images(xr_simmetric sm, int64_t* out);
 /* set_mov_imgs_buf_from_ray_caster (xregImgSimMetric2DCPU.cpp:43-72): the moving
  * images are read in place from the ray caster's device buffer at proj_offset. */
 XR_API xr_status xr_sm_set_mov_imgs_buf_from_ray_caster(xr_simmetric sm, xr_raycaster rc, int64_t proj_offset);

@@ -176,6 +176,22 @@ class ImgSimMetric2DCUDA {
   void set_mask(const uint8_t* mask) { check(xr_sm_set_mask(h_, mask)); }
   void set_num_moving_images(int64_t n) { check(xr_sm_set_num_moving_images(h_, n)); n_ = n; }
   int64_t num_moving_images() const { return n_; }
+  int64_t num_pix_per_proj() const { int64_t n = 0; check(xr_sm_num_pix_per_proj(h_, &n)); return n; }
+  // fixed_image / mask (xregImgSimMetric2D.h:72,132): host copies (rows * cols values; empty mask = none)
+  std::vector<float> fixed_image() const {
+    int64_t r = 0, c = 0;
+    check(xr_sm_fixed_image(h_, 0, nullptr, &r, &c));
+    std::vector<float> out((size_t)(r * c));
+    check(xr_sm_fixed_image(h_, r * c, out.data(), &r, &c));
+    return out;
+  }
+  std::vector<uint8_t> mask() const {
+    std::vector<uint8_t> out((size_t)num_pix_per_proj());
+    int32_t has = 0;
+    check(xr_sm_mask(h_, (int64_t)out.size(), out.data(), &has));
+    if (!has) out.clear();
+    return out;
+  }
   void set_mov_imgs_buf_from_ray_caster(RayCasterLineIntCUDA* rc, int64_t proj_offset = 0) {
     check(xr_sm_set_mov_imgs_buf_from_ray_caster(h_, rc->handle(), proj_offset));
   }

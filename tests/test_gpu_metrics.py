@@ -149,3 +149,20 @@ def test_host_buffer_input(xr, oracle):
     host[:] = imgs[2:7]  # the buffer is read again at every compute
     m.compute()
     np.testing.assert_allclose(m.sim_vals(), oracle.grad_ncc(fixed, imgs[2:7]), atol=TOL, rtol=0)
+
+
+def test_metric_getters(xr):
+    """fixed_image, mask, num_pix_per_proj and num_moving_images return what was set."""
+    rng = np.random.default_rng(21)
+    fixed = rng.random((33, 40)).astype(np.float32)
+    mask = (rng.random((33, 40)) > 0.3).astype(np.uint8)
+    m = xr.ImgSimMetric2DGradNCCCUDA()
+    m.set_fixed_image(fixed)
+    assert m.mask() is None
+    m.set_mask(mask)
+    m.set_num_moving_images(3)
+    np.testing.assert_array_equal(m.fixed_image(), fixed)
+    np.testing.assert_array_equal(m.mask(), mask)
+    assert m.num_pix_per_proj() == 33 * 40 and m.num_moving_images() == 3
+    m.set_mask(None)
+    assert m.mask() is None

@@ -139,6 +139,10 @@ _SIGS = {
     "xr_sm_patch_indices_used": [H, i64, P, C.POINTER(i64)],
     "xr_sm_patch_scores": [H, i64, i64, P, C.POINTER(i64)],
     "xr_sm_set_patches_to_use": [H, i64, P],
+    "xr_sm_fixed_image": [H, i64, P, C.POINTER(i64), C.POINTER(i64)],
+    "xr_sm_mask": [H, i64, P, C.POINTER(i32)],
+    "xr_sm_num_pix_per_proj": [H, C.POINTER(i64)],
+    "xr_sm_num_moving_images": [H, C.POINTER(i64)],
     "xr_sm_allocate_resources": [H],
     "xr_sm_compute": [H],
     "xr_sm_sim_vals": [H, P],

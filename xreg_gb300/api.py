@@ -418,6 +418,35 @@ class ImgSimMetric2DCUDA:
         self._n = int(n)
 
     def num_moving_images(self) -> int:
+        v = C.c_int64()
+        call("xr_sm_num_moving_images", self._h, C.byref(v))
+        return v.value
+
+    def num_pix_per_proj(self) -> int:
+        v = C.c_int64()
+        call("xr_sm_num_pix_per_proj", self._h, C.byref(v))
+        return v.value
+
+    def fixed_image(self) -> np.ndarray:
+        r, c = C.c_int64(), C.c_int64()
+        call("xr_sm_fixed_image", self._h, 0, None, C.byref(r), C.byref(c))
+        out = np.empty((r.value, c.value), dtype=np.float32)
+        call("xr_sm_fixed_image", self._h, out.size, _ptr(out), C.byref(r), C.byref(c))
+        return out
+
+    def mask(self):
+        """The mask as set, or None."""
+        has = C.c_int32()
+        n = self.num_pix_per_proj()
+        out = np.empty(n, dtype=np.uint8)
+        call("xr_sm_mask", self._h, n, _ptr(out), C.byref(has))
+        if not has.value:
+            return None
+        r, c = C.c_int64(), C.c_int64()
+        call("xr_sm_fixed_image", self._h, 0, None, C.byref(r), C.byref(c))
+        return out.reshape(r.value, c.value)
+
+    def num_moving_images(self) -> int:
         return self._n
 
     def set_mov_imgs_buf_from_ray_caster(self, rc: RayCasterLineIntCUDA, proj_offset: int = 0) -> None:

@@ -1296,6 +1296,38 @@ extern "C" XR_API xr_status xr_sm_set_mask(xr_simmetric sm, const uint8_t* mask)
   return XR_OK;
 }
 
+extern "C" XR_API xr_status xr_sm_fixed_image(xr_simmetric sm, int64_t cap, float* out, int64_t* rows, int64_t* cols) {
+  XR_CHECK_ARG(sm && rows && cols && (out || cap == 0), "fixed_image: NULL argument");
+  XR_CHECK_ARG(sm->has_fixed, "fixed_image: no fixed image");
+  *rows = sm->rows;
+  *cols = sm->cols;
+  const int64_t n = std::min<int64_t>(cap, sm->rows * sm->cols);
+  if (n <= 0) return XR_OK;
+  DeviceGuard g(sm->device);
+  XR_CUDA_TRY(cudaMemcpy(out, sm->d_fixed.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_mask(xr_simmetric sm, int64_t cap, uint8_t* out, int32_t* has_mask) {
+  XR_CHECK_ARG(sm && has_mask && (out || cap == 0), "mask: NULL argument");
+  *has_mask = sm->has_mask ? 1 : 0;
+  const int64_t n = sm->has_mask ? std::min<int64_t>(cap, (int64_t)sm->h_mask.size()) : 0;
+  if (n > 0) std::memcpy(out, sm->h_mask.data(), (size_t)n);
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_num_pix_per_proj(xr_simmetric sm, int64_t* out) {
+  XR_CHECK_ARG(sm && out, "num_pix_per_proj: NULL argument");
+  *out = sm->rows * sm->cols;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_sm_num_moving_images(xr_simmetric sm, int64_t* out) {
+  XR_CHECK_ARG(sm && out, "num_moving_images: NULL argument");
+  *out = sm->num_mov;
+  return XR_OK;
+}
+
 extern "C" XR_API xr_status xr_sm_set_num_moving_images(xr_simmetric sm, int64_t n) {
   XR_CHECK_ARG(sm && n > 0, "set_num_moving_images: NULL handle or non-positive count");
   XR_CHECK_ARG(!sm->allocated || n <= sm->capacity,
