@@ -219,8 +219,8 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
 // (-inf backward) when none is met before kend.  Macro cell m spans continuous
 // index [8m, 8m + 8) on each axis; positions are clamped to cells as the
 // sampler does.  The walk is bounded by the number of macro cells on a line.
-__device__ __forceinline__ float macro_march(const VolView& v, const float p0[3], const float st[3], float kstart,
-                                             float kend, int dir) {
+__device__ __forceinline__ float macro_march(const VolView& v, const float p0[3], const float st[3],
+                                             const float inv[3], float kstart, float kend, int dir) {
   const int nm[3] = {v.nmx, v.nmy, v.nmz};
   const int n2[3] = {v.nx - 2, v.ny - 2, v.nz - 2};
   int m[3];
@@ -229,6 +229,9 @@ __device__ __forceinline__ float macro_march(const VolView& v, const float p0[3]
     const float q = p0[a] + kstart * st[a];
     m[a] = max(min(__float2int_rd(q), n2[a]), 0) >> kMacroShift;
   }
+  // inv = 1 / st, formed once per ray (a division per axis and step cost more
+  // than the samples the walk saves): the boundary parameters carry a few ulps
+  // of error, far inside the one-sample margin the caller leaves on each side.
   float k = kstart;
   const int cap = nm[0] + nm[1] + nm[2] + 3;
   for (int it = 0; it < cap; ++it) {
@@ -252,7 +255,7 @@ __device__ __forceinline__ float macro_march(const VolView& v, const float p0[3]
       } else {
         continue;
       }
-      const float kk = (bound - p0[a]) / st[a];
+      const float kk = (bound - p0[a]) * inv[a];
       const float tt = dir > 0 ? kk : -kk;  // increases along the walk
       if (tt < best) { best = tt; knext = kk; ax = a; dm = step; }
     }
@@ -398,6 +401,8 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
       }
       const float sc = __fdiv_rn(p.step, lc);
       const float sx = __fmul_rn(dir[0], sc), sy = __fmul_rn(dir[1], sc), sz = __fmul_rn(dir[2], sc);
+      // reciprocal steps for the skipping bounds (never for sample positions)
+      const float inv_st[3] = {1.0f / sx, 1.0f / sy, 1.0f / sz};
       const void* data = (LAYOUT != XR_LAYOUT_LINEAR) ? p.vol.cells : p.vol.voxels;
       // Samples [first, last] may touch non-zero voxels; the others interpolate
       // only zeros, so for the sum they add exactly +0 and need no load.  The
@@ -411,7 +416,8 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           if (fabsf(st[k]) > 1.0e-20f) {
-            float a = (p.vol.sup_lo[k] - p0[k]) / st[k], b = (p.vol.sup_hi[k] - p0[k]) / st[k];
+            // reciprocal steps: a few ulps of error, inside the one-sample margins below
+            float a = (p.vol.sup_lo[k] - p0[k]) * inv_st[k], b = (p.vol.sup_hi[k] - p0[k]) * inv_st[k];
             if (a > b) { const float t = a; a = b; b = t; }
             lo = fmaxf(lo, a);
             hi = fminf(hi, b);
@@ -441,14 +447,14 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
         if (ebits <= 22 && last < (1u << (22 - ebits))) {
           trim_ok = true;
           const float p0[3] = {px, py, pz}, st[3] = {sx, sy, sz};
-          const float kf = macro_march(p.vol, p0, st, (float)first, (float)last, 1);
+          const float kf = macro_march(p.vol, p0, st, inv_st, (float)first, (float)last, 1);
           if (kf == INFINITY) {
             first = 1u;
             last = 0u;  // every sample is zero
           } else {
             const float f = floorf(kf) - 1.0f;
             if (f > (float)first) first = (unsigned int)f;
-            const float kl = macro_march(p.vol, p0, st, (float)last, (float)first, -1);
+            const float kl = macro_march(p.vol, p0, st, inv_st, (float)last, (float)first, -1);
             if (kl == -INFINITY) {
               first = 1u;
               last = 0u;
