@@ -292,34 +292,99 @@ __global__ void __launch_bounds__(kThreads) grad_images_kernel(const float* __re
   }
 }
 
+// Moments of the moving gradients over a 32 x 64-pixel tile per block: each
+// thread owns one column and eight consecutive rows, so the Sobel stencil slides
+// down the column (three shared-memory reads per pixel) and the block reduction
+// is paid once per 2048 pixels.  Per-thread sums are plain float (eight terms);
+// the float-float tree keeps the long sums accurate.  Gradients use the same
+// expressions as GradTile::sobel (identical values).
+constexpr int kGW = 32;                           // tile columns = threads across
+constexpr int kGR = 8;                            // rows per thread
+constexpr int kGH = kGR * (kThreads / kGW);       // tile rows (64)
+
 template <int KR>
 __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __restrict__ imgs, int rows, int cols,
                                                                 const float* __restrict__ fhx,
                                                                 const float* __restrict__ fhy,
                                                                 const uint8_t* __restrict__ mask,
                                                                 double* __restrict__ partials) {
-  __shared__ GradTile<KR> t;
+  constexpr int H = KR + 1;                       // halo: blur radius + Sobel
+  constexpr int WI = kGW + 2 * H, HI = kGH + 2 * H;
+  constexpr int WB = kGW + 2, HB = kGH + 2;       // blurred region (Sobel halo)
+  constexpr int NT = kThreads / kGW;              // thread rows (8)
+  __shared__ float s_in[HI][WI + 1];
+  __shared__ float s_hb[KR > 0 ? HI : 1][WB + 1];
+  __shared__ float s_bl[HB][WB + 1];
   __shared__ FF red[6 * 32];
-  const int tiles_x = (cols + kT - 1) / kT;
-  const int y0 = (blockIdx.x / tiles_x) * kT, x0 = (blockIdx.x % tiles_x) * kT;
+  const int tx = threadIdx.x % kGW, ty = threadIdx.x / kGW;
+  const int tiles_x = (cols + kGW - 1) / kGW;
+  const int y0 = (blockIdx.x / tiles_x) * kGH, x0 = (blockIdx.x % tiles_x) * kGW;
   const int64_t npix = (int64_t)rows * cols;
   const int64_t img = blockIdx.y;
-  t.load(imgs + img * npix, rows, cols, y0, x0);
-  t.blur();
-  Kahan s[6];
-  for (int i = threadIdx.x; i < kT * kT; i += blockDim.x) {
-    const int ty = i / kT, tx = i - ty * kT;
-    if (y0 + ty >= rows || x0 + tx >= cols) continue;
-    const int64_t pix = (int64_t)(y0 + ty) * cols + x0 + tx;
-    if (mask && !mask[pix]) continue;
-    float a, b;
-    t.sobel(ty, tx, a, b);
-    s[0].add(a); s[1].add(a * a); s[2].add(a * fhx[pix]);
-    s[3].add(b); s[4].add(b * b); s[5].add(b * fhy[pix]);
+  const float* src = imgs + img * npix;
+  // stage the tile and its halo; reflect-101 only for tiles touching a border
+  // (rows / cols past the last tile pixel only feed pixels that are skipped)
+  const bool interior = y0 >= H && x0 >= H && y0 + kGH + H <= rows && x0 + kGW + H <= cols;
+  for (int r = ty; r < HI; r += NT)
+    for (int c = tx; c < WI; c += kGW) {
+      int gr = y0 - H + r, gc = x0 - H + c;
+      if (!interior) {
+        gr = reflect101(min(gr, rows - 1 + H), rows);
+        gc = reflect101(min(gc, cols - 1 + H), cols);
+      }
+      s_in[r][c] = src[(int64_t)gr * cols + gc];
+    }
+  __syncthreads();
+  if constexpr (KR == 0) {
+    for (int r = ty; r < HB; r += NT)
+      for (int c = tx; c < WB; c += kGW) s_bl[r][c] = s_in[r][c];
+  } else {
+    for (int r = ty; r < HI; r += NT)
+      for (int c = tx; c < WB; c += kGW) {
+        const float* q = &s_in[r][c];
+        s_hb[r][c] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[1] + 0.375f * q[2] + 0.25f * q[3] + 0.0625f * q[4])
+                               : (0.25f * q[0] + 0.5f * q[1] + 0.25f * q[2]);
+      }
+    __syncthreads();
+    for (int r = ty; r < HB; r += NT)
+      for (int c = tx; c < WB; c += kGW) {
+        s_bl[r][c] = (KR == 2) ? (0.0625f * s_hb[r][c] + 0.25f * s_hb[r + 1][c] + 0.375f * s_hb[r + 2][c] +
+                                  0.25f * s_hb[r + 3][c] + 0.0625f * s_hb[r + 4][c])
+                               : (0.25f * s_hb[r][c] + 0.5f * s_hb[r + 1][c] + 0.25f * s_hb[r + 2][c]);
+      }
+  }
+  __syncthreads();
+  float m[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  const int gxc = x0 + tx;
+  if (gxc < cols) {
+    const int rb = ty * kGR;  // first output row (tile-local); blurred rows rb .. rb + kGR + 1
+    float a0 = s_bl[rb][tx], b0 = s_bl[rb][tx + 1], c0 = s_bl[rb][tx + 2];
+    float a1 = s_bl[rb + 1][tx], b1 = s_bl[rb + 1][tx + 1], c1 = s_bl[rb + 1][tx + 2];
+#pragma unroll
+    for (int k = 0; k < kGR; ++k) {
+      const float a2 = s_bl[rb + k + 2][tx], b2 = s_bl[rb + k + 2][tx + 1], c2 = s_bl[rb + k + 2][tx + 2];
+      const int gyr = y0 + rb + k;
+      if (gyr < rows) {
+        const int64_t pix = (int64_t)gyr * cols + gxc;
+        if (!mask || mask[pix]) {
+          // GradTile::sobel with a = a0, b = b0, cc = c0, d = a1, f = c1, g = a2, h = b2, ii = c2
+          const float gx = ((c0 - a0) + 2.0f * (c1 - a1)) + (c2 - a2);
+          const float gy = ((a2 - a0) + 2.0f * (b2 - b0)) + (c2 - c0);
+          m[0] += gx;
+          m[1] += gx * gx;
+          m[2] += gx * fhx[pix];
+          m[3] += gy;
+          m[4] += gy * gy;
+          m[5] += gy * fhy[pix];
+        }
+      }
+      a0 = a1; b0 = b1; c0 = c1;
+      a1 = a2; b1 = b2; c1 = c2;
+    }
   }
   FF f[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) f[k] = s[k].ff();
+  for (int k = 0; k < 6; ++k) f[k] = FF{m[k], 0.0f};
   double v[6];
   block_sum_ff<6>(f, v, red);
   if (threadIdx.x == 0) {
@@ -851,7 +916,7 @@ cudaError_t launch_grad_images(const float* img, int rows, int cols, int64_t nim
 cudaError_t launch_grad_moments(const float* mov, int rows, int cols, int64_t nimgs, int smooth_ksize,
                                 const float* fhat_x, const float* fhat_y, const uint8_t* mask, double* partials,
                                 cudaStream_t s, int* nblk_out) {
-  const int tiles = ((rows + kT - 1) / kT) * ((cols + kT - 1) / kT);
+  const int tiles = ((rows + kGH - 1) / kGH) * ((cols + kGW - 1) / kGW);
   if (nblk_out) *nblk_out = tiles;
   if (nimgs <= 0 || !partials) return cudaSuccess;
   const dim3 grid(tiles, (unsigned)nimgs);
