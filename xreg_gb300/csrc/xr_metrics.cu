@@ -295,9 +295,10 @@ __global__ void __launch_bounds__(kThreads) grad_images_kernel(const float* __re
 // Moments of the moving gradients over a 32 x 64-pixel tile per block: each
 // thread owns one column and eight consecutive rows, so the Sobel stencil slides
 // down the column (three shared-memory reads per pixel) and the block reduction
-// is paid once per 2048 pixels.  Per-thread sums are plain float (eight terms);
-// the float-float tree keeps the long sums accurate.  Gradients use the same
-// expressions as GradTile::sobel (identical values).
+// is paid once per 2048 pixels.  Sums are plain float per thread (8 terms) and
+// per warp (256 pixels), then float-float across warps and blocks, which keeps
+// the long image-wide sums accurate.  Gradients use the same expressions as
+// GradTile::sobel (identical values).
 constexpr int kGW = 32;                           // tile columns = threads across
 constexpr int kGR = 8;                            // rows per thread
 constexpr int kGH = kGR * (kThreads / kGW);       // tile rows (64)
@@ -382,11 +383,25 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
       a1 = a2; b1 = b2; c1 = c2;
     }
   }
-  FF f[6];
+  // plain-float sums within a warp (256 pixels), float-float across the warps
+  // and the blocks
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) f[k] = FF{m[k], 0.0f};
+  for (int k = 0; k < 6; ++k) {
+    float w = m[k];
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if (lane == 0) red[k * 32 + warp] = FF{w, 0.0f};
+  }
+  __syncthreads();
   double v[6];
-  block_sum_ff<6>(f, v, red);
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      FF w = (lane < kThreads / 32) ? red[k * 32 + lane] : FF{0.0f, 0.0f};
+      for (int o = 16; o > 0; o >>= 1) w = ff_add(w, ff_shfl_down(w, o));
+      v[k] = (double)w.hi + (double)w.lo;
+    }
+  }
   if (threadIdx.x == 0) {
     double* o = partials + (img * gridDim.x + blockIdx.x) * 6;
 #pragma unroll
