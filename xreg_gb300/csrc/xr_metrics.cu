@@ -312,7 +312,6 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
   constexpr int H = KR + 1;                       // halo: blur radius + Sobel
   constexpr int WI = kGW + 2 * H, HI = kGH + 2 * H;
   constexpr int WB = kGW + 2, HB = kGH + 2;       // blurred region (Sobel halo)
-  constexpr int NT = kThreads / kGW;              // thread rows (8)
   __shared__ float s_in[HI][WI + 1];
   __shared__ float s_hb[KR > 0 ? HI : 1][WB + 1];
   __shared__ float s_bl[HB][WB + 1];
@@ -325,34 +324,38 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
   const float* src = imgs + img * npix;
   // stage the tile and its halo; reflect-101 only for tiles touching a border
   // (rows / cols past the last tile pixel only feed pixels that are skipped)
+  // (flat loops over each region: its width is not a multiple of the warp, and
+  // the divisions by the constant widths are multiply-shifts)
   const bool interior = y0 >= H && x0 >= H && y0 + kGH + H <= rows && x0 + kGW + H <= cols;
-  for (int r = ty; r < HI; r += NT)
-    for (int c = tx; c < WI; c += kGW) {
-      int gr = y0 - H + r, gc = x0 - H + c;
-      if (!interior) {
-        gr = reflect101(min(gr, rows - 1 + H), rows);
-        gc = reflect101(min(gc, cols - 1 + H), cols);
-      }
-      s_in[r][c] = src[(int64_t)gr * cols + gc];
+  for (int i = threadIdx.x; i < HI * WI; i += kThreads) {
+    const int r = i / WI, c = i - r * WI;
+    int gr = y0 - H + r, gc = x0 - H + c;
+    if (!interior) {
+      gr = reflect101(min(gr, rows - 1 + H), rows);
+      gc = reflect101(min(gc, cols - 1 + H), cols);
     }
+    s_in[r][c] = src[(int64_t)gr * cols + gc];
+  }
   __syncthreads();
   if constexpr (KR == 0) {
-    for (int r = ty; r < HB; r += NT)
-      for (int c = tx; c < WB; c += kGW) s_bl[r][c] = s_in[r][c];
+    for (int i = threadIdx.x; i < HB * WB; i += kThreads) {
+      const int r = i / WB, c = i - r * WB;
+      s_bl[r][c] = s_in[r][c];
+    }
   } else {
-    for (int r = ty; r < HI; r += NT)
-      for (int c = tx; c < WB; c += kGW) {
-        const float* q = &s_in[r][c];
-        s_hb[r][c] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[1] + 0.375f * q[2] + 0.25f * q[3] + 0.0625f * q[4])
-                               : (0.25f * q[0] + 0.5f * q[1] + 0.25f * q[2]);
-      }
+    for (int i = threadIdx.x; i < HI * WB; i += kThreads) {
+      const int r = i / WB, c = i - r * WB;
+      const float* q = &s_in[r][c];
+      s_hb[r][c] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[1] + 0.375f * q[2] + 0.25f * q[3] + 0.0625f * q[4])
+                             : (0.25f * q[0] + 0.5f * q[1] + 0.25f * q[2]);
+    }
     __syncthreads();
-    for (int r = ty; r < HB; r += NT)
-      for (int c = tx; c < WB; c += kGW) {
-        s_bl[r][c] = (KR == 2) ? (0.0625f * s_hb[r][c] + 0.25f * s_hb[r + 1][c] + 0.375f * s_hb[r + 2][c] +
-                                  0.25f * s_hb[r + 3][c] + 0.0625f * s_hb[r + 4][c])
-                               : (0.25f * s_hb[r][c] + 0.5f * s_hb[r + 1][c] + 0.25f * s_hb[r + 2][c]);
-      }
+    for (int i = threadIdx.x; i < HB * WB; i += kThreads) {
+      const int r = i / WB, c = i - r * WB;
+      s_bl[r][c] = (KR == 2) ? (0.0625f * s_hb[r][c] + 0.25f * s_hb[r + 1][c] + 0.375f * s_hb[r + 2][c] +
+                                0.25f * s_hb[r + 3][c] + 0.0625f * s_hb[r + 4][c])
+                             : (0.25f * s_hb[r][c] + 0.5f * s_hb[r + 1][c] + 0.25f * s_hb[r + 2][c]);
+    }
   }
   __syncthreads();
   float m[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
