@@ -567,20 +567,28 @@ __device__ __forceinline__ float patch_var(const float* __restrict__ m, int P, i
 // from shared memory for every patch whose window holds it.  Per patch the
 // operations and their order are those of patch_score without a mask (sum in
 // row-major order, mean, then variance and covariance in row-major order), so
-// each score has the same bits.
-template <int RB>
+// each score has the same bits.  DC / SC > 0: the patch edge and stride known
+// at compile time (xReg's default 11 x 11, stride 1): each row's columns unroll
+// (no loop control or address arithmetic per element).
+template <int RB, int DC, int SC>
 __device__ __forceinline__ void patch_scores_rows(const float* __restrict__ m, const float* __restrict__ f, int Wc,
-                                                  int rbase, int c0, int d, int stride, const float (&fmean)[RB],
-                                                  const float (&fscale)[RB], float (&score)[RB]) {
+                                                  int rbase, int c0, int d_rt, int stride_rt,
+                                                  const float (&fmean)[RB], const float (&fscale)[RB],
+                                                  float (&score)[RB]) {
+  const int d = DC > 0 ? DC : d_rt;
+  const int stride = SC > 0 ? SC : stride_rt;
   const int span = (RB - 1) * stride + d;
+  constexpr int kUnroll = DC > 0 ? DC : 1;  // the columns of a patch row (the rows stay a loop: registers)
   float acc[RB], v[RB], cov[RB];
 #pragma unroll
   for (int j = 0; j < RB; ++j) { acc[j] = 0.0f; v[j] = 0.0f; cov[j] = 0.0f; }
+#pragma unroll 1
   for (int rr = 0; rr < span; ++rr) {
     bool in[RB];
 #pragma unroll
     for (int j = 0; j < RB; ++j) in[j] = rr >= j * stride && rr < j * stride + d;
     const float* row = m + (rbase + rr) * Wc + c0;
+#pragma unroll kUnroll
     for (int c = 0; c < d; ++c) {
       const float x = row[c];
 #pragma unroll
@@ -592,11 +600,13 @@ __device__ __forceinline__ void patch_scores_rows(const float* __restrict__ m, c
   float mu[RB];
 #pragma unroll
   for (int j = 0; j < RB; ++j) mu[j] = d * d > 1 ? acc[j] / n : acc[j];
+#pragma unroll 1
   for (int rr = 0; rr < span; ++rr) {
     bool in[RB];
 #pragma unroll
     for (int j = 0; j < RB; ++j) in[j] = rr >= j * stride && rr < j * stride + d;
     const int o = (rbase + rr) * Wc + c0;
+#pragma unroll kUnroll
     for (int c = 0; c < d; ++c) {
       const float x = m[o + c], fx = f[o + c];
 #pragma unroll
@@ -620,7 +630,7 @@ __device__ __forceinline__ void patch_scores_rows(const float* __restrict__ m, c
 // centre of count x moving-patch variance (the normaliser of variance weights).
 // PASS 1: per image and direction, the sum over used patches of
 // count x weight x score (weight 1 when not weighting in the combine).
-template <int GRAD, int KR, int PASS, int RB>
+template <int GRAD, int KR, int PASS, int RB, int DC = 0, int SC = 0>
 __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __restrict__ imgs, int rows, int cols,
                                                              int radius, int stride, int ncr, int ncc,
                                                              PatchFixed px, PatchFixed py, PatchRun run,
@@ -734,7 +744,8 @@ __global__ void __launch_bounds__(kThreads) patch_ncc_kernel(const float* __rest
             fs[j] = cnt[j] > 0 ? P.scale[pidx[j]] : 0.0f;
             w[j] = (cnt[j] > 0 && P.w) ? P.w[pidx[j]] : 1.0f;
           }
-          patch_scores_rows<RB>(k == 0 ? s_mx : s_my, k == 0 ? s_fx : s_fy, Wc, rbase, c0, d, stride, fm, fs, sc);
+          patch_scores_rows<RB, DC, SC>(k == 0 ? s_mx : s_my, k == 0 ? s_fx : s_fy, Wc, rbase, c0, d, stride, fm,
+                                        fs, sc);
 #pragma unroll
           for (int j = 0; j < RB; ++j)
             if (cnt[j] > 0 && (!run.weighted || fabsf(w[j]) > 1.0e-6f)) {
@@ -880,7 +891,9 @@ __global__ void combine_mean_kernel(ViewPtrs vp, int nviews, int64_t pop, float*
 
 template <typename K>
 cudaError_t set_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  // above the default 48 KB the kernel must opt in; the kernels' own static
+  // shared memory counts against the same 48 KB, so opt in with room to spare
+  if (bytes > 40 * 1024) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   return cudaSuccess;
 }
 
@@ -993,18 +1006,21 @@ cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs
   if (L.bytes > 200 * 1024) return cudaErrorInvalidValue;
   const dim3 grid(tiles, (unsigned)nimgs);
   cudaError_t e = cudaSuccess;
-#define XR_PATCH_LAUNCH(G, K, P, R)                                                                          \
-  e = set_smem(patch_ncc_kernel<G, K, P, R>, L.bytes);                                                      \
+#define XR_PATCH_R4_11_1 kPatchRows, 11, 1  // xReg's default patches: 11 x 11, stride 1
+#define XR_PATCH_LAUNCH(G, K, P, ...)                                                                        \
+  e = set_smem(patch_ncc_kernel<G, K, P, __VA_ARGS__>, L.bytes);                                            \
   if (e != cudaSuccess) return e;                                                                            \
-  patch_ncc_kernel<G, K, P, R><<<grid, kThreads, L.bytes, s>>>(mov, rows, cols, radius, stride, ncr, ncc, px, py, \
-                                                               run, partials);
-#define XR_PATCH_PASS(G, K)              \
-  if (rb > 1) {                          \
-    XR_PATCH_LAUNCH(G, K, 1, kPatchRows) \
-  } else if (pass == 0) {                \
-    XR_PATCH_LAUNCH(G, K, 0, 1)          \
-  } else {                               \
-    XR_PATCH_LAUNCH(G, K, 1, 1)          \
+  patch_ncc_kernel<G, K, P, __VA_ARGS__><<<grid, kThreads, L.bytes, s>>>(mov, rows, cols, radius, stride, ncr, ncc, \
+                                                                         px, py, run, partials);
+#define XR_PATCH_PASS(G, K)                                   \
+  if (rb > 1 && radius == 5 && stride == 1) {                 \
+    XR_PATCH_LAUNCH(G, K, 1, XR_PATCH_R4_11_1)                \
+  } else if (rb > 1) {                                        \
+    XR_PATCH_LAUNCH(G, K, 1, kPatchRows)                      \
+  } else if (pass == 0) {                                     \
+    XR_PATCH_LAUNCH(G, K, 0, 1)                               \
+  } else {                                                    \
+    XR_PATCH_LAUNCH(G, K, 1, 1)                               \
   }
   if (!grad) {
     XR_PATCH_PASS(0, 0)
@@ -1017,6 +1033,7 @@ cudaError_t launch_patch_ncc(const float* mov, int rows, int cols, int64_t nimgs
   }
 #undef XR_PATCH_PASS
 #undef XR_PATCH_LAUNCH
+#undef XR_PATCH_R4_11_1
   return cudaGetLastError();
 }
 
