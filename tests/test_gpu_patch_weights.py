@@ -337,3 +337,22 @@ def test_patches_to_use(xr, oracle, grad):
     with pytest.raises(Exception):
         m.set_patches_to_use([np_all])  # outside the grid: refused at allocate_resources
         m.allocate_resources()
+
+
+@pytest.mark.parametrize("grad", [0, 1])
+def test_every_patch_size_launches_and_matches(xr, oracle, grad):
+    """Every patch radius the API accepts (1-16) at strides 1 and 3, with and
+    without a mask: each tile shape and launch path (four patches per thread,
+    the compile-time 11 x 11 scorer, one patch per thread, shared memory above
+    48 KB) runs and matches the oracle."""
+    rc, imgs, fixed = _drrs(xr, det=(90, 76), seed=41, px=1.2)
+    mask = _mask(fixed.shape, 15)
+    cls = xr.ImgSimMetric2DPatchGradNCCCUDA if grad else xr.ImgSimMetric2DPatchNCCCUDA
+    fn = oracle.patch_grad_ncc_ex if grad else oracle.patch_ncc_ex
+    for radius in range(1, 17):
+        for stride in (1, 3):
+            for mk in (None, mask):
+                _, got = _eval(xr, cls, rc, fixed, 3, radius, stride, mask=mk)
+                ref = fn(fixed, imgs[1:4], radius=radius, stride=stride, mask=mk)
+                np.testing.assert_allclose(got, ref, atol=TOL, rtol=2e-6,
+                                           err_msg=f"radius {radius} stride {stride} masked {mk is not None}")
