@@ -100,6 +100,24 @@ int main(int argc, char** argv) {
     PopulationObjective obj(rc2, {&m2}, npose);
     write_all(dir + "/obj.f32", obj(poses));
 
+    // SimpleRayCasterWrapperFn about an intermediate frame (F, R from frames.f64)
+    const auto fr = read_all<double>(dir + "/frames.f64");
+    Mat4 F{}, R{};
+    for (int k = 0; k < 16; ++k) { F[(size_t)k] = fr[(size_t)k]; R[(size_t)k] = fr[(size_t)(16 + k)]; }
+    SimpleRayCasterWrapperFn wrap;
+    wrap.ray_caster = &rc2;
+    wrap.cam_world_to_vols = {poses[0]};
+    wrap.inter_frames = {F};
+    wrap.inter_frames_wrt_vol = {true};
+    wrap.ref_frames_cam_world_to_vol = {R};
+    wrap();
+    write_all(dir + "/wrap.f32", wrap.projs[0]);
+
+    // a pose through an ITK text transform file and back
+    WriteITKAffineTransform(dir + "/pose.txt", poses[1]);
+    const Mat4 back = ReadITKAffineTransformFromFile(dir + "/pose.txt");
+    write_all(dir + "/pose_back.f64", std::vector<double>(back.begin(), back.end()));
+
     // error path: unsupported interpolation surfaces as UnsupportedOperationException
     rc.set_interp_method(XR_INTERP_SINC);
     try {

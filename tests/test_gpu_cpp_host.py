@@ -47,6 +47,9 @@ def test_cpp_host_classes_match_oracle(xr, oracle, tmp_path):
     fixed.tofile(tmp_path / "fixed.f32")
     mask = (np.random.default_rng(7).random((rows, cols)) > 0.3).astype(np.uint8)
     mask.tofile(tmp_path / "mask.u8")
+    F = synth.perturb(vol, np.eye(4), [0.0, 3.0, 1.0], [2.0, 0.0, -1.0])
+    R = synth.perturb(vol, np.eye(4), [1.0, 0.0, 0.0], [0.0, 1.5, 0.0])
+    np.concatenate([F.ravel(), R.ravel()]).astype(np.float64).tofile(tmp_path / "frames.f64")
     r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     drr = np.fromfile(tmp_path / "drr.f32", np.float32).reshape(len(poses), rows, cols)
@@ -58,6 +61,15 @@ def test_cpp_host_classes_match_oracle(xr, oracle, tmp_path):
     ref_sims = oracle.grad_ncc(fixed, ref)
     np.testing.assert_allclose(sims, ref_sims, atol=1e-5, rtol=0)
     np.testing.assert_array_equal(obj, sims)
+    # SimpleRayCasterWrapperFn in the C++ header: pose F P F^-1 R
+    wrap = np.fromfile(tmp_path / "wrap.f32", np.float32).reshape(rows, cols)
+    ref_w = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams([cam]),
+                           (F @ poses[0] @ np.linalg.inv(F) @ R)[None], step=step)[0]
+    np.testing.assert_allclose(wrap, ref_w, rtol=1e-4, atol=1e-5)
+    back = np.fromfile(tmp_path / "pose_back.f64", np.float64).reshape(4, 4)
+    want = poses[1].astype(np.float32).astype(np.float64)
+    want[3] = [0, 0, 0, 1]
+    np.testing.assert_array_equal(back, want)
     psims = np.fromfile(tmp_path / "psims.f32", np.float32)
     ref_p = oracle.patch_ncc_ex(fixed, drr, radius=3, stride=2, mask=mask, use_mov_var_wgts=1)
     np.testing.assert_allclose(psims, ref_p, atol=1e-5, rtol=2e-6)
