@@ -667,6 +667,7 @@ def _serving(dev, n_req: int, rate: float):
                 "pose_error_mm_median": round(float(np.median([e[1] for e in errs])), 4),
                 "pose_error_deg_max": round(float(np.max([e[0] for e in errs])), 4),
                 "pose_error_mm_max": round(float(np.max([e[1] for e in errs])), 4),
+                "generation_step": "one xr_regi_jobset_step call per server step (sample, evaluate, update)",
                 "clocks": clk.summary()}
 
     # the headline rate three times (latency depends on how arrivals overlap the

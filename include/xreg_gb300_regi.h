@@ -40,6 +40,8 @@ XR_API xr_status xr_cmaes_update_distribution(xr_cmaes e, const double* fvals);
 XR_API xr_status xr_cmaes_test_termination(xr_cmaes e, int32_t* reason);
 /* Current mean, best candidate seen and its value, step size, generation count
  * (any pointer may be NULL). */
+/* Candidates per generation (lambda). */
+XR_API xr_status xr_cmaes_lambda(xr_cmaes e, int32_t* lambda);
 XR_API xr_status xr_cmaes_get(xr_cmaes e, double* mean, double* best_x, double* best_f, double* sigma,
                               int64_t* generation);
 
@@ -149,6 +151,35 @@ XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t num_jobs, const xr_
                                        const int64_t* pops, const double* const* d_xforms, float* const* d_sims);
 /* Work items and persistent blocks of the last launch. */
 XR_API xr_status xr_jobset_last_launch(xr_jobset js, int64_t* work_items, int32_t* blocks);
+
+/* One generation of several registrations in one call: for each job the loop
+ * body of Intensity2D3DRegiCMAES::run (xregIntensity2D3DRegiCMAES.cpp:154-226:
+ * sample, redraw candidates outside the bounds, evaluate, update, test for
+ * termination) or of the trust-region level (ask, evaluate, tell, test), with
+ * every job's population evaluated by ONE xr_jobset_eval.  The optimizer state
+ * lives in the caller's xr_cmaes / xr_dfo handle, which advances here; the
+ * offsets x map to poses  centre * ExpSE3(x) * centre^-1 * start_pose  as in
+ * xr_regi_run_level.  stop[i] receives job i's termination reason (0 = keep
+ * going; xr_cmaes_test_termination / xr_dfo_test_termination codes). */
+typedef struct {
+  xr_objective obj;
+  int32_t optimizer;   /* XR_REGI_CMAES (opt is an xr_cmaes) or XR_REGI_DFO (an xr_dfo) */
+  int32_t reserved;    /* 0 */
+  void* opt;
+  double centre[16];
+  double start_pose[16];
+  double bounds[6];    /* CMA-ES: |x_i| <= bounds[i] (0 = unbounded) */
+} xr_regi_step_job;
+XR_API xr_status xr_regi_jobset_step(xr_jobset js, int32_t num_jobs, const xr_regi_step_job* jobs, int32_t* stop,
+                                     int32_t* evaluated /* [num_jobs] poses evaluated per job, or NULL */);
+
+/* The pose of each parameter vector x (an se(3) tangent: 3 rotation, 3
+ * translation) in a registration level: pose = C * Exp(x) * C^-1 * start_pose,
+ * C the centre of rotation frame (Intensity2D3DRegiCMAES::run's
+ * SE3OptVarsLieAlg x centre-of-rotation composition, xregIntensity2D3DRegiCMAES.cpp).
+ * xs [n, 6], poses [n, 16] row-major; the map every level driver here uses. */
+XR_API xr_status xr_regi_pose_map(const double* centre, const double* start_pose, int64_t n, const double* xs,
+                                  double* poses);
 
 #ifdef __cplusplus
 }

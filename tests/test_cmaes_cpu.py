@@ -138,3 +138,18 @@ def test_trust_region_dfo_on_quadratics_and_rosenbrock(xr):
     # Rosenbrock in 4-D from a bounded start
     st3, _ = _run_dfo(rosenbrock, np.full(4, -0.5), -2 * np.ones(4), 2 * np.ones(4), 0.5, 1e-9, max_iter=4000)
     assert st3["best_f"] < 1e-3, st3
+
+
+def test_regi_pose_map(xr):
+    """xr_regi_pose_map: C @ Exp(x) @ inv(C) @ start for each row, against the
+    same composition in numpy (host code only)."""
+    from xreg_gb300 import api
+    from xreg_gb300.se3 import exp_se3_batch
+    rng = np.random.default_rng(5)
+    C = exp_se3_batch(np.concatenate([rng.normal(0, 0.3, 3), rng.normal(0, 50, 3)])[None])[0]
+    start = exp_se3_batch(np.concatenate([rng.normal(0, 0.3, 3), rng.normal(0, 200, 3)])[None])[0]
+    xs = np.concatenate([rng.normal(0, 0.1, (9, 3)), rng.normal(0, 10, (9, 3))], axis=1)
+    got = api.regi_pose_map(C, start, xs)
+    want = np.einsum("ij,njk,kl->nil", C, exp_se3_batch(xs), np.linalg.inv(C) @ start)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-9)
+    assert api.regi_pose_map(C, start, np.zeros((0, 6))).shape == (0, 4, 4)

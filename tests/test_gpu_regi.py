@@ -6,7 +6,8 @@
   0.05 deg / 0.1 mm.
 * The continuous-batching server gives every job exactly the result it gets
   when run alone (its optimizer has its own random stream and the job-set values
-  equal the single-job values), while several jobs share each GPU step.
+  equal the single-job values), while several jobs share each GPU step, whether
+  the generation is stepped in the library (xr_regi_jobset_step) or from Python.
 """
 import numpy as np
 import pytest
@@ -34,7 +35,10 @@ def test_two_level_registration_recovers_pose(xr):
     assert len(job.results) == 2 and job.results[1].best_value <= job.results[0].best_value + 0.05
 
 
-def test_server_results_equal_alone(xr):
+@pytest.mark.parametrize("native_step", [True, False])
+def test_server_results_equal_alone(xr, native_step):
+    """native_step: each generation of all jobs in one xr_regi_jobset_step call;
+    otherwise sampled and updated from Python.  Both give the alone results."""
     from xreg_gb300.serving import RegistrationServer
     specs = [_spec(10 + k, size=s, views=v, ds=d, pop=p) for k, (s, v, d, p) in enumerate([
         ((96, 96, 80), (0.0,), 0.125, 16), ((128, 112, 96), (0.0, 25.0), 0.125, 20),
@@ -43,7 +47,7 @@ def test_server_results_equal_alone(xr):
     for s in specs:
         job, _ = synth.job_registration(s, iters=(25, 10), level2_pop=6)
         alone.append(job.run())
-    srv = RegistrationServer(hbm_budget_bytes=180e9)
+    srv = RegistrationServer(hbm_budget_bytes=180e9, native_step=native_step)
     jobs = []
     for s in specs:
         job, _ = synth.job_registration(s, iters=(25, 10), level2_pop=6)

@@ -57,6 +57,11 @@ class xr_regi_level_params(C.Structure):
                 ("tol_x", C.c_double), ("rho_beg", C.c_double), ("rho_end", C.c_double), ("seed", C.c_uint64)]
 
 
+class xr_regi_step_job(C.Structure):
+    _fields_ = [("obj", C.c_void_p), ("optimizer", C.c_int32), ("reserved", C.c_int32), ("opt", C.c_void_p),
+                ("centre", C.c_double * 16), ("start_pose", C.c_double * 16), ("bounds", C.c_double * 6)]
+
+
 class XRegError(RuntimeError):
     """A C-ABI call returned a non-zero xr_status."""
 
@@ -181,6 +186,9 @@ _SIGS = {
     "xr_jobset_eval": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
     "xr_jobset_eval_device": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
     "xr_jobset_last_launch": [H, C.POINTER(i64), C.POINTER(i32)],
+    "xr_regi_pose_map": [C.c_void_p, C.c_void_p, i64, C.c_void_p, C.c_void_p],
+    "xr_regi_jobset_step": [H, i32, C.POINTER(xr_regi_step_job), C.POINTER(i32), C.POINTER(i32)],
+    "xr_cmaes_lambda": [H, C.POINTER(i32)],
     "xr_itk_affine_transform_read": [C.c_char_p, P],
     "xr_itk_slicer_affine_transform_read": [C.c_char_p, P],
     "xr_itk_affine_transform_write": [C.c_char_p, P],

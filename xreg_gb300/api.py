@@ -651,6 +651,16 @@ class JobSet:
         sp = (C.c_void_p * n)(*[int(p) for p in d_sims])
         call("xr_jobset_eval_device", self._h, n, objs, pp, xp, sp)
 
+    def regi_step(self, step_jobs) -> tuple:
+        """xr_regi_jobset_step: one generation of every job (xr_regi_step_job
+        structs); returns (stop codes, poses evaluated) per job."""
+        n = len(step_jobs)
+        arr = (L.xr_regi_step_job * n)(*step_jobs)
+        stop = (C.c_int32 * n)()
+        ev = (C.c_int32 * n)()
+        call("xr_regi_jobset_step", self._h, n, arr, stop, ev)
+        return list(stop), list(ev)
+
     def last_launch(self):
         a, b = C.c_int64(), C.c_int32()
         call("xr_jobset_last_launch", self._h, C.byref(a), C.byref(b))
@@ -730,6 +740,16 @@ def proj_preproc(img: np.ndarray, cam: CameraModel, crop_width: int = 50, no_log
 
 
 # ------------------------------------------------------------ poses on disk
+def regi_pose_map(centre, start_pose, xs) -> np.ndarray:
+    """xr_regi_pose_map: pose = centre @ Exp(x) @ inv(centre) @ start_pose for each row x."""
+    c = np.ascontiguousarray(centre, dtype=np.float64)
+    s = np.ascontiguousarray(start_pose, dtype=np.float64)
+    x = np.ascontiguousarray(xs, dtype=np.float64).reshape(-1, 6)
+    out = np.empty((x.shape[0], 4, 4), dtype=np.float64)
+    call("xr_regi_pose_map", _ptr(c), _ptr(s), x.shape[0], _ptr(x), _ptr(out))
+    return out
+
+
 def read_itk_affine_transform(path: str) -> np.ndarray:
     """ReadITKAffineTransformFromFile: the 4x4 pose in an ITK text transform file
     (".txt" / ".tfm"; xr_itk_affine_transform_read)."""

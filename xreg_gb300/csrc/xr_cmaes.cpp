@@ -310,6 +310,12 @@ extern "C" XR_API xr_status xr_cmaes_test_termination(xr_cmaes e, int32_t* reaso
   return XR_OK;
 }
 
+extern "C" XR_API xr_status xr_cmaes_lambda(xr_cmaes e, int32_t* lambda) {
+  if (!e || !lambda) return fail(XR_ERR_INVALID_ARG, "cmaes_lambda: NULL argument");
+  *lambda = e->lambda;
+  return XR_OK;
+}
+
 extern "C" XR_API xr_status xr_cmaes_get(xr_cmaes e, double* mean, double* best_x, double* best_f, double* sigma,
                                          int64_t* generation) {
   if (!e) return fail(XR_ERR_INVALID_ARG, "xr_cmaes_get: NULL handle");

@@ -224,3 +224,95 @@ extern "C" XR_API xr_status xr_regi_run_level(xr_objective obj, const double* ce
   if (stop_reason) *stop_reason = reason;
   return XR_OK;
 }
+
+extern "C" XR_API xr_status xr_regi_pose_map(const double* centre, const double* start_pose, int64_t n,
+                                             const double* xs, double* poses) {
+  if (!centre || !start_pose || n < 0 || (n > 0 && (!xs || !poses)))
+    return fail(XR_ERR_INVALID_ARG, "regi_pose_map: NULL argument or negative count");
+  PoseMap map;
+  std::memcpy(map.C, centre, sizeof(map.C));
+  double Ci[16];
+  rigid_inverse(centre, Ci);
+  mat_mul(Ci, start_pose, map.B);
+  for (int64_t k = 0; k < n; ++k) map(xs + k * 6, poses + k * 16);
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_regi_jobset_step(xr_jobset js, int32_t n, const xr_regi_step_job* jobs, int32_t* stop,
+                                                int32_t* evaluated) {
+  if (!js || !jobs || !stop || n <= 0) return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: NULL argument or no job");
+  std::vector<std::vector<double>> xs((size_t)n), poses((size_t)n);
+  std::vector<std::vector<float>> vals((size_t)n);
+  std::vector<xr_objective> objs((size_t)n);
+  std::vector<int64_t> pops((size_t)n);
+  std::vector<const double*> pp((size_t)n);
+  std::vector<float*> vp((size_t)n);
+  xr_status st = XR_OK;
+  // sample (or ask) every job's candidates and map them to poses
+  for (int32_t j = 0; j < n; ++j) {
+    const xr_regi_step_job& J = jobs[j];
+    if (!J.obj || !J.opt) return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: job without objective or optimizer");
+    int32_t pop = 0;
+    if (J.optimizer == XR_REGI_CMAES) {
+      xr_cmaes es = static_cast<xr_cmaes>(J.opt);
+      int32_t lam = 0;
+      if ((st = xr_cmaes_lambda(es, &lam)) != XR_OK) return st;
+      pop = lam;
+      xs[(size_t)j].resize((size_t)pop * 6);
+      double* x = xs[(size_t)j].data();
+      if ((st = xr_cmaes_sample_population(es, x)) != XR_OK) return st;
+      bool bounded = false;
+      for (int i = 0; i < 6; ++i) bounded = bounded || J.bounds[i] > 0.0;
+      for (int32_t k = 0; bounded && k < pop; ++k) {
+        for (int tries = 0;; ++tries) {
+          bool inside = true;
+          for (int i = 0; i < 6; ++i)
+            if (J.bounds[i] > 0.0 && std::fabs(x[(size_t)k * 6 + i]) > J.bounds[i]) inside = false;
+          if (inside) break;
+          if (tries > 100000)
+            return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: could not sample a candidate inside the bounds");
+          if ((st = xr_cmaes_resample_single(es, k, x)) != XR_OK) return st;
+        }
+      }
+    } else if (J.optimizer == XR_REGI_DFO) {
+      xs[(size_t)j].resize((size_t)(2 * 6 + 2) * 6);
+      if ((st = xr_dfo_ask(static_cast<xr_dfo>(J.opt), xs[(size_t)j].data(), &pop)) != XR_OK) return st;
+    } else {
+      return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: unknown optimizer");
+    }
+    PoseMap map;
+    std::memcpy(map.C, J.centre, sizeof(map.C));
+    {
+      double Ci[16];
+      rigid_inverse(J.centre, Ci);
+      mat_mul(Ci, J.start_pose, map.B);
+    }
+    poses[(size_t)j].resize((size_t)pop * 16);
+    for (int32_t k = 0; k < pop; ++k)
+      map(xs[(size_t)j].data() + (size_t)k * 6, poses[(size_t)j].data() + (size_t)k * 16);
+    vals[(size_t)j].resize((size_t)pop);
+    objs[(size_t)j] = J.obj;
+    pops[(size_t)j] = pop;
+    pp[(size_t)j] = poses[(size_t)j].data();
+    vp[(size_t)j] = vals[(size_t)j].data();
+  }
+  if ((st = xr_jobset_eval(js, n, objs.data(), pops.data(), pp.data(), vp.data())) != XR_OK) return st;
+  // update every optimizer and test it for termination
+  for (int32_t j = 0; j < n; ++j) {
+    const xr_regi_step_job& J = jobs[j];
+    std::vector<double> f(vals[(size_t)j].begin(), vals[(size_t)j].end());
+    int32_t reason = 0;
+    if (J.optimizer == XR_REGI_CMAES) {
+      xr_cmaes es = static_cast<xr_cmaes>(J.opt);
+      if ((st = xr_cmaes_update_distribution(es, f.data())) != XR_OK) return st;
+      if ((st = xr_cmaes_test_termination(es, &reason)) != XR_OK) return st;
+    } else {
+      xr_dfo d = static_cast<xr_dfo>(J.opt);
+      if ((st = xr_dfo_tell(d, f.data())) != XR_OK) return st;
+      if ((st = xr_dfo_test_termination(d, &reason)) != XR_OK) return st;
+    }
+    stop[j] = reason;
+    if (evaluated) evaluated[j] = (int32_t)pops[(size_t)j];
+  }
+  return XR_OK;
+}

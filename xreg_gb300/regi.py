@@ -26,7 +26,6 @@ import numpy as np
 
 from . import api
 from .cmaes import CMAES, TrustRegionDFO
-from .se3 import exp_se3_batch
 
 # Bounds of xReg's single-view BOBYQA level (+-2.5 deg rotations, +-5, 5, 10 mm).
 DFO_BOUNDS = np.array([np.radians(2.5)] * 3 + [5.0, 5.0, 10.0])
@@ -155,8 +154,9 @@ class Registration:
             self.es.set_stop(tol_fun=L.tol_fun, tol_x=L.tol_x, max_iter=L.max_iters)
 
     def poses_of(self, xs: np.ndarray) -> np.ndarray:
-        B = self.Ci @ self.start_pose
-        return np.einsum("ij,njk,kl->nil", self.C, exp_se3_batch(xs), B)
+        # the library's map, so a job stepped natively (xr_regi_jobset_step)
+        # sees bit-identical poses
+        return api.regi_pose_map(self.C, self.start_pose, xs)
 
     # ---------------------------------------------------------- stepping
     def propose(self) -> np.ndarray:
@@ -176,16 +176,43 @@ class Registration:
             self.es.update_distribution(np.asarray(values, dtype=np.float64))
         stop = self.es.test_for_termination()
         if stop is not None:
-            st = self.es.state()
-            x = st["best_x"]
-            pose = self.poses_of(x[None])[0]
-            gens = st.get("generation", st.get("iterations", 0))
-            self.results.append(LevelResult(pose, x, st["best_f"], gens, stop))
-            self.start_pose = pose
-            if self.level + 1 < len(self.levels):
-                self._enter_level(self.level + 1)
-            else:
-                self.finish()
+            self.end_level(stop)
+
+    # ----------------------------------------------------- native stepping
+    def step_job(self):
+        """This generation as an xr_regi_step_job for xr_regi_jobset_step (the
+        optimizer advances inside the library)."""
+        from ._lib import XR_REGI_CMAES, XR_REGI_DFO, xr_regi_step_job
+        L = self.levels[self.level]
+        j = xr_regi_step_job()
+        j.obj = self.obj._h.value
+        j.optimizer = XR_REGI_DFO if L.optimizer == "dfo" else XR_REGI_CMAES
+        j.opt = self.es._h.value
+        j.centre[:] = np.ascontiguousarray(self.C, dtype=np.float64).ravel().tolist()
+        j.start_pose[:] = np.ascontiguousarray(self.start_pose, dtype=np.float64).ravel().tolist()
+        b = L.bounds if (L.optimizer != "dfo" and L.bounds is not None) else np.zeros(6)
+        j.bounds[:] = np.asarray(b, dtype=np.float64).ravel().tolist()
+        return j
+
+    def stop_reason(self, code: int) -> str:
+        """The name of a termination code of the current level's optimizer."""
+        from .cmaes import STOP_REASONS
+        if self.levels[self.level].optimizer == "dfo":
+            return {2: "rho_end", 3: "max_iter"}.get(code, "unknown")
+        return STOP_REASONS.get(code, "unknown")
+
+    def end_level(self, stop: str) -> None:
+        """The current level has stopped (reason stop): keep its best pose, go on or finish."""
+        st = self.es.state()
+        x = st["best_x"]
+        pose = self.poses_of(x[None])[0]
+        gens = st.get("generation", st.get("iterations", 0))
+        self.results.append(LevelResult(pose, x, st["best_f"], gens, stop))
+        self.start_pose = pose
+        if self.level + 1 < len(self.levels):
+            self._enter_level(self.level + 1)
+        else:
+            self.finish()
 
     def finish(self) -> None:
         self.done = True

@@ -47,8 +47,12 @@ class ServerStats:
 
 
 class RegistrationServer:
-    def __init__(self, device: int = -1, hbm_budget_bytes: float = 180e9, max_active: int = 64):
+    def __init__(self, device: int = -1, hbm_budget_bytes: float = 180e9, max_active: int = 64,
+                 native_step: bool = True):
         self.device = device
+        # native_step: each generation of all active jobs (sample, evaluate,
+        # update, stop test) in one library call; otherwise driven from Python
+        self.native_step = bool(native_step)
         self.budget = float(hbm_budget_bytes)
         self.max_active = int(max_active)
         self.queue: collections.deque = collections.deque()
@@ -84,14 +88,22 @@ class RegistrationServer:
             return 0
         t0 = time.perf_counter()
         jobs = list(self.active)
-        poses = [j.propose() for j in jobs]
-        values = self.jobset.eval([j.obj for j in jobs], poses)
-        for j, v in zip(jobs, values):
-            j.tell(v)
+        if self.native_step:
+            stop, evaluated = self.jobset.regi_step([j.step_job() for j in jobs])
+            for j, code in zip(jobs, stop):
+                if code:
+                    j.end_level(j.stop_reason(code))
+            n_eval = sum(evaluated)
+        else:
+            poses = [j.propose() for j in jobs]
+            values = self.jobset.eval([j.obj for j in jobs], poses)
+            for j, v in zip(jobs, values):
+                j.tell(v)
+            n_eval = sum(len(p) for p in poses)
         now = time.perf_counter()
         self.stats.busy_s += now - t0
         self.stats.steps += 1
-        self.stats.poses_evaluated += sum(len(p) for p in poses)
+        self.stats.poses_evaluated += n_eval
         still = []
         for j in jobs:
             if j.done:
