@@ -319,6 +319,7 @@ class PopulationObjective {
     check(xr_obj_eval(h_, (int64_t)poses.size(), poses.empty() ? nullptr : poses[0].data(), out.data()));
     return out;
   }
+  xr_objective handle() const { return h_; }
 
  private:
   xr_objective h_ = nullptr;

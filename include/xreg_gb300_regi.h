@@ -38,10 +38,10 @@ XR_API xr_status xr_cmaes_update_distribution(xr_cmaes e, const double* fvals);
 /* cmaes_TestForTermination: *reason = 0 continue, 1 function-value range below
  * tol_fun, 2 step sizes below tol_x, 3 iteration limit, 4 numerical failure. */
 XR_API xr_status xr_cmaes_test_termination(xr_cmaes e, int32_t* reason);
-/* Current mean, best candidate seen and its value, step size, generation count
- * (any pointer may be NULL). */
 /* Candidates per generation (lambda). */
 XR_API xr_status xr_cmaes_lambda(xr_cmaes e, int32_t* lambda);
+/* Current mean, best candidate seen and its value, step size, generation count
+ * (any pointer may be NULL). */
 XR_API xr_status xr_cmaes_get(xr_cmaes e, double* mean, double* best_x, double* best_f, double* sigma,
                               int64_t* generation);
 

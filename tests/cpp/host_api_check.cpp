@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "xreg_gb300/xreg_gb300.hpp"
+#include "xreg_gb300/xreg_gb300_regi.hpp"
 
 template <typename T>
 static std::vector<T> read_all(const std::string& path) {
@@ -112,6 +113,45 @@ int main(int argc, char** argv) {
     wrap.ref_frames_cam_world_to_vol = {R};
     wrap();
     write_all(dir + "/wrap.f32", wrap.projs[0]);
+
+    // a CMA-ES level run in the library, and the same level stepped one
+    // generation at a time through a job set (xreg_gb300_regi.hpp)
+    {
+      RayCasterLineIntCUDA rc3;
+      rc3.set_volume(vol);
+      rc3.set_camera_model(cam);
+      rc3.set_ray_step_size(step);
+      ImgSimMetric2DGradNCCCUDA m3;
+      m3.set_fixed_image(fixed.data(), rows, cols);
+      PopulationObjective obj3(rc3, {&m3}, 8);
+      xr_regi_level_params lp = DefaultLevelParams(XR_REGI_CMAES);
+      lp.lambda = 8;
+      lp.max_iters = 6;
+      lp.seed = 11;
+      Mat4 centre{};
+      for (int i = 0; i < 4; ++i) centre[(size_t)(i * 5)] = 1.0;
+      centre[3] = 0.5 * sp * (double)nx;
+      centre[7] = 0.5 * sp * (double)ny;
+      centre[11] = 0.5 * sp * (double)nz;
+      const LevelResult a = RunLevel(obj3, centre, poses[0], lp);
+      CMAES es(6, std::vector<double>(6, 0.0), std::vector<double>(lp.sigma, lp.sigma + 6), lp.lambda, lp.seed);
+      es.set_stop(lp.tol_fun, lp.tol_x, lp.max_iters);
+      JobSet js;
+      int32_t reason = 0, gens = 0;
+      while (reason == 0 && gens < 100) {
+        const auto r = js.regi_step({StepJob(obj3, es, centre, poses[0], lp.bounds)});
+        if (r.second[0] != lp.lambda) throw Error(XR_ERR_INVALID_ARG, "regi_step: wrong evaluation count");
+        reason = r.first[0];
+        ++gens;
+      }
+      double bf = 0.0;
+      int64_t g = 0;
+      const Mat4 b = RegiPoseMap(centre, poses[0], es.best_x(&bf, &g))[0];
+      std::vector<double> lv(a.pose.begin(), a.pose.end());
+      lv.insert(lv.end(), b.begin(), b.end());
+      lv.insert(lv.end(), {a.value, bf, (double)a.iterations, (double)g, (double)a.stop_reason, (double)reason});
+      write_all(dir + "/levels.f64", lv);
+    }
 
     // a pose through an ITK text transform file and back
     WriteITKAffineTransform(dir + "/pose.txt", poses[1]);

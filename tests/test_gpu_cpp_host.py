@@ -70,6 +70,10 @@ def test_cpp_host_classes_match_oracle(xr, oracle, tmp_path):
     want = poses[1].astype(np.float32).astype(np.float64)
     want[3] = [0, 0, 0, 1]
     np.testing.assert_array_equal(back, want)
+    # RunLevel and the same CMA-ES level stepped through JobSet::regi_step agree exactly
+    lv = np.fromfile(tmp_path / "levels.f64", np.float64)
+    np.testing.assert_array_equal(lv[:16], lv[16:32])
+    assert lv[32] == lv[33] and lv[34] == lv[35] and lv[36] == lv[37] != 0
     psims = np.fromfile(tmp_path / "psims.f32", np.float32)
     ref_p = oracle.patch_ncc_ex(fixed, drr, radius=3, stride=2, mask=mask, use_mov_var_wgts=1)
     np.testing.assert_allclose(psims, ref_p, atol=1e-5, rtol=2e-6)
