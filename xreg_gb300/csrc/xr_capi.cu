@@ -2086,6 +2086,8 @@ struct xr_jobset_s {
   std::vector<MultiJobDrr> h_jobs;
   int blocks = 0;
   long long last_items = 0;
+  unsigned int* h_err = nullptr;  // pinned: every job's step-guard flag, read with one synchronisation
+  size_t h_err_cap = 0;
   cudaStream_t stream() const { return has_ext ? ext_stream : own_stream; }
 };
 
@@ -2109,6 +2111,7 @@ extern "C" XR_API xr_status xr_jobset_destroy(xr_jobset js) {
   DeviceGuard g(js->device);
   cudaStreamSynchronize(js->stream());
   cudaStreamDestroy(js->own_stream);
+  if (js->h_err) cudaFreeHost(js->h_err);
   delete js;
   return XR_OK;
 }
@@ -2237,13 +2240,23 @@ extern "C" XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t n, const xr_obj
                                            const double* const* host_xforms, float* const* host_sims) {
   xr_status st = jobset_enqueue(js, n, objs, pops, host_xforms, true, host_sims, true);
   if (st != XR_OK) return st;
-  XR_CUDA_TRY(cudaStreamSynchronize(js->stream()));
+  DeviceGuard g(js->device);
+  if (js->h_err_cap < (size_t)n) {
+    if (js->h_err) cudaFreeHost(js->h_err);
+    js->h_err = nullptr;
+    js->h_err_cap = 0;
+    XR_CUDA_TRY(cudaMallocHost(&js->h_err, (size_t)n * sizeof(unsigned int)));
+    js->h_err_cap = (size_t)n;
+  }
+  cudaStream_t s = js->stream();
+  for (int32_t i = 0; i < n; ++i)
+    XR_CUDA_TRY(cudaMemcpyAsync(js->h_err + i, objs[i]->rc->d_counters.as<char>() + 8, sizeof(unsigned int),
+                                cudaMemcpyDeviceToHost, s));
+  XR_CUDA_TRY(cudaStreamSynchronize(s));
   for (int32_t i = 0; i < n; ++i) {
-    unsigned int err = 0;
     xr_raycaster rc = objs[i]->rc;
-    XR_CUDA_TRY(cudaMemcpy(&err, rc->d_counters.as<char>() + 8, sizeof(err), cudaMemcpyDeviceToHost));
-    if (err) {
-      cudaMemset(rc->d_counters.as<char>() + 8, 0, sizeof(err));
+    if (js->h_err[i]) {
+      cudaMemset(rc->d_counters.as<char>() + 8, 0, sizeof(unsigned int));
       return fail(XR_ERR_DEVICE_CHECK, "xr_jobset_eval: a job's rays exceeded the step-count guard");
     }
   }
