@@ -23,6 +23,7 @@ Multi-GPU: replicas only (each rank evaluates its own populations; no collective
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import faulthandler
 import json
 import os
@@ -482,10 +483,23 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
                                      "how": "per pose: pose upload, DRR launch, grad-NCC launches, host read"}
     ref = d_sims[a.warmup][:n].cpu().numpy()
     out["plain_single_pose_fp32"]["max_abs_diff_vs_batched"] = float(np.max(np.abs(np.array(vals) - ref)))
-    for vname, vt in (("f16", 1), ("bf16", 2)):
+    # the same volume in half precision; then float32 with empty-space skipping
+    # off, and float32 with CT-like air (noise of 10 HU about -1000: about half
+    # of the air voxels convert to small positive attenuations, so only the
+    # clamped half can be skipped)
+    from xreg_gb300 import synth
+    v_air = w.vol.voxels.copy()
+    air = v_air == 0.0
+    v_air[air] = synth.hu_to_lin_att(-1000.0 + np.random.default_rng(17).standard_normal(
+        int(air.sum()), dtype=np.float32) * 10.0)
+    noisy_air = dataclasses.replace(w.vol, voxels=v_air)
+    for key, vol_k, vt, skipping in (("batched_f16_volume", w.vol, 1, True), ("batched_bf16_volume", w.vol, 2, True),
+                                     ("batched_f32_skipping_off", w.vol, 0, False),
+                                     ("batched_f32_noisy_air", noisy_air, 0, True)):
         rch = xr.RayCasterLineIntCUDA(dev)
         rch.set_stream(stream.cuda_stream)
-        rch.set_volume(w.vol, vt)
+        rch.set_volume(vol_k, vt)
+        rch.set_empty_space_skipping(skipping)
         rch.set_camera_model(w.cams[0])
         rch.set_ray_step_size(w.step)
         mh = xr.ImgSimMetric2DGradNCCCUDA(dev)
@@ -505,10 +519,13 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
                 e.record(stream)
         torch.cuda.synchronize()
         t = np.mean([s.elapsed_time(e) for s, e in evs]) / 1e3
-        out[f"batched_{vname}_volume"] = {"value": round(POP / t, 2), "unit": "poses/s",
-                                          "max_abs_sim_diff_vs_f32": float(
-                                              np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
+        out[key] = {"value": round(POP / t, 2), "unit": "poses/s",
+                    "max_abs_sim_diff_vs_f32": float(
+                        np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
+        if key == "batched_f32_noisy_air":
+            out[key]["air_voxels_nonzero_frac"] = round(float(np.mean(v_air[air] > 0)), 3)
         objh.close()
+    del v_air, noisy_air
     for key, fn in (("plain_small_config", lambda: _plain_small(xr, dev, min(3.0, a.cpu_seconds))),
                     ("precision_large", lambda: _precision(xr, dev, stream)),
                     ("uneven_multi_job", lambda: _multi_job(xr, dev)),
