@@ -299,6 +299,51 @@ def test_empty_space_skipping_is_exact(xr, oracle, vt):
 
 
 @pytest.mark.parametrize("vt", [0, 1])
+def test_skipping_keeps_tiny_and_negative_voxels(xr, vt):
+    """Only cells whose eight corners compare equal to zero are skipped: single
+    voxels in the air holding a subnormal, a tiny positive, a negative value or
+    -0.0 are sampled exactly as with skipping off (bit-identical images, same
+    sample count), and the images see the non-zero ones."""
+    ph = synth.phantom_volume((30, 28, 26), (1.5, 1.5, 1.5), 23).voxels
+    big = np.zeros((64, 72, 70), np.float32)
+    big[19:45, 22:50, 20:50] = ph
+    rng = np.random.default_rng(4)
+    vals = np.array([1e-40, 1e-30, 3e-7, -0.01, -0.0, 0.05], np.float32)
+    k = 0
+    while k < 60:
+        z, y, x = rng.integers(0, 64), rng.integers(0, 72), rng.integers(0, 70)
+        if 17 <= z < 47 and 20 <= y < 52 and 18 <= x < 52:
+            continue  # keep them in the air around the body
+        big[z, y, x] = vals[k % len(vals)]
+        k += 1
+    vol = xr.Volume(big, spacing=(1.5, 1.5, 1.5))
+    cam = small_camera((56, 60), 3.0)
+    poses = synth.sample_poses(vol, synth.gt_pose(vol), 4, 10.0, 15.0, seed=5)
+    rc = _rc(xr, vol, [cam], 0.5, vt)
+    rc.set_num_projs(len(poses))
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(poses)
+    rc.set_count_samples(True)
+    outs = []
+    for skip, un in ((False, 1), (True, 3), (True, 4), (True, 5)):
+        rc.set_empty_space_skipping(skip)
+        rc.set_launch_config(1, 2, un)
+        rc.compute()
+        outs.append((rc.projs(), rc.last_num_samples()))
+    for img, ns in outs[1:]:
+        np.testing.assert_array_equal(img, outs[0][0])
+        assert ns == outs[0][1]
+    # the scattered voxels are seen: the body alone gives other images
+    body = np.pad(ph, ((19, 19), (22, 22), (20, 20))).astype(np.float32)
+    rb = _rc(xr, xr.Volume(body, spacing=(1.5, 1.5, 1.5)), [cam], 0.5, vt)
+    rb.set_num_projs(len(poses))
+    rb.allocate_resources()
+    rb.distribute_xforms_among_cam_models(poses)
+    rb.compute()
+    assert not np.array_equal(rb.projs(), outs[0][0])
+
+
+@pytest.mark.parametrize("vt", [0, 1])
 def test_macro_cell_skipping_is_exact(xr, oracle, vt):
     """The macro-cell trim (loop 3) changes no bit where the bounding box does
     not help: two blobs in opposite corners and a one-voxel sheet in between

@@ -99,3 +99,37 @@ def test_jobset_errors(xr):
     obj.close()
     with pytest.raises(_lib.XRegError):
         js.eval([obj], [p[:2]]) if obj._h else (_ for _ in ()).throw(_lib.XRegError(-1, "closed"))
+
+
+def test_regi_step_errors_and_counts(xr):
+    """xr_regi_jobset_step: refuses an unknown optimizer, a job without an
+    objective or optimizer and an empty job list; reports lambda evaluations for
+    a CMA-ES job and the ask size for a trust-region job."""
+    from xreg_gb300 import _lib
+    from xreg_gb300.cmaes import CMAES, TrustRegionDFO
+    obj, vol, cams, ms = _job(xr, 8, (32, 32, 32), 0, (24, 24), 1, xr.ImgSimMetric2DGradNCCCUDA, 16)
+    obj2, vol2, _, ms2 = _job(xr, 9, (32, 32, 32), 0, (24, 24), 1, xr.ImgSimMetric2DGradNCCCUDA, 16)
+    js = xr.JobSet()
+    C = vol.xform_img_center_to_itk_phys()
+    start = synth.gt_pose(vol)
+    es = CMAES(np.zeros(6), np.array([0.05] * 3 + [5.0] * 3), 6, seed=3)
+    b = np.array([0.2] * 3 + [20.0] * 3)
+    d = TrustRegionDFO(np.zeros(6), -b, b, 2.0, 0.01, 5)
+
+    def job(o, opt, kind, bounds=None):
+        j = _lib.xr_regi_step_job()
+        j.obj = o._h.value if o is not None else None
+        j.optimizer = kind
+        j.opt = opt._h.value if opt is not None else None
+        j.centre[:] = C.ravel().tolist()
+        j.start_pose[:] = start.ravel().tolist()
+        j.bounds[:] = (bounds if bounds is not None else np.zeros(6)).tolist()
+        return j
+
+    stop, ev = js.regi_step([job(obj, es, _lib.XR_REGI_CMAES, b), job(obj2, d, _lib.XR_REGI_DFO)])
+    assert ev[0] == 6 and 1 <= ev[1] <= 14 and stop == [0, 0]
+    for bad in (job(obj, es, 7), job(None, es, _lib.XR_REGI_CMAES), job(obj, None, _lib.XR_REGI_CMAES)):
+        with pytest.raises(_lib.XRegError):
+            js.regi_step([bad])
+    with pytest.raises(_lib.XRegError):
+        _lib.call("xr_regi_jobset_step", js._h, 0, None, None, None)
