@@ -495,7 +495,8 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
     noisy_air = dataclasses.replace(w.vol, voxels=v_air)
     for key, vol_k, vt, skipping in (("batched_f16_volume", w.vol, 1, True), ("batched_bf16_volume", w.vol, 2, True),
                                      ("batched_f32_skipping_off", w.vol, 0, False),
-                                     ("batched_f32_noisy_air", noisy_air, 0, True)):
+                                     ("batched_f32_noisy_air", noisy_air, 0, True),
+                                     ("batched_f16_noisy_air", noisy_air, 1, True)):
         rch = xr.RayCasterLineIntCUDA(dev)
         rch.set_stream(stream.cuda_stream)
         rch.set_volume(vol_k, vt)
@@ -522,7 +523,7 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
         out[key] = {"value": round(POP / t, 2), "unit": "poses/s",
                     "max_abs_sim_diff_vs_f32": float(
                         np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
-        if key == "batched_f32_noisy_air":
+        if key.endswith("noisy_air"):
             out[key]["air_voxels_nonzero_frac"] = round(float(np.mean(v_air[air] > 0)), 3)
         objh.close()
     del v_air, noisy_air

@@ -52,7 +52,7 @@ class CMAES:
         b = np.asarray(bounds, dtype=np.float64)
         for k in range(self.lam):
             tries = 0
-            while np.any(np.abs(pop[k]) > b):
+            while np.any((b > 0.0) & (np.abs(pop[k]) > b)):  # a bound of 0 leaves its coordinate free
                 self.resample_single(k)
                 tries += 1
                 if tries > 100000:
