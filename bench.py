@@ -680,6 +680,7 @@ def _serving(dev, n_req: int, rate: float):
         return {"p50_latency_s": round(s["p50_s"], 3), "p99_latency_s": round(s["p99_s"], 3),
                 "registrations_per_s": round(n_req / makespan, 3), "arrival_rate_per_s": r, "requests": n_req,
                 "poses_evaluated": s["poses_evaluated"], "server_steps": s["steps"], "max_active": s["max_active"],
+                "makespan_s": round(makespan, 3), "step_s": round(s["busy_s"], 3), "admit_s": round(s["admit_s"], 3),
                 "max_footprint_gb": round(s["max_footprint_gb"], 2),
                 "pose_error_deg_median": round(float(np.median([e[0] for e in errs])), 4),
                 "pose_error_mm_median": round(float(np.median([e[1] for e in errs])), 4),

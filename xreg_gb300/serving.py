@@ -35,6 +35,7 @@ class ServerStats:
     steps: int = 0
     poses_evaluated: int = 0
     busy_s: float = 0.0
+    admit_s: float = 0.0  # job starts: volume upload, device set-up of the first level
     max_active: int = 0
     max_footprint: int = 0
 
@@ -42,7 +43,8 @@ class ServerStats:
         lat = np.array(self.latencies_s) if self.latencies_s else np.zeros(1)
         return {"completed": self.completed, "p50_s": float(np.percentile(lat, 50)),
                 "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "steps": self.steps,
-                "poses_evaluated": self.poses_evaluated, "busy_s": self.busy_s, "max_active": self.max_active,
+                "poses_evaluated": self.poses_evaluated, "busy_s": self.busy_s, "admit_s": self.admit_s,
+                "max_active": self.max_active,
                 "max_footprint_gb": self.max_footprint / 1e9}
 
 
@@ -75,7 +77,9 @@ class RegistrationServer:
             if self.active and used + need > self.budget:
                 break
             job = self.queue.popleft()
+            t0 = time.perf_counter()
             job.start()
+            self.stats.admit_s += time.perf_counter() - t0
             self.active.append(job)
             used += need
         self.stats.max_active = max(self.stats.max_active, len(self.active))
