@@ -85,13 +85,16 @@ struct Vox<XR_VOXEL_BF16> {
   __device__ __forceinline__ static float ld(const void* b, int i) {
     return __bfloat162float(__ldg(static_cast<const __nv_bfloat16*>(b) + i));
   }
+  // A bf16 value is the upper half of the float with the same value, so each
+  // packed pair widens with one shift (low) and one mask (high), exactly.
   __device__ __forceinline__ static void cell(const void* b, int c, float v[8]) {
     const uint4 q = __ldg(static_cast<const uint4*>(b) + c);
-    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.x));
-    const float2 bb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.y));
-    const float2 cc = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.z));
-    const float2 d = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.w));
-    v[0] = a.x; v[1] = a.y; v[2] = bb.x; v[3] = bb.y; v[4] = cc.x; v[5] = cc.y; v[6] = d.x; v[7] = d.y;
+    const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[2 * k] = __uint_as_float(w[k] << 16);
+      v[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+    }
   }
 };
 
