@@ -496,7 +496,8 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
     for key, vol_k, vt, skipping in (("batched_f16_volume", w.vol, 1, True), ("batched_bf16_volume", w.vol, 2, True),
                                      ("batched_f32_skipping_off", w.vol, 0, False),
                                      ("batched_f32_noisy_air", noisy_air, 0, True),
-                                     ("batched_f16_noisy_air", noisy_air, 1, True)):
+                                     ("batched_f16_noisy_air", noisy_air, 1, True),
+                                     ("batched_bf16_noisy_air", noisy_air, 2, True)):
         rch = xr.RayCasterLineIntCUDA(dev)
         rch.set_stream(stream.cuda_stream)
         rch.set_volume(vol_k, vt)
