@@ -59,7 +59,7 @@ def test_server_results_equal_alone(xr, native_step):
     srv.step()
     srv.submit(jobs[2])
     srv.submit(jobs[3])
-    while srv.queue or srv.active:
+    while srv.queue or srv.active or srv.starting:
         srv.step()
     st = srv.stats.summary()
     assert st["completed"] == 4 and st["max_active"] >= 3
@@ -77,7 +77,7 @@ def test_server_admission_respects_budget(xr):
         srv.submit(j)
     srv.step()
     assert len(srv.active) == 1 and len(srv.queue) == 2  # only one fits
-    while srv.queue or srv.active:
+    while srv.queue or srv.active or srv.starting:
         srv.step()
     assert srv.stats.completed == 3 and srv.stats.max_active == 1
 

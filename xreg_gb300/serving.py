@@ -4,8 +4,11 @@ Requests (a `Registration`: volume, cameras, fixed images per level, initial
 pose, optimizer schedule) arrive at any time.  Each server step:
 
   1. admits queued jobs in arrival order while the summed device footprint of
-     the active jobs stays within the HBM budget (their volumes are uploaded
-     once and stay resident, as do fixed-image gradients and optimizer state);
+     the active and starting jobs stays within the HBM budget (their volumes
+     are uploaded once and stay resident, as do fixed-image gradients and
+     optimizer state); a job starts (volume upload, first level set-up) on a
+     worker thread while the active jobs keep stepping, and joins the steps
+     once it has started;
   2. asks every active job for its current population (CMA-ES sample);
   3. evaluates all populations with ONE job-set call: one persistent DRR launch
      over every job's (tile, pose) work, then each job's metrics;
@@ -19,6 +22,7 @@ other jobs share its steps.
 from __future__ import annotations
 
 import collections
+import concurrent.futures
 import time
 from dataclasses import dataclass, field
 
@@ -35,7 +39,7 @@ class ServerStats:
     steps: int = 0
     poses_evaluated: int = 0
     busy_s: float = 0.0
-    admit_s: float = 0.0  # job starts: volume upload, device set-up of the first level
+    admit_s: float = 0.0  # steps spent waiting for a job start (nothing else to step)
     max_active: int = 0
     max_footprint: int = 0
 
@@ -62,28 +66,40 @@ class RegistrationServer:
         self.finished: list = []
         self.jobset = api.JobSet(device)
         self.stats = ServerStats()
+        self.starting: list = []  # (job, future) of jobs starting on the worker thread
+        self._pool = concurrent.futures.ThreadPoolExecutor(max_workers=1)
 
     def submit(self, job: Registration, t_arrival: float | None = None) -> None:
         job.t_submit = time.perf_counter() if t_arrival is None else t_arrival
         self.queue.append(job)
 
     def footprint(self) -> int:
-        return sum(j.footprint_bytes() for j in self.active)
+        return sum(j.footprint_bytes() for j in self.active) + sum(j.footprint_bytes() for j, _ in self.starting)
 
     def _admit(self) -> None:
         used = self.footprint()
-        while self.queue and len(self.active) < self.max_active:
+        while self.queue and len(self.active) + len(self.starting) < self.max_active:
             need = self.queue[0].footprint_bytes()
-            if self.active and used + need > self.budget:
+            if (self.active or self.starting) and used + need > self.budget:
                 break
             job = self.queue.popleft()
-            t0 = time.perf_counter()
-            job.start()
-            self.stats.admit_s += time.perf_counter() - t0
-            self.active.append(job)
+            self.starting.append((job, self._pool.submit(job.start)))
             used += need
-        self.stats.max_active = max(self.stats.max_active, len(self.active))
         self.stats.max_footprint = max(self.stats.max_footprint, used)
+        # started jobs join the steps; with nothing to step, wait for the first start
+        if self.starting and not self.active:
+            t0 = time.perf_counter()
+            concurrent.futures.wait([self.starting[0][1]])
+            self.stats.admit_s += time.perf_counter() - t0
+        still = []
+        for job, fut in self.starting:
+            if fut.done():
+                fut.result()  # a failed start raises here
+                self.active.append(job)
+            else:
+                still.append((job, fut))
+        self.starting = still
+        self.stats.max_active = max(self.stats.max_active, len(self.active))
 
     def step(self) -> int:
         """One optimizer generation for every active job; returns the number of jobs stepped."""
@@ -125,12 +141,12 @@ class RegistrationServer:
         pending = sorted(arrivals or [], key=lambda a: a[0])
         t0 = time.perf_counter()
         i = 0
-        while i < len(pending) or self.queue or self.active:
+        while i < len(pending) or self.queue or self.active or self.starting:
             now = time.perf_counter() - t0
             while i < len(pending) and pending[i][0] <= now:
                 self.submit(pending[i][1], t0 + pending[i][0])
                 i += 1
-            if not self.queue and not self.active:
+            if not self.queue and not self.active and not self.starting:
                 time.sleep(max(0.0, min(0.01, pending[i][0] - now)) if i < len(pending) else 0.0)
                 continue
             self.step()
