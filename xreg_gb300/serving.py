@@ -9,10 +9,12 @@ pose, optimizer schedule) arrive at any time.  Each server step:
      optimizer state); a job starts (volume upload, first level set-up) on a
      worker thread while the active jobs keep stepping, and joins the steps
      once it has started;
-  2. asks every active job for its current population (CMA-ES sample);
-  3. evaluates all populations with ONE job-set call: one persistent DRR launch
-     over every job's (tile, pose) work, then each job's metrics;
-  4. hands each job its values (CMA-ES update, level change, completion) and
+  2. samples every active job's population (CMA-ES sample or trust-region ask),
+     evaluates all populations with one persistent DRR launch over every job's
+     (tile, pose) work followed by each job's metrics, and updates every
+     optimizer: one xr_regi_jobset_step call (native_step; otherwise the same
+     steps driven from Python around one job-set evaluation);
+  3. ends levels whose optimizer stopped (level change or completion) and
      retires finished jobs, recording their latency from arrival.
 
 Because each job's optimizer has its own random stream and the job-set values
