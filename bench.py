@@ -676,6 +676,7 @@ def _serving(dev, n_req: int, rate: float):
             t0 = time.perf_counter()
             st = srv.run(arrivals=list(zip(offsets.tolist(), jobs)))
             makespan = time.perf_counter() - t0
+        srv.close()
         errs = [pose_error(j.final_pose, g, j.vol) for j, g in zip(jobs, gts)]
         s = st.summary()
         return {"p50_latency_s": round(s["p50_s"], 3), "p99_latency_s": round(s["p99_s"], 3),

@@ -71,6 +71,10 @@ class RegistrationServer:
         self.starting: list = []  # (job, future) of jobs starting on the worker thread
         self._pool = concurrent.futures.ThreadPoolExecutor(max_workers=1)
 
+    def close(self) -> None:
+        """Waits for job starts in flight and ends the worker thread."""
+        self._pool.shutdown(wait=True)
+
     def submit(self, job: Registration, t_arrival: float | None = None) -> None:
         job.t_submit = time.perf_counter() if t_arrival is None else t_arrival
         self.queue.append(job)
