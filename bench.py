@@ -723,32 +723,36 @@ def _max_over_ranks(x, world):
     return float(t.item())
 
 
-def _config(w, voxel: str) -> dict:
+def _config_fields(step_mm: float, voxel: str) -> dict:
     """The workload as both arms name it."""
     return {"workload": "batched population: 256^3 phantom @1 mm, 1536^2@0.194 mm detector ds 4x -> 384^2, "
                         "lambda=100, grad-NCC 5x5 Gaussian + Sobel",
-            "volume": "256x256x256 " + voxel, "detector": "384x384", "pop": POP, "step_mm": w.step}
+            "volume": "256x256x256 " + voxel, "detector": "384x384", "pop": POP, "step_mm": step_mm}
+
+
+def _config(w, voxel: str) -> dict:
+    return _config_fields(w.step, voxel)
 
 
 def run_reference(a, rank, world):
-    """The reference's CPU path (restated: the reference cannot be compiled here)
-    timed on the host cores: each step evaluates a bounded sample of poses."""
+    """The reference's CPU path timed on the host cores, on the same workload:
+    every step evaluates one full population of lambda = 100 poses (DRR +
+    grad-NCC).  xReg's ray caster cannot be compiled here (ITK, Eigen, OpenCV,
+    TBB absent), so its restatement in C (oracle/) runs, with all host threads.
+    Nothing of the product is imported or loaded on this path; the inputs come
+    from oracle/workload.py (the same seeded generators)."""
     if rank != 0:
         return None
-    from xreg_gb300 import synth
     from oracle import oracle as O
-    from tests.helpers import oracle_cams, oracle_geom
-    w = _workload(0)
+    from oracle import workload as W
+    w = W.Batched(0, POP)
     cores = O.set_threads(os.cpu_count() or 1)
-    geom, cams = oracle_geom(w.vol), oracle_cams(w.cams)
-    fixed = synth.add_noise(O.drr_f32(w.vol.voxels, geom, cams, synth.fixed_pose(w)[None], step=w.step)[0], 0.01,
-                            w.seed + 2)
-    poses = _populations(w, 1, 999)[0]
-    per_step = 2
+    fixed = W.add_noise(O.drr_f32(w.voxels, w.geom, w.cams, w.fixed_pose()[None], step=w.step)[0], 0.01,
+                        w.seed + 2)
+    pops = w.populations(a.warmup + a.steps, 1234)
 
     def one_step(k):
-        d = O.drr_f32(w.vol.voxels, geom, cams, poses[(k * per_step) % POP:(k * per_step) % POP + per_step],
-                      step=w.step)
+        d = O.drr_f32(w.voxels, w.geom, w.cams, pops[k], step=w.step)
         O.grad_ncc(fixed, d)
 
     for k in range(a.warmup):
@@ -757,20 +761,32 @@ def run_reference(a, rank, world):
     for k in range(a.steps):
         one_step(a.warmup + k)
     t = time.perf_counter() - t0
-    v = a.steps * per_step / t
+    v = a.steps * POP / t
+    cfg = _config_fields(w.step, "f32")
     return {
         "impl": "reference",
         "metric": "poses/sec (DRR+grad-NCC pose evaluations, batched population)",
         "value": round(v, 3), "unit": "poses/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": round(t * 1e3 / a.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantom, sampled poses, noisy fixed DRR)",
-        "config": dict(_config(w, "f32"), pop_per_step=per_step,
-                       parallelism="rank 0 on the host cores"),
+        "config": dict(cfg, parallelism="rank 0 on the host cores"),
         "cpu_baseline": {"value": round(v, 3), "unit": "poses/s", "cores": cores, "kind": "port",
-                         "sample": f"{per_step} poses per step; xReg's CPU ray caster + grad-NCC restated in C "
-                                   "(the reference needs ITK/OpenCV/TBB, absent here)"},
+                         "sample": f"{a.steps} full populations of {POP} poses; xReg's CPU ray caster + grad-NCC "
+                                   "restated in C (the reference needs ITK/OpenCV/TBB, absent here)"},
         "e2e": {"value": round(v, 3), "unit": "poses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "product_loaded": _product_loaded(),
     }
+
+
+def _product_loaded() -> bool:
+    """Whether this process imported the product package or mapped its library."""
+    if any(m == "xreg_gb300" or m.startswith("xreg_gb300.") for m in sys.modules):
+        return True
+    try:
+        with open("/proc/self/maps") as f:
+            return "libxreg_gb300" in f.read()
+    except OSError:
+        return False
 
 
 def main():

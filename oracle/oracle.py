@@ -31,7 +31,9 @@ class camera(C.Structure):
 
 
 class proj_geom(C.Structure):
-    _fields_ = [(n, C.c_float * 3) for n in ("src", "d0", "dc", "dr", "e0", "ec", "er", "pad")]
+    """Per-projection float set-up (xo_proj_geom): 44 floats."""
+    _fields_ = [("M", C.c_float * 12), ("pin_idx", C.c_float * 3), ("Ki", C.c_float * 9), ("dz", C.c_float),
+                ("zadj", C.c_float), ("Ei", C.c_float * 12), ("pin", C.c_float * 3), ("pad", C.c_float * 3)]
 
 
 def build(force: bool = False) -> Path:
@@ -40,11 +42,19 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
-def build_ref(ref_dir: str = "/root/reference") -> Path | None:
-    """Compiles the reference's vendored CMA-ES when its sources are present."""
+def reference_dir() -> str | None:
+    """The xReg source tree named by XREG_REFERENCE_DIR, if it is set and present."""
+    d = os.environ.get("XREG_REFERENCE_DIR")
+    return d if d and Path(d).is_dir() else None
+
+
+def build_ref(ref_dir: str | None = None) -> Path | None:
+    """Compiles the reference's vendored CMA-ES when its sources are present
+    (ref_dir, else XREG_REFERENCE_DIR)."""
     if CMAES_REF.exists():
         return CMAES_REF
-    if not Path(ref_dir, "third_party", "cmaes", "cmaes.c").exists():
+    ref_dir = ref_dir or reference_dir()
+    if not ref_dir or not Path(ref_dir, "third_party", "cmaes", "cmaes.c").exists():
         return None
     subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_DIR={ref_dir}"], check=True)
     return CMAES_REF
@@ -70,6 +80,9 @@ def lib() -> C.CDLL:
         L.xo_camera_setup_naive.argtypes = [C.c_double, i64, i64, C.c_double, C.c_double, C.c_int32,
                                             C.POINTER(camera)]
         L.xo_camera_downsample.argtypes = [C.POINTER(camera), C.c_double, C.c_int, C.POINTER(camera)]
+        L.xo_camera_crop_boundary.argtypes = [C.POINTER(camera), i64, C.POINTER(camera)]
+        L.xo_frame_mul_f32.argtypes = [P, P, P]
+        L.xo_ray_setups.argtypes = [C.POINTER(vol_geom), C.POINTER(camera), i64, P, P, i64, C.c_float, P, P, P, P]
         L.xo_grad_images.argtypes = [P, i64, i64, C.c_int, P, P]
         L.xo_ncc.argtypes = [P, P, i64, i64, P, P]
         L.xo_grad_ncc.argtypes = [P, P, i64, i64, i64, C.c_int, P, P]
@@ -129,6 +142,45 @@ def camera_downsample(c: camera, ds: float, force_even: bool = False) -> camera:
     return d
 
 
+def camera_crop_boundary(c: camera, width: int) -> camera:
+    d = camera()
+    lib().xo_camera_crop_boundary(C.byref(c), int(width), C.byref(d))
+    return d
+
+
+def camera_fields(c: camera) -> tuple:
+    """Every field of a camera, for field-by-field comparisons."""
+    return (tuple(c.intrins), tuple(c.extrins), c.num_det_rows, c.num_det_cols, c.det_row_spacing,
+            c.det_col_spacing, c.focal_len, c.coord_frame_type)
+
+
+def frame_mul_f32(a, b) -> np.ndarray:
+    """FrameTransform product a * b in xReg's float arithmetic (4x4 in, 4x4 out)."""
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(16)
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(16)
+    out = np.zeros(16)
+    lib().xo_frame_mul_f32(_p(a), _p(b), _p(out))
+    return out.reshape(4, 4)
+
+
+def ray_setups(geom: vol_geom, cams, poses, cam_idx=None, step=1.0):
+    """xReg's per-ray float set-up of every pixel: (hit, samples, start, step vector),
+    shapes [n, rows, cols] and [n, rows, cols, 3]."""
+    poses = np.ascontiguousarray(np.asarray(poses, dtype=np.float64).reshape(-1, 16))
+    n = poses.shape[0]
+    cams = list(cams)
+    ci = np.zeros(n, dtype=np.int32) if cam_idx is None else np.ascontiguousarray(cam_idx, dtype=np.int32)
+    carr = (camera * len(cams))(*cams)
+    rows, cols = cams[0].num_det_rows, cams[0].num_det_cols
+    hit = np.zeros((n, rows, cols), np.int32)
+    ns = np.zeros((n, rows, cols), np.uint64)
+    st = np.zeros((n, rows, cols, 3), np.float32)
+    sv = np.zeros((n, rows, cols, 3), np.float32)
+    assert lib().xo_ray_setups(C.byref(geom), carr, len(cams), _p(poses), _p(ci), n, step, _p(hit), _p(ns), _p(st),
+                               _p(sv)) == 0
+    return hit, ns, st, sv
+
+
 def drr_f32(voxels, geom: vol_geom, cams, poses, cam_idx=None, step=1.0, kernel=0, store=0, default_bg=0.0,
             bg_projs=None, out=None, count=False):
     """FP32 xReg-CPU semantics.  poses: [n, 4, 4] cam -> ITK phys. Returns [n, rows, cols]."""
@@ -172,7 +224,7 @@ def proj_geoms(geom: vol_geom, cams, poses, cam_idx=None) -> np.ndarray:
     carr = (camera * len(cams))(*cams)
     out = (proj_geom * n)()
     lib().xo_proj_geoms(C.byref(geom), carr, _p(poses), _p(ci), n, out)
-    return np.frombuffer(out, dtype=np.float32).reshape(n, 24).copy()
+    return np.frombuffer(out, dtype=np.float32).reshape(n, 44).copy()
 
 
 def grad_images(img, smooth_ksize=5):

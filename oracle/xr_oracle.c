@@ -48,13 +48,15 @@
  *     order 3 (Unser, "Splines: a perfect fit for signal and image processing",
  *     1999, Box 2): mirror-boundary recursive prefilter, 4 x 4 weights.
  *
- * Geometry precision contract (shared with the CUDA kernels on purpose): the
- * per-projection set-up (index<->physical inverse, camera inverse, pose
- * composition) is done in double with a fixed operation order, rounded to float,
- * and the per-ray work is done in float with a fixed operation order and no
- * fused multiply-add.  Compile with -ffp-contract=off.  This makes the sample
- * count floor(len/step)+1 of every ray identical between this file and the GPU,
- * so one-sample flips cannot break the DRR tolerance.
+ * Geometry precision contract: the FP32 restatement repeats xReg's own float
+ * geometry -- camera set-up (MakeNaiveIntrins, DownsampleCameraModel, SE3Inv,
+ * Matrix3f::inverse), the index <-> physical inverse, the per-ray
+ * phys_to_idx * pose composition, detector point, slab test, nudge, lengths
+ * and step count -- in Eigen 3.3's evaluation order (see "xReg's float
+ * geometry" below) with no fused multiply-add (compile with -ffp-contract=off).
+ * A one-sample difference on a ray moves its pixel by about 1/300, so this is
+ * what makes the sample counts xReg's.  The FP64 twin does the same algorithm
+ * with every quantity in double and is the error reference.
  */
 #include <math.h>
 #include <float.h>
@@ -91,15 +93,18 @@ typedef struct {
   int32_t pad_;
 } xo_camera;
 
-/* Per-projection ray set-up, all in volume index coordinates. */
+/* Per-projection ray set-up in float, as xReg evaluates it for each ray of a
+ * projection (the same result for every ray): camera -> index transform M,
+ * pinhole in index coordinates, intrins_inv, det_z_val, z_adjust(2),
+ * extrins_inv and the pinhole in camera-world coordinates. */
 typedef struct {
-  float src[3];   /* pinhole                                                  */
-  float d0[3];    /* pinhole -> detector pixel (0,0)                          */
-  float dc[3];    /* + per detector column                                    */
-  float dr[3];    /* + per detector row                                       */
-  float e0[3];    /* same vectors in camera-world coords (for the mm length)  */
-  float ec[3];
-  float er[3];
+  float M[12];      /* L row-major, then t */
+  float pin_idx[3];
+  float Ki[9];
+  float dz;
+  float zadj;
+  float Ei[12];     /* L row-major, then t */
+  float pin[3];
   float pad[3];
 } xo_proj_geom;
 
@@ -184,82 +189,192 @@ static void m3_vec(const double a[9], const double v[3], double out[3]) {
     out[i] = (a[i * 3 + 0] * v[0] + a[i * 3 + 1] * v[1]) + a[i * 3 + 2] * v[2];
 }
 
-/* Per-projection set-up in double.  The CUDA geometry kernel evaluates the same
- * expressions in the same order (explicitly rounded double ops). */
+/* ------------------------------------------------------------------------- */
+/* xReg's float geometry in Eigen 3.3's evaluation order                      */
+/* ------------------------------------------------------------------------- */
+/* xReg keeps poses, cameras and the index <-> physical transform as Eigen float
+ * objects and sets up each ray in float (xregRayCastLineIntCPU.cpp:196-259), so
+ * the FP32 restatement repeats that arithmetic, in the order Eigen 3.3 (the
+ * reference's pinned version, README.md:60-70) evaluates it on x86-64 with its
+ * default SSE2 vectorisation and without FMA:
+ *   fixed-size 3-element products and norms: a0 + (a1 + a2) (unrolled reduction
+ *     split 1 + 2);
+ *   Transform * Vector3: 4x4 matrix times [p; 1] summed by columns:
+ *     ((a0 + a1) + a2) + t;
+ *   products through runtime-sized blocks (block(0,0,3,3) * v and its norm,
+ *     SE3Inv): (a0 + a1) + a2;
+ *   Matrix3f::inverse: adjugate, determinant from the first column, 1 / det. */
+typedef struct { float L[9]; float t[3]; } xo_aff;
+
+static float xf_fix3(float a0, float a1, float a2, float b0, float b1, float b2) {
+  return a0 * b0 + (a1 * b1 + a2 * b2);
+}
+static float xf_loop3(float a0, float a1, float a2, float b0, float b1, float b2) {
+  return (a0 * b0 + a1 * b1) + a2 * b2;
+}
+
+static void xf_inv3(const float m[9], float out[9]) {
+  float cof[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+      cof[i * 3 + j] = m[i1 * 3 + j1] * m[i2 * 3 + j2] - m[i1 * 3 + j2] * m[i2 * 3 + j1];
+    }
+  const float det = xf_fix3(cof[0], cof[3], cof[6], m[0], m[3], m[6]);
+  const float invdet = 1.0f / det;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) out[r * 3 + c] = cof[c * 3 + r] * invdet;
+}
+
+/* Transform * Vector3 */
+static void xf_apply(const xo_aff* a, const float p[3], float out[3]) {
+  float o[3];
+  for (int i = 0; i < 3; ++i) o[i] = xf_loop3(a->L[i * 3], a->L[i * 3 + 1], a->L[i * 3 + 2], p[0], p[1], p[2]) + a->t[i];
+  memcpy(out, o, sizeof(o));
+}
+
+/* Transform * Transform (affine): linear parts, then La tb + ta */
+static void xf_compose(const xo_aff* a, const xo_aff* b, xo_aff* out) {
+  xo_aff r;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j)
+      r.L[i * 3 + j] = xf_fix3(a->L[i * 3], a->L[i * 3 + 1], a->L[i * 3 + 2], b->L[j], b->L[3 + j], b->L[6 + j]);
+    r.t[i] = xf_fix3(a->L[i * 3], a->L[i * 3 + 1], a->L[i * 3 + 2], b->t[0], b->t[1], b->t[2]) + a->t[i];
+  }
+  *out = r;
+}
+
+/* Transform::inverse (affine): L^-1, -(L^-1 t) */
+static void xf_inverse(const xo_aff* a, xo_aff* out) {
+  xo_aff r;
+  xf_inv3(a->L, r.L);
+  for (int i = 0; i < 3; ++i) r.t[i] = -xf_fix3(r.L[i * 3], r.L[i * 3 + 1], r.L[i * 3 + 2], a->t[0], a->t[1], a->t[2]);
+  *out = r;
+}
+
+/* SE3Inv (xregRigidUtils.cpp:29-38) */
+static void xf_se3_inv(const xo_aff* e, xo_aff* out) {
+  xo_aff r;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) r.L[i * 3 + j] = e->L[j * 3 + i];
+  for (int i = 0; i < 3; ++i) r.t[i] = -xf_loop3(r.L[i * 3], r.L[i * 3 + 1], r.L[i * 3 + 2], e->t[0], e->t[1], e->t[2]);
+  *out = r;
+}
+
+/* ITKImagePhysicalPointTransformsAsEigen (xregITKBasicImageUtils.h:133-165),
+ * inverted as in RayCasterLineIntCPU::compute (xregRayCastLineIntCPU.cpp:307-309). */
+static void xo_phys_to_idx_f32(const xo_vol_geom* vg, xo_aff* out) {
+  xo_aff i2p;
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) i2p.L[r * 3 + c] = (float)(vg->direction[r * 3 + c] * vg->spacing[c]);
+    i2p.t[r] = (float)vg->origin[r];
+  }
+  xf_inverse(&i2p, out);
+}
+
+/* Per-projection set-up (CameraModel::setup derived members,
+ * xregPerspectiveXform.cpp:302-334; xform_cam_to_itk_idx and the pinhole,
+ * xregRayCastLineIntCPU.cpp:206-212).  The camera's fields and the pose are the
+ * float values xReg holds (double fields rounded to float). */
+static void xo_proj_geom_from(const xo_aff* p2i, const xo_camera* cam, const double pose_cam_to_phys[16],
+                              xo_proj_geom* out) {
+  float K[9];
+  for (int k = 0; k < 9; ++k) K[k] = (float)cam->intrins[k];
+  float Ki[9];
+  xf_inv3(K, Ki);
+  xo_aff E, Ei;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) E.L[i * 3 + j] = (float)cam->extrins[i * 4 + j];
+    E.t[i] = (float)cam->extrins[i * 4 + 3];
+  }
+  xf_se3_inv(&E, &Ei);
+  const float f = (float)cam->focal_len;
+  float pin[3];
+  if (cam->coord_frame_type == 2) {
+    const float pz[3] = {0.0f, 0.0f, f};
+    xf_apply(&Ei, pz, pin);
+  } else {
+    memcpy(pin, Ei.t, sizeof(pin));
+  }
+  xo_aff pose, M;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) pose.L[i * 3 + j] = (float)pose_cam_to_phys[i * 4 + j];
+    pose.t[i] = (float)pose_cam_to_phys[i * 4 + 3];
+  }
+  xf_compose(p2i, &pose, &M);
+  float pi[3];
+  xf_apply(&M, pin, pi);
+  memset(out, 0, sizeof(*out));
+  memcpy(out->M, M.L, sizeof(M.L));
+  memcpy(out->M + 9, M.t, sizeof(M.t));
+  memcpy(out->pin_idx, pi, sizeof(pi));
+  memcpy(out->Ki, Ki, sizeof(Ki));
+  out->dz = (cam->coord_frame_type == 1) ? -f : f;
+  out->zadj = (cam->coord_frame_type == 2) ? -f : 0.0f;
+  memcpy(out->Ei, Ei.L, sizeof(Ei.L));
+  memcpy(out->Ei + 9, Ei.t, sizeof(Ei.t));
+  memcpy(out->pin, pin, sizeof(pin));
+}
+
 XO_EXPORT void xo_proj_geom_one(const xo_vol_geom* vg, const xo_camera* cam,
                                 const double pose_cam_to_phys[16], xo_proj_geom* out) {
-  /* index -> physical: A = D * diag(spacing), origin o (xregITKBasicImageUtils.h:133-165) */
-  double A[9];
+  xo_aff p2i;
+  xo_phys_to_idx_f32(vg, &p2i);
+  xo_proj_geom_from(&p2i, cam, pose_cam_to_phys, out);
+}
+
+/* One ray (xregRayCastLineIntCPU.cpp:196-259): returns 1 and the start point,
+ * step vector and num_steps quotient when the segment is sampled, 0 otherwise. */
+static int xo_ray_setup_f32(const xo_proj_geom* g, float col, float row, const float maxb[3], float step,
+                            float start[3], float stepv[3], float* quot) {
+  /* ind_pt_to_phys_det_pt (xregPerspectiveXform.cpp:401-414) */
+  const float s0 = g->dz * col, s1 = g->dz * row, s2 = g->dz * 1.0f;
+  float q[3];
+  for (int i = 0; i < 3; ++i) q[i] = xf_fix3(g->Ki[i * 3], g->Ki[i * 3 + 1], g->Ki[i * 3 + 2], s0, s1, s2);
+  q[0] = q[0] + 0.0f;
+  q[1] = q[1] + 0.0f;
+  q[2] = q[2] + g->zadj;
+  float det[3];
+  for (int i = 0; i < 3; ++i) det[i] = xf_loop3(g->Ei[i * 3], g->Ei[i * 3 + 1], g->Ei[i * 3 + 2], q[0], q[1], q[2]) + g->Ei[9 + i];
+  float d[3];
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) A[i * 3 + j] = vg->direction[i * 3 + j] * vg->spacing[j];
-  double Ai[9];
-  m3_inverse(A, Ai);
-  double ti[3];
-  m3_vec(Ai, vg->origin, ti);
-  ti[0] = -ti[0]; ti[1] = -ti[1]; ti[2] = -ti[2];
-
-  /* camera: K^-1, extrinsic inverse (rigid), pinhole (xregPerspectiveXform.cpp:230-334) */
-  double Ki[9];
-  m3_inverse(cam->intrins, Ki);
-  double ER[9], Et[3];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) ER[i * 3 + j] = cam->extrins[j * 4 + i];  /* R^T */
-  {
-    double t[3] = {cam->extrins[3], cam->extrins[7], cam->extrins[11]};
-    m3_vec(ER, t, Et);
-    Et[0] = -Et[0]; Et[1] = -Et[1]; Et[2] = -Et[2];
-  }
-  const double f = cam->focal_len;
-  double pin[3];
-  if (cam->coord_frame_type == 2) {
-    double pz[3] = {0.0, 0.0, f}, tmp[3];
-    m3_vec(ER, pz, tmp);
-    pin[0] = tmp[0] + Et[0]; pin[1] = tmp[1] + Et[1]; pin[2] = tmp[2] + Et[2];
-  } else {
-    pin[0] = Et[0]; pin[1] = Et[1]; pin[2] = Et[2];
-  }
-  const double dz = (cam->coord_frame_type == 1) ? -f : f;
-  const double zadj = (cam->coord_frame_type == 2) ? -f : 0.0;
-
-  /* detector point of pixel (c, r): E^-1 (K^-1 (dz [c r 1]) + zadj) (xregPerspectiveXform.cpp:401-414) */
-  double kc[3] = {Ki[0] * dz, Ki[3] * dz, Ki[6] * dz};
-  double kr[3] = {Ki[1] * dz, Ki[4] * dz, Ki[7] * dz};
-  double k0[3] = {Ki[2] * dz, Ki[5] * dz, Ki[8] * dz + zadj};
-  double dcol[3], drow[3], det0[3];
-  m3_vec(ER, kc, dcol);
-  m3_vec(ER, kr, drow);
-  m3_vec(ER, k0, det0);
-  det0[0] += Et[0]; det0[1] += Et[1]; det0[2] += Et[2];
-  double e0[3] = {det0[0] - pin[0], det0[1] - pin[1], det0[2] - pin[2]};
-
-  /* camera -> index: M = phys_to_idx * pose (xregRayCastLineIntCPU.cpp:207-208) */
-  double TR[9], Tt[3];
-  for (int i = 0; i < 3; ++i) {
-    for (int j = 0; j < 3; ++j) TR[i * 3 + j] = pose_cam_to_phys[i * 4 + j];
-    Tt[i] = pose_cam_to_phys[i * 4 + 3];
-  }
-  double MR[9], Mt[3];
-  m3_mul(Ai, TR, MR);
-  m3_vec(Ai, Tt, Mt);
-  Mt[0] += ti[0]; Mt[1] += ti[1]; Mt[2] += ti[2];
-
-  double src[3], d0[3], dc[3], dr[3];
-  m3_vec(MR, pin, src);
-  src[0] += Mt[0]; src[1] += Mt[1]; src[2] += Mt[2];
-  m3_vec(MR, e0, d0);
-  m3_vec(MR, dcol, dc);
-  m3_vec(MR, drow, dr);
-
+    d[i] = (xf_loop3(g->M[i * 3], g->M[i * 3 + 1], g->M[i * 3 + 2], det[0], det[1], det[2]) + g->M[9 + i]) - g->pin_idx[i];
+  /* RayRectIntersect, limited to the segment (xregSpatialPrimitives.cpp:176-221) */
+  float t0 = 0.0f, t1 = 1.0f;
   for (int k = 0; k < 3; ++k) {
-    out->src[k] = (float)src[k];
-    out->d0[k] = (float)d0[k];
-    out->dc[k] = (float)dc[k];
-    out->dr[k] = (float)dr[k];
-    out->e0[k] = (float)e0[k];
-    out->ec[k] = (float)dcol[k];
-    out->er[k] = (float)drow[k];
-    out->pad[k] = 0.0f;
+    if ((double)fabsf(d[k]) > 1.0e-8) {
+      const float inv = 1.0f / d[k];
+      float ta = (0.0f - g->pin_idx[k]) * inv;
+      float tb = (maxb[k] - g->pin_idx[k]) * inv;
+      if (tb < ta) { float tmp = ta; ta = tb; tb = tmp; }
+      t0 = (t0 < ta) ? ta : t0;
+      t1 = (tb < t1) ? tb : t1;
+      if (t0 > t1) return 0;
+    } else if (g->pin_idx[k] < 0.0f || g->pin_idx[k] > maxb[k]) {
+      return 0;
+    }
   }
+  if (!((t1 - t0) > 2.0f * 1.0e-3f)) return 0;
+  t0 = t0 + 1.0e-3f;
+  t1 = t1 - 1.0e-3f;
+  for (int i = 0; i < 3; ++i) start[i] = g->pin_idx[i] + t0 * d[i];
+  const float dlen = sqrtf(xf_fix3(d[0], d[1], d[2], d[0], d[1], d[2]));
+  const float ilen = (t1 - t0) * dlen;
+  float u[3];
+  for (int i = 0; i < 3; ++i) u[i] = det[i] - g->pin[i];
+  const float z = xf_fix3(u[0], u[1], u[2], u[0], u[1], u[2]);
+  if (z > 0.0f) {
+    const float n = sqrtf(z);
+    for (int i = 0; i < 3; ++i) u[i] = u[i] / n;
+  }
+  for (int i = 0; i < 3; ++i) u[i] = u[i] * step;
+  float w[3];
+  for (int i = 0; i < 3; ++i) w[i] = xf_loop3(g->M[i * 3], g->M[i * 3 + 1], g->M[i * 3 + 2], u[0], u[1], u[2]);
+  const float slen = sqrtf(xf_loop3(w[0], w[1], w[2], w[0], w[1], w[2]));
+  *quot = ilen / slen;
+  const float sc = slen / dlen;
+  for (int i = 0; i < 3; ++i) stepv[i] = d[i] * sc;
+  return 1;
 }
 
 /* ------------------------------------------------------------------------- */
@@ -311,7 +426,8 @@ typedef struct {
   const double* geo64;       /* FP64 mode: per projection 21 doubles */
 } xo_drr_ctx;
 
-/* FP32 per-ray semantics (the "xReg CPU" target), fixed op order, no FMA. */
+/* FP32 per-ray semantics (the "xReg CPU" target): xReg's float set-up, then
+ * the sample loop (xregRayCastLineIntCPU.cpp:253-282). */
 static void xo_drr_f32_range(void* vctx, int64_t b, int64_t e) {
   xo_drr_ctx* c = (xo_drr_ctx*)vctx;
   const int64_t npix = c->rows * c->cols;
@@ -321,54 +437,11 @@ static void xo_drr_f32_range(void* vctx, int64_t b, int64_t e) {
     const int64_t off = idx - p * npix;
     const int64_t row = off / c->cols;
     const int64_t col = off - row * c->cols;
-    const xo_proj_geom* g = &c->geo[p];
-    const float fc = (float)col, fr = (float)row;
-    float dir[3], v[3];
-    for (int k = 0; k < 3; ++k) {
-      float t1 = fc * g->dc[k];
-      float t2 = g->d0[k] + t1;
-      float t3 = fr * g->dr[k];
-      dir[k] = t2 + t3;
-      float u1 = fc * g->ec[k];
-      float u2 = g->e0[k] + u1;
-      float u3 = fr * g->er[k];
-      v[k] = u2 + u3;
-    }
-    /* RayRectIntersect, limited to the segment (xregSpatialPrimitives.cpp:176-221) */
-    int hit = 1;
-    float t0 = 0.0f, t1 = 1.0f;
-    for (int k = 0; k < 3; ++k) {
-      if ((double)fabsf(dir[k]) > 1.0e-8) {
-        const float inv = 1.0f / dir[k];
-        float ta = (0.0f - g->src[k]) * inv;
-        float tb = (maxb[k] - g->src[k]) * inv;
-        if (tb < ta) { float tmp = ta; ta = tb; tb = tmp; }
-        t0 = (t0 < ta) ? ta : t0;
-        t1 = (tb < t1) ? tb : t1;
-        if (t0 > t1) { hit = 0; break; }
-      } else if (g->src[k] < 0.0f || g->src[k] > maxb[k]) {
-        hit = 0; break;
-      }
-    }
     float sum = (c->kernel == XO_KERNEL_MAX) ? -FLT_MAX : 0.0f;
     uint64_t ns = 0;
-    if (hit && ((t1 - t0) > 2.0e-3f)) {
-      t0 = t0 + 1.0e-3f;
-      t1 = t1 - 1.0e-3f;
-      float pos[3];
-      for (int k = 0; k < 3; ++k) {
-        float a = t0 * dir[k];
-        pos[k] = g->src[k] + a;
-      }
-      const float vv0 = v[0] * v[0];
-      const float vv1 = v[1] * v[1];
-      const float vv2 = v[2] * v[2];
-      const float lc = sqrtf((vv0 + vv1) + vv2);
-      const float dt = t1 - t0;
-      const float len = dt * lc;
-      const uint64_t nsteps = (uint64_t)(len / c->step);
-      const float sc = c->step / lc;
-      float stepv[3] = {dir[0] * sc, dir[1] * sc, dir[2] * sc};
+    float pos[3], stepv[3], quot;
+    if (xo_ray_setup_f32(&c->geo[p], (float)col, (float)row, maxb, c->step, pos, stepv, &quot)) {
+      const uint64_t nsteps = (uint64_t)quot;
       for (uint64_t s = 0; s <= nsteps; ++s) {
         const float val = (float)xo_trilinear(c->vol, c->n[0], c->n[1], c->n[2], pos[0], pos[1], pos[2]);
         if (c->kernel == XO_KERNEL_MAX) sum = (sum < val) ? val : sum;
@@ -532,7 +605,9 @@ XO_EXPORT int xo_drr_f32(const float* vol, const xo_vol_geom* vg,
                          const float* bg_projs, float* out, uint64_t* nsamples) {
   if (xo_check_cams(cams, ncams)) return -1;
   xo_proj_geom* geo = (xo_proj_geom*)malloc(sizeof(xo_proj_geom) * (size_t)nproj);
-  for (int64_t p = 0; p < nproj; ++p) xo_proj_geom_one(vg, &cams[cam_idx[p]], poses + 16 * p, &geo[p]);
+  xo_aff p2i;
+  xo_phys_to_idx_f32(vg, &p2i);
+  for (int64_t p = 0; p < nproj; ++p) xo_proj_geom_from(&p2i, &cams[cam_idx[p]], poses + 16 * p, &geo[p]);
   const int64_t rows = cams[0].num_det_rows, cols = cams[0].num_det_cols;
   xo_pre_compute_f32(out, nproj, rows * cols, store, default_bg, bg_projs, cam_idx);
   xo_drr_ctx c;
@@ -566,7 +641,7 @@ XO_EXPORT int xo_drr_f64(const float* vol, const xo_vol_geom* vg,
   return 0;
 }
 
-/* Exposes the float set-up vectors (for tests of the geometry contract). */
+/* Exposes the per-projection float set-up (for tests of the geometry contract). */
 XO_EXPORT void xo_proj_geoms(const xo_vol_geom* vg, const xo_camera* cams, const double* poses,
                              const int32_t* cam_idx, int64_t nproj, xo_proj_geom* out) {
   for (int64_t p = 0; p < nproj; ++p) xo_proj_geom_one(vg, &cams[cam_idx[p]], poses + 16 * p, &out[p]);
@@ -576,35 +651,111 @@ XO_EXPORT void xo_proj_geoms(const xo_vol_geom* vg, const xo_camera* cams, const
 /* Camera model helpers                                                       */
 /* ------------------------------------------------------------------------- */
 /* CameraModel::setup(f, nr, nc, rs, cs) with MakeNaiveIntrins
- * (xregPerspectiveXform.cpp:200-254); frame type 1 (-z) by default. */
+ * (xregPerspectiveXform.cpp:200-254): CameraModel's members are floats, so the
+ * arguments become floats and K is formed in float; frame type 1 (-z) by
+ * default.  The double fields hold those float values. */
 XO_EXPORT void xo_camera_setup_naive(double f, int64_t nr, int64_t nc, double rs, double cs,
                                      int32_t frame_type, xo_camera* cam) {
   memset(cam, 0, sizeof(*cam));
+  const float ff = (float)f, fr = (float)rs, fc = (float)cs;
   cam->coord_frame_type = frame_type;
-  cam->focal_len = f;
+  cam->focal_len = ff;
   cam->num_det_rows = nr; cam->num_det_cols = nc;
-  cam->det_row_spacing = rs; cam->det_col_spacing = cs;
-  double K[9] = {f / cs, 0, 0, 0, f / rs, 0, 0, 0, 1};
-  if (frame_type == 1) { K[0] = -K[0]; K[4] = -K[4]; }
-  K[2] = (double)(nc - 1) * 0.5;
-  K[5] = (double)(nr - 1) * 0.5;
-  memcpy(cam->intrins, K, sizeof(K));
+  cam->det_row_spacing = fr; cam->det_col_spacing = fc;
+  float K[9] = {ff / fc, 0, 0, 0, ff / fr, 0, 0, 0, 1};
+  if (frame_type == 1) { K[0] *= -1.0f; K[4] *= -1.0f; }
+  /* (num_cols - 1) * 0.5 in double, stored into the float matrix */
+  K[2] = (float)((double)(nc - 1) * 0.5);
+  K[5] = (float)((double)(nr - 1) * 0.5);
+  for (int i = 0; i < 9; ++i) cam->intrins[i] = K[i];
   for (int i = 0; i < 16; ++i) cam->extrins[i] = (i % 5 == 0) ? 1.0 : 0.0;
 }
 
-/* DownsampleCameraModel (xregPerspectiveXform.cpp:654-689). */
+/* FocalLenFromIntrins (xregPerspectiveXform.cpp:186-190), float. */
+static float xo_focal_from_intrins(const float K[9], float xps, float yps) {
+  return (fabsf(K[0] * xps) + fabsf(K[4] * ((yps < 0) ? xps : yps))) / 2.0f;
+}
+
+/* DownsampleCameraModel (xregPerspectiveXform.cpp:654-689) in float; the new
+ * camera's focal length comes from CameraModel::setup(K, E, ...). */
 XO_EXPORT void xo_camera_downsample(const xo_camera* src, double ds, int force_even, xo_camera* dst) {
+  const float fds = (float)ds;
   *dst = *src;
-  dst->intrins[0] *= ds; dst->intrins[4] *= ds; dst->intrins[2] *= ds; dst->intrins[5] *= ds;
-  long nr = lround((double)src->num_det_rows * ds);
-  long nc = lround((double)src->num_det_cols * ds);
+  float K[9];
+  for (int i = 0; i < 9; ++i) K[i] = (float)src->intrins[i];
+  K[0] *= fds; K[4] *= fds; K[2] *= fds; K[5] *= fds;
+  long nr = lroundf((float)src->num_det_rows * fds);
+  long nc = lroundf((float)src->num_det_cols * fds);
   if (force_even) { if (nr % 2) --nr; if (nc % 2) --nc; }
+  for (int i = 0; i < 9; ++i) dst->intrins[i] = K[i];
+  for (int i = 0; i < 16; ++i) dst->extrins[i] = (float)src->extrins[i];
   dst->num_det_rows = nr; dst->num_det_cols = nc;
-  dst->det_row_spacing = src->det_row_spacing / ds;
-  dst->det_col_spacing = src->det_col_spacing / ds;
-  /* FocalLenFromIntrins (xregPerspectiveXform.cpp:186-190) */
-  const double xps = dst->det_col_spacing, yps = dst->det_row_spacing;
-  dst->focal_len = (fabs(dst->intrins[0] * xps) + fabs(dst->intrins[4] * ((yps < 0) ? xps : yps))) / 2.0;
+  const float rs = (float)src->det_row_spacing / fds, cs = (float)src->det_col_spacing / fds;
+  dst->det_row_spacing = rs;
+  dst->det_col_spacing = cs;
+  dst->focal_len = xo_focal_from_intrins(K, cs, rs);
+}
+
+/* UpdateCameraModelFor2DROI (xregPerspectiveXform.cpp:482-503) for a crop of
+ * `width` pixels on every side (CropBoundaryPixels, xregProjData.cpp:543-567). */
+XO_EXPORT void xo_camera_crop_boundary(const xo_camera* src, int64_t width, xo_camera* dst) {
+  *dst = *src;
+  float K[9];
+  for (int i = 0; i < 9; ++i) K[i] = (float)src->intrins[i];
+  K[2] -= (float)width;
+  K[5] -= (float)width;
+  for (int i = 0; i < 9; ++i) dst->intrins[i] = K[i];
+  for (int i = 0; i < 16; ++i) dst->extrins[i] = (float)src->extrins[i];
+  const float rs = (float)src->det_row_spacing, cs = (float)src->det_col_spacing;
+  dst->det_row_spacing = rs;
+  dst->det_col_spacing = cs;
+  dst->focal_len = xo_focal_from_intrins(K, cs, rs);
+  dst->num_det_rows = src->num_det_rows - 2 * width;
+  dst->num_det_cols = src->num_det_cols - 2 * width;
+}
+
+/* FrameTransform * FrameTransform in float (pre_multiply_all_xforms /
+ * post_multiply_all_xforms, xregRayCastInterface.cpp:235-261); row-major 4x4
+ * doubles holding float values in and out. */
+XO_EXPORT void xo_frame_mul_f32(const double* a, const double* b, double* out) {
+  xo_aff fa, fb, r;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) { fa.L[i * 3 + j] = (float)a[i * 4 + j]; fb.L[i * 3 + j] = (float)b[i * 4 + j]; }
+    fa.t[i] = (float)a[i * 4 + 3];
+    fb.t[i] = (float)b[i * 4 + 3];
+  }
+  xf_compose(&fa, &fb, &r);
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) out[i * 4 + j] = r.L[i * 3 + j];
+    out[i * 4 + 3] = r.t[i];
+    out[12 + i] = 0.0;
+  }
+  out[15] = 1.0;
+}
+
+/* Per-ray set-up of every pixel (test access to the geometry): hit flag,
+ * sample count, start point and step vector, [nproj][rows][cols]. */
+XO_EXPORT int xo_ray_setups(const xo_vol_geom* vg, const xo_camera* cams, int64_t ncams, const double* poses,
+                            const int32_t* cam_idx, int64_t nproj, float step, int32_t* hit, uint64_t* nsamples,
+                            float* start, float* stepv) {
+  if (xo_check_cams(cams, ncams)) return -1;
+  xo_aff p2i;
+  xo_phys_to_idx_f32(vg, &p2i);
+  const int64_t rows = cams[0].num_det_rows, cols = cams[0].num_det_cols;
+  const float maxb[3] = {(float)(vg->n[0] - 1), (float)(vg->n[1] - 1), (float)(vg->n[2] - 1)};
+  for (int64_t p = 0; p < nproj; ++p) {
+    xo_proj_geom g;
+    xo_proj_geom_from(&p2i, &cams[cam_idx[p]], poses + 16 * p, &g);
+    for (int64_t r = 0; r < rows; ++r)
+      for (int64_t c = 0; c < cols; ++c) {
+        const int64_t i = (p * rows + r) * cols + c;
+        float q = 0.0f;
+        hit[i] = xo_ray_setup_f32(&g, (float)c, (float)r, maxb, step, start + 3 * i, stepv + 3 * i, &q);
+        nsamples[i] = hit[i] ? (uint64_t)q + 1 : 0;
+        if (!hit[i]) for (int k = 0; k < 3; ++k) start[3 * i + k] = stepv[3 * i + k] = 0.0f;
+      }
+  }
+  return 0;
 }
 
 /* ------------------------------------------------------------------------- */

@@ -8,8 +8,30 @@ from oracle import oracle as O
 from xreg_gb300 import synth
 
 
+def oracle_camera(cam):
+    """The oracle's own camera model built by the same steps as the product's
+    (naive set-up, downsampling, crop, extrinsics); every field must agree."""
+    assert cam.recipe is not None, "a camera built from a raw descriptor has no set-up steps to repeat"
+    c = None
+    for step in cam.recipe:
+        kind, args = step[0], step[1:]
+        if kind == "naive":
+            c = O.camera_naive(*args)
+        elif kind == "downsample":
+            c = O.camera_downsample(c, args[0], args[1])
+        elif kind == "crop":
+            c = O.camera_crop_boundary(c, args[0])
+        elif kind == "extrins":
+            for i in range(16):
+                c.extrins[i] = args[0][i]
+        else:
+            raise ValueError(kind)
+    assert O.camera_fields(c) == cam.as_tuple(), (O.camera_fields(c), cam.as_tuple())
+    return c
+
+
 def oracle_cams(cams):
-    return [O.camera_from_tuple(c.as_tuple()) for c in cams]
+    return [oracle_camera(c) for c in cams]
 
 
 def oracle_geom(vol):

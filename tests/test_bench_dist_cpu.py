@@ -60,3 +60,6 @@ def test_reference_arm_under_torchrun():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+    # the reference arm loads nothing of the product and times whole populations
+    assert d["product_loaded"] is False
+    assert d["config"]["pop"] == 100 and "100 poses" in d["cpu_baseline"]["sample"]

@@ -31,20 +31,48 @@ def test_library_exports_every_declared_symbol(xr):
 
 
 def test_camera_helpers_match_oracle(xr, oracle):
+    """The product's camera set-up (naive, downsample, crop) equals the oracle's
+    own restatement of xReg's float CameraModel field for field."""
     from xreg_gb300.api import CameraModel
-    from tests.helpers import oracle_cams
-    for args in [(1020.0, 1536, 1536, 0.194, 0.194), (1000.0, 255, 257, 0.3, 0.31), (900.0, 7, 9, 1.1, 0.9)]:
+    for args in [(1020.0, 1536, 1536, 0.194, 0.194), (1000.0, 255, 257, 0.3, 0.31), (900.0, 7, 9, 1.1, 0.9),
+                 (1020.0, 256, 256, 1.55, 1.55)]:
         for frame in (0, 1, 2):
             mine = CameraModel.naive(*args, coord_frame_type=frame)
             ref = oracle.camera_naive(*args, frame)
-            assert oracle_cams([mine])[0].intrins[:] == ref.intrins[:]
+            assert mine.as_tuple() == oracle.camera_fields(ref)
             for ds in (0.25, 0.5, 0.125, 0.33):
-                a = mine.downsample(ds)
-                b = oracle.camera_downsample(ref, ds)
-                assert (a.num_det_rows, a.num_det_cols) == (b.num_det_rows, b.num_det_cols)
-                assert a.desc.intrins[:] == b.intrins[:]
-                assert a.focal_len == b.focal_len
-                assert a.desc.det_row_spacing == b.det_row_spacing
+                for even in (False, True):
+                    b = oracle.camera_downsample(ref, ds, even)
+                    if b.num_det_rows < 1 or b.num_det_cols < 1:
+                        with pytest.raises(Exception):
+                            mine.downsample(ds, even)  # no pixels left: refused
+                        continue
+                    a = mine.downsample(ds, even)
+                    assert a.as_tuple() == oracle.camera_fields(b)
+                    if a.num_det_rows > 8 and a.num_det_cols > 8:
+                        assert a.crop_boundary(3).as_tuple() == oracle.camera_fields(
+                            oracle.camera_crop_boundary(b, 3))
+
+
+def test_camera_fields_are_xreg_floats(xr, oracle):
+    """CameraModel's members are floats in xReg: every field holds a float value,
+    the intrinsics are divided in float, and a downsampled camera's focal length
+    is FocalLenFromIntrins of its float intrinsics."""
+    from xreg_gb300.api import CameraModel
+    cam = CameraModel.naive(1020.0, 1536, 1536, 0.194, 0.194)
+    for v in cam.as_tuple()[0] + (cam.desc.focal_len, cam.desc.det_row_spacing):
+        assert float(np.float32(v)) == v
+    assert cam.intrins[0, 0] == float(-(np.float32(1020.0) / np.float32(0.194)))
+    ds = cam.downsample(0.25)
+    k = np.float32(cam.intrins[0, 0]) * np.float32(0.25)
+    cs = np.float32(0.194) / np.float32(0.25)
+    assert ds.focal_len == float((abs(k * cs) + abs(k * cs)) / np.float32(2.0))
+    # the helpers rebuild the oracle's cameras from its own set-up
+    from tests.helpers import oracle_camera
+    view = CameraModel.naive(1020.0, 64, 64, 0.5, 0.5).downsample(0.5)
+    c, s = np.cos(0.3), np.sin(0.3)
+    view.set_extrins(np.array([[c, 0, s, 1.5], [0, 1, 0, -2.0], [-s, 0, c, 3.25], [0, 0, 0, 1.0]]))
+    assert oracle.camera_fields(oracle_camera(view)) == view.as_tuple()
 
 
 def test_invalid_arguments_report_errors(xr):

@@ -44,34 +44,105 @@ def test_uniform_box_step_rule(oracle):
 
 
 def test_linear_volume_riemann_sum(oracle):
-    """Trilinear interpolation is exact on an affine field, so the ray sum is an
-    arithmetic series: (n_samples) * (first + last) / 2 * step."""
+    """Trilinear interpolation is exact on an affine field, so a ray sum is an
+    arithmetic series over its samples p0 + k v, k < m:
+    step * (m f(p0) + grad(f).v m (m - 1) / 2), with p0, v and m from xReg's
+    float ray set-up.  Both restatements agree with it."""
     n = (16, 16, 16)
     z, y, x = np.meshgrid(np.arange(16), np.arange(16), np.arange(16), indexing="ij")
-    vox = (0.01 * x + 0.02 * y + 0.03 * z + 0.5).astype(np.float32)
+    slope = np.array([0.01, 0.02, 0.03])
+    vox = (slope[0] * x + slope[1] * y + slope[2] * z + 0.5).astype(np.float32)
     g = oracle.vol_geom_of(vox, (1.0, 1.0, 1.0))
     cam = oracle.camera_naive(1020.0, 5, 5, 1.0, 1.0)
     pose = _axis_pose(n, (1.0, 1.0, 1.0))
-    d64, ns = oracle.drr_f64(vox, g, [cam], pose[None], step=0.25, count=True)
-    # recompute first/last sample positions for the central ray analytically
+    hit, ns, st, sv = oracle.ray_setups(g, [cam], pose[None], step=0.25)
+    d32, n32 = oracle.drr_f32(vox, g, [cam], pose[None], step=0.25, count=True)
+    d64 = oracle.drr_f64(vox, g, [cam], pose[None], step=0.25)
+    assert hit.all() and (ns == n32).all()
+    for r in range(5):
+        for c in range(5):
+            m = int(ns[0, r, c])
+            p0 = st[0, r, c].astype(np.float64)
+            v = sv[0, r, c].astype(np.float64)
+            f0 = float(slope @ p0 + 0.5)
+            expect = 0.25 * (m * f0 + float(slope @ v) * m * (m - 1) / 2.0)
+            # float positions by repeated addition and a float sum: a few 1e-7
+            assert abs(d32[0, r, c] - expect) < 2e-6 * expect
+            # double geometry: the segment differs from the float one at ~1e-7
+            assert abs(d64[0, r, c] - expect) < 2e-6 * expect
+
+
+def test_ray_setup_follows_xreg_float_steps(oracle):
+    """The per-ray set-up equals a numpy restatement of the same float
+    operations (xregRayCastLineIntCPU.cpp:196-259 in Eigen's order), and the
+    start point and step vector are the values the DRR samples at."""
+    f32 = np.float32
+    vol = synth.phantom_volume((20, 18, 16), (1.5, 1.25, 2.0), 2)
+    g = oracle_geom(vol)
+    cam = oracle.camera_naive(1020.0, 6, 7, 4.0, 4.5)
+    pose = synth.perturb(vol, synth.gt_pose(vol), [3.0, -2.0, 1.0], [2.0, 1.0, -3.0])
+    hit, ns, st, sv = oracle.ray_setups(g, [cam], pose[None], step=0.5)
     geo = oracle.proj_geoms(g, [cam], pose[None])[0]
-    src, d0, dc, dr = geo[0:3], geo[3:6], geo[6:9], geo[9:12]
-    d = d0.astype(np.float64) + 2 * dc + 2 * dr
-    t0, t1 = 0.0, 1.0
-    for k in range(3):
-        if abs(d[k]) > 1e-8:
-            a, b = (0 - src[k]) / d[k], (n[k] - 1 - src[k]) / d[k]
-            t0, t1 = max(t0, min(a, b)), min(t1, max(a, b))
-    t0 += 1e-3
-    t1 -= 1e-3
-    m = int(ns[0, 2, 2])
-    lc = np.linalg.norm(geo[12:15].astype(np.float64) + 2 * geo[15:18] + 2 * geo[18:21])
-    p0 = src + t0 * d
-    p1 = p0 + (m - 1) * d * (0.25 / lc)
-    f = lambda p: 0.01 * p[0] + 0.02 * p[1] + 0.03 * p[2] + 0.5
-    expect = m * (f(p0) + f(p1)) / 2.0 * 0.25
-    # the analytic check uses the float-rounded set-up vectors, the FP64 twin the double ones
-    assert abs(d64[0, 2, 2] - expect) < 1e-7 * abs(expect)
+    M, pin_idx = geo[0:12], geo[12:15]
+    Ki, dz, zadj, Ei, pin = geo[15:24], geo[24], geo[25], geo[26:38], geo[38:41]
+
+    def fix3(a, b):  # a0 b0 + (a1 b1 + a2 b2)
+        return f32(f32(a[0] * b[0]) + f32(f32(a[1] * b[1]) + f32(a[2] * b[2])))
+
+    def loop3(a, b):  # (a0 b0 + a1 b1) + a2 b2
+        return f32(f32(f32(a[0] * b[0]) + f32(a[1] * b[1])) + f32(a[2] * b[2]))
+
+    maxb = [f32(19), f32(17), f32(15)]
+    for r in range(6):
+        for c in range(7):
+            s_ = [f32(dz * f32(c)), f32(dz * f32(r)), f32(dz)]
+            q = [fix3(Ki[3 * i:3 * i + 3], s_) for i in range(3)]
+            q[2] = f32(q[2] + zadj)
+            det = [f32(loop3(Ei[3 * i:3 * i + 3], q) + Ei[9 + i]) for i in range(3)]
+            d = [f32(f32(loop3(M[3 * i:3 * i + 3], det) + M[9 + i]) - pin_idx[i]) for i in range(3)]
+            t0, t1, ok = f32(0), f32(1), True
+            for k in range(3):
+                inv = f32(f32(1) / d[k])
+                ta, tb = f32(f32(0 - pin_idx[k]) * inv), f32(f32(maxb[k] - pin_idx[k]) * inv)
+                ta, tb = min(ta, tb), max(ta, tb)
+                t0, t1 = max(t0, ta), min(t1, tb)
+                ok = ok and t0 <= t1
+            ok = ok and f32(t1 - t0) > f32(2e-3)
+            assert bool(hit[0, r, c]) == ok
+            if not ok:
+                continue
+            t0, t1 = f32(t0 + f32(1e-3)), f32(t1 - f32(1e-3))
+            start = [f32(pin_idx[i] + f32(t0 * d[i])) for i in range(3)]
+            dlen = f32(np.sqrt(fix3(d, d)))
+            u = [f32(det[i] - pin[i]) for i in range(3)]
+            nrm = f32(np.sqrt(fix3(u, u)))
+            u = [f32(f32(ui / nrm) * f32(0.5)) for ui in u]
+            w = [loop3(M[3 * i:3 * i + 3], u) for i in range(3)]
+            slen = f32(np.sqrt(loop3(w, w)))
+            m = int(f32(f32(f32(t1 - t0) * dlen) / slen)) + 1
+            sc = f32(slen / dlen)
+            assert int(ns[0, r, c]) == m
+            assert st[0, r, c].tolist() == [float(v) for v in start]
+            assert sv[0, r, c].tolist() == [float(f32(d[i] * sc)) for i in range(3)]
+
+
+def test_frame_product_in_float(oracle):
+    """FrameTransform * FrameTransform: linear part a0 + (a1 + a2) per entry,
+    translation La tb + ta, in float."""
+    f32 = np.float32
+    rng = np.random.default_rng(3)
+    A = rigid(exp_se3(rng.normal(0, 0.3, 6))[:3, :3], rng.normal(0, 50, 3))
+    B = rigid(exp_se3(rng.normal(0, 0.3, 6))[:3, :3], rng.normal(0, 50, 3))
+    A, B = A.astype(f32).astype(np.float64), B.astype(f32).astype(np.float64)
+    got = oracle.frame_mul_f32(A, B)
+    for i in range(3):
+        for j in range(3):
+            a, b = A[i, :3].astype(f32), B[:3, j].astype(f32)
+            assert got[i, j] == float(f32(f32(a[0] * b[0]) + f32(f32(a[1] * b[1]) + f32(a[2] * b[2]))))
+        a, t = A[i, :3].astype(f32), B[:3, 3].astype(f32)
+        lt = f32(f32(a[0] * t[0]) + f32(f32(a[1] * t[1]) + f32(a[2] * t[2])))
+        assert got[i, 3] == float(f32(lt + f32(A[i, 3])))
+    np.testing.assert_allclose(got, A @ B, atol=1e-4)
 
 
 def test_fp32_matches_fp64_except_count_flips(oracle):
@@ -162,14 +233,21 @@ def test_patch_ncc_self(oracle):
 
 
 def test_camera_model(oracle):
+    """MakeNaiveIntrins / DownsampleCameraModel in float (CameraModel's members
+    are CoordScalar = float)."""
+    f32 = np.float32
     c = oracle.camera_naive(1020.0, 1536, 1536, 0.194, 0.194)
     K = np.array(c.intrins[:]).reshape(3, 3)
-    assert K[0, 0] == -1020.0 / 0.194 and K[1, 1] == -1020.0 / 0.194
+    k00 = -(f32(1020.0) / f32(0.194))
+    assert K[0, 0] == k00 and K[1, 1] == k00
     assert K[0, 2] == 767.5 and K[1, 2] == 767.5
     d = oracle.camera_downsample(c, 0.25)
     assert d.num_det_rows == 384 and d.num_det_cols == 384
-    assert abs(d.det_row_spacing - 0.776) < 1e-12
-    assert abs(d.focal_len - 1020.0) < 1e-9
+    assert d.det_row_spacing == f32(0.194) / f32(0.25)
+    # FocalLenFromIntrins of the downsampled float intrinsics: within an ulp of f
+    kd, cs = f32(k00 * f32(0.25)), f32(f32(0.194) / f32(0.25))
+    assert d.focal_len == float((abs(f32(kd * cs)) + abs(f32(kd * cs))) / f32(2.0))
+    assert abs(d.focal_len - 1020.0) < 2e-4
     assert np.array(d.intrins[:]).reshape(3, 3)[0, 2] == 767.5 * 0.25
 
 

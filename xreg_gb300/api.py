@@ -23,30 +23,37 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
 class CameraModel:
     """xreg::CameraModel (xregPerspectiveXform.h:108-273) as an xr_camera_desc."""
 
-    def __init__(self, desc: L.xr_camera_desc | None = None):
+    def __init__(self, desc: L.xr_camera_desc | None = None, recipe: tuple | None = None):
         self.desc = desc if desc is not None else L.xr_camera_desc()
+        # How the model was built (set-up, downsampling, crop, extrinsics), step
+        # by step; None for a model given as a raw descriptor.
+        self.recipe = recipe
+
+    def _derived(self, d, step) -> "CameraModel":
+        return CameraModel(d, None if self.recipe is None else self.recipe + (step,))
 
     @classmethod
     def naive(cls, focal_len: float, num_rows: int, num_cols: int, row_spacing: float, col_spacing: float,
               coord_frame_type: int = L.XR_CAM_FOCAL_NEG_Z) -> "CameraModel":
         """CameraModel::setup(f, nr, nc, rs, cs) (xregPerspectiveXform.cpp:230-254)."""
         d = L.xr_camera_desc()
-        call("xr_camera_setup_naive", float(focal_len), int(num_rows), int(num_cols), float(row_spacing),
-             float(col_spacing), int(coord_frame_type), C.byref(d))
-        return cls(d)
+        args = (float(focal_len), int(num_rows), int(num_cols), float(row_spacing), float(col_spacing),
+                int(coord_frame_type))
+        call("xr_camera_setup_naive", *args, C.byref(d))
+        return cls(d, (("naive",) + args,))
 
     def downsample(self, ds_factor: float, force_even_dims: bool = False) -> "CameraModel":
         """DownsampleCameraModel (xregPerspectiveXform.cpp:654-689)."""
         d = L.xr_camera_desc()
         call("xr_camera_downsample", C.byref(self.desc), float(ds_factor), int(force_even_dims), C.byref(d))
-        return CameraModel(d)
+        return self._derived(d, ("downsample", float(ds_factor), bool(force_even_dims)))
 
     def crop_boundary(self, width: int) -> "CameraModel":
         """The camera of CropBoundaryPixels (xregProjData.cpp:543-567 ->
         UpdateCameraModelFor2DROI, xregPerspectiveXform.cpp:482-503)."""
         d = L.xr_camera_desc()
         call("xr_camera_crop_boundary", C.byref(self.desc), int(width), C.byref(d))
-        return CameraModel(d)
+        return self._derived(d, ("crop", int(width)))
 
     @property
     def num_det_rows(self) -> int:
@@ -69,9 +76,12 @@ class CameraModel:
         return np.array(self.desc.extrins[:], dtype=np.float64).reshape(4, 4)
 
     def set_extrins(self, extrins: np.ndarray) -> None:
-        e = np.asarray(extrins, dtype=np.float64).reshape(16)
+        """The world -> camera transform; CameraModel holds it in float."""
+        e = np.asarray(extrins, dtype=np.float64).reshape(16).astype(np.float32)
         for i in range(16):
             self.desc.extrins[i] = float(e[i])
+        if self.recipe is not None:
+            self.recipe = self.recipe + (("extrins", tuple(float(v) for v in e)),)
 
     def as_tuple(self):
         d = self.desc

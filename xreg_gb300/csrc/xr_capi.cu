@@ -302,18 +302,21 @@ extern "C" XR_API xr_status xr_camera_setup_naive(double f, int64_t nr, int64_t 
   XR_CHECK_ARG(nr > 0 && nc > 0, "xr_camera_setup_naive: rows and cols must be positive");
   XR_CHECK_ARG(rs > 1.0e-8 && cs > 1.0e-8, "xr_camera_setup_naive: spacings must be > 1e-8");
   XR_CHECK_ARG(frame >= 0 && frame <= 2, "xr_camera_setup_naive: bad coord_frame_type");
+  // xReg's CameraModel holds float members (CoordScalar): the arguments are
+  // floats there, and MakeNaiveIntrins divides in float.
+  const float ff = (float)f, frs = (float)rs, fcs = (float)cs;
   std::memset(out, 0, sizeof(*out));
   out->coord_frame_type = frame;
-  out->focal_len = f;
+  out->focal_len = ff;
   out->num_det_rows = nr;
   out->num_det_cols = nc;
-  out->det_row_spacing = rs;
-  out->det_col_spacing = cs;
-  double K[9] = {f / cs, 0, 0, 0, f / rs, 0, 0, 0, 1};
+  out->det_row_spacing = frs;
+  out->det_col_spacing = fcs;
+  float K[9] = {ff / fcs, 0, 0, 0, ff / frs, 0, 0, 0, 1};
   if (frame == XR_CAM_FOCAL_NEG_Z) { K[0] = -K[0]; K[4] = -K[4]; }
-  K[2] = (double)(nc - 1) * 0.5;
-  K[5] = (double)(nr - 1) * 0.5;
-  std::memcpy(out->intrins, K, sizeof(K));
+  K[2] = (float)((double)(nc - 1) * 0.5);
+  K[5] = (float)((double)(nr - 1) * 0.5);
+  for (int i = 0; i < 9; ++i) out->intrins[i] = K[i];
   for (int i = 0; i < 16; ++i) out->extrins[i] = (i % 5 == 0) ? 1.0 : 0.0;
   return XR_OK;
 }
@@ -322,18 +325,26 @@ extern "C" XR_API xr_status xr_camera_downsample(const xr_camera_desc* src, doub
                                                  xr_camera_desc* dst) {
   XR_CHECK_ARG(src && dst, "xr_camera_downsample: NULL argument");
   XR_CHECK_ARG(ds > 0.0, "xr_camera_downsample: factor must be positive");
+  // float arithmetic throughout, as CameraModel holds its members
+  const float fds = (float)ds;
   xr_camera_desc d = *src;
-  d.intrins[0] *= ds; d.intrins[4] *= ds; d.intrins[2] *= ds; d.intrins[5] *= ds;
-  long nr = std::lround((double)src->num_det_rows * ds);
-  long nc = std::lround((double)src->num_det_cols * ds);
+  float K[9];
+  for (int i = 0; i < 9; ++i) K[i] = (float)src->intrins[i];
+  K[0] *= fds; K[4] *= fds; K[2] *= fds; K[5] *= fds;
+  // lround(num_det_rows * ds_factor): the count converts to float first
+  long nr = std::lround((float)src->num_det_rows * fds);
+  long nc = std::lround((float)src->num_det_cols * fds);
   if (force_even) { if (nr % 2) --nr; if (nc % 2) --nc; }
   XR_CHECK_ARG(nr > 0 && nc > 0, "xr_camera_downsample: result has no pixels");
+  for (int i = 0; i < 9; ++i) d.intrins[i] = K[i];
+  for (int i = 0; i < 16; ++i) d.extrins[i] = (float)src->extrins[i];
   d.num_det_rows = nr;
   d.num_det_cols = nc;
-  d.det_row_spacing = src->det_row_spacing / ds;
-  d.det_col_spacing = src->det_col_spacing / ds;
-  const double xps = d.det_col_spacing, yps = d.det_row_spacing;
-  d.focal_len = (std::fabs(d.intrins[0] * xps) + std::fabs(d.intrins[4] * ((yps < 0) ? xps : yps))) / 2.0;
+  const float rs = (float)src->det_row_spacing / fds, cs = (float)src->det_col_spacing / fds;
+  d.det_row_spacing = rs;
+  d.det_col_spacing = cs;
+  // FocalLenFromIntrins (xregPerspectiveXform.cpp:186-190)
+  d.focal_len = (std::fabs(K[0] * cs) + std::fabs(K[4] * ((rs < 0) ? cs : rs))) / 2.0f;
   *dst = d;
   return XR_OK;
 }
@@ -638,15 +649,25 @@ extern "C" XR_API xr_status xr_rc_distribute_xforms_among_cam_models(xr_raycaste
 }
 
 namespace {
-void mat4_mul(const double* a, const double* b, double* out) {
-  double t[16];
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) {
-      double s = 0.0;
-      for (int k = 0; k < 4; ++k) s += a[i * 4 + k] * b[k * 4 + j];
-      t[i * 4 + j] = s;
+// FrameTransform * FrameTransform in float, Eigen's order (xf::compose); the
+// result is stored back as double.
+void frame_mul_f32(const double* a, const double* b, double* out) {
+  xf::Affine fa, fb, r;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) {
+      fa.L[i * 3 + j] = (float)a[i * 4 + j];
+      fb.L[i * 3 + j] = (float)b[i * 4 + j];
     }
-  std::memcpy(out, t, sizeof(t));
+    fa.t[i] = (float)a[i * 4 + 3];
+    fb.t[i] = (float)b[i * 4 + 3];
+  }
+  xf::compose(fa, fb, r);
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) out[i * 4 + j] = r.L[i * 3 + j];
+    out[i * 4 + 3] = r.t[i];
+    out[12 + i] = 0.0;
+  }
+  out[15] = 1.0;
 }
 }  // namespace
 
@@ -665,7 +686,8 @@ static xr_status rc_host_xforms(xr_raycaster rc, const char* fn) {
 }
 
 // RayCaster::pre_multiply_all_xforms / post_multiply_all_xforms
-// (xregRayCastInterface.cpp:235-261), in double.
+// (xregRayCastInterface.cpp:235-261): FrameTransform products, in float as xReg
+// computes them.
 static xr_status rc_multiply_all(xr_raycaster rc, const double* m, bool pre, const char* fn) {
   XR_CHECK_ARG(rc && m, std::string(fn) + ": NULL argument");
   XR_CHECK_ARG(finite_all(m, 16), std::string(fn) + ": non-finite transform");
@@ -673,8 +695,8 @@ static xr_status rc_multiply_all(xr_raycaster rc, const double* m, bool pre, con
   if (st != XR_OK) return st;
   for (int64_t k = 0; k < rc->pose_count; ++k) {
     double* x = rc->xforms.data() + 16 * k;
-    if (pre) mat4_mul(m, x, x);
-    else mat4_mul(x, m, x);
+    if (pre) frame_mul_f32(m, x, x);
+    else frame_mul_f32(x, m, x);
   }
   rc->xforms_dirty = true;
   return XR_OK;

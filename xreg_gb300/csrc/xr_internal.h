@@ -9,24 +9,15 @@
 #include <string>
 
 #include "xreg_gb300.h"
+#include "xr_xfloat.h"
 
 namespace xr {
 
-// Per-projection ray set-up in volume index coordinates (96 bytes).  Produced by
-// the FP64 geometry kernel, consumed by every ray-marching kernel.
-//   ray direction for pixel (c, r):   d0 + c*dc + r*dr   (pinhole -> pixel)
-//   same vector in camera-world mm:   e0 + c*ec + r*er   (gives the step count)
-struct ProjGeom {
-  float src[3];
-  float d0[3];
-  float dc[3];
-  float dr[3];
-  float e0[3];
-  float ec[3];
-  float er[3];
-  float pad[3];
-};
-static_assert(sizeof(ProjGeom) == 96, "ProjGeom layout");
+// Per-projection ray set-up (176 bytes): the camera's inverses and pinhole and
+// the camera -> index transform, all in float as xReg holds them; every
+// ray-marching kernel finishes the set-up per ray with xf::ray_setup.
+using ProjGeom = xf::RayFrame;
+static_assert(sizeof(ProjGeom) == 176, "ProjGeom layout");
 
 // Volume as the kernels see it.
 struct VolView {
@@ -71,8 +62,10 @@ struct DrrParams {
 };
 
 // ---- launchers (xr_geom.cu) ----
-// One thread per projection: FP64 composition phys_to_idx * pose, camera
-// inverses, rounded to float ProjGeom.
+// ITK physical -> index transform of a volume in xReg's float arithmetic.
+xf::Affine phys_to_idx_xform(const xr_volume_desc& vol);
+// One thread per projection: camera inverses and the camera -> index transform
+// phys_to_idx * pose in xReg's float order (xf::ray_frame).
 cudaError_t launch_proj_geom(const xr_volume_desc& vol, const xr_camera_desc* d_cams,
                              const double* d_poses, const int32_t* d_cam_idx, int64_t num_projs,
                              int64_t pose_stride_projs, ProjGeom* d_out, cudaStream_t s);

@@ -281,9 +281,20 @@ extern "C" XR_API xr_status xr_camera_crop_boundary(const xr_camera_desc* src, i
   if (!src || !out) return fail(XR_ERR_INVALID_ARG, "xr_camera_crop_boundary: NULL argument");
   if (width < 0 || src->num_det_rows - 2 * width < 2 || src->num_det_cols - 2 * width < 2)
     return fail(XR_ERR_INVALID_ARG, "xr_camera_crop_boundary: the crop leaves fewer than 2 rows or columns");
+  // UpdateCameraModelFor2DROI in float: the principal point moves by the crop,
+  // and CameraModel::setup(K, E, ...) derives the focal length again from K
+  // (FocalLenFromIntrins, xregPerspectiveXform.cpp:186-190)
   xr_camera_desc d = *src;
-  d.intrins[2] -= (double)width;
-  d.intrins[5] -= (double)width;
+  float K[9];
+  for (int i = 0; i < 9; ++i) K[i] = (float)src->intrins[i];
+  K[2] -= (float)width;
+  K[5] -= (float)width;
+  for (int i = 0; i < 9; ++i) d.intrins[i] = K[i];
+  for (int i = 0; i < 16; ++i) d.extrins[i] = (float)src->extrins[i];
+  const float rs = (float)src->det_row_spacing, cs = (float)src->det_col_spacing;
+  d.det_row_spacing = rs;
+  d.det_col_spacing = cs;
+  d.focal_len = (std::fabs(K[0] * cs) + std::fabs(K[4] * ((rs < 0) ? cs : rs))) / 2.0f;
   d.num_det_rows = src->num_det_rows - 2 * width;
   d.num_det_cols = src->num_det_cols - 2 * width;
   *out = d;

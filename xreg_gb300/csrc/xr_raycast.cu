@@ -13,10 +13,11 @@
 //   * ray sum (or max) times the step in mm (:279); replace / accumulate /
 //     background images as in RayCasterCPU::pre_compute (xregRayCastBaseCPU.cpp:128-158).
 //
-// The per-ray geometry (direction, slab test, nudge, step count, start point,
-// step vector) uses explicitly rounded float intrinsics in the same order as the
-// CPU oracle, so sample counts and sample positions are bit-identical.  The
-// interpolation and the sum use ordinary float arithmetic.
+// The per-ray geometry (detector point, slab test, nudge, step count, start
+// point, step vector) is xReg's own float arithmetic in Eigen's evaluation order
+// (xf::ray_setup, xr_xfloat.h), so sample counts and sample positions are the
+// reference's, bit for bit.  The interpolation and the sum use ordinary float
+// arithmetic.
 //
 // Volume layouts (same values, same arithmetic, bit-identical results):
 //   LINEAR  voxels x-fastest; a sample issues 8 scalar loads.
@@ -352,48 +353,17 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
   float sum = (KERNEL == XR_LINE_INT_MAX) ? -FLT_MAX : 0.0f;
   unsigned long long ns = 0;
   {
-    const ProjGeom& g = p.geo[proj];
-    const float fc = (float)col, fr = (float)row;
-    float dir[3], v[3], src[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      src[k] = g.src[k];
-      dir[k] = __fadd_rn(__fadd_rn(g.d0[k], __fmul_rn(fc, g.dc[k])), __fmul_rn(fr, g.dr[k]));
-      v[k] = __fadd_rn(__fadd_rn(g.e0[k], __fmul_rn(fc, g.ec[k])), __fmul_rn(fr, g.er[k]));
-    }
+    // xReg's per-ray float set-up (xf::ray_setup): clipped, nudged segment,
+    // start point, step vector and the step-count quotient
     const float maxb[3] = {(float)(p.vol.nx - 1), (float)(p.vol.ny - 1), (float)(p.vol.nz - 1)};
-    bool hit = true;
-    float t0 = 0.0f, t1 = 1.0f;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      if (!hit) break;
-      // |v| > 1e-8 compared in double by the reference; 1.0e-8f is the largest
-      // float not above 1e-8, so the float comparison decides the same
-      if (fabsf(dir[k]) > 1.0e-8f) {
-        const float inv = __frcp_rn(dir[k]);
-        float ta = __fmul_rn(__fsub_rn(0.0f, src[k]), inv);
-        float tb = __fmul_rn(__fsub_rn(maxb[k], src[k]), inv);
-        if (tb < ta) { const float tmp = ta; ta = tb; tb = tmp; }
-        t0 = (t0 < ta) ? ta : t0;
-        t1 = (tb < t1) ? tb : t1;
-        if (t0 > t1) hit = false;
-      } else if (src[k] < 0.0f || src[k] > maxb[k]) {
-        hit = false;
-      }
-    }
-    if (hit && (__fsub_rn(t1, t0) > 2.0e-3f)) {
-      t0 = __fadd_rn(t0, 1.0e-3f);
-      t1 = __fsub_rn(t1, 1.0e-3f);
-      float px = __fadd_rn(src[0], __fmul_rn(t0, dir[0]));
-      float py = __fadd_rn(src[1], __fmul_rn(t0, dir[1]));
-      float pz = __fadd_rn(src[2], __fmul_rn(t0, dir[2]));
-      const float lc = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(v[0], v[0]), __fmul_rn(v[1], v[1])),
-                                            __fmul_rn(v[2], v[2])));
-      const float len = __fmul_rn(__fsub_rn(t1, t0), lc);
-      // floor(len / step) through a saturating 32-bit conversion (a 64-bit one
-      // runs on the slow FP64 pipe): above 2^32 - 1 it saturates and NaN gives
-      // 0, so the max_steps test (max_steps < 2^31) decides as with 64 bits
-      unsigned long long nsteps = __float2uint_rz(__fdiv_rn(len, p.step));
+    float st0[3], stv[3], quot;
+    bool hit = xf::ray_setup(p.geo[proj], (float)col, (float)row, maxb, p.step, st0, stv, quot);
+    if (hit) {
+      float px = st0[0], py = st0[1], pz = st0[2];
+      // num_steps = size_t(quotient) through a saturating 32-bit conversion (a
+      // 64-bit one runs on the slow FP64 pipe): above 2^32 - 1 it saturates and
+      // NaN gives 0, so the max_steps test (max_steps < 2^31) decides as with 64 bits
+      unsigned long long nsteps = __float2uint_rz(quot);
       if (!(nsteps <= p.max_steps)) {
         // A ray longer than the volume diagonal allows can only come from a
         // non-finite or degenerate pose: count it and leave the pixel unsampled
@@ -402,8 +372,7 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
         nsteps = 0;
         hit = false;
       }
-      const float sc = __fdiv_rn(p.step, lc);
-      const float sx = __fmul_rn(dir[0], sc), sy = __fmul_rn(dir[1], sc), sz = __fmul_rn(dir[2], sc);
+      const float sx = stv[0], sy = stv[1], sz = stv[2];
       // reciprocal steps for the skipping bounds (never for sample positions)
       const float inv_st[3] = {1.0f / sx, 1.0f / sy, 1.0f / sz};
       const void* data = (LAYOUT != XR_LAYOUT_LINEAR) ? p.vol.cells : p.vol.voxels;
