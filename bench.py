@@ -12,12 +12,19 @@ for this path).
             256 MB buffer outside the timed events.
   e2e       poses/s through the public C ABI (xr_obj_eval) from pinned host
             poses to host similarity values, copies inside the timed region.
-  roofline  DRR kernel: algorithmic bytes 8 * bytes_per_voxel * samples per
-            launch over its CUDA-event duration, against MEASURED_PEAKS.json.
+  roofline  DRR kernel (the dominant launch): bytes of the voxel cells it
+            loads per launch over its CUDA-event duration, against the L2 read
+            bandwidth measured in the same run; beside it the cost model's
+            algorithmic bytes (8 neighbour reads x voxel bytes x every sample)
+            against the measured HBM peak, ncu DRAM traffic, and the same
+            figures with every sample loaded (skipping off, CT-like air).
   cpu_baseline  the CPU oracle (a restatement of xReg's TBB CPU path) on a
             bounded sample of the same workload, all host cores.
+  errors_vs_oracle  DRR and grad-NCC errors of the float32 / FP16 / BF16 paths
+            against the oracle's FP32 restatement and its FP64 twin.
 
---impl reference times that CPU path alone as the reference arm.
+--impl reference times that CPU path alone as the reference arm, one full
+population per step, with nothing of the product loaded.
 Multi-GPU: replicas only (each rank evaluates its own populations; no collective).
 """
 from __future__ import annotations
@@ -189,6 +196,105 @@ def _ncu_traffic(workload_tag: str, what: str = "traffic_bytes_per_launch"):
     return None
 
 
+def _drr_kernel_stats(rc, d_pose_ptr: int, reps: int, stream, flush):
+    """The DRR launch alone for one device-resident population: mean CUDA-event
+    duration over reps launches (L2 flushed before each, outside the events),
+    the samples of the reference step rule and the samples loaded."""
+    import torch
+    rc.set_count_samples(True)
+    rc.distribute_xforms_device(POP, d_pose_ptr)
+    rc.compute()
+    samples, loaded = rc.last_num_samples(), rc.last_num_loaded_samples()
+    rc.set_count_samples(False)
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    with torch.cuda.stream(stream):
+        for i in range(reps):
+            flush.fill_(float(i))
+            kev[i][0].record(stream)
+            rc.compute()
+            kev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return float(np.mean([s.elapsed_time(e) for s, e in kev])), samples, loaded
+
+
+def _roofline(vt: int, layout: int, drr_ms: float, samples: int, loaded: int, l2_peak: float, tag: str) -> dict:
+    """Gather roofline of the DRR kernel.  achieved = bytes of the voxel cells it
+    loads (one CELL8 cell per loaded sample: 32 B float32, 16 B half; 8 corner
+    reads for the linear layout) over its CUDA-event time; peak = the L2 read
+    bandwidth measured in this run.  Beside it: the cost model's algorithmic
+    bytes (8 neighbour reads x voxel bytes x every sample of the reference step
+    rule) against the measured HBM copy peak, and the ncu DRAM traffic."""
+    per_sample = (32 if vt == 0 else 16) if layout != 0 else 8 * (4 if vt == 0 else 2)
+    t = drr_ms / 1e3
+    gather = per_sample * loaded
+    achieved = gather / t / 1e9
+    hbm, hbm_kind = _peaks()
+    alg = 8.0 * (4 if vt == 0 else 2) * samples
+    traffic = _ncu_traffic(tag)
+    out = {"bound": "l2", "achieved": round(achieved, 1), "peak": round(l2_peak, 1), "unit": "GB/s",
+           "frac": round(achieved / l2_peak, 4), "traffic": traffic,
+           "peak_source": "measured in this run: xr_measure_l2_read_bandwidth (48 MB made L2-resident, read 40 "
+                          "times with 16-byte L2 loads from every SM, CUDA events)",
+           "achieved_bytes": f"{per_sample} B of voxel cell per loaded sample x {loaded} loaded samples",
+           "samples_per_launch": samples, "loaded_samples_per_launch": loaded,
+           "loaded_frac": round(loaded / max(samples, 1), 4), "kernel_ms": round(drr_ms, 4),
+           "warp_instructions_per_loaded_sample": _ncu_traffic(tag, "warp_instructions_per_loaded_sample"),
+           "cost_model": {"achieved": round(alg / t / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                          "frac": round(alg / t / 1e9 / hbm, 4),
+                          "peak_source": f"{hbm_kind} hbm_gbs (MEASURED_PEAKS.json)",
+                          "bytes_per_launch": alg,
+                          "note": "8 neighbour reads x voxel bytes x every sample, loaded or skipped; above 1 "
+                                  "because the reads hit L1/L2 and proven-zero samples are not loaded"}}
+    if traffic:
+        out["hbm_traffic_frac"] = round(traffic / t / 1e9 / hbm, 4)
+    return out
+
+
+def _errors_vs_oracle(xr, w, fixed, dev, poses):
+    """DRR and grad-NCC errors of the float32 / FP16 / BF16 volume paths on two
+    poses of a timed population, against the oracle's FP32 restatement of
+    xReg's ray caster and its FP64 twin, and the similarity values against the
+    oracle's double arithmetic (on the oracle's FP32 DRRs and on the GPU's own)."""
+    from oracle import oracle as O
+    from tests.helpers import oracle_cams, oracle_geom
+    O.set_threads(os.cpu_count() or 1)
+    geom, cams = oracle_geom(w.vol), oracle_cams(w.cams)
+    r32, ns = O.drr_f32(w.vol.voxels, geom, cams, poses, step=w.step, count=True)
+    r64 = O.drr_f64(w.vol.voxels, geom, cams, poses, step=w.step)
+    s32 = O.grad_ncc(fixed, r32)
+    s64 = O.grad_ncc(fixed, r64.astype(np.float32))
+    body = r64 > 0.1 * r64.max()
+    out = {"poses": len(poses), "samples": int(ns.sum()),
+           "fp32_oracle_itself": {"drr_max_rel_vs_fp64_body": float(np.max(np.abs(r32[body] - r64[body]) / r64[body]))}}
+    tol = {0: 1e-4, 1: 2e-3, 2: 2e-3}
+    for name, vt in (("f32", 0), ("f16", 1), ("bf16", 2)):
+        rc = xr.RayCasterLineIntCUDA(dev)
+        rc.set_volume(w.vol, vt)
+        rc.set_camera_models(w.cams)
+        rc.set_ray_step_size(w.step)
+        m = xr.ImgSimMetric2DGradNCCCUDA(dev)
+        m.set_fixed_image(fixed)
+        obj = xr.PopulationObjective(rc, [m], len(poses))
+        sims = obj.eval(poses)
+        g = rc.projs()
+        nz = r32 != 0
+        rel32 = float(np.max(np.abs(g[nz] - r32[nz]) / r32[nz]))
+        r64b = np.abs(g[body] - r64[body]) / r64[body]
+        e = {"drr_max_rel_vs_fp32_oracle": rel32, "background_equal": bool(np.all(g[~nz] == 0)),
+             "drr_max_rel_vs_fp64_oracle_body": float(r64b.max()),
+             "drr_median_rel_vs_fp64_oracle_body": float(np.median(r64b)),
+             "grad_ncc_max_abs_vs_oracle_fp32_drrs": float(np.max(np.abs(sims - s32))),
+             "grad_ncc_max_abs_vs_oracle_fp64_drrs": float(np.max(np.abs(sims - s64))),
+             "grad_ncc_max_abs_vs_oracle_on_same_drrs": float(np.max(np.abs(sims - O.grad_ncc(fixed, g)))),
+             "drr_tolerance": tol[vt], "within_drr_tolerance": rel32 <= tol[vt]}
+        if vt == 2:
+            e["note"] = "BF16 volume: an 8-bit significand rounds a voxel by up to 2^-8; outside the 2e-3 " \
+                        "half-precision tolerance (held to 2^-8 in the tests)"
+        out[name] = e
+        obj.close()
+    return out
+
+
 # ------------------------------------------------------------- CPU baseline
 def cpu_baseline(w, fixed, budget_s: float):
     """The oracle's FP32 DRR + grad-NCC on all host cores, on as many poses of the
@@ -305,46 +411,24 @@ def run_ours(a, rank, world, local):
     e2e = world * a.steps * POP / e2e_t
     np.testing.assert_array_equal(hs, d_sims[a.warmup:].cpu().numpy())  # same values both ways
 
-    # ---- DRR kernel alone: duration and exact sample count (roofline)
-    rc.set_count_samples(True)
-    rc.distribute_xforms_device(POP, d_pops[a.warmup].data_ptr())
-    rc.compute()
-    samples = rc.last_num_samples()
+    # ---- DRR kernel alone: duration and sample counts (roofline)
+    drr_ms, samples, loaded = _drr_kernel_stats(rc, d_pops[a.warmup].data_ptr(), a.steps, stream, flush)
     layout, bw, unroll, wrows = rc.launch_config_ex()
     lname = {0: "linear", 1: "cell8", 2: "cell8-256bit"}.get(layout, str(layout))
     wcols = 32 // wrows
     wshape = "" if wrows == 4 else f"-warp{wcols}x{wrows}"
     block = f"{wcols * bw}x{(8 // bw) * wrows}"
-    rc.set_count_samples(False)
-    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
-    with torch.cuda.stream(stream):
-        for i in range(a.steps):
-            flush.fill_(float(i))
-            rc.distribute_xforms_device(POP, d_pops[a.warmup + i].data_ptr())
-            kev[i][0].record(stream)
-            rc.compute()
-            kev[i][1].record(stream)
-    torch.cuda.synchronize()
-    drr_ms = float(np.mean([s.elapsed_time(e) for s, e in kev]))
-    bvox = 4 if vt == 0 else 2
-    alg_bytes = 8.0 * bvox * samples
-    achieved = alg_bytes / (drr_ms / 1e3) / 1e9
-    peak, peak_kind = _peaks()
     tag = f"batched-256^3-384^2-pop100-{a.voxel}-{lname}-loop{unroll}{wshape}"
-    traffic = _ncu_traffic(tag)
-    l2_bytes = _ncu_traffic(tag, "l2_bytes_per_launch")
-    l2_peak = _ncu_traffic("", "l2_sector_peak_gbs")
-    l2 = None
-    if l2_peak:
-        l2 = {"peak": l2_peak, "unit": "GB/s",
-              "peak_source": "ncu: lts__t_sectors per second / its pct_of_peak_sustained_elapsed (profiles/)",
-              "algorithmic_frac": round(achieved / l2_peak, 4),
-              "traffic": l2_bytes,
-              "traffic_frac": None if l2_bytes is None else round(l2_bytes / (drr_ms / 1e3) / 1e9 / l2_peak, 4)}
+    l2_peak = xr.measure_l2_read_bandwidth(dev)
+    roofline = _roofline(vt, layout, drr_ms, samples, loaded, l2_peak, tag)
+    roofline["kernel"] = f"drr_kernel<{a.voxel},sum,{lname},unroll{unroll}> block {block}, warps {wcols}x{wrows}"
 
     extras = {}
     if not a.no_extras and rank == 0:
-        extras = _extras(xr, w, fixed, dev, stream, pops[a.warmup], d_sims, a)
+        extras = _extras(xr, w, fixed, dev, stream, pops[a.warmup], d_sims, a, flush, l2_peak)
+        for key in ("batched_f32_skipping_off", "batched_f32_noisy_air"):
+            if isinstance(extras.get(key), dict) and "drr_kernel" in extras[key]:
+                roofline["dense" if key.endswith("off") else "noisy_air"] = extras[key]["drr_kernel"]
 
     res = {
         "metric": "poses/sec (DRR+grad-NCC pose evaluations, batched population)",
@@ -364,19 +448,7 @@ def run_ours(a, rank, world, local):
         "e2e": {"value": round(e2e, 2), "unit": "poses/s", "h2d_bytes_per_step": POP * 16 * 8,
                 "d2h_bytes_per_step": POP * 4},
         "gpu_launches": a.steps * 5,
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4),
-                     "traffic": None if traffic is None else traffic,
-                     "kernel": f"drr_kernel<{a.voxel},sum,{lname},unroll{unroll}> block {block}, warps {wcols}x{wrows}",
-                     "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
-                     else "fallback 6.8 TB/s",
-                     "alg_bytes_per_launch": alg_bytes, "samples_per_launch": samples,
-                     "kernel_ms": round(drr_ms, 4),
-                     "l2": l2,
-                     "note": "algorithmic bytes = 8 neighbour reads x voxel bytes x every sample of the "
-                             "reference step rule; frac > 1 because those reads hit L1/L2 (HBM carries "
-                             "`traffic`, under 1 % of them) and samples proven zero are not loaded; the kernel "
-                             "is instruction-issue bound (see profiles/)"},
+        "roofline": roofline,
         "clocks": clk.summary(t_clk0, t_clk1 + 0.06),
     }
     if rank == 0:
@@ -449,11 +521,16 @@ def _plain_small(xr, dev, cpu_budget_s: float):
             "max_abs_ncc_diff_vs_oracle": diff}
 
 
-def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
+def _extras(xr, w, fixed, dev, stream, poses, d_sims, a, flush, l2_peak):
     """Plain single-pose path (one DRR + one metric launch per pose, host sync per
-    pose as xReg's OpenCL path does) and half-precision volumes, for context."""
+    pose as xReg's OpenCL path does), half-precision volumes, dense sampling,
+    errors against the oracle, and the other workloads, for context."""
     import torch
     out = {}
+    try:
+        out["errors_vs_oracle"] = _errors_vs_oracle(xr, w, fixed, dev, poses[:2])
+    except Exception as e:  # reported, never fatal to the headline line
+        out["errors_vs_oracle"] = {"error": f"{type(e).__name__}: {e}"}
     rc = xr.RayCasterLineIntCUDA(dev)
     rc.set_volume(w.vol)
     rc.set_camera_model(w.cams[0])
@@ -526,6 +603,16 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a):
                         np.max(np.abs(ds.cpu().numpy() - d_sims[a.warmup].cpu().numpy())))}
         if key.endswith("noisy_air"):
             out[key]["air_voxels_nonzero_frac"] = round(float(np.mean(v_air[air] > 0)), 3)
+        if vt == 2:
+            out[key]["tolerance"] = "BF16 volume: DRRs held to 2^-8 of the float32 oracle, outside the 2e-3 " \
+                                    "half-precision tolerance"
+        if key in ("batched_f32_skipping_off", "batched_f32_noisy_air"):
+            ms_k, smp, ld = _drr_kernel_stats(rch, dp.data_ptr(), 5, stream, flush)
+            lay = rch.launch_config_ex()
+            rf = _roofline(vt, lay[0], ms_k, smp, ld, l2_peak, "")
+            out[key]["drr_kernel"] = {k: rf[k] for k in ("achieved", "peak", "unit", "frac", "kernel_ms",
+                                                         "samples_per_launch", "loaded_samples_per_launch",
+                                                         "loaded_frac")}
         objh.close()
     del v_air, noisy_air
     for key, fn in (("plain_small_config", lambda: _plain_small(xr, dev, min(3.0, a.cpu_seconds))),
@@ -565,6 +652,14 @@ def _precision(xr, dev, stream, pop: int = 20, reps: int = 5):
     out = {"volume": "512x512x400 @0.8x0.8x1 mm", "detector": "768x768", "metric": "patch grad-NCC 11x11 stride 1",
            "pop": pop}
     ref_drr = ref_sims = None
+    from oracle import oracle as O
+    from tests.helpers import oracle_cams, oracle_geom
+    O.set_threads(os.cpu_count() or 1)
+    o_geom, o_cams = oracle_geom(w.vol), oracle_cams(w.cams)
+    o32 = O.drr_f32(w.vol.voxels, o_geom, o_cams, poses[:1], step=w.step)[0]
+    o64 = O.drr_f64(w.vol.voxels, o_geom, o_cams, poses[:1], step=w.step)[0]
+    o_body = o64 > 0.1 * o64.max()
+    o_sim = float(O.patch_grad_ncc(fixed, o32[None], smooth_ksize=5, radius=5, stride=1)[0])
     for vname, vt in (("f32", 0), ("f16", 1), ("bf16", 2)):
         rcv = xr.RayCasterLineIntCUDA(dev)
         rcv.set_stream(stream.cuda_stream)
@@ -590,6 +685,12 @@ def _precision(xr, dev, stream, pop: int = 20, reps: int = 5):
         torch.cuda.synchronize()
         t = float(np.mean([s0.elapsed_time(e0) for s0, e0 in evs])) / 1e3
         entry = {"poses_per_s": round(pop / t, 2)}
+        nz = o32 != 0
+        entry["errors_vs_oracle_pose0"] = {
+            "drr_max_rel_vs_fp32_oracle": float(np.max(np.abs(drr[nz] - o32[nz]) / o32[nz])),
+            "drr_max_rel_vs_fp64_oracle_body": float(np.max(np.abs(drr[o_body] - o64[o_body]) / o64[o_body])),
+            "drr_median_rel_vs_fp64_oracle_body": float(np.median(np.abs(drr[o_body] - o64[o_body]) / o64[o_body])),
+            "patch_grad_ncc_abs_vs_oracle_fp32_drr": abs(float(sims[0]) - o_sim)}
         if ref_drr is None:
             ref_drr, ref_sims = drr, sims
         else:
@@ -640,7 +741,29 @@ def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
         alone = [o.eval(p[k]) for o, p in zip(objs, poses_sets)]
     t_alone = time.perf_counter() - t0
     same = all(np.array_equal(x, y) for x, y in zip(mixed, alone))
+    # one pose of the largest job against the oracle (its DRRs from the last job-set call)
+    errs = None
+    try:
+        from oracle import oracle as O
+        from tests.helpers import oracle_cams, oracle_geom
+        big = int(np.argmax([np.prod(sp.size) * len(sp.view_angles) for sp in specs]))
+        sp, ob = specs[big], objs[big]
+        jvol = synth.phantom_volume(sp.size, sp.spacing, sp.seed)
+        jcams = synth.view_cameras(sp.view_angles, sp.ds_first)
+        nv = len(jcams)
+        p0 = poses_sets[big][steps][0]
+        ref = O.drr_f32(jvol.voxels, oracle_geom(jvol), oracle_cams(jcams), np.stack([p0] * nv),
+                        cam_idx=list(range(nv)), step=0.5)
+        g = ob.rc.projs()
+        got = np.stack([g[v * sp.pop] for v in range(nv)])
+        nz = ref != 0
+        errs = {"job": f"{sp.size[0]}x{sp.size[1]}x{sp.size[2]} v{nv} ds{int(round(1 / sp.ds_first))} FP16 volume",
+                "drr_max_rel_vs_fp32_oracle": float(np.max(np.abs(got[nz] - ref[nz]) / ref[nz])),
+                "background_equal": bool(np.all(got[~nz] == 0)), "drr_tolerance": 2e-3}
+    except Exception as e:
+        errs = {"error": f"{type(e).__name__}: {e}"}
     return {"value": round(steps * total / t_mixed, 2), "unit": "poses/s",
+            "errors_vs_oracle_largest_job_pose0": errs,
             "one_job_at_a_time": round(steps * total / t_alone, 2),
             "ms_per_step": round(1e3 * t_mixed / steps, 3), "jobs": njobs, "poses_per_step": total,
             "identical_to_alone": bool(same),

@@ -199,6 +199,10 @@ XR_API xr_status xr_rc_use_external_host_pixel_buf(xr_raycaster rc, float* host_
 /* Exact number of trilinear samples the last compute took (algorithmic-bytes
  * accounting); synchronises. */
 XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* out);
+/* How many of those samples the kernel loaded: the rest lie in cells whose
+ * eight corners are zero and were skipped (they add exactly +0); synchronises.
+ * No counterpart in xReg (it loads every sample). */
+XR_API xr_status xr_rc_last_num_loaded_samples(xr_raycaster rc, uint64_t* out);
 /* Enables (1) or disables (0) per-compute sample counting (default off). */
 XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
 /* Launch configuration of the DRR kernel: volume layout (XR_LAYOUT_*), warps
@@ -389,6 +393,13 @@ XR_API xr_status xr_obj_eval_device(xr_objective obj, int64_t pop, const double*
  * No counterpart in the reference (xReg's metrics always allocate their buffers). */
 XR_API xr_status xr_grad_ncc_noalloc(const float* d_fixed, const float* d_moving, int64_t rows, int64_t cols,
                                      int64_t num_moving, int32_t smooth_ksize, float* d_sims, void* cuda_stream);
+
+/* ---------------------------------------------------------- diagnostics -- */
+/* Measured L2 read bandwidth of a device (device < 0: the current one), in
+ * GB/s: a buffer of `bytes` (at most half the L2) made resident, then read
+ * `reps` times with 16-byte L2-cached loads from every SM.  It is the
+ * denominator of the DRR kernel's gather roofline.  No counterpart in xReg. */
+XR_API xr_status xr_measure_l2_read_bandwidth(int32_t device, int64_t bytes, int32_t reps, double* gbs);
 
 #ifdef __cplusplus
 }

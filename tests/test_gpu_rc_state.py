@@ -22,7 +22,7 @@ def _rc(xr, vols, cams, n):
     return rc
 
 
-def test_pre_post_multiply_and_getters(xr):
+def test_pre_post_multiply_and_getters(xr, oracle):
     vol = small_volume(41, (40, 36, 32), (1.5, 1.5, 1.5))
     cams = [small_camera((24, 28), 3.0), small_camera((24, 28), 2.5)]
     gt = synth.gt_pose(vol)
@@ -37,7 +37,10 @@ def test_pre_post_multiply_and_getters(xr):
     rc.pre_multiply_all_xforms(pre)
     rc.post_multiply_all_xforms(post)
     x = rc.xforms_cam_to_itk_phys()
-    np.testing.assert_allclose(x, np.concatenate([pre @ poses @ post] * 2), rtol=0, atol=1e-9)
+    # FrameTransform products in float, as xReg computes them (pre * pose, then * post)
+    want = np.stack([oracle.frame_mul_f32(oracle.frame_mul_f32(pre, p), post) for p in poses])
+    np.testing.assert_array_equal(x, np.concatenate([want] * 2))
+    np.testing.assert_allclose(x, np.concatenate([pre @ poses @ post] * 2), rtol=0, atol=1e-4)
     rc.compute()
     mine = rc.projs()
     # the same poses given directly: identical images

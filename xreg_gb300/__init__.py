@@ -23,6 +23,7 @@ from .api import (  # noqa: F401
     downsample_size,
     hu_to_lin_att_device,
     log_remap,
+    measure_l2_read_bandwidth,
     proj_preproc,
     read_itk_affine_transform,
     read_slicer_affine_transform,

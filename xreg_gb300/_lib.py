@@ -118,6 +118,8 @@ _SIGS = {
     "xr_rc_use_other_proj_buf": [H, H],
     "xr_rc_use_external_host_pixel_buf": [H, P],
     "xr_rc_last_num_samples": [H, C.POINTER(u64)],
+    "xr_rc_last_num_loaded_samples": [H, C.POINTER(u64)],
+    "xr_measure_l2_read_bandwidth": [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_double)],
     "xr_rc_set_count_samples": [H, i32],
     "xr_rc_set_launch_config": [H, i32, i32, i32],
     "xr_rc_get_launch_config": [H, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],

@@ -379,6 +379,13 @@ class RayCasterLineIntCUDA:
         call("xr_rc_last_num_samples", self._h, C.byref(v))
         return int(v.value)
 
+    def last_num_loaded_samples(self) -> int:
+        """Samples the last compute loaded (the others were proven zero and
+        skipped); needs set_count_samples(True)."""
+        v = C.c_uint64()
+        call("xr_rc_last_num_loaded_samples", self._h, C.byref(v))
+        return int(v.value)
+
 
 # -------------------------------------------------------------------- metrics
 class ImgSimMetric2DCUDA:
@@ -822,3 +829,10 @@ def simple_ray_cast(rc: RayCasterLineIntCUDA, cam_world_to_vols, inter_frames=No
     if prev_n > 0 and assocs.size == prev_n:
         rc.set_camera_model_proj_associations(assocs)
     return projs
+
+
+def measure_l2_read_bandwidth(device: int = -1, nbytes: int = 48 << 20, reps: int = 40) -> float:
+    """Measured L2 read bandwidth of a device in GB/s (xr_measure_l2_read_bandwidth)."""
+    v = C.c_double()
+    call("xr_measure_l2_read_bandwidth", int(device), int(nbytes), int(reps), C.byref(v))
+    return float(v.value)

@@ -17,7 +17,7 @@ REPO_DIR = PKG_DIR.parent
 CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_PATH = BUILD_DIR / "libxreg_gb300.so"
-SOURCES = ["xr_capi.cu", "xr_geom.cu", "xr_raycast.cu", "xr_metrics.cu", "xr_noalloc.cu", "xr_preproc.cu",
+SOURCES = ["xr_capi.cu", "xr_geom.cu", "xr_raycast.cu", "xr_metrics.cu", "xr_noalloc.cu", "xr_preproc.cu", "xr_probe.cu",
            "xr_cmaes.cpp", "xr_dfo.cpp", "xr_regi.cpp", "xr_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

@@ -1042,6 +1042,8 @@ static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, Dr
     }
   }
   p.sample_counter = rc->count_samples ? reinterpret_cast<unsigned long long*>(rc->d_counters.p) : nullptr;
+  p.loaded_counter =
+      rc->count_samples ? reinterpret_cast<unsigned long long*>(rc->d_counters.as<char>() + 56) : nullptr;
   p.err_counter = reinterpret_cast<unsigned int*>(rc->d_counters.as<char>() + 8);
   {
     // Longest possible chord: the index-box diagonal scaled to mm by the largest
@@ -1138,7 +1140,10 @@ extern "C" XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t
 extern "C" XR_API xr_status xr_rc_compute(xr_raycaster rc, int32_t vol_idx) {
   XR_CHECK_ARG(rc, "compute: NULL handle");
   DeviceGuard g(rc->device);
-  if (rc->count_samples) XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.p, 0, 8, rc->stream()));
+  if (rc->count_samples) {
+    XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.p, 0, 8, rc->stream()));
+    XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.as<char>() + 56, 0, 8, rc->stream()));
+  }
   return rc_enqueue_compute(rc, vol_idx);
 }
 
@@ -1203,6 +1208,18 @@ extern "C" XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* ou
   DeviceGuard g(rc->device);
   unsigned long long v = 0;
   XR_CUDA_TRY(cudaMemcpy(&v, rc->d_counters.p, 8, cudaMemcpyDeviceToHost));
+  *out = v;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_rc_last_num_loaded_samples(xr_raycaster rc, uint64_t* out) {
+  XR_CHECK_ARG(rc && out, "last_num_loaded_samples: NULL argument");
+  XR_CHECK_ARG(rc->count_samples, "last_num_loaded_samples: counting is disabled (xr_rc_set_count_samples)");
+  xr_status st = xr_rc_synchronize(rc);
+  if (st != XR_OK) return st;
+  DeviceGuard g(rc->device);
+  unsigned long long v = 0;
+  XR_CUDA_TRY(cudaMemcpy(&v, rc->d_counters.as<char>() + 56, 8, cudaMemcpyDeviceToHost));
   *out = v;
   return XR_OK;
 }

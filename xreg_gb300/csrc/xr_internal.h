@@ -48,6 +48,7 @@ struct DrrParams {
   const float* bg_projs;  // [num_cams][rows*cols] or nullptr
   float* out;             // [num_projs][rows][cols]
   unsigned long long* sample_counter;  // nullptr = no counting
+  unsigned long long* loaded_counter;  // samples loaded (not skipped as provably zero); with sample_counter
   unsigned int* err_counter;          // rays whose step count exceeded max_steps
   unsigned long long max_steps;       // guard against non-finite / absurd poses
   int64_t num_projs;

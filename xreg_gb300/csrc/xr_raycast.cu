@@ -346,12 +346,15 @@ __device__ __forceinline__ float march_samples(const DrrParams& p, const void* d
 }
 
 // Traces the ray of pixel (row, col) of projection proj and stores the result
-// (the caller checks that the pixel exists).  Returns the number of samples.
+// (the caller checks that the pixel exists).  Returns the number of samples of
+// the reference step rule; *loaded receives how many of them were loaded (the
+// others were proven zero and skipped).
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
 __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, const int64_t proj, const int row,
-                                                          const int col) {
+                                                          const int col, unsigned int* loaded) {
   float sum = (KERNEL == XR_LINE_INT_MAX) ? -FLT_MAX : 0.0f;
   unsigned long long ns = 0;
+  *loaded = 0;
   {
     // xReg's per-ray float set-up (xf::ray_setup): clipped, nudged segment,
     // start point, step vector and the step-count quotient
@@ -466,6 +469,7 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
         }
         // samples first..last in order; the sum order never changes with UNROLL
         unsigned int n = first <= last ? last - first + 1u : 0u;
+        *loaded = n;
         if (inside)
           sum = march_samples<VT, KERNEL, LAYOUT, UNROLL, true>(p, data, px, py, pz, sx, sy, sz, n, sum);
         else
@@ -506,10 +510,16 @@ drr_kernel(const DrrParams p, const int64_t proj_base) {
   const int row = blockIdx.z * ((8 / bw) * wr) + (warp / bw) * wr + (lane >> wl);
   const int64_t proj = proj_base + blockIdx.x;
   unsigned long long ns = 0;
-  if (col < p.cols && row < p.rows) ns = trace_pixel<VT, KERNEL, LAYOUT, UNROLL>(p, proj, row, col);
+  unsigned int nl = 0;
+  if (col < p.cols && row < p.rows) ns = trace_pixel<VT, KERNEL, LAYOUT, UNROLL>(p, proj, row, col, &nl);
   if (p.sample_counter) {
-    for (int o = 16; o > 0; o >>= 1) ns += __shfl_down_sync(0xffffffffu, ns, o);
+    unsigned long long nlw = nl;
+    for (int o = 16; o > 0; o >>= 1) {
+      ns += __shfl_down_sync(0xffffffffu, ns, o);
+      nlw += __shfl_down_sync(0xffffffffu, nlw, o);
+    }
     if (lane == 0 && ns) atomicAdd(p.sample_counter, ns);
+    if (lane == 0 && nlw && p.loaded_counter) atomicAdd(p.loaded_counter, nlw);
   }
 }
 
@@ -541,7 +551,8 @@ drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long tota
     const int ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
     const int col = tx * 16 + (warp & 1) * 8 + (lane & 7);
     const int row = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
-    if (col < J.p.cols && row < J.p.rows) trace_pixel<VT, XR_LINE_INT_SUM, LAYOUT, UNROLL>(J.p, proj, row, col);
+    unsigned int nl;
+    if (col < J.p.cols && row < J.p.rows) trace_pixel<VT, XR_LINE_INT_SUM, LAYOUT, UNROLL>(J.p, proj, row, col, &nl);
   }
 }
 
