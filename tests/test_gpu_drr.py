@@ -225,13 +225,13 @@ def test_launch_configs_are_bit_identical(xr, oracle, vt):
     rc.compute()
     auto = rc.projs()
     lay, bw, un, wr = rc.launch_config_ex()
-    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2, 3, 4, 5) and wr in (4, 8)
+    assert lay in (0, 1, 2) and bw in (1, 2, 4) and un in (1, 2, 3, 4, 5, 6) and wr in (4, 8)
     # layout 2: the float32 cell copy read with one 256-bit load per sample;
     # loops 3 / 4: two / four samples per iteration after the macro-cell trim;
-    # warps of 8x4 or 4x8 pixels
+    # loop 6: loop 4 on packed FP32 pairs; warps of 8x4 or 4x8 pixels
     for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
         for bw in (1, 2, 4, 8):
-            for un in (1, 2, 3, 4, 5):
+            for un in (1, 2, 3, 4, 5, 6):
                 for wr in (4, 8):
                     rc.set_launch_config(layout, bw, un, wr)
                     rc.compute()
@@ -279,7 +279,7 @@ def test_empty_space_skipping_is_exact(xr, oracle, vt):
     for skip in (False, True):
         rc.set_empty_space_skipping(skip)
         for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
-            for un in (2, 3, 4, 5):
+            for un in (2, 3, 4, 5, 6):
                 rc.set_launch_config(layout, 2, un)
                 rc.compute()
                 outs.append((rc.projs(), rc.last_num_samples()))
@@ -366,7 +366,7 @@ def test_macro_cell_skipping_is_exact(xr, oracle, vt):
         rc.distribute_xforms_among_cam_models(poses)
         rc.set_count_samples(True)
         outs = []
-        for skip, un in ((False, 1), (True, 1), (True, 3), (True, 4), (True, 5)):
+        for skip, un in ((False, 1), (True, 1), (True, 3), (True, 4), (True, 5), (True, 6)):
             rc.set_empty_space_skipping(skip)
             for layout in ((0, 1, 2) if vt == 0 else (0, 1)):
                 rc.set_launch_config(layout, 2, un)

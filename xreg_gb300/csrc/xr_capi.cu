@@ -924,15 +924,15 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   const int32_t bws[3] = {1, 2, 4};
   // loops 3 and 4 = 2 and 4 samples per iteration after the macro-cell trim (sum
   // kernel); 5 = loop 3 whose pairs share one load when both samples fall in one
-  // cell (256-bit float32 CELL8 read)
-  const int32_t unrolls[5] = {1, 2, 3, 4, 5};
+  // cell, 6 = loop 4 on packed FP32 pairs (both for the 256-bit float32 CELL8 read)
+  const int32_t unrolls[6] = {1, 2, 3, 4, 5, 6};
   for (int32_t lay : layouts) {
     if (lay != XR_LAYOUT_LINEAR && !has_cells) continue;
     if (lay == 2 && vol.type != XR_VOXEL_F32) continue;
     for (int32_t bw : bws)
       for (int32_t un : unrolls) {
         if (un >= 3 && !(p.vol.occ && p.kernel_id == XR_LINE_INT_SUM)) continue;
-        if (un == 5 && lay != 2) continue;
+        if ((un == 5 || un == 6) && lay != 2) continue;
         t.vol.layout = lay;
         t.block_warps_x = bw;
         t.unroll = un;
@@ -1096,8 +1096,8 @@ extern "C" XR_API xr_status xr_rc_set_launch_config_ex(xr_raycaster rc, int32_t 
   XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= 2, "set_launch_config: bad layout");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || bw == 1 || bw == 2 || bw == 4 || bw == 8,
                "set_launch_config: block_warps_x must be 1, 2, 4 or 8");
-  XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || (unroll >= 1 && unroll <= 5),
-               "set_launch_config: unroll must be 1 to 5");
+  XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || (unroll >= 1 && unroll <= 6),
+               "set_launch_config: unroll must be 1 to 6");
   rc->cfg_layout = layout;
   rc->cfg_bw = bw;
   rc->cfg_unroll = unroll;

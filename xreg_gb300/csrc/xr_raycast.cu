@@ -22,11 +22,12 @@
 // Volume layouts (same values, same arithmetic, bit-identical results):
 //   LINEAR  voxels x-fastest; a sample issues 8 scalar loads.
 //   CELL8   for every trilinear cell (ix, iy, iz) in [0, n-2]^3 the 8 corner
-//           values are stored contiguously (v000 v100 v010 v110 v001 v101 v011
-//           v111): one 16-byte load per sample for FP16/BF16, two for FP32,
-//           or one 32-byte load for FP32 (the 256-bit read, layout 2).  It
-//           spends 8x the voxel bytes of HBM to cut L1 requests per sample from
-//           8 to 1-2; the linear kernel is bound by exactly those requests.
+//           values are stored contiguously as z-pairs (v000 v001 v100 v101 v010
+//           v011 v110 v111, vxyz), so each pair the packed FP32 blend needs is
+//           one 64-bit register: one 16-byte load per sample for FP16/BF16, two
+//           for FP32, or one 32-byte load for FP32 (the 256-bit read, layout 2).
+//           It spends 8x the voxel bytes of HBM to cut L1 requests per sample
+//           from 8 to 1-2; the linear kernel is bound by exactly those requests.
 #include "xr_internal.h"
 
 #include <atomic>
@@ -109,6 +110,7 @@ constexpr int kLayoutCell8Wide = 2;
 constexpr int kUnrollMacroSkip = 3;  // loop 2 after the macro-cell trim
 constexpr int kUnrollTrim4 = 4;      // four samples per iteration after the macro-cell trim
 constexpr int kUnrollPairShare = 5;  // loop 3 whose second sample of a pair reuses the first's cell
+constexpr int kUnrollPacked = 6;     // loop 4 on packed FP32 pairs (float32 256-bit CELL8 reads)
 
 // Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
 // the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
@@ -158,16 +160,72 @@ __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, f
   return (iz * (ny - 1) + iy) * (nx - 1) + ix;
 }
 
-// Weighted-form trilinear of the 8 corners v000 v100 v010 v110 v001 v101 v011 v111.
+// Weighted-form trilinear of the 8 corners in cell order (z-pairs):
+// v000 v001 v100 v101 v010 v011 v110 v111 (vxyz).
 __device__ __forceinline__ float interp8(const float v[8], float fx, float fy, float fz) {
   const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-  const float a00 = fmaf(v[1], fx, v[0] * gx);
-  const float a10 = fmaf(v[3], fx, v[2] * gx);
-  const float a01 = fmaf(v[5], fx, v[4] * gx);
-  const float a11 = fmaf(v[7], fx, v[6] * gx);
+  const float a00 = fmaf(v[2], fx, v[0] * gx);
+  const float a01 = fmaf(v[3], fx, v[1] * gx);
+  const float a10 = fmaf(v[6], fx, v[4] * gx);
+  const float a11 = fmaf(v[7], fx, v[5] * gx);
   const float b0 = fmaf(a10, fy, a00 * gy);
   const float b1 = fmaf(a11, fy, a01 * gy);
   return fmaf(b1, fz, b0 * gz);
+}
+
+// ---- packed FP32 pairs (sm_100+ f32x2): each lane rounds exactly as the
+// scalar instruction with the same rounding mode, so results are bit-identical
+// to the scalar code and only the instruction count changes.
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long add2_rm(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("add.rm.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// The 32-byte float32 cell as four z-pairs with one 256-bit load.
+__device__ __forceinline__ void cell_pairs(const void* b, int c, unsigned long long q[4]) {
+  const unsigned long long* p = static_cast<const unsigned long long*>(b) + 4 * (size_t)c;
+  asm("ld.global.nc.v4.b64 {%0,%1,%2,%3}, [%4];" : "=l"(q[0]), "=l"(q[1]), "=l"(q[2]), "=l"(q[3]) : "l"(p));
+}
+// interp8 on z-pairs: q0 = (v000, v001), q1 = (v100, v101), q2 = (v010, v011),
+// q3 = (v110, v111); the x and y blends run on pairs, the z blend in scalar.
+__device__ __forceinline__ float interp8_pairs(const unsigned long long q[4], float fx, float fy, float fz) {
+  const unsigned long long one = pk2(1.0f, 1.0f);
+  const unsigned long long FX = pk2(fx, fx), FY = pk2(fy, fy);
+  const unsigned long long GX = sub2(one, FX), GY = sub2(one, FY);
+  const unsigned long long ay0 = fma2(q[1], FX, mul2(q[0], GX));  // (a00, a01)
+  const unsigned long long ay1 = fma2(q[3], FX, mul2(q[2], GX));  // (a10, a11)
+  const unsigned long long B = fma2(ay1, FY, mul2(ay0, GY));      // (b0, b1)
+  float b0, b1;
+  upk2(B, b0, b1);
+  return fmaf(b1, fz, b0 * (1.0f - fz));
 }
 
 // Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
@@ -206,12 +264,12 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
     const int sy = nx, sz = nx * ny;
     const int b = (iz * ny + iy) * nx + ix;
     v[0] = Vox<VT>::ld(data, b);
-    v[1] = Vox<VT>::ld(data, b + 1);
-    v[2] = Vox<VT>::ld(data, b + sy);
-    v[3] = Vox<VT>::ld(data, b + sy + 1);
-    v[4] = Vox<VT>::ld(data, b + sz);
-    v[5] = Vox<VT>::ld(data, b + sz + 1);
-    v[6] = Vox<VT>::ld(data, b + sz + sy);
+    v[1] = Vox<VT>::ld(data, b + sz);
+    v[2] = Vox<VT>::ld(data, b + 1);
+    v[3] = Vox<VT>::ld(data, b + sz + 1);
+    v[4] = Vox<VT>::ld(data, b + sy);
+    v[5] = Vox<VT>::ld(data, b + sz + sy);
+    v[6] = Vox<VT>::ld(data, b + sy + 1);
     v[7] = Vox<VT>::ld(data, b + sz + sy + 1);
   }
   return interp8(v, fx, fy, fz);
@@ -272,6 +330,52 @@ __device__ __forceinline__ float macro_march(const VolView& v, const float p0[3]
   return k;  // walk limit: treat the rest as occupied
 }
 
+// Loop 6: the four-sample loop of loop 4 for float32 256-bit CELL8 cells on
+// rays proven inside the volume, with the x and y coordinates kept as one
+// packed pair: position advance, the round-down floor (see cell_of) and the
+// fractions of x and y are one f32x2 instruction each, the corners arrive as
+// z-pairs and blend along x and y on pairs (interp8_pairs).  Same positions,
+// cells, fractions and sums as loop 4, bit for bit.
+__device__ __forceinline__ float march_packed_inside(const VolView& vol, const void* data, float px, float py,
+                                                     float pz, const float sx, const float sy, const float sz,
+                                                     unsigned int n, float sum) {
+  constexpr float kTwo23 = 8388608.0f;
+  const unsigned long long K = pk2(kTwo23, kTwo23), S = pk2(sx, sy);
+  unsigned long long P = pk2(px, py);
+  const unsigned int ux = (unsigned int)(vol.nx - 1), uy = (unsigned int)(vol.ny - 1), kb = 0x4B000000u;
+  const unsigned int bias = kb * (uy * ux + ux + 1u);
+  // cell index and fractions of the current position, then advance it
+  auto locate = [&](float& fx, float& fy, float& fz) -> int {
+    const unsigned long long T = add2_rm(P, K);
+    const float tz = __fadd_rd(pz, kTwo23);
+    const unsigned long long F = sub2(P, sub2(T, K));
+    fz = __fsub_rn(pz, __fsub_rn(tz, kTwo23));
+    float tx, ty;
+    upk2(T, tx, ty);
+    upk2(F, fx, fy);
+    const unsigned int bx = (unsigned int)__float_as_int(tx), by = (unsigned int)__float_as_int(ty),
+                       bz = (unsigned int)__float_as_int(tz);
+    P = add2(P, S);
+    pz = __fadd_rn(pz, sz);
+    return (int)((bz * uy + by) * ux + bx - bias);
+  };
+  for (; n >= 4; n -= 4) {
+    float f[4][3];
+    unsigned long long q[4][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cell_pairs(data, locate(f[k][0], f[k][1], f[k][2]), q[k]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sum = __fadd_rn(sum, interp8_pairs(q[k], f[k][0], f[k][1], f[k][2]));
+  }
+  for (; n > 0; --n) {
+    float fx, fy, fz;
+    unsigned long long q[4];
+    cell_pairs(data, locate(fx, fy, fz), q);
+    sum = __fadd_rn(sum, interp8_pairs(q, fx, fy, fz));
+  }
+  return sum;
+}
+
 // The samples of one ray from the current position on, n of them, in order
 // (the sum order never changes with UNROLL).  INSIDE: every position stays in
 // [0, n-1) on every axis (see sample()).
@@ -279,7 +383,10 @@ template <int VT, int KERNEL, int LAYOUT, int UNROLL, bool INSIDE>
 __device__ __forceinline__ float march_samples(const DrrParams& p, const void* data, float px, float py, float pz,
                                                const float sx, const float sy, const float sz, unsigned int n,
                                                float sum) {
-  if (UNROLL == kUnrollTrim4) {  // four loads in flight per thread
+  if constexpr (UNROLL == kUnrollPacked && INSIDE && VT == XR_VOXEL_F32 && LAYOUT == kLayoutCell8Wide &&
+                KERNEL == XR_LINE_INT_SUM)
+    return march_packed_inside(p.vol, data, px, py, pz, sx, sy, sz, n, sum);
+  if (UNROLL == kUnrollTrim4 || UNROLL == kUnrollPacked) {  // four loads in flight per thread
     for (; n >= 4; n -= 4) {
       const float v0 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
       px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
@@ -496,7 +603,9 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
 // Loop 4 keeps four cells (32 floats) in flight per thread: capped at 48
 // registers (5 blocks per SM), measured faster than 40 (small spills) or 64.
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, UNROLL == kUnrollTrim4 ? kMinBlocksPerSM - 1 : kMinBlocksPerSM)
+__global__ void __launch_bounds__(kThreads,
+                                  (UNROLL == kUnrollTrim4 || UNROLL == kUnrollPacked) ? kMinBlocksPerSM - 1
+                                                                                       : kMinBlocksPerSM)
 drr_kernel(const DrrParams p, const int64_t proj_base) {
   // Each warp covers an 8 x 4 (or, tall, 4 x 8) patch of pixels so its 32 rays
   // stay close inside the volume; a block is bw x (8 / bw) warps.  The
@@ -627,6 +736,9 @@ cudaError_t launch_unroll(const DrrParams& p, cudaStream_t s) {
     if constexpr (KERNEL == XR_LINE_INT_SUM) {
       if (p.unroll == kUnrollTrim4) return launch_t<VT, KERNEL, LAYOUT, kUnrollTrim4>(p, s);
       if constexpr (LAYOUT == kLayoutCell8Wide && VT == XR_VOXEL_F32)
+        if (p.unroll == kUnrollPacked) return launch_t<VT, KERNEL, LAYOUT, kUnrollPacked>(p, s);
+      if (p.unroll == kUnrollPacked) return launch_t<VT, KERNEL, LAYOUT, kUnrollTrim4>(p, s);
+      if constexpr (LAYOUT == kLayoutCell8Wide && VT == XR_VOXEL_F32)
         if (p.unroll == kUnrollPairShare) return launch_t<VT, KERNEL, LAYOUT, kUnrollPairShare>(p, s);
       return launch_t<VT, KERNEL, LAYOUT, kUnrollMacroSkip>(p, s);
     }
@@ -659,8 +771,9 @@ __global__ void build_cells_kernel(const float* __restrict__ vox, int nx, int ny
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ix = c % ncx, iy = (c / ncx) % ncy, iz = c / (ncx * ncy);
     const int64_t b = (iz * ny + iy) * nx + ix, sy = nx, sz = (int64_t)nx * ny;
-    const float v[8] = {vox[b], vox[b + 1], vox[b + sy], vox[b + sy + 1],
-                        vox[b + sz], vox[b + sz + 1], vox[b + sz + sy], vox[b + sz + sy + 1]};
+    // z-pairs: v000 v001 v100 v101 v010 v011 v110 v111 (vxyz)
+    const float v[8] = {vox[b], vox[b + sz], vox[b + 1], vox[b + sz + 1],
+                        vox[b + sy], vox[b + sz + sy], vox[b + sy + 1], vox[b + sz + sy + 1]};
     if (VT == XR_VOXEL_F32) {
       float4* o = static_cast<float4*>(out) + 2 * c;
       o[0] = make_float4(v[0], v[1], v[2], v[3]);
