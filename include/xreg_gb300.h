@@ -212,7 +212,8 @@ XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
  * kernel with empty-space skipping on; otherwise 3 and 4 run as 2), or 5 = 3
  * with the second sample of a pair reusing the first's corners when both lie in
  * one cell (256-bit float32 CELL8 read; elsewhere 5 runs as 3), or 6 = 4 on
- * packed FP32 pairs (256-bit float32 CELL8 read; elsewhere 6 runs as 4).  layout
+ * packed FP32 pairs (float32 256-bit or FP16 / BF16 CELL8 reads; elsewhere 6
+ * runs as 4).  layout
  * XR_LAYOUT_AUTO (the default) lets
  * the autotuner time the candidates on the first compute of each shape (volume
  * size, voxel type, detector, projection count) and cache the fastest for the

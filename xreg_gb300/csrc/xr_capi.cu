@@ -924,7 +924,8 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
   const int32_t bws[3] = {1, 2, 4};
   // loops 3 and 4 = 2 and 4 samples per iteration after the macro-cell trim (sum
   // kernel); 5 = loop 3 whose pairs share one load when both samples fall in one
-  // cell, 6 = loop 4 on packed FP32 pairs (both for the 256-bit float32 CELL8 read)
+  // cell (256-bit float32 CELL8 read), 6 = loop 4 on packed FP32 pairs (256-bit
+  // float32 or 128-bit half CELL8 reads)
   const int32_t unrolls[6] = {1, 2, 3, 4, 5, 6};
   for (int32_t lay : layouts) {
     if (lay != XR_LAYOUT_LINEAR && !has_cells) continue;
@@ -932,7 +933,8 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
     for (int32_t bw : bws)
       for (int32_t un : unrolls) {
         if (un >= 3 && !(p.vol.occ && p.kernel_id == XR_LINE_INT_SUM)) continue;
-        if ((un == 5 || un == 6) && lay != 2) continue;
+        if (un == 5 && lay != 2) continue;
+        if (un == 6 && !(lay == 2 || (lay == XR_LAYOUT_CELL8 && vol.type != XR_VOXEL_F32))) continue;
         t.vol.layout = lay;
         t.block_warps_x = bw;
         t.unroll = un;

@@ -209,10 +209,27 @@ __device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigne
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
   return d;
 }
-// The 32-byte float32 cell as four z-pairs with one 256-bit load.
+// A cell as four z-pairs of float32 values: the 32-byte float32 cell with one
+// 256-bit load; a 16-byte FP16 / BF16 cell with one 128-bit load, each 32-bit
+// word (v_z0, v_z1) widened to a pair (BF16: a shift and a mask, exactly).
+template <int VT>
 __device__ __forceinline__ void cell_pairs(const void* b, int c, unsigned long long q[4]) {
-  const unsigned long long* p = static_cast<const unsigned long long*>(b) + 4 * (size_t)c;
-  asm("ld.global.nc.v4.b64 {%0,%1,%2,%3}, [%4];" : "=l"(q[0]), "=l"(q[1]), "=l"(q[2]), "=l"(q[3]) : "l"(p));
+  if constexpr (VT == XR_VOXEL_F32) {
+    const unsigned long long* p = static_cast<const unsigned long long*>(b) + 4 * (size_t)c;
+    asm("ld.global.nc.v4.b64 {%0,%1,%2,%3}, [%4];" : "=l"(q[0]), "=l"(q[1]), "=l"(q[2]), "=l"(q[3]) : "l"(p));
+  } else {
+    const uint4 w = __ldg(static_cast<const uint4*>(b) + c);
+    const unsigned int ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if constexpr (VT == XR_VOXEL_BF16) {
+        q[k] = pk2(__uint_as_float(ws[k] << 16), __uint_as_float(ws[k] & 0xffff0000u));
+      } else {
+        const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&ws[k]));
+        q[k] = pk2(f.x, f.y);
+      }
+    }
+  }
 }
 // interp8 on z-pairs: q0 = (v000, v001), q1 = (v100, v101), q2 = (v010, v011),
 // q3 = (v110, v111); the x and y blends run on pairs, the z blend in scalar.
@@ -330,12 +347,14 @@ __device__ __forceinline__ float macro_march(const VolView& v, const float p0[3]
   return k;  // walk limit: treat the rest as occupied
 }
 
-// Loop 6: the four-sample loop of loop 4 for float32 256-bit CELL8 cells on
-// rays proven inside the volume, with the x and y coordinates kept as one
+// Loop 6: the four-sample loop of loop 4 for CELL8 cells (float32 256-bit
+// reads, FP16 / BF16 128-bit reads) on rays proven inside the volume, with the
+// x and y coordinates kept as one
 // packed pair: position advance, the round-down floor (see cell_of) and the
 // fractions of x and y are one f32x2 instruction each, the corners arrive as
 // z-pairs and blend along x and y on pairs (interp8_pairs).  Same positions,
 // cells, fractions and sums as loop 4, bit for bit.
+template <int VT>
 __device__ __forceinline__ float march_packed_inside(const VolView& vol, const void* data, float px, float py,
                                                      float pz, const float sx, const float sy, const float sz,
                                                      unsigned int n, float sum) {
@@ -363,14 +382,14 @@ __device__ __forceinline__ float march_packed_inside(const VolView& vol, const v
     float f[4][3];
     unsigned long long q[4][4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) cell_pairs(data, locate(f[k][0], f[k][1], f[k][2]), q[k]);
+    for (int k = 0; k < 4; ++k) cell_pairs<VT>(data, locate(f[k][0], f[k][1], f[k][2]), q[k]);
 #pragma unroll
     for (int k = 0; k < 4; ++k) sum = __fadd_rn(sum, interp8_pairs(q[k], f[k][0], f[k][1], f[k][2]));
   }
   for (; n > 0; --n) {
     float fx, fy, fz;
     unsigned long long q[4];
-    cell_pairs(data, locate(fx, fy, fz), q);
+    cell_pairs<VT>(data, locate(fx, fy, fz), q);
     sum = __fadd_rn(sum, interp8_pairs(q, fx, fy, fz));
   }
   return sum;
@@ -383,9 +402,10 @@ template <int VT, int KERNEL, int LAYOUT, int UNROLL, bool INSIDE>
 __device__ __forceinline__ float march_samples(const DrrParams& p, const void* data, float px, float py, float pz,
                                                const float sx, const float sy, const float sz, unsigned int n,
                                                float sum) {
-  if constexpr (UNROLL == kUnrollPacked && INSIDE && VT == XR_VOXEL_F32 && LAYOUT == kLayoutCell8Wide &&
-                KERNEL == XR_LINE_INT_SUM)
-    return march_packed_inside(p.vol, data, px, py, pz, sx, sy, sz, n, sum);
+  if constexpr (UNROLL == kUnrollPacked && INSIDE && KERNEL == XR_LINE_INT_SUM &&
+                ((VT == XR_VOXEL_F32 && LAYOUT == kLayoutCell8Wide) ||
+                 (VT != XR_VOXEL_F32 && LAYOUT == XR_LAYOUT_CELL8)))
+    return march_packed_inside<VT>(p.vol, data, px, py, pz, sx, sy, sz, n, sum);
   if (UNROLL == kUnrollTrim4 || UNROLL == kUnrollPacked) {  // four loads in flight per thread
     for (; n >= 4; n -= 4) {
       const float v0 = sample<VT, LAYOUT, INSIDE>(p.vol, data, px, py, pz);
@@ -735,7 +755,8 @@ cudaError_t launch_unroll(const DrrParams& p, cudaStream_t s) {
     // loop exists for the 256-bit float32 CELL8 read (elsewhere loop 3 runs)
     if constexpr (KERNEL == XR_LINE_INT_SUM) {
       if (p.unroll == kUnrollTrim4) return launch_t<VT, KERNEL, LAYOUT, kUnrollTrim4>(p, s);
-      if constexpr (LAYOUT == kLayoutCell8Wide && VT == XR_VOXEL_F32)
+      if constexpr ((LAYOUT == kLayoutCell8Wide && VT == XR_VOXEL_F32) ||
+                    (LAYOUT == XR_LAYOUT_CELL8 && VT != XR_VOXEL_F32))
         if (p.unroll == kUnrollPacked) return launch_t<VT, KERNEL, LAYOUT, kUnrollPacked>(p, s);
       if (p.unroll == kUnrollPacked) return launch_t<VT, KERNEL, LAYOUT, kUnrollTrim4>(p, s);
       if constexpr (LAYOUT == kLayoutCell8Wide && VT == XR_VOXEL_F32)
