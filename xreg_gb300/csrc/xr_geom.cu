@@ -38,7 +38,39 @@ __global__ void proj_geom_kernel(xf::Affine phys_to_idx, const xr_camera_desc* _
   out[p] = g;
 }
 
+// One thread per projection of every job (jobs in order of `first`).
+__global__ void proj_geom_jobs_kernel(const GeomJob* __restrict__ jobs, int njobs, int64_t total) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  int j = 0;
+  while (j + 1 < njobs && jobs[j + 1].first <= t) ++j;
+  const GeomJob& J = jobs[j];
+  const int64_t p = t - J.first;
+  const xr_camera_desc& cd = J.cams[J.cam_idx[p]];
+  xf::Camera cam;
+  for (int k = 0; k < 9; ++k) cam.K[k] = __double2float_rn(cd.intrins[k]);
+  for (int k = 0; k < 16; ++k) cam.E[k] = __double2float_rn(cd.extrins[k]);
+  cam.focal_len = __double2float_rn(cd.focal_len);
+  cam.frame = cd.coord_frame_type;
+  const double* pd = J.poses + 16 * (p % J.pose_stride);
+  xf::Affine pose;
+  for (int i = 0; i < 3; ++i) {
+    for (int jj = 0; jj < 3; ++jj) pose.L[i * 3 + jj] = __double2float_rn(pd[i * 4 + jj]);
+    pose.t[i] = __double2float_rn(pd[i * 4 + 3]);
+  }
+  ProjGeom g;
+  xf::ray_frame(cam, J.p2i, pose, g);
+  J.out[p] = g;
+}
+
 }  // namespace
+
+cudaError_t launch_proj_geom_jobs(const GeomJob* d_jobs, int njobs, int64_t total, cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  const int threads = 128;
+  proj_geom_jobs_kernel<<<(unsigned)((total + threads - 1) / threads), threads, 0, s>>>(d_jobs, njobs, total);
+  return cudaGetLastError();
+}
 
 xf::Affine phys_to_idx_xform(const xr_volume_desc& vol) {
   // ITKImagePhysicalPointTransformsAsEigen (xregITKBasicImageUtils.h:133-165):

@@ -1,0 +1,256 @@
+// xr_gradtile.cuh -- device code shared by the split grad-NCC metric kernels
+// (xr_metrics.cu) and the fused evaluation kernel (xr_raycast.cu): compensated
+// reductions, the moments of one 32 x 64-pixel tile of a moving image's
+// gradients, and the per-image FP64 combine.  Both paths run exactly this code
+// on the same tiles, so their similarity values are identical bit for bit.
+//
+// Gradients (xregImgSimMetric2DGradImgCPU.cpp:48-65,86-101): OpenCV's sigma-0
+// Gaussian [1 4 6 4 1]/16 (or [1 2 1]/4), then the 3x3 Sobel in x and y, with
+// BORDER_REFLECT_101; NCC of each direction (xregImgSimMetric2DNCCCPU.cpp:
+// 53-63,164-209), sim = 0.5 (s_x + s_y) (xregImgSimMetric2DGradNCCCPU.cpp:51-65).
+#pragma once
+
+#include "xr_internal.h"
+
+namespace xr {
+namespace gt {
+
+constexpr int kThreads = 256;                     // block size of every tile kernel
+constexpr int kGW = 32;                           // tile columns = threads across
+constexpr int kGR = 8;                            // rows per thread
+constexpr int kGH = kGR * (kThreads / kGW);       // tile rows (64)
+constexpr int kFinalizeThreads = 128;             // threads of the per-image combine
+
+__device__ __forceinline__ int reflect101(int i, int n) {
+  if (i < 0) i = -i;
+  if (i >= n) i = 2 * (n - 1) - i;
+  return i;
+}
+
+// A float-float value hi + lo (about 48 significant bits).
+struct FF {
+  float hi, lo;
+};
+
+// Knuth's two-sum on the FP32 pipe for float-float values: this GPU's FP64 pipe
+// is slow enough that block reductions in double kept it 82 % busy and bounded
+// the grad-NCC moment kernel.  Explicit _rn intrinsics keep every step unfused.
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));  // s + e = a.hi + b.hi exactly
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  const float hi = __fadd_rn(s, e);
+  return FF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+
+// a b exactly as a float-float (the rounding error of the product from one fma).
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return FF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_shfl_down(FF v, int o) {
+  return FF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of K doubles per thread over the first nw warps (the others
+// must hold zeros); result valid in thread 0.
+template <int K>
+__device__ __forceinline__ void block_sum_d(double (&v)[K], double* red /* [K][32] */, int nw) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const double w = warp_sum_d(v[k]);
+    if (lane == 0 && warp < nw) red[k * 32 + warp] = w;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double w = (lane < nw) ? red[k * 32 + lane] : 0.0;
+      w = warp_sum_d(w);
+      v[k] = w;
+    }
+  }
+}
+
+__device__ __forceinline__ double ncc_sim_from_moments(double sm, double smm, double smf, double n,
+                                                       const FixedNCC& fx) {
+  const double mean = sm / n;
+  double var = (smm - n * mean * mean) / (n - 1.0);
+  if (var < 0.0) var = 0.0;
+  double sd = sqrt(var);
+  if (sd < 1.0e-6) sd = 1.0e-6;
+  const double cov = smf - mean * fx.sum_fhat;
+  const double ncc = cov / (n * fx.sd * sd);
+  return (1.0 - ncc) * 0.5;
+}
+
+// Shared memory of one tile: the horizontally blurred rows, blurred in place
+// down the columns (the vertical pass reads every input before it writes).
+template <int KR>
+struct GradTileSmem {
+  static constexpr int H = KR + 1;                // halo: blur radius + Sobel
+  static constexpr int WI = kGW + 2 * H, HI = kGH + 2 * H;
+  static constexpr int WB = kGW + 2, HB = kGH + 2;
+  float hb[HI][WB + 1];
+  FF red[6 * 32];
+};
+
+// Image pixel (row, col) of a tile's input; CG reads through L2 only (pixels
+// written earlier in the same kernel by other blocks).
+template <bool CG>
+__device__ __forceinline__ float tile_px(const float* __restrict__ src, int cols, int gr, int gc) {
+  const float* p = src + (int64_t)gr * cols + gc;
+  return CG ? __ldcg(p) : __ldg(p);
+}
+
+// Moments of the moving gradients over the 32 x 64-pixel tile at (y0, x0),
+// 256 threads: each thread owns one column and eight consecutive rows, so the
+// Sobel stencil slides down the column; sums are plain float per thread (8
+// terms) and per warp (256 pixels), float-float across the warps.  v (valid in
+// thread 0): S_gx, S_gx^2, S_gx fx, S_gy, S_gy^2, S_gy fy.
+template <int KR, bool CG>
+__device__ void grad_tile_moments(const float* __restrict__ src, int rows, int cols, int y0, int x0,
+                                  const float* __restrict__ fhx, const float* __restrict__ fhy,
+                                  const uint8_t* __restrict__ mask, GradTileSmem<KR>& sm, double (&v)[6]) {
+  using S = GradTileSmem<KR>;
+  constexpr int H = S::H, HI = S::HI, WB = S::WB, HB = S::HB;
+  const int tx = threadIdx.x % kGW, ty = threadIdx.x / kGW;
+  // Rows / cols past the last tile pixel only feed pixels that are skipped;
+  // clamping before the reflection keeps every read inside the image.
+  const bool interior = y0 >= H && x0 >= H && y0 + kGH + H <= rows && x0 + kGW + H <= cols;
+  auto in = [&](int r, int c) -> float {
+    int gr = y0 - H + r, gc = x0 - H + c;
+    if (!interior) {
+      gr = reflect101(min(gr, rows - 1 + H), rows);
+      gc = reflect101(min(gc, cols - 1 + H), cols);
+    }
+    return tile_px<CG>(src, cols, gr, gc);
+  };
+  if constexpr (KR == 0) {
+    for (int i = threadIdx.x; i < HB * WB; i += kThreads) {
+      const int r = i / WB, c = i - r * WB;
+      sm.hb[r][c] = in(r, c);
+    }
+  } else {
+    // horizontal pass over all input rows, blurred columns [x0-1, x0+kGW+1)
+    for (int i = threadIdx.x; i < HI * WB; i += kThreads) {
+      const int r = i / WB, c = i - r * WB;
+      sm.hb[r][c] = (KR == 2) ? (0.0625f * in(r, c) + 0.25f * in(r, c + 1) + 0.375f * in(r, c + 2) +
+                                 0.25f * in(r, c + 3) + 0.0625f * in(r, c + 4))
+                              : (0.25f * in(r, c) + 0.5f * in(r, c + 1) + 0.25f * in(r, c + 2));
+    }
+    __syncthreads();
+    // vertical pass in place: WB columns x 4 chunks of rows, every output of a
+    // chunk computed before the barrier, written after it
+    constexpr int kChunks = 4, kCh = (HB + kChunks - 1) / kChunks;
+    const int c = threadIdx.x % WB, j = threadIdx.x / WB;
+    float o[kCh];
+    if (j < kChunks) {
+#pragma unroll
+      for (int k = 0; k < kCh; ++k) {
+        const int r = j * kCh + k;
+        if (r < HB)
+          o[k] = (KR == 2) ? (0.0625f * sm.hb[r][c] + 0.25f * sm.hb[r + 1][c] + 0.375f * sm.hb[r + 2][c] +
+                              0.25f * sm.hb[r + 3][c] + 0.0625f * sm.hb[r + 4][c])
+                           : (0.25f * sm.hb[r][c] + 0.5f * sm.hb[r + 1][c] + 0.25f * sm.hb[r + 2][c]);
+      }
+    }
+    __syncthreads();
+    if (j < kChunks) {
+#pragma unroll
+      for (int k = 0; k < kCh; ++k) {
+        const int r = j * kCh + k;
+        if (r < HB) sm.hb[r][c] = o[k];
+      }
+    }
+  }
+  __syncthreads();
+  const auto& bl = sm.hb;  // blurred region [HB][WB]
+  float m[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  const int gxc = x0 + tx;
+  if (gxc < cols) {
+    const int rb = ty * kGR;  // first output row (tile-local); blurred rows rb .. rb + kGR + 1
+    float a0 = bl[rb][tx], b0 = bl[rb][tx + 1], c0 = bl[rb][tx + 2];
+    float a1 = bl[rb + 1][tx], b1 = bl[rb + 1][tx + 1], c1 = bl[rb + 1][tx + 2];
+#pragma unroll
+    for (int k = 0; k < kGR; ++k) {
+      const float a2 = bl[rb + k + 2][tx], b2 = bl[rb + k + 2][tx + 1], c2 = bl[rb + k + 2][tx + 2];
+      const int gyr = y0 + rb + k;
+      if (gyr < rows) {
+        const int64_t pix = (int64_t)gyr * cols + gxc;
+        if (!mask || mask[pix]) {
+          // Sobel at (r, c) from the blurred 3x3 neighbourhood a0 b0 c0 / a1 . c1 / a2 b2 c2
+          const float gx = ((c0 - a0) + 2.0f * (c1 - a1)) + (c2 - a2);
+          const float gy = ((a2 - a0) + 2.0f * (b2 - b0)) + (c2 - c0);
+          m[0] += gx;
+          m[1] += gx * gx;
+          m[2] += gx * fhx[pix];
+          m[3] += gy;
+          m[4] += gy * gy;
+          m[5] += gy * fhy[pix];
+        }
+      }
+      a0 = a1; b0 = b1; c0 = c1;
+      a1 = a2; b1 = b2; c1 = c2;
+    }
+  }
+  // plain-float sums within a warp (256 pixels), float-float across the warps
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    float w = m[k];
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if (lane == 0) sm.red[k * 32 + warp] = FF{w, 0.0f};
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      FF w = (lane < kThreads / 32) ? sm.red[k * 32 + lane] : FF{0.0f, 0.0f};
+      for (int o = 16; o > 0; o >>= 1) w = ff_add(w, ff_shfl_down(w, o));
+      v[k] = (double)w.hi + (double)w.lo;
+    }
+  }
+  __syncthreads();  // sm is reused by the caller's next tile
+}
+
+// Per-image combine: the tile partials (nblk x 6 doubles, read through L2 when
+// CG) summed by the first kFinalizeThreads threads with that stride, then
+// across their warps; the similarity value (valid in thread 0).
+template <bool CG>
+__device__ float grad_finalize_image(const double* __restrict__ p, int nblk, double n, const FixedNCC& fx,
+                                     const FixedNCC& fy, double* red /* [6][32] */) {
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  if (threadIdx.x < kFinalizeThreads)
+    for (int k = threadIdx.x; k < nblk; k += kFinalizeThreads)
+      for (int j = 0; j < 6; ++j) a[j] += CG ? __ldcg(p + 6 * k + j) : p[6 * k + j];
+  block_sum_d<6>(a, red, kFinalizeThreads / 32);
+  float out = 0.0f;
+  if (threadIdx.x == 0) {
+    const double sx = ncc_sim_from_moments(a[0], a[1], a[2], n, fx);
+    const double sy = ncc_sim_from_moments(a[3], a[4], a[5], n, fy);
+    // 0.5 * (float(s_x) + float(s_y)) as in ImgSimMetric2DGradNCCCPU::compute
+    out = 0.5f * ((float)sx + (float)sy);
+  }
+  __syncthreads();  // red is reused
+  return out;
+}
+
+// Mean over views of one candidate's values (ImgSimMetric2DCombineMean,
+// xregImgSimMetric2DCombine.cpp:79-96).
+__device__ __forceinline__ float combine_mean(const float* const* view_sims, int nviews, int64_t i, bool cg) {
+  float s = 0.0f;
+  for (int v = 0; v < nviews; ++v) s += cg ? __ldcg(view_sims[v] + i) : view_sims[v][i];
+  return s / (float)nviews;
+}
+
+}  // namespace gt
+}  // namespace xr

@@ -106,6 +106,51 @@ struct FixedNCC {           // per direction (one for NCC, x and y for grad-NCC)
   double sum_fhat;          // sum of fhat over used pixels (exact decomposition)
 };
 
+// ---- fused evaluation (xr_raycast.cu) ----
+// One view of a job whose grad-NCC (5x5 smoothing) runs inside the evaluation
+// kernel: the fixed side, the per-tile partials and the view's values.
+struct FusedView {
+  const float* fhx;       // zero-mean fixed gradients
+  const float* fhy;
+  const uint8_t* mask;    // or nullptr
+  FixedNCC fx, fy;
+  double n_used;
+  double* partials;       // [pop][metric tiles][6]
+  float* sims;            // [pop]
+};
+// A job of a fused evaluation launch: its DRR work items (16x16-pixel tiles,
+// projection fastest), and when `metric` is 1 the grad-NCC of every image
+// computed tile by tile as soon as the DRR pixels a 32x64 metric tile reads are
+// written, then each image's value, then each pose's mean over views.
+// Counters live in `cnt` (zero between launches; the block that completes a
+// counter resets it): [nviews * pop * mt] DRR tiles done per metric tile, then
+// [nviews * pop] metric tiles done per image, then [pop] views done per pose.
+constexpr int kMaxFusedViews = 16;
+struct FusedJob {
+  MultiJobDrr d;
+  int32_t metric;         // 1: grad-NCC fused behind the DRR; 0: DRR only
+  int32_t nviews;
+  int64_t pop;
+  int32_t mt_x, mt_y;     // metric tiles across / down
+  const FusedView* views; // [nviews]
+  float* out;             // [pop] mean over views
+  unsigned int* cnt;
+};
+// One persistent launch over the jobs of one (voxel type, layout) group.
+cudaError_t launch_eval_fused(const FusedJob* d_jobs, int njobs, long long total_items, int32_t voxel_type,
+                              int32_t layout, int32_t unroll, unsigned long long* d_counter, int* blocks_out,
+                              cudaStream_t s);
+// Geometry of many ray casters' projections in one launch.
+struct GeomJob {
+  xf::Affine p2i;
+  const xr_camera_desc* cams;
+  const double* poses;
+  const int32_t* cam_idx;
+  int64_t num_projs, pose_stride, first;  // first: index of this job's first projection over all jobs
+  ProjGeom* out;
+};
+cudaError_t launch_proj_geom_jobs(const GeomJob* d_jobs, int njobs, int64_t total_projs, cudaStream_t s);
+
 struct PatchFixed {         // per direction
   const float* img;         // fixed image (or its gradient), rows*cols
   const float* mean;        // per patch mean

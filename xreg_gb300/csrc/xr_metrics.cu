@@ -17,7 +17,7 @@
 // patch centre, two-pass mean / sample std dev over the (2r+1)^2 window from a
 // shared-memory tile, score 1 - sum((m - mu_m)/sd_m * fhat), unit weights, mean
 // over patches.  The fixed side (per-patch mean and 1/(sd n)) is pre-computed once.
-#include "xr_internal.h"
+#include "xr_gradtile.cuh"
 
 #include <cfloat>
 
@@ -25,18 +25,15 @@ namespace xr {
 namespace {
 
 constexpr int kT = 32;          // output tile edge for gradient kernels
-constexpr int kThreads = 256;
+using gt::kThreads;
 
-__device__ __forceinline__ int reflect101(int i, int n) {
-  if (i < 0) i = -i;
-  if (i >= n) i = 2 * (n - 1) - i;
-  return i;
-}
-
-// A float-float value hi + lo (about 48 significant bits).
-struct FF {
-  float hi, lo;
-};
+using gt::FF;
+using gt::ff_add;
+using gt::ff_prod;
+using gt::ff_shfl_down;
+using gt::reflect101;
+using gt::warp_sum_d;
+using gt::ncc_sim_from_moments;
 
 struct Kahan {
   float s = 0.0f, c = 0.0f;
@@ -49,29 +46,6 @@ struct Kahan {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
   __device__ __forceinline__ FF ff() const { return FF{s, -c}; }
 };
-
-// Knuth's two-sum on the FP32 pipe for float-float values (FF, before Kahan):
-// this GPU's FP64 pipe is slow enough that block reductions in double kept it
-// 82 % busy and bounded the grad-NCC moment kernel.  Explicit _rn intrinsics
-// keep every step unfused.
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  const float s = __fadd_rn(a.hi, b.hi);
-  const float bb = __fsub_rn(s, a.hi);
-  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));  // s + e = a.hi + b.hi exactly
-  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-  const float hi = __fadd_rn(s, e);
-  return FF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
-}
-
-// a b exactly as a float-float (the rounding error of the product from one fma).
-__device__ __forceinline__ FF ff_prod(float a, float b) {
-  const float p = __fmul_rn(a, b);
-  return FF{p, fmaf(a, b, -p)};
-}
-
-__device__ __forceinline__ FF ff_shfl_down(FF v, int o) {
-  return FF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
-}
 
 // Block-wide sum of K float-float values per thread, returned in double by
 // thread 0 (the other threads get undefined values).
@@ -95,29 +69,10 @@ __device__ __forceinline__ void block_sum_ff(FF (&v)[K], double (&out)[K], FF* r
   }
 }
 
-__device__ __forceinline__ double warp_sum_d(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Block-wide sum of K doubles per thread; result valid in thread 0.
+// Block-wide sum of K doubles per thread over all warps; result valid in thread 0.
 template <int K>
 __device__ __forceinline__ void block_sum_d(double (&v)[K], double* red /* [K][32] */) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const double w = warp_sum_d(v[k]);
-    if (lane == 0) red[k * 32 + warp] = w;
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double w = (lane < nw) ? red[k * 32 + lane] : 0.0;
-      w = warp_sum_d(w);
-      v[k] = w;
-    }
-  }
+  gt::block_sum_d<K>(v, red, (int)(blockDim.x >> 5));
 }
 
 // ------------------------------------------------------------------ setup --
@@ -170,18 +125,6 @@ __global__ void __launch_bounds__(kThreads) ncc_moments_kernel(const float* __re
     double* o = partials + (img * gridDim.x + blockIdx.x) * 3;
     o[0] = v[0]; o[1] = v[1]; o[2] = v[2];
   }
-}
-
-__device__ __forceinline__ double ncc_sim_from_moments(double sm, double smm, double smf, double n,
-                                                       const FixedNCC& fx) {
-  const double mean = sm / n;
-  double var = (smm - n * mean * mean) / (n - 1.0);
-  if (var < 0.0) var = 0.0;
-  double sd = sqrt(var);
-  if (sd < 1.0e-6) sd = 1.0e-6;
-  const double cov = smf - mean * fx.sum_fhat;
-  const double ncc = cov / (n * fx.sd * sd);
-  return (1.0 - ncc) * 0.5;
 }
 
 // One block per image (as grad_finalize_kernel).
@@ -292,16 +235,10 @@ __global__ void __launch_bounds__(kThreads) grad_images_kernel(const float* __re
   }
 }
 
-// Moments of the moving gradients over a 32 x 64-pixel tile per block: each
-// thread owns one column and eight consecutive rows, so the Sobel stencil slides
-// down the column (three shared-memory reads per pixel) and the block reduction
-// is paid once per 2048 pixels.  Sums are plain float per thread (8 terms) and
-// per warp (256 pixels), then float-float across warps and blocks, which keeps
-// the long image-wide sums accurate.  Gradients use the same expressions as
-// GradTile::sobel (identical values).
-constexpr int kGW = 32;                           // tile columns = threads across
-constexpr int kGR = 8;                            // rows per thread
-constexpr int kGH = kGR * (kThreads / kGW);       // tile rows (64)
+// Moments of the moving gradients, one 32 x 64-pixel tile per block
+// (gt::grad_tile_moments, shared with the fused evaluation kernel).
+using gt::kGH;
+using gt::kGW;
 
 template <int KR>
 __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __restrict__ imgs, int rows, int cols,
@@ -309,102 +246,12 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
                                                                 const float* __restrict__ fhy,
                                                                 const uint8_t* __restrict__ mask,
                                                                 double* __restrict__ partials) {
-  constexpr int H = KR + 1;                       // halo: blur radius + Sobel
-  constexpr int WI = kGW + 2 * H, HI = kGH + 2 * H;
-  constexpr int WB = kGW + 2, HB = kGH + 2;       // blurred region (Sobel halo)
-  __shared__ float s_in[HI][WI + 1];
-  __shared__ float s_hb[KR > 0 ? HI : 1][WB + 1];
-  __shared__ float s_bl[HB][WB + 1];
-  __shared__ FF red[6 * 32];
-  const int tx = threadIdx.x % kGW, ty = threadIdx.x / kGW;
+  __shared__ gt::GradTileSmem<KR> sm;
   const int tiles_x = (cols + kGW - 1) / kGW;
   const int y0 = (blockIdx.x / tiles_x) * kGH, x0 = (blockIdx.x % tiles_x) * kGW;
-  const int64_t npix = (int64_t)rows * cols;
   const int64_t img = blockIdx.y;
-  const float* src = imgs + img * npix;
-  // stage the tile and its halo; reflect-101 only for tiles touching a border
-  // (rows / cols past the last tile pixel only feed pixels that are skipped)
-  // (flat loops over each region: its width is not a multiple of the warp, and
-  // the divisions by the constant widths are multiply-shifts)
-  const bool interior = y0 >= H && x0 >= H && y0 + kGH + H <= rows && x0 + kGW + H <= cols;
-  for (int i = threadIdx.x; i < HI * WI; i += kThreads) {
-    const int r = i / WI, c = i - r * WI;
-    int gr = y0 - H + r, gc = x0 - H + c;
-    if (!interior) {
-      gr = reflect101(min(gr, rows - 1 + H), rows);
-      gc = reflect101(min(gc, cols - 1 + H), cols);
-    }
-    s_in[r][c] = src[(int64_t)gr * cols + gc];
-  }
-  __syncthreads();
-  if constexpr (KR == 0) {
-    for (int i = threadIdx.x; i < HB * WB; i += kThreads) {
-      const int r = i / WB, c = i - r * WB;
-      s_bl[r][c] = s_in[r][c];
-    }
-  } else {
-    for (int i = threadIdx.x; i < HI * WB; i += kThreads) {
-      const int r = i / WB, c = i - r * WB;
-      const float* q = &s_in[r][c];
-      s_hb[r][c] = (KR == 2) ? (0.0625f * q[0] + 0.25f * q[1] + 0.375f * q[2] + 0.25f * q[3] + 0.0625f * q[4])
-                             : (0.25f * q[0] + 0.5f * q[1] + 0.25f * q[2]);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < HB * WB; i += kThreads) {
-      const int r = i / WB, c = i - r * WB;
-      s_bl[r][c] = (KR == 2) ? (0.0625f * s_hb[r][c] + 0.25f * s_hb[r + 1][c] + 0.375f * s_hb[r + 2][c] +
-                                0.25f * s_hb[r + 3][c] + 0.0625f * s_hb[r + 4][c])
-                             : (0.25f * s_hb[r][c] + 0.5f * s_hb[r + 1][c] + 0.25f * s_hb[r + 2][c]);
-    }
-  }
-  __syncthreads();
-  float m[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-  const int gxc = x0 + tx;
-  if (gxc < cols) {
-    const int rb = ty * kGR;  // first output row (tile-local); blurred rows rb .. rb + kGR + 1
-    float a0 = s_bl[rb][tx], b0 = s_bl[rb][tx + 1], c0 = s_bl[rb][tx + 2];
-    float a1 = s_bl[rb + 1][tx], b1 = s_bl[rb + 1][tx + 1], c1 = s_bl[rb + 1][tx + 2];
-#pragma unroll
-    for (int k = 0; k < kGR; ++k) {
-      const float a2 = s_bl[rb + k + 2][tx], b2 = s_bl[rb + k + 2][tx + 1], c2 = s_bl[rb + k + 2][tx + 2];
-      const int gyr = y0 + rb + k;
-      if (gyr < rows) {
-        const int64_t pix = (int64_t)gyr * cols + gxc;
-        if (!mask || mask[pix]) {
-          // GradTile::sobel with a = a0, b = b0, cc = c0, d = a1, f = c1, g = a2, h = b2, ii = c2
-          const float gx = ((c0 - a0) + 2.0f * (c1 - a1)) + (c2 - a2);
-          const float gy = ((a2 - a0) + 2.0f * (b2 - b0)) + (c2 - c0);
-          m[0] += gx;
-          m[1] += gx * gx;
-          m[2] += gx * fhx[pix];
-          m[3] += gy;
-          m[4] += gy * gy;
-          m[5] += gy * fhy[pix];
-        }
-      }
-      a0 = a1; b0 = b1; c0 = c1;
-      a1 = a2; b1 = b2; c1 = c2;
-    }
-  }
-  // plain-float sums within a warp (256 pixels), float-float across the warps
-  // and the blocks
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    float w = m[k];
-    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-    if (lane == 0) red[k * 32 + warp] = FF{w, 0.0f};
-  }
-  __syncthreads();
   double v[6];
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      FF w = (lane < kThreads / 32) ? red[k * 32 + lane] : FF{0.0f, 0.0f};
-      for (int o = 16; o > 0; o >>= 1) w = ff_add(w, ff_shfl_down(w, o));
-      v[k] = (double)w.hi + (double)w.lo;
-    }
-  }
+  gt::grad_tile_moments<KR, false>(imgs + img * (int64_t)rows * cols, rows, cols, y0, x0, fhx, fhy, mask, sm, v);
   if (threadIdx.x == 0) {
     double* o = partials + (img * gridDim.x + blockIdx.x) * 6;
 #pragma unroll
@@ -412,22 +259,14 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
   }
 }
 
-// One block per image: the block partials summed by all threads in double,
-// then across the block.
+// One block of 128 threads per image: the tile partials combined in double
+// (gt::grad_finalize_image, shared with the fused evaluation kernel).
 __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double n,
                                      FixedNCC fx, FixedNCC fy, float* __restrict__ sims) {
   __shared__ double red[6 * 32];
   const int64_t img = blockIdx.x;
-  double a[6] = {0, 0, 0, 0, 0, 0};
-  const double* p = partials + img * nblk * 6;
-  for (int k = threadIdx.x; k < nblk; k += blockDim.x)
-    for (int j = 0; j < 6; ++j) a[j] += p[6 * k + j];
-  block_sum_d<6>(a, red);
-  if (threadIdx.x != 0) return;
-  const double sx = ncc_sim_from_moments(a[0], a[1], a[2], n, fx);
-  const double sy = ncc_sim_from_moments(a[3], a[4], a[5], n, fy);
-  // 0.5 * (float(s_x) + float(s_y)) as in ImgSimMetric2DGradNCCCPU::compute
-  sims[img] = 0.5f * ((float)sx + (float)sy);
+  const float v = gt::grad_finalize_image<false>(partials + img * nblk * 6, nblk, n, fx, fy, red);
+  if (threadIdx.x == 0) sims[img] = v;
 }
 
 // ------------------------------------------------------------ patch NCC ---
@@ -884,9 +723,7 @@ struct ViewPtrs {
 __global__ void combine_mean_kernel(ViewPtrs vp, int nviews, int64_t pop, float* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= pop) return;
-  float s = 0.0f;
-  for (int v = 0; v < nviews; ++v) s += vp.p[v][i];
-  out[i] = s / (float)nviews;
+  out[i] = gt::combine_mean(vp.p, nviews, i, false);
 }
 
 template <typename K>
