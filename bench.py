@@ -55,6 +55,8 @@ def _args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--voxel", default="f32", choices=["f32", "f16", "bf16"])
+    p.add_argument("--path", default="fused", choices=["fused", "split"],
+                   help="evaluation path timed as the headline (the other is timed beside it)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true")
     p.add_argument("--only", default="", choices=["", "plain-small", "precision", "multi-job", "serving"],
@@ -357,6 +359,7 @@ def run_ours(a, rank, world, local):
     m = xr.ImgSimMetric2DGradNCCCUDA(dev)
     m.set_fixed_image(fixed)
     obj = xr.PopulationObjective(rc, [m], POP)
+    obj.set_fused(a.path == "fused")
 
     nsteps = a.warmup + a.steps
     pops = _populations(w, nsteps, 1234 + rank)
@@ -393,6 +396,29 @@ def run_ours(a, rank, world, local):
     ms = [s.elapsed_time(e) for s, e in evs]
     t_total = _max_over_ranks(sum(ms) / 1e3, world)
     value = world * a.steps * POP / t_total
+
+    # ---- the other evaluation path on the same populations, for comparison
+    other = "split" if a.path == "fused" else "fused"
+    obj.set_fused(other == "fused")
+    d_other = torch.empty((a.steps, POP), dtype=torch.float32, device=f"cuda:{dev}")
+    with torch.cuda.stream(stream):
+        for k in range(3):
+            obj.eval_device(POP, d_pops[k].data_ptr(), d_other[0].data_ptr())
+    oev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(a.steps):
+            flush.fill_(float(i))
+            oev[i][0].record(stream)
+            obj.eval_device(POP, d_pops[a.warmup + i].data_ptr(), d_other[i].data_ptr())
+            oev[i][1].record(stream)
+    torch.cuda.synchronize()
+    t_other = sum(s0.elapsed_time(e0) for s0, e0 in oev) / 1e3
+    paths = {a.path: round(a.steps * POP / (t_total / world), 2), other: round(a.steps * POP / t_other, 2),
+             "values_identical": bool(torch.equal(d_other, d_sims[a.warmup:])),
+             "fused": "one persistent kernel: DRR tiles, then each image's grad-NCC tile by tile behind them "
+                      "(+ one geometry launch)",
+             "split": "DRR launch, then grad-NCC moment and combine launches, replayed as a CUDA graph"}
+    obj.set_fused(a.path == "fused")
 
     # ---- e2e through the C ABI with host buffers (pinned poses in, sims out)
     h_pops = torch.empty((a.steps, POP, 16), dtype=torch.float64, pin_memory=True)
@@ -447,7 +473,8 @@ def run_ours(a, rank, world, local):
                        parallelism=f"replicas x{world}"),
         "e2e": {"value": round(e2e, 2), "unit": "poses/s", "h2d_bytes_per_step": POP * 16 * 8,
                 "d2h_bytes_per_step": POP * 4},
-        "gpu_launches": a.steps * 5,
+        "gpu_launches": a.steps * (2 if a.path == "fused" else 5),
+        "evaluation_paths_poses_per_s": paths,
         "roofline": roofline,
         "clocks": clk.summary(t_clk0, t_clk1 + 0.06),
     }

@@ -158,6 +158,7 @@ _SIGS = {
     "xr_obj_destroy": [H],
     "xr_obj_eval": [H, i64, P, P],
     "xr_obj_eval_device": [H, i64, P, P],
+    "xr_obj_set_fused": [H, i32],
     "xr_grad_ncc_noalloc": [P, P, i64, i64, i64, i32, P, P],
     "xr_cmaes_create": [i32, P, P, i32, u64, C.POINTER(H)],
     "xr_cmaes_destroy": [H],
@@ -188,6 +189,8 @@ _SIGS = {
     "xr_jobset_eval": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
     "xr_jobset_eval_device": [H, i32, C.POINTER(H), C.POINTER(i64), C.POINTER(P), C.POINTER(P)],
     "xr_jobset_last_launch": [H, C.POINTER(i64), C.POINTER(i32)],
+    "xr_jobset_set_fused": [H, i32],
+    "xr_jobset_last_kernel_launches": [H, C.POINTER(i32)],
     "xr_regi_pose_map": [C.c_void_p, C.c_void_p, i64, C.c_void_p, C.c_void_p],
     "xr_regi_jobset_step": [H, i32, C.POINTER(xr_regi_step_job), C.POINTER(i32), C.POINTER(i32)],
     "xr_cmaes_lambda": [H, C.POINTER(i32)],

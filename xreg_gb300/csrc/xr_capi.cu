@@ -259,6 +259,16 @@ struct xr_simmetric_s {
   }
 };
 
+// Device descriptors and work counter of a fused evaluation step (see
+// fused_enqueue), owned by each objective and job set.
+struct FusedWork {
+  DevBuf d_desc, d_counter;
+  std::vector<unsigned char> h_desc;  // staging: pageable, consumed by the copy call itself
+  int blocks = 0;
+  long long items = 0;
+  int launches = 0;                   // kernel launches of the last step
+};
+
 struct xr_objective_s {
   xr_raycaster rc = nullptr;
   uint64_t rc_id = 0;
@@ -274,6 +284,12 @@ struct xr_objective_s {
   int64_t max_pop = 0;
   uint64_t id = 0;
   DevBuf d_poses, d_sims;
+  // fused evaluation: mode (1 fused, 0 split DRR and metric launches), its
+  // counters (zero between launches) and descriptors
+  int32_t fused = 1;
+  DevBuf d_fcnt;
+  size_t fcnt_words = 0;
+  FusedWork fw;
   // captured launch sequence
   cudaGraphExec_t graph_exec = nullptr;
   int64_t graph_pop = -1;
@@ -973,8 +989,6 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
 
 static xr_status rc_distribute_device_on(xr_raycaster rc, int64_t n, const double* d_xf, cudaStream_t s);
 
-// Uploads dirty host state, enqueues the geometry kernel on stream s and fills
-// the DRR launch parameters (without choosing a launch configuration).
 // The device buffer a caster's images go to: its own, or the one of the caster
 // given to use_other_proj_buf while that one is alive; *cap = images it holds.
 static float* rc_out(xr_raycaster rc, int64_t* cap) {
@@ -987,7 +1001,10 @@ static float* rc_out(xr_raycaster rc, int64_t* cap) {
   return rc->d_proj.as<float>();
 }
 
-static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, DrrParams& p) {
+// Fills the DRR launch parameters of a compute on stream s (uploading dirty host
+// state); with `geometry` false the per-projection set-up is left to the caller
+// (one launch for many ray casters, see rc_geom_job).
+static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, DrrParams& p, bool geometry = true) {
   XR_CHECK_ARG(rc, "compute: NULL handle");
   if (!rc->allocated) return fail(XR_ERR_NOT_ALLOCATED, "compute: allocate_resources has not been called");
   if (rc->interp != XR_INTERP_LINEAR)
@@ -1012,8 +1029,9 @@ static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, Dr
     rc->xforms_dirty = false;
   }
   const auto& vol = *rc->vols[(size_t)vol_idx];
-  XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
-                               rc->d_cam_idx.as<int32_t>(), n, rc->pose_count, rc->d_geo.as<ProjGeom>(), s));
+  if (geometry)
+    XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
+                                 rc->d_cam_idx.as<int32_t>(), n, rc->pose_count, rc->d_geo.as<ProjGeom>(), s));
   p = DrrParams{};
   p.vol.voxels = vol.voxels.p;
   p.vol.cells = vol.cells.p;
@@ -2016,6 +2034,201 @@ extern "C" XR_API xr_status xr_obj_destroy(xr_objective obj) {
   return XR_OK;
 }
 
+// ======================================================= fused evaluation
+// Whether an objective's metric can run inside the fused evaluation kernel:
+// every view grad-NCC with the default 5x5 smoothing, reading its images from
+// the objective's ray caster.
+static bool obj_metric_fusable(xr_objective obj) {
+  for (xr_simmetric m : obj->metrics) {
+    if (m->kind != XR_SIM_GRAD_NCC || m->smooth_ksize != 5 || !m->allocated) return false;
+    if (m->rows != obj->rc->rows() || m->cols != obj->rc->cols()) return false;
+  }
+  return true;
+}
+
+static size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
+
+// One evaluation step of n objectives, fused: per job the poses are copied in,
+// then ONE geometry launch covers every job's projections and ONE persistent
+// launch per (voxel type, layout) group traces every DRR tile and computes the
+// grad-NCC of each image behind it (eval_fused_kernel); objectives whose
+// metrics cannot run fused get their metric launches afterwards.  Values are
+// copied to sims[i].  Everything is ordered on stream s.
+static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_objective* objs, const int64_t* pops,
+                               const double* const* xforms, bool host_in, float* const* sims, bool host_out,
+                               cudaStream_t s) {
+  XR_CHECK_ARG(objs && pops && xforms && sims && n > 0, "evaluation: NULL argument or no jobs");
+  std::vector<GeomJob> gj;
+  std::vector<FusedJob> fj;
+  std::vector<std::vector<FusedView>> fv((size_t)n);
+  std::vector<int32_t> key;
+  int64_t first = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    xr_objective obj = objs[i];
+    XR_CHECK_ARG(obj && reg_contains(obj), "evaluation: unknown or destroyed objective");
+    XR_CHECK_ARG(obj->peers_alive(), "evaluation: a ray caster or metric of an objective was destroyed");
+    XR_CHECK_ARG(obj->rc->device == device, "evaluation: objective lives on another device");
+    for (int32_t k = 0; k < i; ++k) XR_CHECK_ARG(objs[k] != obj, "evaluation: an objective is listed twice");
+    const int64_t pop = pops[i];
+    XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "evaluation: population outside [1, max_pop]");
+    XR_CHECK_ARG(xforms[i] && sims[i], "evaluation: NULL pose or value pointer");
+    if (host_in) XR_CHECK_ARG(finite_all(xforms[i], 16 * pop), "evaluation: non-finite transform");
+    if (xforms[i] != obj->d_poses.as<double>())
+      XR_CUDA_TRY(cudaMemcpyAsync(obj->d_poses.p, xforms[i], (size_t)pop * 16 * 8,
+                                  host_in ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    xr_raycaster rc = obj->rc;
+    const int32_t nv = (int32_t)obj->metrics.size();
+    xr_status st = xr_rc_set_num_projs(rc, (int64_t)nv * pop);
+    if (st != XR_OK) return st;
+    if ((st = rc_distribute_device_on(rc, pop, obj->d_poses.as<double>(), s)) != XR_OK) return st;
+    rc->store = XR_PROJ_STORE_REPLACE;  // use_proj_store_replace_method (xregIntensity2D3DRegi.cpp:598)
+    FusedJob J{};
+    if ((st = rc_prepare(rc, obj->vol_idx, s, J.d.p, false)) != XR_OK) return st;
+    XR_CHECK_ARG(J.d.p.kernel_id == XR_LINE_INT_SUM, "evaluation: the fused step uses the line-integral sum kernel");
+    const auto& vol = *rc->vols[(size_t)obj->vol_idx];
+    // float32 volumes read their cell copy with one 256-bit load, half volumes
+    // with one 128-bit load; BF16 cells run the packed four-sample loop
+    J.d.p.vol.layout = vol.cells.p ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
+    J.d.p.block_warps_x = 2;
+    J.d.p.unroll = (vol.type == XR_VOXEL_BF16 && vol.cells.p) ? 6 : 4;
+    J.d.tiles_x = (int32_t)((J.d.p.cols + 15) / 16);
+    J.d.tiles_y = (int32_t)((J.d.p.rows + 15) / 16);
+    rc->last_layout = J.d.p.vol.layout;
+    rc->last_bw = 2;
+    rc->last_unroll = J.d.p.unroll;
+    rc->last_warp_rows = 4;
+    GeomJob G{};
+    G.p2i = phys_to_idx_xform(vol.desc);
+    G.cams = rc->d_cams.as<xr_camera_desc>();
+    G.poses = rc->d_xforms.as<double>();
+    G.cam_idx = rc->d_cam_idx.as<int32_t>();
+    G.num_projs = rc->num_projs;
+    G.pose_stride = rc->pose_count;
+    G.first = first;
+    G.out = rc->d_geo.as<ProjGeom>();
+    first += rc->num_projs;
+    gj.push_back(G);
+    // the metric behind the DRR
+    const int rows = (int)rc->rows(), cols = (int)rc->cols();
+    J.nviews = nv;
+    J.pop = pop;
+    J.mt_x = (cols + 31) / 32;
+    J.mt_y = (rows + 63) / 64;
+    J.out = obj->d_sims.as<float>();
+    J.metric = (obj->fused && obj_metric_fusable(obj)) ? 1 : 0;
+    for (int32_t v = 0; v < nv; ++v) {
+      xr_simmetric m = obj->metrics[(size_t)v];
+      m->num_mov = pop;
+      m->rc = rc;
+      m->rc_id = rc->id;
+      m->proj_offset = (int64_t)v * pop;
+      if (J.metric) {
+        XR_CHECK_ARG(m->nblk == J.mt_x * J.mt_y && m->capacity >= pop, "evaluation: metric buffers do not fit");
+        FusedView V{};
+        V.fhx = m->fx.fhat;
+        V.fhy = m->fy.fhat;
+        V.mask = m->has_mask ? m->d_mask.as<uint8_t>() : nullptr;
+        V.fx = m->fx;
+        V.fy = m->fy;
+        V.n_used = (double)m->n_used;
+        V.partials = m->d_partials.as<double>();
+        V.sims = m->d_sims.as<float>();
+        fv[(size_t)i].push_back(V);
+      }
+    }
+    if (J.metric) {
+      const size_t words = (size_t)obj->max_pop * nv * (size_t)(J.mt_x * J.mt_y + 1) + (size_t)obj->max_pop;
+      if (obj->fcnt_words < words) {
+        XR_CUDA_TRY(obj->d_fcnt.reserve(words * 4));
+        XR_CUDA_TRY(cudaMemsetAsync(obj->d_fcnt.p, 0, words * 4, s));
+        obj->fcnt_words = words;
+      }
+      J.cnt = obj->d_fcnt.as<unsigned int>();
+    }
+    fj.push_back(J);
+    key.push_back((vol.type * 4 + J.d.p.vol.layout) * 8 + J.d.p.unroll);
+  }
+  // jobs ordered by group; item numbering restarts in each group
+  std::vector<int32_t> keys(key);
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  std::vector<int32_t> order;
+  std::vector<std::pair<size_t, size_t>> ranges;
+  std::vector<long long> group_items;
+  for (int32_t k : keys) {
+    const size_t b = order.size();
+    long long items = 0;
+    for (int32_t i = 0; i < n; ++i)
+      if (key[(size_t)i] == k) {
+        fj[(size_t)i].d.item_begin = items;
+        items += (long long)fj[(size_t)i].d.p.num_projs * fj[(size_t)i].d.tiles_x * fj[(size_t)i].d.tiles_y;
+        order.push_back(i);
+      }
+    ranges.emplace_back(b, order.size());
+    group_items.push_back(items);
+  }
+  // one descriptor upload: geometry jobs, fused jobs (group order), views
+  const size_t off_f = align16(gj.size() * sizeof(GeomJob));
+  const size_t off_v = off_f + align16(fj.size() * sizeof(FusedJob));
+  size_t nviews_total = 0;
+  for (auto& v : fv) nviews_total += v.size();
+  const size_t bytes = off_v + nviews_total * sizeof(FusedView) + 16;
+  XR_CUDA_TRY(fw.d_desc.reserve(bytes));
+  XR_CUDA_TRY(fw.d_counter.reserve(256));
+  fw.h_desc.assign(bytes, 0);
+  unsigned char* h = fw.h_desc.data();
+  unsigned char* d = fw.d_desc.as<unsigned char>();
+  std::memcpy(h, gj.data(), gj.size() * sizeof(GeomJob));
+  size_t vpos = 0;
+  for (size_t r = 0; r < order.size(); ++r) {
+    FusedJob J = fj[(size_t)order[r]];
+    const auto& views = fv[(size_t)order[r]];
+    J.views = views.empty() ? nullptr : reinterpret_cast<const FusedView*>(d + off_v + vpos * sizeof(FusedView));
+    if (!views.empty()) std::memcpy(h + off_v + vpos * sizeof(FusedView), views.data(), views.size() * sizeof(FusedView));
+    vpos += views.size();
+    std::memcpy(h + off_f + r * sizeof(FusedJob), &J, sizeof(FusedJob));
+  }
+  XR_CUDA_TRY(cudaMemcpyAsync(fw.d_desc.p, h, bytes, cudaMemcpyHostToDevice, s));
+  XR_CUDA_TRY(launch_proj_geom_jobs(reinterpret_cast<const GeomJob*>(d), (int)gj.size(), first, s));
+  fw.launches = 1;
+  fw.items = 0;
+  fw.blocks = 0;
+  for (size_t gi = 0; gi < ranges.size(); ++gi) {
+    const FusedJob& f0 = fj[(size_t)order[ranges[gi].first]];
+    int blocks = 0;
+    XR_CUDA_TRY(launch_eval_fused(reinterpret_cast<const FusedJob*>(d + off_f) + ranges[gi].first,
+                                  (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
+                                  f0.d.p.vol.voxel_type, f0.d.p.vol.layout, f0.d.p.unroll,
+                                  fw.d_counter.as<unsigned long long>(), &blocks, s));
+    fw.items += group_items[gi];
+    fw.blocks = std::max(fw.blocks, blocks);
+    ++fw.launches;
+  }
+  for (int32_t i = 0; i < n; ++i) {
+    xr_objective obj = objs[i];
+    xr_raycaster rc = obj->rc;
+    if (rc->ext_host)
+      XR_CUDA_TRY(cudaMemcpyAsync(rc->ext_host, rc_out(rc, nullptr),
+                                  (size_t)rc->num_projs * (size_t)(rc->rows() * rc->cols()) * 4,
+                                  cudaMemcpyDeviceToHost, s));
+    if (!fj[(size_t)i].metric) {
+      const int32_t nv = (int32_t)obj->metrics.size();
+      const float* view_sims[16];
+      for (int32_t v = 0; v < nv; ++v) {
+        xr_simmetric m = obj->metrics[(size_t)v];
+        xr_status st = sm_enqueue_compute_on(m, s);
+        if (st != XR_OK) return st;
+        view_sims[v] = m->d_sims.as<float>();
+      }
+      XR_CUDA_TRY(launch_combine_mean(view_sims, nv, pops[i], obj->d_sims.as<float>(), s));
+    }
+    if (sims[i] != obj->d_sims.as<float>())
+      XR_CUDA_TRY(cudaMemcpyAsync(sims[i], obj->d_sims.p, (size_t)pops[i] * 4,
+                                  host_out ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  }
+  return XR_OK;
+}
+
 // Enqueues the whole objective for obj->d_poses (pop poses) on the rc stream.
 static xr_status obj_enqueue(xr_objective obj, int64_t pop) {
   xr_raycaster rc = obj->rc;
@@ -2051,6 +2264,11 @@ static bool obj_graph_valid(xr_objective obj, int64_t pop) {
 static xr_status obj_run(xr_objective obj, int64_t pop) {
   xr_raycaster rc = obj->rc;
   cudaStream_t s = rc->stream();
+  if (obj->fused && obj_metric_fusable(obj)) {
+    const double* x = obj->d_poses.as<double>();
+    float* v = obj->d_sims.as<float>();
+    return fused_enqueue(obj->fw, rc->device, 1, &obj, &pop, &x, false, &v, false, s);
+  }
   // A metric that draws random patches on the host at every compute, or a copy
   // into an external host buffer, is run directly (a captured graph would replay
   // one draw; pageable copies cannot be captured).
@@ -2082,6 +2300,12 @@ static xr_status obj_run(xr_objective obj, int64_t pop) {
   obj->graph_stream = s;
   obj->graph_sm_gen.resize(obj->metrics.size());
   for (size_t v = 0; v < obj->metrics.size(); ++v) obj->graph_sm_gen[v] = obj->metrics[v]->generation;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_obj_set_fused(xr_objective obj, int32_t enable) {
+  XR_CHECK_ARG(obj, "xr_obj_set_fused: NULL handle");
+  obj->fused = enable ? 1 : 0;
   return XR_OK;
 }
 
@@ -2129,6 +2353,8 @@ struct xr_jobset_s {
   long long last_items = 0;
   unsigned int* h_err = nullptr;  // pinned: every job's step-guard flag, read with one synchronisation
   size_t h_err_cap = 0;
+  int32_t fused = 1;               // 1: fused evaluation step; 0: DRR launch, then metric launches per job
+  FusedWork fw;
   cudaStream_t stream() const { return has_ext ? ext_stream : own_stream; }
 };
 
@@ -2173,6 +2399,12 @@ static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* obj
   XR_CHECK_ARG(js && objs && pops && xforms && sims && n > 0, "xr_jobset_eval: NULL argument or no jobs");
   DeviceGuard g(js->device);
   cudaStream_t s = js->stream();
+  if (js->fused) {
+    xr_status st = fused_enqueue(js->fw, js->device, n, objs, pops, xforms, host_in, sims, host_out, s);
+    js->last_items = js->fw.items;
+    js->blocks = js->fw.blocks;
+    return st;
+  }
   js->h_jobs.clear();
   std::vector<int32_t> group;  // voxel type * 4 + layout of each job
   for (int32_t i = 0; i < n; ++i) {
@@ -2308,6 +2540,18 @@ extern "C" XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t n, const
                                                   const int64_t* pops, const double* const* d_xforms,
                                                   float* const* d_sims) {
   return jobset_enqueue(js, n, objs, pops, d_xforms, false, d_sims, false);
+}
+
+extern "C" XR_API xr_status xr_jobset_set_fused(xr_jobset js, int32_t enable) {
+  XR_CHECK_ARG(js, "xr_jobset_set_fused: NULL handle");
+  js->fused = enable ? 1 : 0;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_jobset_last_kernel_launches(xr_jobset js, int32_t* launches) {
+  XR_CHECK_ARG(js && launches, "xr_jobset_last_kernel_launches: NULL argument");
+  *launches = js->fused ? js->fw.launches : -1;
+  return XR_OK;
 }
 
 extern "C" XR_API xr_status xr_jobset_last_launch(xr_jobset js, int64_t* work_items, int32_t* blocks) {

@@ -29,6 +29,7 @@
 //           It spends 8x the voxel bytes of HBM to cut L1 requests per sample
 //           from 8 to 1-2; the linear kernel is bound by exactly those requests.
 #include "xr_internal.h"
+#include "xr_gradtile.cuh"
 
 #include <atomic>
 #include <cfloat>
@@ -685,6 +686,125 @@ drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long tota
   }
 }
 
+// Fused evaluation: the persistent multi-job DRR loop of drr_multi_kernel,
+// with each job's grad-NCC (5x5 smoothing) computed inside the same launch.
+// No block ever waits for another.  After a block writes a 16x16 DRR tile it
+// counts the tile towards every 32x64 metric tile whose input (the tile with
+// its 3-pixel blur + Sobel halo, clipped to the image) the tile overlaps; the
+// block whose count completes a metric tile computes that tile's moments at
+// once, reading the DRR pixels back through L2 (gt::grad_tile_moments, the
+// split path's own tile code); the block that completes an image's metric
+// tiles combines its partials in FP64 (gt::grad_finalize_image), and the block
+// that completes a pose's views writes the mean over views.  Counters are
+// zero between launches: whoever completes one resets it.  Stores are made
+// visible device-wide (fence) before each count; counted data is read through
+// L2 (ld.global.cg), never through the incoherent L1.
+constexpr int kFusedKR = 2;  // 5x5 smoothing, xReg's default
+using FusedSmem = gt::GradTileSmem<kFusedKR>;
+
+// Metric tiles the DRR tile [r0, r1) x [c0, c1) feeds, and how many DRR tiles
+// feed each; claims (into claim[]) those whose count this tile completes.
+__device__ __forceinline__ int fused_count_tile(const FusedJob& J, unsigned int* cnt_tile, int r0, int r1, int c0,
+                                                int c1, int* claim) {
+  constexpr int H = kFusedKR + 1;
+  const int rows = J.d.p.rows, cols = J.d.p.cols;
+  int n = 0;
+  const int my0 = max(0, (r0 - H) / gt::kGH - 1), my1 = min(J.mt_y - 1, (r1 - 1 + H) / gt::kGH);
+  const int mx0 = max(0, (c0 - H) / gt::kGW - 1), mx1 = min(J.mt_x - 1, (c1 - 1 + H) / gt::kGW);
+  for (int my = my0; my <= my1; ++my) {
+    const int er0 = max(0, my * gt::kGH - H), er1 = min(rows, my * gt::kGH + gt::kGH + H);
+    if (!(er0 < r1 && r0 < er1)) continue;
+    for (int mx = mx0; mx <= mx1; ++mx) {
+      const int ec0 = max(0, mx * gt::kGW - H), ec1 = min(cols, mx * gt::kGW + gt::kGW + H);
+      if (!(ec0 < c1 && c0 < ec1)) continue;
+      const unsigned int target = (unsigned int)(((er1 - 1) / 16 - er0 / 16 + 1) * ((ec1 - 1) / 16 - ec0 / 16 + 1));
+      unsigned int* c = cnt_tile + my * J.mt_x + mx;
+      if (atomicAdd(c, 1u) + 1u == target) {
+        *c = 0u;  // completed: zero for the next launch
+        claim[n++] = my * J.mt_x + mx;
+      }
+    }
+  }
+  return n;
+}
+
+template <int VT, int LAYOUT, int UNROLL>
+__global__ void __launch_bounds__(kThreads, UNROLL >= kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
+eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total, unsigned long long* counter) {
+  __shared__ long long s_item;
+  __shared__ FusedSmem gsm;
+  __shared__ int s_claim[8];
+  __shared__ int s_nclaim, s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= total) break;
+    int j = 0;
+    while (j + 1 < njobs && jobs[j + 1].d.item_begin <= item) ++j;
+    const FusedJob& J = jobs[j];
+    const DrrParams& P = J.d.p;
+    const long long local = item - J.d.item_begin;
+    const int64_t proj = (int64_t)(local % P.num_projs);
+    const int tile = (int)(local / P.num_projs);
+    const int ty = tile / J.d.tiles_x, tx = tile - ty * J.d.tiles_x;
+    const int col = tx * 16 + (warp & 1) * 8 + (lane & 7);
+    const int row = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
+    unsigned int nl;
+    if (col < P.cols && row < P.rows) trace_pixel<VT, XR_LINE_INT_SUM, LAYOUT, UNROLL>(P, proj, row, col, &nl);
+    if (!J.metric) continue;
+    __threadfence();  // this block's DRR pixels, visible device-wide before they are counted
+    __syncthreads();
+    const int rows = P.rows, cols = P.cols;
+    const int mt = J.mt_x * J.mt_y;
+    const int64_t nimg = (int64_t)J.nviews * J.pop;
+    if (threadIdx.x == 0)
+      s_nclaim = fused_count_tile(J, J.cnt + proj * mt, ty * 16, min(ty * 16 + 16, rows), tx * 16,
+                                  min(tx * 16 + 16, cols), s_claim);
+    __syncthreads();
+    const int nclaim = s_nclaim;
+    const int64_t v = proj / J.pop, k = proj - v * J.pop;
+    const FusedView& V = J.views[v];
+    for (int c = 0; c < nclaim; ++c) {
+      __threadfence();
+      const int M = s_claim[c];
+      double vals[6];
+      gt::grad_tile_moments<kFusedKR, true>(P.out + proj * (int64_t)rows * cols, rows, cols, (M / J.mt_x) * gt::kGH,
+                                            (M % J.mt_x) * gt::kGW, V.fhx, V.fhy, V.mask, gsm, vals);
+      if (threadIdx.x == 0) {
+        double* o = V.partials + (k * mt + M) * 6;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) o[q] = vals[q];
+        __threadfence();
+        unsigned int* ci = J.cnt + nimg * mt + proj;
+        s_last = atomicAdd(ci, 1u) + 1u == (unsigned int)mt;
+        if (s_last) *ci = 0u;
+      }
+      __syncthreads();
+      if (s_last) {  // every tile of this image is in: its FP64 combine
+        __threadfence();
+        const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy,
+                                                        reinterpret_cast<double*>(gsm.red));
+        if (threadIdx.x == 0) {
+          V.sims[k] = sim;
+          __threadfence();
+          unsigned int* cp = J.cnt + nimg * mt + nimg + k;
+          if (atomicAdd(cp, 1u) + 1u == (unsigned int)J.nviews) {  // every view of this pose
+            *cp = 0u;
+            __threadfence();
+            float sum = 0.0f;
+            for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
+            J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 constexpr int kMaxDevices = 64;
 
 template <int VT, int LAYOUT, int UNROLL>
@@ -712,6 +832,34 @@ cudaError_t launch_multi_t(const MultiJobDrr* d_jobs, int njobs, long long total
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   drr_multi_kernel<VT, LAYOUT, UNROLL><<<blocks, kThreads, 0, s>>>(d_jobs, njobs, total, d_counter);
+  return cudaGetLastError();
+}
+
+template <int VT, int LAYOUT, int UNROLL>
+cudaError_t launch_fused_t(const FusedJob* d_jobs, int njobs, long long total, unsigned long long* d_counter,
+                           int* blocks_out, cudaStream_t s) {
+  static std::atomic<int> cached[kMaxDevices];  // blocks per device; zero = not known yet
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  int blocks = cached[dev].load(std::memory_order_relaxed);
+  if (!blocks) {
+    // the metric tile's shared memory is small: keep the rest of the SM's
+    // unified L1 for the DRR gathers
+    const int pct = 25;
+    cudaError_t e = cudaFuncSetAttribute(eval_fused_kernel<VT, LAYOUT, UNROLL>,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_fused_kernel<VT, LAYOUT, UNROLL>, kThreads, 0);
+    if (e != cudaSuccess) return e;
+    blocks = sms * (per_sm > 0 ? per_sm : 1);
+    cached[dev].store(blocks, std::memory_order_relaxed);
+  }
+  *blocks_out = blocks;
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  eval_fused_kernel<VT, LAYOUT, UNROLL><<<blocks, kThreads, 0, s>>>(d_jobs, njobs, total, d_counter);
   return cudaGetLastError();
 }
 
@@ -922,6 +1070,35 @@ cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long tot
       return launch_multi_unroll<XR_VOXEL_BF16, XR_LAYOUT_LINEAR>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
     case XR_VOXEL_BF16 * 4 + XR_LAYOUT_CELL8:
       return launch_multi_unroll<XR_VOXEL_BF16, XR_LAYOUT_CELL8>(d_jobs, njobs, total_items, d_counter, unroll, blocks_out, s);
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_eval_fused(const FusedJob* d_jobs, int njobs, long long total, int32_t voxel_type, int32_t layout,
+                              int32_t unroll, unsigned long long* d_counter, int* blocks_out, cudaStream_t s) {
+  *blocks_out = 0;
+  if (total <= 0) return cudaSuccess;
+  const bool packed = unroll == kUnrollPacked;
+  switch (voxel_type * 4 + layout) {
+    case XR_VOXEL_F32 * 4 + XR_LAYOUT_LINEAR:
+      return launch_fused_t<XR_VOXEL_F32, XR_LAYOUT_LINEAR, kUnrollTrim4>(d_jobs, njobs, total, d_counter, blocks_out, s);
+    case XR_VOXEL_F32 * 4 + kLayoutCell8Wide:
+      return packed ? launch_fused_t<XR_VOXEL_F32, kLayoutCell8Wide, kUnrollPacked>(d_jobs, njobs, total, d_counter,
+                                                                                   blocks_out, s)
+                    : launch_fused_t<XR_VOXEL_F32, kLayoutCell8Wide, kUnrollTrim4>(d_jobs, njobs, total, d_counter,
+                                                                                  blocks_out, s);
+    case XR_VOXEL_F16 * 4 + XR_LAYOUT_LINEAR:
+      return launch_fused_t<XR_VOXEL_F16, XR_LAYOUT_LINEAR, kUnrollTrim4>(d_jobs, njobs, total, d_counter, blocks_out, s);
+    case XR_VOXEL_F16 * 4 + XR_LAYOUT_CELL8:
+      return launch_fused_t<XR_VOXEL_F16, XR_LAYOUT_CELL8, kUnrollTrim4>(d_jobs, njobs, total, d_counter, blocks_out, s);
+    case XR_VOXEL_BF16 * 4 + XR_LAYOUT_LINEAR:
+      return launch_fused_t<XR_VOXEL_BF16, XR_LAYOUT_LINEAR, kUnrollTrim4>(d_jobs, njobs, total, d_counter, blocks_out, s);
+    case XR_VOXEL_BF16 * 4 + XR_LAYOUT_CELL8:
+      return packed ? launch_fused_t<XR_VOXEL_BF16, XR_LAYOUT_CELL8, kUnrollPacked>(d_jobs, njobs, total, d_counter,
+                                                                                   blocks_out, s)
+                    : launch_fused_t<XR_VOXEL_BF16, XR_LAYOUT_CELL8, kUnrollTrim4>(d_jobs, njobs, total, d_counter,
+                                                                                  blocks_out, s);
     default:
       return cudaErrorInvalidValue;
   }
