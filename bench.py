@@ -415,9 +415,9 @@ def run_ours(a, rank, world, local):
     t_other = sum(s0.elapsed_time(e0) for s0, e0 in oev) / 1e3
     paths = {a.path: round(a.steps * POP / (t_total / world), 2), other: round(a.steps * POP / t_other, 2),
              "values_identical": bool(torch.equal(d_other, d_sims[a.warmup:])),
-             "fused": "one persistent kernel: DRR tiles, then each image's grad-NCC tile by tile behind them "
-                      "(+ one geometry launch)",
-             "split": "DRR launch, then grad-NCC moment and combine launches, replayed as a CUDA graph"}
+             "fused_path": "one persistent kernel: DRR tiles, then each image's grad-NCC tile by tile behind "
+                           "them (+ one geometry launch)",
+             "split_path": "DRR launch, then grad-NCC moment and combine launches, replayed as a CUDA graph"}
     obj.set_fused(a.path == "fused")
 
     # ---- e2e through the C ABI with host buffers (pinned poses in, sims out)

@@ -44,7 +44,7 @@ def _stale(target: Path, deps) -> bool:
 def build(verbose: bool = False, force: bool = False) -> Path:
     nvcc = nvcc_path()
     BUILD_DIR.mkdir(exist_ok=True)
-    headers = [*sorted((REPO_DIR / "include").glob("*.h")), *sorted(CSRC.glob("*.h"))]
+    headers = [*sorted((REPO_DIR / "include").glob("*.h")), *sorted(CSRC.glob("*.h")), *sorted(CSRC.glob("*.cuh"))]
     objs = []
     jobs = []
     for src in SOURCES:

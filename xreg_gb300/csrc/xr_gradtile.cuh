@@ -54,6 +54,32 @@ __device__ __forceinline__ FF ff_shfl_down(FF v, int o) {
   return FF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
 }
 
+// Blur and Sobel arithmetic with every rounding explicit (no contraction), so
+// the shared-memory and the register forms of the tile give the same bits.
+__device__ __forceinline__ float blur5(float a, float b, float c, float d, float e) {
+  return __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(0.0625f, a), __fmul_rn(0.25f, b)), __fmul_rn(0.375f, c)),
+                             __fmul_rn(0.25f, d)),
+                   __fmul_rn(0.0625f, e));
+}
+__device__ __forceinline__ float blur3(float a, float b, float c) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(0.25f, a), __fmul_rn(0.5f, b)), __fmul_rn(0.25f, c));
+}
+// Sobel at the centre of the blurred 3x3 neighbourhood a0 b0 c0 / a1 . c1 / a2 b2 c2
+__device__ __forceinline__ void sobel3(float a0, float b0, float c0, float a1, float c1, float a2, float b2, float c2,
+                                       float& gx, float& gy) {
+  gx = __fadd_rn(__fadd_rn(__fsub_rn(c0, a0), __fmul_rn(2.0f, __fsub_rn(c1, a1))), __fsub_rn(c2, a2));
+  gy = __fadd_rn(__fadd_rn(__fsub_rn(a2, a0), __fmul_rn(2.0f, __fsub_rn(b2, b0))), __fsub_rn(c2, c0));
+}
+// One pixel's contribution to the six moments.
+__device__ __forceinline__ void moments_add(float (&m)[6], float gx, float gy, float fx, float fy) {
+  m[0] = __fadd_rn(m[0], gx);
+  m[1] = __fmaf_rn(gx, gx, m[1]);
+  m[2] = __fmaf_rn(gx, fx, m[2]);
+  m[3] = __fadd_rn(m[3], gy);
+  m[4] = __fmaf_rn(gy, gy, m[4]);
+  m[5] = __fmaf_rn(gy, fy, m[5]);
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
@@ -100,8 +126,32 @@ struct GradTileSmem {
   static constexpr int WI = kGW + 2 * H, HI = kGH + 2 * H;
   static constexpr int WB = kGW + 2, HB = kGH + 2;
   float hb[HI][WB + 1];
-  FF red[6 * 32];
+  FF red[6 * (kThreads / 32)];
 };
+
+// The tile's six moments from every thread's partial sums: plain float within
+// a warp (256 pixels), float-float across the warps (red: [6][8]); v valid in
+// thread 0.
+__device__ __forceinline__ void tile_moments_reduce(const float (&m)[6], FF* red, double (&v)[6]) {
+  constexpr int kWarps = kThreads / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    float w = m[k];
+    for (int o = 16; o > 0; o >>= 1) w = __fadd_rn(w, __shfl_down_sync(0xffffffffu, w, o));
+    if (lane == 0) red[k * kWarps + warp] = FF{w, 0.0f};
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      FF w = (lane < kWarps) ? red[k * kWarps + lane] : FF{0.0f, 0.0f};
+      for (int o = 16; o > 0; o >>= 1) w = ff_add(w, ff_shfl_down(w, o));
+      v[k] = (double)w.hi + (double)w.lo;
+    }
+  }
+  __syncthreads();  // red (and the tile's shared memory) is reused by the caller's next tile
+}
 
 // Image pixel (row, col) of a tile's input; CG reads through L2 only (pixels
 // written earlier in the same kernel by other blocks).
@@ -143,9 +193,8 @@ __device__ void grad_tile_moments(const float* __restrict__ src, int rows, int c
     // horizontal pass over all input rows, blurred columns [x0-1, x0+kGW+1)
     for (int i = threadIdx.x; i < HI * WB; i += kThreads) {
       const int r = i / WB, c = i - r * WB;
-      sm.hb[r][c] = (KR == 2) ? (0.0625f * in(r, c) + 0.25f * in(r, c + 1) + 0.375f * in(r, c + 2) +
-                                 0.25f * in(r, c + 3) + 0.0625f * in(r, c + 4))
-                              : (0.25f * in(r, c) + 0.5f * in(r, c + 1) + 0.25f * in(r, c + 2));
+      sm.hb[r][c] = (KR == 2) ? blur5(in(r, c), in(r, c + 1), in(r, c + 2), in(r, c + 3), in(r, c + 4))
+                              : blur3(in(r, c), in(r, c + 1), in(r, c + 2));
     }
     __syncthreads();
     // vertical pass in place: WB columns x 4 chunks of rows, every output of a
@@ -158,9 +207,8 @@ __device__ void grad_tile_moments(const float* __restrict__ src, int rows, int c
       for (int k = 0; k < kCh; ++k) {
         const int r = j * kCh + k;
         if (r < HB)
-          o[k] = (KR == 2) ? (0.0625f * sm.hb[r][c] + 0.25f * sm.hb[r + 1][c] + 0.375f * sm.hb[r + 2][c] +
-                              0.25f * sm.hb[r + 3][c] + 0.0625f * sm.hb[r + 4][c])
-                           : (0.25f * sm.hb[r][c] + 0.5f * sm.hb[r + 1][c] + 0.25f * sm.hb[r + 2][c]);
+          o[k] = (KR == 2) ? blur5(sm.hb[r][c], sm.hb[r + 1][c], sm.hb[r + 2][c], sm.hb[r + 3][c], sm.hb[r + 4][c])
+                           : blur3(sm.hb[r][c], sm.hb[r + 1][c], sm.hb[r + 2][c]);
       }
     }
     __syncthreads();
@@ -187,39 +235,75 @@ __device__ void grad_tile_moments(const float* __restrict__ src, int rows, int c
       if (gyr < rows) {
         const int64_t pix = (int64_t)gyr * cols + gxc;
         if (!mask || mask[pix]) {
-          // Sobel at (r, c) from the blurred 3x3 neighbourhood a0 b0 c0 / a1 . c1 / a2 b2 c2
-          const float gx = ((c0 - a0) + 2.0f * (c1 - a1)) + (c2 - a2);
-          const float gy = ((a2 - a0) + 2.0f * (b2 - b0)) + (c2 - c0);
-          m[0] += gx;
-          m[1] += gx * gx;
-          m[2] += gx * fhx[pix];
-          m[3] += gy;
-          m[4] += gy * gy;
-          m[5] += gy * fhy[pix];
+          float gx, gy;
+          sobel3(a0, b0, c0, a1, c1, a2, b2, c2, gx, gy);
+          moments_add(m, gx, gy, fhx[pix], fhy[pix]);
         }
       }
       a0 = a1; b0 = b1; c0 = c1;
       a1 = a2; b1 = b2; c1 = c2;
     }
   }
-  // plain-float sums within a warp (256 pixels), float-float across the warps
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  tile_moments_reduce(m, sm.red, v);
+}
+
+// The same moments with the 5x5 blur (KR = 2) computed in registers, without
+// the tile's shared-memory rows: each thread streams down its rows (plus the
+// halo), keeping the last five horizontally blurred rows and the last three
+// blurred rows of the three columns its Sobel stencil reads; reads go through
+// L2 only.  Every value comes from the same operations as in
+// grad_tile_moments, so the moments are identical bit for bit; red: [6][8].
+__device__ inline void grad_tile_moments_regs5(const float* __restrict__ src, int rows, int cols, int y0, int x0,
+                                               const float* __restrict__ fhx, const float* __restrict__ fhy,
+                                               const uint8_t* __restrict__ mask, FF* red, double (&v)[6]) {
+  constexpr int H = 3;
+  const int tx = threadIdx.x % kGW, ty = threadIdx.x / kGW;
+  const bool interior = y0 >= H && x0 >= H && y0 + kGH + H <= rows && x0 + kGW + H <= cols;
+  auto in = [&](int r, int c) -> float {  // tile input coordinates, as grad_tile_moments
+    int gr = y0 - H + r, gc = x0 - H + c;
+    if (!interior) {
+      gr = reflect101(min(gr, rows - 1 + H), rows);
+      gc = reflect101(min(gc, cols - 1 + H), cols);
+    }
+    return __ldcg(src + (int64_t)gr * cols + gc);
+  };
+  float m[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  const int gxc = x0 + tx;
+  if (gxc < cols) {
+    const int rb = ty * kGR;
+    float h[5][3], b[3][3];  // horizontally blurred rows r-4 .. r; blurred rows q-2 .. q (columns tx .. tx + 2)
+#pragma unroll 1
+    for (int r = 0; r < kGR + 6; ++r) {
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    float w = m[k];
-    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-    if (lane == 0) sm.red[k * 32 + warp] = FF{w, 0.0f};
-  }
-  __syncthreads();
-  if (warp == 0) {
+      for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      FF w = (lane < kThreads / 32) ? sm.red[k * 32 + lane] : FF{0.0f, 0.0f};
-      for (int o = 16; o > 0; o >>= 1) w = ff_add(w, ff_shfl_down(w, o));
-      v[k] = (double)w.hi + (double)w.lo;
+        for (int j = 0; j < 3; ++j) h[i][j] = h[i + 1][j];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        h[4][j] = blur5(in(rb + r, tx + j), in(rb + r, tx + j + 1), in(rb + r, tx + j + 2), in(rb + r, tx + j + 3),
+                        in(rb + r, tx + j + 4));
+      if (r >= 4) {  // blurred row rb + r - 4
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          b[0][j] = b[1][j];
+          b[1][j] = b[2][j];
+          b[2][j] = blur5(h[0][j], h[1][j], h[2][j], h[3][j], h[4][j]);
+        }
+        if (r >= 6) {  // output row rb + r - 6 from blurred rows r - 6 .. r - 4
+          const int gyr = y0 + rb + r - 6;
+          if (gyr < rows) {
+            const int64_t pix = (int64_t)gyr * cols + gxc;
+            if (!mask || mask[pix]) {
+              float gx, gy;
+              sobel3(b[0][0], b[0][1], b[0][2], b[1][0], b[1][2], b[2][0], b[2][1], b[2][2], gx, gy);
+              moments_add(m, gx, gy, fhx[pix], fhy[pix]);
+            }
+          }
+        }
+      }
     }
   }
-  __syncthreads();  // sm is reused by the caller's next tile
+  tile_moments_reduce(m, red, v);
 }
 
 // Per-image combine: the tile partials (nblk x 6 doubles, read through L2 when
@@ -227,12 +311,25 @@ __device__ void grad_tile_moments(const float* __restrict__ src, int rows, int c
 // across their warps; the similarity value (valid in thread 0).
 template <bool CG>
 __device__ float grad_finalize_image(const double* __restrict__ p, int nblk, double n, const FixedNCC& fx,
-                                     const FixedNCC& fy, double* red /* [6][32] */) {
+                                     const FixedNCC& fy, double* red /* [6][4] */) {
+  constexpr int kW = kFinalizeThreads / 32;
   double a[6] = {0, 0, 0, 0, 0, 0};
   if (threadIdx.x < kFinalizeThreads)
     for (int k = threadIdx.x; k < nblk; k += kFinalizeThreads)
-      for (int j = 0; j < 6; ++j) a[j] += CG ? __ldcg(p + 6 * k + j) : p[6 * k + j];
-  block_sum_d<6>(a, red, kFinalizeThreads / 32);
+      for (int j = 0; j < 6; ++j) a[j] = __dadd_rn(a[j], CG ? __ldcg(p + 6 * k + j) : p[6 * k + j]);
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const double w = warp_sum_d(a[k]);
+      if (lane == 0 && warp < kW) red[k * kW + warp] = w;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) a[k] = warp_sum_d((lane < kW) ? red[k * kW + lane] : 0.0);
+    }
+  }
   float out = 0.0f;
   if (threadIdx.x == 0) {
     const double sx = ncc_sim_from_moments(a[0], a[1], a[2], n, fx);

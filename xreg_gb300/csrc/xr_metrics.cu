@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kThreads) grad_moments_kernel(const float* __r
 // (gt::grad_finalize_image, shared with the fused evaluation kernel).
 __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs, double n,
                                      FixedNCC fx, FixedNCC fy, float* __restrict__ sims) {
-  __shared__ double red[6 * 32];
+  __shared__ double red[6 * (gt::kFinalizeThreads / 32)];
   const int64_t img = blockIdx.x;
   const float v = gt::grad_finalize_image<false>(partials + img * nblk * 6, nblk, n, fx, fy, red);
   if (threadIdx.x == 0) sims[img] = v;

@@ -31,7 +31,9 @@
 #include "xr_internal.h"
 #include "xr_gradtile.cuh"
 
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cfloat>
 
 namespace xr {
@@ -700,7 +702,6 @@ drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long tota
 // visible device-wide (fence) before each count; counted data is read through
 // L2 (ld.global.cg), never through the incoherent L1.
 constexpr int kFusedKR = 2;  // 5x5 smoothing, xReg's default
-using FusedSmem = gt::GradTileSmem<kFusedKR>;
 
 // Metric tiles the DRR tile [r0, r1) x [c0, c1) feeds, and how many DRR tiles
 // feed each; claims (into claim[]) those whose count this tile completes.
@@ -729,10 +730,12 @@ __device__ __forceinline__ int fused_count_tile(const FusedJob& J, unsigned int*
 }
 
 template <int VT, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, UNROLL >= kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
+__global__ void __launch_bounds__(kThreads, kMinBlocksPerSM - 1)
 eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total, unsigned long long* counter) {
+  // under 1 KB of shared memory: the SM's unified L1 stays with the DRR gathers
   __shared__ long long s_item;
-  __shared__ FusedSmem gsm;
+  __shared__ gt::FF s_red[6 * (kThreads / 32)];
+  __shared__ double s_dred[6 * (gt::kFinalizeThreads / 32)];
   __shared__ int s_claim[8];
   __shared__ int s_nclaim, s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -771,8 +774,8 @@ eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total,
       __threadfence();
       const int M = s_claim[c];
       double vals[6];
-      gt::grad_tile_moments<kFusedKR, true>(P.out + proj * (int64_t)rows * cols, rows, cols, (M / J.mt_x) * gt::kGH,
-                                            (M % J.mt_x) * gt::kGW, V.fhx, V.fhy, V.mask, gsm, vals);
+      gt::grad_tile_moments_regs5(P.out + proj * (int64_t)rows * cols, rows, cols, (M / J.mt_x) * gt::kGH,
+                                  (M % J.mt_x) * gt::kGW, V.fhx, V.fhy, V.mask, s_red, vals);
       if (threadIdx.x == 0) {
         double* o = V.partials + (k * mt + M) * 6;
 #pragma unroll
@@ -785,8 +788,7 @@ eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total,
       __syncthreads();
       if (s_last) {  // every tile of this image is in: its FP64 combine
         __threadfence();
-        const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy,
-                                                        reinterpret_cast<double*>(gsm.red));
+        const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy, s_dred);
         if (threadIdx.x == 0) {
           V.sims[k] = sim;
           __threadfence();
@@ -843,11 +845,16 @@ cudaError_t launch_fused_t(const FusedJob* d_jobs, int njobs, long long total, u
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   int blocks = cached[dev].load(std::memory_order_relaxed);
   if (!blocks) {
-    // the metric tile's shared memory is small: keep the rest of the SM's
-    // unified L1 for the DRR gathers
-    const int pct = 25;
-    cudaError_t e = cudaFuncSetAttribute(eval_fused_kernel<VT, LAYOUT, UNROLL>,
-                                         cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    // the kernel's shared memory is small: the smallest carve-out that holds
+    // every resident block leaves the rest of the SM's unified L1 to the gathers
+    cudaFuncAttributes fa{};
+    int smem_sm = 0;
+    cudaError_t e = cudaFuncGetAttributes(&fa, eval_fused_kernel<VT, LAYOUT, UNROLL>);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e != cudaSuccess) return e;
+    const double need = (double)(fa.sharedSizeBytes + 1024) * (kMinBlocksPerSM - 1);
+    const int pct = std::min(100, (int)std::ceil(100.0 * need / (double)std::max(smem_sm, 1)) + 1);
+    e = cudaFuncSetAttribute(eval_fused_kernel<VT, LAYOUT, UNROLL>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
