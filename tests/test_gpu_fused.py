@@ -68,6 +68,12 @@ def test_fused_equals_split(xr, oracle, det, nviews, vt, masked):
         split = obj.eval(poses)
         drr_s = rc.projs()[:nviews * pop].copy()
         np.testing.assert_array_equal(drr_f, drr_s)
+        # each path against the metric restated in double on the same DRRs
+        mk = [None] * nviews if masks is None else masks
+        want = np.mean([oracle.grad_ncc(fixed[v], drr_f[v * pop:(v + 1) * pop], mask=mk[v])
+                        for v in range(nviews)], axis=0)
+        np.testing.assert_allclose(split, want, atol=1e-5, rtol=0, err_msg="split path vs oracle")
+        np.testing.assert_allclose(fused, want, atol=1e-5, rtol=0, err_msg="fused path vs oracle")
         np.testing.assert_array_equal(fused, split)
     if vt == 0 and not masked:
         ref = oracle.drr_f32(vol.voxels, oracle_geom(vol), oracle_cams(cams),

@@ -271,7 +271,9 @@ __device__ inline void grad_tile_moments_regs5(const float* __restrict__ src, in
   const int gxc = x0 + tx;
   if (gxc < cols) {
     const int rb = ty * kGR;
-    float h[5][3], b[3][3];  // horizontally blurred rows r-4 .. r; blurred rows q-2 .. q (columns tx .. tx + 2)
+    // horizontally blurred rows r-4 .. r and blurred rows q-2 .. q of columns
+    // tx .. tx + 2 (zero until filled: the first iterations shift them in)
+    float h[5][3] = {}, b[3][3] = {};
 #pragma unroll 1
     for (int r = 0; r < kGR + 6; ++r) {
 #pragma unroll
