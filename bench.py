@@ -763,11 +763,21 @@ def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
     for k in range(1, steps + 1):
         mixed = js.eval(objs, [p[k] for p in poses_sets])
     t_mixed = time.perf_counter() - t0
+    launches = js.last_kernel_launches()
     t0 = time.perf_counter()
     for k in range(1, steps + 1):
         alone = [o.eval(p[k]) for o, p in zip(objs, poses_sets)]
     t_alone = time.perf_counter() - t0
-    same = all(np.array_equal(x, y) for x, y in zip(mixed, alone))
+    # the split step: one DRR launch per voxel group, then per job its metric launches
+    js.set_fused(False)
+    js.eval(objs, [p[0] for p in poses_sets])
+    t0 = time.perf_counter()
+    for k in range(1, steps + 1):
+        split = js.eval(objs, [p[k] for p in poses_sets])
+    t_split = time.perf_counter() - t0
+    js.set_fused(True)
+    same = all(np.array_equal(x, y) for x, y in zip(mixed, alone)) and \
+        all(np.array_equal(x, y) for x, y in zip(mixed, split))
     # one pose of the largest job against the oracle (its DRRs from the last job-set call)
     errs = None
     try:
@@ -792,6 +802,8 @@ def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
     return {"value": round(steps * total / t_mixed, 2), "unit": "poses/s",
             "errors_vs_oracle_largest_job_pose0": errs,
             "one_job_at_a_time": round(steps * total / t_alone, 2),
+            "split_step": round(steps * total / t_split, 2),
+            "kernel_launches_per_step": launches,
             "ms_per_step": round(1e3 * t_mixed / steps, 3), "jobs": njobs, "poses_per_step": total,
             "identical_to_alone": bool(same),
             "job_shapes": [f"{s.size[0]}x{s.size[1]}x{s.size[2]} v{len(s.view_angles)} "

@@ -729,8 +729,56 @@ __device__ __forceinline__ int fused_count_tile(const FusedJob& J, unsigned int*
   return n;
 }
 
+// The metric stage of a claimed tile, out of line: its registers do not
+// constrain the DRR loop's (it runs a few times per image, the loop for every
+// sample).  Returns, in thread 0, whether the image is complete.
+__device__ __noinline__ bool fused_metric_tile(const FusedJob& J, int64_t proj, int M, gt::FF* red) {
+  const DrrParams& P = J.d.p;
+  const int rows = P.rows, cols = P.cols, mt = J.mt_x * J.mt_y;
+  const int64_t nimg = (int64_t)J.nviews * J.pop;
+  const int64_t v = proj / J.pop, k = proj - v * J.pop;
+  const FusedView& V = J.views[v];
+  double vals[6];
+  gt::grad_tile_moments_regs5(P.out + proj * (int64_t)rows * cols, rows, cols, (M / J.mt_x) * gt::kGH,
+                              (M % J.mt_x) * gt::kGW, V.fhx, V.fhy, V.mask, red, vals);
+  bool last = false;
+  if (threadIdx.x == 0) {
+    double* o = V.partials + (k * mt + M) * 6;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) o[q] = vals[q];
+    __threadfence();
+    unsigned int* ci = J.cnt + nimg * mt + proj;
+    last = atomicAdd(ci, 1u) + 1u == (unsigned int)mt;
+    if (last) *ci = 0u;
+  }
+  return last;
+}
+
+// Every metric tile of image proj is in: its FP64 combine, then (by the block
+// that completes the pose's views) the mean over views.
+__device__ __noinline__ void fused_metric_image(const FusedJob& J, int64_t proj, double* red) {
+  const int mt = J.mt_x * J.mt_y;
+  const int64_t nimg = (int64_t)J.nviews * J.pop;
+  const int64_t v = proj / J.pop, k = proj - v * J.pop;
+  const FusedView& V = J.views[v];
+  __threadfence();
+  const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy, red);
+  if (threadIdx.x == 0) {
+    V.sims[k] = sim;
+    __threadfence();
+    unsigned int* cp = J.cnt + nimg * mt + nimg + k;
+    if (atomicAdd(cp, 1u) + 1u == (unsigned int)J.nviews) {  // every view of this pose
+      *cp = 0u;
+      __threadfence();
+      float sum = 0.0f;
+      for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
+      J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
+    }
+  }
+}
+
 template <int VT, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, kMinBlocksPerSM - 1)
+__global__ void __launch_bounds__(kThreads, UNROLL >= kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
 eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total, unsigned long long* counter) {
   // under 1 KB of shared memory: the SM's unified L1 stays with the DRR gathers
   __shared__ long long s_item;
@@ -760,48 +808,18 @@ eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total,
     if (!J.metric) continue;
     __threadfence();  // this block's DRR pixels, visible device-wide before they are counted
     __syncthreads();
-    const int rows = P.rows, cols = P.cols;
     const int mt = J.mt_x * J.mt_y;
-    const int64_t nimg = (int64_t)J.nviews * J.pop;
     if (threadIdx.x == 0)
-      s_nclaim = fused_count_tile(J, J.cnt + proj * mt, ty * 16, min(ty * 16 + 16, rows), tx * 16,
-                                  min(tx * 16 + 16, cols), s_claim);
+      s_nclaim = fused_count_tile(J, J.cnt + proj * mt, ty * 16, min(ty * 16 + 16, P.rows), tx * 16,
+                                  min(tx * 16 + 16, P.cols), s_claim);
     __syncthreads();
     const int nclaim = s_nclaim;
-    const int64_t v = proj / J.pop, k = proj - v * J.pop;
-    const FusedView& V = J.views[v];
     for (int c = 0; c < nclaim; ++c) {
       __threadfence();
-      const int M = s_claim[c];
-      double vals[6];
-      gt::grad_tile_moments_regs5(P.out + proj * (int64_t)rows * cols, rows, cols, (M / J.mt_x) * gt::kGH,
-                                  (M % J.mt_x) * gt::kGW, V.fhx, V.fhy, V.mask, s_red, vals);
-      if (threadIdx.x == 0) {
-        double* o = V.partials + (k * mt + M) * 6;
-#pragma unroll
-        for (int q = 0; q < 6; ++q) o[q] = vals[q];
-        __threadfence();
-        unsigned int* ci = J.cnt + nimg * mt + proj;
-        s_last = atomicAdd(ci, 1u) + 1u == (unsigned int)mt;
-        if (s_last) *ci = 0u;
-      }
+      const bool last = fused_metric_tile(J, proj, s_claim[c], s_red);
+      if (threadIdx.x == 0) s_last = last;
       __syncthreads();
-      if (s_last) {  // every tile of this image is in: its FP64 combine
-        __threadfence();
-        const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy, s_dred);
-        if (threadIdx.x == 0) {
-          V.sims[k] = sim;
-          __threadfence();
-          unsigned int* cp = J.cnt + nimg * mt + nimg + k;
-          if (atomicAdd(cp, 1u) + 1u == (unsigned int)J.nviews) {  // every view of this pose
-            *cp = 0u;
-            __threadfence();
-            float sum = 0.0f;
-            for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
-            J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
-          }
-        }
-      }
+      if (s_last) fused_metric_image(J, proj, s_dred);  // every tile of this image is in
       __syncthreads();
     }
   }
