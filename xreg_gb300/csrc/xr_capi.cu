@@ -895,6 +895,19 @@ xr_status time_config(DrrParams p, cudaStream_t s, float* ms_out) {
 }
 }  // namespace
 
+static TuneKey tune_key(xr_raycaster rc, const xr_raycaster_s::Vol& vol, const DrrParams& p) {
+  return TuneKey{vol.desc.n[0], vol.desc.n[1], vol.desc.n[2], rc->rows(), rc->cols(), pow2_bucket(p.num_projs),
+                 vol.type, p.kernel_id, (vol.cells.p != nullptr ? 1 : 0) | (p.vol.occ ? 2 : 0)};
+}
+
+// Whether rc_choose_config decides without timing launches (a configuration
+// fixed by the caller, or one cached for this shape).
+static bool rc_config_cached(xr_raycaster rc, const xr_raycaster_s::Vol& vol, const DrrParams& p) {
+  if (rc->cfg_layout != XR_LAYOUT_AUTO) return true;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  return g_tune.find(tune_key(rc, vol, p)) != g_tune.end();
+}
+
 // Picks the launch configuration for p (layout, block_warps_x, unroll, warp shape).
 static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vol, DrrParams& p, cudaStream_t s) {
   const bool has_cells = vol.cells.p != nullptr;
@@ -909,8 +922,7 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
     p.warp_tall = rc->cfg_warp_rows == 8 ? 1 : 0;
     return XR_OK;
   }
-  const TuneKey key{vol.desc.n[0], vol.desc.n[1], vol.desc.n[2], rc->rows(), rc->cols(), pow2_bucket(p.num_projs),
-                    vol.type, p.kernel_id, (has_cells ? 1 : 0) | (p.vol.occ ? 2 : 0)};
+  const TuneKey key = tune_key(rc, vol, p);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -2063,6 +2075,7 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
   std::vector<std::vector<FusedView>> fv((size_t)n);
   std::vector<int32_t> key;
   int64_t first = 0;
+  int tuning_launches = 0;  // a shape's first step: geometry for the autotuner's timed launches
   for (int32_t i = 0; i < n; ++i) {
     xr_objective obj = objs[i];
     XR_CHECK_ARG(obj && reg_contains(obj), "evaluation: unknown or destroyed objective");
@@ -2086,17 +2099,30 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
     if ((st = rc_prepare(rc, obj->vol_idx, s, J.d.p, false)) != XR_OK) return st;
     XR_CHECK_ARG(J.d.p.kernel_id == XR_LINE_INT_SUM, "evaluation: the fused step uses the line-integral sum kernel");
     const auto& vol = *rc->vols[(size_t)obj->vol_idx];
-    // float32 volumes read their cell copy with one 256-bit load, half volumes
-    // with one 128-bit load; BF16 cells run the packed four-sample loop
-    J.d.p.vol.layout = vol.cells.p ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
-    J.d.p.block_warps_x = 2;
-    J.d.p.unroll = (vol.type == XR_VOXEL_BF16 && vol.cells.p) ? 6 : 4;
-    J.d.tiles_x = (int32_t)((J.d.p.cols + 15) / 16);
-    J.d.tiles_y = (int32_t)((J.d.p.rows + 15) / 16);
-    rc->last_layout = J.d.p.vol.layout;
-    rc->last_bw = 2;
-    rc->last_unroll = J.d.p.unroll;
-    rc->last_warp_rows = 4;
+    // the ray caster's autotuned layout and block shape; the fused kernel runs
+    // the four-sample loop (packed pairs where the tuner chose them); without
+    // the macro-cell trim, or with a configuration fixed by the caller that the
+    // fused kernel lacks, float32 volumes read their cell copy with one 256-bit
+    // load and half volumes with one 128-bit load
+    DrrParams& P = J.d.p;
+    if (!rc_config_cached(rc, vol, P)) {  // the tuner times real launches: this caster's geometry first
+      XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
+                                   rc->d_cam_idx.as<int32_t>(), rc->num_projs, rc->pose_count,
+                                   rc->d_geo.as<ProjGeom>(), s));
+      ++tuning_launches;
+    }
+    if ((st = rc_choose_config(rc, vol, P, s)) != XR_OK) return st;
+    const bool cells = vol.cells.p != nullptr;
+    const int32_t wide = cells ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
+    if (P.vol.layout != wide) P.vol.layout = wide;
+    P.unroll = (P.unroll == 6 && cells) ? 6 : 4;
+    const int wc = P.warp_tall ? 4 : 8, tw = wc * P.block_warps_x, th = (8 / P.block_warps_x) * (32 / wc);
+    J.d.tiles_x = (int32_t)((P.cols + tw - 1) / tw);
+    J.d.tiles_y = (int32_t)((P.rows + th - 1) / th);
+    rc->last_layout = P.vol.layout;
+    rc->last_bw = P.block_warps_x;
+    rc->last_unroll = P.unroll;
+    rc->last_warp_rows = P.warp_tall ? 8 : 4;
     GeomJob G{};
     G.p2i = phys_to_idx_xform(vol.desc);
     G.cams = rc->d_cams.as<xr_camera_desc>();
@@ -2190,7 +2216,7 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
   }
   XR_CUDA_TRY(cudaMemcpyAsync(fw.d_desc.p, h, bytes, cudaMemcpyHostToDevice, s));
   XR_CUDA_TRY(launch_proj_geom_jobs(reinterpret_cast<const GeomJob*>(d), (int)gj.size(), first, s));
-  fw.launches = 1;
+  fw.launches = 1 + tuning_launches;
   fw.items = 0;
   fw.blocks = 0;
   for (size_t gi = 0; gi < ranges.size(); ++gi) {

@@ -704,9 +704,10 @@ drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long tota
 constexpr int kFusedKR = 2;  // 5x5 smoothing, xReg's default
 
 // Metric tiles the DRR tile [r0, r1) x [c0, c1) feeds, and how many DRR tiles
-// feed each; claims (into claim[]) those whose count this tile completes.
+// (tw x th pixels) feed each; claims (into claim[]) those whose count this
+// tile completes.
 __device__ __forceinline__ int fused_count_tile(const FusedJob& J, unsigned int* cnt_tile, int r0, int r1, int c0,
-                                                int c1, int* claim) {
+                                                int c1, int tw, int th, int* claim) {
   constexpr int H = kFusedKR + 1;
   const int rows = J.d.p.rows, cols = J.d.p.cols;
   int n = 0;
@@ -718,7 +719,7 @@ __device__ __forceinline__ int fused_count_tile(const FusedJob& J, unsigned int*
     for (int mx = mx0; mx <= mx1; ++mx) {
       const int ec0 = max(0, mx * gt::kGW - H), ec1 = min(cols, mx * gt::kGW + gt::kGW + H);
       if (!(ec0 < c1 && c0 < ec1)) continue;
-      const unsigned int target = (unsigned int)(((er1 - 1) / 16 - er0 / 16 + 1) * ((ec1 - 1) / 16 - ec0 / 16 + 1));
+      const unsigned int target = (unsigned int)(((er1 - 1) / th - er0 / th + 1) * ((ec1 - 1) / tw - ec0 / tw + 1));
       unsigned int* c = cnt_tile + my * J.mt_x + mx;
       if (atomicAdd(c, 1u) + 1u == target) {
         *c = 0u;  // completed: zero for the next launch
@@ -784,7 +785,7 @@ eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total,
   __shared__ long long s_item;
   __shared__ gt::FF s_red[6 * (kThreads / 32)];
   __shared__ double s_dred[6 * (gt::kFinalizeThreads / 32)];
-  __shared__ int s_claim[8];
+  __shared__ int s_claim[16];
   __shared__ int s_nclaim, s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
@@ -801,8 +802,12 @@ eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total,
     const int64_t proj = (int64_t)(local % P.num_projs);
     const int tile = (int)(local / P.num_projs);
     const int ty = tile / J.d.tiles_x, tx = tile - ty * J.d.tiles_x;
-    const int col = tx * 16 + (warp & 1) * 8 + (lane & 7);
-    const int row = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
+    // the job's block shape (as drr_kernel): bw warps across, each warp 8x4
+    // pixels (or 4x8 when tall)
+    const int bw = P.block_warps_x, wl = P.warp_tall ? 2 : 3;
+    const int wc = 1 << wl, wr = 32 >> wl, tw = wc * bw, th = (8 / bw) * wr;
+    const int col = tx * tw + (warp % bw) * wc + (lane & (wc - 1));
+    const int row = ty * th + (warp / bw) * wr + (lane >> wl);
     unsigned int nl;
     if (col < P.cols && row < P.rows) trace_pixel<VT, XR_LINE_INT_SUM, LAYOUT, UNROLL>(P, proj, row, col, &nl);
     if (!J.metric) continue;
@@ -810,8 +815,8 @@ eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total,
     __syncthreads();
     const int mt = J.mt_x * J.mt_y;
     if (threadIdx.x == 0)
-      s_nclaim = fused_count_tile(J, J.cnt + proj * mt, ty * 16, min(ty * 16 + 16, P.rows), tx * 16,
-                                  min(tx * 16 + 16, P.cols), s_claim);
+      s_nclaim = fused_count_tile(J, J.cnt + proj * mt, ty * th, min(ty * th + th, P.rows), tx * tw,
+                                  min(tx * tw + tw, P.cols), tw, th, s_claim);
     __syncthreads();
     const int nclaim = s_nclaim;
     for (int c = 0; c < nclaim; ++c) {
