@@ -779,7 +779,7 @@ __device__ __noinline__ void fused_metric_image(const FusedJob& J, int64_t proj,
 }
 
 template <int VT, int LAYOUT, int UNROLL>
-__global__ void __launch_bounds__(kThreads, UNROLL >= kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
+__global__ void __launch_bounds__(kThreads, kMinBlocksPerSM - 1)
 eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total, unsigned long long* counter) {
   // under 1 KB of shared memory: the SM's unified L1 stays with the DRR gathers
   __shared__ long long s_item;
