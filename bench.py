@@ -55,7 +55,7 @@ def _args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--voxel", default="f32", choices=["f32", "f16", "bf16"])
-    p.add_argument("--path", default="fused", choices=["fused", "split"],
+    p.add_argument("--path", default="split", choices=["fused", "split"],
                    help="evaluation path timed as the headline (the other is timed beside it)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true")
@@ -732,8 +732,9 @@ def _precision(xr, dev, stream, pop: int = 20, reps: int = 5):
 def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
     """8 concurrent registrations of uneven size (volumes 192^3 .. 512x512x300,
     1-3 views, detector 4x or 8x downsampled, lambda 20-100; FP16 volumes), one
-    population per job per optimizer step: one job-set call (one persistent DRR
-    launch) per step versus the same populations evaluated job by job."""
+    population per job per optimizer step: one job-set call per step (geometry,
+    one persistent DRR launch, one batched grad-NCC launch), the fused job-set
+    step beside it, and the same populations evaluated job by job."""
     from xreg_gb300 import synth
     specs = synth.uneven_job_specs(njobs, seed=4)
     objs, poses_sets, total = [], [], 0
@@ -768,16 +769,17 @@ def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
     for k in range(1, steps + 1):
         alone = [o.eval(p[k]) for o, p in zip(objs, poses_sets)]
     t_alone = time.perf_counter() - t0
-    # the split step: one DRR launch per voxel group, then per job its metric launches
-    js.set_fused(False)
+    # the fused step: geometry, then one DRR + grad-NCC launch per voxel group
+    js.set_fused(True)
     js.eval(objs, [p[0] for p in poses_sets])
     t0 = time.perf_counter()
     for k in range(1, steps + 1):
-        split = js.eval(objs, [p[k] for p in poses_sets])
-    t_split = time.perf_counter() - t0
-    js.set_fused(True)
+        fused = js.eval(objs, [p[k] for p in poses_sets])
+    t_fused = time.perf_counter() - t0
+    fused_launches = js.last_kernel_launches()
+    js.set_fused(False)
     same = all(np.array_equal(x, y) for x, y in zip(mixed, alone)) and \
-        all(np.array_equal(x, y) for x, y in zip(mixed, split))
+        all(np.array_equal(x, y) for x, y in zip(mixed, fused))
     # one pose of the largest job against the oracle (its DRRs from the last job-set call)
     errs = None
     try:
@@ -802,8 +804,8 @@ def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
     return {"value": round(steps * total / t_mixed, 2), "unit": "poses/s",
             "errors_vs_oracle_largest_job_pose0": errs,
             "one_job_at_a_time": round(steps * total / t_alone, 2),
-            "split_step": round(steps * total / t_split, 2),
-            "kernel_launches_per_step": launches,
+            "fused_step": round(steps * total / t_fused, 2),
+            "kernel_launches_per_step": launches, "fused_step_kernel_launches": fused_launches,
             "ms_per_step": round(1e3 * t_mixed / steps, 3), "jobs": njobs, "poses_per_step": total,
             "identical_to_alone": bool(same),
             "job_shapes": [f"{s.size[0]}x{s.size[1]}x{s.size[2]} v{len(s.view_angles)} "

@@ -379,12 +379,14 @@ XR_API xr_status xr_obj_destroy(xr_objective obj);
 XR_API xr_status xr_obj_eval(xr_objective obj, int64_t pop, const double* host_xforms, float* host_sims);
 /* Same with device pointers; asynchronous on the ray caster's stream. */
 XR_API xr_status xr_obj_eval_device(xr_objective obj, int64_t pop, const double* d_xforms, float* d_sims);
-/* Evaluation path of an objective: 1 (default) = fused: one persistent kernel
- * traces every DRR tile and, as soon as the DRR pixels a metric tile reads are
- * written, computes that tile's grad-NCC moments, then each image's value and
- * each pose's mean over views (grad-NCC with 5x5 smoothing; other metrics run
- * their own launches after the DRR); 0 = split: the DRR launch, then each
- * metric's launches, replayed as a CUDA graph.  Both give identical values.
+/* Evaluation path of an objective: 0 (default) = split: the DRR launch, then
+ * each metric's launches, replayed as a CUDA graph; 1 = fused: one persistent
+ * kernel traces every DRR tile and, as soon as the DRR pixels a metric tile
+ * reads are written, computes that tile's grad-NCC moments, then each image's
+ * value and each pose's mean over views (grad-NCC with 5x5 smoothing; other
+ * metrics keep the split path).  Both give identical values; split measured
+ * faster on GB300 (the fused kernel's per-tile barriers and metric reads cost
+ * more than the DRR's trip through L2/HBM saves).
  * No counterpart in xReg (its ray caster and metrics are separate passes,
  * xregRayCastLineIntOCL.cpp:39-117 then xregImgSimMetric2DGradImgOCL.cpp:41-163). */
 XR_API xr_status xr_obj_set_fused(xr_objective obj, int32_t enable);

@@ -151,13 +151,16 @@ XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t num_jobs, const xr_
                                        const int64_t* pops, const double* const* d_xforms, float* const* d_sims);
 /* Work items and persistent blocks of the last launch. */
 XR_API xr_status xr_jobset_last_launch(xr_jobset js, int64_t* work_items, int32_t* blocks);
-/* Evaluation path of a job set (as xr_obj_set_fused): 1 (default) = one
- * geometry launch for every job and one fused DRR + grad-NCC launch per
- * (voxel type, layout) group; 0 = one DRR launch per group, then per job its
- * metric launches and mean over views.  Values identical either way. */
+/* Evaluation path of a job set.  0 (default): one geometry launch for every
+ * job, one persistent DRR launch per (voxel type, layout) group, one batched
+ * grad-NCC launch over every job's images (with the per-image FP64 combine and
+ * the mean over views): three launches for jobs of one voxel type.  1: one
+ * geometry launch and one fused DRR + grad-NCC launch per group.  Jobs with
+ * other metrics run their metric launches after the DRR either way.  Values
+ * identical either way.  No counterpart in xReg. */
 XR_API xr_status xr_jobset_set_fused(xr_jobset js, int32_t enable);
-/* Kernel launches the last fused step issued (geometry + fused launches), or
- * -1 when the job set runs split. */
+/* Kernel launches the last step issued (not counting the autotuner's timed
+ * launches on a shape's first fused step). */
 XR_API xr_status xr_jobset_last_kernel_launches(xr_jobset js, int32_t* launches);
 
 /* One generation of several registrations in one call: for each job the loop

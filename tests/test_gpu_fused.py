@@ -8,8 +8,9 @@ usual tolerances hold (DRR <= 1e-4 float32 volume, grad-NCC <= 1e-5).  Image
 sizes that are not multiples of the 16x16 DRR tiles or the 32x64 metric
 tiles, masks, several views, populations below the objective's maximum, and
 repeated steps (the kernel's counters reset themselves) are covered; a job
-set of uneven jobs runs as one geometry launch plus one fused launch per
-voxel-type group and equals each job alone."""
+set of uneven jobs equals each job alone on both job-set steps (geometry, DRR
+and one batched grad-NCC launch; geometry and one fused launch per voxel-type
+group)."""
 import numpy as np
 import pytest
 
@@ -104,10 +105,11 @@ def test_fused_device_entry_and_graph_path(xr):
     np.testing.assert_array_equal(out[True], out[False])
 
 
-def test_fused_jobset_launches_and_alone(xr):
+def test_jobset_steps_launches_and_alone(xr):
     """Uneven jobs (sizes, views, detectors, voxel types, one NCC job that runs
-    its metric after the fused launch): values equal each job alone; same-type
-    jobs take one geometry launch plus one fused launch."""
+    its own metric launches): values equal each job alone, on the batched split
+    step (geometry, DRR per voxel group, one grad-NCC launch) and the fused step
+    (geometry, one fused launch per voxel group)."""
     def job(seed, size, vt, det, nviews, kind=None):
         vol = small_volume(seed, size, (1.5, 1.5, 1.5))
         cams = _views(nviews, det)
@@ -119,33 +121,27 @@ def test_fused_jobset_launches_and_alone(xr):
     jobs = [job(1, (48, 44, 40), 1, (48, 52), 1), job(2, (40, 36, 44), 1, (32, 36), 2),
             job(3, (36, 40, 30), 1, (40, 40), 3)]
     poses = [synth.sample_poses(v, synth.gt_pose(v), 7 - i, 8.0, 10.0, seed=10 + i) for i, (_, v) in enumerate(jobs)]
-    alone = []
-    for (o, _), p in zip(jobs, poses):
-        o.set_fused(False)
-        alone.append(o.eval(p))
-        o.set_fused(True)
+    alone = [o.eval(p) for (o, _), p in zip(jobs, poses)]
     js = xr.JobSet()
-    for rep in range(2):
-        mixed = js.eval([o for o, _ in jobs], poses)
-        for a, m in zip(alone, mixed):
-            np.testing.assert_array_equal(m, a)
-        assert js.last_kernel_launches() == 2
-    # mixed voxel types and an NCC job: one fused launch per group, the NCC metric after
+    for fused, launches in ((False, 3), (True, 2)):
+        js.set_fused(fused)
+        for rep in range(2):
+            mixed = js.eval([o for o, _ in jobs], poses)
+            for a, m in zip(alone, mixed):
+                np.testing.assert_array_equal(m, a)
+            if rep:
+                assert js.last_kernel_launches() == launches
+    # mixed voxel types and an NCC job (moments, finalize and its mean over views after the DRR)
     more = jobs + [job(4, (40, 40, 40), 0, (36, 36), 1), job(5, (32, 36, 40), 2, (30, 34), 1),
                    job(6, (36, 36, 36), 0, (28, 28), 2, xr.ImgSimMetric2DNCCCUDA)]
     p2 = poses + [synth.sample_poses(v, synth.gt_pose(v), 5, 8.0, 10.0, seed=20 + i)
                   for i, (_, v) in enumerate(more[3:])]
-    alone2 = []
-    for (o, _), p in zip(more, p2):
-        o.set_fused(False)
-        alone2.append(o.eval(p))
-        o.set_fused(True)
-    mixed = js.eval([o for o, _ in more], p2)
-    for a, m in zip(alone2, mixed):
-        np.testing.assert_array_equal(m, a)
-    assert js.last_kernel_launches() == 4  # geometry + F16, F32 and BF16 groups
-    js.set_fused(False)
-    split = js.eval([o for o, _ in more], p2)
-    for a, m in zip(alone2, split):
-        np.testing.assert_array_equal(m, a)
-    assert js.last_kernel_launches() == -1
+    alone2 = [o.eval(p) for (o, _), p in zip(more, p2)]
+    for fused, launches in ((False, 1 + 3 + 1 + 5), (True, 1 + 3 + 5)):
+        js.set_fused(fused)
+        for rep in range(2):
+            mixed = js.eval([o for o, _ in more], p2)
+            for a, m in zip(alone2, mixed):
+                np.testing.assert_array_equal(m, a)
+            if rep:
+                assert js.last_kernel_launches() == launches

@@ -622,15 +622,15 @@ class PopulationObjective:
         call("xr_obj_eval_device", self._h, int(pop), C.c_void_p(int(d_xforms)), C.c_void_p(int(d_sims)))
 
     def set_fused(self, enable: bool) -> None:
-        """Fused (default) or split evaluation path; identical values (xr_obj_set_fused)."""
+        """Split (default) or fused evaluation path; identical values (xr_obj_set_fused)."""
         call("xr_obj_set_fused", self._h, int(bool(enable)))
 
 
 # ------------------------------------------------------------------ job sets
 class JobSet:
-    """One step of several registrations at once: one geometry launch and one
-    persistent DRR + grad-NCC launch over every listed objective's work (or, split,
-    one DRR launch then each objective's metrics) (xr_jobset_*)."""
+    """One step of several registrations at once: one geometry launch, one
+    persistent DRR launch and one batched grad-NCC launch over every listed
+    objective's work (or the fused DRR + grad-NCC launch) (xr_jobset_*)."""
 
     def __init__(self, device: int = -1):
         load()
@@ -689,11 +689,11 @@ class JobSet:
         return a.value, b.value
 
     def set_fused(self, enable: bool) -> None:
-        """Fused (default) or split evaluation step; identical values (xr_jobset_set_fused)."""
+        """Batched split (default) or fused evaluation step; identical values (xr_jobset_set_fused)."""
         call("xr_jobset_set_fused", self._h, int(bool(enable)))
 
     def last_kernel_launches(self) -> int:
-        """Kernel launches of the last fused step (-1 when split)."""
+        """Kernel launches of the last step."""
         v = C.c_int32()
         call("xr_jobset_last_kernel_launches", self._h, C.byref(v))
         return int(v.value)

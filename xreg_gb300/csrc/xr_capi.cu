@@ -286,7 +286,7 @@ struct xr_objective_s {
   DevBuf d_poses, d_sims;
   // fused evaluation: mode (1 fused, 0 split DRR and metric launches), its
   // counters (zero between launches) and descriptors
-  int32_t fused = 1;
+  int32_t fused = 0;
   DevBuf d_fcnt;
   size_t fcnt_words = 0;
   FusedWork fw;
@@ -2060,15 +2060,26 @@ static bool obj_metric_fusable(xr_objective obj) {
 
 static size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
 
-// One evaluation step of n objectives, fused: per job the poses are copied in,
-// then ONE geometry launch covers every job's projections and ONE persistent
-// launch per (voxel type, layout) group traces every DRR tile and computes the
-// grad-NCC of each image behind it (eval_fused_kernel); objectives whose
-// metrics cannot run fused get their metric launches afterwards.  Values are
-// copied to sims[i].  Everything is ordered on stream s.
-static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_objective* objs, const int64_t* pops,
-                               const double* const* xforms, bool host_in, float* const* sims, bool host_out,
-                               cudaStream_t s) {
+// Kernel launches of one metric compute (sm_enqueue_compute_on).
+static int metric_launches(const xr_simmetric_s* m) {
+  if (m->kind == XR_SIM_NCC || m->kind == XR_SIM_GRAD_NCC) return 2;
+  return 2 + (m->mvar_mode ? 2 : 0) + (m->popt.choose_rand_patches ? 1 : 0);
+}
+
+// One evaluation step of n objectives: per job the poses are copied in, then
+// ONE geometry launch covers every job's projections; then
+//   fused: ONE persistent launch per (voxel type, layout) group traces every
+//     DRR tile and computes the grad-NCC of each image behind it
+//     (eval_fused_kernel), each job in its autotuned block shape;
+//   split: ONE persistent DRR launch per group (drr_multi_kernel, 16x16
+//     tiles), then ONE batched grad-NCC launch over every job's images
+//     (grad_multi_kernel, with the per-image combine and the mean over views).
+// Objectives whose metrics are not grad-NCC with 5x5 smoothing get their own
+// metric launches afterwards.  Values are copied to sims[i].  Everything is
+// ordered on stream s.  Both ways give identical values.
+static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_objective* objs, const int64_t* pops,
+                              const double* const* xforms, bool host_in, float* const* sims, bool host_out,
+                              cudaStream_t s, bool fused) {
   XR_CHECK_ARG(objs && pops && xforms && sims && n > 0, "evaluation: NULL argument or no jobs");
   std::vector<GeomJob> gj;
   std::vector<FusedJob> fj;
@@ -2105,17 +2116,23 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
     // fused kernel lacks, float32 volumes read their cell copy with one 256-bit
     // load and half volumes with one 128-bit load
     DrrParams& P = J.d.p;
-    if (!rc_config_cached(rc, vol, P)) {  // the tuner times real launches: this caster's geometry first
-      XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
-                                   rc->d_cam_idx.as<int32_t>(), rc->num_projs, rc->pose_count,
-                                   rc->d_geo.as<ProjGeom>(), s));
-      ++tuning_launches;
-    }
-    if ((st = rc_choose_config(rc, vol, P, s)) != XR_OK) return st;
     const bool cells = vol.cells.p != nullptr;
     const int32_t wide = cells ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
-    if (P.vol.layout != wide) P.vol.layout = wide;
-    P.unroll = (P.unroll == 6 && cells) ? 6 : 4;
+    if (fused) {
+      if (!rc_config_cached(rc, vol, P)) {  // the tuner times real launches: this caster's geometry first
+        XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
+                                     rc->d_cam_idx.as<int32_t>(), rc->num_projs, rc->pose_count,
+                                     rc->d_geo.as<ProjGeom>(), s));
+        ++tuning_launches;
+      }
+      if ((st = rc_choose_config(rc, vol, P, s)) != XR_OK) return st;
+      P.unroll = (P.unroll == 6 && cells) ? 6 : 4;
+    } else {
+      P.block_warps_x = 2;  // drr_multi_kernel: 16x16 tiles of 8x4-pixel warps, four-sample loop
+      P.warp_tall = 0;
+      P.unroll = 4;
+    }
+    P.vol.layout = wide;
     const int wc = P.warp_tall ? 4 : 8, tw = wc * P.block_warps_x, th = (8 / P.block_warps_x) * (32 / wc);
     J.d.tiles_x = (int32_t)((P.cols + tw - 1) / tw);
     J.d.tiles_y = (int32_t)((P.rows + th - 1) / th);
@@ -2141,7 +2158,7 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
     J.mt_x = (cols + 31) / 32;
     J.mt_y = (rows + 63) / 64;
     J.out = obj->d_sims.as<float>();
-    J.metric = (obj->fused && obj_metric_fusable(obj)) ? 1 : 0;
+    J.metric = obj_metric_fusable(obj) ? 1 : 0;
     for (int32_t v = 0; v < nv; ++v) {
       xr_simmetric m = obj->metrics[(size_t)v];
       m->num_mov = pop;
@@ -2193,9 +2210,18 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
     ranges.emplace_back(b, order.size());
     group_items.push_back(items);
   }
-  // one descriptor upload: geometry jobs, fused jobs (group order), views
+  // metric tiles of the batched grad-NCC launch, in group order
+  long long total_tiles = 0;
+  for (int32_t r : order) {
+    FusedJob& J = fj[(size_t)r];
+    J.tile_begin = total_tiles;
+    if (J.metric) total_tiles += (long long)J.nviews * J.pop * J.mt_x * J.mt_y;
+  }
+  // one descriptor upload: geometry jobs, jobs (group order), their DRR part
+  // alone (drr_multi_kernel's array), views
   const size_t off_f = align16(gj.size() * sizeof(GeomJob));
-  const size_t off_v = off_f + align16(fj.size() * sizeof(FusedJob));
+  const size_t off_m = off_f + align16(fj.size() * sizeof(FusedJob));
+  const size_t off_v = off_m + align16(fj.size() * sizeof(MultiJobDrr));
   size_t nviews_total = 0;
   for (auto& v : fv) nviews_total += v.size();
   const size_t bytes = off_v + nviews_total * sizeof(FusedView) + 16;
@@ -2213,6 +2239,7 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
     if (!views.empty()) std::memcpy(h + off_v + vpos * sizeof(FusedView), views.data(), views.size() * sizeof(FusedView));
     vpos += views.size();
     std::memcpy(h + off_f + r * sizeof(FusedJob), &J, sizeof(FusedJob));
+    std::memcpy(h + off_m + r * sizeof(MultiJobDrr), &J.d, sizeof(MultiJobDrr));
   }
   XR_CUDA_TRY(cudaMemcpyAsync(fw.d_desc.p, h, bytes, cudaMemcpyHostToDevice, s));
   XR_CUDA_TRY(launch_proj_geom_jobs(reinterpret_cast<const GeomJob*>(d), (int)gj.size(), first, s));
@@ -2222,12 +2249,22 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
   for (size_t gi = 0; gi < ranges.size(); ++gi) {
     const FusedJob& f0 = fj[(size_t)order[ranges[gi].first]];
     int blocks = 0;
-    XR_CUDA_TRY(launch_eval_fused(reinterpret_cast<const FusedJob*>(d + off_f) + ranges[gi].first,
-                                  (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
-                                  f0.d.p.vol.voxel_type, f0.d.p.vol.layout, f0.d.p.unroll,
-                                  fw.d_counter.as<unsigned long long>(), &blocks, s));
+    if (fused)
+      XR_CUDA_TRY(launch_eval_fused(reinterpret_cast<const FusedJob*>(d + off_f) + ranges[gi].first,
+                                    (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
+                                    f0.d.p.vol.voxel_type, f0.d.p.vol.layout, f0.d.p.unroll,
+                                    fw.d_counter.as<unsigned long long>(), &blocks, s));
+    else
+      XR_CUDA_TRY(launch_drr_multi(reinterpret_cast<const MultiJobDrr*>(d + off_m) + ranges[gi].first,
+                                   (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
+                                   f0.d.p.vol.voxel_type, f0.d.p.vol.layout, f0.d.p.unroll,
+                                   fw.d_counter.as<unsigned long long>(), &blocks, s));
     fw.items += group_items[gi];
     fw.blocks = std::max(fw.blocks, blocks);
+    ++fw.launches;
+  }
+  if (!fused && total_tiles > 0) {
+    XR_CUDA_TRY(launch_grad_multi(reinterpret_cast<const FusedJob*>(d + off_f), (int)fj.size(), total_tiles, s));
     ++fw.launches;
   }
   for (int32_t i = 0; i < n; ++i) {
@@ -2247,6 +2284,7 @@ static xr_status fused_enqueue(FusedWork& fw, int device, int32_t n, const xr_ob
         view_sims[v] = m->d_sims.as<float>();
       }
       XR_CUDA_TRY(launch_combine_mean(view_sims, nv, pops[i], obj->d_sims.as<float>(), s));
+      fw.launches += nv * metric_launches(obj->metrics[0]) + 1;
     }
     if (sims[i] != obj->d_sims.as<float>())
       XR_CUDA_TRY(cudaMemcpyAsync(sims[i], obj->d_sims.p, (size_t)pops[i] * 4,
@@ -2293,7 +2331,7 @@ static xr_status obj_run(xr_objective obj, int64_t pop) {
   if (obj->fused && obj_metric_fusable(obj)) {
     const double* x = obj->d_poses.as<double>();
     float* v = obj->d_sims.as<float>();
-    return fused_enqueue(obj->fw, rc->device, 1, &obj, &pop, &x, false, &v, false, s);
+    return step_enqueue(obj->fw, rc->device, 1, &obj, &pop, &x, false, &v, false, s, true);
   }
   // A metric that draws random patches on the host at every compute, or a copy
   // into an external host buffer, is run directly (a captured graph would replay
@@ -2373,13 +2411,13 @@ struct xr_jobset_s {
   int device = 0;
   cudaStream_t own_stream = nullptr, ext_stream = nullptr;
   bool has_ext = false;
-  DevBuf d_jobs, d_counter;
-  std::vector<MultiJobDrr> h_jobs;
   int blocks = 0;
   long long last_items = 0;
   unsigned int* h_err = nullptr;  // pinned: every job's step-guard flag, read with one synchronisation
   size_t h_err_cap = 0;
-  int32_t fused = 1;               // 1: fused evaluation step; 0: DRR launch, then metric launches per job
+  // 0 (default): geometry, DRR and batched grad-NCC launches for every job;
+  // 1: fused evaluation step
+  int32_t step_mode = 0;
   FusedWork fw;
   cudaStream_t stream() const { return has_ext ? ext_stream : own_stream; }
 };
@@ -2393,7 +2431,7 @@ extern "C" XR_API xr_status xr_jobset_create(int32_t device, xr_jobset* out) {
   auto js = std::make_unique<xr_jobset_s>();
   js->device = dev;
   XR_CUDA_TRY(cudaStreamCreateWithFlags(&js->own_stream, cudaStreamNonBlocking));
-  XR_CUDA_TRY(js->d_counter.reserve(256));
+  XR_CUDA_TRY(js->fw.d_counter.reserve(256));
   js->blocks = 0;  // sized per launch from the kernel's occupancy
   *out = js.release();
   return XR_OK;
@@ -2416,123 +2454,17 @@ extern "C" XR_API xr_status xr_jobset_set_stream(xr_jobset js, void* s) {
   return XR_OK;
 }
 
-// Sample loop of the job-set kernel: the macro-cell trim, then four samples per
-// iteration (the fastest loop measured on the batched workload).
-constexpr int32_t kJobSetLoop = 4;
 
 static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
                                 const double* const* xforms, bool host_in, float* const* sims, bool host_out) {
   XR_CHECK_ARG(js && objs && pops && xforms && sims && n > 0, "xr_jobset_eval: NULL argument or no jobs");
   DeviceGuard g(js->device);
   cudaStream_t s = js->stream();
-  if (js->fused) {
-    xr_status st = fused_enqueue(js->fw, js->device, n, objs, pops, xforms, host_in, sims, host_out, s);
-    js->last_items = js->fw.items;
-    js->blocks = js->fw.blocks;
-    return st;
-  }
-  js->h_jobs.clear();
-  std::vector<int32_t> group;  // voxel type * 4 + layout of each job
-  for (int32_t i = 0; i < n; ++i) {
-    xr_objective obj = objs[i];
-    XR_CHECK_ARG(obj && reg_contains(obj), "xr_jobset_eval: unknown or destroyed objective");
-    XR_CHECK_ARG(obj->peers_alive(), "xr_jobset_eval: a ray caster or metric of an objective was destroyed");
-    XR_CHECK_ARG(obj->rc->device == js->device, "xr_jobset_eval: objective lives on another device");
-    for (int32_t k = 0; k < i; ++k) XR_CHECK_ARG(objs[k] != obj, "xr_jobset_eval: an objective is listed twice");
-    const int64_t pop = pops[i];
-    XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "xr_jobset_eval: population outside [1, max_pop]");
-    XR_CHECK_ARG(xforms[i] && sims[i], "xr_jobset_eval: NULL pose or value pointer");
-    if (host_in) XR_CHECK_ARG(finite_all(xforms[i], 16 * pop), "xr_jobset_eval: non-finite transform");
-    XR_CUDA_TRY(cudaMemcpyAsync(obj->d_poses.p, xforms[i], (size_t)pop * 16 * 8,
-                                host_in ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-    xr_raycaster rc = obj->rc;
-    const int32_t nv = (int32_t)obj->metrics.size();
-    xr_status st = xr_rc_set_num_projs(rc, (int64_t)nv * pop);
-    if (st != XR_OK) return st;
-    if ((st = rc_distribute_device_on(rc, pop, obj->d_poses.as<double>(), s)) != XR_OK) return st;
-    rc->store = XR_PROJ_STORE_REPLACE;
-    MultiJobDrr J{};
-    if ((st = rc_prepare(rc, obj->vol_idx, s, J.p)) != XR_OK) return st;
-    XR_CHECK_ARG(J.p.kernel_id == XR_LINE_INT_SUM, "xr_jobset_eval: job sets use the line-integral sum kernel");
-    const auto& vol = *rc->vols[(size_t)obj->vol_idx];
-    // float32 volumes read their cell copy with one 256-bit load; half volumes with one 128-bit load
-    J.p.vol.layout = vol.cells.p ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
-    J.p.block_warps_x = 2;
-    J.p.unroll = kJobSetLoop;
-    J.tiles_x = (int32_t)((J.p.cols + 15) / 16);
-    J.tiles_y = (int32_t)((J.p.rows + 15) / 16);
-    rc->last_layout = J.p.vol.layout;
-    rc->last_bw = 2;
-    rc->last_unroll = kJobSetLoop;
-    rc->last_warp_rows = 4;
-    js->h_jobs.push_back(J);
-    group.push_back(vol.type * 4 + J.p.vol.layout);
-  }
-  // One persistent launch per (voxel type, layout) group, jobs of a group
-  // contiguous; item numbering restarts in each group.
-  std::vector<MultiJobDrr> ordered;
-  std::vector<std::pair<size_t, size_t>> ranges;  // [begin, end) of each group in `ordered`
-  std::vector<long long> group_items;
-  {
-    std::vector<int32_t> keys(group);
-    std::sort(keys.begin(), keys.end());
-    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-    for (int32_t k : keys) {
-      const size_t b = ordered.size();
-      long long items = 0;
-      for (size_t i = 0; i < js->h_jobs.size(); ++i)
-        if (group[i] == k) {
-          MultiJobDrr J = js->h_jobs[i];
-          J.item_begin = items;
-          items += (long long)J.p.num_projs * J.tiles_x * J.tiles_y;
-          ordered.push_back(J);
-        }
-      ranges.emplace_back(b, ordered.size());
-      group_items.push_back(items);
-    }
-  }
-  XR_CUDA_TRY(js->d_jobs.reserve(ordered.size() * sizeof(MultiJobDrr)));
-  XR_CUDA_TRY(cudaMemcpyAsync(js->d_jobs.p, ordered.data(), ordered.size() * sizeof(MultiJobDrr),
-                              cudaMemcpyHostToDevice, s));
-  js->last_items = 0;
-  js->blocks = 0;
-  for (size_t gi = 0; gi < ranges.size(); ++gi) {
-    const MultiJobDrr& first = ordered[ranges[gi].first];
-    int blocks = 0;
-    XR_CUDA_TRY(launch_drr_multi(js->d_jobs.as<MultiJobDrr>() + ranges[gi].first,
-                                 (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
-                                 first.p.vol.voxel_type, first.p.vol.layout, kJobSetLoop,
-                                 js->d_counter.as<unsigned long long>(), &blocks, s));
-    js->last_items += group_items[gi];
-    js->blocks = std::max(js->blocks, blocks);
-  }
-  for (int32_t i = 0; i < n; ++i) {
-    xr_raycaster rc = objs[i]->rc;
-    if (rc->ext_host)
-      XR_CUDA_TRY(cudaMemcpyAsync(rc->ext_host, rc_out(rc, nullptr),
-                                  (size_t)rc->num_projs * (size_t)(rc->rows() * rc->cols()) * 4,
-                                  cudaMemcpyDeviceToHost, s));
-  }
-  for (int32_t i = 0; i < n; ++i) {
-    xr_objective obj = objs[i];
-    const int64_t pop = pops[i];
-    const int32_t nv = (int32_t)obj->metrics.size();
-    const float* view_sims[16];
-    for (int32_t v = 0; v < nv; ++v) {
-      xr_simmetric m = obj->metrics[(size_t)v];
-      m->num_mov = pop;
-      m->rc = obj->rc;
-      m->rc_id = obj->rc->id;
-      m->proj_offset = (int64_t)v * pop;
-      xr_status st = sm_enqueue_compute_on(m, s);
-      if (st != XR_OK) return st;
-      view_sims[v] = m->d_sims.as<float>();
-    }
-    XR_CUDA_TRY(launch_combine_mean(view_sims, nv, pop, obj->d_sims.as<float>(), s));
-    XR_CUDA_TRY(cudaMemcpyAsync(sims[i], obj->d_sims.p, (size_t)pop * 4,
-                                host_out ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
-  }
-  return XR_OK;
+  xr_status st = step_enqueue(js->fw, js->device, n, objs, pops, xforms, host_in, sims, host_out, s,
+                              js->step_mode == 1);
+  js->last_items = js->fw.items;
+  js->blocks = js->fw.blocks;
+  return st;
 }
 
 extern "C" XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
@@ -2570,13 +2502,13 @@ extern "C" XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t n, const
 
 extern "C" XR_API xr_status xr_jobset_set_fused(xr_jobset js, int32_t enable) {
   XR_CHECK_ARG(js, "xr_jobset_set_fused: NULL handle");
-  js->fused = enable ? 1 : 0;
+  js->step_mode = enable ? 1 : 0;
   return XR_OK;
 }
 
 extern "C" XR_API xr_status xr_jobset_last_kernel_launches(xr_jobset js, int32_t* launches) {
   XR_CHECK_ARG(js && launches, "xr_jobset_last_kernel_launches: NULL argument");
-  *launches = js->fused ? js->fw.launches : -1;
+  *launches = js->fw.launches;
   return XR_OK;
 }
 

@@ -135,11 +135,17 @@ struct FusedJob {
   const FusedView* views; // [nviews]
   float* out;             // [pop] mean over views
   unsigned int* cnt;
+  long long tile_begin;   // first metric tile of this job in a batched metric launch
 };
 // One persistent launch over the jobs of one (voxel type, layout) group.
 cudaError_t launch_eval_fused(const FusedJob* d_jobs, int njobs, long long total_items, int32_t voxel_type,
                               int32_t layout, int32_t unroll, unsigned long long* d_counter, int* blocks_out,
                               cudaStream_t s);
+// Grad-NCC (5x5 smoothing) of every image of the jobs with `metric` set, their
+// DRRs already written: one launch over all their 32x64 tiles (the split
+// path's tile code), each image's FP64 combine by the block that completes its
+// tiles, each pose's mean over views by the block that completes its views.
+cudaError_t launch_grad_multi(const FusedJob* d_jobs, int njobs, long long total_tiles, cudaStream_t s);
 // Geometry of many ray casters' projections in one launch.
 struct GeomJob {
   xf::Affine p2i;

@@ -269,6 +269,57 @@ __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nb
   if (threadIdx.x == 0) sims[img] = v;
 }
 
+// Batched grad-NCC over many jobs' images (launch_grad_multi): one block per
+// 32x64 tile, grid-stride; the counters of FusedJob::cnt (images, then poses)
+// chain the per-image combine and the mean over views behind the tiles.
+__global__ void __launch_bounds__(kThreads) grad_multi_kernel(const FusedJob* __restrict__ jobs, int njobs,
+                                                              long long total) {
+  __shared__ gt::GradTileSmem<2> sm;
+  __shared__ double dred[6 * (gt::kFinalizeThreads / 32)];
+  __shared__ int s_last;
+  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    int j = 0;
+    while (j + 1 < njobs && jobs[j + 1].tile_begin <= t) ++j;
+    const FusedJob& J = jobs[j];
+    const int rows = J.d.p.rows, cols = J.d.p.cols, mt = J.mt_x * J.mt_y;
+    const long long local = t - J.tile_begin;
+    const int64_t img = local / mt;  // projection: view-major (view * pop + pose)
+    const int M = (int)(local - img * mt);
+    const int64_t nimg = (int64_t)J.nviews * J.pop, v = img / J.pop, k = img - v * J.pop;
+    const FusedView& V = J.views[v];
+    double vals[6];
+    gt::grad_tile_moments<2, false>(J.d.p.out + img * (int64_t)rows * cols, rows, cols, (M / J.mt_x) * kGH,
+                                    (M % J.mt_x) * kGW, V.fhx, V.fhy, V.mask, sm, vals);
+    if (threadIdx.x == 0) {
+      double* o = V.partials + (k * mt + M) * 6;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) o[q] = vals[q];
+      __threadfence();
+      unsigned int* ci = J.cnt + nimg * mt + img;
+      s_last = atomicAdd(ci, 1u) + 1u == (unsigned int)mt;
+      if (s_last) *ci = 0u;
+    }
+    __syncthreads();
+    if (s_last) {  // every tile of this image is in: its FP64 combine
+      __threadfence();
+      const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy, dred);
+      if (threadIdx.x == 0) {
+        V.sims[k] = sim;
+        __threadfence();
+        unsigned int* cp = J.cnt + nimg * mt + nimg + k;
+        if (atomicAdd(cp, 1u) + 1u == (unsigned int)J.nviews) {  // every view of this pose
+          *cp = 0u;
+          __threadfence();
+          float sum = 0.0f;
+          for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
+          J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------ patch NCC ---
 constexpr int kPC = 16;  // patch centres per tile edge
 
@@ -794,6 +845,18 @@ cudaError_t launch_grad_moments(const float* mov, int rows, int cols, int64_t ni
     case 5: grad_moments_kernel<2><<<grid, kThreads, 0, s>>>(mov, rows, cols, fhat_x, fhat_y, mask, partials); break;
     default: return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grad_multi(const FusedJob* d_jobs, int njobs, long long total, cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grad_multi_kernel, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  const long long cap = (long long)sms * (per_sm > 0 ? per_sm : 1);
+  grad_multi_kernel<<<(unsigned)(total < cap ? total : cap), kThreads, 0, s>>>(d_jobs, njobs, total);
   return cudaGetLastError();
 }
 
