@@ -2071,8 +2071,8 @@ static int metric_launches(const xr_simmetric_s* m) {
 //   fused: ONE persistent launch per (voxel type, layout) group traces every
 //     DRR tile and computes the grad-NCC of each image behind it
 //     (eval_fused_kernel), each job in its autotuned block shape;
-//   split: ONE persistent DRR launch per group (drr_multi_kernel, 16x16
-//     tiles), then ONE batched grad-NCC launch over every job's images
+//   split: ONE persistent DRR launch per group (drr_multi_kernel, each job
+//     in its autotuned block shape), then ONE batched grad-NCC launch over every job's images
 //     (grad_multi_kernel, with the per-image combine and the mean over views).
 // Objectives whose metrics are not grad-NCC with 5x5 smoothing get their own
 // metric launches afterwards.  Values are copied to sims[i].  Everything is
@@ -2118,20 +2118,16 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     DrrParams& P = J.d.p;
     const bool cells = vol.cells.p != nullptr;
     const int32_t wide = cells ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
-    if (fused) {
-      if (!rc_config_cached(rc, vol, P)) {  // the tuner times real launches: this caster's geometry first
-        XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
-                                     rc->d_cam_idx.as<int32_t>(), rc->num_projs, rc->pose_count,
-                                     rc->d_geo.as<ProjGeom>(), s));
-        ++tuning_launches;
-      }
-      if ((st = rc_choose_config(rc, vol, P, s)) != XR_OK) return st;
-      P.unroll = (P.unroll == 6 && cells) ? 6 : 4;
-    } else {
-      P.block_warps_x = 2;  // drr_multi_kernel: 16x16 tiles of 8x4-pixel warps, four-sample loop
-      P.warp_tall = 0;
-      P.unroll = 4;
+    // each job in its autotuned block shape; the persistent kernels run the
+    // four-sample loop (the fused one the packed pairs where the tuner chose them)
+    if (!rc_config_cached(rc, vol, P)) {  // the tuner times real launches: this caster's geometry first
+      XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
+                                   rc->d_cam_idx.as<int32_t>(), rc->num_projs, rc->pose_count,
+                                   rc->d_geo.as<ProjGeom>(), s));
+      ++tuning_launches;
     }
+    if ((st = rc_choose_config(rc, vol, P, s)) != XR_OK) return st;
+    P.unroll = (fused && P.unroll == 6 && cells) ? 6 : 4;
     P.vol.layout = wide;
     const int wc = P.warp_tall ? 4 : 8, tw = wc * P.block_warps_x, th = (8 / P.block_warps_x) * (32 / wc);
     J.d.tiles_x = (int32_t)((P.cols + tw - 1) / tw);

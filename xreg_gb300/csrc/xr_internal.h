@@ -75,7 +75,8 @@ cudaError_t launch_proj_geom(const xr_volume_desc& vol, const xr_camera_desc* d_
 cudaError_t launch_drr(const DrrParams& p, cudaStream_t s);
 
 // One job of a multi-job DRR launch: its parameters (sum kernel; any store
-// rule), where its work items start, and its 16x16-pixel tile grid.
+// rule; p.block_warps_x and p.warp_tall give its tile shape as for
+// drr_kernel), where its work items start, and its tile grid.
 struct MultiJobDrr {
   DrrParams p;
   long long item_begin;  // items of this job: [item_begin, item_begin + num_projs * tiles_x * tiles_y)

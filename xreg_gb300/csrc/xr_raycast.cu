@@ -659,9 +659,10 @@ drr_kernel(const DrrParams p, const int64_t proj_base) {
 // (job, tile, projection) from a global counter until all are done; projections
 // are the fastest index within a job for L2 reuse across nearby poses.  Blocks
 // never wait on one another (the counter is only incremented), so a block that
-// finds no work simply exits.  Line-integral sum kernel, 16x16-pixel tiles; one
-// instantiation per voxel type, layout and sample loop, so the jobs of one
-// launch share those (the host groups them).
+// finds no work simply exits.  Line-integral sum kernel; each job in its own
+// block shape (MultiJobDrr::p.block_warps_x / warp_tall, tiles_x x tiles_y
+// tiles); one instantiation per voxel type, layout and sample loop, so the
+// jobs of one launch share those (the host groups them).
 template <int VT, int LAYOUT, int UNROLL>
 __global__ void __launch_bounds__(kThreads, UNROLL == kUnrollTrim4 ? kMinBlocksPerSM - 2 : kMinBlocksPerSM)
 drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long total, unsigned long long* counter) {
@@ -681,8 +682,11 @@ drr_multi_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long tota
     const int64_t proj = (int64_t)(local % nproj);
     const int tile = (int)(local / nproj);
     const int ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
-    const int col = tx * 16 + (warp & 1) * 8 + (lane & 7);
-    const int row = ty * 16 + (warp >> 1) * 4 + (lane >> 3);
+    // the job's block shape (as drr_kernel): bw warps across, each 8x4 pixels (4x8 when tall)
+    const int bw = J.p.block_warps_x, wl = J.p.warp_tall ? 2 : 3;
+    const int wc = 1 << wl, wr = 32 >> wl;
+    const int col = tx * (wc * bw) + (warp % bw) * wc + (lane & (wc - 1));
+    const int row = ty * ((8 / bw) * wr) + (warp / bw) * wr + (lane >> wl);
     unsigned int nl;
     if (col < J.p.cols && row < J.p.rows) trace_pixel<VT, XR_LINE_INT_SUM, LAYOUT, UNROLL>(J.p, proj, row, col, &nl);
   }
