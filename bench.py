@@ -733,7 +733,7 @@ def _multi_job(xr, dev, steps: int = 5, njobs: int = 8):
     """8 concurrent registrations of uneven size (volumes 192^3 .. 512x512x300,
     1-3 views, detector 4x or 8x downsampled, lambda 20-100; FP16 volumes), one
     population per job per optimizer step: one job-set call per step (geometry,
-    one persistent DRR launch, one batched grad-NCC launch), the fused job-set
+    one DRR launch, one batched grad-NCC launch), the fused job-set
     step beside it, and the same populations evaluated job by job."""
     from xreg_gb300 import synth
     specs = synth.uneven_job_specs(njobs, seed=4)

@@ -131,8 +131,9 @@ XR_API xr_status xr_log_remap(const float* d_src, int64_t rows, int64_t cols, in
 
 /* Job set: evaluates one population for each of several registrations (each an
  * xr_objective with its own volume, cameras, fixed images and population size)
- * with ONE persistent DRR launch over all their (tile, projection) work items,
- * followed by each job's metrics.  This is the multi-job batching of many
+ * with ONE DRR launch over all their (tile, projection) work items (each job
+ * in its autotuned block shape and sample loop), followed by one batched
+ * grad-NCC launch over every job's images.  This is the multi-job batching of many
  * concurrent Intensity2D3DRegiCMAES runs (each calls obj_fn per iteration,
  * xregIntensity2D3DRegi.cpp:571-742); xReg itself has no counterpart and runs
  * them one after another.  Values are identical to evaluating each objective
@@ -149,10 +150,12 @@ XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t num_jobs, const xr_objecti
 /* Same with device pointers; asynchronous on the job set's stream. */
 XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t num_jobs, const xr_objective* objs,
                                        const int64_t* pops, const double* const* d_xforms, float* const* d_sims);
-/* Work items and persistent blocks of the last launch. */
+/* Work items of the last step's DRR launches and blocks of the largest one
+ * (one block per item on the split path; the device-filling grid of the fused
+ * kernel). */
 XR_API xr_status xr_jobset_last_launch(xr_jobset js, int64_t* work_items, int32_t* blocks);
 /* Evaluation path of a job set.  0 (default): one geometry launch for every
- * job, one persistent DRR launch per (voxel type, layout) group, one batched
+ * job, one DRR launch per (voxel type, layout) group, one batched
  * grad-NCC launch over every job's images (with the per-image FP64 combine and
  * the mean over views): three launches for jobs of one voxel type.  1: one
  * geometry launch and one fused DRR + grad-NCC launch per group.  Jobs with

@@ -1,4 +1,4 @@
-"""Job sets: several registrations' populations in one persistent DRR launch.
+"""Job sets: several registrations' populations in one DRR launch.
 
 Uneven jobs (volume sizes, voxel types, layouts, views, detectors, metrics,
 population sizes) evaluated together must give exactly the values each gives
@@ -55,7 +55,7 @@ def test_jobset_equals_alone(xr, oracle):
     for a, m in zip(alone, mixed):
         np.testing.assert_array_equal(m, a)
     items, blocks = js.last_launch()
-    assert blocks >= 152 and items > 0
+    assert 0 < blocks <= items  # one block per (tile, projection) item of the largest voxel-type group
     # subsets in another order, other population sizes
     sub = [jobs[2], jobs[0]]
     p2 = [poses[2][:2], poses[0][:5]]

@@ -629,8 +629,8 @@ class PopulationObjective:
 # ------------------------------------------------------------------ job sets
 class JobSet:
     """One step of several registrations at once: one geometry launch, one
-    persistent DRR launch and one batched grad-NCC launch over every listed
-    objective's work (or the fused DRR + grad-NCC launch) (xr_jobset_*)."""
+    DRR launch and one batched grad-NCC launch over every listed objective's
+    work (or the fused DRR + grad-NCC launch) (xr_jobset_*)."""
 
     def __init__(self, device: int = -1):
         load()

@@ -2071,8 +2071,9 @@ static int metric_launches(const xr_simmetric_s* m) {
 //   fused: ONE persistent launch per (voxel type, layout) group traces every
 //     DRR tile and computes the grad-NCC of each image behind it
 //     (eval_fused_kernel), each job in its autotuned block shape;
-//   split: ONE persistent DRR launch per group (drr_multi_kernel, each job
-//     in its autotuned block shape), then ONE batched grad-NCC launch over every job's images
+//   split: ONE DRR launch per group whose grid covers every job's tiles
+//     (drr_jobs_kernel, each job in its autotuned block shape and loop), then
+//     ONE batched grad-NCC launch over every job's images
 //     (grad_multi_kernel, with the per-image combine and the mean over views).
 // Objectives whose metrics are not grad-NCC with 5x5 smoothing get their own
 // metric launches afterwards.  Values are copied to sims[i].  Everything is
@@ -2118,8 +2119,9 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     DrrParams& P = J.d.p;
     const bool cells = vol.cells.p != nullptr;
     const int32_t wide = cells ? (vol.type == XR_VOXEL_F32 ? 2 : XR_LAYOUT_CELL8) : XR_LAYOUT_LINEAR;
-    // each job in its autotuned block shape; the persistent kernels run the
-    // four-sample loop (the fused one the packed pairs where the tuner chose them)
+    // each job in its autotuned block shape and sample loop: the DRR job
+    // kernel runs loop 3 (for the tuner's 1 to 3), 4 (4, 5) or the packed 6,
+    // the fused kernel loop 4 or 6
     if (!rc_config_cached(rc, vol, P)) {  // the tuner times real launches: this caster's geometry first
       XR_CUDA_TRY(launch_proj_geom(vol.desc, rc->d_cams.as<xr_camera_desc>(), rc->d_xforms.as<double>(),
                                    rc->d_cam_idx.as<int32_t>(), rc->num_projs, rc->pose_count,
@@ -2127,7 +2129,7 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
       ++tuning_launches;
     }
     if ((st = rc_choose_config(rc, vol, P, s)) != XR_OK) return st;
-    P.unroll = (fused && P.unroll == 6 && cells) ? 6 : 4;
+    P.unroll = (P.unroll == 6 && cells) ? 6 : (!fused && P.unroll <= 3 ? 3 : 4);
     P.vol.layout = wide;
     const int wc = P.warp_tall ? 4 : 8, tw = wc * P.block_warps_x, th = (8 / P.block_warps_x) * (32 / wc);
     J.d.tiles_x = (int32_t)((P.cols + tw - 1) / tw);
@@ -2185,7 +2187,7 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
       J.cnt = obj->d_fcnt.as<unsigned int>();
     }
     fj.push_back(J);
-    key.push_back((vol.type * 4 + J.d.p.vol.layout) * 8 + J.d.p.unroll);
+    key.push_back((vol.type * 4 + J.d.p.vol.layout) * 8 + (fused ? J.d.p.unroll : 0));
   }
   // jobs ordered by group; item numbering restarts in each group
   std::vector<int32_t> keys(key);
@@ -2214,7 +2216,7 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     if (J.metric) total_tiles += (long long)J.nviews * J.pop * J.mt_x * J.mt_y;
   }
   // one descriptor upload: geometry jobs, jobs (group order), their DRR part
-  // alone (drr_multi_kernel's array), views
+  // alone (drr_jobs_kernel's array), views
   const size_t off_f = align16(gj.size() * sizeof(GeomJob));
   const size_t off_m = off_f + align16(fj.size() * sizeof(FusedJob));
   const size_t off_v = off_m + align16(fj.size() * sizeof(MultiJobDrr));
@@ -2250,11 +2252,12 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
                                     (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
                                     f0.d.p.vol.voxel_type, f0.d.p.vol.layout, f0.d.p.unroll,
                                     fw.d_counter.as<unsigned long long>(), &blocks, s));
-    else
-      XR_CUDA_TRY(launch_drr_multi(reinterpret_cast<const MultiJobDrr*>(d + off_m) + ranges[gi].first,
-                                   (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
-                                   f0.d.p.vol.voxel_type, f0.d.p.vol.layout, f0.d.p.unroll,
-                                   fw.d_counter.as<unsigned long long>(), &blocks, s));
+    else {
+      XR_CUDA_TRY(launch_drr_jobs(reinterpret_cast<const MultiJobDrr*>(d + off_m) + ranges[gi].first,
+                                  (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
+                                  f0.d.p.vol.voxel_type, f0.d.p.vol.layout, s));
+      blocks = (int)std::min<long long>(group_items[gi], 0x7fffffff);
+    }
     fw.items += group_items[gi];
     fw.blocks = std::max(fw.blocks, blocks);
     ++fw.launches;
@@ -2398,11 +2401,12 @@ extern "C" XR_API xr_status xr_obj_eval(xr_objective obj, int64_t pop, const dou
 }
 
 // ================================================================== job sets
-// Several registration objectives evaluated in one step: per job the poses are
-// copied in and its geometry kernel runs, then ONE persistent DRR launch covers
-// every job's (tile, projection) work items, then each job's metrics and mean
-// over views run and the values are copied out.  Everything is ordered on the
-// job set's stream.
+// Several registration objectives evaluated in one step (step_enqueue): every
+// job's poses are copied in, ONE geometry launch covers all jobs, ONE DRR
+// launch per (voxel type, layout) group covers every job's (tile, projection)
+// work items, ONE grad-NCC launch covers every job's images (per-image FP64
+// combine and mean over views included), and the values are copied out.
+// Everything is ordered on the job set's stream.
 struct xr_jobset_s {
   int device = 0;
   cudaStream_t own_stream = nullptr, ext_stream = nullptr;

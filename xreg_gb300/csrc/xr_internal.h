@@ -82,13 +82,11 @@ struct MultiJobDrr {
   long long item_begin;  // items of this job: [item_begin, item_begin + num_projs * tiles_x * tiles_y)
   int32_t tiles_x, tiles_y;
 };
-// Persistent kernel over the (tile, projection) items of jobs that share a voxel
-// type and layout, one grid filling the current device once; unroll 3 or 4 is
-// the sample loop (macro-cell trim, 2 or 4 samples per iteration); d_counter is
-// reset here.
-cudaError_t launch_drr_multi(const MultiJobDrr* d_jobs, int njobs, long long total_items, int32_t voxel_type,
-                             int32_t layout, int32_t unroll, unsigned long long* d_counter, int* blocks_out,
-                             cudaStream_t s);
+// One launch whose grid covers the (tile, projection) items of jobs sharing a
+// voxel type and layout (no work counter: one block per item); each job runs
+// its own sample loop, p.unroll 3, 4 or 6 (6 with the cell layouts only).
+cudaError_t launch_drr_jobs(const MultiJobDrr* d_jobs, int njobs, long long total_items, int32_t voxel_type,
+                            int32_t layout, cudaStream_t s);
 // Macro-cell occupancy bitmask of a volume (see VolView::occ); d_occ holds
 // ceil(nmx * nmy * nmz / 32) words and is cleared here.
 cudaError_t launch_build_occupancy(const float* vox_f32, int nx, int ny, int nz, uint32_t* d_occ, int nmx, int nmy,

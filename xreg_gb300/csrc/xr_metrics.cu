@@ -272,8 +272,30 @@ __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nb
 // Batched grad-NCC over many jobs' images (launch_grad_multi): one block per
 // 32x64 tile, grid-stride; the counters of FusedJob::cnt (images, then poses)
 // chain the per-image combine and the mean over views behind the tiles.
-__global__ void __launch_bounds__(kThreads) grad_multi_kernel(const FusedJob* __restrict__ jobs, int njobs,
-                                                              long long total) {
+// The last tile of an image combines its moments (FP64) and, the last view of
+// a pose, the mean over views; out of line so the tile loop keeps the
+// register budget of the per-view moments kernel (40 registers, 6 blocks per
+// SM, where the inlined FP64 combine took 80 and 3).
+__device__ __noinline__ void grad_multi_finish(const FusedJob& J, const FusedView& V, int64_t k, int mt, int64_t nimg,
+                                               double* dred) {
+  __threadfence();
+  const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy, dred);
+  if (threadIdx.x == 0) {
+    V.sims[k] = sim;
+    __threadfence();
+    unsigned int* cp = J.cnt + nimg * mt + nimg + k;
+    if (atomicAdd(cp, 1u) + 1u == (unsigned int)J.nviews) {  // every view of this pose
+      *cp = 0u;
+      __threadfence();
+      float sum = 0.0f;
+      for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
+      J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 6) grad_multi_kernel(const FusedJob* __restrict__ jobs, int njobs,
+                                                                 long long total) {
   __shared__ gt::GradTileSmem<2> sm;
   __shared__ double dred[6 * (gt::kFinalizeThreads / 32)];
   __shared__ int s_last;
@@ -300,22 +322,7 @@ __global__ void __launch_bounds__(kThreads) grad_multi_kernel(const FusedJob* __
       if (s_last) *ci = 0u;
     }
     __syncthreads();
-    if (s_last) {  // every tile of this image is in: its FP64 combine
-      __threadfence();
-      const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy, dred);
-      if (threadIdx.x == 0) {
-        V.sims[k] = sim;
-        __threadfence();
-        unsigned int* cp = J.cnt + nimg * mt + nimg + k;
-        if (atomicAdd(cp, 1u) + 1u == (unsigned int)J.nviews) {  // every view of this pose
-          *cp = 0u;
-          __threadfence();
-          float sum = 0.0f;
-          for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
-          J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
-        }
-      }
-    }
+    if (s_last) grad_multi_finish(J, V, k, mt, nimg, dred);  // every tile of this image is in
     __syncthreads();
   }
 }

@@ -10,8 +10,8 @@ pose, optimizer schedule) arrive at any time.  Each server step:
      worker thread while the active jobs keep stepping, and joins the steps
      once it has started;
   2. samples every active job's population (CMA-ES sample or trust-region ask),
-     evaluates all populations with one persistent DRR launch over every job's
-     (tile, pose) work followed by each job's metrics, and updates every
+     evaluates all populations with one DRR launch over every job's (tile,
+     pose) work and one batched grad-NCC launch, and updates every
      optimizer: one xr_regi_jobset_step call (native_step; otherwise the same
      steps driven from Python around one job-set evaluation);
   3. ends levels whose optimizer stopped (level change or completion) and
