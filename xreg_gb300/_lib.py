@@ -168,6 +168,10 @@ _SIGS = {
     "xr_cmaes_update_distribution": [H, P],
     "xr_cmaes_test_termination": [H, C.POINTER(i32)],
     "xr_cmaes_get": [H, P, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
+    "xr_cmaes_state_bytes": [H, C.POINTER(i64)],
+    "xr_cmaes_export_state": [H, P, i64],
+    "xr_cmaes_attach_device": [H, i32],
+    "xr_cmaes_detach_device": [H],
     "xr_dfo_create": [i32, P, P, P, f64, f64, i64, C.POINTER(H)],
     "xr_dfo_destroy": [H],
     "xr_dfo_ask": [H, P, C.POINTER(i32)],

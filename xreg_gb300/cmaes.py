@@ -25,6 +25,7 @@ class CMAES:
         self.n = int(x0.size)
         self.lam = int(lam)
         self._pop = np.zeros((self.lam, self.n))
+        self.on_device = False
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -68,6 +69,27 @@ class CMAES:
         r = C.c_int32()
         call("xr_cmaes_test_termination", self._h, C.byref(r))
         return STOP_REASONS.get(r.value, "unknown")
+
+    def attach_device(self, device: int = -1) -> None:
+        """Moves the state to device memory: the job-set step
+        (api.JobSet.regi_step) then draws and updates it inside its own
+        launches, with the same bits as the host methods (which refuse while
+        attached; state() and test_for_termination() read the device copy)."""
+        call("xr_cmaes_attach_device", self._h, int(device))
+        self.on_device = True
+
+    def detach_device(self) -> None:
+        """Brings the state back to host memory."""
+        call("xr_cmaes_detach_device", self._h)
+        self.on_device = False
+
+    def export_state(self) -> bytes:
+        """The whole state block (parameters, distribution, last population)."""
+        nb = C.c_int64()
+        call("xr_cmaes_state_bytes", self._h, C.byref(nb))
+        buf = (C.c_ubyte * nb.value)()
+        call("xr_cmaes_export_state", self._h, C.cast(buf, C.c_void_p), nb.value)
+        return bytes(buf)
 
     def state(self) -> dict:
         mean = np.zeros(self.n)

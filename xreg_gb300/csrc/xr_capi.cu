@@ -262,7 +262,7 @@ struct xr_simmetric_s {
 // Device descriptors and work counter of a fused evaluation step (see
 // fused_enqueue), owned by each objective and job set.
 struct FusedWork {
-  DevBuf d_desc, d_counter;
+  DevBuf d_desc, d_counter, d_report;  // d_report: CmaReport per job of a device-optimizer step
   std::vector<unsigned char> h_desc;  // staging: pageable, consumed by the copy call itself
   int blocks = 0;
   long long items = 0;
@@ -1257,19 +1257,21 @@ extern "C" XR_API xr_status xr_rc_last_num_loaded_samples(xr_raycaster rc, uint6
 }
 
 extern "C" XR_API xr_status xr_rc_distribute_xforms_device(xr_raycaster rc, int64_t n, const double* d_xf) {
-  XR_CHECK_ARG(rc, "distribute_xforms_device: NULL handle");
+  XR_CHECK_ARG(rc && d_xf, "distribute_xforms_device: NULL argument");
   DeviceGuard g(rc->device);
   return rc_distribute_device_on(rc, n, d_xf, rc->stream());
 }
 
-// distribute_xforms_among_cam_models with device poses, enqueued on stream s.
+// distribute_xforms_among_cam_models with device poses, enqueued on stream s;
+// d_xf NULL: the poses are written into the caster's transforms by a later
+// launch on s (a device optimizer's sampling).
 static xr_status rc_distribute_device_on(xr_raycaster rc, int64_t n, const double* d_xf, cudaStream_t s) {
-  XR_CHECK_ARG(rc && d_xf && n > 0, "distribute_xforms_device: NULL argument");
+  XR_CHECK_ARG(rc && n > 0, "distribute_xforms_device: NULL argument");
   XR_CHECK_ARG(!rc->cams.empty(), "distribute_xforms_device: no camera models");
   XR_CHECK_ARG(rc->allocated, "distribute_xforms_device: allocate_resources first");
   XR_CHECK_ARG(n * (int64_t)rc->cams.size() == rc->num_projs,
                "distribute_xforms_device: num_xforms * num_cams must equal num_projs");
-  XR_CUDA_TRY(cudaMemcpyAsync(rc->d_xforms.p, d_xf, (size_t)n * 16 * 8, cudaMemcpyDeviceToDevice, s));
+  if (d_xf) XR_CUDA_TRY(cudaMemcpyAsync(rc->d_xforms.p, d_xf, (size_t)n * 16 * 8, cudaMemcpyDeviceToDevice, s));
   rc->pose_count = n;
   rc->xforms_dirty = false;
   rc->xforms_on_device = true;
@@ -2080,8 +2082,17 @@ static int metric_launches(const xr_simmetric_s* m) {
 // ordered on stream s.  Both ways give identical values.
 static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_objective* objs, const int64_t* pops,
                               const double* const* xforms, bool host_in, float* const* sims, bool host_out,
-                              cudaStream_t s, bool fused) {
+                              cudaStream_t s, bool fused, const CmaStepJob* cma = nullptr) {
   XR_CHECK_ARG(objs && pops && xforms && sims && n > 0, "evaluation: NULL argument or no jobs");
+  auto dev_opt = [&](int32_t i) { return cma != nullptr && cma[i].state != nullptr; };
+  bool any_dev = false;
+  for (int32_t i = 0; i < n; ++i) any_dev = any_dev || dev_opt(i);
+  if (any_dev) {
+    XR_CUDA_TRY(fw.d_report.reserve((size_t)n * sizeof(CmaReport)));
+    XR_CUDA_TRY(cudaMemsetAsync(fw.d_report.p, 0, (size_t)n * sizeof(CmaReport), s));
+  }
+  CmaReport* d_report = any_dev ? fw.d_report.as<CmaReport>() : nullptr;
+  std::vector<CmaUpdateJob> cu;  // device optimizers whose update has a launch of its own
   std::vector<GeomJob> gj;
   std::vector<FusedJob> fj;
   std::vector<std::vector<FusedView>> fv((size_t)n);
@@ -2096,16 +2107,22 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     for (int32_t k = 0; k < i; ++k) XR_CHECK_ARG(objs[k] != obj, "evaluation: an objective is listed twice");
     const int64_t pop = pops[i];
     XR_CHECK_ARG(pop > 0 && pop <= obj->max_pop, "evaluation: population outside [1, max_pop]");
-    XR_CHECK_ARG(xforms[i] && sims[i], "evaluation: NULL pose or value pointer");
-    if (host_in) XR_CHECK_ARG(finite_all(xforms[i], 16 * pop), "evaluation: non-finite transform");
-    if (xforms[i] != obj->d_poses.as<double>())
-      XR_CUDA_TRY(cudaMemcpyAsync(obj->d_poses.p, xforms[i], (size_t)pop * 16 * 8,
-                                  host_in ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    const bool dopt = dev_opt(i);
+    if (dopt) {  // candidates drawn on the device by the geometry launch
+      XR_CHECK_ARG(cma[i].lam == pop && cma[i].dim >= 1 && cma[i].dim <= kCmaDeviceMaxDim,
+                   "evaluation: a device optimizer's population must be its lambda");
+    } else {
+      XR_CHECK_ARG(xforms[i] && sims[i], "evaluation: NULL pose or value pointer");
+      if (host_in) XR_CHECK_ARG(finite_all(xforms[i], 16 * pop), "evaluation: non-finite transform");
+      if (xforms[i] != obj->d_poses.as<double>())
+        XR_CUDA_TRY(cudaMemcpyAsync(obj->d_poses.p, xforms[i], (size_t)pop * 16 * 8,
+                                    host_in ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    }
     xr_raycaster rc = obj->rc;
     const int32_t nv = (int32_t)obj->metrics.size();
     xr_status st = xr_rc_set_num_projs(rc, (int64_t)nv * pop);
     if (st != XR_OK) return st;
-    if ((st = rc_distribute_device_on(rc, pop, obj->d_poses.as<double>(), s)) != XR_OK) return st;
+    if ((st = rc_distribute_device_on(rc, pop, dopt ? nullptr : obj->d_poses.as<double>(), s)) != XR_OK) return st;
     rc->store = XR_PROJ_STORE_REPLACE;  // use_proj_store_replace_method (xregIntensity2D3DRegi.cpp:598)
     FusedJob J{};
     if ((st = rc_prepare(rc, obj->vol_idx, s, J.d.p, false)) != XR_OK) return st;
@@ -2147,6 +2164,13 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     G.pose_stride = rc->pose_count;
     G.first = first;
     G.out = rc->d_geo.as<ProjGeom>();
+    if (dopt) {
+      G.cma = cma[i].state;
+      G.report = d_report + i;
+      std::memcpy(G.C, cma[i].C, sizeof(G.C));
+      std::memcpy(G.B, cma[i].B, sizeof(G.B));
+      std::memcpy(G.bounds, cma[i].bounds, sizeof(G.bounds));
+    }
     first += rc->num_projs;
     gj.push_back(G);
     // the metric behind the DRR
@@ -2177,8 +2201,14 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
         fv[(size_t)i].push_back(V);
       }
     }
+    if (dopt) {
+      J.report = d_report + i;
+      if (!fused && J.metric) J.cma = cma[i].state;  // updated by the batched grad-NCC launch
+      else cu.push_back(CmaUpdateJob{cma[i].state, obj->d_sims.as<float>(), d_report + i});
+    }
     if (J.metric) {
-      const size_t words = (size_t)obj->max_pop * nv * (size_t)(J.mt_x * J.mt_y + 1) + (size_t)obj->max_pop;
+      // per metric tile, per image, per pose, and one for the job (its optimizer's update)
+      const size_t words = (size_t)obj->max_pop * nv * (size_t)(J.mt_x * J.mt_y + 1) + (size_t)obj->max_pop + 1;
       if (obj->fcnt_words < words) {
         XR_CUDA_TRY(obj->d_fcnt.reserve(words * 4));
         XR_CUDA_TRY(cudaMemsetAsync(obj->d_fcnt.p, 0, words * 4, s));
@@ -2222,7 +2252,8 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
   const size_t off_v = off_m + align16(fj.size() * sizeof(MultiJobDrr));
   size_t nviews_total = 0;
   for (auto& v : fv) nviews_total += v.size();
-  const size_t bytes = off_v + nviews_total * sizeof(FusedView) + 16;
+  const size_t off_u = off_v + align16(nviews_total * sizeof(FusedView));
+  const size_t bytes = off_u + cu.size() * sizeof(CmaUpdateJob) + 16;
   XR_CUDA_TRY(fw.d_desc.reserve(bytes));
   XR_CUDA_TRY(fw.d_counter.reserve(256));
   fw.h_desc.assign(bytes, 0);
@@ -2239,6 +2270,7 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     std::memcpy(h + off_f + r * sizeof(FusedJob), &J, sizeof(FusedJob));
     std::memcpy(h + off_m + r * sizeof(MultiJobDrr), &J.d, sizeof(MultiJobDrr));
   }
+  if (!cu.empty()) std::memcpy(h + off_u, cu.data(), cu.size() * sizeof(CmaUpdateJob));
   XR_CUDA_TRY(cudaMemcpyAsync(fw.d_desc.p, h, bytes, cudaMemcpyHostToDevice, s));
   XR_CUDA_TRY(launch_proj_geom_jobs(reinterpret_cast<const GeomJob*>(d), (int)gj.size(), first, s));
   fw.launches = 1 + tuning_launches;
@@ -2285,9 +2317,13 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
       XR_CUDA_TRY(launch_combine_mean(view_sims, nv, pops[i], obj->d_sims.as<float>(), s));
       fw.launches += nv * metric_launches(obj->metrics[0]) + 1;
     }
-    if (sims[i] != obj->d_sims.as<float>())
+    if (sims[i] && sims[i] != obj->d_sims.as<float>())
       XR_CUDA_TRY(cudaMemcpyAsync(sims[i], obj->d_sims.p, (size_t)pops[i] * 4,
                                   host_out ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  }
+  if (!cu.empty()) {  // device optimizers whose values came from other launches
+    XR_CUDA_TRY(launch_cma_updates(reinterpret_cast<const CmaUpdateJob*>(d + off_u), (int)cu.size(), s));
+    ++fw.launches;
   }
   return XR_OK;
 }
@@ -2415,6 +2451,8 @@ struct xr_jobset_s {
   long long last_items = 0;
   unsigned int* h_err = nullptr;  // pinned: every job's step-guard flag, read with one synchronisation
   size_t h_err_cap = 0;
+  CmaReport* h_report = nullptr;  // pinned: device optimizers' reports of the last step
+  size_t h_report_cap = 0;
   // 0 (default): geometry, DRR and batched grad-NCC launches for every job;
   // 1: fused evaluation step
   int32_t step_mode = 0;
@@ -2443,6 +2481,7 @@ extern "C" XR_API xr_status xr_jobset_destroy(xr_jobset js) {
   cudaStreamSynchronize(js->stream());
   cudaStreamDestroy(js->own_stream);
   if (js->h_err) cudaFreeHost(js->h_err);
+  if (js->h_report) cudaFreeHost(js->h_report);
   delete js;
   return XR_OK;
 }
@@ -2467,11 +2506,9 @@ static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* obj
   return st;
 }
 
-extern "C" XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
-                                           const double* const* host_xforms, float* const* host_sims) {
-  xr_status st = jobset_enqueue(js, n, objs, pops, host_xforms, true, host_sims, true);
-  if (st != XR_OK) return st;
-  DeviceGuard g(js->device);
+// Waits for a step enqueued on the job set's stream (after `extra` copies of
+// its own were enqueued) and turns a job's step-guard flag into an error.
+static xr_status jobset_finish(xr_jobset js, int32_t n, const xr_objective* objs, const char* who) {
   if (js->h_err_cap < (size_t)n) {
     if (js->h_err) cudaFreeHost(js->h_err);
     js->h_err = nullptr;
@@ -2488,11 +2525,59 @@ extern "C" XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t n, const xr_obj
     xr_raycaster rc = objs[i]->rc;
     if (js->h_err[i]) {
       cudaMemset(rc->d_counters.as<char>() + 8, 0, sizeof(unsigned int));
-      return fail(XR_ERR_DEVICE_CHECK, "xr_jobset_eval: a job's rays exceeded the step-count guard");
+      return fail(XR_ERR_DEVICE_CHECK, std::string(who) + ": a job's rays exceeded the step-count guard");
     }
   }
   return XR_OK;
 }
+
+extern "C" XR_API xr_status xr_jobset_eval(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
+                                           const double* const* host_xforms, float* const* host_sims) {
+  xr_status st = jobset_enqueue(js, n, objs, pops, host_xforms, true, host_sims, true);
+  if (st != XR_OK) return st;
+  DeviceGuard g(js->device);
+  return jobset_finish(js, n, objs, "xr_jobset_eval");
+}
+
+namespace xr {
+xr_status jobset_step_cma(xr_jobset js, int32_t n, const xr_objective* objs, const int64_t* pops,
+                          const double* const* host_xforms, float* const* host_sims, const CmaStepJob* cma,
+                          CmaReport* reports) {
+  XR_CHECK_ARG(js && objs && pops && host_xforms && host_sims && cma && reports && n > 0,
+               "regi_jobset_step: NULL argument or no jobs");
+  DeviceGuard g(js->device);
+  cudaStream_t s = js->stream();
+  bool any_dev = false;
+  for (int32_t i = 0; i < n; ++i) {
+    if (!cma[i].state) continue;
+    any_dev = true;
+    void* st_ptr = cma[i].state;
+    cudaPointerAttributes pa{};
+    XR_CUDA_TRY(cudaPointerGetAttributes(&pa, st_ptr));
+    XR_CHECK_ARG(pa.type == cudaMemoryTypeDevice && pa.device == js->device,
+                 "regi_jobset_step: a device optimizer lives on another device than the job set");
+  }
+  xr_status st = step_enqueue(js->fw, js->device, n, objs, pops, host_xforms, true, host_sims, true, s,
+                              js->step_mode == 1, cma);
+  js->last_items = js->fw.items;
+  js->blocks = js->fw.blocks;
+  if (st != XR_OK) return st;
+  if (any_dev) {
+    if (js->h_report_cap < (size_t)n) {
+      if (js->h_report) cudaFreeHost(js->h_report);
+      js->h_report = nullptr;
+      js->h_report_cap = 0;
+      XR_CUDA_TRY(cudaMallocHost(&js->h_report, (size_t)n * sizeof(CmaReport)));
+      js->h_report_cap = (size_t)n;
+    }
+    XR_CUDA_TRY(cudaMemcpyAsync(js->h_report, js->fw.d_report.p, (size_t)n * sizeof(CmaReport),
+                                cudaMemcpyDeviceToHost, s));
+  }
+  if ((st = jobset_finish(js, n, objs, "regi_jobset_step")) != XR_OK) return st;
+  for (int32_t i = 0; i < n; ++i) reports[i] = any_dev ? js->h_report[i] : CmaReport{0, 0};
+  return XR_OK;
+}
+}  // namespace xr
 
 extern "C" XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t n, const xr_objective* objs,
                                                   const int64_t* pops, const double* const* d_xforms,

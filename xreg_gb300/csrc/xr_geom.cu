@@ -8,6 +8,7 @@
 // with the pinhole in index coordinates.  The arithmetic is xf:: (xr_xfloat.h):
 // float, explicitly rounded, in Eigen's evaluation order, so per-ray step counts
 // and sample positions follow the reference's float geometry bit for bit.
+#include "xr_cmaes_core.h"
 #include "xr_internal.h"
 
 namespace xr {
@@ -38,6 +39,35 @@ __global__ void proj_geom_kernel(xf::Affine phys_to_idx, const xr_camera_desc* _
   out[p] = g;
 }
 
+// Candidate k of a device CMA-ES job (cmaes_SamplePopulation, then
+// cmaes_ReSampleSingle while outside the bounds, xregIntensity2D3DRegiCMAES.cpp:154-191)
+// and its pose.  Every view's projection of candidate k draws the same bits;
+// the first view's (owner) stores the candidate, its draw count and its pose.
+__device__ __noinline__ void sample_candidate(const GeomJob& J, int64_t k, bool owner, double* pose_out) {
+  const cma::View s = cma::view(J.cma);
+  const int n = s.h->n;
+  double z[kCmaDeviceMaxDim], x[kCmaDeviceMaxDim];
+  int attempt = 0;
+  for (;; ++attempt) {
+    cma::draw(s, (int)k, attempt, z, x);
+    if (cma::inside(x, J.bounds, n)) break;
+    if (attempt > kCmaMaxRedraws) {
+      if (owner) J.report->sample_error = 1;
+      break;
+    }
+  }
+  pose::map(J.C, J.B, x, pose_out);
+  if (owner) {
+    for (int i = 0; i < n; ++i) {
+      s.z[k * n + i] = z[i];
+      s.pop[k * n + i] = x[i];
+    }
+    s.att[k] = attempt;
+    for (int i = 0; i < 16; ++i) J.poses[16 * k + i] = pose_out[i];
+    if (k == 0) s.h->sampled = 1;
+  }
+}
+
 // One thread per projection of every job (jobs in order of `first`).
 __global__ void proj_geom_jobs_kernel(const GeomJob* __restrict__ jobs, int njobs, int64_t total) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -52,7 +82,13 @@ __global__ void proj_geom_jobs_kernel(const GeomJob* __restrict__ jobs, int njob
   for (int k = 0; k < 16; ++k) cam.E[k] = __double2float_rn(cd.extrins[k]);
   cam.focal_len = __double2float_rn(cd.focal_len);
   cam.frame = cd.coord_frame_type;
-  const double* pd = J.poses + 16 * (p % J.pose_stride);
+  const int64_t k = p % J.pose_stride;
+  double drawn[16];
+  const double* pd = J.poses + 16 * k;
+  if (J.cma) {
+    sample_candidate(J, k, p < J.pose_stride, drawn);
+    pd = drawn;
+  }
   xf::Affine pose;
   for (int i = 0; i < 3; ++i) {
     for (int jj = 0; jj < 3; ++jj) pose.L[i * 3 + jj] = __double2float_rn(pd[i * 4 + jj]);

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "xreg_gb300.h"
+#include "xr_step.h"
 #include "xr_xfloat.h"
 
 namespace xr {
@@ -135,6 +136,8 @@ struct FusedJob {
   float* out;             // [pop] mean over views
   unsigned int* cnt;
   long long tile_begin;   // first metric tile of this job in a batched metric launch
+  void* cma;              // CMA-ES state updated by the batched grad-NCC launch once every pose has its value
+  CmaReport* report;      // where that update reports its termination code
 };
 // One persistent launch over the jobs of one (voxel type, layout) group.
 cudaError_t launch_eval_fused(const FusedJob* d_jobs, int njobs, long long total_items, int32_t voxel_type,
@@ -143,17 +146,32 @@ cudaError_t launch_eval_fused(const FusedJob* d_jobs, int njobs, long long total
 // Grad-NCC (5x5 smoothing) of every image of the jobs with `metric` set, their
 // DRRs already written: one launch over all their 32x64 tiles (the split
 // path's tile code), each image's FP64 combine by the block that completes its
-// tiles, each pose's mean over views by the block that completes its views.
+// tiles, each pose's mean over views by the block that completes its views,
+// and (jobs with `cma`) the CMA-ES update by the block that completes the
+// job's last pose.
 cudaError_t launch_grad_multi(const FusedJob* d_jobs, int njobs, long long total_tiles, cudaStream_t s);
 // Geometry of many ray casters' projections in one launch.
 struct GeomJob {
   xf::Affine p2i;
   const xr_camera_desc* cams;
-  const double* poses;
+  double* poses;          // [pose_stride] read, or written when cma is set
   const int32_t* cam_idx;
   int64_t num_projs, pose_stride, first;  // first: index of this job's first projection over all jobs
   ProjGeom* out;
+  // set: candidate (p % pose_stride) of the CMA-ES state `cma` is drawn here
+  // (redrawn until inside `bounds`) and its pose C Exp(x) B written to poses
+  void* cma;
+  CmaReport* report;
+  double C[16], B[16], bounds[kCmaDeviceMaxDim];
 };
+// CMA-ES updates of device-optimizer jobs whose values come from other
+// launches (one block per job).
+struct CmaUpdateJob {
+  void* cma;
+  const float* vals;  // [lambda]
+  CmaReport* report;
+};
+cudaError_t launch_cma_updates(const CmaUpdateJob* d_jobs, int njobs, cudaStream_t s);
 cudaError_t launch_proj_geom_jobs(const GeomJob* d_jobs, int njobs, int64_t total_projs, cudaStream_t s);
 
 struct PatchFixed {         // per direction

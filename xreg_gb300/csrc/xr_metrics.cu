@@ -17,6 +17,7 @@
 // patch centre, two-pass mean / sample std dev over the (2r+1)^2 window from a
 // shared-memory tile, score 1 - sum((m - mu_m)/sd_m * fhat), unit weights, mean
 // over patches.  The fixed side (per-patch mean and 1/(sd n)) is pre-computed once.
+#include "xr_cmaes_core.h"
 #include "xr_gradtile.cuh"
 
 #include <cfloat>
@@ -272,6 +273,21 @@ __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nb
 // Batched grad-NCC over many jobs' images (launch_grad_multi): one block per
 // 32x64 tile, grid-stride; the counters of FusedJob::cnt (images, then poses)
 // chain the per-image combine and the mean over views behind the tiles.
+// A device CMA-ES job's update from its lambda values (the float means over
+// views, widened to double as the host step does): cmaes_UpdateDistribution,
+// then cmaes_TestForTermination, whose code goes to the state and the report.
+__device__ __noinline__ void cma_update_device(void* state, const float* vals, CmaReport* report) {
+  const cma::View s = cma::view(state);
+  const int lam = s.h->lam;
+  for (int k = 0; k < lam; ++k) s.fv[k] = (double)__ldcg(vals + k);
+  cma::update(s);
+  if (report) report->reason = s.h->reason;
+}
+
+__global__ void cma_update_kernel(const CmaUpdateJob* __restrict__ jobs) {
+  if (threadIdx.x == 0) cma_update_device(jobs[blockIdx.x].cma, jobs[blockIdx.x].vals, jobs[blockIdx.x].report);
+}
+
 // The last tile of an image combines its moments (FP64) and, the last view of
 // a pose, the mean over views; out of line so the tile loop keeps the
 // register budget of the per-view moments kernel (40 registers, 6 blocks per
@@ -290,6 +306,15 @@ __device__ __noinline__ void grad_multi_finish(const FusedJob& J, const FusedVie
       float sum = 0.0f;
       for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
       J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
+      if (J.cma) {  // the job's last pose: its optimizer's update
+        __threadfence();
+        unsigned int* cj = J.cnt + nimg * mt + nimg + J.pop;
+        if (atomicAdd(cj, 1u) + 1u == (unsigned int)J.pop) {
+          *cj = 0u;
+          __threadfence();
+          cma_update_device(J.cma, J.out, J.report);
+        }
+      }
     }
   }
 }
@@ -864,6 +889,12 @@ cudaError_t launch_grad_multi(const FusedJob* d_jobs, int njobs, long long total
   if (e != cudaSuccess) return e;
   const long long cap = (long long)sms * (per_sm > 0 ? per_sm : 1);
   grad_multi_kernel<<<(unsigned)(total < cap ? total : cap), kThreads, 0, s>>>(d_jobs, njobs, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cma_updates(const CmaUpdateJob* d_jobs, int njobs, cudaStream_t s) {
+  if (njobs <= 0) return cudaSuccess;
+  cma_update_kernel<<<(unsigned)njobs, 32, 0, s>>>(d_jobs);
   return cudaGetLastError();
 }
 

@@ -19,6 +19,8 @@
 #include <string>
 #include <vector>
 
+#include "xr_cmaes_core.h"
+#include "xr_step.h"
 #include "xreg_gb300.h"
 #include "xreg_gb300_regi.h"
 
@@ -28,66 +30,17 @@ xr_status fail(xr_status code, const std::string& msg);
 
 namespace {
 
-using M4 = double[16];
-
-void mat_mul(const double* a, const double* b, double* out) {
-  double t[16];
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) {
-      double s = 0.0;
-      for (int k = 0; k < 4; ++k) s += a[i * 4 + k] * b[k * 4 + j];
-      t[i * 4 + j] = s;
-    }
-  std::memcpy(out, t, sizeof(t));
-}
-
-// Inverse of a rigid transform [R t; 0 1]: [R^T, -R^T t].
-void rigid_inverse(const double* m, double* out) {
-  double t[16] = {0};
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) t[i * 4 + j] = m[j * 4 + i];
-  for (int i = 0; i < 3; ++i) t[i * 4 + 3] = -(t[i * 4 + 0] * m[3] + t[i * 4 + 1] * m[7] + t[i * 4 + 2] * m[11]);
-  t[15] = 1.0;
-  std::memcpy(out, t, sizeof(t));
-}
-
-void exp_se3(const double* x, double* out) {
-  const double w[3] = {x[0], x[1], x[2]}, v[3] = {x[3], x[4], x[5]};
-  const double th = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-  double W[9] = {0.0, -w[2], w[1], w[2], 0.0, -w[0], -w[1], w[0], 0.0};
-  double WW[9];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double s = 0.0;
-      for (int k = 0; k < 3; ++k) s += W[i * 3 + k] * W[k * 3 + j];
-      WW[i * 3 + j] = s;
-    }
-  double R[9], A[9];
-  const bool big = th > 1.0e-14;
-  const double a = big ? std::sin(th) / th : 1.0;
-  const double b = big ? (1.0 - std::cos(th)) / (th * th) : 0.0;
-  const double c = big ? (th - std::sin(th)) / (th * th * th) : 0.0;
-  for (int i = 0; i < 9; ++i) {
-    const double id = (i % 4 == 0) ? 1.0 : 0.0;
-    R[i] = big ? id + a * W[i] + b * WW[i] : id;
-    A[i] = big ? id + b * W[i] + c * WW[i] : id;
-  }
-  std::memset(out, 0, 16 * sizeof(double));
-  for (int i = 0; i < 3; ++i) {
-    for (int j = 0; j < 3; ++j) out[i * 4 + j] = R[i * 3 + j];
-    out[i * 4 + 3] = A[i * 3 + 0] * v[0] + A[i * 3 + 1] * v[1] + A[i * 3 + 2] * v[2];
-  }
-  out[15] = 1.0;
-}
-
+// pose(x) = C Exp(x) B with B = C^-1 start (the shared host/device map of
+// xr_cmaes_core.h, so host and device candidates give the same poses)
 struct PoseMap {
-  double C[16], B[16];  // pose(x) = C * Exp(x) * B,  B = C^-1 * start
-  void operator()(const double* x, double* out) const {
-    double E[16], CE[16];
-    exp_se3(x, E);
-    mat_mul(C, E, CE);
-    mat_mul(CE, B, out);
+  double C[16], B[16];
+  PoseMap(const double* centre, const double* start) {
+    std::memcpy(C, centre, sizeof(C));
+    double Ci[16];
+    xr::pose::rigid_inverse(centre, Ci);
+    xr::pose::mat_mul4(Ci, start, B);
   }
+  void operator()(const double* x, double* out) const { xr::pose::map(C, B, x, out); }
 };
 
 bool finite6(const double* v) {
@@ -136,13 +89,7 @@ extern "C" XR_API xr_status xr_regi_run_level(xr_objective obj, const double* ce
   if (!obj || !centre || !start_pose || !p || !best_pose)
     return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: NULL argument");
   if (p->max_iters <= 0) return fail(XR_ERR_INVALID_ARG, "xr_regi_run_level: max_iters must be positive");
-  PoseMap map;
-  std::memcpy(map.C, centre, sizeof(map.C));
-  {
-    double Ci[16];
-    rigid_inverse(centre, Ci);
-    mat_mul(Ci, start_pose, map.B);
-  }
+  const PoseMap map(centre, start_pose);
   const double zero[6] = {0, 0, 0, 0, 0, 0};
   std::vector<double> poses, pop;
   std::vector<float> sims;
@@ -229,11 +176,7 @@ extern "C" XR_API xr_status xr_regi_pose_map(const double* centre, const double*
                                              const double* xs, double* poses) {
   if (!centre || !start_pose || n < 0 || (n > 0 && (!xs || !poses)))
     return fail(XR_ERR_INVALID_ARG, "regi_pose_map: NULL argument or negative count");
-  PoseMap map;
-  std::memcpy(map.C, centre, sizeof(map.C));
-  double Ci[16];
-  rigid_inverse(centre, Ci);
-  mat_mul(Ci, start_pose, map.B);
+  const PoseMap map(centre, start_pose);
   for (int64_t k = 0; k < n; ++k) map(xs + k * 6, poses + k * 16);
   return XR_OK;
 }
@@ -247,15 +190,33 @@ extern "C" XR_API xr_status xr_regi_jobset_step(xr_jobset js, int32_t n, const x
   std::vector<int64_t> pops((size_t)n);
   std::vector<const double*> pp((size_t)n);
   std::vector<float*> vp((size_t)n);
+  std::vector<CmaStepJob> cj((size_t)n);
+  std::vector<CmaReport> reports((size_t)n);
   xr_status st = XR_OK;
-  // sample (or ask) every job's candidates and map them to poses
+  // sample (or ask) every host optimizer's candidates and map them to poses;
+  // an optimizer attached to the device samples inside the step
   for (int32_t j = 0; j < n; ++j) {
     const xr_regi_step_job& J = jobs[j];
     if (!J.obj || !J.opt) return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: job without objective or optimizer");
+    objs[(size_t)j] = J.obj;
     int32_t pop = 0;
     if (J.optimizer == XR_REGI_CMAES) {
       xr_cmaes es = static_cast<xr_cmaes>(J.opt);
-      int32_t lam = 0;
+      int32_t lam = 0, dim = 0, dev = 0;
+      void* d_state = nullptr;
+      if (cmaes_device_state(es, &d_state, &lam, &dim, &dev)) {
+        if (dim != 6) return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: a pose optimizer has 6 parameters");
+        CmaStepJob& c = cj[(size_t)j];
+        const PoseMap map(J.centre, J.start_pose);
+        c.state = d_state;
+        std::memcpy(c.C, map.C, sizeof(c.C));
+        std::memcpy(c.B, map.B, sizeof(c.B));
+        for (int i = 0; i < 6; ++i) c.bounds[i] = J.bounds[i];
+        c.lam = lam;
+        c.dim = dim;
+        pops[(size_t)j] = lam;
+        continue;
+      }
       if ((st = xr_cmaes_lambda(es, &lam)) != XR_OK) return st;
       pop = lam;
       xs[(size_t)j].resize((size_t)pop * 6);
@@ -265,11 +226,8 @@ extern "C" XR_API xr_status xr_regi_jobset_step(xr_jobset js, int32_t n, const x
       for (int i = 0; i < 6; ++i) bounded = bounded || J.bounds[i] > 0.0;
       for (int32_t k = 0; bounded && k < pop; ++k) {
         for (int tries = 0;; ++tries) {
-          bool inside = true;
-          for (int i = 0; i < 6; ++i)
-            if (J.bounds[i] > 0.0 && std::fabs(x[(size_t)k * 6 + i]) > J.bounds[i]) inside = false;
-          if (inside) break;
-          if (tries > 100000)
+          if (cma::inside(x + (size_t)k * 6, J.bounds, 6)) break;
+          if (tries > kCmaMaxRedraws)
             return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: could not sample a candidate inside the bounds");
           if ((st = xr_cmaes_resample_single(es, k, x)) != XR_OK) return st;
         }
@@ -280,33 +238,34 @@ extern "C" XR_API xr_status xr_regi_jobset_step(xr_jobset js, int32_t n, const x
     } else {
       return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: unknown optimizer");
     }
-    PoseMap map;
-    std::memcpy(map.C, J.centre, sizeof(map.C));
-    {
-      double Ci[16];
-      rigid_inverse(J.centre, Ci);
-      mat_mul(Ci, J.start_pose, map.B);
-    }
+    const PoseMap map(J.centre, J.start_pose);
     poses[(size_t)j].resize((size_t)pop * 16);
     for (int32_t k = 0; k < pop; ++k)
       map(xs[(size_t)j].data() + (size_t)k * 6, poses[(size_t)j].data() + (size_t)k * 16);
     vals[(size_t)j].resize((size_t)pop);
-    objs[(size_t)j] = J.obj;
     pops[(size_t)j] = pop;
     pp[(size_t)j] = poses[(size_t)j].data();
     vp[(size_t)j] = vals[(size_t)j].data();
   }
-  if ((st = xr_jobset_eval(js, n, objs.data(), pops.data(), pp.data(), vp.data())) != XR_OK) return st;
-  // update every optimizer and test it for termination
+  if ((st = jobset_step_cma(js, n, objs.data(), pops.data(), pp.data(), vp.data(), cj.data(), reports.data())) !=
+      XR_OK)
+    return st;
+  // update every host optimizer and test it for termination; a device
+  // optimizer was updated inside the step
   for (int32_t j = 0; j < n; ++j) {
     const xr_regi_step_job& J = jobs[j];
-    std::vector<double> f(vals[(size_t)j].begin(), vals[(size_t)j].end());
     int32_t reason = 0;
-    if (J.optimizer == XR_REGI_CMAES) {
+    if (cj[(size_t)j].state) {
+      if (reports[(size_t)j].sample_error)
+        return fail(XR_ERR_INVALID_ARG, "regi_jobset_step: could not sample a candidate inside the bounds");
+      reason = reports[(size_t)j].reason;
+    } else if (J.optimizer == XR_REGI_CMAES) {
+      std::vector<double> f(vals[(size_t)j].begin(), vals[(size_t)j].end());
       xr_cmaes es = static_cast<xr_cmaes>(J.opt);
       if ((st = xr_cmaes_update_distribution(es, f.data())) != XR_OK) return st;
       if ((st = xr_cmaes_test_termination(es, &reason)) != XR_OK) return st;
     } else {
+      std::vector<double> f(vals[(size_t)j].begin(), vals[(size_t)j].end());
       xr_dfo d = static_cast<xr_dfo>(J.opt);
       if ((st = xr_dfo_tell(d, f.data())) != XR_OK) return st;
       if ((st = xr_dfo_test_termination(d, &reason)) != XR_OK) return st;

@@ -72,7 +72,8 @@ class LevelResult:
 
 class Registration:
     def __init__(self, vol: api.Volume, levels: list, init_pose: np.ndarray, step: float = 0.5,
-                 voxel_type: int = 0, seed: int = 0, device: int = -1, name: str = ""):
+                 voxel_type: int = 0, seed: int = 0, device: int = -1, name: str = "",
+                 device_optimizer: bool = False):
         self.vol = vol
         self.levels = list(levels)
         self.init_pose = np.asarray(init_pose, dtype=np.float64)
@@ -81,6 +82,9 @@ class Registration:
         self.seed = int(seed)
         self.device = device
         self.name = name
+        # CMA-ES levels keep their optimizer state in device memory, sampled and
+        # updated inside the job-set step (stepped by xr_regi_jobset_step only)
+        self.device_optimizer = bool(device_optimizer)
         self.C = vol.xform_img_center_to_itk_phys()
         self.Ci = np.linalg.inv(self.C)
         self.rc = None
@@ -152,6 +156,8 @@ class Registration:
             self.obj = api.PopulationObjective(self.rc, ms, L.pop)
             self.es = CMAES(np.zeros(6), L.sigma, L.pop, seed=self.seed * 1009 + k)
             self.es.set_stop(tol_fun=L.tol_fun, tol_x=L.tol_x, max_iter=L.max_iters)
+            if self.device_optimizer:
+                self.es.attach_device(self.device)
 
     def poses_of(self, xs: np.ndarray) -> np.ndarray:
         # the library's map, so a job stepped natively (xr_regi_jobset_step)
@@ -165,6 +171,8 @@ class Registration:
         if L.optimizer == "dfo":
             self._pop_x = self.es.ask()
         else:
+            if self.es.on_device:
+                raise RuntimeError("propose: this level's optimizer lives on the device; step it with JobSet.regi_step")
             self._pop_x = self.es.sample_within_bounds(L.bounds).copy()
         return self.poses_of(self._pop_x)
 
@@ -229,10 +237,18 @@ class Registration:
         return self.results[-1].pose if self.results else self.init_pose
 
     def run(self) -> np.ndarray:
-        """Runs the job alone to completion."""
+        """Runs the job alone to completion (with a device optimizer, through a
+        job set of one: sampling and update stay on the device)."""
         if not self.started:
             self.start()
+        js = api.JobSet(self.device) if self.device_optimizer else None
         while not self.done:
+            L = self.levels[self.level]
+            if js is not None and L.optimizer != "dfo":
+                stop, _ = js.regi_step([self.step_job()])
+                if stop[0]:
+                    self.end_level(self.stop_reason(stop[0]))
+                continue
             poses = self.propose()
             self.tell(self.obj.eval(poses))
         return self.final_pose

@@ -9,9 +9,11 @@ pose, optimizer schedule) arrive at any time.  Each server step:
      optimizer state); a job starts (volume upload, first level set-up) on a
      worker thread while the active jobs keep stepping, and joins the steps
      once it has started;
-  2. samples every active job's population (CMA-ES sample or trust-region ask),
-     evaluates all populations with one DRR launch over every job's (tile,
-     pose) work and one batched grad-NCC launch, and updates every
+  2. samples every active job's population (CMA-ES sample or trust-region ask;
+     a CMA-ES state in device memory is sampled inside the geometry launch and
+     updated by the grad-NCC launch), evaluates all populations with one DRR
+     launch over every job's (tile, pose) work and one batched grad-NCC launch,
+     and updates every
      optimizer: one xr_regi_jobset_step call (native_step; otherwise the same
      steps driven from Python around one job-set evaluation);
   3. ends levels whose optimizer stopped (level change or completion) and
@@ -56,11 +58,14 @@ class ServerStats:
 
 class RegistrationServer:
     def __init__(self, device: int = -1, hbm_budget_bytes: float = 180e9, max_active: int = 64,
-                 native_step: bool = True):
+                 native_step: bool = True, device_optimizer: bool = True):
         self.device = device
         # native_step: each generation of all active jobs (sample, evaluate,
         # update, stop test) in one library call; otherwise driven from Python
         self.native_step = bool(native_step)
+        # device_optimizer (native steps only): CMA-ES levels keep their state in
+        # device memory and are sampled and updated inside the step's launches
+        self.device_optimizer = bool(device_optimizer) and self.native_step
         self.budget = float(hbm_budget_bytes)
         self.max_active = int(max_active)
         self.queue: collections.deque = collections.deque()
@@ -89,6 +94,7 @@ class RegistrationServer:
             if (self.active or self.starting) and used + need > self.budget:
                 break
             job = self.queue.popleft()
+            job.device_optimizer = self.device_optimizer
             self.starting.append((job, self._pool.submit(job.start)))
             used += need
         self.stats.max_footprint = max(self.stats.max_footprint, used)
