@@ -45,23 +45,36 @@ XR_API xr_status xr_cmaes_lambda(xr_cmaes e, int32_t* lambda);
 XR_API xr_status xr_cmaes_get(xr_cmaes e, double* mean, double* best_x, double* best_f, double* sigma,
                               int64_t* generation);
 
-/* Bound-constrained model-based trust-region optimizer for a final level, in
+/* Bound-constrained derivative-free trust-region optimizer for a final level, in
  * place of NLopt's LN_BOBYQA (Intensity2D3DRegiBOBYQA, xregIntensity2D3DRegiBOBYQA.cpp:28-39;
  * Intensity2D3DRegiNLOptInterface::run, xregIntensity2D3DRegiNLOptInterface.cpp:83-188):
- * 2n+1-point quadratic models around the best point, box-constrained trust-region
- * steps, rho halved on stalls, stop at rho_end or max_iter.  Each iteration asks
- * for one batch of up to 2*dim+2 points (evaluate them together) and is told
- * their values in the same order. */
+ * Powell's BOBYQA method -- a full quadratic model through 2n+1 interpolation
+ * points, changed by the least Frobenius norm of its Hessian change as each new
+ * point replaces one, box- and ball-constrained trust-region steps, geometry
+ * steps, rho shrunk to rho_end -- with at most 2n+1 + max_iter evaluations as
+ * xReg caps NLopt.  The first ask is the 2n+1 initial points; each later ask
+ * is one point (or `points` of them after xr_dfo_set_batch); tell takes their
+ * values in the same order.  rho is in the units of the coordinate with the
+ * widest bounds; the others are scaled by their widths. */
 typedef struct xr_dfo_s* xr_dfo;
 XR_API xr_status xr_dfo_create(int32_t dim, const double* x0, const double* lower, const double* upper,
                                double rho_beg, double rho_end, int64_t max_iter, xr_dfo* out);
 XR_API xr_status xr_dfo_destroy(xr_dfo d);
-/* Writes the batch (rows of dim doubles) into pts, room for 2*dim+2 rows; *count = rows. */
+/* Points per ask after the initial set (1 <= points <= 2*dim+2; default 1):
+ * the trust-region step and points-1 geometry steps of the farthest
+ * interpolation points, to evaluate together; max_iter then counts asks.
+ * Before the first tell. */
+XR_API xr_status xr_dfo_set_batch(xr_dfo d, int32_t points);
+/* Writes the points to evaluate (rows of dim doubles) into pts, room for
+ * 2*dim+2 rows; *count = rows.  Refused once the optimizer has stopped. */
 XR_API xr_status xr_dfo_ask(xr_dfo d, double* pts, int32_t* count);
+/* Values of the last asked points, in order (not finite = worse than every finite value). */
 XR_API xr_status xr_dfo_tell(xr_dfo d, const double* fvals);
-/* *reason: 0 continue, 2 rho below rho_end, 3 iteration limit. */
+/* *reason: 0 continue, 2 rho reached rho_end, 3 evaluation limit. */
 XR_API xr_status xr_dfo_test_termination(xr_dfo d, int32_t* reason);
 XR_API xr_status xr_dfo_get(xr_dfo d, double* best_x, double* best_f, double* rho, int64_t* iterations);
+/* Objective values told so far. */
+XR_API xr_status xr_dfo_evaluations(xr_dfo d, int64_t* evaluations);
 
 /* ------------------------------------------------ one registration level -- */
 /* The level loop of Intensity2D3DRegiCMAES::run (xregIntensity2D3DRegiCMAES.cpp:76-247)

@@ -169,6 +169,8 @@ _SIGS = {
     "xr_cmaes_test_termination": [H, C.POINTER(i32)],
     "xr_cmaes_get": [H, P, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
     "xr_cmaes_state_bytes": [H, C.POINTER(i64)],
+    "xr_dfo_set_batch": [H, i32],
+    "xr_dfo_evaluations": [H, C.POINTER(i64)],
     "xr_cmaes_export_state": [H, P, i64],
     "xr_cmaes_attach_device": [H, i32],
     "xr_cmaes_detach_device": [H],

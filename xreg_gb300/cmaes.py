@@ -101,10 +101,12 @@ class CMAES:
 
 
 class TrustRegionDFO:
-    """Bound-constrained model-based trust-region optimizer (xr_dfo_*), the
-    final-level optimizer in place of xReg's NLopt LN_BOBYQA; batch ask / tell."""
+    """Bound-constrained derivative-free trust-region optimizer (xr_dfo_*,
+    Powell's BOBYQA method), the final-level optimizer in place of xReg's NLopt
+    LN_BOBYQA: the first ask is the 2n+1 initial points, each later one the
+    trust-region or geometry point (or `batch` points, set_batch)."""
 
-    def __init__(self, x0, lower, upper, rho_beg: float, rho_end: float, max_iter: int):
+    def __init__(self, x0, lower, upper, rho_beg: float, rho_end: float, max_iter: int, batch: int = 1):
         load()
         x0 = np.ascontiguousarray(x0, dtype=np.float64)
         lo = np.ascontiguousarray(lower, dtype=np.float64)
@@ -115,6 +117,8 @@ class TrustRegionDFO:
         self._h = h
         self.n = int(x0.size)
         self._buf = np.zeros((2 * self.n + 2, self.n))
+        if batch != 1:
+            call("xr_dfo_set_batch", self._h, int(batch))
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -140,4 +144,6 @@ class TrustRegionDFO:
         x = np.zeros(self.n)
         bf, rho, it = C.c_double(), C.c_double(), C.c_int64()
         call("xr_dfo_get", self._h, x.ctypes.data_as(C.c_void_p), C.byref(bf), C.byref(rho), C.byref(it))
-        return {"best_x": x, "best_f": bf.value, "rho": rho.value, "iterations": it.value}
+        ne = C.c_int64()
+        call("xr_dfo_evaluations", self._h, C.byref(ne))
+        return {"best_x": x, "best_f": bf.value, "rho": rho.value, "iterations": it.value, "evaluations": ne.value}
