@@ -876,7 +876,15 @@ int64_t pow2_bucket(int64_t n) {
   return b;
 }
 
+// Times one launch configuration on the first projections of p: as many as
+// give about eight waves of blocks (all of them when there are fewer).
 xr_status time_config(DrrParams p, cudaStream_t s, float* ms_out) {
+  int dev = 0, sms = 0;
+  XR_CUDA_TRY(cudaGetDevice(&dev));
+  XR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t px = (int64_t)p.rows * p.cols;  // rays per projection; 256 per block, up to 6 blocks per SM
+  const int64_t waves8 = (8LL * sms * 6 * 256 + px - 1) / std::max<int64_t>(px, 1);
+  p.num_projs = std::min<int64_t>(p.num_projs, std::max<int64_t>(waves8, 4));
   cudaEvent_t a, b;
   XR_CUDA_TRY(cudaEventCreate(&a));
   XR_CUDA_TRY(cudaEventCreate(&b));
@@ -2217,7 +2225,9 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
       J.cnt = obj->d_fcnt.as<unsigned int>();
     }
     fj.push_back(J);
-    key.push_back((vol.type * 4 + J.d.p.vol.layout) * 8 + (fused ? J.d.p.unroll : 0));
+    // one launch per (voxel type, layout): the DRR job kernel runs each job's
+    // loop, the fused kernel the group's first job's (every loop gives the same bits)
+    key.push_back(vol.type * 4 + J.d.p.vol.layout);
   }
   // jobs ordered by group; item numbering restarts in each group
   std::vector<int32_t> keys(key);

@@ -7,8 +7,9 @@
 // Algorithm: the (mu/mu_w, lambda)-CMA-ES as published by N. Hansen ("The CMA
 // Evolution Strategy: A Tutorial", 2016): log-rank weights over the best half,
 // cumulative step-size adaptation, rank-one plus rank-mu covariance update with
-// the h_sigma stall, eigendecomposition of C each generation (cyclic Jacobi,
-// fine for the 6-parameter poses here).  Initialisation follows the convention
+// the h_sigma stall, eigendecomposition of C each generation (Jacobi rotations
+// in round-robin order, warm-started from the last eigenbasis, so a
+// generation's few sweeps run in parallel on a device block).  Initialisation follows the convention
 // of Hansen's C code that xReg calls: sigma = RMS of the per-coordinate initial
 // standard deviations and C = diag(s_i^2) / sigma^2, so sigma^2 C = diag(s_i^2).
 // Termination: function-value range over the recent generations below tol_fun,

@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 
 #if defined(__CUDACC__)
 #define XR_CMA_HD __host__ __device__ inline
@@ -220,14 +221,14 @@ XR_CMA_HD void normal_pair(uint64_t seed, int64_t gen, int32_t k, int32_t attemp
 
 // The optimizer state: this header, then (doubles) w[mu] m[n] pc[n] ps[n]
 // C[n*n] B[n*n] D[n] best[n] hist[hlen] pop[lam*n] z[lam*n] fv[lam] and the
-// update's scratch A[n*n] mold[n] yw[n] zw[n] bz[n] dv[n], then (int32)
-// att[lam] idx[lam].  One contiguous block, so it moves between host and
-// device memory with one copy.
+// update's scratch A[n*n] T[n*n] V[n*n] ys[mu*n] mold[n] yw[n] zw[n] bz[n]
+// rot[2n], then (int32) att[lam] idx[lam].  One contiguous block, so it moves
+// between host and device memory with one copy.
 struct Hdr {
   int32_t n, lam, mu, hlen;
   int32_t hcount, hhead;  // function-value history: entries stored, next slot
   int32_t sampled, reason;
-  int32_t sample_error, reserved;
+  int32_t sample_error, rotated;  // rotated: the eigen sweep in progress applied a rotation
   int64_t gen, max_iter;
   uint64_t seed;
   double mueff, cs, ds, cc, c1, cmu, chin, sigma, best_f, last_range, tol_fun, tol_x;
@@ -236,13 +237,13 @@ static_assert(sizeof(Hdr) % 16 == 0, "state header keeps the arrays 16-byte alig
 
 struct View {
   Hdr* h;
-  double *w, *m, *pc, *ps, *C, *B, *D, *best, *hist, *pop, *z, *fv, *A, *mold, *yw, *zw, *bz, *dv;
+  double *w, *m, *pc, *ps, *C, *B, *D, *best, *hist, *pop, *z, *fv, *A, *T, *V, *ys, *mold, *yw, *zw, *bz, *rot;
   int32_t *att, *idx;
 };
 
 XR_CMA_HD size_t num_doubles(int n, int lam, int mu, int hlen) {
   return (size_t)mu + 3 * (size_t)n + 2 * (size_t)n * n + 2 * (size_t)n + (size_t)hlen + 2 * (size_t)lam * n +
-         (size_t)lam + (size_t)n * n + 5 * (size_t)n;
+         (size_t)lam + 3 * (size_t)n * n + (size_t)mu * n + 6 * (size_t)n;
 }
 
 XR_CMA_HD size_t state_bytes(int n, int lam, int mu, int hlen) {
@@ -267,11 +268,14 @@ XR_CMA_HD View view(void* base) {
   v.z = d; d += lam * n;
   v.fv = d; d += lam;
   v.A = d; d += n * n;
+  v.T = d; d += n * n;
+  v.V = d; d += n * n;
+  v.ys = d; d += mu * n;
   v.mold = d; d += n;
   v.yw = d; d += n;
   v.zw = d; d += n;
   v.bz = d; d += n;
-  v.dv = d; d += n;
+  v.rot = d; d += 2 * n;
   v.att = reinterpret_cast<int32_t*>(d);
   v.idx = v.att + lam;
   return v;
@@ -302,52 +306,85 @@ XR_CMA_HD bool inside(const double* x, const double* bounds, int n) {
   return true;
 }
 
-// Whether value a (candidate ia) comes before b (candidate ib): ascending,
-// NaN after every number, ties in candidate order (a stable sort).
-XR_CMA_HD bool before(double a, int ia, double b, int ib) {
-  const bool na = a != a, nb = b != b;
-  if (na != nb) return nb;
-  if (!na && a != b) return a < b;
-  return ia < ib;
+// Order-preserving integer key of an objective value: ascending numbers (-0
+// as +0), NaN after every number.
+XR_CMA_HD uint64_t order_key(double v) {
+  if (v != v) return ~0ull;
+  if (v == 0.0) v = 0.0;
+#ifdef __CUDA_ARCH__
+  const uint64_t b = (uint64_t)__double_as_longlong(v);
+#else
+  uint64_t b;
+  std::memcpy(&b, &v, sizeof(b));
+#endif
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-// Eigen-decomposition of the symmetric n x n matrix A (destroyed) by cyclic
-// Jacobi rotations: A = V diag(d) V^T, V column-wise.
-XR_CMA_HD void jacobi(int n, double* A, double* V, double* d) {
-  for (int i = 0; i < n * n; ++i) V[i] = 0.0;
-  for (int i = 0; i < n; ++i) V[i * n + i] = 1.0;
-  for (int sweep = 0; sweep < 64; ++sweep) {
-    double off = 0.0;
-    for (int p = 0; p < n; ++p)
-      for (int q = p + 1; q < n; ++q) off = dm::add(off, dm::mul(A[p * n + q], A[p * n + q]));
-    if (off < 1e-300) break;
-    for (int p = 0; p < n; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = A[p * n + q];
-        if (dm::fabs(apq) < 1e-300) continue;
-        const double app = A[p * n + p], aqq = A[q * n + q];
-        const double theta = dm::div(dm::sub(aqq, app), dm::mul(2.0, apq));
-        const double t = dm::div(theta >= 0.0 ? 1.0 : -1.0,
-                                 dm::add(dm::fabs(theta), dm::sqrt(dm::add(dm::mul(theta, theta), 1.0))));
-        const double c = dm::div(1.0, dm::sqrt(dm::add(dm::mul(t, t), 1.0))), s = dm::mul(t, c);
-        for (int k = 0; k < n; ++k) {
-          const double akp = A[k * n + p], akq = A[k * n + q];
-          A[k * n + p] = dm::sub(dm::mul(c, akp), dm::mul(s, akq));
-          A[k * n + q] = dm::add(dm::mul(s, akp), dm::mul(c, akq));
-        }
-        for (int k = 0; k < n; ++k) {
-          const double apk = A[p * n + k], aqk = A[q * n + k];
-          A[p * n + k] = dm::sub(dm::mul(c, apk), dm::mul(s, aqk));
-          A[q * n + k] = dm::add(dm::mul(s, apk), dm::mul(c, aqk));
-        }
-        for (int k = 0; k < n; ++k) {
-          const double vkp = V[k * n + p], vkq = V[k * n + q];
-          V[k * n + p] = dm::sub(dm::mul(c, vkp), dm::mul(s, vkq));
-          V[k * n + q] = dm::add(dm::mul(s, vkp), dm::mul(c, vkq));
-        }
-      }
+// Eigen-decomposition by Jacobi rotations in round-robin order: each round
+// rotates disjoint index pairs, whose parameters all come from the matrix at
+// the start of the round; the column updates of every pair come first, then
+// the row updates (so a round's elements are independent of one another).
+// Pair i of round r (the circle method over N = n rounded up to even; a pair
+// with the index n of odd n is idle): *p < *q, false when idle.
+XR_CMA_HD bool rr_pair(int n, int r, int i, int* p, int* q) {
+  const int N = n + (n & 1), M = N - 1;
+  int a, b;
+  if (i == 0) {
+    a = r;
+    b = M;
+  } else {
+    a = (r + i) % M;
+    b = (r - i + M) % M;
   }
-  for (int i = 0; i < n; ++i) d[i] = A[i * n + i];
+  if (a >= n || b >= n) return false;
+  *p = a < b ? a : b;
+  *q = a < b ? b : a;
+  return true;
+}
+XR_CMA_HD int rr_rounds(int n) { return n + (n & 1) - 1; }
+XR_CMA_HD int rr_pairs(int n) { return (n + 1) / 2; }
+
+// Rotation of pair i of round r from A: (c, s) into rot[2i..2i+1]; s = 0 when
+// the off-diagonal entry is negligible (below 2^-56 of the two diagonal
+// entries); sets *rotated when it is not.
+XR_CMA_HD void rot_params(int n, const double* A, int r, int i, double* rot, int32_t* rotated) {
+  int p, q;
+  rot[2 * i] = 1.0;
+  rot[2 * i + 1] = 0.0;
+  if (!rr_pair(n, r, i, &p, &q)) return;
+  const double apq = A[p * n + q], app = A[p * n + p], aqq = A[q * n + q];
+  if (dm::fabs(apq) <= 1e-300 || dm::fabs(apq) <= dm::mul(0x1p-56, dm::add(dm::fabs(app), dm::fabs(aqq)))) return;
+  const double theta = dm::div(dm::sub(aqq, app), dm::mul(2.0, apq));
+  const double t = dm::div(theta >= 0.0 ? 1.0 : -1.0,
+                           dm::add(dm::fabs(theta), dm::sqrt(dm::add(dm::mul(theta, theta), 1.0))));
+  const double c = dm::div(1.0, dm::sqrt(dm::add(dm::mul(t, t), 1.0)));
+  rot[2 * i] = c;
+  rot[2 * i + 1] = dm::mul(t, c);
+  *rotated = 1;
+}
+
+// Column update (row k of columns p, q) of pair i, in A and in the rotation
+// product V.
+XR_CMA_HD void rot_cols(int n, double* A, double* V, int r, int i, const double* rot, int k) {
+  int p, q;
+  const double c = rot[2 * i], s = rot[2 * i + 1];
+  if (s == 0.0 || !rr_pair(n, r, i, &p, &q)) return;
+  const double akp = A[k * n + p], akq = A[k * n + q];
+  A[k * n + p] = dm::sub(dm::mul(c, akp), dm::mul(s, akq));
+  A[k * n + q] = dm::add(dm::mul(s, akp), dm::mul(c, akq));
+  const double vkp = V[k * n + p], vkq = V[k * n + q];
+  V[k * n + p] = dm::sub(dm::mul(c, vkp), dm::mul(s, vkq));
+  V[k * n + q] = dm::add(dm::mul(s, vkp), dm::mul(c, vkq));
+}
+
+// Row update (column k of rows p, q) of pair i.
+XR_CMA_HD void rot_rows(int n, double* A, int r, int i, const double* rot, int k) {
+  int p, q;
+  const double c = rot[2 * i], s = rot[2 * i + 1];
+  if (s == 0.0 || !rr_pair(n, r, i, &p, &q)) return;
+  const double apk = A[p * n + k], aqk = A[q * n + k];
+  A[p * n + k] = dm::sub(dm::mul(c, apk), dm::mul(s, aqk));
+  A[q * n + k] = dm::add(dm::mul(s, apk), dm::mul(c, aqk));
 }
 
 // Stop reason: 0 continue, 1 tol_fun, 2 tol_x, 3 max_iter, 4 numerical (sigma not finite).
@@ -367,32 +404,56 @@ XR_CMA_HD int32_t termination(const View& s) {
 // candidates in s.pop / s.z): ranking, weighted recombination of the best mu,
 // cumulative step-size adaptation, rank-one + rank-mu covariance update with
 // the h_sigma stall, new eigen-decomposition, function-value history; the
-// termination code after it goes to h.reason.
-XR_CMA_HD void update(const View& s) {
-  Hdr& h = *s.h;
-  const int n = h.n, lam = h.lam, mu = h.mu;
-  const double* f = s.fv;
-  for (int k = 0; k < lam; ++k) {
-    int r = 0;
-    for (int j = 0; j < lam; ++j) r += before(f[j], j, f[k], k) ? 1 : 0;
-    s.idx[r] = k;
+// termination code after it goes to h.reason.  The stages below are what
+// update() runs in order; the ranks, the 2n recombination sums and the
+// n(n+1)/2 covariance entries are independent of one another within their
+// stage (each summed in the same order wherever it runs), so a device block
+// can run them in parallel with the same bits.
+
+// Stage 1 (each k): position of candidate k in the ranking.
+XR_CMA_HD void rank(const View& s, int k) {
+  const int lam = s.h->lam;
+  const uint64_t kk = order_key(s.fv[k]);
+  int r = 0;
+  for (int j = 0; j < lam; ++j) {
+    const uint64_t kj = order_key(s.fv[j]);
+    r += (kj < kk || (kj == kk && j < k)) ? 1 : 0;
   }
-  const int best = s.idx[0];
-  if (f[best] < h.best_f) {
-    h.best_f = f[best];
+  s.idx[r] = k;
+}
+
+// Stage 2: best value so far; the old mean.
+XR_CMA_HD void keep_best(const View& s) {
+  Hdr& h = *s.h;
+  const int n = h.n, best = s.idx[0];
+  if (s.fv[best] < h.best_f) {
+    h.best_f = s.fv[best];
     for (int i = 0; i < n; ++i) s.best[i] = s.pop[best * n + i];
   }
   for (int i = 0; i < n; ++i) s.mold[i] = s.m[i];
-  for (int i = 0; i < n; ++i) {
-    double a = 0.0, b = 0.0;
-    for (int k = 0; k < mu; ++k) {
-      a = dm::add(a, dm::mul(s.w[k], s.pop[s.idx[k] * n + i]));
-      b = dm::add(b, dm::mul(s.w[k], s.z[s.idx[k] * n + i]));
-    }
+}
+
+// Stage 3 (each t < 2n): weighted recombination of coordinate t % n of the
+// candidates (t < n, the new mean and y_w) or of their draws (t >= n, z_w).
+XR_CMA_HD void recombine(const View& s, int t) {
+  const Hdr& h = *s.h;
+  const int n = h.n, mu = h.mu, i = t % n;
+  const double* src = t < n ? s.pop : s.z;
+  double a = 0.0;
+  for (int k = 0; k < mu; ++k) a = dm::add(a, dm::mul(s.w[k], src[s.idx[k] * n + i]));
+  if (t < n) {
     s.m[i] = a;
     s.yw[i] = dm::div(dm::sub(a, s.mold[i]), h.sigma);
-    s.zw[i] = b;
+  } else {
+    s.zw[i] = a;
   }
+}
+
+// Stage 4: evolution paths; returns in scal[0] the norm of p_sigma, in
+// scal[1] the h_sigma stall factor d_h, in scal[2] 1 - c1 - cmu.
+XR_CMA_HD void paths(const View& s, double* scal) {
+  Hdr& h = *s.h;
+  const int n = h.n;
   for (int i = 0; i < n; ++i) {  // C^{-1/2} y_w = B z_w
     double a = 0.0;
     for (int j = 0; j < n; ++j) a = dm::add(a, dm::mul(s.B[i * n + j], s.zw[j]));
@@ -413,29 +474,88 @@ XR_CMA_HD void update(const View& s) {
   const double a_c = dm::sqrt(dm::mul(dm::mul(h.cc, dm::sub(2.0, h.cc)), h.mueff));
   for (int i = 0; i < n; ++i)
     s.pc[i] = dm::add(dm::mul(dm::sub(1.0, h.cc), s.pc[i]), dm::mul(dm::mul(hsig, a_c), s.yw[i]));
-  const double dh = dm::mul(dm::mul(dm::sub(1.0, hsig), h.cc), dm::sub(2.0, h.cc));
-  const double keep = dm::sub(dm::sub(1.0, h.c1), h.cmu);
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j <= i; ++j) {
-      double rmu = 0.0;
-      for (int k = 0; k < mu; ++k) {
-        const int c = s.idx[k];
-        const double yi = dm::div(dm::sub(s.pop[c * n + i], s.mold[i]), h.sigma);
-        const double yj = dm::div(dm::sub(s.pop[c * n + j], s.mold[j]), h.sigma);
-        rmu = dm::add(rmu, dm::mul(dm::mul(s.w[k], yi), yj));
-      }
-      const double cij = s.C[i * n + j];
-      const double v = dm::add(dm::add(dm::mul(keep, cij),
-                                       dm::mul(h.c1, dm::add(dm::mul(s.pc[i], s.pc[j]), dm::mul(dh, cij)))),
-                               dm::mul(h.cmu, rmu));
-      s.C[i * n + j] = v;
-      s.C[j * n + i] = v;
-    }
-  h.sigma = dm::mul(h.sigma, dm::exp(dm::mul(dm::div(h.cs, h.ds), dm::sub(dm::div(psn, h.chin), 1.0))));
-  for (int i = 0; i < n * n; ++i) s.A[i] = s.C[i];
-  jacobi(n, s.A, s.B, s.dv);
-  for (int i = 0; i < n; ++i) s.D[i] = dm::sqrt(s.dv[i] > 1e-300 ? s.dv[i] : 1e-300);
+  scal[0] = psn;
+  scal[1] = dm::mul(dm::mul(dm::sub(1.0, hsig), h.cc), dm::sub(2.0, h.cc));
+  scal[2] = dm::sub(dm::sub(1.0, h.c1), h.cmu);
+}
+
+// Stage 5 (each t < mu n): step (x_k - m_old) / sigma of coordinate t % n of
+// the (t / n)-th best candidate.
+XR_CMA_HD void steps(const View& s, int t) {
+  const Hdr& h = *s.h;
+  const int n = h.n, k = t / n, i = t % n;
+  s.ys[t] = dm::div(dm::sub(s.pop[s.idx[k] * n + i], s.mold[i]), h.sigma);
+}
+
+// Stage 6 (each e < n(n+1)/2, the lower triangle row by row): covariance
+// entry (i, j), j <= i, and its mirror.  Reads only its own old entry.
+XR_CMA_HD void tri(int e, int* i, int* j) {
+  int r = 0;
+  while ((r + 1) * (r + 2) / 2 <= e) ++r;
+  *i = r;
+  *j = e - r * (r + 1) / 2;
+}
+XR_CMA_HD void covariance(const View& s, int e, const double* scal) {
+  const Hdr& h = *s.h;
+  const int n = h.n, mu = h.mu;
+  int i, j;
+  tri(e, &i, &j);
+  double rmu = 0.0;
+  for (int k = 0; k < mu; ++k) rmu = dm::add(rmu, dm::mul(dm::mul(s.w[k], s.ys[k * n + i]), s.ys[k * n + j]));
+  const double cij = s.C[i * n + j];
+  const double v = dm::add(dm::add(dm::mul(scal[2], cij),
+                                   dm::mul(h.c1, dm::add(dm::mul(s.pc[i], s.pc[j]), dm::mul(scal[1], cij)))),
+                           dm::mul(h.cmu, rmu));
+  s.C[i * n + j] = v;
+  s.C[j * n + i] = v;
+}
+
+// Stage 7: the step size.
+XR_CMA_HD void step_size(const View& s, const double* scal) {
+  Hdr& h = *s.h;
+  h.sigma = dm::mul(h.sigma, dm::exp(dm::mul(dm::div(h.cs, h.ds), dm::sub(dm::div(scal[0], h.chin), 1.0))));
+}
+
+// Stage 8, the eigen-decomposition of C warm-started from the last basis B:
+// (a, each e < n n) T = C B; (b, each e < n(n+1)/2) A = B^T T, lower triangle
+// mirrored, and V = I; then Jacobi sweeps on A (rot_params, rot_cols,
+// rot_rows per round) until a sweep rotates nothing; (c, each e < n n)
+// T = B V; (d, each e < n n) B = T.
+XR_CMA_HD void eig_cb(const View& s, int e) {
+  const int n = s.h->n, i = e / n, j = e % n;
+  double a = 0.0;
+  for (int k = 0; k < n; ++k) a = dm::add(a, dm::mul(s.C[i * n + k], s.B[k * n + j]));
+  s.T[e] = a;
+}
+XR_CMA_HD void eig_btcb(const View& s, int e) {
+  const int n = s.h->n;
+  int i, j;
+  tri(e, &i, &j);
+  double a = 0.0;
+  for (int k = 0; k < n; ++k) a = dm::add(a, dm::mul(s.B[k * n + i], s.T[k * n + j]));
+  s.A[i * n + j] = a;
+  s.A[j * n + i] = a;
+  s.V[i * n + j] = i == j ? 1.0 : 0.0;
+  s.V[j * n + i] = i == j ? 1.0 : 0.0;
+}
+XR_CMA_HD void eig_bv(const View& s, int e) {
+  const int n = s.h->n, i = e / n, j = e % n;
+  double a = 0.0;
+  for (int k = 0; k < n; ++k) a = dm::add(a, dm::mul(s.B[i * n + k], s.V[k * n + j]));
+  s.T[e] = a;
+}
+
+// Stage 9: D from the eigenvalues, history, termination code.
+XR_CMA_HD void finish(const View& s) {
+  Hdr& h = *s.h;
+  const int n = h.n, lam = h.lam;
+  const double* f = s.fv;
+  for (int i = 0; i < n; ++i) {
+    const double d = s.A[i * n + i];
+    s.D[i] = dm::sqrt(d > 1e-300 ? d : 1e-300);
+  }
   // best value of the last hlen generations (the TolFun test's range)
+  const int best = s.idx[0];
   s.hist[h.hhead] = f[best];
   h.hhead = (h.hhead + 1) % h.hlen;
   if (h.hcount < h.hlen) h.hcount += 1;
@@ -447,6 +567,36 @@ XR_CMA_HD void update(const View& s) {
   h.last_range = dm::sub(hi, lo);
   h.sampled = 0;
   h.reason = termination(s);
+}
+
+constexpr int kMaxSweeps = 64;
+
+XR_CMA_HD void update(const View& s) {
+  const int n = s.h->n, lam = s.h->lam, mu = s.h->mu;
+  double scal[3];
+  for (int k = 0; k < lam; ++k) rank(s, k);
+  keep_best(s);
+  for (int t = 0; t < 2 * n; ++t) recombine(s, t);
+  paths(s, scal);
+  for (int t = 0; t < mu * n; ++t) steps(s, t);
+  for (int e = 0; e < n * (n + 1) / 2; ++e) covariance(s, e, scal);
+  step_size(s, scal);
+  for (int e = 0; e < n * n; ++e) eig_cb(s, e);
+  for (int e = 0; e < n * (n + 1) / 2; ++e) eig_btcb(s, e);
+  for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
+    s.h->rotated = 0;
+    for (int r = 0; r < rr_rounds(n); ++r) {
+      for (int i = 0; i < rr_pairs(n); ++i) rot_params(n, s.A, r, i, s.rot, &s.h->rotated);
+      for (int i = 0; i < rr_pairs(n); ++i)
+        for (int k = 0; k < n; ++k) rot_cols(n, s.A, s.V, r, i, s.rot, k);
+      for (int i = 0; i < rr_pairs(n); ++i)
+        for (int k = 0; k < n; ++k) rot_rows(n, s.A, r, i, s.rot, k);
+    }
+    if (!s.h->rotated) break;
+  }
+  for (int e = 0; e < n * n; ++e) eig_bv(s, e);
+  for (int e = 0; e < n * n; ++e) s.B[e] = s.T[e];
+  finish(s);
 }
 
 }  // namespace cma

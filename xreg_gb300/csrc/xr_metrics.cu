@@ -274,29 +274,74 @@ __global__ void grad_finalize_kernel(const double* __restrict__ partials, int nb
 // 32x64 tile, grid-stride; the counters of FusedJob::cnt (images, then poses)
 // chain the per-image combine and the mean over views behind the tiles.
 // A device CMA-ES job's update from its lambda values (the float means over
-// views, widened to double as the host step does): cmaes_UpdateDistribution,
-// then cmaes_TestForTermination, whose code goes to the state and the report.
-__device__ __noinline__ void cma_update_device(void* state, const float* vals, CmaReport* report) {
+// views, widened to double as the host step does) by a whole block: the stages
+// of cma::update (cmaes_UpdateDistribution, then cmaes_TestForTermination),
+// the ranks, recombination sums and covariance entries one per thread.
+__device__ __noinline__ void cma_update_block(void* state, const float* vals, CmaReport* report) {
+  __shared__ double scal[3];
   const cma::View s = cma::view(state);
-  const int lam = s.h->lam;
-  for (int k = 0; k < lam; ++k) s.fv[k] = (double)__ldcg(vals + k);
-  cma::update(s);
-  if (report) report->reason = s.h->reason;
+  const int n = s.h->n, lam = s.h->lam, mu = s.h->mu, nt = blockDim.x, tid = threadIdx.x;
+  for (int k = tid; k < lam; k += nt) s.fv[k] = (double)__ldcg(vals + k);
+  __syncthreads();
+  for (int k = tid; k < lam; k += nt) cma::rank(s, k);
+  __syncthreads();
+  if (tid == 0) cma::keep_best(s);
+  __syncthreads();
+  for (int t = tid; t < 2 * n; t += nt) cma::recombine(s, t);
+  __syncthreads();
+  if (tid == 0) cma::paths(s, scal);
+  __syncthreads();
+  for (int t = tid; t < mu * n; t += nt) cma::steps(s, t);
+  __syncthreads();
+  for (int e = tid; e < n * (n + 1) / 2; e += nt) cma::covariance(s, e, scal);
+  __syncthreads();
+  if (tid == 0) cma::step_size(s, scal);
+  for (int e = tid; e < n * n; e += nt) cma::eig_cb(s, e);
+  __syncthreads();
+  for (int e = tid; e < n * (n + 1) / 2; e += nt) cma::eig_btcb(s, e);
+  __syncthreads();
+  const int pairs = cma::rr_pairs(n), rounds = cma::rr_rounds(n);
+  for (int sweep = 0; sweep < cma::kMaxSweeps; ++sweep) {
+    if (tid == 0) s.h->rotated = 0;
+    __syncthreads();
+    for (int r = 0; r < rounds; ++r) {
+      for (int i = tid; i < pairs; i += nt) cma::rot_params(n, s.A, r, i, s.rot, &s.h->rotated);
+      __syncthreads();
+      for (int e = tid; e < pairs * n; e += nt) cma::rot_cols(n, s.A, s.V, r, e / n, s.rot, e % n);
+      __syncthreads();
+      for (int e = tid; e < pairs * n; e += nt) cma::rot_rows(n, s.A, r, e / n, s.rot, e % n);
+      __syncthreads();
+    }
+    const int rotated = *(volatile int32_t*)&s.h->rotated;
+    __syncthreads();  // every thread has read the flag before the next sweep clears it
+    if (!rotated) break;
+  }
+  for (int e = tid; e < n * n; e += nt) cma::eig_bv(s, e);
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) s.B[e] = s.T[e];
+  __syncthreads();
+  if (tid == 0) {
+    cma::finish(s);
+    if (report) report->reason = s.h->reason;
+  }
+  __syncthreads();
 }
 
 __global__ void cma_update_kernel(const CmaUpdateJob* __restrict__ jobs) {
-  if (threadIdx.x == 0) cma_update_device(jobs[blockIdx.x].cma, jobs[blockIdx.x].vals, jobs[blockIdx.x].report);
+  cma_update_block(jobs[blockIdx.x].cma, jobs[blockIdx.x].vals, jobs[blockIdx.x].report);
 }
 
-// The last tile of an image combines its moments (FP64) and, the last view of
-// a pose, the mean over views; out of line so the tile loop keeps the
-// register budget of the per-view moments kernel (40 registers, 6 blocks per
-// SM, where the inlined FP64 combine took 80 and 3).
+// The last tile of an image combines its moments (FP64); the last view of a
+// pose, the mean over views; the last pose of a job with a device optimizer,
+// the optimizer's update (the whole block).  Out of line so the tile loop keeps
+// the register budget of the per-view moments kernel (40 registers, 6 blocks
+// per SM, where the inlined FP64 combine took 80 and 3).
 __device__ __noinline__ void grad_multi_finish(const FusedJob& J, const FusedView& V, int64_t k, int mt, int64_t nimg,
-                                               double* dred) {
+                                               double* dred, int* job_done) {
   __threadfence();
   const float sim = gt::grad_finalize_image<true>(V.partials + k * mt * 6, mt, V.n_used, V.fx, V.fy, dred);
   if (threadIdx.x == 0) {
+    int done = 0;
     V.sims[k] = sim;
     __threadfence();
     unsigned int* cp = J.cnt + nimg * mt + nimg + k;
@@ -306,16 +351,21 @@ __device__ __noinline__ void grad_multi_finish(const FusedJob& J, const FusedVie
       float sum = 0.0f;
       for (int w = 0; w < J.nviews; ++w) sum += __ldcg(J.views[w].sims + k);
       J.out[k] = sum / (float)J.nviews;  // ImgSimMetric2DCombineMean (as gt::combine_mean)
-      if (J.cma) {  // the job's last pose: its optimizer's update
+      if (J.cma) {  // the job's last pose: its optimizer's update by this block
         __threadfence();
         unsigned int* cj = J.cnt + nimg * mt + nimg + J.pop;
         if (atomicAdd(cj, 1u) + 1u == (unsigned int)J.pop) {
           *cj = 0u;
-          __threadfence();
-          cma_update_device(J.cma, J.out, J.report);
+          done = 1;
         }
       }
     }
+    *job_done = done;
+  }
+  __syncthreads();
+  if (*job_done) {
+    __threadfence();
+    cma_update_block(J.cma, J.out, J.report);
   }
 }
 
@@ -323,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 6) grad_multi_kernel(const FusedJob*
                                                                  long long total) {
   __shared__ gt::GradTileSmem<2> sm;
   __shared__ double dred[6 * (gt::kFinalizeThreads / 32)];
-  __shared__ int s_last;
+  __shared__ int s_last, s_job_done;
   for (long long t = blockIdx.x; t < total; t += gridDim.x) {
     int j = 0;
     while (j + 1 < njobs && jobs[j + 1].tile_begin <= t) ++j;
@@ -347,7 +397,7 @@ __global__ void __launch_bounds__(kThreads, 6) grad_multi_kernel(const FusedJob*
       if (s_last) *ci = 0u;
     }
     __syncthreads();
-    if (s_last) grad_multi_finish(J, V, k, mt, nimg, dred);  // every tile of this image is in
+    if (s_last) grad_multi_finish(J, V, k, mt, nimg, dred, &s_job_done);  // every tile of this image is in
     __syncthreads();
   }
 }
@@ -894,7 +944,7 @@ cudaError_t launch_grad_multi(const FusedJob* d_jobs, int njobs, long long total
 
 cudaError_t launch_cma_updates(const CmaUpdateJob* d_jobs, int njobs, cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
-  cma_update_kernel<<<(unsigned)njobs, 32, 0, s>>>(d_jobs);
+  cma_update_kernel<<<(unsigned)njobs, 128, 0, s>>>(d_jobs);
   return cudaGetLastError();
 }
 

@@ -130,11 +130,13 @@ class Registration:
         return int(vol + lev + (16 << 20))
 
     def start(self) -> None:
+        """Admission: the volume upload and the first level's set-up (t_start
+        marks the start of the service, the end of the queue wait)."""
+        self.t_start = time.perf_counter()
         self.rc = api.RayCasterLineIntCUDA(self.device)
         self.rc.set_volume(self.vol, self.voxel_type)
         self.rc.set_ray_step_size(self.step)
         self.started = True
-        self.t_start = time.perf_counter()
         self._enter_level(0)
 
     def _enter_level(self, k: int) -> None:

@@ -39,7 +39,9 @@ from .regi import Registration
 @dataclass
 class ServerStats:
     completed: int = 0
-    latencies_s: list = field(default_factory=list)
+    latencies_s: list = field(default_factory=list)   # arrival to completion
+    queue_waits_s: list = field(default_factory=list)  # arrival to start (admission)
+    services_s: list = field(default_factory=list)     # start to completion
     steps: int = 0
     poses_evaluated: int = 0
     busy_s: float = 0.0
@@ -49,8 +51,13 @@ class ServerStats:
 
     def summary(self) -> dict:
         lat = np.array(self.latencies_s) if self.latencies_s else np.zeros(1)
+        wait = np.array(self.queue_waits_s) if self.queue_waits_s else np.zeros(1)
+        serv = np.array(self.services_s) if self.services_s else np.zeros(1)
         return {"completed": self.completed, "p50_s": float(np.percentile(lat, 50)),
-                "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "steps": self.steps,
+                "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+                "queue_wait_p50_s": float(np.percentile(wait, 50)), "queue_wait_p99_s": float(np.percentile(wait, 99)),
+                "service_p50_s": float(np.percentile(serv, 50)), "service_p99_s": float(np.percentile(serv, 99)),
+                "steps": self.steps,
                 "poses_evaluated": self.poses_evaluated, "busy_s": self.busy_s, "admit_s": self.admit_s,
                 "max_active": self.max_active,
                 "max_footprint_gb": self.max_footprint / 1e9}
@@ -142,6 +149,8 @@ class RegistrationServer:
                 self.finished.append(j)
                 self.stats.completed += 1
                 self.stats.latencies_s.append(j.t_done - j.t_submit)
+                self.stats.queue_waits_s.append(j.t_start - j.t_submit)
+                self.stats.services_s.append(j.t_done - j.t_start)
             else:
                 still.append(j)
         self.active = still

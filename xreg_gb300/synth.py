@@ -238,6 +238,18 @@ def job_registration(spec: JobSpec, levels=None, iters=(150, 100), level2_pop: i
                         name=f"job{spec.seed}"), gt
 
 
+def request_like(template, gt: np.ndarray, seed: int):
+    """Another registration request of the same patient and views as template
+    (its volume, cameras and fixed images shared), with its own start pose,
+    perturbed from the ground truth by N(0, 5 deg) / N(0, 10 mm), and its own
+    optimizer seed."""
+    from .regi import Registration
+    rng = np.random.default_rng(seed)
+    init = perturb(template.vol, gt, rng.normal(0.0, 5.0, 3), rng.normal(0.0, 10.0, 3))
+    return Registration(template.vol, template.levels, init, step=template.step, voxel_type=template.voxel_type,
+                        seed=seed, device=template.device, name=f"{template.name}-r{seed}")
+
+
 def view_cameras(angles, ds: float) -> list:
     """One naive camera per view; view k orbits angles[k] degrees about the volume centre."""
     from .se3 import rigid
