@@ -399,10 +399,14 @@ XR_API xr_status xr_obj_set_fused(xr_objective obj, int32_t enable);
  * memory belongs to another allocator, or that hand the library only device
  * pointers.  Every intermediate lives in one fixed 16 MiB array inside the
  * library (held on each GPU that loads it until the process exits); requests
- * that need more are refused with XR_ERR_INVALID_ARG.  The first call on a device
- * looks up that array's address (once per device); make it before any stream
- * capture.  Calls share the array, so calls that overlap on the GPU race: keep
- * them on one stream.  smooth_ksize is 5, 3 or 0 as for XR_SIM_GRAD_NCC; no mask.
+ * that need more, or more than 65535 moving images, are refused with
+ * XR_ERR_INVALID_ARG.  The first call on a device looks up that array's address
+ * (once per device, kept for the life of the process); make it before any
+ * stream capture, and do not call this function on a device again after
+ * cudaDeviceReset or anything else that recreates its primary context (the
+ * kept address is then stale).  Calls share the array, so calls that overlap
+ * on the GPU race: keep them on one stream.  smooth_ksize is 5, 3 or 0 as for
+ * XR_SIM_GRAD_NCC; no mask.
  * No counterpart in the reference (xReg's metrics always allocate their buffers). */
 XR_API xr_status xr_grad_ncc_noalloc(const float* d_fixed, const float* d_moving, int64_t rows, int64_t cols,
                                      int64_t num_moving, int32_t smooth_ksize, float* d_sims, void* cuda_stream);

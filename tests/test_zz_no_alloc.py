@@ -56,3 +56,8 @@ def test_grad_ncc_noalloc_matches_allocating_metric(xr):
                                  C.c_void_p(d_sims.data_ptr()), C.c_void_p(stream.cuda_stream))
     assert st == _lib.XR_ERR_INVALID_ARG
     assert b"scratch" in lib.xr_last_error()
+    # more moving images than one launch's grid rows: refused before any launch
+    st = lib.xr_grad_ncc_noalloc(C.c_void_p(d_fixed.data_ptr()), C.c_void_p(d_movs.data_ptr()), 8, 8, 70000, 5,
+                                 C.c_void_p(d_sims.data_ptr()), C.c_void_p(stream.cuda_stream))
+    assert st == _lib.XR_ERR_INVALID_ARG
+    assert b"65535" in lib.xr_last_error()

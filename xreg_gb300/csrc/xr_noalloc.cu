@@ -17,12 +17,17 @@
 //     giving the bytes needed;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture;
+//     that first call before any stream capture.  The address is kept for the
+//     life of the process: after cudaDeviceReset (or anything else that tears
+//     down and recreates the device's primary context) the array is a new one
+//     and this library must not be called on that device again;
+//   * at most 65535 moving images per call;
 //   * all calls share the one array: two calls whose work overlaps on the GPU
 //     (different streams, or different host threads) race and give wrong values.
 //     Calls serialised on one stream are fine.  Each call overwrites everything
 //     it reads later, and the statistics words are cleared at the start of
 //     every call.
+#include "xr_gradtile.cuh"
 #include "xr_internal.h"
 
 #include <mutex>
@@ -62,30 +67,18 @@ __global__ void zero_mean_from_stats_kernel(const float* __restrict__ g, int64_t
     out[i] = g[i] - mean;
 }
 
-__device__ double sim_from(double sm, double smm, double smf, double n, double sd_f, double sum_f) {
-  const double mean = sm / n;
-  double var = (smm - n * mean * mean) / (n - 1.0);
-  if (var < 0.0) var = 0.0;
-  double sd = sqrt(var);
-  if (sd < 1.0e-6) sd = 1.0e-6;
-  return (1.0 - (smf - mean * sum_f) / (n * sd_f * sd)) * 0.5;
-}
-
-__global__ void finalize_from_stats_kernel(const double* __restrict__ partials, int nblk, int64_t nimgs,
+// One block per image, as the allocating path's grad_finalize_kernel (the same
+// reduction and similarity), the fixed side's standard deviations (clamped at
+// 1e-6) and zero-mean sums read from the statistics words.
+__global__ void finalize_from_stats_kernel(const double* __restrict__ partials, int nblk,
                                            const double* __restrict__ st, float* __restrict__ sims) {
-  const int64_t img = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (img >= nimgs) return;
+  __shared__ double red[6 * (gt::kFinalizeThreads / 32)];
   const double n = st[2];
-  double sdx = sqrt(st[1] / (n - 1.0)), sdy = sqrt(st[4] / (n - 1.0));
-  if (sdx < 1.0e-6) sdx = 1.0e-6;
-  if (sdy < 1.0e-6) sdy = 1.0e-6;
-  double a[6] = {0, 0, 0, 0, 0, 0};
-  const double* p = partials + img * nblk * 6;
-  for (int k = 0; k < nblk; ++k)
-    for (int j = 0; j < 6; ++j) a[j] += p[6 * k + j];
-  const double sx = sim_from(a[0], a[1], a[2], n, sdx, st[6]);
-  const double sy = sim_from(a[3], a[4], a[5], n, sdy, st[8]);
-  sims[img] = 0.5f * ((float)sx + (float)sy);
+  FixedNCC fx{nullptr, sqrt(st[1] / (n - 1.0)), st[6]}, fy{nullptr, sqrt(st[4] / (n - 1.0)), st[8]};
+  if (fx.sd < 1.0e-6) fx.sd = 1.0e-6;
+  if (fy.sd < 1.0e-6) fy.sd = 1.0e-6;
+  const float sim = gt::grad_finalize_image<false>(partials + (int64_t)blockIdx.x * nblk * 6, nblk, n, fx, fy, red);
+  if (threadIdx.x == 0) sims[blockIdx.x] = sim;
 }
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -103,8 +96,11 @@ extern "C" XR_API xr_status xr_grad_ncc_noalloc(const float* d_fixed, const floa
   if (num_moving < 1) return fail(XR_ERR_INVALID_ARG, "xr_grad_ncc_noalloc: num_moving must be >= 1");
   if (smooth_ksize != 0 && smooth_ksize != 3 && smooth_ksize != 5)
     return fail(XR_ERR_UNSUPPORTED, "xr_grad_ncc_noalloc: smoothing kernel must be 0, 3 or 5");
-  if (rows > (1 << 20) || cols > (1 << 20) || num_moving > (1 << 24))
+  if (rows > (1 << 20) || cols > (1 << 20))
     return fail(XR_ERR_INVALID_ARG, "xr_grad_ncc_noalloc: size out of range");
+  if (num_moving > 65535)  // one grid row of the moments launch per moving image
+    return fail(XR_ERR_INVALID_ARG, "xr_grad_ncc_noalloc: at most 65535 moving images per call (got " +
+                                        std::to_string(num_moving) + ")");
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   int nblk = 0;
   XR_CUDA_TRY(launch_grad_moments(nullptr, (int)rows, (int)cols, 0, smooth_ksize, nullptr, nullptr, nullptr, nullptr,
@@ -143,8 +139,7 @@ extern "C" XR_API xr_status xr_grad_ncc_noalloc(const float* d_fixed, const floa
   // moving images: fused blur + Sobel + moments, then the double combine
   XR_CUDA_TRY(launch_grad_moments(d_moving, (int)rows, (int)cols, num_moving, smooth_ksize, fhx, fhy, nullptr,
                                   partials, s, nullptr));
-  finalize_from_stats_kernel<<<(unsigned)((num_moving + 127) / 128), 128, 0, s>>>(partials, nblk, num_moving, stats,
-                                                                                  d_sims);
+  finalize_from_stats_kernel<<<(unsigned)num_moving, gt::kFinalizeThreads, 0, s>>>(partials, nblk, stats, d_sims);
   XR_CUDA_TRY(cudaGetLastError());
   return XR_OK;
 }
