@@ -319,6 +319,8 @@ class PopulationObjective {
     check(xr_obj_eval(h_, (int64_t)poses.size(), poses.empty() ? nullptr : poses[0].data(), out.data()));
     return out;
   }
+  // the fused DRR + grad-NCC kernel instead of the split launches (identical values)
+  void set_fused(bool enable) { check(xr_obj_set_fused(h_, enable ? 1 : 0)); }
   xr_objective handle() const { return h_; }
 
  private:

@@ -57,6 +57,19 @@ class CMAES {
     check(xr_cmaes_get(h_, nullptr, x.data(), best_f, nullptr, generation));
     return x;
   }
+  // The state to device memory: JobSet::regi_step then samples and updates it
+  // inside the step's launches (same bits as the host methods, which refuse
+  // while it is attached); detach_device brings it back.
+  void attach_device(int32_t device = -1) { check(xr_cmaes_attach_device(h_, device)); }
+  void detach_device() { check(xr_cmaes_detach_device(h_)); }
+  // The whole state block (parameters, distribution, last population).
+  std::vector<unsigned char> export_state() const {
+    int64_t n = 0;
+    check(xr_cmaes_state_bytes(h_, &n));
+    std::vector<unsigned char> b((size_t)n);
+    check(xr_cmaes_export_state(h_, b.data(), n));
+    return b;
+  }
   xr_cmaes handle() const { return h_; }
 
  private:
@@ -65,7 +78,8 @@ class CMAES {
 };
 
 // The bound-constrained trust-region optimizer in LN_BOBYQA's level
-// (xregIntensity2D3DRegiNLOptInterface.cpp:83-188): batched asks.
+// (xregIntensity2D3DRegiNLOptInterface.cpp:83-188): Powell's BOBYQA method,
+// the 2n+1 initial points then one point per ask (set_batch for more).
 class TrustRegionDFO {
  public:
   TrustRegionDFO(int32_t dim, const std::vector<double>& x0, const std::vector<double>& lower,
@@ -87,7 +101,14 @@ class TrustRegionDFO {
     return pts;
   }
   void tell(const std::vector<double>& fvals) { check(xr_dfo_tell(h_, fvals.data())); }
-  // 0 continue, 2 rho below rho_end, 3 iteration limit
+  // points per ask after the initial set (before the first tell)
+  void set_batch(int32_t points) { check(xr_dfo_set_batch(h_, points)); }
+  int64_t evaluations() const {
+    int64_t n = 0;
+    check(xr_dfo_evaluations(h_, &n));
+    return n;
+  }
+  // 0 continue, 2 rho reached rho_end, 3 evaluation limit
   int32_t test_for_termination() {
     int32_t r = 0;
     check(xr_dfo_test_termination(h_, &r));
@@ -158,7 +179,8 @@ inline xr_regi_step_job StepJob(PopulationObjective& obj, TrustRegionDFO& d, con
   return j;
 }
 
-// Many registrations' populations with one persistent DRR launch (xr_jobset_*).
+// Many registrations' populations in one step: geometry, DRR and grad-NCC
+// launches over every job (xr_jobset_*).
 class JobSet {
  public:
   explicit JobSet(int32_t device = -1) { check(xr_jobset_create(device, &h_)); }
@@ -166,6 +188,13 @@ class JobSet {
   JobSet(const JobSet&) = delete;
   JobSet& operator=(const JobSet&) = delete;
   void set_stream(void* cuda_stream) { check(xr_jobset_set_stream(h_, cuda_stream)); }
+  // the fused DRR + grad-NCC step instead of the split one (identical values)
+  void set_fused(bool enable) { check(xr_jobset_set_fused(h_, enable ? 1 : 0)); }
+  int32_t last_kernel_launches() const {
+    int32_t n = 0;
+    check(xr_jobset_last_kernel_launches(h_, &n));
+    return n;
+  }
   // values[i][k] for pose k of objs[i]; every objective listed at most once
   std::vector<std::vector<float>> eval(const std::vector<PopulationObjective*>& objs,
                                        const std::vector<std::vector<Mat4>>& poses) {

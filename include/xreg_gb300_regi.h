@@ -13,7 +13,7 @@
 extern "C" {
 #endif
 
-/* CMA-ES state (host, double precision).  Replaces the vendored cmaes.c calls in
+/* CMA-ES state (double precision, on the host or attached to a device).  Replaces the vendored cmaes.c calls in
  * Intensity2D3DRegiCMAES::run (xregIntensity2D3DRegiCMAES.cpp:122-224):
  * cmaes_init, cmaes_SamplePopulation, cmaes_ReSampleSingle,
  * cmaes_UpdateDistribution, cmaes_TestForTermination, cmaes_GetPtr("xmean"/"xbestever"). */
@@ -44,6 +44,22 @@ XR_API xr_status xr_cmaes_lambda(xr_cmaes e, int32_t* lambda);
  * (any pointer may be NULL). */
 XR_API xr_status xr_cmaes_get(xr_cmaes e, double* mean, double* best_x, double* best_f, double* sigma,
                               int64_t* generation);
+/* Moves the state to device memory (device < 0: the current one; at most 8
+ * parameters).  While attached, xr_regi_jobset_step draws each generation's
+ * candidates inside its geometry launch and runs the update inside its metric
+ * launch, with the same bits as the host methods: one source for both
+ * (counter-based normals, one rounding per operation, the transcendental
+ * functions as series of our own).  sample_population, resample_single,
+ * update_distribution and set_stop refuse while attached; get,
+ * test_termination and export_state read the device copy.  No counterpart in
+ * xReg (its optimizer runs on the host between evaluations). */
+XR_API xr_status xr_cmaes_attach_device(xr_cmaes e, int32_t device);
+/* Brings an attached state back to host memory (no-op when on the host). */
+XR_API xr_status xr_cmaes_detach_device(xr_cmaes e);
+/* Size of the whole state block, and a copy of it (parameters, distribution,
+ * eigenbasis, last population with its draws and values, history). */
+XR_API xr_status xr_cmaes_state_bytes(xr_cmaes e, int64_t* bytes);
+XR_API xr_status xr_cmaes_export_state(xr_cmaes e, void* out, int64_t bytes);
 
 /* Bound-constrained derivative-free trust-region optimizer for a final level, in
  * place of NLopt's LN_BOBYQA (Intensity2D3DRegiBOBYQA, xregIntensity2D3DRegiBOBYQA.cpp:28-39;

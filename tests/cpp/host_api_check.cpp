@@ -144,6 +144,20 @@ int main(int argc, char** argv) {
         reason = r.first[0];
         ++gens;
       }
+      // the same level with the optimizer's state on the device: sampled and
+      // updated inside the step's launches, the same state block at the end
+      CMAES es_dev(6, std::vector<double>(6, 0.0), std::vector<double>(lp.sigma, lp.sigma + 6), lp.lambda, lp.seed);
+      es_dev.set_stop(lp.tol_fun, lp.tol_x, lp.max_iters);
+      es_dev.attach_device();
+      int32_t reason_dev = 0, gens_dev = 0;
+      while (reason_dev == 0 && gens_dev < 100) {
+        reason_dev = js.regi_step({StepJob(obj3, es_dev, centre, poses[0], lp.bounds)}).first[0];
+        ++gens_dev;
+      }
+      if (js.last_kernel_launches() != 3) throw Error(XR_ERR_INVALID_ARG, "regi_step: expected 3 launches");
+      es_dev.detach_device();
+      if (gens_dev != gens || reason_dev != reason || es_dev.export_state() != es.export_state())
+        throw Error(XR_ERR_INVALID_ARG, "device CMA-ES state differs from the host optimizer's");
       double bf = 0.0;
       int64_t g = 0;
       const Mat4 b = RegiPoseMap(centre, poses[0], es.best_x(&bf, &g))[0];
