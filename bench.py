@@ -599,12 +599,18 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a, flush, l2_peak):
     v_air[air] = synth.hu_to_lin_att(-1000.0 + np.random.default_rng(17).standard_normal(
         int(air.sum()), dtype=np.float32) * 10.0)
     noisy_air = dataclasses.replace(w.vol, voxels=v_air)
-    for key, vol_k, vt, skipping in (("batched_f16_volume", w.vol, 1, True), ("batched_bf16_volume", w.vol, 2, True),
-                                     ("batched_f32_skipping_off", w.vol, 0, False),
-                                     ("batched_f32_noisy_air", noisy_air, 0, True),
-                                     ("batched_f16_noisy_air", noisy_air, 1, True),
-                                     ("batched_bf16_noisy_air", noisy_air, 2, True)):
+    brick = (3, 1, 1, 4)  # the brick-staged layout: each slab's cells copied to shared memory
+    for key, vol_k, vt, skipping, cfg in (("batched_f16_volume", w.vol, 1, True, None),
+                                          ("batched_bf16_volume", w.vol, 2, True, None),
+                                          ("batched_f32_skipping_off", w.vol, 0, False, None),
+                                          ("batched_f32_noisy_air", noisy_air, 0, True, None),
+                                          ("batched_f16_noisy_air", noisy_air, 1, True, None),
+                                          ("batched_bf16_noisy_air", noisy_air, 2, True, None),
+                                          ("batched_f32_brick_staged", w.vol, 0, True, brick),
+                                          ("batched_f32_brick_staged_skipping_off", w.vol, 0, False, brick)):
         rch = xr.RayCasterLineIntCUDA(dev)
+        if cfg:
+            rch.set_launch_config(*cfg)
         rch.set_stream(stream.cuda_stream)
         rch.set_volume(vol_k, vt)
         rch.set_empty_space_skipping(skipping)
@@ -635,7 +641,7 @@ def _extras(xr, w, fixed, dev, stream, poses, d_sims, a, flush, l2_peak):
         if vt == 2:
             out[key]["tolerance"] = "BF16 volume: DRRs held to 2^-8 of the float32 oracle, outside the 2e-3 " \
                                     "half-precision tolerance"
-        if key in ("batched_f32_skipping_off", "batched_f32_noisy_air"):
+        if key in ("batched_f32_skipping_off", "batched_f32_noisy_air") or cfg:
             ms_k, smp, ld = _drr_kernel_stats(rch, dp.data_ptr(), 5, stream, flush)
             lay = rch.launch_config_ex()
             rf = _roofline(vt, lay[0], ms_k, smp, ld, l2_peak, "")

@@ -242,6 +242,52 @@ def test_launch_configs_are_bit_identical(xr, oracle, vt):
     assert zero == 0.0 and rel <= (TOL32 if vt == 0 else (TOL16 if vt == 1 else TOLBF16))
 
 
+def test_brick_staged_layout_is_bit_identical(xr):
+    """Layout 3 stages each slab's cells in shared memory: every sample, the
+    sample counts and the stored images equal the gathered layouts bit for bit,
+    with skipping on and off, for rays along every axis and oblique ones,
+    detectors that are not multiples of the 16x16 tile, a box too wide for the
+    copy (divergent rays: those slabs read global memory) and store methods."""
+    from xreg_gb300 import _lib
+    from xreg_gb300.se3 import euler_xyz, rigid
+    cases = [(small_volume(9, (40, 36, 44), (1.5, 1.5, 1.5)), small_camera((37, 45), 3.0)),
+             (small_volume(12, (96, 80, 120), (1.0, 1.25, 0.9)), small_camera((53, 71), 2.0)),
+             (small_volume(14, (64, 64, 64), (1.5, 1.5, 1.5)), small_camera((20, 24), 24.0))]
+    for vol, cam in cases:
+        gt = synth.gt_pose(vol)
+        C = vol.xform_img_center_to_itk_phys()
+        extra = [C @ rigid(euler_xyz(*np.radians(a)), np.zeros(3)) @ np.linalg.inv(C) @ gt
+                 for a in ((90.0, 0.0, 0.0), (0.0, 90.0, 0.0), (35.0, 40.0, 10.0), (0.0, 0.0, 180.0))]
+        poses = np.concatenate([synth.sample_poses(vol, gt, 3, 15.0, 10.0, seed=8), np.stack(extra)])
+        for skip in (True, False):
+            rc = _rc(xr, vol, [cam], 0.5)
+            rc.set_empty_space_skipping(skip)
+            rc.set_num_projs(len(poses))
+            rc.allocate_resources()
+            rc.distribute_xforms_among_cam_models(poses)
+            rc.set_count_samples(True)
+            rc.set_launch_config(2, 1, 4, 8)
+            rc.compute()
+            ref, n_ref = rc.projs(), rc.last_num_samples()
+            rc.set_launch_config(3, 1, 1, 4)
+            rc.compute()
+            np.testing.assert_array_equal(rc.projs(), ref)
+            assert rc.last_num_samples() == n_ref
+            # accumulate on top of the last images
+            rc.use_proj_store_accum_method()
+            rc.compute()
+            np.testing.assert_array_equal(rc.projs(), 2.0 * ref)
+    # float32 cells and the sum kernel only
+    vol, cam = cases[0]
+    rc = _rc(xr, vol, [cam], 0.5, 1)
+    rc.set_num_projs(1)
+    rc.allocate_resources()
+    rc.distribute_xforms_among_cam_models(synth.gt_pose(vol)[None])
+    rc.set_launch_config(3, 1, 1, 4)
+    with pytest.raises(_lib.XRegError):
+        rc.compute()
+
+
 def test_cell_layout_can_be_disabled(xr):
     from xreg_gb300 import _lib
     vol = small_volume(10, (16, 16, 16))

@@ -924,6 +924,8 @@ static xr_status rc_choose_config(xr_raycaster rc, const xr_raycaster_s::Vol& vo
       return fail(XR_ERR_INVALID_ARG, "compute: CELL8 layout requested but the volume has no cell copy");
     if (rc->cfg_layout == 2 && vol.type != XR_VOXEL_F32)
       return fail(XR_ERR_INVALID_ARG, "compute: the 256-bit CELL8 read needs a float32 volume");
+    if (rc->cfg_layout == 3 && (vol.type != XR_VOXEL_F32 || p.kernel_id != XR_LINE_INT_SUM))
+      return fail(XR_ERR_INVALID_ARG, "compute: the brick-staged layout needs a float32 volume and the sum kernel");
     p.vol.layout = rc->cfg_layout;
     p.block_warps_x = rc->cfg_bw;
     p.unroll = rc->cfg_unroll;
@@ -1133,7 +1135,7 @@ extern "C" XR_API xr_status xr_rc_set_launch_config_ex(xr_raycaster rc, int32_t 
   XR_CHECK_ARG(rc, "set_launch_config: NULL handle");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || warp_rows == 4 || warp_rows == 8,
                "set_launch_config: warp_rows must be 4 (8x4-pixel warps) or 8 (4x8)");
-  XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= 2, "set_launch_config: bad layout");
+  XR_CHECK_ARG(layout >= XR_LAYOUT_AUTO && layout <= 3, "set_launch_config: bad layout");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || bw == 1 || bw == 2 || bw == 4 || bw == 8,
                "set_launch_config: block_warps_x must be 1, 2, 4 or 8");
   XR_CHECK_ARG(layout == XR_LAYOUT_AUTO || (unroll >= 1 && unroll <= 6),

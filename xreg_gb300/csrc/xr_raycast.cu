@@ -655,6 +655,248 @@ drr_kernel(const DrrParams p, const int64_t proj_base) {
   }
 }
 
+// ---- brick-staged variant (layout 3: float32 CELL8 cells, sum kernel) ----
+// One block traces 16x16 rays of one projection.  Their samples are taken in
+// slabs of cells along the rays' dominant axis: for each slab the block copies
+// the cells its rays reach there (a box from every ray's cell at the slab entry
+// and an estimate of its exit, widened by one cell) into shared memory, then
+// each ray takes its samples in that slab from the copy; a sample whose cell
+// falls outside the box reads global memory.  Positions, cells, fractions and
+// the order of the sum are those of drr_kernel (support-box skipping included,
+// no macro-cell trim), so every value is identical.  The staged alternative to
+// gathering through L1, measured against it; never chosen by the autotuner.
+constexpr int kLayoutBrick = 3;
+constexpr int kBrickCells = 1400;  // 43.75 KB of 32-byte cells
+constexpr int kBrickDepth = 16;    // cells per slab along the dominant axis
+
+// Cell and fractions of a position with drr_kernel's clamping (cell_of, not INSIDE).
+__device__ __forceinline__ void cell3(const VolView& vol, const float pos[3], int c[3], float f[3]) {
+  c[0] = max(min(__float2int_rd(pos[0]), vol.nx - 2), 0);
+  c[1] = max(min(__float2int_rd(pos[1]), vol.ny - 2), 0);
+  c[2] = max(min(__float2int_rd(pos[2]), vol.nz - 2), 0);
+  f[0] = __saturatef(pos[0] - (float)c[0]);
+  f[1] = __saturatef(pos[1] - (float)c[1]);
+  f[2] = __saturatef(pos[2] - (float)c[2]);
+}
+
+// The ray's remaining samples k..last from global memory, in order.
+__device__ __forceinline__ float brick_march_global(const VolView& vol, float pos[3], const float st[3],
+                                                    unsigned int& k, unsigned int last, float sum) {
+  for (; k <= last; ++k) {
+    int c[3];
+    float f[3], v[8];
+    cell3(vol, pos, c, f);
+    Vox<XR_VOXEL_F32>::cell_wide(vol.cells, (c[2] * (vol.ny - 1) + c[1]) * (vol.nx - 1) + c[0], v);
+    sum = __fadd_rn(sum, interp8(v, f[0], f[1], f[2]));
+    pos[0] = __fadd_rn(pos[0], st[0]);
+    pos[1] = __fadd_rn(pos[1], st[1]);
+    pos[2] = __fadd_rn(pos[2], st[2]);
+  }
+  return sum;
+}
+
+__global__ void __launch_bounds__(kThreads, 4) drr_brick_kernel(const DrrParams p, const int64_t proj_base) {
+  __shared__ float4 s_cells[2 * kBrickCells];
+  __shared__ int s_code, s_amin, s_amax, s_lo[3], s_hi[3];
+  const int tid = threadIdx.x;
+  const int col = blockIdx.y * 16 + (tid & 15), row = blockIdx.z * 16 + (tid >> 4);
+  const int64_t proj = proj_base + blockIdx.x;
+  const VolView& vol = p.vol;
+  const int ncell[3] = {vol.nx - 1, vol.ny - 1, vol.nz - 1};
+  const float4* cells = static_cast<const float4*>(vol.cells);
+  if (tid == 0) {
+    s_code = -1;
+    s_amin = 0x7fffffff;
+    s_amax = -1;
+  }
+  const bool pixel = col < p.cols && row < p.rows;
+  float sum = 0.0f, pos[3] = {0.0f, 0.0f, 0.0f}, st[3] = {0.0f, 0.0f, 0.0f};
+  unsigned long long ns = 0;
+  unsigned int nl = 0, k = 1, last = 0;  // samples k..last remain
+  if (pixel) {
+    // xReg's per-ray float set-up and drr_kernel's support-box bounds
+    const float maxb[3] = {(float)(vol.nx - 1), (float)(vol.ny - 1), (float)(vol.nz - 1)};
+    float st0[3], quot;
+    bool hit = xf::ray_setup(p.geo[proj], (float)col, (float)row, maxb, p.step, st0, st, quot);
+    unsigned long long nsteps = hit ? __float2uint_rz(quot) : 0ull;
+    if (hit && !(nsteps <= p.max_steps)) {
+      atomicAdd(p.err_counter, 1u);
+      nsteps = 0;
+      hit = false;
+    }
+    if (hit) {
+      unsigned int first = 0, lst = (unsigned int)nsteps;
+      if (vol.has_support) {
+        float lo = 0.0f, hi = (float)nsteps;
+        if (vol.sup_lo[0] > vol.sup_hi[0]) hi = -1.0f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          if (fabsf(st[a]) > 1.0e-20f) {
+            const float inv = 1.0f / st[a];
+            float u = (vol.sup_lo[a] - st0[a]) * inv, w = (vol.sup_hi[a] - st0[a]) * inv;
+            if (u > w) { const float t = u; u = w; w = t; }
+            lo = fmaxf(lo, u);
+            hi = fminf(hi, w);
+          } else if (!(st0[a] > vol.sup_lo[a] && st0[a] < vol.sup_hi[a])) {
+            hi = -1.0f;
+          }
+        }
+        if (!(lo <= hi)) {
+          lst = 0;
+          first = 1;
+        } else {
+          const float f0 = floorf(lo) - 1.0f, f1 = ceilf(hi) + 1.0f;
+          first = f0 > 0.0f ? (unsigned int)f0 : 0u;
+          lst = f1 < (float)nsteps ? (unsigned int)f1 : (unsigned int)nsteps;
+        }
+      }
+      pos[0] = st0[0]; pos[1] = st0[1]; pos[2] = st0[2];
+      for (unsigned int i = 0, skip = first <= lst ? first : lst + 1u; i < skip; ++i) {
+        pos[0] = __fadd_rn(pos[0], st[0]);
+        pos[1] = __fadd_rn(pos[1], st[1]);
+        pos[2] = __fadd_rn(pos[2], st[2]);
+      }
+      k = first;
+      last = lst;
+      nl = first <= lst ? lst - first + 1u : 0u;
+      ns = nsteps + 1;
+    }
+  }
+  __syncthreads();
+  // the block's axis and direction: claimed by the first ray that has samples
+  int code = -1;
+  if (k <= last) {
+    int a = 0;
+    float m = fabsf(st[0]);
+    if (fabsf(st[1]) > m) { a = 1; m = fabsf(st[1]); }
+    if (fabsf(st[2]) > m) { a = 2; m = fabsf(st[2]); }
+    code = m > 0.0f ? 2 * a + (st[a] > 0.0f ? 1 : 0) : -1;
+    if (code >= 0) atomicCAS(&s_code, -1, code);
+  }
+  __syncthreads();
+  const int bcode = s_code, ax = bcode >> 1, dir = (bcode & 1) ? 1 : -1;
+  const bool staged = k <= last && bcode >= 0 && code == bcode;
+  if (k <= last && !staged) sum = brick_march_global(vol, pos, st, k, last, sum);  // another axis: global reads
+  if (staged) {  // the cells of this ray's first and (about) last samples along the axis
+    int c0[3], c1[3];
+    float f[3];
+    cell3(vol, pos, c0, f);
+    const float e = (float)(last - k);
+    const float pe[3] = {pos[0] + e * st[0], pos[1] + e * st[1], pos[2] + e * st[2]};
+    cell3(vol, pe, c1, f);
+    atomicMin(&s_amin, min(c0[ax], c1[ax]) - 1);
+    atomicMax(&s_amax, max(c0[ax], c1[ax]) + 1);
+  }
+  __syncthreads();
+  if (bcode >= 0) {
+    const int amin = max(s_amin, 0), amax = min(s_amax, ncell[ax] - 1);
+    int z = dir > 0 ? amin : amax;  // first cell of the slab along the axis
+    for (int guard = 0; guard < 8192 && (dir > 0 ? z <= amax : z >= amin); ++guard) {
+      if (tid < 3) {
+        s_lo[tid] = 0x7fffffff;
+        s_hi[tid] = -1;
+      }
+      __syncthreads();
+      const int zfar = dir > 0 ? z + kBrickDepth : z - kBrickDepth;  // first cell past a full slab
+      if (staged && k <= last) {
+        int ce[3], cx[3];
+        float f[3];
+        cell3(vol, pos, ce, f);
+        float m = ((float)zfar - pos[ax]) / st[ax];  // samples to the slab's far side, about
+        m = fminf(fmaxf(m, 0.0f), (float)(last - k));
+        const float pe[3] = {pos[0] + m * st[0], pos[1] + m * st[1], pos[2] + m * st[2]};
+        cell3(vol, pe, cx, f);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          if (a == ax) continue;
+          atomicMin(&s_lo[a], min(ce[a], cx[a]) - 1);
+          atomicMax(&s_hi[a], max(ce[a], cx[a]) + 1);
+        }
+      }
+      __syncthreads();
+      int lo[3], hi[3], lat = 1;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        if (a == ax) continue;
+        lo[a] = max(s_lo[a], 0);
+        hi[a] = min(s_hi[a], ncell[a] - 1);
+        lat *= hi[a] >= lo[a] ? hi[a] - lo[a] + 1 : 0;
+      }
+      // slab depth: the full one, thinner when the box would not fit
+      int d = kBrickDepth;
+      bool use = lat > 0;
+      if (use && lat * d > kBrickCells) {
+        d = kBrickCells / lat;
+        if (d < 1) {
+          d = kBrickDepth;
+          use = false;  // too wide a box: this slab reads global memory
+        }
+      }
+      lo[ax] = dir > 0 ? z : max(z - d + 1, 0);
+      hi[ax] = dir > 0 ? min(z + d - 1, ncell[ax] - 1) : z;
+      const int W = hi[0] - lo[0] + 1, H = hi[1] - lo[1] + 1, Dz = hi[2] - lo[2] + 1;
+      if (use) {
+        const int total = W * H * Dz;
+        for (int i = tid; i < total; i += kThreads) {
+          const int x = lo[0] + i % W, y = lo[1] + (i / W) % H, zz = lo[2] + i / (W * H);
+          const int64_t c = ((int64_t)zz * ncell[1] + y) * ncell[0] + x;
+          s_cells[2 * i] = __ldg(cells + 2 * c);
+          s_cells[2 * i + 1] = __ldg(cells + 2 * c + 1);
+        }
+      }
+      __syncthreads();
+      const int zend = dir > 0 ? z + d : z - d;  // first cell past this slab
+      if (staged) {
+        for (; k <= last; ++k) {
+          int c[3];
+          float f[3], v[8];
+          cell3(vol, pos, c, f);
+          if (dir > 0 ? c[ax] >= zend : c[ax] <= zend) break;
+          const bool in = use && c[0] >= lo[0] && c[0] <= hi[0] && c[1] >= lo[1] && c[1] <= hi[1] && c[2] >= lo[2] &&
+                          c[2] <= hi[2];
+          if (in) {
+            const int i = (c[0] - lo[0]) + W * ((c[1] - lo[1]) + H * (c[2] - lo[2]));
+            const float4 q0 = s_cells[2 * i], q1 = s_cells[2 * i + 1];
+            v[0] = q0.x; v[1] = q0.y; v[2] = q0.z; v[3] = q0.w;
+            v[4] = q1.x; v[5] = q1.y; v[6] = q1.z; v[7] = q1.w;
+          } else {
+            Vox<XR_VOXEL_F32>::cell_wide(vol.cells, (c[2] * ncell[1] + c[1]) * ncell[0] + c[0], v);
+          }
+          sum = __fadd_rn(sum, interp8(v, f[0], f[1], f[2]));
+          pos[0] = __fadd_rn(pos[0], st[0]);
+          pos[1] = __fadd_rn(pos[1], st[1]);
+          pos[2] = __fadd_rn(pos[2], st[2]);
+        }
+      }
+      __syncthreads();  // the copy is read by every ray before the next slab overwrites it
+      z = zend;
+    }
+  }
+  if (k <= last) sum = brick_march_global(vol, pos, st, k, last, sum);  // past the estimated range
+  if (pixel) {
+    sum = __fmul_rn(sum, p.step);
+    const float aa = __fadd_rn(0.0f, sum);
+    const int64_t npix = (int64_t)p.rows * p.cols;
+    const int64_t pix = (int64_t)row * p.cols + col;
+    const int64_t oidx = proj * npix + pix;
+    float prev;
+    if (p.bg_projs) prev = p.bg_projs[(int64_t)p.cam_idx[proj] * npix + pix];
+    else if (p.store == XR_PROJ_STORE_REPLACE) prev = p.default_bg;
+    else prev = p.out[oidx];
+    p.out[oidx] = __fadd_rn(prev, aa);
+  }
+  if (p.sample_counter) {
+    const int lane = tid & 31;
+    unsigned long long nlw = nl;
+    for (int o = 16; o > 0; o >>= 1) {
+      ns += __shfl_down_sync(0xffffffffu, ns, o);
+      nlw += __shfl_down_sync(0xffffffffu, nlw, o);
+    }
+    if (lane == 0 && ns) atomicAdd(p.sample_counter, ns);
+    if (lane == 0 && nlw && p.loaded_counter) atomicAdd(p.loaded_counter, nlw);
+  }
+}
+
 // Fused evaluation: a persistent multi-job DRR loop (every block takes the
 // next (job, tile, projection) item from a global counter; projections are
 // the fastest index within a job), with each job's grad-NCC (5x5 smoothing) computed inside the same launch.
@@ -983,8 +1225,28 @@ __global__ void build_cells_kernel(const float* __restrict__ vox, int nx, int ny
 
 }  // namespace
 
+cudaError_t launch_brick(const DrrParams& p, cudaStream_t s) {
+  if (p.vol.voxel_type != XR_VOXEL_F32 || !p.vol.cells || p.kernel_id != XR_LINE_INT_SUM) return cudaErrorInvalidValue;
+  static std::atomic<bool> carveout_set[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices &&
+      !carveout_set[dev].load(std::memory_order_relaxed)) {
+    // four resident blocks of 44 KB each, the rest of the SM's unified L1 for the global reads
+    cudaFuncSetAttribute(drr_brick_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 80);
+    carveout_set[dev].store(true, std::memory_order_relaxed);
+  }
+  const int64_t max_x = 0x7fffffff;
+  for (int64_t base = 0; base < p.num_projs; base += max_x) {
+    const int64_t n = (p.num_projs - base) < max_x ? (p.num_projs - base) : max_x;
+    const dim3 grid((unsigned)n, (p.cols + 15) / 16, (p.rows + 15) / 16);
+    drr_brick_kernel<<<grid, kThreads, 0, s>>>(p, base);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_drr(const DrrParams& p, cudaStream_t s) {
   if (p.num_projs <= 0) return cudaSuccess;
+  if (p.vol.layout == kLayoutBrick) return launch_brick(p, s);
   if (!(p.block_warps_x == 1 || p.block_warps_x == 2 || p.block_warps_x == 4 || p.block_warps_x == 8))
     return cudaErrorInvalidValue;
   if (p.warp_tall != 0 && p.warp_tall != 1) return cudaErrorInvalidValue;
