@@ -205,7 +205,12 @@ XR_API xr_status xr_rc_last_num_samples(xr_raycaster rc, uint64_t* out);
 XR_API xr_status xr_rc_last_num_loaded_samples(xr_raycaster rc, uint64_t* out);
 /* Enables (1) or disables (0) per-compute sample counting (default off). */
 XR_API xr_status xr_rc_set_count_samples(xr_raycaster rc, int32_t enable);
-/* Launch configuration of the DRR kernel: volume layout (XR_LAYOUT_*), warps
+/* Launch configuration of the DRR kernel: volume layout (XR_LAYOUT_LINEAR,
+ * XR_LAYOUT_CELL8, 2 = the float32 CELL8 copy read with one 256-bit load, or
+ * 3 = brick-staged: 16x16 rays per block, each slab of cells along the rays'
+ * axis copied to shared memory and sampled from there; float32 volumes and the
+ * sum kernel; identical values, measured 3-4x slower than the gather, never
+ * autotuned; block shape and loop are ignored), warps
  * across a 256-thread block (1, 2, 4 or 8; each warp covers 8x4 pixels) and
  * the sample loop: 1 or 2 samples per iteration, or 3 / 4 = 2 / 4 per iteration
  * after each ray is trimmed to its first and last occupied macro cell (sum
