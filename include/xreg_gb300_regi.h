@@ -191,6 +191,20 @@ XR_API xr_status xr_jobset_last_launch(xr_jobset js, int64_t* work_items, int32_
  * other metrics run their metric launches after the DRR either way.  Values
  * identical either way.  No counterpart in xReg. */
 XR_API xr_status xr_jobset_set_fused(xr_jobset js, int32_t enable);
+/* DRR work items of the split step.  Mode 0 (default): one item per (tile,
+ * projection) in each job's autotuned block shape.  Mode 2: every job's items
+ * are (8x8-pixel tile, 4 consecutive projections), each block mapping the 4
+ * poses' rays to threads by how close they are: a 2x4-pixel sub-tile under all
+ * 4 poses per warp when the tile's central ray enters and leaves the volume
+ * within a voxel under all 4 poses (the lanes share cells), one projection per
+ * pair of warps otherwise.  Mode 1: grouped items only for jobs whose next
+ * poses lie within a voxel of each other -- host poses whose volume corners
+ * move less than the smallest spacing between them; a device optimizer's
+ * sampling distribution (3 sigma sqrt(C_ii) after its last update) that does.
+ * Identical values in every mode.  No counterpart in xReg. */
+XR_API xr_status xr_jobset_set_pose_groups(xr_jobset js, int32_t mode);
+/* Jobs of the last step that ran pose-grouped DRR items. */
+XR_API xr_status xr_jobset_last_pose_grouped(xr_jobset js, int32_t* jobs);
 /* Kernel launches the last step issued (not counting the autotuner's timed
  * launches on a shape's first fused step). */
 XR_API xr_status xr_jobset_last_kernel_launches(xr_jobset js, int32_t* launches);

@@ -133,3 +133,35 @@ def test_regi_step_errors_and_counts(xr):
             js.regi_step([bad])
     with pytest.raises(_lib.XRegError):
         _lib.call("xr_regi_jobset_step", js._h, 0, None, None, None)
+
+
+def test_pose_groups_are_identical(xr):
+    """Job-set DRR items of 4 consecutive projections (xr_jobset_set_pose_groups):
+    the same values and DRRs as the per-projection items, for tight populations
+    (the 4 poses' rays within a voxel: one warp per 2x4-pixel sub-tile under all
+    4 poses) and wide ones (one projection per pair of warps), populations that
+    are not multiples of 4, several views, detectors not multiples of 8.  Mode 1
+    groups the tight populations only; mode 2 every one."""
+    jobs = [_job(xr, 31, (48, 44, 40), 0, (37, 45), 1, xr.ImgSimMetric2DGradNCCCUDA, 11),
+            _job(xr, 32, (40, 36, 44), 1, (30, 34), 2, xr.ImgSimMetric2DGradNCCCUDA, 9),
+            _job(xr, 33, (36, 40, 30), 2, (26, 29), 3, xr.ImgSimMetric2DGradNCCCUDA, 7)]
+    for spread in ((10.0, 10.0), (0.02, 0.03)):
+        poses = [synth.sample_poses(j[1], synth.gt_pose(j[1]), p, *spread, seed=40 + i)
+                 for i, (j, p) in enumerate(zip(jobs, (11, 9, 6)))]
+        js = xr.JobSet()
+        base = js.eval([j[0] for j in jobs], poses)
+        drr0 = [j[0].rc.projs().copy() for j in jobs]
+        assert js.last_pose_grouped() == 0
+        for mode in (2, 1):
+            js.set_pose_groups(mode)
+            for rep in range(2):
+                got = js.eval([j[0] for j in jobs], poses)
+                for a, b in zip(base, got):
+                    np.testing.assert_array_equal(a, b)
+                for j, d in zip(jobs, drr0):
+                    np.testing.assert_array_equal(j[0].rc.projs(), d)
+            # geometry, one DRR launch per voxel type (three here), one grad-NCC launch
+            assert js.last_kernel_launches() == 1 + 3 + 1
+            assert js.last_pose_grouped() == (3 if mode == 2 or spread[0] < 1.0 else 0), (mode, spread)
+        with pytest.raises(xr.XRegError):
+            js.set_pose_groups(3)

@@ -170,6 +170,8 @@ _SIGS = {
     "xr_cmaes_get": [H, P, P, C.POINTER(f64), C.POINTER(f64), C.POINTER(i64)],
     "xr_cmaes_state_bytes": [H, C.POINTER(i64)],
     "xr_dfo_set_batch": [H, i32],
+    "xr_jobset_set_pose_groups": [H, i32],
+    "xr_jobset_last_pose_grouped": [H, C.POINTER(i32)],
     "xr_dfo_evaluations": [H, C.POINTER(i64)],
     "xr_cmaes_export_state": [H, P, i64],
     "xr_cmaes_attach_device": [H, i32],

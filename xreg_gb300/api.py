@@ -692,6 +692,18 @@ class JobSet:
         """Batched split (default) or fused evaluation step; identical values (xr_jobset_set_fused)."""
         call("xr_jobset_set_fused", self._h, int(bool(enable)))
 
+    def set_pose_groups(self, mode: int) -> None:
+        """DRR items of 4 consecutive projections mapped by their coherence:
+        0 never, 1 for jobs whose poses lie within a voxel, 2 for every job
+        (xr_jobset_set_pose_groups); identical values in every mode."""
+        call("xr_jobset_set_pose_groups", self._h, int(mode))
+
+    def last_pose_grouped(self) -> int:
+        """Jobs of the last step that ran pose-grouped DRR items."""
+        v = C.c_int32()
+        call("xr_jobset_last_pose_grouped", self._h, C.byref(v))
+        return int(v.value)
+
     def last_kernel_launches(self) -> int:
         """Kernel launches of the last step."""
         v = C.c_int32()

@@ -267,6 +267,7 @@ struct FusedWork {
   int blocks = 0;
   long long items = 0;
   int launches = 0;                   // kernel launches of the last step
+  int pose_grouped = 0;               // jobs of the last step with pose-grouped DRR items
 };
 
 struct xr_objective_s {
@@ -287,6 +288,9 @@ struct xr_objective_s {
   // fused evaluation: mode (1 fused, 0 split DRR and metric launches), its
   // counters (zero between launches) and descriptors
   int32_t fused = 0;
+  // spread of the next population of an attached device optimizer (from the last step's report; < 0 unknown)
+  double next_sd_rot = -1.0, next_sd_trans = -1.0;
+  const void* next_sd_state = nullptr;  // the device state those figures belong to
   DevBuf d_fcnt;
   size_t fcnt_words = 0;
   FusedWork fw;
@@ -2092,7 +2096,7 @@ static int metric_launches(const xr_simmetric_s* m) {
 // ordered on stream s.  Both ways give identical values.
 static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_objective* objs, const int64_t* pops,
                               const double* const* xforms, bool host_in, float* const* sims, bool host_out,
-                              cudaStream_t s, bool fused, const CmaStepJob* cma = nullptr) {
+                              cudaStream_t s, bool fused, const CmaStepJob* cma = nullptr, int pose_group = 0) {
   XR_CHECK_ARG(objs && pops && xforms && sims && n > 0, "evaluation: NULL argument or no jobs");
   auto dev_opt = [&](int32_t i) { return cma != nullptr && cma[i].state != nullptr; };
   bool any_dev = false;
@@ -2103,6 +2107,53 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
   }
   CmaReport* d_report = any_dev ? fw.d_report.as<CmaReport>() : nullptr;
   std::vector<CmaUpdateJob> cu;  // device optimizers whose update has a launch of its own
+  // how far a job's poses spread, in voxels at the volume (nearby poses: pose-grouped DRR items)
+  auto pose_spread_vox = [&](int32_t i, const xr_raycaster_s::Vol& vol, int64_t pop) -> double {
+    const double* sp = vol.desc.spacing;
+    const double vmin = std::min(sp[0], std::min(sp[1], sp[2]));
+    double half[3], radius2 = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      half[a] = 0.5 * (double)vol.desc.n[a] * sp[a];
+      radius2 += half[a] * half[a];
+    }
+    if (dev_opt(i)) {  // the distribution the device optimizer samples next: 3 sigma
+      const xr_objective obj = objs[i];
+      if (obj->next_sd_state != cma[i].state || !(obj->next_sd_rot >= 0.0)) return INFINITY;
+      return 3.0 * (obj->next_sd_trans + obj->next_sd_rot * std::sqrt(radius2)) / vmin;
+    }
+    if (!host_in || pop < 2) return INFINITY;
+    // the volume's corners in each pose's camera frame, against the first pose's
+    const double* P = xforms[i];
+    double Ri[9], ti[3], best = 0.0;
+    auto inv = [&](const double* p, double* R, double* t) {
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) R[r * 3 + c] = p[c * 4 + r];
+      for (int r = 0; r < 3; ++r) t[r] = -(R[r * 3] * p[3] + R[r * 3 + 1] * p[7] + R[r * 3 + 2] * p[11]);
+    };
+    inv(P, Ri, ti);
+    const double* o = vol.desc.origin;
+    const double* dirm = vol.desc.direction;
+    for (int64_t k = 1; k < pop; ++k) {
+      double Rk[9], tk[3];
+      inv(P + 16 * k, Rk, tk);
+      for (int c = 0; c < 8; ++c) {
+        double x[3];
+        for (int a = 0; a < 3; ++a) {
+          double s = o[a];
+          for (int b = 0; b < 3; ++b) s += dirm[a * 3 + b] * (((c >> b) & 1) ? (double)(vol.desc.n[b] - 1) : 0.0) * sp[b];
+          x[a] = s;
+        }
+        double d2 = 0.0;
+        for (int r = 0; r < 3; ++r) {
+          const double u = Rk[r * 3] * x[0] + Rk[r * 3 + 1] * x[1] + Rk[r * 3 + 2] * x[2] + tk[r];
+          const double v = Ri[r * 3] * x[0] + Ri[r * 3 + 1] * x[1] + Ri[r * 3 + 2] * x[2] + ti[r];
+          d2 += (u - v) * (u - v);
+        }
+        best = std::max(best, std::sqrt(d2));
+      }
+    }
+    return best / vmin;
+  };
   std::vector<GeomJob> gj;
   std::vector<FusedJob> fj;
   std::vector<std::vector<FusedView>> fv((size_t)n);
@@ -2161,6 +2212,13 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     const int wc = P.warp_tall ? 4 : 8, tw = wc * P.block_warps_x, th = (8 / P.block_warps_x) * (32 / wc);
     J.d.tiles_x = (int32_t)((P.cols + tw - 1) / tw);
     J.d.tiles_y = (int32_t)((P.rows + th - 1) / th);
+    J.d.pose_group = 0;
+    // items of 4 projections x 8x8 pixels: every job (mode 2) or those whose poses lie within a voxel (mode 1)
+    if (!fused && (pose_group == 2 || (pose_group == 1 && pose_spread_vox(i, vol, pop) < 1.0))) {
+      J.d.pose_group = 4;
+      J.d.tiles_x = (int32_t)((P.cols + 7) / 8);
+      J.d.tiles_y = (int32_t)((P.rows + 7) / 8);
+    }
     rc->last_layout = P.vol.layout;
     rc->last_bw = P.block_warps_x;
     rc->last_unroll = P.unroll;
@@ -2227,9 +2285,10 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
       J.cnt = obj->d_fcnt.as<unsigned int>();
     }
     fj.push_back(J);
-    // one launch per (voxel type, layout): the DRR job kernel runs each job's
-    // loop, the fused kernel the group's first job's (every loop gives the same bits)
-    key.push_back(vol.type * 4 + J.d.p.vol.layout);
+    // one launch per (voxel type, layout, pose-grouped or not): the DRR job kernel
+    // runs each job's loop, the fused kernel the group's first job's (every loop
+    // gives the same bits)
+    key.push_back((vol.type * 4 + J.d.p.vol.layout) * 2 + (J.d.pose_group ? 1 : 0));
   }
   // jobs ordered by group; item numbering restarts in each group
   std::vector<int32_t> keys(key);
@@ -2244,7 +2303,7 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     for (int32_t i = 0; i < n; ++i)
       if (key[(size_t)i] == k) {
         fj[(size_t)i].d.item_begin = items;
-        items += (long long)fj[(size_t)i].d.p.num_projs * fj[(size_t)i].d.tiles_x * fj[(size_t)i].d.tiles_y;
+        items += fj[(size_t)i].d.items();
         order.push_back(i);
       }
     ranges.emplace_back(b, order.size());
@@ -2286,6 +2345,8 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
   XR_CUDA_TRY(cudaMemcpyAsync(fw.d_desc.p, h, bytes, cudaMemcpyHostToDevice, s));
   XR_CUDA_TRY(launch_proj_geom_jobs(reinterpret_cast<const GeomJob*>(d), (int)gj.size(), first, s));
   fw.launches = 1 + tuning_launches;
+  fw.pose_grouped = 0;
+  for (const FusedJob& f : fj) fw.pose_grouped += f.d.pose_group ? 1 : 0;
   fw.items = 0;
   fw.blocks = 0;
   for (size_t gi = 0; gi < ranges.size(); ++gi) {
@@ -2299,7 +2360,7 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
     else {
       XR_CUDA_TRY(launch_drr_jobs(reinterpret_cast<const MultiJobDrr*>(d + off_m) + ranges[gi].first,
                                   (int)(ranges[gi].second - ranges[gi].first), group_items[gi],
-                                  f0.d.p.vol.voxel_type, f0.d.p.vol.layout, s));
+                                  f0.d.p.vol.voxel_type, f0.d.p.vol.layout, f0.d.pose_group != 0, s));
       blocks = (int)std::min<long long>(group_items[gi], 0x7fffffff);
     }
     fw.items += group_items[gi];
@@ -2468,6 +2529,9 @@ struct xr_jobset_s {
   // 0 (default): geometry, DRR and batched grad-NCC launches for every job;
   // 1: fused evaluation step
   int32_t step_mode = 0;
+  // DRR items of 4 consecutive projections: 0 never, 1 for jobs whose poses
+  // lie within a voxel of each other, 2 for every job
+  int32_t pose_group = 0;
   FusedWork fw;
   cudaStream_t stream() const { return has_ext ? ext_stream : own_stream; }
 };
@@ -2512,7 +2576,7 @@ static xr_status jobset_enqueue(xr_jobset js, int32_t n, const xr_objective* obj
   DeviceGuard g(js->device);
   cudaStream_t s = js->stream();
   xr_status st = step_enqueue(js->fw, js->device, n, objs, pops, xforms, host_in, sims, host_out, s,
-                              js->step_mode == 1);
+                              js->step_mode == 1, nullptr, js->pose_group);
   js->last_items = js->fw.items;
   js->blocks = js->fw.blocks;
   return st;
@@ -2570,7 +2634,7 @@ xr_status jobset_step_cma(xr_jobset js, int32_t n, const xr_objective* objs, con
                  "regi_jobset_step: a device optimizer lives on another device than the job set");
   }
   xr_status st = step_enqueue(js->fw, js->device, n, objs, pops, host_xforms, true, host_sims, true, s,
-                              js->step_mode == 1, cma);
+                              js->step_mode == 1, cma, js->pose_group);
   js->last_items = js->fw.items;
   js->blocks = js->fw.blocks;
   if (st != XR_OK) return st;
@@ -2586,7 +2650,14 @@ xr_status jobset_step_cma(xr_jobset js, int32_t n, const xr_objective* objs, con
                                 cudaMemcpyDeviceToHost, s));
   }
   if ((st = jobset_finish(js, n, objs, "regi_jobset_step")) != XR_OK) return st;
-  for (int32_t i = 0; i < n; ++i) reports[i] = any_dev ? js->h_report[i] : CmaReport{0, 0};
+  for (int32_t i = 0; i < n; ++i) {
+    reports[i] = any_dev ? js->h_report[i] : CmaReport{0, 0, -1.0, -1.0};
+    if (cma[i].state) {
+      objs[i]->next_sd_rot = reports[i].sd_rot;
+      objs[i]->next_sd_trans = reports[i].sd_trans;
+      objs[i]->next_sd_state = cma[i].state;
+    }
+  }
   return XR_OK;
 }
 }  // namespace xr
@@ -2600,6 +2671,19 @@ extern "C" XR_API xr_status xr_jobset_eval_device(xr_jobset js, int32_t n, const
 extern "C" XR_API xr_status xr_jobset_set_fused(xr_jobset js, int32_t enable) {
   XR_CHECK_ARG(js, "xr_jobset_set_fused: NULL handle");
   js->step_mode = enable ? 1 : 0;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_jobset_set_pose_groups(xr_jobset js, int32_t mode) {
+  XR_CHECK_ARG(js, "xr_jobset_set_pose_groups: NULL handle");
+  XR_CHECK_ARG(mode >= 0 && mode <= 2, "xr_jobset_set_pose_groups: mode must be 0, 1 or 2");
+  js->pose_group = mode;
+  return XR_OK;
+}
+
+extern "C" XR_API xr_status xr_jobset_last_pose_grouped(xr_jobset js, int32_t* jobs) {
+  XR_CHECK_ARG(js && jobs, "xr_jobset_last_pose_grouped: NULL argument");
+  *jobs = js->fw.pose_grouped;
   return XR_OK;
 }
 

@@ -80,14 +80,23 @@ cudaError_t launch_drr(const DrrParams& p, cudaStream_t s);
 // drr_kernel), where its work items start, and its tile grid.
 struct MultiJobDrr {
   DrrParams p;
-  long long item_begin;  // items of this job: [item_begin, item_begin + num_projs * tiles_x * tiles_y)
+  long long item_begin;  // items of this job: [item_begin, item_begin + items())
   int32_t tiles_x, tiles_y;
+  // 0: one item per (tile, projection) in the job's block shape; 4: one item per
+  // (8x8-pixel tile, group of 4 consecutive projections), mapped to threads by
+  // how close the group's rays are (drr_jobs_kernel)
+  int32_t pose_group;
+  __host__ __device__ long long items() const {
+    const long long units = pose_group ? (p.num_projs + pose_group - 1) / pose_group : p.num_projs;
+    return units * tiles_x * tiles_y;
+  }
 };
 // One launch whose grid covers the (tile, projection) items of jobs sharing a
 // voxel type and layout (no work counter: one block per item); each job runs
 // its own sample loop, p.unroll 3, 4 or 6 (6 with the cell layouts only).
+// grouped: every job's pose_group is 4 (otherwise every job's is 0).
 cudaError_t launch_drr_jobs(const MultiJobDrr* d_jobs, int njobs, long long total_items, int32_t voxel_type,
-                            int32_t layout, cudaStream_t s);
+                            int32_t layout, bool grouped, cudaStream_t s);
 // Macro-cell occupancy bitmask of a volume (see VolView::occ); d_occ holds
 // ceil(nmx * nmy * nmz / 32) words and is cleared here.
 cudaError_t launch_build_occupancy(const float* vox_f32, int nx, int ny, int nz, uint32_t* d_occ, int nmx, int nmy,

@@ -322,7 +322,17 @@ __device__ __noinline__ void cma_update_block(void* state, const float* vals, Cm
   __syncthreads();
   if (tid == 0) {
     cma::finish(s);
-    if (report) report->reason = s.h->reason;
+    if (report) {
+      report->reason = s.h->reason;
+      double r = 0.0, t = 0.0;
+      for (int i = 0; i < n; ++i) {
+        const double sd = s.h->sigma * sqrt(s.C[i * n + i]);
+        if (i < 3) r = fmax(r, sd);
+        else t = fmax(t, sd);
+      }
+      report->sd_rot = r;
+      report->sd_trans = t;
+    }
   }
   __syncthreads();
 }

@@ -1046,7 +1046,9 @@ eval_fused_kernel(const FusedJob* __restrict__ jobs, int njobs, long long total,
 // job's block shape, as drr_kernel.  Each job runs the sample loop its caster's
 // tuner chose (J.p.unroll: loop 3, 4 or, PACKED, 6), at 64 registers (4
 // blocks per SM; measured 3.4% faster than 48 on an uneven set of 8 jobs).
-template <int VT, int LAYOUT, bool PACKED>
+// GROUPED: every job's items are pose groups (MultiJobDrr::pose_group); a
+// separate instantiation, so the per-projection kernels keep their registers.
+template <int VT, int LAYOUT, bool PACKED, bool GROUPED>
 __global__ void __launch_bounds__(kThreads, kMinBlocksPerSM - 2)
 drr_jobs_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long item0) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1059,13 +1061,77 @@ drr_jobs_kernel(const MultiJobDrr* __restrict__ jobs, int njobs, long long item0
   const MultiJobDrr& J = jobs[lo];
   const long long local = item - J.item_begin;
   const long long nproj = J.p.num_projs;
-  const int64_t proj = (int64_t)(local % nproj);
-  const int tile = (int)(local / nproj);
-  const int ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
-  const int bw = J.p.block_warps_x, wl = J.p.warp_tall ? 2 : 3;
-  const int wc = 1 << wl, wr = 32 >> wl;
-  const int col = tx * (wc * bw) + (warp % bw) * wc + (lane & (wc - 1));
-  const int row = ty * ((8 / bw) * wr) + (warp / bw) * wr + (lane >> wl);
+  int64_t proj;
+  int col, row;
+  if constexpr (GROUPED) {
+    // 4 consecutive projections x an 8x8-pixel tile.  When the 4 share a camera
+    // and the tile's central ray meets the volume at nearly the same cells under
+    // all 4 poses (late CMA-ES generations), their rays through a pixel nearly
+    // coincide: each warp takes a 2x4-pixel sub-tile under all 4 poses, so its
+    // lanes share cells; otherwise each pair of warps takes one projection's
+    // tile.  The rays and their values are the same either way.
+    const long long ngrp = (nproj + 3) / 4;
+    const int64_t p0 = (int64_t)(local % ngrp) * 4;
+    const int tile = (int)(local / ngrp);
+    const int ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
+    bool coherent = p0 + 3 < nproj;
+    if (coherent) {
+      // where the tile's central ray of the first pose enters and leaves the
+      // volume, in that pose's camera coordinates; the other poses' camera ->
+      // index affines must put those points within a voxel of it (the
+      // deviation is affine, so the segment's ends bound it along the ray)
+      const ProjGeom& g0 = J.p.geo[p0];
+      const float maxb[3] = {(float)(J.p.vol.nx - 1), (float)(J.p.vol.ny - 1), (float)(J.p.vol.nz - 1)};
+      float st0[3], stv[3], quot;
+      const int cc = min(tx * 8 + 4, J.p.cols - 1), rc = min(ty * 8 + 4, J.p.rows - 1);
+      coherent = xf::ray_setup(g0, (float)cc, (float)rc, maxb, J.p.step, st0, stv, quot) && quot < 1.0e6f;
+      if (coherent) {
+        xf::Affine M0, Mi;
+        for (int k = 0; k < 9; ++k) M0.L[k] = g0.M[k];
+        for (int k = 0; k < 3; ++k) M0.t[k] = g0.M[9 + k];
+        xf::inverse(M0, Mi);
+        float ends[2][3], cam[2][3];
+        for (int k = 0; k < 3; ++k) {
+          ends[0][k] = st0[k];
+          ends[1][k] = st0[k] + quot * stv[k];
+        }
+        xf::apply(Mi, ends[0], cam[0]);
+        xf::apply(Mi, ends[1], cam[1]);
+        float dev = 0.0f;
+        for (int q = 1; q < 4; ++q) {
+          const ProjGeom& g = J.p.geo[p0 + q];
+          coherent = coherent && J.p.cam_idx[p0 + q] == J.p.cam_idx[p0];
+          for (int e = 0; e < 2; ++e)
+            for (int i = 0; i < 3; ++i) {
+              const float v = g.M[3 * i] * cam[e][0] + g.M[3 * i + 1] * cam[e][1] + g.M[3 * i + 2] * cam[e][2] +
+                              g.M[9 + i];
+              dev = fmaxf(dev, fabsf(v - ends[e][i]));
+            }
+        }
+        coherent = coherent && dev < 1.0f;
+      }
+    }
+    int q;
+    if (coherent) {
+      q = lane >> 3;
+      col = tx * 8 + (warp & 3) * 2 + (lane & 1);
+      row = ty * 8 + (warp >> 2) * 4 + ((lane & 7) >> 1);
+    } else {
+      q = warp >> 1;
+      col = tx * 8 + (lane & 7);
+      row = ty * 8 + (warp & 1) * 4 + (lane >> 3);
+    }
+    proj = p0 + q;
+    if (proj >= nproj) return;
+  } else {
+    proj = (int64_t)(local % nproj);
+    const int tile = (int)(local / nproj);
+    const int ty = tile / J.tiles_x, tx = tile - ty * J.tiles_x;
+    const int bw = J.p.block_warps_x, wl = J.p.warp_tall ? 2 : 3;
+    const int wc = 1 << wl, wr = 32 >> wl;
+    col = tx * (wc * bw) + (warp % bw) * wc + (lane & (wc - 1));
+    row = ty * ((8 / bw) * wr) + (warp / bw) * wr + (lane >> wl);
+  }
   if (col >= J.p.cols || row >= J.p.rows) return;
   unsigned int nl;
   const int loop = J.p.unroll;
@@ -1112,22 +1178,28 @@ cudaError_t launch_fused_t(const FusedJob* d_jobs, int njobs, long long total, u
   return cudaGetLastError();
 }
 
-template <int VT, int LAYOUT, bool PACKED>
-cudaError_t launch_jobs_t(const MultiJobDrr* d_jobs, int njobs, long long total, cudaStream_t s) {
+template <int VT, int LAYOUT, bool PACKED, bool GROUPED>
+cudaError_t launch_jobs_g(const MultiJobDrr* d_jobs, int njobs, long long total, cudaStream_t s) {
   static std::atomic<bool> carveout_set[kMaxDevices];
   int dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices &&
       !carveout_set[dev].load(std::memory_order_relaxed)) {
-    cudaFuncSetAttribute(drr_jobs_kernel<VT, LAYOUT, PACKED>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(drr_jobs_kernel<VT, LAYOUT, PACKED, GROUPED>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxL1);
     carveout_set[dev].store(true, std::memory_order_relaxed);
   }
   const long long max_x = 0x7fffffff;
   for (long long base = 0; base < total; base += max_x) {
     const long long n = (total - base) < max_x ? (total - base) : max_x;
-    drr_jobs_kernel<VT, LAYOUT, PACKED><<<(unsigned)n, kThreads, 0, s>>>(d_jobs, njobs, base);
+    drr_jobs_kernel<VT, LAYOUT, PACKED, GROUPED><<<(unsigned)n, kThreads, 0, s>>>(d_jobs, njobs, base);
   }
   return cudaGetLastError();
+}
+
+template <int VT, int LAYOUT, bool PACKED>
+cudaError_t launch_jobs_t(const MultiJobDrr* d_jobs, int njobs, long long total, bool grouped, cudaStream_t s) {
+  return grouped ? launch_jobs_g<VT, LAYOUT, PACKED, true>(d_jobs, njobs, total, s)
+                 : launch_jobs_g<VT, LAYOUT, PACKED, false>(d_jobs, njobs, total, s);
 }
 
 template <int VT, int KERNEL, int LAYOUT, int UNROLL>
@@ -1359,21 +1431,21 @@ cudaError_t launch_eval_fused(const FusedJob* d_jobs, int njobs, long long total
 }
 
 cudaError_t launch_drr_jobs(const MultiJobDrr* d_jobs, int njobs, long long total, int32_t voxel_type, int32_t layout,
-                            cudaStream_t s) {
+                            bool grouped, cudaStream_t s) {
   if (total <= 0) return cudaSuccess;
   switch (voxel_type * 4 + layout) {
     case XR_VOXEL_F32 * 4 + XR_LAYOUT_LINEAR:
-      return launch_jobs_t<XR_VOXEL_F32, XR_LAYOUT_LINEAR, false>(d_jobs, njobs, total, s);
+      return launch_jobs_t<XR_VOXEL_F32, XR_LAYOUT_LINEAR, false>(d_jobs, njobs, total, grouped, s);
     case XR_VOXEL_F32 * 4 + kLayoutCell8Wide:
-      return launch_jobs_t<XR_VOXEL_F32, kLayoutCell8Wide, true>(d_jobs, njobs, total, s);
+      return launch_jobs_t<XR_VOXEL_F32, kLayoutCell8Wide, true>(d_jobs, njobs, total, grouped, s);
     case XR_VOXEL_F16 * 4 + XR_LAYOUT_LINEAR:
-      return launch_jobs_t<XR_VOXEL_F16, XR_LAYOUT_LINEAR, false>(d_jobs, njobs, total, s);
+      return launch_jobs_t<XR_VOXEL_F16, XR_LAYOUT_LINEAR, false>(d_jobs, njobs, total, grouped, s);
     case XR_VOXEL_F16 * 4 + XR_LAYOUT_CELL8:
-      return launch_jobs_t<XR_VOXEL_F16, XR_LAYOUT_CELL8, true>(d_jobs, njobs, total, s);
+      return launch_jobs_t<XR_VOXEL_F16, XR_LAYOUT_CELL8, true>(d_jobs, njobs, total, grouped, s);
     case XR_VOXEL_BF16 * 4 + XR_LAYOUT_LINEAR:
-      return launch_jobs_t<XR_VOXEL_BF16, XR_LAYOUT_LINEAR, false>(d_jobs, njobs, total, s);
+      return launch_jobs_t<XR_VOXEL_BF16, XR_LAYOUT_LINEAR, false>(d_jobs, njobs, total, grouped, s);
     case XR_VOXEL_BF16 * 4 + XR_LAYOUT_CELL8:
-      return launch_jobs_t<XR_VOXEL_BF16, XR_LAYOUT_CELL8, true>(d_jobs, njobs, total, s);
+      return launch_jobs_t<XR_VOXEL_BF16, XR_LAYOUT_CELL8, true>(d_jobs, njobs, total, grouped, s);
     default:
       return cudaErrorInvalidValue;
   }

@@ -30,6 +30,7 @@ struct CmaStepJob {
 struct CmaReport {
   int32_t reason;        // xr_cmaes_test_termination's code after the update
   int32_t sample_error;  // 1: a candidate stayed outside the bounds after kCmaMaxRedraws redraws
+  double sd_rot, sd_trans;  // largest sigma sqrt(C_ii) of the rotation / translation parameters after the update
 };
 
 // The device state of an attached optimizer (false when its state is on the host).
