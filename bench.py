@@ -469,7 +469,7 @@ def run_ours(a, rank, world, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": {"f32": "f32", "f16": "f16-volume/f32-accum", "bf16": "bf16-volume/f32-accum"}[a.voxel],
+        "dtype": {"f32": "f32", "f16": "f16-volume/f16x2-x-blend/f32-accum", "bf16": "bf16-volume/f32-accum"}[a.voxel],
         "data": "synthetic (seeded ellipsoid phantom, sampled poses, noisy fixed DRR)",
         "config": dict(_config(w, a.voxel), l2="flushed between timed steps (256 MB write)",
                        parallelism=f"replicas x{world}"),

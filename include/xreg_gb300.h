@@ -112,7 +112,10 @@ XR_API xr_status xr_rc_synchronize(xr_raycaster rc);
 /* RayCaster::set_volumes (xregRayCastInterface.cpp:38-43).  Voxels are float32 on
  * the host; they are copied to the device now and stored as voxel_type
  * (XR_VOXEL_F16 / BF16 store scale * mu and undo the scale after the ray sum;
- * scale <= 0 picks a power of two automatically). */
+ * scale <= 0 picks a power of two automatically: BF16 1, FP16 the one that
+ * puts max|mu| * scale in [0.5, 1), where the FP16 blend's scaled weights keep
+ * the most precision.  FP16 refuses scale * max|mu| >= 65504 and non-finite
+ * voxels with XR_ERR_INVALID_ARG). */
 XR_API xr_status xr_rc_set_volumes(xr_raycaster rc, int32_t num_vols, const xr_volume_desc* descs,
                                    const float* const* host_voxels, int32_t voxel_type, float scale);
 /* Same, with float32 voxels already in device memory (copied, not borrowed). */

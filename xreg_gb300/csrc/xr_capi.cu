@@ -153,6 +153,7 @@ struct xr_raycaster_s {
     DevBuf cells;            // CELL8 copy (empty when not built)
     int32_t type = XR_VOXEL_F32;
     float inv_scale = 1.0f;
+    float wscale = 1.0f;        // F16: scale of the x weights (VolView::wscale)
     bool has_support = false;   // support box of the non-zero voxels (empty-space skipping)
     float sup_lo[3] = {0, 0, 0}, sup_hi[3] = {0, 0, 0};
     DevBuf occ;                 // macro-cell occupancy bitmask
@@ -498,26 +499,30 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
         XR_CUDA_TRY(cudaMemcpyAsync(tmp.p, voxels[i], (size_t)nv * 4, cudaMemcpyHostToDevice, s));
         src = tmp.as<float>();
       }
-      float sc = scale;
-      if (!(sc > 0.0f)) {
-        sc = 1.0f;
-        if (vt == XR_VOXEL_F16) {
-          XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.as<char>() + 16, 0, 4, s));
-          max_abs_kernel<<<1024, 256, 0, s>>>(src, nv, reinterpret_cast<unsigned int*>(rc->d_counters.as<char>() + 16));
-          XR_CUDA_TRY(cudaGetLastError());
-          unsigned int bits = 0;
-          XR_CUDA_TRY(cudaMemcpyAsync(&bits, rc->d_counters.as<char>() + 16, 4, cudaMemcpyDeviceToHost, s));
-          XR_CUDA_TRY(cudaStreamSynchronize(s));
-          float mx;
-          std::memcpy(&mx, &bits, 4);
-          if (mx > 0.0f && std::isfinite(mx)) {
-            // largest power of two with max * scale < 2^15 (FP16 max is 65504)
-            const int e = (int)std::floor(std::log2(32768.0 / (double)mx));
-            sc = (float)std::ldexp(1.0, e);
-          }
-        }
+      float sc = scale > 0.0f ? scale : 1.0f;
+      if (vt == XR_VOXEL_F16) {
+        // The half2 blend multiplies stored values by x weights scaled by
+        // wscale (so that fractions down to 2^-24 stay normal halves), and the
+        // y blend scales by 2^15 more; the stored maximum times wscale stays
+        // below 2^15.  Automatic scale: the stored maximum in [0.5, 1).
+        XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.as<char>() + 16, 0, 4, s));
+        max_abs_kernel<<<1024, 256, 0, s>>>(src, nv, reinterpret_cast<unsigned int*>(rc->d_counters.as<char>() + 16));
+        XR_CUDA_TRY(cudaGetLastError());
+        unsigned int bits = 0;
+        XR_CUDA_TRY(cudaMemcpyAsync(&bits, rc->d_counters.as<char>() + 16, 4, cudaMemcpyDeviceToHost, s));
+        XR_CUDA_TRY(cudaStreamSynchronize(s));
+        float mx;
+        std::memcpy(&mx, &bits, 4);
+        XR_CHECK_ARG(std::isfinite(mx), "set_volumes: non-finite voxel");
+        if (!(scale > 0.0f) && mx > 0.0f) sc = (float)std::ldexp(1.0, (int)std::floor(std::log2(1.0 / (double)mx)));
+        const double stored = (double)mx * (double)sc;
+        XR_CHECK_ARG(stored < 65504.0, "set_volumes: scale * max|voxel| exceeds the FP16 range");
+        const int we = stored > 0.0 ? (int)std::floor(std::log2(32768.0 / stored)) : 15;
+        v->wscale = (float)std::ldexp(1.0, std::min(we, 15));
+        v->inv_scale = (float)(1.0 / ((double)sc * (double)v->wscale * 32768.0));
+      } else {
+        v->inv_scale = 1.0f / sc;
       }
-      v->inv_scale = 1.0f / sc;
       convert_voxels_kernel<<<2048, 256, 0, s>>>(src, nv, sc, vt, v->voxels.p);
       XR_CUDA_TRY(cudaGetLastError());
       if (rc->build_cells) {
@@ -1066,6 +1071,7 @@ static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, Dr
   p.vol.nz = (int32_t)vol.desc.n[2];
   p.vol.voxel_type = vol.type;
   p.vol.inv_scale = vol.inv_scale;
+  p.vol.wscale = vol.wscale;
   p.vol.has_support = (rc->skip_empty && vol.has_support) ? 1 : 0;
   p.vol.occ = rc->skip_empty ? vol.occ.as<uint32_t>() : nullptr;
   p.vol.nmx = vol.nmx;

@@ -28,6 +28,7 @@ struct VolView {
   int32_t voxel_type;
   int32_t layout;      // XR_LAYOUT_LINEAR / XR_LAYOUT_CELL8
   float inv_scale;     // multiplies the ray sum (1 for F32)
+  float wscale;        // F16: power of two scaling the x weights of the half2 blend
   // Support box: every sample whose continuous index lies outside
   // (sup_lo, sup_hi) on some axis interpolates only zero voxels.  has_support 0
   // disables sample skipping; an all-zero volume has an empty box (lo > hi).

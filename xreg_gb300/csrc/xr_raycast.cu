@@ -71,18 +71,17 @@ struct Vox<XR_VOXEL_F32> {
         : "l"(p), "r"((unsigned)pred));
   }
 };
+// FP16 volumes are blended on their half2 words (interp8_h16 below), so their
+// corners are read as raw 16-bit values and never widened.
 template <>
 struct Vox<XR_VOXEL_F16> {
-  __device__ __forceinline__ static float ld(const void* b, int i) {
-    return __half2float(__ldg(static_cast<const __half*>(b) + i));
+  __device__ __forceinline__ static unsigned int ld16(const void* b, int i) {
+    return __ldg(static_cast<const unsigned short*>(b) + i);
   }
-  __device__ __forceinline__ static void cell(const void* b, int c, float v[8]) {
+  // the 4 z-pair words of cell c (CELL8 layout)
+  __device__ __forceinline__ static void cell_words(const void* b, int c, unsigned int w[4]) {
     const uint4 q = __ldg(static_cast<const uint4*>(b) + c);
-    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
-    const float2 bb = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
-    const float2 cc = __half22float2(*reinterpret_cast<const __half2*>(&q.z));
-    const float2 d = __half22float2(*reinterpret_cast<const __half2*>(&q.w));
-    v[0] = a.x; v[1] = a.y; v[2] = bb.x; v[3] = bb.y; v[4] = cc.x; v[5] = cc.y; v[6] = d.x; v[7] = d.y;
+    w[0] = q.x; w[1] = q.y; w[2] = q.z; w[3] = q.w;
   }
 };
 template <>
@@ -213,8 +212,8 @@ __device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigne
   return d;
 }
 // A cell as four z-pairs of float32 values: the 32-byte float32 cell with one
-// 256-bit load; a 16-byte FP16 / BF16 cell with one 128-bit load, each 32-bit
-// word (v_z0, v_z1) widened to a pair (BF16: a shift and a mask, exactly).
+// 256-bit load; a 16-byte BF16 cell with one 128-bit load, each 32-bit word
+// (v_z0, v_z1) widened to a pair by a shift and a mask, exactly.
 template <int VT>
 __device__ __forceinline__ void cell_pairs(const void* b, int c, unsigned long long q[4]) {
   if constexpr (VT == XR_VOXEL_F32) {
@@ -225,12 +224,8 @@ __device__ __forceinline__ void cell_pairs(const void* b, int c, unsigned long l
     const unsigned int ws[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      if constexpr (VT == XR_VOXEL_BF16) {
-        q[k] = pk2(__uint_as_float(ws[k] << 16), __uint_as_float(ws[k] & 0xffff0000u));
-      } else {
-        const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&ws[k]));
-        q[k] = pk2(f.x, f.y);
-      }
+      static_assert(VT == XR_VOXEL_BF16, "FP16 cells are blended as half2 words");
+      q[k] = pk2(__uint_as_float(ws[k] << 16), __uint_as_float(ws[k] & 0xffff0000u));
     }
   }
 }
@@ -248,6 +243,56 @@ __device__ __forceinline__ float interp8_pairs(const unsigned long long q[4], fl
   return fmaf(b1, fz, b0 * (1.0f - fz));
 }
 
+// ---- FP16 cells: the trilinear on the stored half2 words, with no
+// conversion of the corners.  The x blend runs on the (z0, z1) pairs in half
+// arithmetic (fma.rn.f16x2); the y blend is four mixed-precision fmas
+// (fma.rn.f32.f16: exact products of halves added in float); the z blend is
+// float.  The x weights are scaled by wscale and the y weights by 2^15 before
+// they are rounded to half, so a fraction as small as one float ulp of a
+// position (>= 2^-24) is still a normal half; the stored values times wscale
+// stay below 2^15, so the half blend cannot overflow; the volume's inv_scale
+// removes both scales exactly.  Error: the half rounding of the four weights
+// and of the x blend, about 1e-3 of a sample at worst, within the 2e-3 bound
+// for half-precision volumes.  Every FP16 path (layouts, loops, the fused
+// kernel) uses this one function, so they agree bit for bit.
+__device__ __forceinline__ unsigned int h2_splat(float a) {
+  unsigned int d;
+  asm("cvt.rn.f16x2.f32 %0, %1, %1;" : "=r"(d) : "f"(a));
+  return d;
+}
+__device__ __forceinline__ unsigned int h2_mul(unsigned int a, unsigned int b) {
+  unsigned int d;
+  asm("mul.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned int h2_fma(unsigned int a, unsigned int b, unsigned int c) {
+  unsigned int d;
+  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+// y blend of the half pairs a0 = (a00, a01), a1 = (a10, a11) with the half
+// weights (low gy, high fy) of wy: b0 = a00 gy + a10 fy, b1 = a01 gy + a11 fy
+__device__ __forceinline__ void h2_yblend(unsigned int a0, unsigned int a1, unsigned int wy, float& b0, float& b1) {
+  asm("{\n\t.reg .b16 p0, p1, q0, q1, g, f;\n\t.reg .f32 t, u;\n\t"
+      "mov.b32 {p0, p1}, %2;\n\tmov.b32 {q0, q1}, %3;\n\tmov.b32 {g, f}, %4;\n\t"
+      "fma.rn.f32.f16 t, p0, g, %5;\n\tfma.rn.f32.f16 %0, q0, f, t;\n\t"
+      "fma.rn.f32.f16 u, p1, g, %5;\n\tfma.rn.f32.f16 %1, q1, f, u;\n\t}"
+      : "=f"(b0), "=f"(b1)
+      : "r"(a0), "r"(a1), "r"(wy), "f"(0.0f));
+}
+// w: (v000, v001) (v100, v101) (v010, v011) (v110, v111), low half z = 0;
+// returns the sample times wscale * 2^15
+__device__ __forceinline__ float interp8_h16(const unsigned int w[4], float fx, float fy, float fz, float ws) {
+  constexpr float kYs = 32768.0f;
+  const unsigned int FX = h2_splat(__fmul_rn(fx, ws)), GX = h2_splat(__fmaf_rn(-fx, ws, ws));
+  const __half2 wy = __floats2half2_rn(__fmaf_rn(-fy, kYs, kYs), __fmul_rn(fy, kYs));  // (gy, fy)
+  const unsigned int A0 = h2_fma(w[1], FX, h2_mul(w[0], GX));  // (a00, a01)
+  const unsigned int A1 = h2_fma(w[3], FX, h2_mul(w[2], GX));  // (a10, a11)
+  float b0, b1;
+  h2_yblend(A0, A1, *reinterpret_cast<const unsigned int*>(&wy), b0, b1);
+  return __fmaf_rn(b1, fz, __fmul_rn(b0, __fsub_rn(1.0f, fz)));
+}
+
 // Trilinear sample at index position (px, py, pz) with ITK's boundary rule:
 // the position is clamped to [0, n-1], the cell to [0, n-2], so a neighbour past
 // the last index gets weight 0 (weight 1 on the last voxel).  The weighted form
@@ -260,12 +305,14 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
   // 0 the cell is 0 and the fraction 0, above n-1 the cell is n-2 and the
   // fraction 1, and a NaN position reads cell 0 with fraction 0.
   float v[8], fx, fy, fz;
+  [[maybe_unused]] unsigned int w[4];
   if (LAYOUT == kLayoutCell8Wide) {
     const int c = cell_of<INSIDE, true>(vol, px, py, pz, fx, fy, fz);
     if constexpr (VT == XR_VOXEL_F32) Vox<VT>::cell_wide(data, c, v);
   } else if (LAYOUT == XR_LAYOUT_CELL8) {
     const int c = cell_of<INSIDE, VT == XR_VOXEL_F32>(vol, px, py, pz, fx, fy, fz);
-    Vox<VT>::cell(data, c, v);
+    if constexpr (VT == XR_VOXEL_F16) Vox<VT>::cell_words(data, c, w);
+    else Vox<VT>::cell(data, c, v);
   } else {
     const int nx = vol.nx, ny = vol.ny;
     int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
@@ -283,16 +330,24 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
     }
     const int sy = nx, sz = nx * ny;
     const int b = (iz * ny + iy) * nx + ix;
-    v[0] = Vox<VT>::ld(data, b);
-    v[1] = Vox<VT>::ld(data, b + sz);
-    v[2] = Vox<VT>::ld(data, b + 1);
-    v[3] = Vox<VT>::ld(data, b + sz + 1);
-    v[4] = Vox<VT>::ld(data, b + sy);
-    v[5] = Vox<VT>::ld(data, b + sz + sy);
-    v[6] = Vox<VT>::ld(data, b + sy + 1);
-    v[7] = Vox<VT>::ld(data, b + sz + sy + 1);
+    if constexpr (VT == XR_VOXEL_F16) {  // the CELL8 words, packed from 8 scalar reads
+      w[0] = Vox<VT>::ld16(data, b) | (Vox<VT>::ld16(data, b + sz) << 16);
+      w[1] = Vox<VT>::ld16(data, b + 1) | (Vox<VT>::ld16(data, b + sz + 1) << 16);
+      w[2] = Vox<VT>::ld16(data, b + sy) | (Vox<VT>::ld16(data, b + sz + sy) << 16);
+      w[3] = Vox<VT>::ld16(data, b + sy + 1) | (Vox<VT>::ld16(data, b + sz + sy + 1) << 16);
+    } else {
+      v[0] = Vox<VT>::ld(data, b);
+      v[1] = Vox<VT>::ld(data, b + sz);
+      v[2] = Vox<VT>::ld(data, b + 1);
+      v[3] = Vox<VT>::ld(data, b + sz + 1);
+      v[4] = Vox<VT>::ld(data, b + sy);
+      v[5] = Vox<VT>::ld(data, b + sz + sy);
+      v[6] = Vox<VT>::ld(data, b + sy + 1);
+      v[7] = Vox<VT>::ld(data, b + sz + sy + 1);
+    }
   }
-  return interp8(v, fx, fy, fz);
+  if constexpr (VT == XR_VOXEL_F16) return interp8_h16(w, fx, fy, fz, vol.wscale);
+  else return interp8(v, fx, fy, fz);
 }
 
 // Walks the macro cells of the ray p0 + k st from k = kstart towards kend
@@ -381,19 +436,36 @@ __device__ __forceinline__ float march_packed_inside(const VolView& vol, const v
     pz = __fadd_rn(pz, sz);
     return (int)((bz * uy + by) * ux + bx - bias);
   };
-  for (; n >= 4; n -= 4) {
-    float f[4][3];
-    unsigned long long q[4][4];
+  if constexpr (VT == XR_VOXEL_F16) {  // half2 words blended as stored
+    for (; n >= 4; n -= 4) {
+      float f[4][3];
+      unsigned int w[4][4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) cell_pairs<VT>(data, locate(f[k][0], f[k][1], f[k][2]), q[k]);
+      for (int k = 0; k < 4; ++k) Vox<VT>::cell_words(data, locate(f[k][0], f[k][1], f[k][2]), w[k]);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) sum = __fadd_rn(sum, interp8_pairs(q[k], f[k][0], f[k][1], f[k][2]));
-  }
-  for (; n > 0; --n) {
-    float fx, fy, fz;
-    unsigned long long q[4];
-    cell_pairs<VT>(data, locate(fx, fy, fz), q);
-    sum = __fadd_rn(sum, interp8_pairs(q, fx, fy, fz));
+      for (int k = 0; k < 4; ++k) sum = __fadd_rn(sum, interp8_h16(w[k], f[k][0], f[k][1], f[k][2], vol.wscale));
+    }
+    for (; n > 0; --n) {
+      float fx, fy, fz;
+      unsigned int w[4];
+      Vox<VT>::cell_words(data, locate(fx, fy, fz), w);
+      sum = __fadd_rn(sum, interp8_h16(w, fx, fy, fz, vol.wscale));
+    }
+  } else {
+    for (; n >= 4; n -= 4) {
+      float f[4][3];
+      unsigned long long q[4][4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) cell_pairs<VT>(data, locate(f[k][0], f[k][1], f[k][2]), q[k]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) sum = __fadd_rn(sum, interp8_pairs(q[k], f[k][0], f[k][1], f[k][2]));
+    }
+    for (; n > 0; --n) {
+      float fx, fy, fz;
+      unsigned long long q[4];
+      cell_pairs<VT>(data, locate(fx, fy, fz), q);
+      sum = __fadd_rn(sum, interp8_pairs(q, fx, fy, fz));
+    }
   }
   return sum;
 }
