@@ -238,6 +238,14 @@ XR_API xr_status xr_rc_get_launch_config_ex(xr_raycaster rc, int32_t* layout, in
                                             int32_t* unroll, int32_t* warp_rows);
 /* Whether set_volumes also builds the CELL8 copy (default 1).  Set before set_volumes. */
 XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable);
+/* Order of the CELL8 cells in memory for volumes set after this call:
+ * 0 = x fastest, then y, then z; 1 (default) = z fastest, then x, then y.  A
+ * warp's rays meet a few neighbouring cells per sample, and the order whose
+ * fastest axis runs across the rays (z for C-arm views orbiting the patient's
+ * long axis) puts more of them in one 128-byte line: measured 2.7 % faster
+ * on a 256^3 float32 volume with 384^2 views about z, no change with FP16
+ * cells or without empty-space skipping.  Values identical in either order. */
+XR_API xr_status xr_rc_set_cell_order(xr_raycaster rc, int32_t order);
 /* Empty-space skipping for the line-integral sum (default 1): samples whose
  * trilinear cell lies outside the bounding box of the volume's non-zero voxels
  * add exactly zero, so they are not loaded; positions still advance by the same

@@ -28,6 +28,8 @@
 //           for FP32, or one 32-byte load for FP32 (the 256-bit read, layout 2).
 //           It spends 8x the voxel bytes of HBM to cut L1 requests per sample
 //           from 8 to 1-2; the linear kernel is bound by exactly those requests.
+//           Cells are numbered by the strides VolView::cs: z fastest by
+//           default, x fastest selectable (xr_rc_set_cell_order).
 #include "xr_internal.h"
 #include "xr_gradtile.cuh"
 
@@ -140,11 +142,11 @@ __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, f
     fx = __fsub_rn(px, __fsub_rn(tx, kTwo23));
     fy = __fsub_rn(py, __fsub_rn(ty, kTwo23));
     fz = __fsub_rn(pz, __fsub_rn(tz, kTwo23));
-    const unsigned int ux = (unsigned int)(nx - 1), uy = (unsigned int)(ny - 1), kb = 0x4B000000u;
-    const unsigned int bias = kb * (uy * ux + ux + 1u);
+    const unsigned int sx = (unsigned int)vol.cs[0], sy = (unsigned int)vol.cs[1], sz = (unsigned int)vol.cs[2];
+    const unsigned int bias = 0x4B000000u * (sx + sy + sz);
     const unsigned int bx = (unsigned int)__float_as_int(tx), by = (unsigned int)__float_as_int(ty),
                        bz = (unsigned int)__float_as_int(tz);
-    return (int)((bz * uy + by) * ux + bx - bias);
+    return (int)(bx * sx + by * sy + bz * sz - bias);
   }
   int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
   if (INSIDE) {
@@ -159,7 +161,7 @@ __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, f
     fy = __saturatef(py - (float)iy);
     fz = __saturatef(pz - (float)iz);
   }
-  return (iz * (ny - 1) + iy) * (nx - 1) + ix;
+  return ix * vol.cs[0] + iy * vol.cs[1] + iz * vol.cs[2];
 }
 
 // Weighted-form trilinear of the 8 corners in cell order (z-pairs):
@@ -419,8 +421,8 @@ __device__ __forceinline__ float march_packed_inside(const VolView& vol, const v
   constexpr float kTwo23 = 8388608.0f;
   const unsigned long long K = pk2(kTwo23, kTwo23), S = pk2(sx, sy);
   unsigned long long P = pk2(px, py);
-  const unsigned int ux = (unsigned int)(vol.nx - 1), uy = (unsigned int)(vol.ny - 1), kb = 0x4B000000u;
-  const unsigned int bias = kb * (uy * ux + ux + 1u);
+  const unsigned int csx = (unsigned int)vol.cs[0], csy = (unsigned int)vol.cs[1], csz = (unsigned int)vol.cs[2];
+  const unsigned int bias = 0x4B000000u * (csx + csy + csz);
   // cell index and fractions of the current position, then advance it
   auto locate = [&](float& fx, float& fy, float& fz) -> int {
     const unsigned long long T = add2_rm(P, K);
@@ -434,7 +436,7 @@ __device__ __forceinline__ float march_packed_inside(const VolView& vol, const v
                        bz = (unsigned int)__float_as_int(tz);
     P = add2(P, S);
     pz = __fadd_rn(pz, sz);
-    return (int)((bz * uy + by) * ux + bx - bias);
+    return (int)(bx * csx + by * csy + bz * csz - bias);
   };
   if constexpr (VT == XR_VOXEL_F16) {  // half2 words blended as stored
     for (; n >= 4; n -= 4) {
@@ -758,7 +760,7 @@ __device__ __forceinline__ float brick_march_global(const VolView& vol, float po
     int c[3];
     float f[3], v[8];
     cell3(vol, pos, c, f);
-    Vox<XR_VOXEL_F32>::cell_wide(vol.cells, (c[2] * (vol.ny - 1) + c[1]) * (vol.nx - 1) + c[0], v);
+    Vox<XR_VOXEL_F32>::cell_wide(vol.cells, c[0] * vol.cs[0] + c[1] * vol.cs[1] + c[2] * vol.cs[2], v);
     sum = __fadd_rn(sum, interp8(v, f[0], f[1], f[2]));
     pos[0] = __fadd_rn(pos[0], st[0]);
     pos[1] = __fadd_rn(pos[1], st[1]);
@@ -911,7 +913,7 @@ __global__ void __launch_bounds__(kThreads, 4) drr_brick_kernel(const DrrParams 
         const int total = W * H * Dz;
         for (int i = tid; i < total; i += kThreads) {
           const int x = lo[0] + i % W, y = lo[1] + (i / W) % H, zz = lo[2] + i / (W * H);
-          const int64_t c = ((int64_t)zz * ncell[1] + y) * ncell[0] + x;
+          const int64_t c = (int64_t)x * vol.cs[0] + (int64_t)y * vol.cs[1] + (int64_t)zz * vol.cs[2];
           s_cells[2 * i] = __ldg(cells + 2 * c);
           s_cells[2 * i + 1] = __ldg(cells + 2 * c + 1);
         }
@@ -932,7 +934,7 @@ __global__ void __launch_bounds__(kThreads, 4) drr_brick_kernel(const DrrParams 
             v[0] = q0.x; v[1] = q0.y; v[2] = q0.z; v[3] = q0.w;
             v[4] = q1.x; v[5] = q1.y; v[6] = q1.z; v[7] = q1.w;
           } else {
-            Vox<XR_VOXEL_F32>::cell_wide(vol.cells, (c[2] * ncell[1] + c[1]) * ncell[0] + c[0], v);
+            Vox<XR_VOXEL_F32>::cell_wide(vol.cells, c[0] * vol.cs[0] + c[1] * vol.cs[1] + c[2] * vol.cs[2], v);
           }
           sum = __fadd_rn(sum, interp8(v, f[0], f[1], f[2]));
           pos[0] = __fadd_rn(pos[0], st[0]);
@@ -1335,13 +1337,17 @@ cudaError_t launch_kernel_id(const DrrParams& p, cudaStream_t s) {
                                         : launch_layout<VT, XR_LINE_INT_SUM>(p, s);
 }
 
-// One thread per cell: gathers the 8 corners from the float32 voxels.
+// One thread per cell (x fastest, so the voxel reads coalesce): gathers the 8
+// corners from the float32 voxels and stores them as cell number
+// ix cs[0] + iy cs[1] + iz cs[2].
 template <int VT>
-__global__ void build_cells_kernel(const float* __restrict__ vox, int nx, int ny, int nz, float scale, void* out) {
+__global__ void build_cells_kernel(const float* __restrict__ vox, int nx, int ny, int nz, float scale, int32_t csx,
+                                   int32_t csy, int32_t csz, void* out) {
   const int64_t ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
   const int64_t ncell = ncx * ncy * ncz;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t ix = c % ncx, iy = (c / ncx) % ncy, iz = c / (ncx * ncy);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ix = t % ncx, iy = (t / ncx) % ncy, iz = t / (ncx * ncy);
+    const int64_t c = ix * csx + iy * csy + iz * csz;
     const int64_t b = (iz * ny + iy) * nx + ix, sy = nx, sz = (int64_t)nx * ny;
     // z-pairs: v000 v001 v100 v101 v010 v011 v110 v111 (vxyz)
     const float v[8] = {vox[b], vox[b + sz], vox[b + 1], vox[b + sz + 1],
@@ -1529,14 +1535,33 @@ size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type)
 }
 
 cudaError_t launch_build_cells(const float* vox_f32, int nx, int ny, int nz, int32_t voxel_type, float scale,
-                               void* out, cudaStream_t s) {
+                               const int32_t cs[3], void* out, cudaStream_t s) {
   switch (voxel_type) {
-    case XR_VOXEL_F32: build_cells_kernel<XR_VOXEL_F32><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, 1.0f, out); break;
-    case XR_VOXEL_F16: build_cells_kernel<XR_VOXEL_F16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, out); break;
-    case XR_VOXEL_BF16: build_cells_kernel<XR_VOXEL_BF16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, out); break;
+    case XR_VOXEL_F32:
+      build_cells_kernel<XR_VOXEL_F32><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, 1.0f, cs[0], cs[1], cs[2], out);
+      break;
+    case XR_VOXEL_F16:
+      build_cells_kernel<XR_VOXEL_F16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, cs[0], cs[1], cs[2], out);
+      break;
+    case XR_VOXEL_BF16:
+      build_cells_kernel<XR_VOXEL_BF16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, cs[0], cs[1], cs[2], out);
+      break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+void cell_strides(int64_t nx, int64_t ny, int64_t nz, int32_t order, int32_t cs[3]) {
+  const int32_t cx = (int32_t)(nx - 1), cy = (int32_t)(ny - 1), cz = (int32_t)(nz - 1);
+  if (order == 1) {
+    cs[2] = 1;
+    cs[0] = cz;
+    cs[1] = cz * cx;
+  } else {
+    cs[0] = 1;
+    cs[1] = cx;
+    cs[2] = cx * cy;
+  }
 }
 
 }  // namespace xr
