@@ -190,9 +190,16 @@ class JobSet {
   void set_stream(void* cuda_stream) { check(xr_jobset_set_stream(h_, cuda_stream)); }
   // the fused DRR + grad-NCC step instead of the split one (identical values)
   void set_fused(bool enable) { check(xr_jobset_set_fused(h_, enable ? 1 : 0)); }
+  // DRR items of 4 consecutive projections: 0 never, 1 tight populations, 2 every job (identical values)
+  void set_pose_groups(int32_t mode) { check(xr_jobset_set_pose_groups(h_, mode)); }
   int32_t last_kernel_launches() const {
     int32_t n = 0;
     check(xr_jobset_last_kernel_launches(h_, &n));
+    return n;
+  }
+  int32_t last_pose_grouped() const {
+    int32_t n = 0;
+    check(xr_jobset_last_pose_grouped(h_, &n));
     return n;
   }
   // values[i][k] for pose k of objs[i]; every objective listed at most once

@@ -158,6 +158,22 @@ int main(int argc, char** argv) {
       es_dev.detach_device();
       if (gens_dev != gens || reason_dev != reason || es_dev.export_state() != es.export_state())
         throw Error(XR_ERR_INVALID_ARG, "device CMA-ES state differs from the host optimizer's");
+      // again with pose-grouped DRR items for the generations whose samples lie within a voxel
+      CMAES es_pg(6, std::vector<double>(6, 0.0), std::vector<double>(lp.sigma, lp.sigma + 6), lp.lambda, lp.seed);
+      es_pg.set_stop(lp.tol_fun, lp.tol_x, lp.max_iters);
+      es_pg.attach_device();
+      js.set_pose_groups(1);
+      int32_t reason_pg = 0, gens_pg = 0, grouped = 0;
+      while (reason_pg == 0 && gens_pg < 100) {
+        reason_pg = js.regi_step({StepJob(obj3, es_pg, centre, poses[0], lp.bounds)}).first[0];
+        grouped += js.last_pose_grouped();
+        ++gens_pg;
+      }
+      js.set_pose_groups(0);
+      es_pg.detach_device();
+      if (gens_pg != gens || reason_pg != reason || es_pg.export_state() != es.export_state())
+        throw Error(XR_ERR_INVALID_ARG, "pose-grouped items changed the device optimizer's run");
+      std::printf("pose-grouped generations: %d of %d\n", grouped, gens_pg);
       double bf = 0.0;
       int64_t g = 0;
       const Mat4 b = RegiPoseMap(centre, poses[0], es.best_x(&bf, &g))[0];
