@@ -112,10 +112,10 @@ XR_API xr_status xr_rc_synchronize(xr_raycaster rc);
 /* RayCaster::set_volumes (xregRayCastInterface.cpp:38-43).  Voxels are float32 on
  * the host; they are copied to the device now and stored as voxel_type
  * (XR_VOXEL_F16 / BF16 store scale * mu and undo the scale after the ray sum;
- * scale <= 0 picks a power of two automatically: BF16 1, FP16 the one that
- * puts max|mu| * scale in [0.5, 1), where the FP16 blend's scaled weights keep
- * the most precision.  FP16 refuses scale * max|mu| >= 65504 and non-finite
- * voxels with XR_ERR_INVALID_ARG). */
+ * scale <= 0 picks a power of two automatically (BF16: 1).  FP16 always
+ * stores max|mu| scaled into [0.5, 1) by a power of two, which its blend's
+ * scaled weights need, and does not use scale; it refuses non-finite voxels
+ * and a nonzero maximum below 2^-90 with XR_ERR_INVALID_ARG). */
 XR_API xr_status xr_rc_set_volumes(xr_raycaster rc, int32_t num_vols, const xr_volume_desc* descs,
                                    const float* const* host_voxels, int32_t voxel_type, float scale);
 /* Same, with float32 voxels already in device memory (copied, not borrowed). */
@@ -238,14 +238,6 @@ XR_API xr_status xr_rc_get_launch_config_ex(xr_raycaster rc, int32_t* layout, in
                                             int32_t* unroll, int32_t* warp_rows);
 /* Whether set_volumes also builds the CELL8 copy (default 1).  Set before set_volumes. */
 XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable);
-/* Order of the CELL8 cells in memory for volumes set after this call:
- * 0 = x fastest, then y, then z; 1 (default) = z fastest, then x, then y.  A
- * warp's rays meet a few neighbouring cells per sample, and the order whose
- * fastest axis runs across the rays (z for C-arm views orbiting the patient's
- * long axis) puts more of them in one 128-byte line: measured 2.7 % faster
- * on a 256^3 float32 volume with 384^2 views about z, no change with FP16
- * cells or without empty-space skipping.  Values identical in either order. */
-XR_API xr_status xr_rc_set_cell_order(xr_raycaster rc, int32_t order);
 /* Empty-space skipping for the line-integral sum (default 1): samples whose
  * trilinear cell lies outside the bounding box of the volume's non-zero voxels
  * add exactly zero, so they are not loaded; positions still advance by the same

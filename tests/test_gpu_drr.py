@@ -22,9 +22,8 @@ TOL16 = 2e-3
 TOLBF16 = 2.0 ** -8
 
 
-def _rc(xr, vol, cams, step, voxel_type=0, cell_order=1):
+def _rc(xr, vol, cams, step, voxel_type=0):
     rc = xr.RayCasterLineIntCUDA()
-    rc.set_cell_order(cell_order)
     rc.set_volume(vol, voxel_type)
     rc.set_camera_models(cams)
     rc.set_ray_step_size(step)
@@ -287,41 +286,6 @@ def test_brick_staged_layout_is_bit_identical(xr):
     rc.set_launch_config(3, 1, 1, 4)
     with pytest.raises(_lib.XRegError):
         rc.compute()
-
-
-@pytest.mark.parametrize("vt", [0, 1, 2])
-def test_cell_orders_are_bit_identical(xr, vt):
-    """CELL8 cells stored z fastest (xr_rc_set_cell_order(1)) give the same
-    bits as x fastest, in every cell layout (the brick-staged one too) and
-    loop, with skipping on and off, for rays along every axis and oblique ones
-    on an anisotropic volume whose dimensions differ."""
-    from xreg_gb300.se3 import euler_xyz, rigid
-    vol = small_volume(15, (46, 38, 52), (1.1, 1.4, 0.9))
-    cam = small_camera((37, 45), 3.0)
-    gt = synth.gt_pose(vol)
-    C = vol.xform_img_center_to_itk_phys()
-    extra = [C @ rigid(euler_xyz(*np.radians(a)), np.zeros(3)) @ np.linalg.inv(C) @ gt
-             for a in ((90.0, 0.0, 0.0), (0.0, 90.0, 0.0), (35.0, 40.0, 10.0))]
-    poses = np.concatenate([synth.sample_poses(vol, gt, 3, 15.0, 10.0, seed=9), np.stack(extra)])
-    configs = [(1, 2, 3, 4), (1, 1, 4, 8), (1, 1, 6, 8)]
-    if vt == 0:
-        configs += [(2, 1, 4, 8), (2, 2, 6, 4), (2, 1, 5, 8), (3, 1, 1, 4)]
-    for skip in (True, False):
-        ref = None
-        for order in (0, 1):
-            rc = _rc(xr, vol, [cam], 0.5, vt, order)
-            rc.set_empty_space_skipping(skip)
-            rc.set_num_projs(len(poses))
-            rc.allocate_resources()
-            rc.distribute_xforms_among_cam_models(poses)
-            for cfg in configs:
-                rc.set_launch_config(*cfg)
-                rc.compute()
-                if ref is None:
-                    ref = rc.projs()
-                np.testing.assert_array_equal(rc.projs(), ref, err_msg=f"order {order} config {cfg}")
-    with pytest.raises(xr.XRegError):
-        xr.RayCasterLineIntCUDA().set_cell_order(2)
 
 
 def test_cell_layout_can_be_disabled(xr):

@@ -126,7 +126,6 @@ _SIGS = {
     "xr_rc_set_launch_config_ex": [H, i32, i32, i32, i32],
     "xr_rc_get_launch_config_ex": [H, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],
     "xr_rc_set_build_cell_layout": [H, i32],
-    "xr_rc_set_cell_order": [H, i32],
     "xr_rc_set_empty_space_skipping": [H, i32],
     "xr_sm_create": [i32, i32, C.POINTER(H)],
     "xr_sm_destroy": [H],

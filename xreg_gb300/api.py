@@ -331,11 +331,6 @@ class RayCasterLineIntCUDA:
     def set_build_cell_layout(self, enable: bool) -> None:
         call("xr_rc_set_build_cell_layout", self._h, int(bool(enable)))
 
-    def set_cell_order(self, order: int) -> None:
-        """CELL8 cell order of volumes set from now on: 0 x fastest, 1 z fastest
-        (the default; xr_rc_set_cell_order); values identical in either order."""
-        call("xr_rc_set_cell_order", self._h, int(order))
-
     def set_empty_space_skipping(self, enable: bool) -> None:
         call("xr_rc_set_empty_space_skipping", self._h, int(bool(enable)))
 

@@ -153,9 +153,7 @@ struct xr_raycaster_s {
     DevBuf cells;            // CELL8 copy (empty when not built)
     int32_t type = XR_VOXEL_F32;
     float inv_scale = 1.0f;
-    float wscale = 1.0f;        // F16: scale of the x weights (VolView::wscale)
-    int32_t cell_order = 0;     // CELL8 order (cell_strides) and its strides (VolView::cs)
-    int32_t cs[3] = {0, 0, 0};
+    int32_t cs[2] = {0, 0};     // CELL8 cell strides (VolView::cs)
     bool has_support = false;   // support box of the non-zero voxels (empty-space skipping)
     float sup_lo[3] = {0, 0, 0}, sup_hi[3] = {0, 0, 0};
     DevBuf occ;                 // macro-cell occupancy bitmask
@@ -163,7 +161,6 @@ struct xr_raycaster_s {
   };
   bool skip_empty = true;
   bool build_cells = true;
-  int32_t cell_order = 1;  // CELL8 order of volumes set from now on (cell_strides): z fastest
   int32_t cfg_layout = XR_LAYOUT_AUTO, cfg_bw = 2, cfg_unroll = 1, cfg_warp_rows = 4;  // requested
   int32_t last_layout = -1, last_bw = 0, last_unroll = 0, last_warp_rows = 0;          // used by the last compute
   std::vector<std::unique_ptr<Vol>> vols;
@@ -481,8 +478,7 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
     auto v = std::make_unique<xr_raycaster_s::Vol>();
     v->desc = d;
     v->type = vt;
-    v->cell_order = rc->cell_order;
-    cell_strides(d.n[0], d.n[1], d.n[2], v->cell_order, v->cs);
+    cell_strides(d.n[0], d.n[1], d.n[2], v->cs);
     const size_t esz = vt == XR_VOXEL_F32 ? 4 : 2;
     XR_CUDA_TRY(v->voxels.reserve((size_t)nv * esz));
     if (vt == XR_VOXEL_F32) {
@@ -492,7 +488,7 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
       if (rc->build_cells) {
         XR_CUDA_TRY(v->cells.reserve(cell_layout_bytes(d.n[0], d.n[1], d.n[2], vt)));
         XR_CUDA_TRY(launch_build_cells(v->voxels.as<float>(), (int)d.n[0], (int)d.n[1], (int)d.n[2], vt, 1.0f,
-                                       v->cs, v->cells.p, s));
+                                       v->cells.p, s));
       }
       xr_status st = vol_support(rc, *v, v->voxels.as<float>(), s);
       if (st != XR_OK) return st;
@@ -506,10 +502,10 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
       }
       float sc = scale > 0.0f ? scale : 1.0f;
       if (vt == XR_VOXEL_F16) {
-        // The half2 blend multiplies stored values by x weights scaled by
-        // wscale (so that fractions down to 2^-24 stay normal halves), and the
-        // y blend scales by 2^15 more; the stored maximum times wscale stays
-        // below 2^15.  Automatic scale: the stored maximum in [0.5, 1).
+        // The half2 blend multiplies stored values by x weights scaled by 2^15
+        // (so that fractions down to 2^-24 stay normal halves) and the y blend
+        // by 2^15 more; stored values below 1 keep the blend below 2^15.  So
+        // FP16 always stores the maximum in [0.5, 1) (a given scale is not used).
         XR_CUDA_TRY(cudaMemsetAsync(rc->d_counters.as<char>() + 16, 0, 4, s));
         max_abs_kernel<<<1024, 256, 0, s>>>(src, nv, reinterpret_cast<unsigned int*>(rc->d_counters.as<char>() + 16));
         XR_CUDA_TRY(cudaGetLastError());
@@ -519,12 +515,10 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
         float mx;
         std::memcpy(&mx, &bits, 4);
         XR_CHECK_ARG(std::isfinite(mx), "set_volumes: non-finite voxel");
-        if (!(scale > 0.0f) && mx > 0.0f) sc = (float)std::ldexp(1.0, (int)std::floor(std::log2(1.0 / (double)mx)));
-        const double stored = (double)mx * (double)sc;
-        XR_CHECK_ARG(stored < 65504.0, "set_volumes: scale * max|voxel| exceeds the FP16 range");
-        const int we = stored > 0.0 ? (int)std::floor(std::log2(32768.0 / stored)) : 15;
-        v->wscale = (float)std::ldexp(1.0, std::min(we, 15));
-        v->inv_scale = (float)(1.0 / ((double)sc * (double)v->wscale * 32768.0));
+        // the scale (at most 2^90) and its inverse times 2^-30 stay normal floats
+        XR_CHECK_ARG(mx == 0.0f || mx >= 0x1p-90f, "set_volumes: FP16 volume maximum below 2^-90");
+        sc = mx > 0.0f ? (float)std::ldexp(1.0, (int)std::floor(std::log2(1.0 / (double)mx))) : 1.0f;
+        v->inv_scale = (float)(1.0 / ((double)sc * 32768.0 * 32768.0));
       } else {
         v->inv_scale = 1.0f / sc;
       }
@@ -532,7 +526,7 @@ static xr_status rc_set_volumes_impl(xr_raycaster rc, int32_t n, const xr_volume
       XR_CUDA_TRY(cudaGetLastError());
       if (rc->build_cells) {
         XR_CUDA_TRY(v->cells.reserve(cell_layout_bytes(d.n[0], d.n[1], d.n[2], vt)));
-        XR_CUDA_TRY(launch_build_cells(src, (int)d.n[0], (int)d.n[1], (int)d.n[2], vt, sc, v->cs, v->cells.p, s));
+        XR_CUDA_TRY(launch_build_cells(src, (int)d.n[0], (int)d.n[1], (int)d.n[2], vt, sc, v->cells.p, s));
       }
       xr_status st = vol_support(rc, *v, src, s);
       if (st != XR_OK) return st;
@@ -919,8 +913,7 @@ xr_status time_config(DrrParams p, cudaStream_t s, float* ms_out) {
 
 static TuneKey tune_key(xr_raycaster rc, const xr_raycaster_s::Vol& vol, const DrrParams& p) {
   return TuneKey{vol.desc.n[0], vol.desc.n[1], vol.desc.n[2], rc->rows(), rc->cols(), pow2_bucket(p.num_projs),
-                 vol.type, p.kernel_id,
-                 (vol.cells.p != nullptr ? 1 : 0) | (p.vol.occ ? 2 : 0) | (vol.cell_order ? 4 : 0)};
+                 vol.type, p.kernel_id, (vol.cells.p != nullptr ? 1 : 0) | (p.vol.occ ? 2 : 0)};
 }
 
 // Whether rc_choose_config decides without timing launches (a configuration
@@ -1077,8 +1070,8 @@ static xr_status rc_prepare(xr_raycaster rc, int32_t vol_idx, cudaStream_t s, Dr
   p.vol.nz = (int32_t)vol.desc.n[2];
   p.vol.voxel_type = vol.type;
   p.vol.inv_scale = vol.inv_scale;
-  p.vol.wscale = vol.wscale;
-  for (int k = 0; k < 3; ++k) p.vol.cs[k] = vol.cs[k];
+  p.vol.cs[0] = vol.cs[0];
+  p.vol.cs[1] = vol.cs[1];
   p.vol.has_support = (rc->skip_empty && vol.has_support) ? 1 : 0;
   p.vol.occ = rc->skip_empty ? vol.occ.as<uint32_t>() : nullptr;
   p.vol.nmx = vol.nmx;
@@ -1193,13 +1186,6 @@ extern "C" XR_API xr_status xr_rc_set_empty_space_skipping(xr_raycaster rc, int3
 extern "C" XR_API xr_status xr_rc_set_build_cell_layout(xr_raycaster rc, int32_t enable) {
   XR_CHECK_ARG(rc, "set_build_cell_layout: NULL handle");
   rc->build_cells = enable != 0;
-  return XR_OK;
-}
-
-extern "C" XR_API xr_status xr_rc_set_cell_order(xr_raycaster rc, int32_t order) {
-  XR_CHECK_ARG(rc, "set_cell_order: NULL handle");
-  XR_CHECK_ARG(order == 0 || order == 1, "set_cell_order: order must be 0 or 1");
-  rc->cell_order = order;
   return XR_OK;
 }
 

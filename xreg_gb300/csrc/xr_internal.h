@@ -28,9 +28,8 @@ struct VolView {
   int32_t voxel_type;
   int32_t layout;      // XR_LAYOUT_LINEAR / XR_LAYOUT_CELL8
   float inv_scale;     // multiplies the ray sum (1 for F32)
-  float wscale;        // F16: power of two scaling the x weights of the half2 blend
-  // CELL8 cell order: cell (ix, iy, iz) is number ix cs[0] + iy cs[1] + iz cs[2]
-  int32_t cs[3];
+  // CELL8 cell order, z fastest: cell (ix, iy, iz) is number ix cs[0] + iy cs[1] + iz
+  int32_t cs[2];
   // Support box: every sample whose continuous index lies outside
   // (sup_lo, sup_hi) on some axis interpolates only zero voxels.  has_support 0
   // disables sample skipping; an all-zero volume has an empty box (lo > hi).
@@ -107,12 +106,12 @@ cudaError_t launch_build_occupancy(const float* vox_f32, int nx, int ny, int nz,
 // Index bounds of the non-zero voxels into d_box[6] (min xyz, max xyz; max < min if none).
 cudaError_t launch_support_box(const float* vox_f32, int nx, int ny, int nz, int* d_box, cudaStream_t s);
 // Bytes of the CELL8 copy of a volume, and the kernel that builds it from
-// float32 voxels in the cell order of the strides cs (VolView::cs).
+// float32 voxels (cells numbered z fastest, then x, then y: VolView::cs).
 size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type);
 cudaError_t launch_build_cells(const float* vox_f32, int nx, int ny, int nz, int32_t voxel_type, float scale,
-                               const int32_t cs[3], void* out, cudaStream_t s);
-// Cell strides of a CELL8 order: 0 x fastest (then y, z), 1 z fastest (then x, y).
-void cell_strides(int64_t nx, int64_t ny, int64_t nz, int32_t order, int32_t cs[3]);
+                               void* out, cudaStream_t s);
+// The x and y cell strides of that order (VolView::cs).
+void cell_strides(int64_t nx, int64_t ny, int64_t nz, int32_t cs[2]);
 
 // ---- launchers (xr_metrics.cu) ----
 struct FixedNCC {           // per direction (one for NCC, x and y for grad-NCC)

@@ -28,8 +28,7 @@
 //           for FP32, or one 32-byte load for FP32 (the 256-bit read, layout 2).
 //           It spends 8x the voxel bytes of HBM to cut L1 requests per sample
 //           from 8 to 1-2; the linear kernel is bound by exactly those requests.
-//           Cells are numbered by the strides VolView::cs: z fastest by
-//           default, x fastest selectable (xr_rc_set_cell_order).
+//           Cells are numbered z fastest, then x, then y (VolView::cs).
 #include "xr_internal.h"
 #include "xr_gradtile.cuh"
 
@@ -142,11 +141,11 @@ __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, f
     fx = __fsub_rn(px, __fsub_rn(tx, kTwo23));
     fy = __fsub_rn(py, __fsub_rn(ty, kTwo23));
     fz = __fsub_rn(pz, __fsub_rn(tz, kTwo23));
-    const unsigned int sx = (unsigned int)vol.cs[0], sy = (unsigned int)vol.cs[1], sz = (unsigned int)vol.cs[2];
-    const unsigned int bias = 0x4B000000u * (sx + sy + sz);
+    const unsigned int sx = (unsigned int)vol.cs[0], sy = (unsigned int)vol.cs[1];
+    const unsigned int bias = 0x4B000000u * (sx + sy + 1u);
     const unsigned int bx = (unsigned int)__float_as_int(tx), by = (unsigned int)__float_as_int(ty),
                        bz = (unsigned int)__float_as_int(tz);
-    return (int)(bx * sx + by * sy + bz * sz - bias);
+    return (int)(bx * sx + by * sy + bz - bias);
   }
   int ix = __float2int_rd(px), iy = __float2int_rd(py), iz = __float2int_rd(pz);
   if (INSIDE) {
@@ -161,7 +160,7 @@ __device__ __forceinline__ int cell_of(const VolView& vol, float px, float py, f
     fy = __saturatef(py - (float)iy);
     fz = __saturatef(pz - (float)iz);
   }
-  return ix * vol.cs[0] + iy * vol.cs[1] + iz * vol.cs[2];
+  return ix * vol.cs[0] + iy * vol.cs[1] + iz;
 }
 
 // Weighted-form trilinear of the 8 corners in cell order (z-pairs):
@@ -249,11 +248,11 @@ __device__ __forceinline__ float interp8_pairs(const unsigned long long q[4], fl
 // conversion of the corners.  The x blend runs on the (z0, z1) pairs in half
 // arithmetic (fma.rn.f16x2); the y blend is four mixed-precision fmas
 // (fma.rn.f32.f16: exact products of halves added in float); the z blend is
-// float.  The x weights are scaled by wscale and the y weights by 2^15 before
-// they are rounded to half, so a fraction as small as one float ulp of a
-// position (>= 2^-24) is still a normal half; the stored values times wscale
-// stay below 2^15, so the half blend cannot overflow; the volume's inv_scale
-// removes both scales exactly.  Error: the half rounding of the four weights
+// float.  The x and y weights are scaled by 2^15 before they are rounded to
+// half, so a fraction as small as one float ulp of a position (>= 2^-24) is
+// still a normal half; the stored values are below 1 (the volume's maximum is
+// stored in [0.5, 1)), so the half blend cannot overflow; the volume's
+// inv_scale removes the scales exactly.  Error: the half rounding of the four weights
 // and of the x blend, about 1e-3 of a sample at worst, within the 2e-3 bound
 // for half-precision volumes.  Every FP16 path (layouts, loops, the fused
 // kernel) uses this one function, so they agree bit for bit.
@@ -283,10 +282,10 @@ __device__ __forceinline__ void h2_yblend(unsigned int a0, unsigned int a1, unsi
       : "r"(a0), "r"(a1), "r"(wy), "f"(0.0f));
 }
 // w: (v000, v001) (v100, v101) (v010, v011) (v110, v111), low half z = 0;
-// returns the sample times wscale * 2^15
-__device__ __forceinline__ float interp8_h16(const unsigned int w[4], float fx, float fy, float fz, float ws) {
-  constexpr float kYs = 32768.0f;
-  const unsigned int FX = h2_splat(__fmul_rn(fx, ws)), GX = h2_splat(__fmaf_rn(-fx, ws, ws));
+// returns the sample times 2^30
+__device__ __forceinline__ float interp8_h16(const unsigned int w[4], float fx, float fy, float fz) {
+  constexpr float kXs = 32768.0f, kYs = 32768.0f;
+  const unsigned int FX = h2_splat(__fmul_rn(fx, kXs)), GX = h2_splat(__fmaf_rn(-fx, kXs, kXs));
   const __half2 wy = __floats2half2_rn(__fmaf_rn(-fy, kYs, kYs), __fmul_rn(fy, kYs));  // (gy, fy)
   const unsigned int A0 = h2_fma(w[1], FX, h2_mul(w[0], GX));  // (a00, a01)
   const unsigned int A1 = h2_fma(w[3], FX, h2_mul(w[2], GX));  // (a10, a11)
@@ -348,7 +347,7 @@ __device__ __forceinline__ float sample(const VolView& vol, const void* data, fl
       v[7] = Vox<VT>::ld(data, b + sz + sy + 1);
     }
   }
-  if constexpr (VT == XR_VOXEL_F16) return interp8_h16(w, fx, fy, fz, vol.wscale);
+  if constexpr (VT == XR_VOXEL_F16) return interp8_h16(w, fx, fy, fz);
   else return interp8(v, fx, fy, fz);
 }
 
@@ -421,8 +420,8 @@ __device__ __forceinline__ float march_packed_inside(const VolView& vol, const v
   constexpr float kTwo23 = 8388608.0f;
   const unsigned long long K = pk2(kTwo23, kTwo23), S = pk2(sx, sy);
   unsigned long long P = pk2(px, py);
-  const unsigned int csx = (unsigned int)vol.cs[0], csy = (unsigned int)vol.cs[1], csz = (unsigned int)vol.cs[2];
-  const unsigned int bias = 0x4B000000u * (csx + csy + csz);
+  const unsigned int csx = (unsigned int)vol.cs[0], csy = (unsigned int)vol.cs[1];
+  const unsigned int bias = 0x4B000000u * (csx + csy + 1u);
   // cell index and fractions of the current position, then advance it
   auto locate = [&](float& fx, float& fy, float& fz) -> int {
     const unsigned long long T = add2_rm(P, K);
@@ -436,7 +435,7 @@ __device__ __forceinline__ float march_packed_inside(const VolView& vol, const v
                        bz = (unsigned int)__float_as_int(tz);
     P = add2(P, S);
     pz = __fadd_rn(pz, sz);
-    return (int)(bx * csx + by * csy + bz * csz - bias);
+    return (int)(bx * csx + by * csy + bz - bias);
   };
   if constexpr (VT == XR_VOXEL_F16) {  // half2 words blended as stored
     for (; n >= 4; n -= 4) {
@@ -445,13 +444,13 @@ __device__ __forceinline__ float march_packed_inside(const VolView& vol, const v
 #pragma unroll
       for (int k = 0; k < 4; ++k) Vox<VT>::cell_words(data, locate(f[k][0], f[k][1], f[k][2]), w[k]);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) sum = __fadd_rn(sum, interp8_h16(w[k], f[k][0], f[k][1], f[k][2], vol.wscale));
+      for (int k = 0; k < 4; ++k) sum = __fadd_rn(sum, interp8_h16(w[k], f[k][0], f[k][1], f[k][2]));
     }
     for (; n > 0; --n) {
       float fx, fy, fz;
       unsigned int w[4];
       Vox<VT>::cell_words(data, locate(fx, fy, fz), w);
-      sum = __fadd_rn(sum, interp8_h16(w, fx, fy, fz, vol.wscale));
+      sum = __fadd_rn(sum, interp8_h16(w, fx, fy, fz));
     }
   } else {
     for (; n >= 4; n -= 4) {
@@ -760,7 +759,7 @@ __device__ __forceinline__ float brick_march_global(const VolView& vol, float po
     int c[3];
     float f[3], v[8];
     cell3(vol, pos, c, f);
-    Vox<XR_VOXEL_F32>::cell_wide(vol.cells, c[0] * vol.cs[0] + c[1] * vol.cs[1] + c[2] * vol.cs[2], v);
+    Vox<XR_VOXEL_F32>::cell_wide(vol.cells, c[0] * vol.cs[0] + c[1] * vol.cs[1] + c[2], v);
     sum = __fadd_rn(sum, interp8(v, f[0], f[1], f[2]));
     pos[0] = __fadd_rn(pos[0], st[0]);
     pos[1] = __fadd_rn(pos[1], st[1]);
@@ -913,7 +912,7 @@ __global__ void __launch_bounds__(kThreads, 4) drr_brick_kernel(const DrrParams 
         const int total = W * H * Dz;
         for (int i = tid; i < total; i += kThreads) {
           const int x = lo[0] + i % W, y = lo[1] + (i / W) % H, zz = lo[2] + i / (W * H);
-          const int64_t c = (int64_t)x * vol.cs[0] + (int64_t)y * vol.cs[1] + (int64_t)zz * vol.cs[2];
+          const int64_t c = (int64_t)x * vol.cs[0] + (int64_t)y * vol.cs[1] + zz;
           s_cells[2 * i] = __ldg(cells + 2 * c);
           s_cells[2 * i + 1] = __ldg(cells + 2 * c + 1);
         }
@@ -934,7 +933,7 @@ __global__ void __launch_bounds__(kThreads, 4) drr_brick_kernel(const DrrParams 
             v[0] = q0.x; v[1] = q0.y; v[2] = q0.z; v[3] = q0.w;
             v[4] = q1.x; v[5] = q1.y; v[6] = q1.z; v[7] = q1.w;
           } else {
-            Vox<XR_VOXEL_F32>::cell_wide(vol.cells, c[0] * vol.cs[0] + c[1] * vol.cs[1] + c[2] * vol.cs[2], v);
+            Vox<XR_VOXEL_F32>::cell_wide(vol.cells, c[0] * vol.cs[0] + c[1] * vol.cs[1] + c[2], v);
           }
           sum = __fadd_rn(sum, interp8(v, f[0], f[1], f[2]));
           pos[0] = __fadd_rn(pos[0], st[0]);
@@ -1339,15 +1338,15 @@ cudaError_t launch_kernel_id(const DrrParams& p, cudaStream_t s) {
 
 // One thread per cell (x fastest, so the voxel reads coalesce): gathers the 8
 // corners from the float32 voxels and stores them as cell number
-// ix cs[0] + iy cs[1] + iz cs[2].
+// ix csx + iy csy + iz (z fastest).
 template <int VT>
 __global__ void build_cells_kernel(const float* __restrict__ vox, int nx, int ny, int nz, float scale, int32_t csx,
-                                   int32_t csy, int32_t csz, void* out) {
+                                   int32_t csy, void* out) {
   const int64_t ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
   const int64_t ncell = ncx * ncy * ncz;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ix = t % ncx, iy = (t / ncx) % ncy, iz = t / (ncx * ncy);
-    const int64_t c = ix * csx + iy * csy + iz * csz;
+    const int64_t c = ix * csx + iy * csy + iz;
     const int64_t b = (iz * ny + iy) * nx + ix, sy = nx, sz = (int64_t)nx * ny;
     // z-pairs: v000 v001 v100 v101 v010 v011 v110 v111 (vxyz)
     const float v[8] = {vox[b], vox[b + sz], vox[b + 1], vox[b + sz + 1],
@@ -1535,33 +1534,29 @@ size_t cell_layout_bytes(int64_t nx, int64_t ny, int64_t nz, int32_t voxel_type)
 }
 
 cudaError_t launch_build_cells(const float* vox_f32, int nx, int ny, int nz, int32_t voxel_type, float scale,
-                               const int32_t cs[3], void* out, cudaStream_t s) {
+                               void* out, cudaStream_t s) {
+  int32_t cs[2];
+  cell_strides(nx, ny, nz, cs);
   switch (voxel_type) {
     case XR_VOXEL_F32:
-      build_cells_kernel<XR_VOXEL_F32><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, 1.0f, cs[0], cs[1], cs[2], out);
+      build_cells_kernel<XR_VOXEL_F32><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, 1.0f, cs[0], cs[1], out);
       break;
     case XR_VOXEL_F16:
-      build_cells_kernel<XR_VOXEL_F16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, cs[0], cs[1], cs[2], out);
+      build_cells_kernel<XR_VOXEL_F16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, cs[0], cs[1], out);
       break;
     case XR_VOXEL_BF16:
-      build_cells_kernel<XR_VOXEL_BF16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, cs[0], cs[1], cs[2], out);
+      build_cells_kernel<XR_VOXEL_BF16><<<2048, 256, 0, s>>>(vox_f32, nx, ny, nz, scale, cs[0], cs[1], out);
       break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-void cell_strides(int64_t nx, int64_t ny, int64_t nz, int32_t order, int32_t cs[3]) {
-  const int32_t cx = (int32_t)(nx - 1), cy = (int32_t)(ny - 1), cz = (int32_t)(nz - 1);
-  if (order == 1) {
-    cs[2] = 1;
-    cs[0] = cz;
-    cs[1] = cz * cx;
-  } else {
-    cs[0] = 1;
-    cs[1] = cx;
-    cs[2] = cx * cy;
-  }
+void cell_strides(int64_t nx, int64_t ny, int64_t nz, int32_t cs[2]) {
+  (void)ny;
+  const int32_t cx = (int32_t)(nx - 1), cz = (int32_t)(nz - 1);
+  cs[0] = cz;       // x
+  cs[1] = cz * cx;  // y
 }
 
 }  // namespace xr
