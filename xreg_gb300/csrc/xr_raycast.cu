@@ -659,16 +659,22 @@ __device__ __forceinline__ unsigned long long trace_pixel(const DrrParams& p, co
       }
       if (hit) {
         // advance to sample `first` (four additions per trip: the skipped samples
-        // are a large part of a trimmed ray)
+        // are a large part of a trimmed ray); x and y as one packed pair, whose
+        // lanes round as the scalar additions do
         unsigned int skip = first <= last ? first : last + 1u;
-        for (; skip >= 4; skip -= 4) {
-          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
-        }
-        for (; skip > 0; --skip) {
-          px = __fadd_rn(px, sx); py = __fadd_rn(py, sy); pz = __fadd_rn(pz, sz);
+        {
+          unsigned long long P = pk2(px, py);
+          const unsigned long long S = pk2(sx, sy);
+          for (; skip >= 4; skip -= 4) {
+            P = add2(P, S); pz = __fadd_rn(pz, sz);
+            P = add2(P, S); pz = __fadd_rn(pz, sz);
+            P = add2(P, S); pz = __fadd_rn(pz, sz);
+            P = add2(P, S); pz = __fadd_rn(pz, sz);
+          }
+          for (; skip > 0; --skip) {
+            P = add2(P, S); pz = __fadd_rn(pz, sz);
+          }
+          upk2(P, px, py);
         }
         // samples first..last in order; the sum order never changes with UNROLL
         unsigned int n = first <= last ? last - first + 1u : 0u;
