@@ -94,6 +94,26 @@ def test_half_precision_volumes(xr, oracle, vt, tol):
     assert zero == 0.0 and rel <= tol, rel
 
 
+def test_fp16_volume_scaling(xr, oracle):
+    """FP16 volumes store their maximum scaled into [0.5, 1) by a power of two
+    and undo it after the ray sum, so a volume of tiny attenuations gives the
+    oracle's DRR of the same volume within the half-precision bound; non-finite
+    voxels and a maximum below 2^-90 are refused."""
+    import dataclasses
+    w = synth.plain_small(6)
+    pose = synth.fixed_pose(w)
+    tiny = dataclasses.replace(w.vol, voxels=(w.vol.voxels * np.float32(1e-20)).astype(np.float32))
+    g, _ = _gpu_drr(xr, tiny, w.cams, pose[None], w.step, voxel_type=1)
+    o = oracle.drr_f32(tiny.voxels, oracle_geom(tiny), oracle_cams(w.cams), pose[None], step=w.step)
+    rel, zero = drr_rel_err(g, o)
+    assert zero == 0.0 and rel <= TOL16, rel
+    for bad in (np.inf, 1e-30):
+        v = np.zeros_like(w.vol.voxels)
+        v[3, 4, 5] = bad
+        with pytest.raises(xr.XRegError):
+            _rc(xr, dataclasses.replace(w.vol, voxels=v), w.cams, w.step, 1)
+
+
 def test_anisotropic_oriented_volume(xr, oracle):
     vol = small_volume(3, (40, 32, 28), (0.8, 1.1, 1.7))
     from xreg_gb300.se3 import euler_xyz
