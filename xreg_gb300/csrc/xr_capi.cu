@@ -2,6 +2,7 @@
 // stream ordering and CUDA-graph capture of the population objective.
 // Nothing here throws across the ABI; every entry point returns an xr_status.
 #include "xr_internal.h"
+#include "xr_posespread.h"
 #include "xreg_gb300_regi.h"
 
 #include <algorithm>
@@ -2115,50 +2116,13 @@ static xr_status step_enqueue(FusedWork& fw, int device, int32_t n, const xr_obj
   std::vector<CmaUpdateJob> cu;  // device optimizers whose update has a launch of its own
   // how far a job's poses spread, in voxels at the volume (nearby poses: pose-grouped DRR items)
   auto pose_spread_vox = [&](int32_t i, const xr_raycaster_s::Vol& vol, int64_t pop) -> double {
-    const double* sp = vol.desc.spacing;
-    const double vmin = std::min(sp[0], std::min(sp[1], sp[2]));
-    double half[3], radius2 = 0.0;
-    for (int a = 0; a < 3; ++a) {
-      half[a] = 0.5 * (double)vol.desc.n[a] * sp[a];
-      radius2 += half[a] * half[a];
-    }
-    if (dev_opt(i)) {  // the distribution the device optimizer samples next: 3 sigma
+    if (dev_opt(i)) {  // the distribution the device optimizer samples next
       const xr_objective obj = objs[i];
       if (obj->next_sd_state != cma[i].state || !(obj->next_sd_rot >= 0.0)) return INFINITY;
-      return 3.0 * (obj->next_sd_trans + obj->next_sd_rot * std::sqrt(radius2)) / vmin;
+      return sampled_spread_voxels(vol.desc, obj->next_sd_rot, obj->next_sd_trans);
     }
     if (!host_in || pop < 2) return INFINITY;
-    // the volume's corners in each pose's camera frame, against the first pose's
-    const double* P = xforms[i];
-    double Ri[9], ti[3], best = 0.0;
-    auto inv = [&](const double* p, double* R, double* t) {
-      for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) R[r * 3 + c] = p[c * 4 + r];
-      for (int r = 0; r < 3; ++r) t[r] = -(R[r * 3] * p[3] + R[r * 3 + 1] * p[7] + R[r * 3 + 2] * p[11]);
-    };
-    inv(P, Ri, ti);
-    const double* o = vol.desc.origin;
-    const double* dirm = vol.desc.direction;
-    for (int64_t k = 1; k < pop; ++k) {
-      double Rk[9], tk[3];
-      inv(P + 16 * k, Rk, tk);
-      for (int c = 0; c < 8; ++c) {
-        double x[3];
-        for (int a = 0; a < 3; ++a) {
-          double s = o[a];
-          for (int b = 0; b < 3; ++b) s += dirm[a * 3 + b] * (((c >> b) & 1) ? (double)(vol.desc.n[b] - 1) : 0.0) * sp[b];
-          x[a] = s;
-        }
-        double d2 = 0.0;
-        for (int r = 0; r < 3; ++r) {
-          const double u = Rk[r * 3] * x[0] + Rk[r * 3 + 1] * x[1] + Rk[r * 3 + 2] * x[2] + tk[r];
-          const double v = Ri[r * 3] * x[0] + Ri[r * 3 + 1] * x[1] + Ri[r * 3 + 2] * x[2] + ti[r];
-          d2 += (u - v) * (u - v);
-        }
-        best = std::max(best, std::sqrt(d2));
-      }
-    }
-    return best / vmin;
+    return pose_spread_voxels(vol.desc, xforms[i], pop);
   };
   std::vector<GeomJob> gj;
   std::vector<FusedJob> fj;
